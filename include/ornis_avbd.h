@@ -1,0 +1,255 @@
+/*
+ * ornis_avbd.h — C ABI of the GB300-native AVBD rigid-body step.
+ *
+ * This is the drop-in boundary for the AVBD step of Ornis's physics crate.
+ * Every entry point replaces one method of the reference's engine seam:
+ *
+ *   trait PhysicsEngine            crates/physics/src/engine.rs:24-133
+ *   impl PhysicsEngine for AvbdEngine   crates/physics/src/avbd/mod.rs:1211-1602
+ *   trait GpuAvbdDispatch          crates/physics/src/gpu/avbd.rs:146-151
+ *
+ * Conventions (kept from the reference):
+ *   - Body handles are dense uint32 indices in insertion order
+ *     (engine.rs:40-43, avbd/mod.rs:1236-1239).
+ *   - A step with a non-finite or non-positive dt is a no-op
+ *     (avbd/mod.rs:1213-1215).
+ *   - Buffers passed in are caller-owned host memory and are copied; the
+ *     library owns all device memory.  One CUDA stream per world; a world is
+ *     not thread-safe, distinct worlds are independent.
+ *   - Every function returns an int status: AVBD_OK (0) or a negative code.
+ *
+ * A world holds one or more independent scenes packed into one flat
+ * structure-of-arrays on the device (scene s owns the body handles
+ * [scene_offsets[s], scene_offsets[s+1])).  Bodies of different scenes never
+ * interact.  A world with one scene is the reference's AvbdEngine.
+ */
+#ifndef ORNIS_AVBD_H
+#define ORNIS_AVBD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AVBD_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define AVBD_OK 0
+#define AVBD_ERR_INVALID_ARG (-1)    /* null pointer, bad size, bad enum       */
+#define AVBD_ERR_CAPACITY (-2)       /* a device buffer would overflow         */
+#define AVBD_ERR_DEVICE (-3)         /* a CUDA call failed                     */
+#define AVBD_ERR_TIMEOUT (-4)        /* a bounded device wait gave up          */
+#define AVBD_ERR_NONFINITE (-5)      /* NaN/Inf in an input body               */
+#define AVBD_ERR_UNSUPPORTED (-6)    /* shape / joint kind not implemented     */
+/* joint admission errors, mirroring JointError (avbd/mod.rs:1323-1328) */
+#define AVBD_ERR_JOINT_SELF (-10)    /* JointError::SelfJoint                  */
+#define AVBD_ERR_JOINT_HANDLES (-11) /* JointError::InvalidHandles             */
+#define AVBD_ERR_JOINT_BAD_AXIS (-12)/* JointError::BadAxis                    */
+#define AVBD_ERR_JOINT_NONFINITE (-13)
+
+/* ---- enums --------------------------------------------------------------- */
+/* Shape variants on the path (collision/shape.rs); shape_params meaning:     */
+#define AVBD_SHAPE_SPHERE 0    /* [radius, -, -]                                */
+#define AVBD_SHAPE_BOX 1       /* [hx, hy, hz] half extents                     */
+#define AVBD_SHAPE_CAPSULE 2   /* [radius, half_height, -], axis = local +Y     */
+#define AVBD_SHAPE_HALFSPACE 3 /* [nx, ny, nz] outward unit normal, body-local */
+
+#define AVBD_BODY_DYNAMIC 0   /* BodyType::Dynamic   */
+#define AVBD_BODY_STATIC 1    /* BodyType::Static    */
+#define AVBD_BODY_KINEMATIC 2 /* BodyType::Kinematic */
+
+#define AVBD_FLAG_TRIGGER 1u /* RigidBody::is_trigger */
+
+#define AVBD_JOINT_BALL 0     /* JointKind::Ball     (joint.rs:209+) */
+#define AVBD_JOINT_REVOLUTE 1 /* JointKind::Revolute (optional limit) */
+
+/* ---- plain-old-data records --------------------------------------------- */
+
+/* One rigid body: the fields of RigidBody (body.rs:248-342) that the AVBD
+ * step reads or writes.  Orientation is a unit quaternion (x, y, z, w). */
+typedef struct AvbdBody {
+    float position[3];
+    float orientation[4];
+    float velocity[3];
+    float angular_velocity[3];
+    float torque[3];
+    float mass;     /* 0 = static                                            */
+    float inv_mass; /* 1/mass, or 0                                           */
+    float inertia[3]; /* body-frame diagonal inertia                          */
+    float restitution;
+    float friction;
+    float friction_transverse;
+    float rolling_friction;
+    float torsion_friction;
+    uint32_t shape;
+    float shape_params[3];
+    uint32_t collision_layer;
+    uint32_t collision_mask;
+    uint32_t body_type;
+    uint32_t flags;
+} AvbdBody;
+
+/* Joint specification (JointKind::Ball / ::Revolute, joint.rs:209-260). */
+typedef struct AvbdJointDesc {
+    uint32_t kind;
+    uint32_t body_a;
+    uint32_t body_b;
+    float local_anchor_a[3];
+    float local_anchor_b[3];
+    float local_axis_a[3]; /* revolute only */
+    float local_axis_b[3]; /* revolute only */
+    int32_t has_limit;     /* revolute only: RevoluteLimit present */
+    float limit_min;
+    float limit_max;
+} AvbdJointDesc;
+
+/* Solver parameters.  avbd_default_params() fills the reference's constants
+ * (avbd/mod.rs:154-247, :1205-1210); dt, iterations and the substep count
+ * are runtime parameters here because the workloads need 1/120 s, 8 or 12
+ * iterations and 2 substeps, which the reference hard-codes. */
+typedef struct AvbdParams {
+    float gravity[3];
+    float step_dt;        /* fixed substep length  (reference DT_STEP 1/60)   */
+    int32_t iterations;   /* primal+dual sweeps    (reference ITERS 10)       */
+    int32_t max_substeps; /* accumulator cap       (reference MAX_SUBSTEPS 4) */
+    int32_t enable_sleep; /* 1 = reference sleep bookkeeping                  */
+    int32_t enable_ccd;   /* 1 = reference linear TOI clamp                   */
+} AvbdParams;
+
+/* Per-body solver state outside RigidBody (avbd/mod.rs:425-464). */
+typedef struct AvbdBodyAux {
+    float prev_position[3];
+    float prev_orientation[4];
+    float sleep_timer;
+    uint32_t asleep;
+} AvbdBodyAux;
+
+/* One contact pair (AvbdPair, avbd/mod.rs:269-281).  Pairs are exported in
+ * ascending (a, b) order; a < b are body handles. */
+typedef struct AvbdPairState {
+    uint32_t a;
+    uint32_t b;
+    float normal[3];
+    float mu[2];
+    float gap;
+    uint32_t npoints;
+} AvbdPairState;
+
+/* One contact point (AvbdPoint, avbd/mod.rs:253-265).  Points are exported
+ * in fixed slots of AVBD_MAX_POINTS per pair.  `matched` is the contact ID
+ * link: the slot of the previous step's point whose warm state this point
+ * inherited, or -1 for a fresh point. */
+#define AVBD_MAX_POINTS 8
+typedef struct AvbdPointState {
+    float ra[3];
+    float rb[3];
+    float lam[3];
+    float pen[3];
+    float roll_lam[3];
+    uint32_t stuck;
+    int32_t matched;
+} AvbdPointState;
+
+/* Joint dual state (AvbdJoint, avbd/mod.rs:327-402). */
+typedef struct AvbdJointState {
+    float lam_l[3];
+    float lam_a[3];
+    float pen_l[3];
+    float pen_a[3];
+    float acc_lim;
+} AvbdJointState;
+
+/* Per-step observability counters (SURVEY "metrics"). */
+typedef struct AvbdCounters {
+    uint64_t steps;        /* fixed substeps taken                            */
+    uint64_t pairs;        /* live contact pairs after the last substep       */
+    uint64_t points;       /* live contact points                             */
+    uint64_t candidates;   /* broadphase candidate pairs (last substep)       */
+    uint64_t colours;      /* colours used by the last substep (max over scenes) */
+    uint64_t breakdowns;   /* LDL^T breakdowns (body skipped its update), cumulative */
+    uint64_t ccd_hits;     /* TOI clamps, cumulative                          */
+    uint64_t sleeping;     /* bodies asleep after the last substep            */
+    uint64_t timeouts;     /* bounded device waits that gave up, cumulative   */
+} AvbdCounters;
+
+typedef struct AvbdWorld AvbdWorld;
+
+/* ---- world lifecycle ----------------------------------------------------- */
+
+/* Fill `p` with the reference's defaults: gravity (0,-9.81,0), 1/60 s,
+ * 10 iterations, 4 max substeps, sleep and CCD on. */
+int avbd_default_params(AvbdParams* p);
+
+/* AvbdEngine::new (avbd/mod.rs:1147).  `device` is the CUDA ordinal. */
+int avbd_world_create(const AvbdParams* params, int device, AvbdWorld** out);
+
+/* Build a multi-scene world in one call: bodies[0..n) with scene s owning
+ * [scene_offsets[s], scene_offsets[s+1]), scene_offsets has nscenes+1
+ * entries, scene_offsets[0] == 0, scene_offsets[nscenes] == n. */
+int avbd_world_create_batch(const AvbdParams* params, int device,
+                            const AvbdBody* bodies, uint32_t n,
+                            const uint32_t* scene_offsets, uint32_t nscenes,
+                            AvbdWorld** out);
+
+int avbd_world_destroy(AvbdWorld* world);
+
+/* PhysicsEngine::add_body (avbd/mod.rs:1236-1239): appends to the last
+ * scene; the first new handle is written to *first_handle. */
+int avbd_world_add_bodies(AvbdWorld* world, const AvbdBody* bodies, uint32_t n,
+                          uint32_t* first_handle);
+
+/* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529), Ball and Revolute. */
+int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
+
+int avbd_world_body_count(const AvbdWorld* world, uint32_t* n);
+int avbd_world_scene_count(const AvbdWorld* world, uint32_t* n);
+
+/* PhysicsEngine::get_body / get_body_mut (engine.rs:45-48) for a range of
+ * handles: host copies of the device body records.  Edits written back by
+ * avbd_world_set_bodies apply at the next step. */
+int avbd_world_get_bodies(AvbdWorld* world, uint32_t first, uint32_t n, AvbdBody* out);
+int avbd_world_set_bodies(AvbdWorld* world, uint32_t first, uint32_t n, const AvbdBody* in);
+
+/* PhysicsEngine::step (avbd/mod.rs:1212-1235): fixed-step accumulator,
+ * at most max_substeps substeps of step_dt per call. */
+int avbd_world_step(AvbdWorld* world, float dt);
+
+/* Advance exactly `substeps` fixed substeps of step_dt (no accumulator). */
+int avbd_world_step_fixed(AvbdWorld* world, int32_t substeps);
+
+/* Same as avbd_world_step_fixed, replayed through a captured CUDA graph of
+ * one substep (captured on first use, re-captured when capacities change). */
+int avbd_world_step_graph(AvbdWorld* world, int32_t substeps);
+
+/* Block until the world's stream is idle. */
+int avbd_world_sync(AvbdWorld* world);
+
+int avbd_world_get_counters(AvbdWorld* world, AvbdCounters* out);
+
+/* ---- state exchange: checkpoint / restore and parity ---------------------- */
+
+/* Sizes of the exported state: bodies, pairs, joints. */
+int avbd_world_state_sizes(AvbdWorld* world, uint32_t* nbodies, uint32_t* npairs,
+                           uint32_t* njoints);
+
+/* Copy the whole solver state to host arrays (points: AVBD_MAX_POINTS slots
+ * per pair).  Any pointer may be NULL to skip that part. */
+int avbd_world_export_state(AvbdWorld* world, AvbdBody* bodies, AvbdBodyAux* aux,
+                            AvbdPairState* pairs, AvbdPointState* points,
+                            AvbdJointState* joints, uint32_t pair_capacity);
+
+/* Replace the whole solver state (body count and joints must match). */
+int avbd_world_import_state(AvbdWorld* world, const AvbdBody* bodies,
+                            const AvbdBodyAux* aux, const AvbdPairState* pairs,
+                            const AvbdPointState* points, uint32_t npairs,
+                            const AvbdJointState* joints);
+
+/* Colour of every body in the last substep's primal sweep (-1 = not swept:
+ * static, kinematic, asleep). */
+int avbd_world_get_colours(AvbdWorld* world, int32_t* colours, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ORNIS_AVBD_H */

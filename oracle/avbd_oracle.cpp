@@ -1,0 +1,1995 @@
+// avbd_oracle.cpp — CPU restatement of the reference AVBD rigid-body step.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle for the
+// GB300 kernels in ornis_gb300/csrc.  Only tests/, __graft_entry__.smoke()
+// and bench.py's CPU-baseline leg may load the library built from it, and
+// only as the checker or the timed CPU baseline — never as the product path.
+//
+// It restates, function by function, the AVBD engine of Ornis's physics
+// crate (the reference is Rust and cannot be built here: no cargo/rustc).
+// Citations are to crates/physics/src/... in the reference tree.
+//
+// Two sweep modes share all arithmetic:
+//   Reference — the reference's exact semantics: pair vector kept in append +
+//               swap_remove order (avbd/rows.rs:905-937), primal sweep in
+//               reverse handle order (avbd/mod.rs:1052-1059).
+//   Coloured  — the GPU's schedule: pairs kept in ascending (a, b) order and
+//               the primal sweep run colour by colour over a greedy colouring
+//               in hash-priority order (identical to the Jones-Plassmann
+//               colouring the GPU computes).  Within a colour bodies are
+//               independent, so the order inside a colour is immaterial.
+// Scalar T = float (bit-level parity) or double (the f64 error column).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "../include/ornis_avbd.h"
+#include "avbd_math.hpp"
+
+namespace orc {
+
+// ---- constants (avbd/mod.rs:154-247, constants.rs:26-79) -------------------
+struct K {
+    static constexpr float ALPHA = 0.99f;
+    static constexpr float GAMMA = 0.999f;
+    static constexpr float BETA = 10000.0f;
+    static constexpr float BETA_ANG = 100.0f;
+    static constexpr float MARGIN = 0.01f;
+    static constexpr float PENALTY_MIN = 1.0f;
+    static constexpr float PENALTY_MAX = 1.0e10f;
+    static constexpr float PENALTY_INIT = 1.0f;
+    static constexpr float JOINT_PENALTY_INIT = 1.0f;
+    static constexpr float GEN_MARGIN = 0.05f;
+    static constexpr float EXPAND_SLOP = 0.005f;
+    static constexpr float POINT_MATCH_DIST = 0.03f;
+    static constexpr float LAMBDA_MATCH_DIST = 0.05f;
+    static constexpr float C_EPS = 1e-7f;
+    static constexpr float STICK_THRESH = 0.00001f;
+    static constexpr float SLEEP_LIN = 0.15f;
+    static constexpr float SLEEP_ANG = 0.15f;
+    static constexpr float HALF = 0.5f;
+    static constexpr float SLEEP_TIME = 0.5f;
+    static constexpr float WAKE_IMPACT_SPEED = 0.5f;
+    static constexpr float WAKE_PENETRATION = 0.01f;
+    static constexpr float LIMIT_SLOP_ANG = 0.005f;
+    static constexpr float LIM_PEN_MAX = 1e4f;
+    static constexpr float ROLL_PEN = 100.0f;
+    static constexpr float MIN_TOI_DISP_LENGTH = 1e-9f;
+    static constexpr float SPIN_REST_EPS = 1e-9f;
+    static constexpr float CCD_BOUNCE_SPEED = 1.0f;
+    static constexpr float DEGENERATE_LEN2 = 1e-12f;
+    static constexpr float NEAR_ZERO = 1e-9f;
+    static constexpr float SHAPE_TOUCH = 1e-3f;
+    static constexpr float AXIS_REST_LEN2 = 1e-16f;
+    static constexpr float CCD_TRAVEL_GATE_FRACTION = 0.5f;
+    static constexpr float DEGENERATE_EPS = 1e-12f;  // distance.rs:24, distance_box.rs:8
+    static constexpr float FACE_AXIS_EPS = 1e-6f;
+    static constexpr float SPINE_ALIGNMENT_EPS = 1e-6f;
+    static constexpr float TANGENT_REF_AXIS_DOT = 0.9f;  // math.rs
+    static constexpr float JOINT_REST_ERROR = 0.005f;    // avbd/sleep.rs:6
+    static constexpr float PI = 3.14159265358979323846f;
+    static constexpr float TAU = 6.28318530717958647692f;
+};
+static constexpr int MAX_POINTS = 8;
+static constexpr int SPATIAL_DOF = 6;
+
+template <class T> static inline T C(float v) { return T(v); }
+
+// ---- shapes --------------------------------------------------------------------
+template <class T> struct Body {
+    V3<T> pos;
+    Qt<T> rot;
+    V3<T> vel, angvel, torque;
+    T mass, inv_mass;
+    V3<T> inertia;
+    T restitution, friction, friction_t, rolling, torsion;
+    uint32_t shape;
+    V3<T> sp;  // shape params
+    uint32_t layer, mask, type, flags;
+    bool trigger() const { return (flags & AVBD_FLAG_TRIGGER) != 0; }
+};
+
+template <class T> struct ShapeRef {
+    const Body<T>* body;  // shape + params
+    uint32_t shape;
+    V3<T> sp;
+    V3<T> pos;
+    Qt<T> rot;
+};
+template <class T> static ShapeRef<T> sref(const Body<T>& b) { return {&b, b.shape, b.sp, b.pos, b.rot}; }
+
+template <class T> struct Dist {
+    T dist;
+    V3<T> pa, pb;
+};
+
+// Shape::inertia (collision/shape.rs:713-790) for the path's shapes.
+template <class T> static V3<T> shape_inertia(uint32_t shape, V3<T> sp, T mass) {
+    if (!(mass > T(0)) || !std::isfinite(mass)) return VZERO<T>();
+    switch (shape) {
+        case AVBD_SHAPE_SPHERE: {
+            T r = sp.x;
+            T v = C<T>(0.4f) * mass * r * r;
+            return {v, v, v};
+        }
+        case AVBD_SHAPE_BOX: {
+            V3<T> s = sp * T(2);
+            T x = s.x * s.x, y = s.y * s.y, z = s.z * s.z;
+            T k = mass / T(12);
+            return {k * (y + z), k * (z + x), k * (x + y)};
+        }
+        case AVBD_SHAPE_CAPSULE: {
+            T r = sp.x, h = sp.y;
+            T iy = C<T>(0.5f) * mass * r * r;
+            T ixz = C<T>(0.25f) * mass * (r * r) + (mass / T(3)) * h * r + C<T>(0.25f) * mass * h * h;
+            return {ixz, iy, ixz};
+        }
+        default:
+            return VZERO<T>();
+    }
+}
+
+// ---- collision/distance.rs ------------------------------------------------------
+template <class T> static V3<T> point_segment_closest(V3<T> p, V3<T> a, V3<T> b) {  // :63-71
+    V3<T> ab = b - a;
+    T l2 = len2(ab);
+    if (l2 < C<T>(K::DEGENERATE_EPS)) return a;
+    T t = fclamp(dot(p - a, ab) / l2, T(0), T(1));
+    return a + ab * t;
+}
+
+template <class T> static void seg_seg_closest(V3<T> a0, V3<T> a1, V3<T> b0, V3<T> b1, V3<T>& oa, V3<T>& ob) {  // :75-113
+    const T E = C<T>(K::DEGENERATE_EPS);
+    V3<T> d1 = a1 - a0, d2 = b1 - b0, r = a0 - b0;
+    T a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    if (a < E && e < E) { oa = a0; ob = b0; return; }
+    if (a < E) {
+        T t = fclamp(f / e, T(0), T(1));
+        oa = a0; ob = b0 + d2 * t;
+        return;
+    }
+    T c = dot(d1, r);
+    if (e < E) {
+        T t = fclamp(-c / a, T(0), T(1));
+        oa = a0 + d1 * t; ob = b0;
+        return;
+    }
+    T b = dot(d1, d2);
+    T denom = a * e - b * b;
+    T s = std::fabs(denom) > E ? fclamp((b * f - c * e) / denom, T(0), T(1)) : T(0);
+    T t = e > E ? (b * s + f) / e : T(0);
+    if (!(t >= T(0) && t <= T(1))) {
+        t = fclamp(t, T(0), T(1));
+        s = fclamp((b * t - c) / a, T(0), T(1));
+    }
+    oa = a0 + d1 * s;
+    ob = b0 + d2 * t;
+}
+
+template <class T> static V3<T> point_obb_closest(V3<T> p, V3<T> pos, V3<T> half, Qt<T> rot) {  // :117-138
+    V3<T> l = qrot(conj(rot), p - pos);
+    V3<T> cl = vclamp(l, -half, half);
+    V3<T> q;
+    if (cl == l) {
+        T dx = half.x - std::fabs(l.x), dy = half.y - std::fabs(l.y), dz = half.z - std::fabs(l.z);
+        q = l;
+        if (dx <= dy && dx <= dz) q.x = std::copysign(half.x, l.x);
+        else if (dy <= dz) q.y = std::copysign(half.y, l.y);
+        else q.z = std::copysign(half.z, l.z);
+    } else {
+        q = cl;
+    }
+    return pos + qrot(rot, q);
+}
+
+template <class T> static void obb_corners(V3<T> pos, V3<T> half, Qt<T> rot, V3<T> c[8]) {  // :142-156
+    V3<T> x = qrot(rot, VX<T>() * half.x);
+    V3<T> y = qrot(rot, VY<T>() * half.y);
+    V3<T> z = qrot(rot, VZ<T>() * half.z);
+    c[0] = pos + x + y + z; c[1] = pos + x + y - z; c[2] = pos + x - y + z; c[3] = pos + x - y - z;
+    c[4] = pos - x + y + z; c[5] = pos - x + y - z; c[6] = pos - x - y + z; c[7] = pos - x - y - z;
+}
+static const int OBB_EDGES[12][2] = {{0, 4}, {1, 5}, {2, 6}, {3, 7}, {0, 2}, {1, 3},
+                                     {4, 6}, {5, 7}, {0, 1}, {2, 3}, {4, 5}, {6, 7}};
+
+template <class T> static void capsule_segment(V3<T> pos, T hh, Qt<T> rot, V3<T>& s0, V3<T>& s1) {
+    V3<T> axis = qrot(rot, VY<T>());
+    s0 = pos - axis * hh;
+    s1 = pos + axis * hh;
+}
+
+template <class T> static Dist<T> sphere_sphere(V3<T> pa, T ra, V3<T> pb, T rb) {  // :180-189
+    V3<T> d = pb - pa;
+    T cd = len(d);
+    V3<T> n = normalize_or(d, VX<T>());
+    return {cd - ra - rb, pa + n * ra, pb - n * rb};
+}
+
+template <class T> static Dist<T> sphere_obb(V3<T> apos, T r, V3<T> bpos, Qt<T> brot, V3<T> half) {  // :192-216
+    V3<T> pb = point_obb_closest(apos, bpos, half, brot);
+    V3<T> d = apos - pb;
+    T core = len(d);
+    V3<T> local = qrot(conj(brot), apos - bpos);
+    V3<T> al = vabs(local);
+    bool inside = al.x <= half.x && al.y <= half.y && al.z <= half.z;
+    V3<T> n;
+    if (inside) {
+        V3<T> cl = half - al;
+        V3<T> axis;
+        if (cl.x <= cl.y && cl.x <= cl.z) axis = VX<T>() * signum(local.x);
+        else if (cl.y <= cl.z) axis = VY<T>() * signum(local.y);
+        else axis = VZ<T>() * signum(local.z);
+        n = normalize_or(pb - apos, qrot(brot, axis));
+    } else {
+        n = normalize_or(d, VX<T>());
+    }
+    return {inside ? -core - r : core - r, apos - n * r, pb};
+}
+
+template <class T> static Dist<T> sphere_capsule(V3<T> apos, T r, V3<T> bpos, Qt<T> brot, T cr, T hh) {  // :219-230
+    V3<T> s0, s1;
+    capsule_segment(bpos, hh, brot, s0, s1);
+    V3<T> cb = point_segment_closest(apos, s0, s1);
+    V3<T> d = apos - cb;
+    T core = len(d);
+    V3<T> n = normalize_or(d, VX<T>());
+    return {core - r - cr, apos - n * r, cb + n * cr};
+}
+
+template <class T> static Dist<T> capsule_capsule(V3<T> apos, Qt<T> arot, T ra, T ha, V3<T> bpos, Qt<T> brot, T rb, T hb) {  // :233-245
+    V3<T> a0, a1, b0, b1, ca, cb;
+    capsule_segment(apos, ha, arot, a0, a1);
+    capsule_segment(bpos, hb, brot, b0, b1);
+    seg_seg_closest(a0, a1, b0, b1, ca, cb);
+    V3<T> d = cb - ca;
+    T core = len(d);
+    V3<T> n = normalize_or(d, VX<T>());
+    return {core - ra - rb, ca + n * ra, cb - n * rb};
+}
+
+// gjk.rs:68-186 (support) for the path's shapes.
+template <class T> static V3<T> support(uint32_t shape, V3<T> sp, V3<T> pos, Qt<T> rot, V3<T> dir) {
+    switch (shape) {
+        case AVBD_SHAPE_SPHERE:
+            return pos + normalize_or(dir, VX<T>()) * sp.x;
+        case AVBD_SHAPE_BOX: {
+            V3<T> l = qrot(conj(rot), dir);
+            V3<T> s{l.x >= T(0) ? T(1) : T(-1), l.y >= T(0) ? T(1) : T(-1), l.z >= T(0) ? T(1) : T(-1)};
+            return pos + qrot(rot, V3<T>{sp.x * s.x, sp.y * s.y, sp.z * s.z});
+        }
+        case AVBD_SHAPE_CAPSULE: {
+            V3<T> axis = qrot(rot, VY<T>());
+            V3<T> tip = (dot(dir, axis) >= T(0) ? axis : -axis) * sp.y;
+            return pos + tip + normalize_or(dir, VX<T>()) * sp.x;
+        }
+        default:
+            return pos;
+    }
+}
+
+// collision/distance_box.rs
+template <class T> static void separating_axis(V3<T> apos, Qt<T> arot, V3<T> ha, V3<T> bpos, Qt<T> brot, V3<T> hb,
+                                               T& gap_out, V3<T>& n_out) {  // :21-50
+    V3<T> aa[3], bb[3];
+    mat3_from_quat(arot, aa);
+    mat3_from_quat(brot, bb);
+    V3<T> axes[15];
+    for (int i = 0; i < 3; i++) axes[i] = aa[i];
+    for (int i = 0; i < 3; i++) axes[3 + i] = bb[i];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            V3<T> c = cross(aa[i], bb[j]);
+            axes[6 + 3 * i + j] = len2(c) > C<T>(K::DEGENERATE_EPS) ? normalize(c) : VZERO<T>();
+        }
+    V3<T> delta = bpos - apos;
+    T best = -std::numeric_limits<T>::infinity();
+    V3<T> bn = VY<T>();
+    for (int k = 0; k < 15; k++) {
+        V3<T> n = axes[k];
+        if (n == VZERO<T>()) continue;
+        T ea = ha.x * std::fabs(dot(n, aa[0])) + ha.y * std::fabs(dot(n, aa[1])) + ha.z * std::fabs(dot(n, aa[2]));
+        T eb = hb.x * std::fabs(dot(n, bb[0])) + hb.y * std::fabs(dot(n, bb[1])) + hb.z * std::fabs(dot(n, bb[2]));
+        T proj = dot(delta, n);
+        T gap = std::fabs(proj) - ea - eb;
+        if (gap > best) {
+            best = gap;
+            bn = proj >= T(0) ? n : -n;
+        }
+    }
+    gap_out = best;
+    n_out = bn;
+}
+
+template <class T> static T box_box_signed_gap(V3<T> apos, Qt<T> arot, V3<T> ha, V3<T> bpos, Qt<T> brot, V3<T> hb) {
+    T g;
+    V3<T> n;
+    separating_axis(apos, arot, ha, bpos, brot, hb, g, n);
+    return g;
+}
+
+template <class T> static void support_face(V3<T> pos, Qt<T> rot, V3<T> half, V3<T> dir, V3<T>& fpos, V3<T>& ext) {  // :80-97
+    V3<T> local = qrot(conj(rot), dir);
+    V3<T> off = VZERO<T>();
+    ext = half;
+    for (int i = 0; i < 3; i++) {
+        if (std::fabs(local[i]) > C<T>(K::FACE_AXIS_EPS)) {
+            off[i] = signum(local[i]) * half[i];
+            ext[i] = T(0);
+        }
+    }
+    fpos = pos + qrot(rot, off);
+}
+
+template <class T> static Dist<T> feature_distance(V3<T> apos, Qt<T> arot, V3<T> ha, V3<T> bpos, Qt<T> brot, V3<T> hb) {  // :99-129
+    V3<T> ca[8], cb[8];
+    obb_corners(apos, ha, arot, ca);
+    obb_corners(bpos, hb, brot, cb);
+    Dist<T> res{std::numeric_limits<T>::infinity(), apos, bpos};
+    T best = std::numeric_limits<T>::infinity();
+    auto consider = [&](V3<T> x, V3<T> y) {
+        T sq = len2(y - x);
+        if (sq < best) {
+            best = sq;
+            res = {std::sqrt(sq), x, y};
+        }
+    };
+    for (int i = 0; i < 8; i++) consider(ca[i], point_obb_closest(ca[i], bpos, hb, brot));
+    for (int i = 0; i < 8; i++) consider(point_obb_closest(cb[i], apos, ha, arot), cb[i]);
+    for (int i = 0; i < 12; i++)
+        for (int j = 0; j < 12; j++) {
+            V3<T> x, y;
+            seg_seg_closest(ca[OBB_EDGES[i][0]], ca[OBB_EDGES[i][1]], cb[OBB_EDGES[j][0]], cb[OBB_EDGES[j][1]], x, y);
+            consider(x, y);
+        }
+    return res;
+}
+
+template <class T> static Dist<T> box_box(V3<T> apos, Qt<T> arot, V3<T> ha, V3<T> bpos, Qt<T> brot, V3<T> hb) {  // :131-142
+    T gap;
+    V3<T> n;
+    separating_axis(apos, arot, ha, bpos, brot, hb, gap, n);
+    if (gap > T(0)) return feature_distance(apos, arot, ha, bpos, brot, hb);
+    V3<T> fa, ea, fb, eb;
+    support_face(apos, arot, ha, n, fa, ea);
+    support_face(bpos, brot, hb, -n, fb, eb);
+    Dist<T> r = feature_distance(fa, arot, ea, fb, brot, eb);
+    r.dist = gap;
+    return r;
+}
+
+template <class T> static void segment_box(V3<T> start, V3<T> end, V3<T> lo, V3<T> hi, V3<T>& opoint, V3<T>& oclosest,
+                                           T& osq) {  // :146-190
+    V3<T> delta = end - start;
+    T cuts[8];
+    int nc = 0;
+    cuts[nc++] = T(0);
+    cuts[nc++] = T(1);
+    for (int i = 0; i < 3; i++) {
+        if (std::fabs(delta[i]) > C<T>(K::DEGENERATE_EPS)) {
+            T bnds[2] = {lo[i], hi[i]};
+            for (T bd : bnds) {
+                T t = (bd - start[i]) / delta[i];
+                if (t > T(0) && t < T(1)) cuts[nc++] = t;
+            }
+        }
+    }
+    for (int i = 1; i < nc; i++)  // ascending (f32::total_cmp on finite values)
+        for (int k = i; k > 0 && cuts[k] < cuts[k - 1]; k--) std::swap(cuts[k], cuts[k - 1]);
+    opoint = start;
+    oclosest = vclamp(start, lo, hi);
+    osq = std::numeric_limits<T>::infinity();
+    for (int w = 0; w + 1 < nc; w++) {
+        T r0 = cuts[w], r1 = cuts[w + 1];
+        T middle = (r0 + r1) * C<T>(K::HALF);
+        V3<T> p = start + middle * delta;
+        T num = T(0), den = T(0);
+        for (int i = 0; i < 3; i++) {
+            bool has = false;
+            T bd = T(0);
+            if (p[i] < lo[i]) { has = true; bd = lo[i]; }
+            else if (p[i] > hi[i]) { has = true; bd = hi[i]; }
+            if (has) {
+                num += delta[i] * (start[i] - bd);
+                den += delta[i] * delta[i];
+            }
+        }
+        T stationary = den > T(0) ? fclamp(-num / den, r0, r1) : middle;
+        T ts[3] = {stationary, r0, r1};
+        for (T t : ts) {
+            V3<T> point = start + t * delta;
+            V3<T> cl = vclamp(point, lo, hi);
+            T sq = len2(point - cl);
+            if (sq < osq) {
+                opoint = point;
+                oclosest = cl;
+                osq = sq;
+            }
+        }
+    }
+}
+
+template <class T> static void spine_penetration(V3<T> center, V3<T> axis, V3<T> half, T radius, T height, T& og,
+                                                 V3<T>& on) {  // :240-265
+    og = -std::numeric_limits<T>::infinity();
+    on = VX<T>();
+    V3<T> es[3] = {VX<T>(), VY<T>(), VZ<T>()};
+    for (auto e : es) {
+        V3<T> ns[2] = {e, normalize_or_zero(cross(axis, e))};
+        for (auto n : ns) {
+            if (n == VZERO<T>()) continue;
+            T proj = dot(center, n);
+            T gap = std::fabs(proj) - dot(half, vabs(n)) - height * std::fabs(dot(axis, n)) - radius;
+            if (gap > og) {
+                og = gap;
+                on = proj >= T(0) ? n : -n;
+            }
+        }
+    }
+}
+
+template <class T> static Dist<T> box_capsule(V3<T> apos, Qt<T> arot, V3<T> half, V3<T> bpos, Qt<T> brot, T radius,
+                                              T height) {  // :192-236
+    Qt<T> inv = conj(arot);
+    V3<T> center = qrot(inv, bpos - apos);
+    V3<T> axis = qrot(inv, qrot(brot, VY<T>()));
+    V3<T> start = center - axis * height, end = center + axis * height;
+    V3<T> core, surface;
+    T sq;
+    segment_box(start, end, -half, half, core, surface, sq);
+    T distance;
+    V3<T> normal;
+    if (sq > C<T>(K::DEGENERATE_EPS)) {
+        T l = std::sqrt(sq);
+        distance = l - radius;
+        normal = (core - surface) / l;
+    } else {
+        T depth;
+        V3<T> nrm;
+        spine_penetration(center, axis, half, radius, height, depth, nrm);
+        V3<T> lo = -half, hi = half;
+        for (int i = 0; i < 3; i++) {
+            if (std::fabs(nrm[i]) > C<T>(K::FACE_AXIS_EPS)) {
+                lo[i] = signum(nrm[i]) * half[i];
+                hi[i] = lo[i];
+            }
+        }
+        T proj = dot(axis, nrm);
+        V3<T> e0, e1;
+        if (proj > C<T>(K::SPINE_ALIGNMENT_EPS)) { e0 = start; e1 = start; }
+        else if (proj < -C<T>(K::SPINE_ALIGNMENT_EPS)) { e0 = end; e1 = end; }
+        else { e0 = start; e1 = end; }
+        T dummy;
+        segment_box(e0, e1, lo, hi, core, surface, dummy);
+        distance = depth;
+        normal = nrm;
+    }
+    return {distance, apos + qrot(arot, surface), apos + qrot(arot, core - normal * radius)};
+}
+
+template <class T> static Dist<T> halfspace_distance(V3<T> hpos, Qt<T> hrot, V3<T> ln, const ShapeRef<T>& o, bool first) {  // :607-642
+    if (o.shape == AVBD_SHAPE_HALFSPACE) {
+        T inf = std::numeric_limits<T>::infinity();
+        return first ? Dist<T>{inf, hpos, o.pos} : Dist<T>{inf, o.pos, hpos};
+    }
+    V3<T> n = qrot(hrot, ln);
+    V3<T> s = support(o.shape, o.sp, o.pos, o.rot, -n);
+    T dist = dot(s - hpos, n);
+    Dist<T> d{dist, s - n * dist, s};
+    if (first) return d;
+    return {d.dist, d.pb, d.pa};
+}
+
+// shape_distance (distance.rs:654-821) for sphere/box/capsule/half-space.
+template <class T> static Dist<T> shape_distance(const ShapeRef<T>& a, const ShapeRef<T>& b) {
+    if (a.shape == AVBD_SHAPE_HALFSPACE) return halfspace_distance(a.pos, a.rot, a.sp, b, true);
+    if (b.shape == AVBD_SHAPE_HALFSPACE) return halfspace_distance(b.pos, b.rot, b.sp, a, false);
+    uint32_t sa = a.shape, sb = b.shape;
+    auto swap = [](Dist<T> d) { return Dist<T>{d.dist, d.pb, d.pa}; };
+    if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_SPHERE) return sphere_sphere(a.pos, a.sp.x, b.pos, b.sp.x);
+    if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_BOX) return sphere_obb(a.pos, a.sp.x, b.pos, b.rot, b.sp);
+    if (sa == AVBD_SHAPE_BOX && sb == AVBD_SHAPE_SPHERE) return swap(sphere_obb(b.pos, b.sp.x, a.pos, a.rot, a.sp));
+    if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_CAPSULE)
+        return sphere_capsule(a.pos, a.sp.x, b.pos, b.rot, b.sp.x, b.sp.y);
+    if (sa == AVBD_SHAPE_CAPSULE && sb == AVBD_SHAPE_SPHERE)
+        return swap(sphere_capsule(b.pos, b.sp.x, a.pos, a.rot, a.sp.x, a.sp.y));
+    if (sa == AVBD_SHAPE_BOX && sb == AVBD_SHAPE_BOX) return box_box(a.pos, a.rot, a.sp, b.pos, b.rot, b.sp);
+    if (sa == AVBD_SHAPE_BOX && sb == AVBD_SHAPE_CAPSULE)
+        return box_capsule(a.pos, a.rot, a.sp, b.pos, b.rot, b.sp.x, b.sp.y);
+    if (sa == AVBD_SHAPE_CAPSULE && sb == AVBD_SHAPE_BOX)
+        return swap(box_capsule(b.pos, b.rot, b.sp, a.pos, a.rot, a.sp.x, a.sp.y));
+    // capsule-capsule
+    return capsule_capsule(a.pos, a.rot, a.sp.x, a.sp.y, b.pos, b.rot, b.sp.x, b.sp.y);
+}
+
+// ---- AVBD engine (avbd/*) ------------------------------------------------------
+template <class T> struct Point {
+    V3<T> ra, rb;
+    T lam[3], pen[3];
+    bool stuck;
+    T roll_lam[3];
+    int32_t matched;
+};
+template <class T> struct Pair {
+    uint32_t a, b;
+    V3<T> n;
+    T mu[2];
+    T gap;
+    std::vector<Point<T>> points;
+};
+template <class T> struct Joint {
+    uint32_t a, b, kind;
+    V3<T> la, lb, ax_a, ax_b;
+    T ref_val;
+    bool has_lim;
+    T lo, hi;
+    T acc_lim;
+    T lam_l[3], lam_a[3], pen_l[3], pen_a[3];
+};
+
+template <class T> static V3<T> tangent_t1(V3<T> n) {  // math.rs:152-160
+    V3<T> axis = std::fabs(n.x) < C<T>(K::TANGENT_REF_AXIS_DOT) ? VX<T>() : VY<T>();
+    return normalize_or(cross(n, axis), VZ<T>());
+}
+template <class T> static void tangent_basis(V3<T> n, V3<T>& t1, V3<T>& t2) {
+    t1 = tangent_t1(n);
+    t2 = cross(t1, n);
+}
+
+// avbd/rows.rs helpers
+template <class T> static Qt<T> quat_integrate(Qt<T> q, V3<T> v) {  // :110-119
+    T theta = len(v);
+    if (theta < C<T>(K::NEAR_ZERO)) return q;
+    T hth = C<T>(K::HALF) * theta;
+    T s = std::sin(hth), c = std::cos(hth);
+    T k = s / theta;
+    Qt<T> dq = qmul(Qt<T>{v.x * k, v.y * k, v.z * k, c}, q);
+    return qnormalize(dq);
+}
+template <class T> static V3<T> quat_diff_vec(Qt<T> a, Qt<T> b) {  // :128-146
+    Qt<T> r = qmul(a, Qt<T>{-b.x, -b.y, -b.z, b.w});
+    V3<T> xyz{r.x, r.y, r.z};
+    if (r.w < T(0)) xyz = -xyz;
+    T s = fmn(len(xyz), T(1));
+    if (s < C<T>(K::NEAR_ZERO)) return VZERO<T>();
+    return xyz * (T(2) * std::asin(s) / s);
+}
+template <class T> static T rem_euclid(T x, T m) {
+    T r = std::fmod(x, m);
+    return r < T(0) ? r + std::fabs(m) : r;
+}
+template <class T> static T wrap_pi(T x) { return rem_euclid(x + C<T>(K::PI), C<T>(K::TAU)) - C<T>(K::PI); }
+template <class T> static T quat_twist(Qt<T> q, V3<T> axis) {  // sequential_impulse/joints.rs:44-48
+    T t = T(2) * std::atan2(dot(V3<T>{q.x, q.y, q.z}, axis), q.w);
+    return rem_euclid(t + C<T>(K::PI), C<T>(K::TAU)) - C<T>(K::PI);
+}
+template <class T> static T hinge_twist(Qt<T> qa, Qt<T> qb, V3<T> axis) { return quat_twist(qmul(conj(qa), qb), axis); }
+
+template <class T> static int limit_state(T v, T lo, T hi, T slop) {  // :156-164  (1 lower, 0 upper, -1 none)
+    if (v <= lo + slop) return 1;
+    if (v >= hi - slop) return 0;
+    return -1;
+}
+template <class T> static int warm_limit_state(T v, T lo, T hi, T slop, T force) {  // :169-183
+    int s = limit_state(v, lo, hi, slop);
+    if (s >= 0) return s;
+    if (force < T(0)) return 1;
+    if (force > T(0)) return 0;
+    return -1;
+}
+template <class T> static T regularized_limit(T value, T initial, T bound, bool lower) {  // :187-191
+    T old = initial - bound;
+    T viol = lower ? fmn(old, T(0)) : fmx(old, T(0));
+    return value - bound - C<T>(K::ALPHA) * viol;
+}
+
+template <class T> static void world_inertia(V3<T> inertia, Qt<T> rot, T m[3][3]) {  // :194-207
+    V3<T> cols[3];
+    mat3_from_quat(rot, cols);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) {
+            T ca0 = cols[0][a], ca1 = cols[1][a], ca2 = cols[2][a];
+            T cb0 = cols[0][b], cb1 = cols[1][b], cb2 = cols[2][b];
+            m[a][b] = ca0 * inertia.x * cb0 + ca1 * inertia.y * cb1 + ca2 * inertia.z * cb2;
+        }
+}
+template <class T> static void inverse_symmetric(const T m[3][3], V3<T> diag, T o[3][3]) {  // :211-241
+    T a = m[0][0], b = m[0][1], c = m[0][2], d = m[1][1], e = m[1][2], f = m[2][2];
+    T det = a * (d * f - e * e) - b * (b * f - c * e) + c * (b * e - c * d);
+    if (std::fabs(det) < C<T>(K::DEGENERATE_LEN2)) {
+        T ix = diag.x > T(0) ? T(1) / diag.x : T(0);
+        T iy = diag.y > T(0) ? T(1) / diag.y : T(0);
+        T iz = diag.z > T(0) ? T(1) / diag.z : T(0);
+        T r[3][3] = {{ix, 0, 0}, {0, iy, 0}, {0, 0, iz}};
+        std::memcpy(o, r, sizeof(r));
+        return;
+    }
+    T id = T(1) / det;
+    o[0][0] = (d * f - e * e) * id; o[0][1] = (c * e - b * f) * id; o[0][2] = (b * e - c * d) * id;
+    o[1][0] = (c * e - b * f) * id; o[1][1] = (a * f - c * c) * id; o[1][2] = (b * c - a * e) * id;
+    o[2][0] = (b * e - c * d) * id; o[2][1] = (b * c - a * e) * id; o[2][2] = (a * d - b * b) * id;
+}
+template <class T> static V3<T> mat3_vec(const T m[3][3], V3<T> v) {
+    return {m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
+            m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z};
+}
+
+template <class T> static T bound_radius(const Body<T>& b) {  // rows.rs:253-292
+    switch (b.shape) {
+        case AVBD_SHAPE_SPHERE: return b.sp.x;
+        case AVBD_SHAPE_BOX: return len(b.sp);
+        case AVBD_SHAPE_CAPSULE: return b.sp.y + b.sp.x;
+        default: return std::numeric_limits<T>::infinity();
+    }
+}
+template <class T> static T shape_min_dimension(const Body<T>& b) {  // rows.rs:373-403
+    switch (b.shape) {
+        case AVBD_SHAPE_SPHERE: return b.sp.x;
+        case AVBD_SHAPE_BOX: return min_element(b.sp);
+        case AVBD_SHAPE_CAPSULE: return b.sp.x;
+        default: return std::numeric_limits<T>::infinity();
+    }
+}
+template <class T> static bool pair_allowed(const Body<T>& a, const Body<T>& b) {  // rows.rs:366-368
+    return (a.layer & b.mask) != 0 && (b.layer & a.mask) != 0;
+}
+template <class T> static T eff_inv_mass(const Body<T>& b) { return b.type == AVBD_BODY_DYNAMIC ? b.inv_mass : T(0); }
+template <class T> static bool row_live(T c, T f) { return std::fabs(c) >= C<T>(K::C_EPS) || f != T(0); }
+
+template <class T> static void outer(V3<T> a, V3<T> b, T o[3][3]) {
+    T av[3] = {a.x, a.y, a.z}, bv[3] = {b.x, b.y, b.z};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) o[i][j] = av[i] * bv[j];
+}
+template <class T> static void stamp_row(T lhs[6][6], T rhs[6], V3<T> axis, T pen, T f, V3<T> r, T sign) {  // :1064-1092
+    V3<T> nn = sign * axis;
+    V3<T> t = cross(r, nn);
+    T onn[3][3], ott[3][3], ont[3][3];
+    outer(nn, nn, onn);
+    outer(t, t, ott);
+    outer(nn, t, ont);
+    for (int x = 0; x < 3; x++)
+        for (int y = 0; y < 3; y++) {
+            lhs[x][y] += pen * onn[x][y];
+            lhs[3 + x][3 + y] += pen * ott[x][y];
+            lhs[x][3 + y] += pen * ont[x][y];
+            lhs[3 + x][y] += pen * ont[y][x];
+        }
+    rhs[0] += f * nn.x; rhs[1] += f * nn.y; rhs[2] += f * nn.z;
+    rhs[3] += f * t.x; rhs[4] += f * t.y; rhs[5] += f * t.z;
+}
+template <class T> static void stamp_angular(T lhs[6][6], T rhs[6], V3<T> g, T pen, T f) {
+    T o[3][3];
+    outer(g, g, o);
+    for (int x = 0; x < 3; x++)
+        for (int y = 0; y < 3; y++) lhs[3 + x][3 + y] += pen * o[x][y];
+    rhs[3] += f * g.x; rhs[4] += f * g.y; rhs[5] += f * g.z;
+}
+
+// avbd/assembly.rs:25-69
+template <class T> static bool solve_6x6(const T lhs[6][6], const T rhs[6], T x[6]) {
+    T l[6][6] = {};
+    T d[6] = {};
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j <= i; j++) {
+            T s = lhs[i][j];
+            for (int k = 0; k < j; k++) s -= l[i][k] * d[k] * l[j][k];
+            if (i == j) {
+                if (s <= C<T>(K::DEGENERATE_LEN2)) return false;
+                d[i] = s;
+                l[i][i] = T(1);
+            } else {
+                l[i][j] = s / d[j];
+            }
+        }
+    T y[6], z[6];
+    for (int i = 0; i < 6; i++) {
+        T s = rhs[i];
+        for (int k = 0; k < i; k++) s -= l[i][k] * y[k];
+        y[i] = s;
+    }
+    for (int i = 0; i < 6; i++) z[i] = y[i] / d[i];
+    for (int i = 5; i >= 0; i--) {
+        T s = z[i];
+        for (int k = i + 1; k < 6; k++) s -= l[k][i] * x[k];
+        x[i] = s;
+    }
+    return true;
+}
+
+// Colouring priority hash (shared definition with the GPU colouring kernel).
+static inline uint32_t colour_hash(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+enum Mode { REFERENCE = 0, COLOURED = 1 };
+
+template <class T> struct Engine {
+    AvbdParams prm;
+    int mode = REFERENCE;
+    int threads = 1;
+    bool faithful_scan = false;  // true: solve_body scans every pair/joint (the reference's O(P) scan)
+    V3<T> gravity;
+    T dt;
+    std::vector<Body<T>> bodies;
+    std::vector<Pair<T>> pairs;
+    std::vector<Joint<T>> joints;
+    std::vector<V3<T>> pos0, inertial, prev_pos;
+    std::vector<Qt<T>> rot0, inertial_rot, prev_rot;
+    std::vector<T> sleep_timer;
+    std::vector<uint8_t> asleep;
+    std::vector<int32_t> colour;
+    T time_debt = T(0);
+    uint64_t steps = 0, breakdowns = 0, ccd_hits = 0;
+    uint64_t ncolours = 0;
+    // adjacency (same order as the pair vector) for the non-faithful sweep
+    std::vector<std::vector<uint32_t>> adj_pairs, adj_joints;
+
+    bool solvable(uint32_t h) const { return bodies[h].type == AVBD_BODY_DYNAMIC && bodies[h].inv_mass > T(0); }
+
+    void ensure_scratch() {  // mod.rs:1183-1200
+        size_t n = bodies.size(), old = pos0.size();
+        pos0.resize(n, VZERO<T>()); rot0.resize(n, qident<T>());
+        inertial.resize(n, VZERO<T>()); inertial_rot.resize(n, qident<T>());
+        sleep_timer.resize(n, T(0)); asleep.resize(n, 0);
+        prev_pos.resize(n, VZERO<T>()); prev_rot.resize(n, qident<T>());
+        colour.resize(n, -1);
+        for (size_t h = std::min(old, n); h < n; h++) { prev_pos[h] = bodies[h].pos; prev_rot[h] = bodies[h].rot; }
+    }
+
+    void sleep_body(uint32_t h) {  // mod.rs:822-828, body.rs:403-408
+        if (h >= asleep.size() || bodies[h].type != AVBD_BODY_DYNAMIC) return;
+        Body<T>& b = bodies[h];
+        b.vel = VZERO<T>(); b.angvel = VZERO<T>(); b.inv_mass = T(0); b.inertia = VZERO<T>();
+        asleep[h] = 1;
+    }
+    void wake_body(uint32_t h) {  // mod.rs:833-842, body.rs:412-418
+        if (h >= asleep.size() || !asleep[h]) return;
+        asleep[h] = 0;
+        sleep_timer[h] = T(0);
+        Body<T>& b = bodies[h];
+        if (b.type == AVBD_BODY_DYNAMIC) {
+            T m = b.mass;
+            b.inv_mass = (m > T(0)) ? T(1) / m : T(0);
+            b.inertia = shape_inertia(b.shape, b.sp, m);
+        }
+    }
+
+    // ---- joints / sleep (avbd/sleep.rs) ----
+    T joint_rest_error(const Joint<T>& j) const {
+        const Body<T>& a = bodies[j.a];
+        const Body<T>& b = bodies[j.b];
+        V3<T> delta = (b.pos + qrot(b.rot, j.lb)) - (a.pos + qrot(a.rot, j.la));
+        if (j.kind == AVBD_JOINT_BALL) return len(delta);
+        V3<T> axis = qrot(a.rot, j.ax_a);
+        return fmx(len(delta), len(axis - qrot(b.rot, j.ax_b)));
+    }
+    bool joint_driven(const Joint<T>& j) const {
+        uint32_t m[2] = {j.a, j.b};
+        for (uint32_t h : m) {
+            const Body<T>& b = bodies[h];
+            if (b.type != AVBD_BODY_DYNAMIC && (b.pos != prev_pos[h] || b.rot != prev_rot[h])) return true;
+        }
+        return false;
+    }
+    void propagate_joint_flags(std::vector<uint8_t>& flags, uint8_t value) const {
+        for (;;) {
+            bool changed = false;
+            for (const Joint<T>& j : joints) {
+                uint32_t mem[4] = {j.a, j.b, j.a, j.b};
+                bool any = false;
+                for (uint32_t h : mem)
+                    if (bodies[h].type == AVBD_BODY_DYNAMIC && flags[h] == value) any = true;
+                if (any)
+                    for (uint32_t h : mem)
+                        if (bodies[h].type == AVBD_BODY_DYNAMIC && flags[h] != value) { flags[h] = value; changed = true; }
+            }
+            if (!changed) break;
+        }
+    }
+    void wake_joint_motion() {
+        size_t n = bodies.size();
+        std::vector<uint8_t> awake(n);
+        for (size_t h = 0; h < n; h++) {
+            const Body<T>& b = bodies[h];
+            awake[h] = b.type == AVBD_BODY_DYNAMIC &&
+                       (!asleep[h] || b.vel != VZERO<T>() || b.angvel != VZERO<T>() || b.torque != VZERO<T>() ||
+                        b.pos != prev_pos[h] || b.rot != prev_rot[h]);
+        }
+        for (const Joint<T>& j : joints) {
+            if (joint_driven(j) || joint_rest_error(j) > C<T>(K::JOINT_REST_ERROR)) {
+                uint32_t mem[2] = {j.a, j.b};
+                for (uint32_t h : mem)
+                    if (bodies[h].type == AVBD_BODY_DYNAMIC) awake[h] = 1;
+            }
+        }
+        propagate_joint_flags(awake, 1);
+        for (size_t h = 0; h < n; h++)
+            if (awake[h] && asleep[h]) wake_body((uint32_t)h);
+    }
+    std::vector<uint8_t> joint_sleep_ready() const {
+        std::vector<uint8_t> ready(bodies.size(), 1);
+        for (const Joint<T>& j : joints)
+            if (joint_driven(j) || joint_rest_error(j) > C<T>(K::JOINT_REST_ERROR)) { ready[j.a] = 0; ready[j.b] = 0; }
+        propagate_joint_flags(ready, 0);
+        return ready;
+    }
+
+    // ---- pair discovery (avbd/rows.rs:432-756) ----
+    struct Discovered {
+        uint32_t ia, ib;
+        bool trigger, exists;
+        V3<T> normal;
+        T mu[2];
+        T sgn;
+        std::vector<std::pair<V3<T>, V3<T>>> fresh;
+        bool wake_vote;
+    };
+    const Pair<T>* find_pair(uint32_t ia, uint32_t ib) const {
+        for (const Pair<T>& p : pairs)
+            if (p.a == ia && p.b == ib) return &p;
+        return nullptr;
+    }
+    static bool no_collide_kind(uint32_t k) { return k == AVBD_JOINT_BALL || k == AVBD_JOINT_REVOLUTE; }
+
+    bool discover_pair(uint32_t ia, uint32_t ib, Discovered& out) const {
+        const Body<T>& a = bodies[ia];
+        const Body<T>& b = bodies[ib];
+        if (!pair_allowed(a, b)) return false;
+        if (!a.trigger() && !b.trigger()) {
+            for (const Joint<T>& j : joints)
+                if (no_collide_kind(j.kind) && ((j.a == ia && j.b == ib) || (j.a == ib && j.b == ia))) return false;
+        }
+        T ra = bound_radius(a), rb = bound_radius(b);
+        if (len(a.pos - b.pos) > ra + rb + C<T>(K::GEN_MARGIN)) return false;
+        Dist<T> d = shape_distance(sref(a), sref(b));
+        T sgn = (a.shape == AVBD_SHAPE_BOX && b.shape == AVBD_SHAPE_BOX)
+                    ? box_box_signed_gap(a.pos, a.rot, a.sp, b.pos, b.rot, b.sp)
+                    : d.dist;
+        out.ia = ia; out.ib = ib;
+        out.fresh.clear();
+        if (a.trigger() || b.trigger()) {
+            out.trigger = true; out.exists = false; out.normal = VY<T>(); out.mu[0] = out.mu[1] = T(0);
+            out.sgn = sgn; out.wake_vote = false;
+            return true;
+        }
+        out.trigger = false;
+        const Pair<T>* stored = find_pair(ia, ib);
+        // orient_contact_normal (rows.rs:303-333)
+        V3<T> normal;
+        if (a.shape == AVBD_SHAPE_HALFSPACE) normal = -qrot(a.rot, a.sp);
+        else if (b.shape == AVBD_SHAPE_HALFSPACE) normal = qrot(b.rot, b.sp);
+        else {
+            V3<T> nm = d.pa - d.pb;
+            if (d.dist < T(0)) nm = -nm;
+            if (len2(nm) < C<T>(K::AXIS_REST_LEN2)) nm = a.pos - b.pos;
+            nm = normalize_or(nm, VY<T>());
+            if (stored) {
+                if (dot(nm, stored->n) < T(0)) nm = -nm;
+            } else if (dot(nm, a.pos - b.pos) < T(0)) {
+                nm = -nm;
+            }
+            normal = nm;
+        }
+        bool exists = stored != nullptr;
+        T approach = fmx(dot(b.vel - a.vel, normal), T(0));
+        T reach = C<T>(K::GEN_MARGIN) + approach * dt;
+        if (sgn > reach && !exists) return false;
+        bool separated = sgn > reach;
+        T mu = fmx(a.friction, b.friction);  // friction_frame, isotropic bodies
+        out.mu[0] = fmx(mu, T(0));
+        out.mu[1] = fmx(mu, T(0));
+        T patch = fmn(ra, rb) + C<T>(K::MARGIN);
+        V3<T> pp = (d.pa + d.pb) * C<T>(K::HALF);
+        V3<T> pa_c = a.pos - normal * dot(a.pos - pp, normal);
+        V3<T> pb_c = b.pos - normal * dot(b.pos - pp, normal);
+        auto plane = [&](const Body<T>& body, V3<T> witness, T sign) -> T {
+            if (body.shape == AVBD_SHAPE_BOX) {
+                T extent = dot(vabs(qrot(conj(body.rot), normal)), body.sp);
+                return dot(normal, body.pos) - sign * extent;
+            }
+            return dot(normal, witness);
+        };
+        T plane_a = plane(a, d.pa, T(1));
+        T plane_b = plane(b, d.pb, T(-1));
+        auto& fresh = out.fresh;
+        auto dup = [&](V3<T> ral, V3<T> rbl) {
+            for (auto& e : fresh)
+                if (len(e.first - ral) < C<T>(K::POINT_MATCH_DIST) && len(e.second - rbl) < C<T>(K::POINT_MATCH_DIST))
+                    return true;
+            return false;
+        };
+        Qt<T> inv_a = conj(a.rot), inv_b = conj(b.rot);
+        if (!separated) {
+            struct Side { uint32_t h; V3<T> witness; T sign; V3<T> pc; };
+            Side sides[2] = {{ia, d.pa, T(1), pa_c}, {ib, d.pb, T(-1), pb_c}};
+            for (const Side& sd : sides) {
+                const Body<T>& body = bodies[sd.h];
+                if (body.shape != AVBD_SHAPE_BOX) continue;
+                bool brk = false;
+                for (int ix = 0; ix < 2 && !brk; ix++)
+                    for (int iy = 0; iy < 2 && !brk; iy++)
+                        for (int iz = 0; iz < 2 && !brk; iz++) {
+                            T sx = ix ? T(1) : T(-1), sy = iy ? T(1) : T(-1), sz = iz ? T(1) : T(-1);
+                            V3<T> corner{sx * body.sp.x, sy * body.sp.y, sz * body.sp.z};
+                            V3<T> world = body.pos + qrot(body.rot, corner);
+                            T along = dot(world - sd.witness, sd.sign * normal);
+                            if (std::fabs(along) > C<T>(K::EXPAND_SLOP) + fmx(-sgn, T(0))) continue;
+                            V3<T> rel = world - sd.pc;
+                            V3<T> tang = rel - normal * dot(rel, normal);
+                            if (len(tang) > patch) continue;
+                            if ((int)fresh.size() >= MAX_POINTS) { brk = true; break; }
+                            V3<T> pa, pb;
+                            if (sd.h == ia) { pa = world; pb = world + normal * (plane_b - dot(normal, world)); }
+                            else { pa = world + normal * (plane_a - dot(normal, world)); pb = world; }
+                            V3<T> ral = qrot(inv_a, pa - a.pos), rbl = qrot(inv_b, pb - b.pos);
+                            if (dup(ral, rbl)) continue;
+                            fresh.push_back({ral, rbl});
+                        }
+            }
+        }
+        if (!separated && fresh.size() >= 2 && (int)fresh.size() < MAX_POINTS) {
+            V3<T> mid = ra < rb ? pa_c : (rb < ra ? pb_c : (pa_c + pb_c) * C<T>(K::HALF));
+            V3<T> pa = mid + normal * (plane_a - dot(normal, mid));
+            V3<T> pb = mid + normal * (plane_b - dot(normal, mid));
+            V3<T> ral = qrot(inv_a, pa - a.pos), rbl = qrot(inv_b, pb - b.pos);
+            if (!dup(ral, rbl)) fresh.push_back({ral, rbl});
+        }
+        if (!separated && fresh.size() < 3) {
+            V3<T> ral = qrot(inv_a, d.pa - a.pos), rbl = qrot(inv_b, d.pb - b.pos);
+            if (!dup(ral, rbl)) fresh.push_back({ral, rbl});
+        }
+        bool wake_vote;
+        if (exists) {
+            wake_vote = (asleep[ia] || asleep[ib]) && sgn < -C<T>(K::WAKE_PENETRATION);
+        } else {
+            bool impact = sgn < -C<T>(K::WAKE_PENETRATION);
+            if (!impact) {
+                uint32_t ss[2] = {ia, ib}, oo[2] = {ib, ia};
+                T sg[2] = {T(1), T(-1)};
+                for (int k = 0; k < 2; k++) {
+                    if (asleep[ss[k]]) {
+                        T app = dot(bodies[oo[k]].vel - bodies[ss[k]].vel, sg[k] * normal);
+                        if (app > C<T>(K::WAKE_IMPACT_SPEED)) { impact = true; break; }
+                    }
+                }
+            }
+            wake_vote = impact;
+        }
+        out.exists = exists; out.normal = normal; out.sgn = sgn; out.wake_vote = wake_vote;
+        return true;
+    }
+
+    // generate_pairs (rows.rs:767-943)
+    void generate_pairs() {
+        uint32_t n = (uint32_t)bodies.size();
+        std::vector<Discovered> disc;
+        if (threads > 1 && n > 256) {
+            // Parallel over the first index, like the rayon split at rows.rs:769-782;
+            // the sort below restores canonical order.
+            int nt = threads;
+            std::vector<std::vector<Discovered>> parts(nt);
+            std::vector<std::thread> th;
+            for (int t = 0; t < nt; t++)
+                th.emplace_back([&, t]() {
+                    Discovered d;
+                    for (uint32_t ia = t; ia < n; ia += nt)
+                        for (uint32_t ib = ia + 1; ib < n; ib++)
+                            if (discover_pair(ia, ib, d)) parts[t].push_back(d);
+                });
+            for (auto& x : th) x.join();
+            for (auto& p : parts)
+                for (auto& d : p) disc.push_back(std::move(d));
+        } else {
+            Discovered d;
+            for (uint32_t ia = 0; ia < n; ia++)
+                for (uint32_t ib = ia + 1; ib < n; ib++)
+                    if (discover_pair(ia, ib, d)) disc.push_back(d);
+        }
+        std::stable_sort(disc.begin(), disc.end(), [](const Discovered& x, const Discovered& y) {
+            return x.ia != y.ia ? x.ia < y.ia : x.ib < y.ib;
+        });
+        std::vector<std::pair<uint32_t, uint32_t>> wake;
+        auto make_points_fresh = [](const Discovered& d) {
+            std::vector<Point<T>> pts;
+            for (auto& f : d.fresh) {
+                Point<T> p{};
+                p.ra = f.first; p.rb = f.second;
+                for (int k = 0; k < 3; k++) { p.lam[k] = T(0); p.pen[k] = C<T>(K::PENALTY_INIT); p.roll_lam[k] = T(0); }
+                p.stuck = true;
+                p.matched = -1;
+                pts.push_back(p);
+            }
+            return pts;
+        };
+        auto merge_points = [&](const Pair<T>& old, const Discovered& d) {
+            std::vector<Point<T>> next;
+            bool touching = d.sgn <= T(0);
+            bool smooth = bodies[d.ia].shape == AVBD_SHAPE_SPHERE || bodies[d.ib].shape == AVBD_SHAPE_SPHERE;
+            for (auto& f : d.fresh) {
+                int m = -1;
+                for (size_t k = 0; k < old.points.size(); k++)
+                    if (len(old.points[k].ra - f.first) < C<T>(K::LAMBDA_MATCH_DIST)) { m = (int)k; break; }
+                Point<T> p{};
+                if (m >= 0) {
+                    const Point<T>& o = old.points[m];
+                    if (o.stuck && touching && !smooth) { p.ra = o.ra; p.rb = o.rb; }
+                    else { p.ra = f.first; p.rb = f.second; }
+                    for (int k = 0; k < 3; k++) { p.lam[k] = o.lam[k]; p.pen[k] = o.pen[k]; p.roll_lam[k] = o.roll_lam[k]; }
+                    p.stuck = o.stuck;
+                    p.matched = m;
+                } else {
+                    p.ra = f.first; p.rb = f.second;
+                    for (int k = 0; k < 3; k++) { p.lam[k] = T(0); p.pen[k] = C<T>(K::PENALTY_INIT); p.roll_lam[k] = T(0); }
+                    p.stuck = true;
+                    p.matched = -1;
+                }
+                next.push_back(p);
+            }
+            return next;
+        };
+        if (mode == REFERENCE) {
+            std::vector<uint8_t> seen(pairs.size(), 0);
+            for (auto& d : disc) {
+                if (d.trigger) continue;
+                if (d.exists) {
+                    size_t idx = 0;
+                    bool found = false;
+                    for (; idx < pairs.size(); idx++)
+                        if (pairs[idx].a == d.ia && pairs[idx].b == d.ib) { found = true; break; }
+                    if (!found) continue;
+                    seen[idx] = 1;
+                    Pair<T>& p = pairs[idx];
+                    p.n = d.normal; p.mu[0] = d.mu[0]; p.mu[1] = d.mu[1]; p.gap = d.sgn;
+                    if (d.wake_vote) wake.push_back({d.ia, d.ib});
+                    p.points = merge_points(p, d);
+                } else {
+                    seen.push_back(1);
+                    if (d.wake_vote) wake.push_back({d.ia, d.ib});
+                    Pair<T> p;
+                    p.a = d.ia; p.b = d.ib; p.n = d.normal; p.mu[0] = d.mu[0]; p.mu[1] = d.mu[1]; p.gap = d.sgn;
+                    p.points = make_points_fresh(d);
+                    pairs.push_back(std::move(p));
+                }
+            }
+            for (size_t idx = seen.size(); idx-- > 0;)
+                if (!seen[idx]) {
+                    pairs[idx] = std::move(pairs.back());
+                    pairs.pop_back();
+                }
+        } else {
+            // Coloured schedule: the pair vector is the discovered set in (a, b)
+            // order.  Same per-pair merge, no swap_remove reordering.
+            std::vector<Pair<T>> next;
+            for (auto& d : disc) {
+                if (d.trigger) continue;
+                Pair<T> p;
+                p.a = d.ia; p.b = d.ib; p.n = d.normal; p.mu[0] = d.mu[0]; p.mu[1] = d.mu[1]; p.gap = d.sgn;
+                if (d.exists) {
+                    const Pair<T>* old = find_pair(d.ia, d.ib);
+                    if (!old) continue;
+                    p.points = merge_points(*old, d);
+                } else {
+                    p.points = make_points_fresh(d);
+                }
+                if (d.wake_vote) wake.push_back({d.ia, d.ib});
+                next.push_back(std::move(p));
+            }
+            pairs = std::move(next);
+        }
+        for (auto& w : wake) { wake_body(w.first); wake_body(w.second); }
+    }
+
+    // ---- contact rows (rows.rs:947-1060, joints_ext.rs:21-32) ----
+    V3<T> lever_a(const Body<T>& a, V3<T> n, const Point<T>& pt) const {
+        return a.shape == AVBD_SHAPE_SPHERE ? -n * a.sp.x : qrot(a.rot, pt.ra);
+    }
+    V3<T> lever_b(const Body<T>& b, V3<T> n, const Point<T>& pt) const {
+        return b.shape == AVBD_SHAPE_SPHERE ? n * b.sp.x : qrot(b.rot, pt.rb);
+    }
+    T gap_c0(const Pair<T>& p, const Point<T>& pt) const {
+        const Body<T>& a = bodies[p.a];
+        const Body<T>& b = bodies[p.b];
+        if (a.shape == AVBD_SHAPE_SPHERE || b.shape == AVBD_SHAPE_SPHERE) return p.gap + C<T>(K::MARGIN);
+        V3<T> pa = pos0[p.a] + qrot(rot0[p.a], pt.ra);
+        V3<T> pb = pos0[p.b] + qrot(rot0[p.b], pt.rb);
+        return dot(p.n, pa - pb) + C<T>(K::MARGIN);
+    }
+    T row_c_levers(const Pair<T>& p, V3<T> u, T c0, V3<T> raw, V3<T> rbw) const {
+        const Body<T>& a = bodies[p.a];
+        const Body<T>& b = bodies[p.b];
+        V3<T> da = a.pos - pos0[p.a] + u * dot(cross(raw, u), quat_diff_vec(a.rot, rot0[p.a]));
+        V3<T> db = b.pos - pos0[p.b] + u * dot(cross(rbw, u), quat_diff_vec(b.rot, rot0[p.b]));
+        return c0 * (T(1) - C<T>(K::ALPHA)) + dot(u, da - db);
+    }
+    void friction_levers(const Pair<T>& p, const Point<T>& pt, V3<T>& raf, V3<T>& rbf) const {
+        const Body<T>& a = bodies[p.a];
+        const Body<T>& b = bodies[p.b];
+        V3<T> raw = lever_a(a, p.n, pt), rbw = lever_b(b, p.n, pt);
+        T sep = dot((a.pos + raw) - (b.pos + rbw), p.n);
+        raf = raw - p.n * (sep * C<T>(K::HALF));
+        rbf = rbw + p.n * (sep * C<T>(K::HALF));
+    }
+    static void contact_force(T cn, const T pens[3], const T lam[3], T ct0, T ct1, const T mu[2], T f[3]) {
+        T fnc = fmn(pens[0] * cn + lam[0], T(0));
+        T fr0 = pens[1] * ct0 + lam[1], fr1 = pens[2] * ct1 + lam[2];
+        T b1 = std::fabs(fnc) * mu[0], b2 = std::fabs(fnc) * mu[1];
+        if (b1 <= T(0) || b2 <= T(0)) {
+            f[0] = fnc;
+            f[1] = b1 <= T(0) ? T(0) : fclamp(fr0, -b1, b1);
+            f[2] = b2 <= T(0) ? T(0) : fclamp(fr1, -b2, b2);
+            return;
+        }
+        T s = (fr0 / b1) * (fr0 / b1) + (fr1 / b2) * (fr1 / b2);
+        T k = s > T(1) ? T(1) / std::sqrt(s) : T(1);
+        f[0] = fnc; f[1] = fr0 * k; f[2] = fr1 * k;
+    }
+
+    void stamp_contacts_for(uint32_t h, uint32_t pi, T lhs[6][6], T rhs[6]) const {
+        const Pair<T>& p = pairs[pi];
+        bool is_a = p.a == h;
+        T sign = is_a ? T(1) : T(-1);
+        const Body<T>& A = bodies[p.a];
+        const Body<T>& B = bodies[p.b];
+        V3<T> n = p.n;
+        for (size_t qi = 0; qi < p.points.size(); qi++) {
+            const Point<T>& pt = p.points[qi];
+            bool touching = p.gap <= T(0);
+            T c0 = touching ? gap_c0(p, pt) : T(0);
+            V3<T> rup = lever_a(A, n, pt), rlo = lever_b(B, n, pt);
+            T cn = row_c_levers(p, n, c0, rup, rlo);
+            V3<T> r_side = is_a ? rup : rlo;
+            if (!touching) {
+                T approach = fmx(dot(B.vel - A.vel, n), T(0));
+                if (p.gap - approach * dt > T(0)) continue;
+                if (std::fabs(cn) >= C<T>(K::C_EPS)) {
+                    T npts = T(std::max<size_t>(p.points.size(), 1));
+                    T ka = eff_inv_mass(A), kb = eff_inv_mass(B);
+                    T m_red = ka + kb > C<T>(K::NEAR_ZERO) ? T(1) / (ka + kb) : T(0);
+                    if (m_red > T(0)) {
+                        T pen_d = fmn(T(2) * m_red / (dt * dt) / npts, C<T>(K::PENALTY_MAX));
+                        T f_d = fmn(pen_d * cn, T(0));
+                        stamp_row(lhs, rhs, n, pen_d, f_d, r_side, sign);
+                    }
+                }
+                continue;
+            }
+            V3<T> t1 = tangent_t1(n);
+            V3<T> t2 = cross(t1, n);
+            V3<T> raf, rbf;
+            friction_levers(p, pt, raf, rbf);
+            V3<T> r_side_f = is_a ? raf : rbf;
+            T ct1 = row_c_levers(p, t1, T(0), raf, rbf);
+            T ct2 = row_c_levers(p, t2, T(0), raf, rbf);
+            T f[3];
+            contact_force(cn, pt.pen, pt.lam, ct1, ct2, p.mu, f);
+            V3<T> axes[3] = {n, t1, t2};
+            T cvs[3] = {cn, ct1, ct2};
+            V3<T> rs[3] = {r_side, r_side_f, r_side_f};
+            for (int row = 0; row < 3; row++) {
+                if (!row_live(cvs[row], f[row])) continue;
+                stamp_row(lhs, rhs, axes[row], pt.pen[row], f[row], rs[row], sign);
+            }
+            T mu_roll = fmx(A.rolling, B.rolling), mu_spin = fmx(A.torsion, B.torsion);
+            if (mu_roll > T(0) || mu_spin > T(0)) {
+                V3<T> wrel = quat_diff_vec(A.rot, rot0[p.a]) - quat_diff_vec(B.rot, rot0[p.b]);
+                V3<T> rax[3] = {t1, t2, n};
+                T murs[3] = {mu_roll, mu_roll, mu_spin};
+                for (int li = 0; li < 3; li++) {
+                    if (murs[li] <= T(0)) continue;
+                    T c = dot(wrel, rax[li]);
+                    T cap = murs[li] * std::fabs(f[0]);
+                    T fr = fclamp(C<T>(K::ROLL_PEN) * c + pt.roll_lam[li], -cap, cap);
+                    V3<T> g = is_a ? rax[li] : -rax[li];
+                    T o[3][3];
+                    outer(g, g, o);
+                    for (int x = 0; x < 3; x++)
+                        for (int y = 0; y < 3; y++) lhs[3 + x][3 + y] += C<T>(K::ROLL_PEN) * o[x][y];
+                    rhs[3] += fr * g.x; rhs[4] += fr * g.y; rhs[5] += fr * g.z;
+                }
+            }
+        }
+    }
+
+    void stamp_joint_for(uint32_t h, const Joint<T>& j, T lhs[6][6], T rhs[6]) const {  // assembly.rs:255-881
+        bool is_a = j.a == h;
+        T sign = is_a ? T(1) : T(-1);
+        const Body<T>& a = bodies[j.a];
+        const Body<T>& b = bodies[j.b];
+        V3<T> pa = a.pos + qrot(a.rot, j.la);
+        V3<T> pb = b.pos + qrot(b.rot, j.lb);
+        V3<T> pa0 = pos0[j.a] + qrot(rot0[j.a], j.la);
+        V3<T> pb0 = pos0[j.b] + qrot(rot0[j.b], j.lb);
+        V3<T> live = pa - pb, c0v = pa0 - pb0;
+        V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+        V3<T> fl = VZERO<T>();
+        for (int k = 0; k < 3; k++) {
+            V3<T> axis = VZERO<T>();
+            axis[k] = T(1);
+            T c = live[k] - C<T>(K::ALPHA) * c0v[k];
+            T f = j.pen_l[k] * c + j.lam_l[k];
+            if (!row_live(c, f)) continue;
+            // Ball/Revolute levers add a zero offset (the Fixed weld's dref slot).
+            V3<T> r_side = is_a ? qrot(a.rot, j.la + VZERO<T>()) : qrot(b.rot, j.lb);
+            stamp_row(lhs, rhs, axis, j.pen_l[k], f, r_side, sign);
+            fl[k] = f;
+        }
+        {
+            V3<T> r = is_a ? qrot(a.rot, j.la + VZERO<T>()) : -qrot(b.rot, j.lb);
+            T hm[3][3] = {};
+            T arr[3] = {r.x, r.y, r.z};
+            for (int k = 0; k < 3; k++) {
+                T g[3][3] = {};
+                g[0][0] = -arr[k]; g[1][1] = -arr[k]; g[2][2] = -arr[k];
+                g[0][k] += arr[0]; g[1][k] += arr[1]; g[2][k] += arr[2];
+                for (int x = 0; x < 3; x++)
+                    for (int y = 0; y < 3; y++) hm[x][y] += g[x][y] * fl[k];
+            }
+            V3<T> hd{len(V3<T>{hm[0][0], hm[1][0], hm[2][0]}), len(V3<T>{hm[0][1], hm[1][1], hm[2][1]}),
+                     len(V3<T>{hm[0][2], hm[1][2], hm[2][2]})};
+            lhs[3][3] += hd.x; lhs[4][4] += hd.y; lhs[5][5] += hd.z;
+        }
+        if (j.kind == AVBD_JOINT_REVOLUTE) {
+            V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
+            V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
+            V3<T> t1, t2;
+            tangent_basis(axa0, t1, t2);
+            V3<T> ts[2] = {t1, t2};
+            for (int li = 0; li < 2; li++) {
+                V3<T> t = ts[li];
+                T c = dot(t, axa - axb) - C<T>(K::ALPHA) * dot(t, axa0 - axb0);
+                T f = j.pen_a[li] * c + j.lam_a[li];
+                if (!row_live(c, f)) continue;
+                V3<T> g = is_a ? cross(axa, t) : -cross(axb, t);
+                stamp_angular(lhs, rhs, g, j.pen_a[li], f);
+            }
+            if (j.has_lim) {
+                T angle = wrap_pi(hinge_twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+                int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
+                if (st >= 0) {
+                    bool lower = st == 1;
+                    T initial = wrap_pi(hinge_twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                    T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
+                    T f_raw = j.pen_a[2] * c + j.acc_lim;
+                    T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
+                    if (row_live(c, f)) stamp_angular(lhs, rhs, is_a ? -wa : wa, j.pen_a[2], f);
+                }
+            }
+        }
+    }
+
+    void solve_body(uint32_t h) {  // assembly.rs:73-903
+        const Body<T>& bd = bodies[h];
+        T dt2 = dt * dt;
+        T m_dt2 = T(1) / eff_inv_mass(bd) / dt2;
+        T iw[3][3];
+        world_inertia(bd.inertia, bd.rot, iw);
+        T lhs[6][6] = {};
+        T rhs[6] = {};
+        for (int i = 0; i < 3; i++) lhs[i][i] = m_dt2;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) lhs[3 + a][3 + b] = iw[a][b] / dt2;
+        V3<T> rl = m_dt2 * (bd.pos - inertial[h]);
+        rhs[0] = rl.x; rhs[1] = rl.y; rhs[2] = rl.z;
+        V3<T> ra = mat3_vec(iw, quat_diff_vec(bd.rot, inertial_rot[h])) / dt2;
+        rhs[3] = ra.x; rhs[4] = ra.y; rhs[5] = ra.z;
+        if (faithful_scan) {
+            for (uint32_t pi = 0; pi < pairs.size(); pi++)
+                if (pairs[pi].a == h || pairs[pi].b == h) stamp_contacts_for(h, pi, lhs, rhs);
+            for (const Joint<T>& j : joints)
+                if (j.a == h || j.b == h) stamp_joint_for(h, j, lhs, rhs);
+        } else {
+            for (uint32_t pi : adj_pairs[h]) stamp_contacts_for(h, pi, lhs, rhs);
+            for (uint32_t ji : adj_joints[h]) stamp_joint_for(h, joints[ji], lhs, rhs);
+        }
+        T neg[6] = {-rhs[0], -rhs[1], -rhs[2], -rhs[3], -rhs[4], -rhs[5]};
+        T dx[6];
+        if (solve_6x6(lhs, neg, dx)) {
+            Body<T>& b = bodies[h];
+            b.pos = b.pos + V3<T>{dx[0], dx[1], dx[2]};
+            b.rot = quat_integrate(b.rot, V3<T>{dx[3], dx[4], dx[5]});
+        } else {
+            breakdowns++;
+        }
+    }
+
+    void dual_update() {  // joints_ext.rs:464-919
+        for (Pair<T>& p : pairs) {
+            V3<T> n = p.n;
+            V3<T> t1 = tangent_t1(n);
+            V3<T> t2 = cross(t1, n);
+            const Body<T>& A = bodies[p.a];
+            const Body<T>& B = bodies[p.b];
+            for (size_t qi = 0; qi < p.points.size(); qi++) {
+                Point<T>& pt = p.points[qi];
+                bool touching = p.gap <= T(0);
+                T c0 = touching ? gap_c0(p, pt) : T(0);
+                T cn = row_c_levers(p, n, c0, lever_a(A, n, pt), lever_b(B, n, pt));
+                V3<T> raf, rbf;
+                friction_levers(p, pt, raf, rbf);
+                T ct1 = row_c_levers(p, t1, T(0), raf, rbf);
+                T ct2 = row_c_levers(p, t2, T(0), raf, rbf);
+                T pen[3] = {pt.pen[0], pt.pen[1], pt.pen[2]};
+                T lam[3] = {pt.lam[0], pt.lam[1], pt.lam[2]};
+                T f[3];
+                contact_force(cn, pen, lam, ct1, ct2, p.mu, f);
+                {
+                    T bnd = std::fabs(f[0]) * fmx(p.mu[0], p.mu[1]);
+                    T fu0 = pen[1] * ct1 + lam[1], fu1 = pen[2] * ct2 + lam[2];
+                    T fs = std::sqrt(fu0 * fu0 + fu1 * fu1);
+                    pt.stuck = fs <= bnd && std::sqrt(ct1 * ct1 + ct2 * ct2) < C<T>(K::STICK_THRESH);
+                }
+                if (touching && std::fabs(cn) >= C<T>(K::C_EPS)) {
+                    pt.lam[0] = f[0];
+                    if (f[0] < T(0)) pt.pen[0] = fmn(pt.pen[0] + C<T>(K::BETA) * std::fabs(cn), C<T>(K::PENALTY_MAX));
+                }
+                T b1 = std::fabs(f[0]) * p.mu[0], b2 = std::fabs(f[0]) * p.mu[1];
+                T fu0 = pen[1] * ct1 + lam[1], fu1 = pen[2] * ct2 + lam[2];
+                T s_ell = (b1 > T(0) && b2 > T(0)) ? (fu0 / b1) * (fu0 / b1) + (fu1 / b2) * (fu1 / b2)
+                                                   : std::numeric_limits<T>::infinity();
+                if (touching) {
+                    pt.lam[1] = f[1];
+                    pt.lam[2] = f[2];
+                    if (s_ell <= T(1)) {
+                        if (std::fabs(ct1) >= C<T>(K::C_EPS)) pt.pen[1] = fmn(pt.pen[1] + C<T>(K::BETA) * std::fabs(ct1), C<T>(K::PENALTY_MAX));
+                        if (std::fabs(ct2) >= C<T>(K::C_EPS)) pt.pen[2] = fmn(pt.pen[2] + C<T>(K::BETA) * std::fabs(ct2), C<T>(K::PENALTY_MAX));
+                    }
+                }
+                T mu_roll = fmx(A.rolling, B.rolling), mu_spin = fmx(A.torsion, B.torsion);
+                if (touching && (mu_roll > T(0) || mu_spin > T(0))) {
+                    V3<T> wrel = quat_diff_vec(A.rot, rot0[p.a]) - quat_diff_vec(B.rot, rot0[p.b]);
+                    T lam_n = std::fabs(pt.lam[0]);
+                    T rl[3] = {pt.roll_lam[0], pt.roll_lam[1], pt.roll_lam[2]};
+                    V3<T> rax[3] = {t1, t2, n};
+                    T murs[3] = {mu_roll, mu_roll, mu_spin};
+                    for (int li = 0; li < 3; li++) {
+                        if (murs[li] <= T(0)) continue;
+                        T c = dot(wrel, rax[li]);
+                        T cap = murs[li] * lam_n;
+                        pt.roll_lam[li] = fclamp(C<T>(K::ROLL_PEN) * c + rl[li], -cap, cap);
+                    }
+                }
+            }
+        }
+        for (Joint<T>& j : joints) {
+            const Body<T>& a = bodies[j.a];
+            const Body<T>& b = bodies[j.b];
+            V3<T> pa = a.pos + qrot(a.rot, j.la);
+            V3<T> pb = b.pos + qrot(b.rot, j.lb);
+            V3<T> pa0 = pos0[j.a] + qrot(rot0[j.a], j.la);
+            V3<T> pb0 = pos0[j.b] + qrot(rot0[j.b], j.lb);
+            V3<T> live = pa - pb, c0v = pa0 - pb0;
+            for (int k = 0; k < 3; k++) {
+                T c = live[k] - C<T>(K::ALPHA) * c0v[k];
+                if (std::fabs(c) >= C<T>(K::C_EPS)) {
+                    j.lam_l[k] += j.pen_l[k] * c;
+                    j.pen_l[k] = fmn(j.pen_l[k] + C<T>(K::BETA) * std::fabs(c), C<T>(K::PENALTY_MAX));
+                }
+            }
+            if (j.kind == AVBD_JOINT_REVOLUTE) {
+                V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
+                V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
+                V3<T> t1, t2;
+                tangent_basis(axa0, t1, t2);
+                V3<T> ts[2] = {t1, t2};
+                for (int li = 0; li < 2; li++) {
+                    T c = dot(ts[li], axa - axb) - C<T>(K::ALPHA) * dot(ts[li], axa0 - axb0);
+                    if (std::fabs(c) < C<T>(K::C_EPS)) continue;
+                    j.lam_a[li] = j.pen_a[li] * c + j.lam_a[li];
+                    j.pen_a[li] = fmn(j.pen_a[li] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::PENALTY_MAX));
+                }
+                if (j.has_lim) {
+                    T angle = wrap_pi(hinge_twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+                    int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
+                    if (st >= 0) {
+                        bool lower = st == 1;
+                        T initial = wrap_pi(hinge_twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                        T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
+                        if (std::fabs(c) >= C<T>(K::C_EPS)) {
+                            T f = j.pen_a[2] * c + j.acc_lim;
+                            j.acc_lim = lower ? fmn(f, T(0)) : fmx(f, T(0));
+                            j.pen_a[2] = fmn(j.pen_a[2] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::LIM_PEN_MAX));
+                        }
+                    } else {
+                        j.acc_lim = T(0);
+                    }
+                }
+            }
+        }
+    }
+
+    // Greedy colouring in descending hash priority == the GPU's Jones-Plassmann colouring.
+    void compute_colouring() {
+        uint32_t n = (uint32_t)bodies.size();
+        std::vector<std::vector<uint32_t>> nb(n);
+        auto solved = [&](uint32_t h) { return solvable(h) && !asleep[h]; };
+        for (const Pair<T>& p : pairs)
+            if (!p.points.empty() && solved(p.a) && solved(p.b)) { nb[p.a].push_back(p.b); nb[p.b].push_back(p.a); }
+        for (const Joint<T>& j : joints)
+            if (solved(j.a) && solved(j.b)) { nb[j.a].push_back(j.b); nb[j.b].push_back(j.a); }
+        std::vector<uint32_t> order;
+        for (uint32_t h = 0; h < n; h++) {
+            colour[h] = -1;
+            if (solved(h)) order.push_back(h);
+        }
+        auto prio_gt = [](uint32_t x, uint32_t y) {
+            uint32_t hx = colour_hash(x), hy = colour_hash(y);
+            return hx != hy ? hx > hy : x > y;
+        };
+        std::sort(order.begin(), order.end(), prio_gt);
+        int32_t maxc = -1;
+        std::vector<uint8_t> used;
+        for (uint32_t h : order) {
+            used.assign(nb[h].size() + 2, 0);
+            for (uint32_t o : nb[h])
+                if (colour[o] >= 0 && colour[o] < (int32_t)used.size()) used[colour[o]] = 1;
+            int32_t c = 0;
+            while (used[c]) c++;
+            colour[h] = c;
+            maxc = std::max(maxc, c);
+        }
+        ncolours = (uint64_t)(maxc + 1);
+    }
+
+    void build_adjacency() {
+        size_t n = bodies.size();
+        adj_pairs.assign(n, {});
+        adj_joints.assign(n, {});
+        for (uint32_t pi = 0; pi < pairs.size(); pi++) {
+            adj_pairs[pairs[pi].a].push_back(pi);
+            if (pairs[pi].b != pairs[pi].a) adj_pairs[pairs[pi].b].push_back(pi);
+        }
+        for (uint32_t ji = 0; ji < joints.size(); ji++) {
+            adj_joints[joints[ji].a].push_back(ji);
+            adj_joints[joints[ji].b].push_back(ji);
+        }
+        // adjacency lists are filled in ascending pair index: same order as
+        // the reference's scan over the pair vector (assembly.rs:99-106).
+        for (size_t h = 0; h < n; h++) std::sort(adj_pairs[h].begin(), adj_pairs[h].end());
+    }
+
+    // ---- CCD (mod.rs:882-978, distance.rs:841-893) ----
+    void ccd_pass() {
+        uint32_t n = (uint32_t)bodies.size();
+        for (uint32_t h = 0; h < n; h++) {
+            if (!solvable(h) || asleep[h] || bodies[h].trigger()) continue;
+            V3<T> disp = bodies[h].vel * dt;
+            if (len(disp) <= C<T>(K::CCD_TRAVEL_GATE_FRACTION) * shape_min_dimension(bodies[h])) continue;
+            std::vector<uint32_t> joined;
+            for (const Joint<T>& j : joints) {
+                if (j.a == h) joined.push_back(j.b);
+                else if (j.b == h) joined.push_back(j.a);
+            }
+            T L = len(disp);
+            if (L < C<T>(K::NEAR_ZERO)) continue;
+            V3<T> dir = disp / L;
+            bool have = false;
+            T best_t = T(0);
+            V3<T> best_n{};
+            uint32_t best_h = 0;
+            const Body<T>& mb = bodies[h];
+            for (uint32_t o = 0; o < n; o++) {
+                if (o == h || bodies[o].trigger() || !pair_allowed(bodies[h], bodies[o])) continue;
+                if (std::find(joined.begin(), joined.end(), o) != joined.end()) continue;
+                ShapeRef<T> tgt = sref(bodies[o]);
+                T t = T(0);
+                bool hit = false;
+                V3<T> hn{};
+                for (int it = 0; it < 24; it++) {
+                    ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot};
+                    Dist<T> d = shape_distance(mv, tgt);
+                    if (d.dist <= C<T>(K::SHAPE_TOUCH)) {
+                        if (t > T(0)) { hit = true; hn = normalize_or(d.pa - d.pb, -dir); }
+                        break;
+                    }
+                    t += d.dist - C<T>(K::SHAPE_TOUCH) * C<T>(K::HALF);
+                    if (t >= L) break;
+                }
+                if (hit && (!have || t < best_t)) { have = true; best_t = t; best_n = hn; best_h = o; }
+            }
+            if (!have) continue;
+            ccd_hits++;
+            T l2 = fmx(L, C<T>(K::MIN_TOI_DISP_LENGTH));
+            T frac = fclamp(best_t / l2, T(0), T(1));
+            T e = fmn(bodies[h].restitution, bodies[best_h].restitution);
+            Body<T>& b = bodies[h];
+            b.pos = b.pos + disp * frac;
+            T vn = dot(b.vel, best_n);
+            if (vn < T(0)) {
+                T bounce = vn < -C<T>(K::CCD_BOUNCE_SPEED) ? T(1) + e : T(1);
+                b.vel = b.vel - best_n * (bounce * vn);
+            }
+            wake_body(best_h);
+            sleep_timer[h] = T(0);
+        }
+    }
+
+    // ---- one fixed substep (mod.rs:846-1143) ----
+    void step_inner() {
+        ensure_scratch();
+        wake_joint_motion();
+        uint32_t n = (uint32_t)bodies.size();
+        for (uint32_t h = 0; h < n; h++) {
+            if (!solvable(h)) continue;
+            Body<T>& b = bodies[h];
+            T iw[3][3], inv[3][3];
+            world_inertia(b.inertia, b.rot, iw);
+            V3<T> dg{b.inertia.x > T(0) ? b.inertia.x : T(0), b.inertia.y > T(0) ? b.inertia.y : T(0),
+                     b.inertia.z > T(0) ? b.inertia.z : T(0)};
+            inverse_symmetric(iw, dg, inv);
+            V3<T> tq = b.torque;
+            b.torque = VZERO<T>();
+            b.angvel = b.angvel + mat3_vec(inv, tq) * dt;
+        }
+        if (prm.enable_ccd) ccd_pass();
+        generate_pairs();
+        wake_joint_motion();
+        for (uint32_t h = 0; h < n; h++)
+            if (asleep[h]) {
+                const Body<T>& b = bodies[h];
+                if (len(b.vel) > C<T>(K::SLEEP_LIN) || len(b.angvel) > C<T>(K::SLEEP_ANG)) wake_body(h);
+            }
+        for (uint32_t h = 0; h < n; h++) {
+            if (bodies[h].type == AVBD_BODY_KINEMATIC) { pos0[h] = prev_pos[h]; rot0[h] = prev_rot[h]; }
+            else { pos0[h] = bodies[h].pos; rot0[h] = bodies[h].rot; }
+            if (!solvable(h)) { inertial[h] = bodies[h].pos; inertial_rot[h] = bodies[h].rot; continue; }
+            const Body<T>& b = bodies[h];
+            inertial[h] = b.pos + b.vel * dt + gravity * (dt * dt);
+            inertial_rot[h] = quat_integrate(b.rot, b.angvel * dt);
+        }
+        const T ag = C<T>(K::ALPHA) * C<T>(K::GAMMA);
+        for (Pair<T>& p : pairs)
+            for (Point<T>& pt : p.points)
+                for (int k = 0; k < 3; k++) {
+                    pt.lam[k] *= ag;
+                    pt.roll_lam[k] *= ag;
+                    pt.pen[k] = fclamp(pt.pen[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
+                }
+        for (Joint<T>& j : joints)
+            for (int k = 0; k < 3; k++) {
+                j.lam_l[k] *= ag;
+                j.lam_a[k] *= ag;
+                j.pen_l[k] = fclamp(j.pen_l[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
+                j.pen_a[k] = fclamp(j.pen_a[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
+            }
+        for (uint32_t h = 0; h < n; h++) {
+            if (!solvable(h) || asleep[h]) continue;
+            bodies[h].pos = inertial[h];
+            bodies[h].rot = inertial_rot[h];
+        }
+        if (!faithful_scan) build_adjacency();
+        std::vector<std::vector<uint32_t>> by_colour;
+        if (mode == COLOURED) {
+            compute_colouring();
+            by_colour.assign(ncolours, {});
+            for (uint32_t h = 0; h < n; h++)
+                if (colour[h] >= 0) by_colour[colour[h]].push_back(h);
+        }
+        for (int it = 0; it < prm.iterations; it++) {
+            if (mode == COLOURED) {
+                for (auto& group : by_colour)
+                    for (uint32_t h : group) solve_body(h);
+            } else {
+                for (uint32_t h = n; h-- > 0;)
+                    if (solvable(h) && !asleep[h]) solve_body(h);
+            }
+            dual_update();
+        }
+        for (uint32_t h = 0; h < n; h++) {
+            if (!solvable(h) || asleep[h]) continue;
+            Body<T>& b = bodies[h];
+            b.vel = (b.pos - pos0[h]) / dt;
+            V3<T> spin = quat_diff_vec(b.rot, rot0[h]);
+            b.angvel = len(spin) < C<T>(K::SPIN_REST_EPS) ? VZERO<T>() : spin / dt;
+            b.rot = qnormalize(b.rot);
+        }
+        if (prm.enable_sleep) {
+            std::vector<uint8_t> supported(n, 0);
+            for (const Pair<T>& p : pairs)
+                if (p.gap <= T(0) && !p.points.empty()) { supported[p.a] = 1; supported[p.b] = 1; }
+            for (const Joint<T>& j : joints) { supported[j.a] = 1; supported[j.b] = 1; }
+            std::vector<uint8_t> ready = joint_sleep_ready();
+            std::vector<uint8_t> freeze(asleep.begin(), asleep.end());
+            for (uint32_t h = 0; h < n; h++) {
+                if (!solvable(h) || asleep[h]) continue;
+                if (!supported[h] || !ready[h]) { sleep_timer[h] = T(0); continue; }
+                const Body<T>& b = bodies[h];
+                if (len(b.vel) < C<T>(K::SLEEP_LIN) && len(b.angvel) < C<T>(K::SLEEP_ANG)) {
+                    sleep_timer[h] += dt;
+                    freeze[h] = sleep_timer[h] >= C<T>(K::SLEEP_TIME);
+                } else {
+                    sleep_timer[h] = T(0);
+                }
+            }
+            propagate_joint_flags(freeze, 0);
+            for (uint32_t h = 0; h < n; h++)
+                if (freeze[h] && !asleep[h]) sleep_body(h);
+        }
+        for (uint32_t h = 0; h < n; h++) { prev_pos[h] = bodies[h].pos; prev_rot[h] = bodies[h].rot; }
+        steps++;
+    }
+
+    void step(float host_dt) {  // mod.rs:1212-1235
+        if (!std::isfinite(host_dt) || host_dt <= 0.0f) return;
+        T sd = dt;
+        time_debt = fmn(time_debt + T(host_dt), sd * T(prm.max_substeps));
+        int k = 0;
+        while (time_debt >= sd && k < prm.max_substeps) {
+            time_debt -= sd;
+            k++;
+            step_inner();
+        }
+    }
+
+    int add_joint(const AvbdJointDesc& d, uint32_t& handle) {  // mod.rs:1310-1529
+        for (int k = 0; k < 3; k++)
+            if (!std::isfinite(d.local_anchor_a[k]) || !std::isfinite(d.local_anchor_b[k]) ||
+                !std::isfinite(d.local_axis_a[k]) || !std::isfinite(d.local_axis_b[k]))
+                return AVBD_ERR_JOINT_NONFINITE;
+        if (d.kind != AVBD_JOINT_BALL && d.kind != AVBD_JOINT_REVOLUTE) return AVBD_ERR_UNSUPPORTED;
+        wake_body(d.body_a);
+        wake_body(d.body_b);
+        if (d.body_a == d.body_b) return AVBD_ERR_JOINT_SELF;
+        if (d.body_a >= bodies.size() || d.body_b >= bodies.size()) return AVBD_ERR_JOINT_HANDLES;
+        Joint<T> j{};
+        j.a = d.body_a; j.b = d.body_b; j.kind = d.kind;
+        j.la = {T(d.local_anchor_a[0]), T(d.local_anchor_a[1]), T(d.local_anchor_a[2])};
+        j.lb = {T(d.local_anchor_b[0]), T(d.local_anchor_b[1]), T(d.local_anchor_b[2])};
+        j.ax_a = VX<T>(); j.ax_b = VX<T>();
+        j.ref_val = T(0);
+        if (d.kind == AVBD_JOINT_REVOLUTE) {
+            V3<T> aa{T(d.local_axis_a[0]), T(d.local_axis_a[1]), T(d.local_axis_a[2])};
+            V3<T> ab{T(d.local_axis_b[0]), T(d.local_axis_b[1]), T(d.local_axis_b[2])};
+            if (len2(aa) < C<T>(K::DEGENERATE_LEN2) || len2(ab) < C<T>(K::DEGENERATE_LEN2)) return AVBD_ERR_JOINT_BAD_AXIS;
+            j.ax_a = normalize_or(aa, VZ<T>());
+            j.ax_b = normalize_or(ab, VZ<T>());
+            j.ref_val = hinge_twist(bodies[j.a].rot, bodies[j.b].rot, j.ax_a);
+            j.has_lim = d.has_limit != 0;
+            j.lo = T(d.limit_min);
+            j.hi = T(d.limit_max);
+        }
+        j.acc_lim = T(0);
+        for (int k = 0; k < 3; k++) {
+            j.lam_l[k] = j.lam_a[k] = T(0);
+            j.pen_l[k] = j.pen_a[k] = C<T>(K::JOINT_PENALTY_INIT);
+        }
+        joints.push_back(j);
+        handle = (uint32_t)(joints.size() - 1);
+        return AVBD_OK;
+    }
+};
+
+template <class T> static Body<T> from_desc(const AvbdBody& s) {
+    Body<T> b;
+    b.pos = {T(s.position[0]), T(s.position[1]), T(s.position[2])};
+    b.rot = {T(s.orientation[0]), T(s.orientation[1]), T(s.orientation[2]), T(s.orientation[3])};
+    b.vel = {T(s.velocity[0]), T(s.velocity[1]), T(s.velocity[2])};
+    b.angvel = {T(s.angular_velocity[0]), T(s.angular_velocity[1]), T(s.angular_velocity[2])};
+    b.torque = {T(s.torque[0]), T(s.torque[1]), T(s.torque[2])};
+    b.mass = T(s.mass); b.inv_mass = T(s.inv_mass);
+    b.inertia = {T(s.inertia[0]), T(s.inertia[1]), T(s.inertia[2])};
+    b.restitution = T(s.restitution); b.friction = T(s.friction); b.friction_t = T(s.friction_transverse);
+    b.rolling = T(s.rolling_friction); b.torsion = T(s.torsion_friction);
+    b.shape = s.shape;
+    b.sp = {T(s.shape_params[0]), T(s.shape_params[1]), T(s.shape_params[2])};
+    b.layer = s.collision_layer; b.mask = s.collision_mask; b.type = s.body_type; b.flags = s.flags;
+    return b;
+}
+template <class T> static void to_desc(const Body<T>& b, AvbdBody& s) {
+    s.position[0] = float(b.pos.x); s.position[1] = float(b.pos.y); s.position[2] = float(b.pos.z);
+    s.orientation[0] = float(b.rot.x); s.orientation[1] = float(b.rot.y); s.orientation[2] = float(b.rot.z); s.orientation[3] = float(b.rot.w);
+    s.velocity[0] = float(b.vel.x); s.velocity[1] = float(b.vel.y); s.velocity[2] = float(b.vel.z);
+    s.angular_velocity[0] = float(b.angvel.x); s.angular_velocity[1] = float(b.angvel.y); s.angular_velocity[2] = float(b.angvel.z);
+    s.torque[0] = float(b.torque.x); s.torque[1] = float(b.torque.y); s.torque[2] = float(b.torque.z);
+    s.mass = float(b.mass); s.inv_mass = float(b.inv_mass);
+    s.inertia[0] = float(b.inertia.x); s.inertia[1] = float(b.inertia.y); s.inertia[2] = float(b.inertia.z);
+    s.restitution = float(b.restitution); s.friction = float(b.friction); s.friction_transverse = float(b.friction_t);
+    s.rolling_friction = float(b.rolling); s.torsion_friction = float(b.torsion);
+    s.shape = b.shape;
+    s.shape_params[0] = float(b.sp.x); s.shape_params[1] = float(b.sp.y); s.shape_params[2] = float(b.sp.z);
+    s.collision_layer = b.layer; s.collision_mask = b.mask; s.body_type = b.type; s.flags = b.flags;
+}
+
+struct OracleBase {
+    virtual ~OracleBase() {}
+};
+template <class T> struct Oracle : OracleBase {
+    Engine<T> e;
+};
+
+}  // namespace orc
+
+// ---- C API for the tests (ctypes) ----------------------------------------------
+using namespace orc;
+
+struct OracleWorld {
+    int dbl;
+    Engine<float>* f;
+    Engine<double>* d;
+};
+
+#define DISPATCH(w, ...)                                 \
+    do {                                                 \
+        if ((w)->dbl) { auto& E = *(w)->d; __VA_ARGS__; } \
+        else { auto& E = *(w)->f; __VA_ARGS__; }          \
+    } while (0)
+
+extern "C" {
+
+// mode: 0 = Reference, 1 = Coloured.  use_double: 0 = f32, 1 = f64.
+OracleWorld* oracle_world_create(const AvbdParams* p, int mode, int use_double, int threads) {
+    OracleWorld* w = new OracleWorld{use_double, nullptr, nullptr};
+    auto init = [&](auto& E) {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        E.prm = *p;
+        E.mode = mode;
+        E.threads = threads;
+        E.gravity = {TT(p->gravity[0]), TT(p->gravity[1]), TT(p->gravity[2])};
+        E.dt = TT(p->step_dt);
+    };
+    if (use_double) { w->d = new Engine<double>(); init(*w->d); }
+    else { w->f = new Engine<float>(); init(*w->f); }
+    return w;
+}
+void oracle_world_destroy(OracleWorld* w) {
+    if (!w) return;
+    delete w->f;
+    delete w->d;
+    delete w;
+}
+void oracle_set_faithful_scan(OracleWorld* w, int on) { DISPATCH(w, E.faithful_scan = on != 0); }
+int oracle_add_bodies(OracleWorld* w, const AvbdBody* b, uint32_t n) {
+    DISPATCH(w, {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        for (uint32_t i = 0; i < n; i++) E.bodies.push_back(from_desc<TT>(b[i]));
+    });
+    return AVBD_OK;
+}
+int oracle_add_joint(OracleWorld* w, const AvbdJointDesc* d, uint32_t* handle) {
+    int rc = 0;
+    DISPATCH(w, rc = E.add_joint(*d, *handle));
+    return rc;
+}
+int oracle_step(OracleWorld* w, float dt) {
+    DISPATCH(w, E.step(dt));
+    return AVBD_OK;
+}
+int oracle_step_fixed(OracleWorld* w, int32_t nsub) {
+    DISPATCH(w, for (int i = 0; i < nsub; i++) E.step_inner());
+    return AVBD_OK;
+}
+uint32_t oracle_body_count(OracleWorld* w) {
+    uint32_t n = 0;
+    DISPATCH(w, n = (uint32_t)E.bodies.size());
+    return n;
+}
+int oracle_get_bodies(OracleWorld* w, AvbdBody* out) {
+    DISPATCH(w, for (size_t i = 0; i < E.bodies.size(); i++) to_desc(E.bodies[i], out[i]));
+    return AVBD_OK;
+}
+// Full-precision body poses/velocities as doubles: 13 per body (pos, quat, vel, angvel).
+int oracle_get_state13(OracleWorld* w, double* out) {
+    DISPATCH(w, for (size_t i = 0; i < E.bodies.size(); i++) {
+        auto& b = E.bodies[i];
+        double v[13] = {double(b.pos.x), double(b.pos.y), double(b.pos.z), double(b.rot.x), double(b.rot.y),
+                        double(b.rot.z), double(b.rot.w), double(b.vel.x), double(b.vel.y), double(b.vel.z),
+                        double(b.angvel.x), double(b.angvel.y), double(b.angvel.z)};
+        std::memcpy(out + 13 * i, v, sizeof(v));
+    });
+    return AVBD_OK;
+}
+int oracle_set_bodies(OracleWorld* w, const AvbdBody* in, uint32_t n) {
+    DISPATCH(w, {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        if (n != E.bodies.size()) return AVBD_ERR_INVALID_ARG;
+        for (uint32_t i = 0; i < n; i++) E.bodies[i] = from_desc<TT>(in[i]);
+    });
+    return AVBD_OK;
+}
+uint32_t oracle_joint_count(OracleWorld* w) {
+    uint32_t n = 0;
+    DISPATCH(w, n = (uint32_t)E.joints.size());
+    return n;
+}
+uint32_t oracle_pair_count(OracleWorld* w) {
+    uint32_t n = 0;
+    DISPATCH(w, n = (uint32_t)E.pairs.size());
+    return n;
+}
+int oracle_export_state(OracleWorld* w, AvbdBody* bodies, AvbdBodyAux* aux, AvbdPairState* pairs,
+                        AvbdPointState* points, AvbdJointState* joints) {
+    DISPATCH(w, {
+        E.ensure_scratch();
+        for (size_t i = 0; i < E.bodies.size(); i++) {
+            if (bodies) to_desc(E.bodies[i], bodies[i]);
+            if (aux) {
+                auto& x = aux[i];
+                x.prev_position[0] = float(E.prev_pos[i].x); x.prev_position[1] = float(E.prev_pos[i].y); x.prev_position[2] = float(E.prev_pos[i].z);
+                x.prev_orientation[0] = float(E.prev_rot[i].x); x.prev_orientation[1] = float(E.prev_rot[i].y);
+                x.prev_orientation[2] = float(E.prev_rot[i].z); x.prev_orientation[3] = float(E.prev_rot[i].w);
+                x.sleep_timer = float(E.sleep_timer[i]);
+                x.asleep = E.asleep[i];
+            }
+        }
+        for (size_t i = 0; i < E.pairs.size(); i++) {
+            auto& p = E.pairs[i];
+            if (pairs) {
+                auto& s = pairs[i];
+                s.a = p.a; s.b = p.b;
+                s.normal[0] = float(p.n.x); s.normal[1] = float(p.n.y); s.normal[2] = float(p.n.z);
+                s.mu[0] = float(p.mu[0]); s.mu[1] = float(p.mu[1]);
+                s.gap = float(p.gap);
+                s.npoints = (uint32_t)p.points.size();
+            }
+            if (points) {
+                for (int k = 0; k < AVBD_MAX_POINTS; k++) {
+                    AvbdPointState& q = points[i * AVBD_MAX_POINTS + k];
+                    std::memset(&q, 0, sizeof(q));
+                    q.matched = -1;
+                    if (k >= (int)p.points.size()) continue;
+                    auto& pt = p.points[k];
+                    for (int c = 0; c < 3; c++) {
+                        q.ra[c] = float(pt.ra[c]); q.rb[c] = float(pt.rb[c]);
+                        q.lam[c] = float(pt.lam[c]); q.pen[c] = float(pt.pen[c]); q.roll_lam[c] = float(pt.roll_lam[c]);
+                    }
+                    q.stuck = pt.stuck;
+                    q.matched = pt.matched;
+                }
+            }
+        }
+        if (joints)
+            for (size_t i = 0; i < E.joints.size(); i++) {
+                auto& j = E.joints[i];
+                auto& s = joints[i];
+                for (int c = 0; c < 3; c++) {
+                    s.lam_l[c] = float(j.lam_l[c]); s.lam_a[c] = float(j.lam_a[c]);
+                    s.pen_l[c] = float(j.pen_l[c]); s.pen_a[c] = float(j.pen_a[c]);
+                }
+                s.acc_lim = float(j.acc_lim);
+            }
+    });
+    return AVBD_OK;
+}
+int oracle_import_state(OracleWorld* w, const AvbdBody* bodies, const AvbdBodyAux* aux, const AvbdPairState* pairs,
+                        const AvbdPointState* points, uint32_t npairs, const AvbdJointState* joints) {
+    DISPATCH(w, {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        E.ensure_scratch();
+        size_t n = E.bodies.size();
+        for (size_t i = 0; i < n; i++) {
+            if (bodies) E.bodies[i] = from_desc<TT>(bodies[i]);
+            if (aux) {
+                E.prev_pos[i] = {TT(aux[i].prev_position[0]), TT(aux[i].prev_position[1]), TT(aux[i].prev_position[2])};
+                E.prev_rot[i] = {TT(aux[i].prev_orientation[0]), TT(aux[i].prev_orientation[1]),
+                                 TT(aux[i].prev_orientation[2]), TT(aux[i].prev_orientation[3])};
+                E.sleep_timer[i] = TT(aux[i].sleep_timer);
+                E.asleep[i] = aux[i].asleep ? 1 : 0;
+            }
+        }
+        if (pairs) {
+            E.pairs.clear();
+            for (uint32_t i = 0; i < npairs; i++) {
+                Pair<TT> p;
+                p.a = pairs[i].a; p.b = pairs[i].b;
+                p.n = {TT(pairs[i].normal[0]), TT(pairs[i].normal[1]), TT(pairs[i].normal[2])};
+                p.mu[0] = TT(pairs[i].mu[0]); p.mu[1] = TT(pairs[i].mu[1]);
+                p.gap = TT(pairs[i].gap);
+                for (uint32_t k = 0; k < pairs[i].npoints && k < AVBD_MAX_POINTS; k++) {
+                    const AvbdPointState& q = points[i * AVBD_MAX_POINTS + k];
+                    Point<TT> pt{};
+                    for (int c = 0; c < 3; c++) {
+                        pt.ra[c] = TT(q.ra[c]); pt.rb[c] = TT(q.rb[c]);
+                        pt.lam[c] = TT(q.lam[c]); pt.pen[c] = TT(q.pen[c]); pt.roll_lam[c] = TT(q.roll_lam[c]);
+                    }
+                    pt.stuck = q.stuck != 0;
+                    pt.matched = q.matched;
+                    p.points.push_back(pt);
+                }
+                E.pairs.push_back(std::move(p));
+            }
+        }
+        if (joints)
+            for (size_t i = 0; i < E.joints.size(); i++) {
+                auto& j = E.joints[i];
+                for (int c = 0; c < 3; c++) {
+                    j.lam_l[c] = TT(joints[i].lam_l[c]); j.lam_a[c] = TT(joints[i].lam_a[c]);
+                    j.pen_l[c] = TT(joints[i].pen_l[c]); j.pen_a[c] = TT(joints[i].pen_a[c]);
+                }
+                j.acc_lim = TT(joints[i].acc_lim);
+            }
+    });
+    return AVBD_OK;
+}
+int oracle_get_colours(OracleWorld* w, int32_t* out) {
+    DISPATCH(w, for (size_t i = 0; i < E.bodies.size(); i++) out[i] = i < E.colour.size() ? E.colour[i] : -1);
+    return AVBD_OK;
+}
+int oracle_get_counters(OracleWorld* w, AvbdCounters* c) {
+    std::memset(c, 0, sizeof(*c));
+    DISPATCH(w, {
+        c->steps = E.steps;
+        c->pairs = E.pairs.size();
+        uint64_t pts = 0;
+        for (auto& p : E.pairs) pts += p.points.size();
+        c->points = pts;
+        c->colours = E.ncolours;
+        c->breakdowns = E.breakdowns;
+        c->ccd_hits = E.ccd_hits;
+        uint64_t sl = 0;
+        for (auto s : E.asleep) sl += s;
+        c->sleeping = sl;
+    });
+    return AVBD_OK;
+}
+
+// ---- row-level known-answer hooks (gpu_batches.rs:781-898) ----
+void oracle_stamp_row(float* lhs36, float* rhs6, const float* axis, float pen, float f, const float* lever, float sign) {
+    float lhs[6][6], rhs[6];
+    std::memcpy(lhs, lhs36, sizeof(lhs));
+    std::memcpy(rhs, rhs6, sizeof(rhs));
+    stamp_row<float>(lhs, rhs, {axis[0], axis[1], axis[2]}, pen, f, {lever[0], lever[1], lever[2]}, sign);
+    std::memcpy(lhs36, lhs, sizeof(lhs));
+    std::memcpy(rhs6, rhs, sizeof(rhs));
+}
+int oracle_solve_6x6(const float* lhs36, const float* rhs6, float* x6) {
+    float lhs[6][6];
+    std::memcpy(lhs, lhs36, sizeof(lhs));
+    bool ok = solve_6x6<float>(lhs, rhs6, x6);
+    if (!ok)
+        for (int i = 0; i < 6; i++) x6[i] = 0.0f;
+    return ok ? 1 : 0;
+}
+void oracle_tangent_basis(const float* n, float* t1, float* t2) {
+    V3<float> a, b;
+    tangent_basis<float>({n[0], n[1], n[2]}, a, b);
+    t1[0] = a.x; t1[1] = a.y; t1[2] = a.z;
+    t2[0] = b.x; t2[1] = b.y; t2[2] = b.z;
+}
+void oracle_shape_inertia(uint32_t shape, const float* sp, float mass, float* out) {
+    V3<float> r = shape_inertia<float>(shape, {sp[0], sp[1], sp[2]}, mass);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+uint32_t oracle_colour_hash(uint32_t x) { return colour_hash(x); }
+
+// RigidBody constructors (body.rs:346-376, :470-576, :873-889): default
+// materials per shape and the mass triple of Mass::from_kind
+// (invariants.rs:175-199).
+int oracle_body_new(uint32_t shape, const float* params, const float* position, float mass, AvbdBody* out) {
+    std::memset(out, 0, sizeof(*out));
+    float rest = 0.3f, fric = 0.5f;
+    float sp[3] = {params[0], params[1], params[2]};
+    if (shape == AVBD_SHAPE_SPHERE) { rest = 0.5f; fric = 0.3f; }
+    else if (shape == AVBD_SHAPE_CAPSULE) { rest = 0.4f; fric = 0.4f; }
+    else if (shape == AVBD_SHAPE_HALFSPACE) {
+        if (mass > 0.0f && std::isfinite(mass)) return AVBD_ERR_INVALID_ARG;
+        V3<float> nn = normalize_or(V3<float>{sp[0], sp[1], sp[2]}, VZERO<float>());
+        if (nn == VZERO<float>()) return AVBD_ERR_INVALID_ARG;
+        sp[0] = nn.x; sp[1] = nn.y; sp[2] = nn.z;
+        rest = 0.3f; fric = 0.6f;
+    } else if (shape != AVBD_SHAPE_BOX) {
+        return AVBD_ERR_UNSUPPORTED;
+    }
+    bool free = mass > 0.0f && std::isfinite(mass);
+    for (int i = 0; i < 3; i++) out->position[i] = position[i];
+    out->orientation[3] = 1.0f;
+    out->mass = free ? mass : 0.0f;
+    out->inv_mass = free ? 1.0f / mass : 0.0f;
+    V3<float> in = shape_inertia<float>(shape, {sp[0], sp[1], sp[2]}, free ? mass : 0.0f);
+    out->inertia[0] = in.x; out->inertia[1] = in.y; out->inertia[2] = in.z;
+    out->restitution = rest;
+    out->friction = fric;
+    out->friction_transverse = fric;
+    out->shape = shape;
+    for (int i = 0; i < 3; i++) out->shape_params[i] = sp[i];
+    out->collision_layer = 1;
+    out->collision_mask = 0xffffffffu;
+    out->body_type = mass > 0.0f ? AVBD_BODY_DYNAMIC : AVBD_BODY_STATIC;
+    out->flags = 0;
+    return AVBD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,202 @@
+"""ctypes mirror of include/ornis_avbd.h (the C ABI of the AVBD step).
+
+Record layouts match the C structs field for field; numpy structured dtypes
+with the same layout let whole arrays cross the boundary without copies.
+"""
+import ctypes as C
+
+import numpy as np
+
+AVBD_OK = 0
+AVBD_ERR_INVALID_ARG = -1
+AVBD_ERR_CAPACITY = -2
+AVBD_ERR_DEVICE = -3
+AVBD_ERR_TIMEOUT = -4
+AVBD_ERR_NONFINITE = -5
+AVBD_ERR_UNSUPPORTED = -6
+AVBD_ERR_JOINT_SELF = -10
+AVBD_ERR_JOINT_HANDLES = -11
+AVBD_ERR_JOINT_BAD_AXIS = -12
+AVBD_ERR_JOINT_NONFINITE = -13
+
+SHAPE_SPHERE = 0
+SHAPE_BOX = 1
+SHAPE_CAPSULE = 2
+SHAPE_HALFSPACE = 3
+
+BODY_DYNAMIC = 0
+BODY_STATIC = 1
+BODY_KINEMATIC = 2
+
+FLAG_TRIGGER = 1
+
+JOINT_BALL = 0
+JOINT_REVOLUTE = 1
+
+MAX_POINTS = 8
+
+F3 = C.c_float * 3
+F4 = C.c_float * 4
+
+
+class AvbdBody(C.Structure):
+    _fields_ = [
+        ("position", F3),
+        ("orientation", F4),
+        ("velocity", F3),
+        ("angular_velocity", F3),
+        ("torque", F3),
+        ("mass", C.c_float),
+        ("inv_mass", C.c_float),
+        ("inertia", F3),
+        ("restitution", C.c_float),
+        ("friction", C.c_float),
+        ("friction_transverse", C.c_float),
+        ("rolling_friction", C.c_float),
+        ("torsion_friction", C.c_float),
+        ("shape", C.c_uint32),
+        ("shape_params", F3),
+        ("collision_layer", C.c_uint32),
+        ("collision_mask", C.c_uint32),
+        ("body_type", C.c_uint32),
+        ("flags", C.c_uint32),
+    ]
+
+
+class AvbdJointDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("body_a", C.c_uint32),
+        ("body_b", C.c_uint32),
+        ("local_anchor_a", F3),
+        ("local_anchor_b", F3),
+        ("local_axis_a", F3),
+        ("local_axis_b", F3),
+        ("has_limit", C.c_int32),
+        ("limit_min", C.c_float),
+        ("limit_max", C.c_float),
+    ]
+
+
+class AvbdParams(C.Structure):
+    _fields_ = [
+        ("gravity", F3),
+        ("step_dt", C.c_float),
+        ("iterations", C.c_int32),
+        ("max_substeps", C.c_int32),
+        ("enable_sleep", C.c_int32),
+        ("enable_ccd", C.c_int32),
+    ]
+
+
+class AvbdBodyAux(C.Structure):
+    _fields_ = [
+        ("prev_position", F3),
+        ("prev_orientation", F4),
+        ("sleep_timer", C.c_float),
+        ("asleep", C.c_uint32),
+    ]
+
+
+class AvbdPairState(C.Structure):
+    _fields_ = [
+        ("a", C.c_uint32),
+        ("b", C.c_uint32),
+        ("normal", F3),
+        ("mu", C.c_float * 2),
+        ("gap", C.c_float),
+        ("npoints", C.c_uint32),
+    ]
+
+
+class AvbdPointState(C.Structure):
+    _fields_ = [
+        ("ra", F3),
+        ("rb", F3),
+        ("lam", F3),
+        ("pen", F3),
+        ("roll_lam", F3),
+        ("stuck", C.c_uint32),
+        ("matched", C.c_int32),
+    ]
+
+
+class AvbdJointState(C.Structure):
+    _fields_ = [
+        ("lam_l", F3),
+        ("lam_a", F3),
+        ("pen_l", F3),
+        ("pen_a", F3),
+        ("acc_lim", C.c_float),
+    ]
+
+
+class AvbdCounters(C.Structure):
+    _fields_ = [
+        ("steps", C.c_uint64),
+        ("pairs", C.c_uint64),
+        ("points", C.c_uint64),
+        ("candidates", C.c_uint64),
+        ("colours", C.c_uint64),
+        ("breakdowns", C.c_uint64),
+        ("ccd_hits", C.c_uint64),
+        ("sleeping", C.c_uint64),
+        ("timeouts", C.c_uint64),
+    ]
+
+
+def _dtype_of(struct):
+    """numpy structured dtype with the exact layout of a ctypes Structure."""
+    fields = []
+    for name, ctype in struct._fields_:
+        if issubclass(ctype, C.Array):
+            base = ctype._type_
+            fields.append((name, np.dtype(base), (ctype._length_,)))
+        else:
+            fields.append((name, np.dtype(ctype)))
+    dt = np.dtype(fields, align=True)
+    assert dt.itemsize == C.sizeof(struct), (struct.__name__, dt.itemsize, C.sizeof(struct))
+    return dt
+
+
+BODY_DTYPE = _dtype_of(AvbdBody)
+AUX_DTYPE = _dtype_of(AvbdBodyAux)
+PAIR_DTYPE = _dtype_of(AvbdPairState)
+POINT_DTYPE = _dtype_of(AvbdPointState)
+JOINT_STATE_DTYPE = _dtype_of(AvbdJointState)
+
+
+def ptr(arr, ctype=C.c_void_p):
+    """Raw pointer to a contiguous numpy array (None for None)."""
+    if arr is None:
+        return None
+    assert arr.flags["C_CONTIGUOUS"]
+    return C.cast(arr.ctypes.data, ctype)
+
+
+def default_params(gravity=(0.0, -9.81, 0.0), step_dt=1.0 / 60.0, iterations=10,
+                   max_substeps=4, enable_sleep=1, enable_ccd=1):
+    p = AvbdParams()
+    p.gravity[:] = [float(g) for g in gravity]
+    p.step_dt = float(np.float32(step_dt))
+    p.iterations = int(iterations)
+    p.max_substeps = int(max_substeps)
+    p.enable_sleep = int(enable_sleep)
+    p.enable_ccd = int(enable_ccd)
+    return p
+
+
+def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0),
+               limit=None):
+    d = AvbdJointDesc()
+    d.kind = kind
+    d.body_a = a
+    d.body_b = b
+    d.local_anchor_a[:] = list(map(float, anchor_a))
+    d.local_anchor_b[:] = list(map(float, anchor_b))
+    d.local_axis_a[:] = list(map(float, axis_a))
+    d.local_axis_b[:] = list(map(float, axis_b))
+    if limit is not None:
+        d.has_limit = 1
+        d.limit_min, d.limit_max = float(limit[0]), float(limit[1])
+    return d

@@ -1,0 +1,161 @@
+"""ctypes access to the CPU oracle (oracle/_build/libavbd_oracle.so).
+
+Test infrastructure: the oracle is the checker for the CUDA path, never the
+thing measured or shipped.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from ornis_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "libavbd_oracle.so")
+
+REFERENCE = 0
+COLOURED = 1
+
+_lib = None
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        L = C.CDLL(ORACLE_SO)
+        vp = C.c_void_p
+        L.oracle_world_create.restype = vp
+        L.oracle_world_create.argtypes = [C.POINTER(abi.AvbdParams), C.c_int, C.c_int, C.c_int]
+        L.oracle_world_destroy.argtypes = [vp]
+        L.oracle_set_faithful_scan.argtypes = [vp, C.c_int]
+        L.oracle_add_bodies.argtypes = [vp, vp, C.c_uint32]
+        L.oracle_add_joint.argtypes = [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(C.c_uint32)]
+        L.oracle_step.argtypes = [vp, C.c_float]
+        L.oracle_step_fixed.argtypes = [vp, C.c_int32]
+        L.oracle_body_count.restype = C.c_uint32
+        L.oracle_body_count.argtypes = [vp]
+        L.oracle_get_bodies.argtypes = [vp, vp]
+        L.oracle_get_state13.argtypes = [vp, vp]
+        L.oracle_set_bodies.argtypes = [vp, vp, C.c_uint32]
+        L.oracle_joint_count.restype = C.c_uint32
+        L.oracle_joint_count.argtypes = [vp]
+        L.oracle_pair_count.restype = C.c_uint32
+        L.oracle_pair_count.argtypes = [vp]
+        L.oracle_export_state.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.oracle_import_state.argtypes = [vp, vp, vp, vp, vp, C.c_uint32, vp]
+        L.oracle_get_colours.argtypes = [vp, vp]
+        L.oracle_get_counters.argtypes = [vp, C.POINTER(abi.AvbdCounters)]
+        L.oracle_stamp_row.argtypes = [vp, vp, vp, C.c_float, C.c_float, vp, C.c_float]
+        L.oracle_solve_6x6.restype = C.c_int
+        L.oracle_solve_6x6.argtypes = [vp, vp, vp]
+        L.oracle_tangent_basis.argtypes = [vp, vp, vp]
+        L.oracle_shape_inertia.argtypes = [C.c_uint32, vp, C.c_float, vp]
+        L.oracle_colour_hash.restype = C.c_uint32
+        L.oracle_colour_hash.argtypes = [C.c_uint32]
+        L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
+        _lib = L
+    return _lib
+
+
+def f32(x):
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+
+
+def body_new(shape, params, position, mass):
+    """RigidBody::new_* through the oracle's restatement of the constructors."""
+    b = abi.AvbdBody()
+    p = f32(list(params) + [0.0] * (3 - len(params)))
+    pos = f32(position)
+    rc = lib().oracle_body_new(shape, abi.ptr(p), abi.ptr(pos), float(mass), C.byref(b))
+    assert rc == 0, rc
+    return b
+
+
+def bodies_to_array(bodies):
+    arr = np.zeros(len(bodies), dtype=abi.BODY_DTYPE)
+    C.memmove(arr.ctypes.data, (abi.AvbdBody * len(bodies))(*bodies), arr.nbytes)
+    return arr
+
+
+class OracleWorld:
+    """One single-scene oracle engine (Reference or Coloured sweep)."""
+
+    def __init__(self, params=None, mode=REFERENCE, use_double=False, threads=1):
+        self.params = params if params is not None else abi.default_params()
+        self.h = lib().oracle_world_create(C.byref(self.params), mode, int(use_double), int(threads))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_world_destroy(self.h)
+            self.h = None
+
+    def faithful_scan(self, on=True):
+        lib().oracle_set_faithful_scan(self.h, int(on))
+
+    def add_bodies(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert arr.dtype == abi.BODY_DTYPE
+        assert lib().oracle_add_bodies(self.h, abi.ptr(arr), len(arr)) == 0
+
+    def add_joint(self, desc):
+        h = C.c_uint32(0)
+        rc = lib().oracle_add_joint(self.h, C.byref(desc), C.byref(h))
+        return rc, h.value
+
+    def step(self, dt):
+        lib().oracle_step(self.h, float(dt))
+
+    def step_fixed(self, n=1):
+        lib().oracle_step_fixed(self.h, int(n))
+
+    @property
+    def nbodies(self):
+        return lib().oracle_body_count(self.h)
+
+    def bodies(self):
+        out = np.zeros(self.nbodies, dtype=abi.BODY_DTYPE)
+        lib().oracle_get_bodies(self.h, abi.ptr(out))
+        return out
+
+    def state13(self):
+        out = np.zeros((self.nbodies, 13), dtype=np.float64)
+        lib().oracle_get_state13(self.h, abi.ptr(out))
+        return out
+
+    def set_bodies(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert lib().oracle_set_bodies(self.h, abi.ptr(arr), len(arr)) == 0
+
+    def export_state(self):
+        n = self.nbodies
+        npairs = lib().oracle_pair_count(self.h)
+        bodies = np.zeros(n, dtype=abi.BODY_DTYPE)
+        aux = np.zeros(n, dtype=abi.AUX_DTYPE)
+        pairs = np.zeros(npairs, dtype=abi.PAIR_DTYPE)
+        points = np.zeros(npairs * abi.MAX_POINTS, dtype=abi.POINT_DTYPE)
+        joints = np.zeros(lib().oracle_joint_count(self.h), dtype=abi.JOINT_STATE_DTYPE)
+        lib().oracle_export_state(self.h, abi.ptr(bodies), abi.ptr(aux), abi.ptr(pairs), abi.ptr(points),
+                                  abi.ptr(joints))
+        return dict(bodies=bodies, aux=aux, pairs=pairs, points=points, joints=joints)
+
+    def import_state(self, st):
+        lib().oracle_import_state(self.h, abi.ptr(st["bodies"]), abi.ptr(st["aux"]), abi.ptr(st["pairs"]),
+                                  abi.ptr(st["points"]), len(st["pairs"]), abi.ptr(st.get("joints")))
+
+    def colours(self):
+        out = np.zeros(self.nbodies, dtype=np.int32)
+        lib().oracle_get_colours(self.h, abi.ptr(out))
+        return out
+
+    def counters(self):
+        c = abi.AvbdCounters()
+        lib().oracle_get_counters(self.h, C.byref(c))
+        return c
