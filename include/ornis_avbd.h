@@ -160,7 +160,8 @@ typedef struct AvbdJointState {
     float acc_lim;
 } AvbdJointState;
 
-/* Per-step observability counters (SURVEY "metrics"). */
+/* Per-step observability counters (the reference exposes sleeping_count(),
+ * avbd/mod.rs:788-790; the rest are new). */
 typedef struct AvbdCounters {
     uint64_t steps;        /* fixed substeps taken                            */
     uint64_t pairs;        /* live contact pairs after the last substep       */
@@ -248,6 +249,22 @@ int avbd_world_import_state(AvbdWorld* world, const AvbdBody* bodies,
 /* Colour of every body in the last substep's primal sweep (-1 = not swept:
  * static, kinematic, asleep). */
 int avbd_world_get_colours(AvbdWorld* world, int32_t* colours, uint32_t n);
+
+/* ---- helpers -------------------------------------------------------------- */
+
+/* RigidBody::new_sphere / new_box / new_capsule / try_new_halfspace
+ * (body.rs:346-376, :470-576, :873-889): fills one body record with the
+ * reference's default material for the shape and the mass triple of
+ * Mass::from_kind (invariants.rs:175-199).  mass <= 0 makes a static body;
+ * a half-space must be static. */
+int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const float* position, float mass);
+
+/* Launch shape of the primal kernel: lanes cooperating on one body (1, 4, 8,
+ * 16 or 32) and threads per block.  No reference counterpart (the reference
+ * sweeps on one CPU thread); picked by the autotuner in ornis_gb300/tune.py. */
+int avbd_set_tuning(AvbdWorld* world, int primal_lanes, int primal_block);
+
+int avbd_abi_version(void);
 
 #ifdef __cplusplus
 }

@@ -1955,6 +1955,23 @@ void oracle_shape_inertia(uint32_t shape, const float* sp, float mass, float* ou
 }
 uint32_t oracle_colour_hash(uint32_t x) { return colour_hash(x); }
 
+// Unit-test hooks mirroring the reference's in-module tests
+// (avbd/contact_tests.rs:38-96): pos0/rot0 = current poses, then one
+// generate_pairs pass; gap_c0 of point qi of pair pi.
+int oracle_generate_pairs(OracleWorld* w) {
+    DISPATCH(w, {
+        E.ensure_scratch();
+        for (size_t h = 0; h < E.bodies.size(); h++) { E.pos0[h] = E.bodies[h].pos; E.rot0[h] = E.bodies[h].rot; }
+        E.generate_pairs();
+    });
+    return AVBD_OK;
+}
+double oracle_gap_c0(OracleWorld* w, uint32_t pi, uint32_t qi) {
+    double r = 0.0;
+    DISPATCH(w, r = (double)E.gap_c0(E.pairs[pi], E.pairs[pi].points[qi]));
+    return r;
+}
+
 // RigidBody constructors (body.rs:346-376, :470-576, :873-889): default
 // materials per shape and the mass triple of Mass::from_kind
 // (invariants.rs:175-199).

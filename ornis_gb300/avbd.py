@@ -1,0 +1,198 @@
+"""Host-side mirror of the reference's AVBD engine API over the C ABI.
+
+`AvbdWorld` follows `AvbdEngine` / `PhysicsEngine` (crates/physics/src/
+avbd/mod.rs:1147-1602, engine.rs:24-133): bodies are added in handle order,
+`step(dt)` runs the fixed-step accumulator, `get_body`/`set_body` read and
+write the body records, `add_joint` returns a handle or raises the
+JointError-style status.  Every call goes to libornis_avbd.so, whose step runs
+only on the GPU: there is no CPU path behind this class.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libornis_avbd.so")
+
+_lib = None
+
+
+class AvbdError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__(f"{what} failed with status {code}")
+        self.code = code
+
+
+def lib():
+    """Load libornis_avbd.so (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build
+            build.build()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        u32 = C.c_uint32
+        sigs = {
+            "avbd_default_params": [C.POINTER(abi.AvbdParams)],
+            "avbd_world_create": [C.POINTER(abi.AvbdParams), C.c_int, C.POINTER(vp)],
+            "avbd_world_create_batch": [C.POINTER(abi.AvbdParams), C.c_int, vp, u32, vp, u32, C.POINTER(vp)],
+            "avbd_world_destroy": [vp],
+            "avbd_world_add_bodies": [vp, vp, u32, C.POINTER(u32)],
+            "avbd_world_add_joint": [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(u32)],
+            "avbd_world_body_count": [vp, C.POINTER(u32)],
+            "avbd_world_scene_count": [vp, C.POINTER(u32)],
+            "avbd_world_get_bodies": [vp, u32, u32, vp],
+            "avbd_world_set_bodies": [vp, u32, u32, vp],
+            "avbd_world_step": [vp, C.c_float],
+            "avbd_world_step_fixed": [vp, C.c_int32],
+            "avbd_world_step_graph": [vp, C.c_int32],
+            "avbd_world_sync": [vp],
+            "avbd_world_get_counters": [vp, C.POINTER(abi.AvbdCounters)],
+            "avbd_world_state_sizes": [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)],
+            "avbd_world_export_state": [vp, vp, vp, vp, vp, vp, u32],
+            "avbd_world_import_state": [vp, vp, vp, vp, vp, u32, vp],
+            "avbd_world_get_colours": [vp, vp, u32],
+            "avbd_body_init": [C.POINTER(abi.AvbdBody), u32, vp, vp, C.c_float],
+            "avbd_set_tuning": [vp, C.c_int, C.c_int],
+            "avbd_abi_version": [],
+        }
+        for name, args in sigs.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc != abi.AVBD_OK:
+        raise AvbdError(rc, what)
+
+
+def body(shape, params, position, mass):
+    """RigidBody::new_* (body.rs:470-576): one body record with default material."""
+    b = abi.AvbdBody()
+    p = np.zeros(3, dtype=np.float32)
+    p[: len(params)] = params
+    pos = np.asarray(position, dtype=np.float32)
+    _check(lib().avbd_body_init(C.byref(b), shape, abi.ptr(p), abi.ptr(pos), float(mass)), "avbd_body_init")
+    return b
+
+
+def bodies_array(records):
+    arr = np.zeros(len(records), dtype=abi.BODY_DTYPE)
+    if records:
+        C.memmove(arr.ctypes.data, (abi.AvbdBody * len(records))(*records), arr.nbytes)
+    return arr
+
+
+class AvbdWorld:
+    """One AVBD world on one GPU: one scene (AvbdEngine) or many (a batch)."""
+
+    def __init__(self, params=None, device=0, bodies=None, scene_offsets=None):
+        self.params = params if params is not None else abi.default_params()
+        h = C.c_void_p()
+        if bodies is not None:
+            bodies = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+            if scene_offsets is None:
+                scene_offsets = [0, len(bodies)]
+            so = np.ascontiguousarray(scene_offsets, dtype=np.uint32)
+            _check(lib().avbd_world_create_batch(C.byref(self.params), device, abi.ptr(bodies), len(bodies),
+                                                 abi.ptr(so), len(so) - 1, C.byref(h)), "avbd_world_create_batch")
+        else:
+            _check(lib().avbd_world_create(C.byref(self.params), device, C.byref(h)), "avbd_world_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().avbd_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # PhysicsEngine::add_body
+    def add_bodies(self, arr):
+        arr = np.ascontiguousarray(arr, dtype=abi.BODY_DTYPE)
+        first = C.c_uint32()
+        _check(lib().avbd_world_add_bodies(self.h, abi.ptr(arr), len(arr), C.byref(first)), "add_bodies")
+        return first.value
+
+    def add_body(self, rec):
+        return self.add_bodies(bodies_array([rec]))
+
+    # PhysicsEngine::add_joint
+    def add_joint(self, desc):
+        hj = C.c_uint32()
+        _check(lib().avbd_world_add_joint(self.h, C.byref(desc), C.byref(hj)), "add_joint")
+        return hj.value
+
+    @property
+    def body_count(self):
+        n = C.c_uint32()
+        _check(lib().avbd_world_body_count(self.h, C.byref(n)), "body_count")
+        return n.value
+
+    # PhysicsEngine::step
+    def step(self, dt):
+        _check(lib().avbd_world_step(self.h, float(dt)), "step")
+
+    def step_fixed(self, substeps=1):
+        _check(lib().avbd_world_step_fixed(self.h, int(substeps)), "step_fixed")
+
+    def step_graph(self, substeps=1):
+        _check(lib().avbd_world_step_graph(self.h, int(substeps)), "step_graph")
+
+    def sync(self):
+        _check(lib().avbd_world_sync(self.h), "sync")
+
+    # PhysicsEngine::get_body / get_body_mut, for all handles at once
+    def bodies(self, first=0, n=None):
+        if n is None:
+            n = self.body_count - first
+        out = np.zeros(n, dtype=abi.BODY_DTYPE)
+        _check(lib().avbd_world_get_bodies(self.h, first, n, abi.ptr(out)), "get_bodies")
+        return out
+
+    def set_bodies(self, arr, first=0):
+        arr = np.ascontiguousarray(arr, dtype=abi.BODY_DTYPE)
+        _check(lib().avbd_world_set_bodies(self.h, first, len(arr), abi.ptr(arr)), "set_bodies")
+
+    def counters(self):
+        c = abi.AvbdCounters()
+        _check(lib().avbd_world_get_counters(self.h, C.byref(c)), "get_counters")
+        return c
+
+    def set_tuning(self, lanes, block):
+        _check(lib().avbd_set_tuning(self.h, int(lanes), int(block)), "set_tuning")
+
+    def colours(self):
+        n = self.body_count
+        out = np.zeros(n, dtype=np.int32)
+        _check(lib().avbd_world_get_colours(self.h, abi.ptr(out), n), "get_colours")
+        return out
+
+    # checkpoint / restore of the whole solver state
+    def export_state(self):
+        nb, npr, nj = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().avbd_world_state_sizes(self.h, C.byref(nb), C.byref(npr), C.byref(nj)), "state_sizes")
+        st = dict(
+            bodies=np.zeros(nb.value, dtype=abi.BODY_DTYPE),
+            aux=np.zeros(nb.value, dtype=abi.AUX_DTYPE),
+            pairs=np.zeros(npr.value, dtype=abi.PAIR_DTYPE),
+            points=np.zeros(npr.value * abi.MAX_POINTS, dtype=abi.POINT_DTYPE),
+            joints=np.zeros(nj.value, dtype=abi.JOINT_STATE_DTYPE),
+        )
+        _check(lib().avbd_world_export_state(self.h, abi.ptr(st["bodies"]), abi.ptr(st["aux"]),
+                                             abi.ptr(st["pairs"]), abi.ptr(st["points"]),
+                                             abi.ptr(st["joints"]), npr.value), "export_state")
+        return st
+
+    def import_state(self, st):
+        _check(lib().avbd_world_import_state(self.h, abi.ptr(st["bodies"]), abi.ptr(st["aux"]),
+                                             abi.ptr(st["pairs"]), abi.ptr(st["points"]), len(st["pairs"]),
+                                             abi.ptr(st.get("joints"))), "import_state")

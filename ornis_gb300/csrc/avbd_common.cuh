@@ -1,0 +1,92 @@
+// avbd_common.cuh — small device helpers shared by the pipeline phases.
+#pragma once
+#include "avbd_kernels.h"
+#include "avbd_rows.cuh"
+#include "avbd_shapes.cuh"
+
+namespace avbd {
+
+static inline unsigned nblk(size_t n, int b) { return (unsigned)((n + (size_t)b - 1) / (size_t)b); }
+
+static __device__ __forceinline__ bool is_dynamic(const DW& w, uint32_t h) {
+    return info_type(w.info[h]) == AVBD_BODY_DYNAMIC;
+}
+// AvbdEngine::solvable (mod.rs:1179-1181)
+static __device__ __forceinline__ bool solvable(const DW& w, uint32_t h) {
+    return info_type(w.info[h]) == AVBD_BODY_DYNAMIC && w.inv_mass[h] > 0.0f;
+}
+// swept by the primal: solvable and awake
+static __device__ __forceinline__ bool solved(const DW& w, uint32_t h) { return solvable(w, h) && !w.asleep[h]; }
+static __device__ __forceinline__ Shape shape_of(const DW& w, uint32_t h) {
+    float4 sp = w.shp[h];
+    return Shape{info_shape(w.info[h]), V3{sp.x, sp.y, sp.z}, ld3(w.pos[h]), ldq(w.rot[h])};
+}
+// rows.rs:366-368
+static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uint32_t b) {
+    uint2 fa = w.filter[a], fb = w.filter[b];
+    return (fa.x & fb.y) != 0u && (fb.x & fa.y) != 0u;
+}
+// a joint links a and b (every kind on this path is no-collide, rows.rs:457-474)
+static __device__ __forceinline__ bool jointed(const DW& w, uint32_t a, uint32_t b) {
+    for (uint32_t k = w.jofs[a]; k < w.jofs[a + 1]; k++) {
+        uint2 ab = w.j_ab[w.jlist[k]];
+        if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return true;
+    }
+    return false;
+}
+// mod.rs:833-842 with RigidBody::wake_restore (body.rs:412-418)
+static __device__ __forceinline__ void wake_body(const DW& w, uint32_t h) {
+    if (!w.asleep[h]) return;
+    w.asleep[h] = 0;
+    w.sleep_timer[h] = 0.0f;
+    if (is_dynamic(w, h)) {
+        w.inv_mass[h] = w.inv_mass_rest[h];
+        w.inertia[h] = w.inertia_rest[h];
+    }
+}
+// A candidate-buffer overflow aborts the rest of the substep (every later
+// kernel returns at once) so the host can grow the buffers and replay it: the
+// kernels that ran before the check (wake, torque, AABBs) are idempotent.
+static __device__ __forceinline__ bool aborted(const DW& w) { return (w.ctr[C_ERR] & E_CAND_OVERFLOW) != 0u; }
+// The iterations of a substep whose colouring needs more colours than the
+// launched iteration covers are skipped; the host finishes that substep.
+static __device__ __forceinline__ bool aborted_solve(const DW& w) {
+    return (w.ctr[C_ERR] & (E_CAND_OVERFLOW | E_COLOUR_RANGE)) != 0u;
+}
+static __device__ __forceinline__ uint32_t n_cand(const DW& w) { return min(w.ctr[C_CAND], w.cand_cap); }
+static __device__ __forceinline__ uint32_t n_pairs(const DW& w) { return w.offA[w.N]; }
+
+// sleep.rs:30-40 (Ball, Revolute)
+static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j) {
+    uint2 ab = w.j_ab[j];
+    V3 pa = ld3(w.pos[ab.x]), pb = ld3(w.pos[ab.y]);
+    Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
+    V3 delta = (pb + qrot(qb, ld3(w.j_lb[j]))) - (pa + qrot(qa, ld3(w.j_la[j])));
+    if (w.j_kind[j] == AVBD_JOINT_BALL) return len(delta);
+    V3 axis = qrot(qa, ld3(w.j_axa[j]));
+    return fmaxf(len(delta), len(axis - qrot(qb, ld3(w.j_axb[j]))));
+}
+// sleep.rs:18-27: a non-dynamic member moved by its driver (no motors here)
+static __device__ __forceinline__ bool joint_driven(const DW& w, uint32_t j) {
+    uint2 ab = w.j_ab[j];
+    uint32_t m[2] = {ab.x, ab.y};
+    for (int k = 0; k < 2; k++) {
+        uint32_t h = m[k];
+        if (is_dynamic(w, h)) continue;
+        float4 p = w.pos[h], pp = w.prev_pos[h], q = w.rot[h], pq = w.prev_rot[h];
+        if (p.x != pp.x || p.y != pp.y || p.z != pp.z || q.x != pq.x || q.y != pq.y || q.z != pq.z || q.w != pq.w)
+            return true;
+    }
+    return false;
+}
+
+static __global__ void k_zero_u32(uint32_t* p, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 0u;
+}
+static __global__ void k_comp_clear(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < (uint32_t)w.N) w.comp_flag[h] = 0;
+}
+
+}  // namespace avbd

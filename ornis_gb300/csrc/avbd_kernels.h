@@ -1,0 +1,51 @@
+// avbd_kernels.h — host-side launchers of the AVBD device pipeline.
+// Every launcher enqueues on `st` and never synchronises.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
+
+#include "avbd_world.cuh"
+
+namespace avbd {
+
+struct Tune {
+    int primal_lanes = 1;        // lanes cooperating on one body in the primal (1, 4, 8, 16, 32)
+    int primal_block = 128;      // threads per block of the primal kernel
+    int small_scene_max = 2048;  // scenes up to this many bodies use the one-CTA broadphase
+};
+
+// exclusive scan of n uint32 values in place (out may alias in); tmp needs
+// scan_tmp_words(n) words
+size_t scan_tmp_words(size_t n);
+void scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, cudaStream_t st);
+
+// stable LSD radix sort of (key, value) pairs, n <= capacity of the buffers
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, size_t n,
+                      uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
+size_t radix_hist_words(size_t n);
+
+// per substep phases
+void launch_begin_substep(const DW& w, cudaStream_t st);
+void launch_wake_joint_motion(const DW& w, cudaStream_t st);
+void launch_torque(const DW& w, cudaStream_t st);
+struct BroadphasePlan {
+    const uint32_t* small_scenes = nullptr;  // device list of scenes swept by one CTA each
+    int n_small = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> large;  // body ranges sorted device-wide
+    uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *scan_tmp = nullptr;
+};
+void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st);
+void launch_ccd(const DW& w, cudaStream_t st);
+void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
+void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
+void launch_colouring(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
+void launch_iteration(const DW& w, const Tune& tune, int ncolours_hint, cudaStream_t st);
+void launch_finish_substep(const DW& w, cudaStream_t st);
+
+void launch_wake_apply(const DW& w, cudaStream_t st);
+void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st);
+void launch_dual(const DW& w, cudaStream_t st);
+
+}  // namespace avbd

@@ -1,0 +1,485 @@
+// avbd_phase_disc.cu — pair discovery (narrowphase, manifold, warm merge),
+// the per-body incidence lists, inertial targets, warmstart decay and the
+// body colouring.
+//
+// Reference: crates/physics/src/avbd/rows.rs:303-343 (contact normal frame),
+// :432-756 (discover_pair), :767-943 (generate_pairs merge),
+// avbd/mod.rs:980-1049 (wake, targets, decay).
+#include "avbd_common.cuh"
+
+namespace avbd {
+
+void launch_wake_apply(const DW& w, cudaStream_t st);
+
+struct Disc {
+    bool keep, exists, separated;
+    int32_t old;  // index of the previous-generation pair, -1 when new
+    V3 normal;
+    float sgn, ra, rb;
+    Dist d;
+};
+
+// discover_pair (rows.rs:432-555): prefilter, signed gap, frame, creation gate.
+static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b) {
+    Disc r;
+    r.keep = false;
+    r.exists = false;
+    r.separated = false;
+    r.old = -1;
+    if (!pair_allowed(w, a, b)) return r;
+    bool trig = info_trigger(w.info[a]) || info_trigger(w.info[b]);
+    if (!trig && jointed(w, a, b)) return r;
+    r.ra = w.shp[a].w;
+    r.rb = w.shp[b].w;
+    Shape sa = shape_of(w, a), sb = shape_of(w, b);
+    if (len(sa.pos - sb.pos) > r.ra + r.rb + GEN_MARGIN) return r;
+    float sat = 0.0f;
+    r.d = shape_distance(sa, sb, &sat);
+    r.sgn = (sa.kind == AVBD_SHAPE_BOX && sb.kind == AVBD_SHAPE_BOX) ? sat : r.d.dist;
+    if (trig) return r;  // trigger overlaps form no contact pair
+    for (uint32_t p = w.o_offA[a]; p < w.o_offA[a + 1]; p++)
+        if (w.o_ab[p].y == b) {
+            r.old = (int32_t)p;
+            break;
+        }
+    r.exists = r.old >= 0;
+    V3 normal;
+    if (sa.kind == AVBD_SHAPE_HALFSPACE) normal = -qrot(sa.rot, sa.p);
+    else if (sb.kind == AVBD_SHAPE_HALFSPACE) normal = qrot(sb.rot, sb.p);
+    else {
+        V3 nm = r.d.pa - r.d.pb;
+        if (r.d.dist < 0.0f) nm = -nm;
+        if (len2(nm) < AXIS_REST_LEN2) nm = sa.pos - sb.pos;
+        nm = normalize_or(nm, VY());
+        if (r.exists) {
+            if (dot(nm, ld3(w.o_n[r.old])) < 0.0f) nm = -nm;
+        } else if (dot(nm, sa.pos - sb.pos) < 0.0f) {
+            nm = -nm;
+        }
+        normal = nm;
+    }
+    r.normal = normal;
+    float approach = fmaxf(dot(ld3(w.vel[b]) - ld3(w.vel[a]), normal), 0.0f);
+    float reach = GEN_MARGIN + approach * w.dt;
+    if (r.sgn > reach && !r.exists) return r;
+    r.separated = r.sgn > reach;
+    r.keep = true;
+    return r;
+}
+
+__global__ void k_disc_filter(DW w) {
+    if (aborted(w)) return;
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cand(w)) return;
+    uint2 ab = w.cand[c];
+    Disc d = discover(w, ab.x, ab.y);
+    w.keep[c] = d.keep;
+    if (d.keep) atomicAdd(&w.cnt[ab.x], 1u);
+}
+__global__ void k_place(DW w) {
+    if (aborted(w)) return;
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cand(w) || !w.keep[c]) return;
+    uint32_t a = w.cand[c].x;
+    w.slot_c[w.offA[a] + atomicAdd(&w.cur[a], 1u)] = c;
+}
+// each body's A-side slots in ascending b: pairs end up in (a, b) order
+__global__ void k_sort_slots(DW w) {
+    if (aborted(w)) return;
+    uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= (uint32_t)w.N) return;
+    uint32_t s0 = w.offA[a], s1 = w.offA[a + 1];
+    for (uint32_t i = s0 + 1; i < s1; i++) {
+        uint32_t c = w.slot_c[i];
+        uint32_t bk = w.cand[c].y;
+        uint32_t k = i;
+        while (k > s0 && w.cand[w.slot_c[k - 1]].y > bk) {
+            w.slot_c[k] = w.slot_c[k - 1];
+            k--;
+        }
+        w.slot_c[k] = c;
+    }
+    if (a == 0) w.ctr[C_PAIRS] = w.offA[w.N];
+}
+
+// Manifold (rows.rs:571-715), wake vote (:716-744) and warm merge with the
+// previous generation (:809-931) for one surviving pair.
+__global__ void k_disc_build(DW w) {
+    if (aborted(w)) return;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs(w)) return;
+    uint32_t c = w.slot_c[p];
+    uint2 ab = w.cand[c];
+    uint32_t ia = ab.x, ib = ab.y;
+    Disc d = discover(w, ia, ib);
+    V3 normal = d.normal;
+    float sgn = d.sgn;
+    float mu = fmaxf(fmaxf(w.mat[ia].y, w.mat[ib].y), 0.0f);
+    V3 posa = ld3(w.pos[ia]), posb = ld3(w.pos[ib]);
+    Q qa = ldq(w.rot[ia]), qb = ldq(w.rot[ib]);
+    uint32_t ka = info_shape(w.info[ia]), kb = info_shape(w.info[ib]);
+    float4 spa = w.shp[ia], spb = w.shp[ib];
+    V3 fra[MAX_PTS], frb[MAX_PTS];
+    int nf = 0;
+    float patch = fminf(d.ra, d.rb) + MARGIN;
+    V3 pp = (d.d.pa + d.d.pb) * HALF;
+    V3 pa_c = posa - normal * dot(posa - pp, normal);
+    V3 pb_c = posb - normal * dot(posb - pp, normal);
+    float plane_a = ka == AVBD_SHAPE_BOX ? dot(normal, posa) - 1.0f * dot(vabs(qrot(conj(qa), normal)), ld3(spa))
+                                         : dot(normal, d.d.pa);
+    float plane_b = kb == AVBD_SHAPE_BOX
+                        ? dot(normal, posb) - (-1.0f) * dot(vabs(qrot(conj(qb), normal)), ld3(spb))
+                        : dot(normal, d.d.pb);
+    Q inv_a = conj(qa), inv_b = conj(qb);
+    auto dup = [&](V3 ral, V3 rbl) {
+        for (int k = 0; k < nf; k++)
+            if (len(fra[k] - ral) < POINT_MATCH_DIST && len(frb[k] - rbl) < POINT_MATCH_DIST) return true;
+        return false;
+    };
+    if (!d.separated) {
+        for (int side = 0; side < 2; side++) {
+            if ((side == 0 ? ka : kb) != AVBD_SHAPE_BOX) continue;
+            V3 bpos = side == 0 ? posa : posb;
+            Q brot = side == 0 ? qa : qb;
+            V3 half = ld3(side == 0 ? spa : spb);
+            V3 witness = side == 0 ? d.d.pa : d.d.pb;
+            float sign = side == 0 ? 1.0f : -1.0f;
+            V3 pc = side == 0 ? pa_c : pb_c;
+            for (int ci = 0; ci < 8; ci++) {
+                // corner order of rows.rs:346-363: x outer, z inner, - before +
+                float sx = (ci & 4) ? 1.0f : -1.0f, sy = (ci & 2) ? 1.0f : -1.0f, sz = (ci & 1) ? 1.0f : -1.0f;
+                V3 corner{sx * half.x, sy * half.y, sz * half.z};
+                V3 world = bpos + qrot(brot, corner);
+                float along = dot(world - witness, sign * normal);
+                if (fabsf(along) > EXPAND_SLOP + fmaxf(-sgn, 0.0f)) continue;
+                V3 rel = world - pc;
+                V3 tang = rel - normal * dot(rel, normal);
+                if (len(tang) > patch) continue;
+                if (nf >= MAX_PTS) break;
+                V3 pa, pb;
+                if (side == 0) {
+                    pa = world;
+                    pb = world + normal * (plane_b - dot(normal, world));
+                } else {
+                    pa = world + normal * (plane_a - dot(normal, world));
+                    pb = world;
+                }
+                V3 ral = qrot(inv_a, pa - posa), rbl = qrot(inv_b, pb - posb);
+                if (dup(ral, rbl)) continue;
+                fra[nf] = ral;
+                frb[nf] = rbl;
+                nf++;
+            }
+        }
+    }
+    if (!d.separated && nf >= 2 && nf < MAX_PTS) {
+        V3 mid = d.ra < d.rb ? pa_c : (d.rb < d.ra ? pb_c : (pa_c + pb_c) * HALF);
+        V3 pa = mid + normal * (plane_a - dot(normal, mid));
+        V3 pb = mid + normal * (plane_b - dot(normal, mid));
+        V3 ral = qrot(inv_a, pa - posa), rbl = qrot(inv_b, pb - posb);
+        if (!dup(ral, rbl)) {
+            fra[nf] = ral;
+            frb[nf] = rbl;
+            nf++;
+        }
+    }
+    if (!d.separated && nf < 3) {
+        V3 ral = qrot(inv_a, d.d.pa - posa), rbl = qrot(inv_b, d.d.pb - posb);
+        if (!dup(ral, rbl)) {
+            fra[nf] = ral;
+            frb[nf] = rbl;
+            nf++;
+        }
+    }
+    bool wake;
+    if (d.exists) {
+        wake = (w.asleep[ia] || w.asleep[ib]) && sgn < -WAKE_PENETRATION;
+    } else {
+        bool impact = sgn < -WAKE_PENETRATION;
+        if (!impact && w.asleep[ia]) impact = dot(ld3(w.vel[ib]) - ld3(w.vel[ia]), 1.0f * normal) > WAKE_IMPACT_SPEED;
+        if (!impact && w.asleep[ib])
+            impact = dot(ld3(w.vel[ia]) - ld3(w.vel[ib]), -1.0f * normal) > WAKE_IMPACT_SPEED;
+        wake = impact;
+    }
+    if (wake) {
+        w.flag[ia] = 1;
+        w.flag[ib] = 1;
+    }
+    w.p_ab[p] = ab;
+    w.p_n[p] = st3(normal, sgn);
+    w.p_mu[p] = make_float2(mu, mu);
+    w.p_np[p] = (uint32_t)nf;
+    bool touching = sgn <= 0.0f;
+    bool smooth = ka == AVBD_SHAPE_SPHERE || kb == AVBD_SHAPE_SPHERE;
+    uint32_t onp = d.exists ? w.o_np[d.old] : 0u;
+    for (int k = 0; k < nf; k++) {
+        uint32_t q = p * MAX_PTS + k;
+        int m = -1;
+        for (uint32_t j = 0; j < onp; j++) {
+            float4 ora = w.oq_ra[(uint32_t)d.old * MAX_PTS + j];
+            if (len(ld3(ora) - fra[k]) < LAMBDA_MATCH_DIST) {
+                m = (int)j;
+                break;
+            }
+        }
+        if (m >= 0) {
+            uint32_t oq = (uint32_t)d.old * MAX_PTS + m;
+            float4 ora = w.oq_ra[oq], orb = w.oq_rb[oq];
+            if (orb.w != 0.0f && touching && !smooth) {  // stuck: anchors stay frozen
+                w.q_ra[q] = make_float4(ora.x, ora.y, ora.z, 0.0f);
+                w.q_rb[q] = orb;
+            } else {
+                w.q_ra[q] = st3(fra[k], 0.0f);
+                w.q_rb[q] = st3(frb[k], orb.w);
+            }
+            w.q_lam[q] = w.oq_lam[oq];
+            w.q_pen[q] = w.oq_pen[oq];
+            w.q_roll[q] = w.oq_roll[oq];
+        } else {
+            w.q_ra[q] = st3(fra[k], 0.0f);
+            w.q_rb[q] = st3(frb[k], 1.0f);
+            w.q_lam[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w.q_pen[q] = make_float4(PENALTY_INIT, PENALTY_INIT, PENALTY_INIT, 0.0f);
+            w.q_roll[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        w.q_matched[q] = m;
+    }
+    atomicAdd(&w.ctr[C_POINTS], (uint32_t)nf);
+}
+__global__ void k_clear_flags(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < (uint32_t)w.N) w.flag[h] = 0;
+}
+
+void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
+    unsigned g1 = nblk(w.N + 1, 256);
+    unsigned gc = nblk(w.cand_cap, 256);
+    k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
+    k_zero_u32<<<g1, 256, 0, st>>>(w.cur, w.N + 1);
+    k_disc_filter<<<nblk(w.cand_cap, 128), 128, 0, st>>>(w);
+    scan_exclusive(w.cnt, w.offA, w.N + 1, scan_tmp, st);
+    k_place<<<gc, 256, 0, st>>>(w);
+    k_sort_slots<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    k_clear_flags<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    k_disc_build<<<nblk(w.pair_cap, 128), 128, 0, st>>>(w);
+}
+
+// ---- after discovery ----------------------------------------------------------
+// mod.rs:985-992: a sleeper kicked above the thresholds wakes before warmstart
+__global__ void k_external_wake(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !w.asleep[h]) return;
+    if (len(ld3(w.vel[h])) > SLEEP_LIN || len(ld3(w.angvel[h])) > SLEEP_ANG) wake_body(w, h);
+}
+__global__ void k_countB(DW w) {
+    if (aborted(w)) return;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs(w)) return;
+    atomicAdd(&w.cnt[w.p_ab[p].y], 1u);
+}
+__global__ void k_placeB(DW w) {
+    if (aborted(w)) return;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs(w)) return;
+    uint32_t b = w.p_ab[p].y;
+    w.listB[w.offB[b] + atomicAdd(&w.cur[b], 1u)] = p;
+}
+__global__ void k_sortB(DW w) {
+    if (aborted(w)) return;
+    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= (uint32_t)w.N) return;
+    uint32_t s0 = w.offB[b], s1 = w.offB[b + 1];
+    for (uint32_t i = s0 + 1; i < s1; i++) {
+        uint32_t v = w.listB[i];
+        uint32_t k = i;
+        while (k > s0 && w.listB[k - 1] > v) {
+            w.listB[k] = w.listB[k - 1];
+            k--;
+        }
+        w.listB[k] = v;
+    }
+}
+// mod.rs:993-1018 (step-start pose, inertial target) and :1043-1049 (x <- y)
+__global__ void k_targets(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    float4 p = w.pos[h], q = w.rot[h];
+    if (info_type(w.info[h]) == AVBD_BODY_KINEMATIC) {
+        w.pos0[h] = w.prev_pos[h];
+        w.rot0[h] = w.prev_rot[h];
+    } else {
+        w.pos0[h] = p;
+        w.rot0[h] = q;
+    }
+    if (!solvable(w, h)) {
+        w.inertial[h] = p;
+        w.inertial_rot[h] = q;
+        return;
+    }
+    float dt = w.dt;
+    V3 y = ld3(p) + ld3(w.vel[h]) * dt + w.gravity * (dt * dt);
+    Q qt = quat_integrate(ldq(q), ld3(w.angvel[h]) * dt);
+    w.inertial[h] = st3(y, 0.0f);
+    w.inertial_rot[h] = stq(qt);
+    if (!w.asleep[h]) {
+        w.pos[h] = st3(y, 0.0f);
+        w.rot[h] = stq(qt);
+    }
+}
+// Eq. 19 warmstart decay (mod.rs:1019-1040)
+__global__ void k_decay_points(DW w) {
+    if (aborted(w)) return;
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t p = q / MAX_PTS, k = q % MAX_PTS;
+    if (p >= n_pairs(w) || k >= w.p_np[p]) return;
+    const float ag = ALPHA * GAMMA;
+    float4 l = w.q_lam[q], r = w.q_roll[q], pn = w.q_pen[q];
+    w.q_lam[q] = make_float4(l.x * ag, l.y * ag, l.z * ag, 0.0f);
+    w.q_roll[q] = make_float4(r.x * ag, r.y * ag, r.z * ag, 0.0f);
+    w.q_pen[q] = make_float4(fclamp(pn.x * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                             fclamp(pn.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                             fclamp(pn.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+}
+__global__ void k_decay_joints(DW w) {
+    if (aborted(w)) return;
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    const float ag = ALPHA * GAMMA;
+    float4 a = w.j_lam_l[j], b = w.j_lam_a[j], c = w.j_pen_l[j], d = w.j_pen_a[j];
+    w.j_lam_l[j] = make_float4(a.x * ag, a.y * ag, a.z * ag, 0.0f);
+    w.j_lam_a[j] = make_float4(b.x * ag, b.y * ag, b.z * ag, 0.0f);
+    w.j_pen_l[j] = make_float4(fclamp(c.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(c.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                               fclamp(c.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+    w.j_pen_a[j] = make_float4(fclamp(d.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(d.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                               fclamp(d.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+}
+
+void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
+    unsigned gb = nblk(w.N, 256);
+    launch_wake_apply(w, st);  // discovery wake votes (rows.rs:938-941)
+    launch_wake_joint_motion(w, st);
+    k_external_wake<<<gb, 256, 0, st>>>(w);
+    unsigned g1 = nblk(w.N + 1, 256);
+    k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
+    k_zero_u32<<<g1, 256, 0, st>>>(w.cur, w.N + 1);
+    k_countB<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+    scan_exclusive(w.cnt, w.offB, w.N + 1, scan_tmp, st);
+    k_placeB<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+    k_sortB<<<gb, 256, 0, st>>>(w);
+    k_targets<<<gb, 256, 0, st>>>(w);
+    k_decay_points<<<nblk((size_t)w.pair_cap * MAX_PTS, 256), 256, 0, st>>>(w);
+    if (w.J) k_decay_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
+}
+
+// ---- colouring --------------------------------------------------------------------
+// Jones-Plassmann with hash priorities, one CTA per scene: a body takes the
+// smallest colour unused by its neighbours once every higher-priority
+// neighbour is coloured.  The result is greedy colouring in descending
+// priority, whatever the thread timing, so the CPU oracle reproduces it.
+// Vertices: swept bodies; edges: pairs with points and joints between them.
+__host__ __device__ __forceinline__ uint32_t colour_hash(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+static __device__ __forceinline__ bool prio_gt(uint32_t la, uint32_t lb) {  // scene-local indices
+    uint32_t ha = colour_hash(la), hb = colour_hash(lb);
+    return ha != hb ? ha > hb : la > lb;
+}
+__global__ void __launch_bounds__(1024) k_colour(DW w) {
+    if (aborted(w)) return;
+    __shared__ int pending;
+    uint32_t s = blockIdx.x;
+    uint32_t b0 = w.scene_off[s], b1 = w.scene_off[s + 1];
+    volatile int32_t* col = w.colour;
+    for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) col[h] = solved(w, h) ? -2 : -1;
+    __syncthreads();
+    int maxc = -1;
+    for (uint32_t round = 0; round <= (b1 - b0) + 1; round++) {
+        if (threadIdx.x == 0) pending = 0;
+        __syncthreads();
+        for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) {
+            if (col[h] != -2) continue;
+            bool ready = true;
+            unsigned long long used = 0ull;
+            uint32_t lh = h - b0;
+            auto visit = [&](uint32_t o) {
+                int32_t c = col[o];
+                if (c == -2) {
+                    if (prio_gt(o - b0, lh)) ready = false;
+                } else if (c >= 0) {
+                    used |= 1ull << c;
+                }
+            };
+            for (uint32_t p = w.offA[h]; p < w.offA[h + 1] && ready; p++)
+                if (w.p_np[p]) visit(w.p_ab[p].y);
+            for (uint32_t k = w.offB[h]; k < w.offB[h + 1] && ready; k++) {
+                uint32_t p = w.listB[k];
+                if (w.p_np[p]) visit(w.p_ab[p].x);
+            }
+            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1] && ready; k++) {
+                uint2 ab = w.j_ab[w.jlist[k]];
+                visit(ab.x == h ? ab.y : ab.x);
+            }
+            if (!ready) {
+                pending = 1;
+                continue;
+            }
+            int c = __ffsll((long long)~used) - 1;
+            if (c < 0) {
+                atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_OVERFLOW);
+                c = MAX_COLOURS - 1;
+            }
+            col[h] = c;
+            maxc = max(maxc, c);
+        }
+        __syncthreads();
+        if (!pending) break;
+        __syncthreads();
+    }
+    if (maxc >= 0) atomicMax(&w.ctr[C_NCOL], (uint32_t)(maxc + 1));
+    if (maxc + 1 > w.max_cols) atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_RANGE);
+}
+__global__ void k_colour_count(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.colour[h];
+    if (c >= 0) atomicAdd(&w.col_cnt[c], 1u);
+}
+// col_cnt: [0, 64) colour starts, [64] total, [65, 129) scatter cursors
+__global__ void k_colour_scan(DW w) {
+    if (aborted(w)) return;
+    if (threadIdx.x != 0) return;
+    uint32_t run = 0;
+    for (int c = 0; c < MAX_COLOURS; c++) {
+        uint32_t v = w.col_cnt[c];
+        w.col_cnt[c] = run;
+        w.col_cnt[MAX_COLOURS + 1 + c] = run;
+        run += v;
+    }
+    w.col_cnt[MAX_COLOURS] = run;
+}
+__global__ void k_colour_scatter(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.colour[h];
+    if (c >= 0) w.col_list[atomicAdd(&w.col_cnt[MAX_COLOURS + 1 + c], 1u)] = h;
+}
+void launch_colouring(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
+    (void)scan_tmp;
+    k_zero_u32<<<1, 256, 0, st>>>(w.col_cnt, 2 * MAX_COLOURS + 2);
+    k_colour<<<w.S, 1024, 0, st>>>(w);
+    k_colour_count<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    k_colour_scan<<<1, 32, 0, st>>>(w);
+    k_colour_scatter<<<nblk(w.N, 256), 256, 0, st>>>(w);
+}
+
+}  // namespace avbd

@@ -1,0 +1,384 @@
+// avbd_phase_pre.cu — substep prologue: wake bookkeeping, torque, broadphase
+// (sweep-and-prune) and the linear CCD clamp.
+//
+// Reference: crates/physics/src/avbd/mod.rs:846-978, avbd/sleep.rs:107-137,
+// avbd/rows.rs:253-292 (bounding radii), :767-793 (the O(n^2) sphere
+// prefilter this broadphase replaces), collision/distance.rs:841-893
+// (cast_shape).
+#include "avbd_common.cuh"
+
+namespace avbd {
+
+__global__ void k_begin(DW w) {
+    if (threadIdx.x == 0) {
+        w.ctr[C_CAND] = 0;
+        w.ctr[C_NCOL] = 0;
+        w.ctr[C_FAST] = 0;
+        w.ctr[C_POINTS] = 0;
+        w.ctr[C_SLEEP] = 0;
+    }
+}
+void launch_begin_substep(const DW& w, cudaStream_t st) { k_begin<<<1, 32, 0, st>>>(w); }
+
+// ---- wake_joint_motion (sleep.rs:107-137) ----------------------------------
+__global__ void k_wake_flags(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    uint8_t f = 0;
+    if (is_dynamic(w, h)) {
+        float4 v = w.vel[h], om = w.angvel[h], tq = w.torque[h];
+        float4 p = w.pos[h], pp = w.prev_pos[h], q = w.rot[h], pq = w.prev_rot[h];
+        f = !w.asleep[h] || v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || om.x != 0.0f || om.y != 0.0f ||
+            om.z != 0.0f || tq.x != 0.0f || tq.y != 0.0f || tq.z != 0.0f || p.x != pp.x || p.y != pp.y ||
+            p.z != pp.z || q.x != pq.x || q.y != pq.y || q.z != pq.z || q.w != pq.w;
+    }
+    w.flag[h] = f;
+}
+__global__ void k_joint_wake(DW w) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    if (joint_driven(w, j) || joint_rest_error(w, j) > JOINT_REST_ERROR) {
+        uint2 ab = w.j_ab[j];
+        if (is_dynamic(w, ab.x)) w.flag[ab.x] = 1;
+        if (is_dynamic(w, ab.y)) w.flag[ab.y] = 1;
+    }
+}
+// propagate_joint_flags (sleep.rs:152-175) with value 1: one awake dynamic
+// member wakes its whole joint component (components precomputed on the host)
+__global__ void k_comp_gather_set(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.comp[h];
+    if (c >= 0 && is_dynamic(w, h) && w.flag[h] == 1) w.comp_flag[c] = 1;
+}
+__global__ void k_comp_scatter_set(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.comp[h];
+    if (c >= 0 && is_dynamic(w, h) && w.comp_flag[c]) w.flag[h] = 1;
+}
+__global__ void k_wake_apply(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    if (w.flag[h] && w.asleep[h]) wake_body(w, h);
+}
+void launch_wake_joint_motion(const DW& w, cudaStream_t st) {
+    unsigned gb = nblk(w.N, 256);
+    k_wake_flags<<<gb, 256, 0, st>>>(w);
+    if (w.J) {
+        k_joint_wake<<<nblk(w.J, 128), 128, 0, st>>>(w);
+        k_comp_clear<<<gb, 256, 0, st>>>(w);
+        k_comp_gather_set<<<gb, 256, 0, st>>>(w);
+        k_comp_scatter_set<<<gb, 256, 0, st>>>(w);
+    }
+    k_wake_apply<<<gb, 256, 0, st>>>(w);
+}
+void launch_wake_apply(const DW& w, cudaStream_t st) { k_wake_apply<<<nblk(w.N, 256), 256, 0, st>>>(w); }
+
+// ---- torque -> angular velocity (mod.rs:855-871) ---------------------------
+__global__ void k_torque(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !solvable(w, h)) return;
+    float4 tq4 = w.torque[h];
+    V3 in = ld3(w.inertia[h]);
+    float iw[3][3], inv[3][3];
+    world_inertia(in, ldq(w.rot[h]), iw);
+    V3 dg{in.x > 0.0f ? in.x : 0.0f, in.y > 0.0f ? in.y : 0.0f, in.z > 0.0f ? in.z : 0.0f};
+    inverse_symmetric(iw, dg, inv);
+    w.torque[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    V3 om = ld3(w.angvel[h]) + mat3_vec(inv, ld3(tq4)) * w.dt;
+    w.angvel[h] = st3(om, 0.0f);
+}
+void launch_torque(const DW& w, cudaStream_t st) { k_torque<<<nblk(w.N, 256), 256, 0, st>>>(w); }
+
+// ---- broadphase ---------------------------------------------------------------
+static __device__ __forceinline__ float min_dim(uint32_t kind, float4 sp) {  // rows.rs:373-403
+    if (kind == AVBD_SHAPE_SPHERE) return sp.x;
+    if (kind == AVBD_SHAPE_BOX) return fminf(sp.x, fminf(sp.y, sp.z));
+    if (kind == AVBD_SHAPE_CAPSULE) return sp.x;
+    return INFINITY;
+}
+// CCD mover gate (mod.rs:882-895): returns the step travel |v h| of a body
+// that sweeps, 0 for every other body.
+static __device__ __forceinline__ float ccd_travel(const DW& w, uint32_t h) {
+    if (!w.enable_ccd || !solvable(w, h) || w.asleep[h] || info_trigger(w.info[h])) return 0.0f;
+    V3 disp = ld3(w.vel[h]) * w.dt;
+    float l = len(disp);
+    if (l <= CCD_TRAVEL_GATE_FRACTION * min_dim(info_shape(w.info[h]), w.shp[h])) return 0.0f;
+    if (l < NEAR_ZERO) return 0.0f;
+    return l;
+}
+
+// Cube around the bounding sphere grown by half the creation margin and by
+// the CCD travel: every pair the sphere prefilter (rows.rs:475-479) can accept,
+// before or after the CCD clamp, and every pair a TOI sweep can hit, has
+// overlapping cubes.
+__global__ void k_aabb(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    float travel = ccd_travel(w, h);
+    w.fast[h] = travel > 0.0f;
+    float e = w.shp[h].w + HALF * GEN_MARGIN + travel;
+    e = e * 1.0001f + 1e-4f;  // outward slack for the rounding of this sum
+    float4 p = w.pos[h];
+    w.aabb_lo[h] = make_float4(p.x - e, p.y - e, p.z - e, 0.0f);
+    w.aabb_hi[h] = make_float4(p.x + e, p.y + e, p.z + e, 0.0f);
+}
+
+static __device__ __forceinline__ void emit_candidate(const DW& w, uint32_t a, uint32_t b) {
+    uint32_t lo = min(a, b), hi = max(a, b);
+    uint32_t slot = atomicAdd(&w.ctr[C_CAND], 1u);
+    if (slot < w.cand_cap) w.cand[slot] = make_uint2(lo, hi);
+    else atomicOr(&w.ctr[C_ERR], (uint32_t)E_CAND_OVERFLOW);
+}
+static __device__ __forceinline__ bool overlap_yz(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    return alo.y <= bhi.y && blo.y <= ahi.y && alo.z <= bhi.z && blo.z <= ahi.z;
+}
+
+// One CTA per small scene: bitonic sort of (min-x key, body) in shared
+// memory, then each thread sweeps forward from its sorted slot.
+constexpr int SAP_SMALL = 2048;
+__global__ void __launch_bounds__(512) k_sap_small(DW w, const uint32_t* scenes, int nscenes) {
+    __shared__ unsigned long long kv[SAP_SMALL];
+    __shared__ int cnt;
+    int si = blockIdx.x;
+    if (si >= nscenes) return;
+    uint32_t s = scenes[si];
+    uint32_t b0 = w.scene_off[s], b1 = w.scene_off[s + 1];
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) {
+        if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) continue;
+        int k = atomicAdd(&cnt, 1);
+        kv[k] = ((unsigned long long)f2key(w.aabb_lo[h].x) << 32) | h;
+    }
+    __syncthreads();
+    int n = cnt;
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = n + threadIdx.x; i < m; i += blockDim.x) kv[i] = ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    unsigned long long x = kv[i], y = kv[ixj];
+                    bool up = (i & k) == 0;
+                    if ((x > y) == up) {
+                        kv[i] = y;
+                        kv[ixj] = x;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        uint32_t a = (uint32_t)(kv[i] & 0xffffffffu);
+        float4 alo = w.aabb_lo[a], ahi = w.aabb_hi[a];
+        for (int j = i + 1; j < n; j++) {
+            uint32_t b = (uint32_t)(kv[j] & 0xffffffffu);
+            float4 blo = w.aabb_lo[b];
+            if (blo.x > ahi.x) break;
+            if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
+        }
+    }
+}
+
+// Large scenes: device-wide radix sort of the scene's min-x keys (half-space
+// bodies get the largest key and end every sweep), then one thread per
+// sorted slot sweeps forward.
+__global__ void k_sap_keys(DW w, uint32_t b0, uint32_t b1) {
+    uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= b1) return;
+    bool plane = info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE;
+    w.sort_key[h - b0] = plane ? 0xffffffffu : f2key(w.aabb_lo[h].x);
+    w.sort_idx[h - b0] = h;
+}
+__global__ void k_sap_sweep(DW w, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t a = w.sort_idx[i];
+    if (info_shape(w.info[a]) == AVBD_SHAPE_HALFSPACE) return;
+    float4 alo = w.aabb_lo[a], ahi = w.aabb_hi[a];
+    for (uint32_t j = i + 1; j < n; j++) {
+        uint32_t b = w.sort_idx[j];
+        if (info_shape(w.info[b]) == AVBD_SHAPE_HALFSPACE) break;
+        float4 blo = w.aabb_lo[b];
+        if (blo.x > ahi.x) break;
+        if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
+    }
+}
+// Half-space bodies have an unbounded prefilter radius (rows.rs:290): every
+// other body of the scene is a candidate.
+__global__ void k_plane_cands(DW w) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) return;
+    uint32_t s = w.scene_of[h];
+    for (uint32_t k = w.plane_off[s]; k < w.plane_off[s + 1]; k++) emit_candidate(w, w.plane_list[k], h);
+}
+
+void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st) {
+    k_aabb<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    k_plane_cands<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    if (plan.n_small) k_sap_small<<<plan.n_small, 512, 0, st>>>(w, plan.small_scenes, plan.n_small);
+    for (size_t i = 0; i < plan.large.size(); i++) {
+        uint32_t b0 = plan.large[i].first, b1 = plan.large[i].second;
+        uint32_t n = b1 - b0;
+        k_sap_keys<<<nblk(n, 256), 256, 0, st>>>(w, b0, b1);
+        radix_sort_pairs(w.sort_key, w.sort_idx, plan.keys_alt, plan.vals_alt, n, plan.hist, plan.scan_tmp, st);
+        k_sap_sweep<<<nblk(n, 128), 128, 0, st>>>(w, n);
+    }
+}
+
+// ---- CCD (mod.rs:882-978, distance.rs:841-893) -------------------------------
+// The reference clamps movers one at a time in handle order, each sweep
+// seeing the already-clamped poses of earlier movers.  Here every mover casts
+// in parallel; a mover whose candidate targets include an earlier mover waits
+// for it (dependency rounds), and recasts if that mover actually moved — the
+// same poses the serial loop would have seen.
+struct Cast {
+    bool hit;
+    float t;
+    V3 normal;
+};
+static __device__ __noinline__ Cast cast_one(const DW& w, uint32_t h, uint32_t o) {
+    Cast c{false, 0.0f, V0()};
+    V3 disp = ld3(w.vel[h]) * w.dt;
+    float L = len(disp);
+    if (L < NEAR_ZERO) return c;
+    V3 dir = disp / L;
+    Shape mv = shape_of(w, h);
+    Shape tg = shape_of(w, o);
+    V3 p0 = mv.pos;
+    float t = 0.0f;
+    for (int it = 0; it < 24; it++) {
+        mv.pos = p0 + dir * t;
+        Dist d = shape_distance(mv, tg, nullptr);
+        if (d.dist <= SHAPE_TOUCH) {
+            if (t > 0.0f) {
+                c.hit = true;
+                c.t = t;
+                c.normal = normalize_or(d.pa - d.pb, -dir);
+            }
+            break;
+        }
+        t += d.dist - SHAPE_TOUCH * HALF;
+        if (t >= L) break;
+    }
+    return c;
+}
+static __device__ __forceinline__ bool ccd_target(const DW& w, uint32_t h, uint32_t o) {
+    return !info_trigger(w.info[o]) && pair_allowed(w, h, o) && !jointed(w, h, o);
+}
+__global__ void k_ccd_init(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    w.ccd_best[h] = ~0ull;
+    w.ccd_deps[h] = 0;
+    w.ccd_state[h] = 0;
+    w.ccd_recompute[h] = 0;
+    if (w.fast[h]) atomicAdd(&w.ctr[C_FAST], 1u);
+}
+// first = 1: every mover casts against its candidates at the step-top poses
+// and counts the earlier movers among its targets.  first = 0: only movers
+// flagged for a recast.
+__global__ void k_ccd_cast(DW w, int first) {
+    if (aborted(w)) return;
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cand(w)) return;
+    uint2 ab = w.cand[c];
+    bool fa = w.fast[ab.x], fb = w.fast[ab.y];
+    if (!fa && !fb) return;
+    for (int k = 0; k < 2; k++) {
+        uint32_t h = k ? ab.y : ab.x, o = k ? ab.x : ab.y;
+        if (!(k ? fb : fa)) continue;
+        if (!first && !(w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1)) continue;
+        if (!ccd_target(w, h, o)) continue;
+        Cast r = cast_one(w, h, o);
+        if (r.hit) {
+            // earliest time wins; equal times keep the lower handle (distance.rs:886-890)
+            unsigned long long key = ((unsigned long long)__float_as_uint(r.t) << 32) | o;
+            atomicMin(&w.ccd_best[h], key);
+        }
+    }
+    if (first && fa && fb && ccd_target(w, ab.x, ab.y)) atomicAdd(&w.ccd_deps[ab.y], 1u);
+}
+static __device__ void ccd_apply(const DW& w, uint32_t h) {
+    unsigned long long key = w.ccd_best[h];
+    bool moved = false;
+    if (key != ~0ull) {
+        uint32_t o = (uint32_t)(key & 0xffffffffu);
+        Cast r = cast_one(w, h, o);  // the winning cast again: same inputs, same t and normal
+        V3 disp = ld3(w.vel[h]) * w.dt;
+        float L = fmaxf(len(disp), MIN_TOI_DISP_LENGTH);
+        float frac = fclamp(r.t / L, 0.0f, 1.0f);
+        float e = fminf(w.mat[h].x, w.mat[o].x);
+        w.pos[h] = st3(ld3(w.pos[h]) + disp * frac, 0.0f);
+        V3 v = ld3(w.vel[h]);
+        float vn = dot(v, r.normal);
+        if (vn < 0.0f) {
+            float bounce = vn < -CCD_BOUNCE_SPEED ? 1.0f + e : 1.0f;
+            w.vel[h] = st3(v - r.normal * (bounce * vn), 0.0f);
+        }
+        wake_body(w, o);
+        w.sleep_timer[h] = 0.0f;
+        atomicAdd(&w.ctr[C_CCD], 1u);
+        moved = true;
+    }
+    w.ccd_state[h] = moved ? 2 : 1;
+}
+__global__ void k_ccd_finalize(DW w, int round, int last) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !w.fast[h] || w.ccd_state[h] != 0) return;
+    if (w.ccd_deps[h] != 0) {
+        if (!last) return;
+        atomicAdd(&w.ctr[C_CCD_LEFT], 1u);  // dependency chain longer than the bounded rounds
+    }
+    ccd_apply(w, h);
+    w.ccd_recompute[h] = (uint8_t)(16 + round);  // "finalised in this round"
+}
+__global__ void k_ccd_release(DW w, int round) {
+    if (aborted(w)) return;
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_cand(w)) return;
+    uint2 ab = w.cand[c];
+    if (!w.fast[ab.x] || !w.fast[ab.y]) return;
+    if (w.ccd_recompute[ab.x] != (uint8_t)(16 + round)) return;
+    if (!ccd_target(w, ab.x, ab.y)) return;
+    atomicSub(&w.ccd_deps[ab.y], 1u);
+    if (w.ccd_state[ab.x] == 2) w.ccd_recompute[ab.y] = 1;  // the earlier mover moved: recast
+}
+__global__ void k_ccd_reset(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !w.fast[h]) return;
+    if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_best[h] = ~0ull;
+}
+__global__ void k_ccd_clear_recast(DW w) {
+    if (aborted(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !w.fast[h]) return;
+    if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_recompute[h] = 0;
+}
+void launch_ccd(const DW& w, cudaStream_t st) {
+    if (!w.enable_ccd) return;
+    unsigned gb = nblk(w.N, 256);
+    unsigned gc = nblk(w.cand_cap, 256);
+    k_ccd_init<<<gb, 256, 0, st>>>(w);
+    k_ccd_cast<<<gc, 256, 0, st>>>(w, 1);
+    for (int r = 0; r < CCD_ROUNDS; r++) {
+        bool last = r == CCD_ROUNDS - 1;
+        k_ccd_finalize<<<gb, 256, 0, st>>>(w, r, last ? 1 : 0);
+        if (last) break;
+        k_ccd_release<<<gc, 256, 0, st>>>(w, r);
+        k_ccd_reset<<<gb, 256, 0, st>>>(w);
+        k_ccd_cast<<<gc, 256, 0, st>>>(w, 0);
+        k_ccd_clear_recast<<<gb, 256, 0, st>>>(w);
+    }
+}
+
+}  // namespace avbd

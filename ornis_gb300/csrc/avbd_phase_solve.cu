@@ -1,0 +1,543 @@
+// avbd_phase_solve.cu — the AVBD iterations: per-colour primal block solves,
+// the order-free dual update, then BDF1 velocities and sleep bookkeeping.
+//
+// Reference: crates/physics/src/avbd/assembly.rs:73-903 (solve_body),
+// avbd/joints_ext.rs:464-919 (dual_update), avbd/mod.rs:1060-1142 (BDF1,
+// sleep, driver baseline), avbd/sleep.rs:140-175.
+#include "avbd_common.cuh"
+
+namespace avbd {
+
+static __device__ __forceinline__ void load_ctx(const DW& w, uint32_t p, PairCtx& c) {
+    uint2 ab = w.p_ab[p];
+    float4 n4 = w.p_n[p];
+    c.a = ab.x;
+    c.b = ab.y;
+    c.n = ld3(n4);
+    c.gap = n4.w;
+    c.mu = w.p_mu[p];
+    c.np = w.p_np[p];
+    c.pa = ld3(w.pos[c.a]);
+    c.pb = ld3(w.pos[c.b]);
+    c.pa0 = ld3(w.pos0[c.a]);
+    c.pb0 = ld3(w.pos0[c.b]);
+    c.qa = ldq(w.rot[c.a]);
+    c.qb = ldq(w.rot[c.b]);
+    c.qa0 = ldq(w.rot0[c.a]);
+    c.qb0 = ldq(w.rot0[c.b]);
+    c.dxa = c.pa - c.pa0;
+    c.dxb = c.pb - c.pb0;
+    c.dra = quat_diff_vec(c.qa, c.qa0);
+    c.drb = quat_diff_vec(c.qb, c.qb0);
+    c.sph_a = info_shape(w.info[c.a]) == AVBD_SHAPE_SPHERE;
+    c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
+    c.rad_a = w.shp[c.a].x;
+    c.rad_b = w.shp[c.b].x;
+}
+
+// Rows of point k of pair p for the body on side is_a (assembly.rs:99-252).
+static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c, uint32_t p, uint32_t k, bool is_a,
+                                                   Sys& s) {
+    uint32_t q = p * MAX_PTS + k;
+    float4 ra = w.q_ra[q], rb = w.q_rb[q];
+    float sign = is_a ? 1.0f : -1.0f;
+    bool touching = c.gap <= 0.0f;
+    float c0 = touching ? gap_c0(c, ra, rb) : 0.0f;
+    V3 rup, rlo;
+    contact_levers(c, ra, rb, rup, rlo);
+    float cn = row_c_levers(c, c.n, c0, rup, rlo);
+    V3 r_side = is_a ? rup : rlo;
+    if (!touching) {
+        // separated damper, imminence-gated (assembly.rs:113-175)
+        float approach = fmaxf(dot(ld3(w.vel[c.b]) - ld3(w.vel[c.a]), c.n), 0.0f);
+        if (c.gap - approach * w.dt > 0.0f) return;
+        if (fabsf(cn) >= C_EPS) {
+            float npts = (float)max(c.np, 1u);
+            float ka = is_dynamic(w, c.a) ? w.inv_mass[c.a] : 0.0f;
+            float kb = is_dynamic(w, c.b) ? w.inv_mass[c.b] : 0.0f;
+            float m_red = ka + kb > NEAR_ZERO ? 1.0f / (ka + kb) : 0.0f;
+            if (m_red > 0.0f) {
+                float pen_d = fminf(2.0f * m_red / (w.dt * w.dt) / npts, PENALTY_MAX);
+                stamp_row(s, c.n, pen_d, fminf(pen_d * cn, 0.0f), r_side, sign);
+            }
+        }
+        return;
+    }
+    V3 t1 = tangent_t1(c.n);
+    V3 t2 = cross(t1, c.n);
+    V3 raf, rbf;
+    friction_levers(c, rup, rlo, raf, rbf);
+    V3 r_side_f = is_a ? raf : rbf;
+    float ct1 = row_c_levers(c, t1, 0.0f, raf, rbf);
+    float ct2 = row_c_levers(c, t2, 0.0f, raf, rbf);
+    float4 pen = w.q_pen[q], lam = w.q_lam[q];
+    float f[3];
+    contact_force(cn, pen, lam, ct1, ct2, c.mu, f);
+    if (row_live(cn, f[0])) stamp_row(s, c.n, pen.x, f[0], r_side, sign);
+    if (row_live(ct1, f[1])) stamp_row(s, t1, pen.y, f[1], r_side_f, sign);
+    if (row_live(ct2, f[2])) stamp_row(s, t2, pen.z, f[2], r_side_f, sign);
+    float mu_roll = fmaxf(w.mat[c.a].z, w.mat[c.b].z), mu_spin = fmaxf(w.mat[c.a].w, w.mat[c.b].w);
+    if (mu_roll > 0.0f || mu_spin > 0.0f) {
+        V3 wrel = c.dra - c.drb;
+        float4 rl = w.q_roll[q];
+        V3 rax[3] = {t1, t2, c.n};
+        float murs[3] = {mu_roll, mu_roll, mu_spin};
+        float rls[3] = {rl.x, rl.y, rl.z};
+        for (int li = 0; li < 3; li++) {
+            if (murs[li] <= 0.0f) continue;
+            float cap = murs[li] * fabsf(f[0]);
+            float fr = fclamp(ROLL_PEN * dot(wrel, rax[li]) + rls[li], -cap, cap);
+            stamp_angular(s, is_a ? rax[li] : -rax[li], ROLL_PEN, fr);
+        }
+    }
+}
+
+// Joint rows for body h (assembly.rs:255-881): Ball, Revolute and its limit.
+static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint32_t h, Sys& s) {
+    uint2 ab = w.j_ab[j];
+    bool is_a = ab.x == h;
+    float sign = is_a ? 1.0f : -1.0f;
+    Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
+    Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
+    V3 la = ld3(w.j_la[j]), lb = ld3(w.j_lb[j]);
+    V3 pa = ld3(w.pos[ab.x]) + qrot(qa, la), pb = ld3(w.pos[ab.y]) + qrot(qb, lb);
+    V3 pa0 = ld3(w.pos0[ab.x]) + qrot(qa0, la), pb0 = ld3(w.pos0[ab.y]) + qrot(qb0, lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    float4 axa4 = w.j_axa[j];
+    V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
+    float4 pl = w.j_pen_l[j], ll = w.j_lam_l[j], pa4 = w.j_pen_a[j], la4 = w.j_lam_a[j];
+    float penl[3] = {pl.x, pl.y, pl.z}, laml[3] = {ll.x, ll.y, ll.z};
+    V3 fl = V0();
+    // Ball/Revolute levers carry a zero offset in the weld-offset slot
+    V3 lever = is_a ? qrot(qa, la + V0()) : qrot(qb, lb);
+    for (int k = 0; k < 3; k++) {
+        V3 axis = V0();
+        axis[k] = 1.0f;
+        float cc = live[k] - ALPHA * c0v[k];
+        float f = penl[k] * cc + laml[k];
+        if (!row_live(cc, f)) continue;
+        stamp_row(s, axis, penl[k], f, lever, sign);
+        fl[k] = f;
+    }
+    {
+        // geometric stiffness (rows.rs:69-88, assembly.rs:589-618)
+        V3 r = is_a ? qrot(qa, la + V0()) : -qrot(qb, lb);
+        float arr[3] = {r.x, r.y, r.z};
+        float hm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int k = 0; k < 3; k++) {
+            float g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            g[0][0] = -arr[k];
+            g[1][1] = -arr[k];
+            g[2][2] = -arr[k];
+            g[0][k] += arr[0];
+            g[1][k] += arr[1];
+            g[2][k] += arr[2];
+            for (int x = 0; x < 3; x++)
+                for (int y = 0; y < 3; y++) hm[x][y] += g[x][y] * fl[k];
+        }
+        s.h[tri(3, 3)] += len(V3{hm[0][0], hm[1][0], hm[2][0]});
+        s.h[tri(4, 4)] += len(V3{hm[0][1], hm[1][1], hm[2][1]});
+        s.h[tri(5, 5)] += len(V3{hm[0][2], hm[1][2], hm[2][2]});
+    }
+    if (w.j_kind[j] != AVBD_JOINT_REVOLUTE) return;
+    V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
+    V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
+    V3 t1 = tangent_t1(axa0);
+    V3 t2 = cross(t1, axa0);
+    V3 ts[2] = {t1, t2};
+    float pens[2] = {pa4.x, pa4.y}, lams[2] = {la4.x, la4.y};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        float f = pens[li] * cc + lams[li];
+        if (!row_live(cc, f)) continue;
+        stamp_angular(s, is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]), pens[li], f);
+    }
+    float4 lim = w.j_lim[j];
+    if (lim.z != 0.0f) {
+        V3 wa = normalize_or(axa, VZ());
+        float refv = axa4.w;
+        float angle = wrap_pi(hinge_twist(qa, qb, axa_l) - refv);
+        int stt = warm_limit_state(angle, lim.x, lim.y, LIMIT_SLOP_ANG, lim.w);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float initial = wrap_pi(hinge_twist(qa0, qb0, axa_l) - refv);
+            float cc = regularized_limit(angle, initial, lower ? lim.x : lim.y, lower);
+            float f_raw = pa4.z * cc + lim.w;
+            float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+            if (row_live(cc, f)) stamp_angular(s, is_a ? -wa : wa, pa4.z, f);
+        }
+    }
+}
+
+// inertial block and rhs (assembly.rs:74-96)
+static __device__ __forceinline__ void inertial_block(const DW& w, uint32_t h, Sys& s) {
+    float dt2 = w.dt * w.dt;
+    float im = is_dynamic(w, h) ? w.inv_mass[h] : 0.0f;
+    float m_dt2 = 1.0f / im / dt2;
+    float iw[3][3];
+    Q q = ldq(w.rot[h]);
+    world_inertia(ld3(w.inertia[h]), q, iw);
+    for (int i = 0; i < 21; i++) s.h[i] = 0.0f;
+    s.h[tri(0, 0)] = m_dt2;
+    s.h[tri(1, 1)] = m_dt2;
+    s.h[tri(2, 2)] = m_dt2;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b <= a; b++) s.h[tri(3 + a, 3 + b)] = iw[a][b] / dt2;
+    V3 rl = m_dt2 * (ld3(w.pos[h]) - ld3(w.inertial[h]));
+    s.r[0] = rl.x;
+    s.r[1] = rl.y;
+    s.r[2] = rl.z;
+    V3 ra = mat3_vec(iw, quat_diff_vec(q, ldq(w.inertial_rot[h]))) / dt2;
+    s.r[3] = ra.x;
+    s.r[4] = ra.y;
+    s.r[5] = ra.z;
+}
+
+static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, const Sys& s) {
+    float dx[6];
+    if (solve_6x6(s, dx)) {
+        w.pos[h] = st3(ld3(w.pos[h]) + V3{dx[0], dx[1], dx[2]}, 0.0f);
+        w.rot[h] = stq(quat_integrate(ldq(w.rot[h]), V3{dx[3], dx[4], dx[5]}));
+    } else {
+        atomicAdd(&w.ctr[C_BREAKDOWN], 1u);  // breakdown: the body skips its update
+    }
+}
+
+// One thread per body: rows accumulate in the reference's order (pairs in
+// ascending index — B-side pairs precede A-side ones — then joints).
+__global__ void k_primal_thread(DW w, int colour) {
+    if (aborted_solve(w)) return;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
+    if (c0 + i >= c1) return;
+    uint32_t h = w.col_list[c0 + i];
+    Sys s;
+    inertial_block(w, h, s);
+    for (uint32_t k = w.offB[h]; k < w.offB[h + 1]; k++) {
+        uint32_t p = w.listB[k];
+        PairCtx c;
+        load_ctx(w, p, c);
+        for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, false, s);
+    }
+    for (uint32_t p = w.offA[h]; p < w.offA[h + 1]; p++) {
+        PairCtx c;
+        load_ctx(w, p, c);
+        for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, true, s);
+    }
+    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+    apply_solve(w, h, s);
+}
+
+// L lanes per body: the body's incident pairs are dealt round-robin over the
+// lanes, the partial systems are summed with shuffles, lane 0 adds the
+// inertial block and the joints and solves.
+template <int L>
+__global__ void k_primal_lanes(DW w, int colour) {
+    if (aborted_solve(w)) return;
+    uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t i = gid / L;
+    int lane = threadIdx.x % L;
+    uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
+    bool active = c0 + i < c1;
+    uint32_t h = active ? w.col_list[c0 + i] : 0u;
+    Sys s;
+#pragma unroll
+    for (int k = 0; k < 21; k++) s.h[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s.r[k] = 0.0f;
+    if (active) {
+        uint32_t nb = w.offB[h + 1] - w.offB[h], na = w.offA[h + 1] - w.offA[h];
+        for (uint32_t e = lane; e < nb + na; e += L) {
+            uint32_t p = e < nb ? w.listB[w.offB[h] + e] : w.offA[h] + (e - nb);
+            PairCtx c;
+            load_ctx(w, p, c);
+            for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, e >= nb, s);
+        }
+    }
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 21; k++) s.h[k] += __shfl_down_sync(0xffffffffu, s.h[k], o, L);
+#pragma unroll
+        for (int k = 0; k < 6; k++) s.r[k] += __shfl_down_sync(0xffffffffu, s.r[k], o, L);
+    }
+    if (!active || lane != 0) return;
+    Sys t;
+    inertial_block(w, h, t);
+#pragma unroll
+    for (int k = 0; k < 21; k++) t.h[k] += s.h[k];
+#pragma unroll
+    for (int k = 0; k < 6; k++) t.r[k] += s.r[k];
+    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, t);
+    apply_solve(w, h, t);
+}
+
+// ---- dual (joints_ext.rs:464-573 contacts, :574-896 Ball/Revolute) ----
+__global__ void k_dual_points(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t p = q / MAX_PTS, k = q % MAX_PTS;
+    if (p >= n_pairs(w) || k >= w.p_np[p]) return;
+    PairCtx c;
+    load_ctx(w, p, c);
+    float4 ra = w.q_ra[q], rb = w.q_rb[q];
+    V3 t1 = tangent_t1(c.n);
+    V3 t2 = cross(t1, c.n);
+    bool touching = c.gap <= 0.0f;
+    float c0 = touching ? gap_c0(c, ra, rb) : 0.0f;
+    V3 raw, rbw;
+    contact_levers(c, ra, rb, raw, rbw);
+    float cn = row_c_levers(c, c.n, c0, raw, rbw);
+    V3 raf, rbf;
+    friction_levers(c, raw, rbw, raf, rbf);
+    float ct1 = row_c_levers(c, t1, 0.0f, raf, rbf);
+    float ct2 = row_c_levers(c, t2, 0.0f, raf, rbf);
+    float4 pen = w.q_pen[q], lam = w.q_lam[q];
+    float f[3];
+    contact_force(cn, pen, lam, ct1, ct2, c.mu, f);
+    float bnd = fabsf(f[0]) * fmaxf(c.mu.x, c.mu.y);
+    float fu0 = pen.y * ct1 + lam.y, fu1 = pen.z * ct2 + lam.z;
+    bool stuck = sqrtf(fu0 * fu0 + fu1 * fu1) <= bnd && sqrtf(ct1 * ct1 + ct2 * ct2) < STICK_THRESH;
+    float4 nl = lam, np4 = pen;
+    if (touching && fabsf(cn) >= C_EPS) {
+        nl.x = f[0];
+        if (f[0] < 0.0f) np4.x = fminf(pen.x + BETA * fabsf(cn), PENALTY_MAX);
+    }
+    float b1 = fabsf(f[0]) * c.mu.x, b2 = fabsf(f[0]) * c.mu.y;
+    float s_ell = (b1 > 0.0f && b2 > 0.0f) ? (fu0 / b1) * (fu0 / b1) + (fu1 / b2) * (fu1 / b2) : INFINITY;
+    if (touching) {
+        nl.y = f[1];
+        nl.z = f[2];
+        if (s_ell <= 1.0f) {
+            if (fabsf(ct1) >= C_EPS) np4.y = fminf(pen.y + BETA * fabsf(ct1), PENALTY_MAX);
+            if (fabsf(ct2) >= C_EPS) np4.z = fminf(pen.z + BETA * fabsf(ct2), PENALTY_MAX);
+        }
+    }
+    w.q_lam[q] = nl;
+    w.q_pen[q] = np4;
+    w.q_rb[q] = make_float4(rb.x, rb.y, rb.z, stuck ? 1.0f : 0.0f);
+    float mu_roll = fmaxf(w.mat[c.a].z, w.mat[c.b].z), mu_spin = fmaxf(w.mat[c.a].w, w.mat[c.b].w);
+    if (touching && (mu_roll > 0.0f || mu_spin > 0.0f)) {
+        V3 wrel = c.dra - c.drb;
+        float lam_n = fabsf(nl.x);
+        float4 rl = w.q_roll[q];
+        float rls[3] = {rl.x, rl.y, rl.z};
+        V3 rax[3] = {t1, t2, c.n};
+        float murs[3] = {mu_roll, mu_roll, mu_spin};
+        for (int li = 0; li < 3; li++) {
+            if (murs[li] <= 0.0f) continue;
+            float cap = murs[li] * lam_n;
+            rls[li] = fclamp(ROLL_PEN * dot(wrel, rax[li]) + rls[li], -cap, cap);
+        }
+        w.q_roll[q] = make_float4(rls[0], rls[1], rls[2], 0.0f);
+    }
+}
+__global__ void k_dual_joints(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    uint2 ab = w.j_ab[j];
+    Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
+    Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
+    V3 la = ld3(w.j_la[j]), lb = ld3(w.j_lb[j]);
+    V3 pa = ld3(w.pos[ab.x]) + qrot(qa, la), pb = ld3(w.pos[ab.y]) + qrot(qb, lb);
+    V3 pa0 = ld3(w.pos0[ab.x]) + qrot(qa0, la), pb0 = ld3(w.pos0[ab.y]) + qrot(qb0, lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    float4 ll = w.j_lam_l[j], pl = w.j_pen_l[j];
+    float laml[3] = {ll.x, ll.y, ll.z}, penl[3] = {pl.x, pl.y, pl.z};
+    for (int k = 0; k < 3; k++) {
+        float cc = live[k] - ALPHA * c0v[k];
+        if (fabsf(cc) >= C_EPS) {
+            laml[k] += penl[k] * cc;
+            penl[k] = fminf(penl[k] + BETA * fabsf(cc), PENALTY_MAX);
+        }
+    }
+    w.j_lam_l[j] = make_float4(laml[0], laml[1], laml[2], 0.0f);
+    w.j_pen_l[j] = make_float4(penl[0], penl[1], penl[2], 0.0f);
+    if (w.j_kind[j] != AVBD_JOINT_REVOLUTE) return;
+    float4 axa4 = w.j_axa[j];
+    V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
+    V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
+    V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
+    V3 t1 = tangent_t1(axa0);
+    V3 t2 = cross(t1, axa0);
+    V3 ts[2] = {t1, t2};
+    float4 la4 = w.j_lam_a[j], pa4 = w.j_pen_a[j];
+    float lama[3] = {la4.x, la4.y, la4.z}, pena[3] = {pa4.x, pa4.y, pa4.z};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        if (fabsf(cc) < C_EPS) continue;
+        lama[li] = pena[li] * cc + lama[li];
+        pena[li] = fminf(pena[li] + BETA_ANG * fabsf(cc), PENALTY_MAX);
+    }
+    float4 lim = w.j_lim[j];
+    if (lim.z != 0.0f) {
+        float refv = axa4.w;
+        float angle = wrap_pi(hinge_twist(qa, qb, axa_l) - refv);
+        int stt = warm_limit_state(angle, lim.x, lim.y, LIMIT_SLOP_ANG, lim.w);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float initial = wrap_pi(hinge_twist(qa0, qb0, axa_l) - refv);
+            float cc = regularized_limit(angle, initial, lower ? lim.x : lim.y, lower);
+            if (fabsf(cc) >= C_EPS) {
+                float f = pena[2] * cc + lim.w;
+                lim.w = lower ? fminf(f, 0.0f) : fmaxf(f, 0.0f);
+                pena[2] = fminf(pena[2] + BETA_ANG * fabsf(cc), LIM_PEN_MAX);
+            }
+        } else {
+            lim.w = 0.0f;
+        }
+        w.j_lim[j] = lim;
+    }
+    w.j_lam_a[j] = make_float4(lama[0], lama[1], lama[2], 0.0f);
+    w.j_pen_a[j] = make_float4(pena[0], pena[1], pena[2], 0.0f);
+}
+
+void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
+    int bs = tune.primal_block;
+    switch (tune.primal_lanes) {
+        case 1: k_primal_thread<<<nblk(max_bodies, bs), bs, 0, st>>>(w, c); break;
+        case 4: k_primal_lanes<4><<<nblk((size_t)max_bodies * 4, bs), bs, 0, st>>>(w, c); break;
+        case 8: k_primal_lanes<8><<<nblk((size_t)max_bodies * 8, bs), bs, 0, st>>>(w, c); break;
+        case 16: k_primal_lanes<16><<<nblk((size_t)max_bodies * 16, bs), bs, 0, st>>>(w, c); break;
+        default: k_primal_lanes<32><<<nblk((size_t)max_bodies * 32, bs), bs, 0, st>>>(w, c); break;
+    }
+}
+void launch_dual(const DW& w, cudaStream_t st) {
+    k_dual_points<<<nblk((size_t)w.pair_cap * MAX_PTS, 256), 256, 0, st>>>(w);
+    if (w.J) k_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
+}
+void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st) {
+    for (int c = 0; c < ncolours; c++) launch_primal_colour(w, tune, c, (uint32_t)w.N, st);
+    launch_dual(w, st);
+}
+
+// ---- BDF1 + sleep + driver baseline (mod.rs:1060-1142) -------------------------
+__global__ void k_bdf1(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N || !solved(w, h)) return;
+    V3 p = ld3(w.pos[h]);
+    w.vel[h] = st3((p - ld3(w.pos0[h])) / w.dt, 0.0f);
+    Q q = ldq(w.rot[h]);
+    V3 spin = quat_diff_vec(q, ldq(w.rot0[h]));
+    w.angvel[h] = st3(len(spin) < SPIN_REST_EPS ? V0() : spin / w.dt, 0.0f);
+    w.rot[h] = stq(qnormalize(q));
+}
+// flag bits for the sleep pass: 1 joint-ready, 2 supported, 4 freeze.  Every
+// writer of a flag byte within one kernel changes the same bit the same way.
+__global__ void k_ready_init(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < (uint32_t)w.N) w.flag[h] = 1;
+}
+__global__ void k_ready_joint(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    if (joint_driven(w, j) || joint_rest_error(w, j) > JOINT_REST_ERROR) {
+        uint2 ab = w.j_ab[j];
+        w.flag[ab.x] &= (uint8_t)~1u;
+        w.flag[ab.y] &= (uint8_t)~1u;
+    }
+}
+__global__ void k_ready_gather(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.comp[h];
+    if (c >= 0 && is_dynamic(w, h) && !(w.flag[h] & 1)) w.comp_flag[c] = 1;
+}
+__global__ void k_ready_scatter(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.comp[h];
+    if (c >= 0 && is_dynamic(w, h) && w.comp_flag[c]) w.flag[h] &= (uint8_t)~1u;
+}
+__global__ void k_support_joints(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    uint2 ab = w.j_ab[j];
+    w.flag[ab.x] |= 2;
+    w.flag[ab.y] |= 2;
+}
+__global__ void k_support(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pairs(w)) return;
+    if (w.p_n[p].w <= 0.0f && w.p_np[p] > 0) {
+        uint2 ab = w.p_ab[p];
+        w.flag[ab.x] |= 2;
+        w.flag[ab.y] |= 2;
+    }
+}
+__global__ void k_sleep_timer(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    uint8_t f = w.flag[h];
+    bool freeze = w.asleep[h] != 0;
+    if (solved(w, h)) {
+        if (!(f & 2) || !(f & 1)) {
+            w.sleep_timer[h] = 0.0f;
+        } else if (len(ld3(w.vel[h])) < SLEEP_LIN && len(ld3(w.angvel[h])) < SLEEP_ANG) {
+            float t = w.sleep_timer[h] + w.dt;
+            w.sleep_timer[h] = t;
+            freeze = t >= SLEEP_TIME;
+        } else {
+            w.sleep_timer[h] = 0.0f;
+        }
+    }
+    w.flag[h] = freeze ? 4 : 0;
+}
+__global__ void k_freeze_gather(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    int c = w.comp[h];
+    if (c >= 0 && is_dynamic(w, h) && !(w.flag[h] & 4)) w.comp_flag[c] = 1;
+}
+__global__ void k_freeze_apply(DW w, int sleep_on) {
+    if (aborted_solve(w)) return;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    if (sleep_on) {
+        bool freeze = (w.flag[h] & 4) != 0;
+        int c = w.comp[h];
+        if (c >= 0 && is_dynamic(w, h) && w.comp_flag[c]) freeze = false;
+        if (freeze && !w.asleep[h] && is_dynamic(w, h)) {  // sleep_staticify (body.rs:403-408)
+            w.vel[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w.angvel[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w.inv_mass[h] = 0.0f;
+            w.inertia[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            w.asleep[h] = 1;
+        }
+        if (w.asleep[h]) atomicAdd(&w.ctr[C_SLEEP], 1u);
+    }
+    w.prev_pos[h] = w.pos[h];
+    w.prev_rot[h] = w.rot[h];
+}
+
+void launch_finish_substep(const DW& w, cudaStream_t st) {
+    unsigned gb = nblk(w.N, 256);
+    k_bdf1<<<gb, 256, 0, st>>>(w);
+    if (w.enable_sleep) {
+        k_ready_init<<<gb, 256, 0, st>>>(w);
+        if (w.J) {
+            k_ready_joint<<<nblk(w.J, 128), 128, 0, st>>>(w);
+            k_comp_clear<<<gb, 256, 0, st>>>(w);
+            k_ready_gather<<<gb, 256, 0, st>>>(w);
+            k_ready_scatter<<<gb, 256, 0, st>>>(w);
+            k_support_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
+        }
+        k_support<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+        k_sleep_timer<<<gb, 256, 0, st>>>(w);
+        k_comp_clear<<<gb, 256, 0, st>>>(w);
+        if (w.J) k_freeze_gather<<<gb, 256, 0, st>>>(w);
+    }
+    k_freeze_apply<<<gb, 256, 0, st>>>(w, w.enable_sleep);
+}
+
+}  // namespace avbd

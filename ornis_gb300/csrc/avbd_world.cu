@@ -1,0 +1,1128 @@
+// avbd_world.cu — the C ABI of include/ornis_avbd.h: world lifecycle, host
+// model <-> device SoA, the substep driver, CUDA-graph replay and the state
+// exchange used for checkpoints and parity checks.
+//
+// Host semantics mirror the reference's engine seam (crates/physics/src/
+// engine.rs:24-133, avbd/mod.rs:1211-1602): dense handles in insertion order,
+// the fixed-step accumulator of PhysicsEngine::step, JointError-style codes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "avbd_kernels.h"
+
+using namespace avbd;
+
+namespace {
+
+struct JointRec {
+    uint32_t kind, a, b;
+    float la[3], lb[3], axa[3], axb[3];
+    float ref;
+    int32_t has_lim;
+    float lo, hi;
+    AvbdJointState st;
+};
+
+struct Alloc {
+    std::vector<void*> ptrs;
+    template <class T> T* get(size_t n) {
+        void* p = nullptr;
+        if (n == 0) n = 1;
+        if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, n * sizeof(T));
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    void release() {
+        for (void* p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+struct PairBuf {
+    uint2* ab;
+    float4* n;
+    float2* mu;
+    uint32_t* np;
+    float4 *ra, *rb, *lam, *pen, *roll;
+    int32_t* matched;
+    uint32_t* offA;
+};
+
+float shape_bound(uint32_t shape, const float* p) {  // rows.rs:253-292
+    switch (shape) {
+        case AVBD_SHAPE_SPHERE: return p[0];
+        case AVBD_SHAPE_BOX: return std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
+        case AVBD_SHAPE_CAPSULE: return p[1] + p[0];
+        default: return INFINITY;
+    }
+}
+// Shape::inertia (collision/shape.rs:713-790)
+void shape_inertia(uint32_t shape, const float* sp, float mass, float out[3]) {
+    out[0] = out[1] = out[2] = 0.0f;
+    if (!(mass > 0.0f) || !std::isfinite(mass)) return;
+    if (shape == AVBD_SHAPE_SPHERE) {
+        float v = 0.4f * mass * sp[0] * sp[0];
+        out[0] = out[1] = out[2] = v;
+    } else if (shape == AVBD_SHAPE_BOX) {
+        float sx = sp[0] * 2.0f, sy = sp[1] * 2.0f, sz = sp[2] * 2.0f;
+        float x = sx * sx, y = sy * sy, z = sz * sz;
+        float k = mass / 12.0f;
+        out[0] = k * (y + z);
+        out[1] = k * (z + x);
+        out[2] = k * (x + y);
+    } else if (shape == AVBD_SHAPE_CAPSULE) {
+        float r = sp[0], h = sp[1];
+        float iy = 0.5f * mass * r * r;
+        float ixz = 0.25f * mass * (r * r) + (mass / 3.0f) * h * r + 0.25f * mass * h * h;
+        out[0] = ixz;
+        out[1] = iy;
+        out[2] = ixz;
+    }
+}
+float hinge_twist_host(const float qa[4], const float qb[4], const float ax[3]) {  // sequential_impulse/joints.rs:38-48
+    // q = conj(qa) * qb (Hamilton product, avbd/rows.rs:91-98 order)
+    float a0 = -qa[0], a1 = -qa[1], a2 = -qa[2], a3 = qa[3];
+    float x = a3 * qb[0] + a0 * qb[3] + a1 * qb[2] - a2 * qb[1];
+    float y = a3 * qb[1] - a0 * qb[2] + a1 * qb[3] + a2 * qb[0];
+    float z = a3 * qb[2] + a0 * qb[1] - a1 * qb[0] + a2 * qb[3];
+    float w = a3 * qb[3] - a0 * qb[0] - a1 * qb[1] - a2 * qb[2];
+    float t = 2.0f * std::atan2((x * ax[0] + y * ax[1]) + z * ax[2], w);
+    const float PI = 3.14159265358979323846f, TAU = 6.28318530717958647692f;
+    float r = std::fmod(t + PI, TAU);
+    if (r < 0.0f) r += std::fabs(TAU);
+    return r - PI;
+}
+
+}  // namespace
+
+struct AvbdWorld {
+    AvbdParams prm;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::vector<uint32_t> scene_off{0};
+    // host model (authoritative while host_valid)
+    std::vector<AvbdBody> bodies;
+    std::vector<AvbdBodyAux> aux;
+    std::vector<AvbdPairState> pairs;
+    std::vector<AvbdPointState> points;
+    std::vector<JointRec> joints;
+    bool host_valid = true;
+    bool dev_valid = false;
+    // device
+    Alloc mem;
+    DW w{};
+    PairBuf pb[2]{};
+    int cur = 0;  // pair buffer holding the current generation
+    uint32_t n_alloc = 0, j_alloc = 0, cand_cap = 0;
+    Tune tune;
+    BroadphasePlan plan;
+    uint32_t* d_small = nullptr;
+    uint32_t* scan_tmp = nullptr;
+    AvbdBody* d_stage = nullptr;
+    uint32_t* h_ctr = nullptr;  // pinned copy of the device counters
+    AvbdCounters cum{};
+    float time_debt = 0.0f;
+    int last_ncol = 0;
+    // graphs: one captured substep per pair-buffer parity
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int graph_cols = 0;
+    uint64_t steps = 0;
+};
+
+#define CK(x)                                    \
+    do {                                         \
+        cudaError_t e_ = (x);                    \
+        if (e_ != cudaSuccess) {                 \
+            fprintf(stderr, "ornis_avbd: %s: %s\n", #x, cudaGetErrorString(e_)); \
+            return AVBD_ERR_DEVICE;              \
+        }                                        \
+    } while (0)
+
+static void set_pair_ptrs(AvbdWorld* W) {
+    PairBuf& c = W->pb[W->cur];
+    PairBuf& o = W->pb[1 - W->cur];
+    DW& w = W->w;
+    w.p_ab = c.ab; w.p_n = c.n; w.p_mu = c.mu; w.p_np = c.np;
+    w.q_ra = c.ra; w.q_rb = c.rb; w.q_lam = c.lam; w.q_pen = c.pen; w.q_roll = c.roll; w.q_matched = c.matched;
+    w.offA = c.offA;
+    w.o_ab = o.ab; w.o_n = o.n; w.o_np = o.np;
+    w.oq_ra = o.ra; w.oq_rb = o.rb; w.oq_lam = o.lam; w.oq_pen = o.pen; w.oq_roll = o.roll;
+    w.o_offA = o.offA;
+}
+
+static void free_graphs(AvbdWorld* W) {
+    for (int i = 0; i < 2; i++)
+        if (W->gexec[i]) {
+            cudaGraphExecDestroy(W->gexec[i]);
+            W->gexec[i] = nullptr;
+        }
+}
+
+// Capacities: candidates are bounded by the sweep-and-prune overlaps plus the
+// half-space pairs; surviving pairs never outnumber candidates.
+static uint32_t default_cand_cap(uint32_t n) { return 12u * n + 4096u; }
+
+static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap) {
+    W->mem.release();
+    free_graphs(W);
+    Alloc& m = W->mem;
+    DW& w = W->w;
+    w = DW{};
+    uint32_t S = (uint32_t)W->scene_off.size() - 1;
+    w.N = (int)N;
+    w.S = (int)S;
+    w.J = (int)J;
+    w.cand_cap = cand_cap;
+    w.pair_cap = cand_cap;
+    w.scene_off = m.get<uint32_t>(S + 1);
+    w.scene_of = m.get<uint32_t>(N);
+    w.plane_off = m.get<uint32_t>(S + 1);
+    w.plane_list = m.get<uint32_t>(N);
+    w.pos = m.get<float4>(N); w.rot = m.get<float4>(N); w.vel = m.get<float4>(N);
+    w.angvel = m.get<float4>(N); w.torque = m.get<float4>(N);
+    w.pos0 = m.get<float4>(N); w.rot0 = m.get<float4>(N);
+    w.inertial = m.get<float4>(N); w.inertial_rot = m.get<float4>(N);
+    w.prev_pos = m.get<float4>(N); w.prev_rot = m.get<float4>(N);
+    w.inertia = m.get<float4>(N); w.inertia_rest = m.get<float4>(N);
+    w.mat = m.get<float4>(N); w.shp = m.get<float4>(N);
+    w.inv_mass = m.get<float>(N); w.inv_mass_rest = m.get<float>(N); w.mass = m.get<float>(N);
+    w.friction_t = m.get<float>(N); w.sleep_timer = m.get<float>(N);
+    w.info = m.get<uint32_t>(N); w.asleep = m.get<uint32_t>(N);
+    w.filter = m.get<uint2>(N);
+    w.colour = m.get<int32_t>(N);
+    w.comp = m.get<int32_t>(N);
+    w.j_kind = m.get<uint32_t>(J); w.j_ab = m.get<uint2>(J);
+    w.j_la = m.get<float4>(J); w.j_lb = m.get<float4>(J); w.j_axa = m.get<float4>(J); w.j_axb = m.get<float4>(J);
+    w.j_lim = m.get<float4>(J);
+    w.j_lam_l = m.get<float4>(J); w.j_lam_a = m.get<float4>(J); w.j_pen_l = m.get<float4>(J); w.j_pen_a = m.get<float4>(J);
+    w.jofs = m.get<uint32_t>(N + 1);
+    w.jlist = m.get<uint32_t>(2 * J);
+    for (int b = 0; b < 2; b++) {
+        PairBuf& p = W->pb[b];
+        p.ab = m.get<uint2>(cand_cap); p.n = m.get<float4>(cand_cap); p.mu = m.get<float2>(cand_cap);
+        p.np = m.get<uint32_t>(cand_cap);
+        size_t q = (size_t)cand_cap * MAX_PTS;
+        p.ra = m.get<float4>(q); p.rb = m.get<float4>(q); p.lam = m.get<float4>(q); p.pen = m.get<float4>(q);
+        p.roll = m.get<float4>(q); p.matched = m.get<int32_t>(q);
+        p.offA = m.get<uint32_t>(N + 1);
+    }
+    w.offB = m.get<uint32_t>(N + 1);
+    w.listB = m.get<uint32_t>(cand_cap);
+    w.cand = m.get<uint2>(cand_cap);
+    w.keep = m.get<uint8_t>(cand_cap);
+    w.cnt = m.get<uint32_t>(N + 1);
+    w.cur = m.get<uint32_t>(N + 1);
+    w.slot_c = m.get<uint32_t>(cand_cap);
+    w.aabb_lo = m.get<float4>(N); w.aabb_hi = m.get<float4>(N);
+    // large-scene sort scratch
+    uint32_t max_large = 0;
+    std::vector<uint32_t> small;
+    W->plan.large.clear();
+    for (uint32_t s = 0; s < S; s++) {
+        uint32_t n = W->scene_off[s + 1] - W->scene_off[s];
+        if (n <= (uint32_t)W->tune.small_scene_max) small.push_back(s);
+        else {
+            W->plan.large.push_back({W->scene_off[s], W->scene_off[s + 1]});
+            max_large = std::max(max_large, n);
+        }
+    }
+    w.sort_key = m.get<uint32_t>(max_large);
+    w.sort_idx = m.get<uint32_t>(max_large);
+    W->plan.keys_alt = m.get<uint32_t>(max_large);
+    W->plan.vals_alt = m.get<uint32_t>(max_large);
+    W->plan.hist = m.get<uint32_t>(radix_hist_words(max_large));
+    size_t scan_words = std::max(scan_tmp_words((size_t)N + 1), scan_tmp_words(radix_hist_words(max_large)));
+    W->scan_tmp = m.get<uint32_t>(scan_words + 16);
+    W->plan.scan_tmp = W->scan_tmp;
+    W->d_small = m.get<uint32_t>(small.size());
+    if (!small.empty())
+        cudaMemcpy(W->d_small, small.data(), small.size() * 4, cudaMemcpyHostToDevice);
+    W->plan.small_scenes = W->d_small;
+    W->plan.n_small = (int)small.size();
+    w.fast = m.get<uint8_t>(N);
+    w.ccd_best = m.get<unsigned long long>(N);
+    w.ccd_deps = m.get<uint32_t>(N);
+    w.ccd_state = m.get<uint8_t>(N);
+    w.ccd_recompute = m.get<uint8_t>(N);
+    w.flag = m.get<uint8_t>(N);
+    w.comp_flag = m.get<uint32_t>(N);
+    w.col_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
+    w.col_list = m.get<uint32_t>(N);
+    w.ctr = m.get<uint32_t>(C_NUM);
+    W->d_stage = m.get<AvbdBody>(N);
+    for (void* p : m.ptrs)
+        if (!p) return AVBD_ERR_DEVICE;
+    if (!w.ctr || !W->d_stage) return AVBD_ERR_DEVICE;
+    W->n_alloc = N;
+    W->j_alloc = J;
+    W->cand_cap = cand_cap;
+    w.dt = W->prm.step_dt;
+    w.gravity = V3{W->prm.gravity[0], W->prm.gravity[1], W->prm.gravity[2]};
+    w.iterations = W->prm.iterations;
+    w.enable_sleep = W->prm.enable_sleep;
+    w.enable_ccd = W->prm.enable_ccd;
+    w.max_cols = MAX_COLOURS;
+    set_pair_ptrs(W);
+    return AVBD_OK;
+}
+
+// ---- AoS <-> SoA kernels ----------------------------------------------------------
+__global__ void k_bodies_in(DW w, const AvbdBody* in, uint32_t first, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const AvbdBody& b = in[i];
+    uint32_t h = first + i;
+    w.pos[h] = make_float4(b.position[0], b.position[1], b.position[2], 0.0f);
+    w.rot[h] = make_float4(b.orientation[0], b.orientation[1], b.orientation[2], b.orientation[3]);
+    w.vel[h] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], 0.0f);
+    w.angvel[h] = make_float4(b.angular_velocity[0], b.angular_velocity[1], b.angular_velocity[2], 0.0f);
+    w.torque[h] = make_float4(b.torque[0], b.torque[1], b.torque[2], 0.0f);
+    w.mass[h] = b.mass;
+    w.inv_mass[h] = b.inv_mass;
+    w.inertia[h] = make_float4(b.inertia[0], b.inertia[1], b.inertia[2], 0.0f);
+    w.mat[h] = make_float4(b.restitution, b.friction, b.rolling_friction, b.torsion_friction);
+    w.friction_t[h] = b.friction_transverse;
+    w.filter[h] = make_uint2(b.collision_layer, b.collision_mask);
+}
+__global__ void k_bodies_out(DW w, AvbdBody* out, uint32_t first, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    AvbdBody& b = out[i];
+    uint32_t h = first + i;
+    float4 p = w.pos[h], q = w.rot[h], v = w.vel[h], om = w.angvel[h], tq = w.torque[h], in = w.inertia[h];
+    b.position[0] = p.x; b.position[1] = p.y; b.position[2] = p.z;
+    b.orientation[0] = q.x; b.orientation[1] = q.y; b.orientation[2] = q.z; b.orientation[3] = q.w;
+    b.velocity[0] = v.x; b.velocity[1] = v.y; b.velocity[2] = v.z;
+    b.angular_velocity[0] = om.x; b.angular_velocity[1] = om.y; b.angular_velocity[2] = om.z;
+    b.torque[0] = tq.x; b.torque[1] = tq.y; b.torque[2] = tq.z;
+    b.mass = w.mass[h];
+    b.inv_mass = w.inv_mass[h];
+    b.inertia[0] = in.x; b.inertia[1] = in.y; b.inertia[2] = in.z;
+    float4 m = w.mat[h];
+    b.restitution = m.x; b.friction = m.y; b.rolling_friction = m.z; b.torsion_friction = m.w;
+    b.friction_transverse = w.friction_t[h];
+    uint32_t info = w.info[h];
+    b.shape = info_shape(info);
+    float4 sp = w.shp[h];
+    b.shape_params[0] = sp.x; b.shape_params[1] = sp.y; b.shape_params[2] = sp.z;
+    uint2 f = w.filter[h];
+    b.collision_layer = f.x; b.collision_mask = f.y;
+    b.body_type = info_type(info);
+    b.flags = info_trigger(info) ? AVBD_FLAG_TRIGGER : 0u;
+}
+
+static bool body_finite(const AvbdBody& b) {
+    const float* f = b.position;
+    for (int i = 0; i < 16; i++)
+        if (!std::isfinite(f[i])) return false;
+    return std::isfinite(b.mass) && std::isfinite(b.inv_mass);
+}
+
+// Upload the whole host model: bodies, aux, joints, pairs.
+static int upload_all(AvbdWorld* W) {
+    uint32_t N = (uint32_t)W->bodies.size();
+    uint32_t J = (uint32_t)W->joints.size();
+    uint32_t S = (uint32_t)W->scene_off.size() - 1;
+    if (N == 0) return AVBD_OK;
+    uint32_t need = std::max(default_cand_cap(N), (uint32_t)W->pairs.size() + 1024u);
+    if (N != W->n_alloc || J != W->j_alloc || need > W->cand_cap || !W->w.ctr) {
+        uint32_t cap = std::max(need, W->cand_cap);
+        int rc = alloc_device(W, N, J, cap);
+        if (rc) return rc;
+    }
+    DW& w = W->w;
+    cudaStream_t st = W->st;
+    // static per-body data
+    std::vector<uint32_t> scene_of(N), info(N);
+    std::vector<float4> shp(N), inertia_rest(N);
+    std::vector<float> inv_rest(N), timer(N);
+    std::vector<uint32_t> asleep(N);
+    std::vector<float4> prev_pos(N), prev_rot(N);
+    std::vector<uint32_t> plane_off(S + 1, 0), plane_list;
+    for (uint32_t s = 0; s < S; s++) {
+        plane_off[s] = (uint32_t)plane_list.size();
+        for (uint32_t h = W->scene_off[s]; h < W->scene_off[s + 1]; h++) {
+            scene_of[h] = s;
+            if (W->bodies[h].shape == AVBD_SHAPE_HALFSPACE) plane_list.push_back(h);
+        }
+    }
+    plane_off[S] = (uint32_t)plane_list.size();
+    for (uint32_t h = 0; h < N; h++) {
+        const AvbdBody& b = W->bodies[h];
+        info[h] = (b.shape & 15u) | ((b.body_type & 3u) << 4) | ((b.flags & AVBD_FLAG_TRIGGER) ? 64u : 0u);
+        shp[h] = make_float4(b.shape_params[0], b.shape_params[1], b.shape_params[2], shape_bound(b.shape, b.shape_params));
+        float in[3];
+        bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
+        shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, in);
+        inertia_rest[h] = make_float4(in[0], in[1], in[2], 0.0f);
+        inv_rest[h] = free_mass ? 1.0f / b.mass : 0.0f;
+        const AvbdBodyAux& a = W->aux[h];
+        timer[h] = a.sleep_timer;
+        asleep[h] = a.asleep;
+        prev_pos[h] = make_float4(a.prev_position[0], a.prev_position[1], a.prev_position[2], 0.0f);
+        prev_rot[h] = make_float4(a.prev_orientation[0], a.prev_orientation[1], a.prev_orientation[2], a.prev_orientation[3]);
+    }
+    // joints: adjacency (ascending joint index per body) and components over
+    // joints whose members are both dynamic (sleep.rs:152-175)
+    std::vector<uint32_t> jofs(N + 1, 0), jlist(2 * J);
+    for (const JointRec& j : W->joints) { jofs[j.a + 1]++; jofs[j.b + 1]++; }
+    for (uint32_t h = 0; h < N; h++) jofs[h + 1] += jofs[h];
+    {
+        std::vector<uint32_t> curj(jofs.begin(), jofs.end() - 1);
+        for (uint32_t ji = 0; ji < J; ji++) {
+            jlist[curj[W->joints[ji].a]++] = ji;
+            jlist[curj[W->joints[ji].b]++] = ji;
+        }
+    }
+    std::vector<int32_t> parent(N);
+    std::iota(parent.begin(), parent.end(), 0);
+    auto find = [&](int32_t x) {
+        while (parent[x] != x) x = parent[x] = parent[parent[x]];
+        return x;
+    };
+    std::vector<uint8_t> in_joint(N, 0);
+    for (const JointRec& j : W->joints) {
+        bool da = W->bodies[j.a].body_type == AVBD_BODY_DYNAMIC, db = W->bodies[j.b].body_type == AVBD_BODY_DYNAMIC;
+        if (da && db) {
+            in_joint[j.a] = in_joint[j.b] = 1;
+            int32_t ra = find((int32_t)j.a), rb = find((int32_t)j.b);
+            if (ra != rb) parent[ra] = rb;
+        }
+    }
+    std::vector<int32_t> comp(N, -1);
+    for (uint32_t h = 0; h < N; h++)
+        if (in_joint[h]) comp[h] = find((int32_t)h);
+    std::vector<uint32_t> j_kind(J);
+    std::vector<uint2> j_ab(J);
+    std::vector<float4> j_la(J), j_lb(J), j_axa(J), j_axb(J), j_lim(J), jll(J), jla(J), jpl(J), jpa(J);
+    for (uint32_t i = 0; i < J; i++) {
+        const JointRec& j = W->joints[i];
+        j_kind[i] = j.kind;
+        j_ab[i] = make_uint2(j.a, j.b);
+        j_la[i] = make_float4(j.la[0], j.la[1], j.la[2], 0.0f);
+        j_lb[i] = make_float4(j.lb[0], j.lb[1], j.lb[2], 0.0f);
+        j_axa[i] = make_float4(j.axa[0], j.axa[1], j.axa[2], j.ref);
+        j_axb[i] = make_float4(j.axb[0], j.axb[1], j.axb[2], 0.0f);
+        j_lim[i] = make_float4(j.lo, j.hi, j.has_lim ? 1.0f : 0.0f, j.st.acc_lim);
+        jll[i] = make_float4(j.st.lam_l[0], j.st.lam_l[1], j.st.lam_l[2], 0.0f);
+        jla[i] = make_float4(j.st.lam_a[0], j.st.lam_a[1], j.st.lam_a[2], 0.0f);
+        jpl[i] = make_float4(j.st.pen_l[0], j.st.pen_l[1], j.st.pen_l[2], 0.0f);
+        jpa[i] = make_float4(j.st.pen_a[0], j.st.pen_a[1], j.st.pen_a[2], 0.0f);
+    }
+    // pairs: current generation, sorted by (a, b), CSR by a
+    std::vector<uint32_t> order(W->pairs.size());
+    std::iota(order.begin(), order.end(), 0u);
+    std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const AvbdPairState &p = W->pairs[x], &q = W->pairs[y];
+        return p.a != q.a ? p.a < q.a : p.b < q.b;
+    });
+    uint32_t P = (uint32_t)order.size();
+    std::vector<uint2> pab(P);
+    std::vector<float4> pn(P);
+    std::vector<float2> pmu(P);
+    std::vector<uint32_t> pnp(P), offA(N + 1, 0);
+    std::vector<float4> qra((size_t)P * MAX_PTS), qrb((size_t)P * MAX_PTS), qlam((size_t)P * MAX_PTS),
+        qpen((size_t)P * MAX_PTS), qroll((size_t)P * MAX_PTS);
+    std::vector<int32_t> qm((size_t)P * MAX_PTS, -1);
+    for (uint32_t i = 0; i < P; i++) {
+        const AvbdPairState& s = W->pairs[order[i]];
+        pab[i] = make_uint2(s.a, s.b);
+        pn[i] = make_float4(s.normal[0], s.normal[1], s.normal[2], s.gap);
+        pmu[i] = make_float2(s.mu[0], s.mu[1]);
+        pnp[i] = std::min<uint32_t>(s.npoints, MAX_PTS);
+        offA[s.a + 1]++;
+        for (int k = 0; k < MAX_PTS; k++) {
+            const AvbdPointState& q = W->points[(size_t)order[i] * MAX_PTS + k];
+            size_t d = (size_t)i * MAX_PTS + k;
+            qra[d] = make_float4(q.ra[0], q.ra[1], q.ra[2], 0.0f);
+            qrb[d] = make_float4(q.rb[0], q.rb[1], q.rb[2], q.stuck ? 1.0f : 0.0f);
+            qlam[d] = make_float4(q.lam[0], q.lam[1], q.lam[2], 0.0f);
+            qpen[d] = make_float4(q.pen[0], q.pen[1], q.pen[2], 0.0f);
+            qroll[d] = make_float4(q.roll_lam[0], q.roll_lam[1], q.roll_lam[2], 0.0f);
+            qm[d] = q.matched;
+        }
+    }
+    for (uint32_t h = 0; h < N; h++) offA[h + 1] += offA[h];
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    up((void*)w.scene_off, W->scene_off.data(), (S + 1) * 4);
+    up((void*)w.scene_of, scene_of.data(), N * 4);
+    up((void*)w.plane_off, plane_off.data(), (S + 1) * 4);
+    up((void*)w.plane_list, plane_list.data(), plane_list.size() * 4);
+    up(w.info, info.data(), N * 4);
+    up(w.shp, shp.data(), N * 16);
+    up(w.inertia_rest, inertia_rest.data(), N * 16);
+    up(w.inv_mass_rest, inv_rest.data(), N * 4);
+    up(w.sleep_timer, timer.data(), N * 4);
+    up(w.asleep, asleep.data(), N * 4);
+    up(w.prev_pos, prev_pos.data(), N * 16);
+    up(w.prev_rot, prev_rot.data(), N * 16);
+    up(w.comp, comp.data(), N * 4);
+    up((void*)w.jofs, jofs.data(), (N + 1) * 4);
+    up((void*)w.jlist, jlist.data(), 2 * J * 4);
+    up(w.j_kind, j_kind.data(), J * 4);
+    up(w.j_ab, j_ab.data(), J * 8);
+    up(w.j_la, j_la.data(), J * 16); up(w.j_lb, j_lb.data(), J * 16);
+    up(w.j_axa, j_axa.data(), J * 16); up(w.j_axb, j_axb.data(), J * 16);
+    up(w.j_lim, j_lim.data(), J * 16);
+    up(w.j_lam_l, jll.data(), J * 16); up(w.j_lam_a, jla.data(), J * 16);
+    up(w.j_pen_l, jpl.data(), J * 16); up(w.j_pen_a, jpa.data(), J * 16);
+    up(w.p_ab, pab.data(), P * 8); up(w.p_n, pn.data(), P * 16); up(w.p_mu, pmu.data(), P * 8);
+    up(w.p_np, pnp.data(), P * 4);
+    up(w.q_ra, qra.data(), qra.size() * 16); up(w.q_rb, qrb.data(), qrb.size() * 16);
+    up(w.q_lam, qlam.data(), qlam.size() * 16); up(w.q_pen, qpen.data(), qpen.size() * 16);
+    up(w.q_roll, qroll.data(), qroll.size() * 16); up(w.q_matched, qm.data(), qm.size() * 4);
+    up(w.offA, offA.data(), (N + 1) * 4);
+    up(W->d_stage, W->bodies.data(), N * sizeof(AvbdBody));
+    k_bodies_in<<<(N + 255) / 256, 256, 0, st>>>(w, W->d_stage, 0, N);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    W->dev_valid = true;
+    return AVBD_OK;
+}
+
+// Refresh the host model from the device.
+static int download_all(AvbdWorld* W) {
+    if (!W->dev_valid || W->host_valid) return AVBD_OK;
+    DW& w = W->w;
+    cudaStream_t st = W->st;
+    uint32_t N = (uint32_t)w.N, J = (uint32_t)w.J;
+    k_bodies_out<<<(N + 255) / 256, 256, 0, st>>>(w, W->d_stage, 0, N);
+    W->bodies.resize(N);
+    CK(cudaMemcpyAsync(W->bodies.data(), W->d_stage, N * sizeof(AvbdBody), cudaMemcpyDeviceToHost, st));
+    std::vector<float4> pp(N), pr(N);
+    std::vector<float> timer(N);
+    std::vector<uint32_t> asleep(N);
+    CK(cudaMemcpyAsync(pp.data(), w.prev_pos, N * 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(pr.data(), w.prev_rot, N * 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(timer.data(), w.sleep_timer, N * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(asleep.data(), w.asleep, N * 4, cudaMemcpyDeviceToHost, st));
+    uint32_t P = 0;
+    CK(cudaMemcpyAsync(&P, w.offA + N, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    W->aux.resize(N);
+    for (uint32_t h = 0; h < N; h++) {
+        AvbdBodyAux& a = W->aux[h];
+        a.prev_position[0] = pp[h].x; a.prev_position[1] = pp[h].y; a.prev_position[2] = pp[h].z;
+        a.prev_orientation[0] = pr[h].x; a.prev_orientation[1] = pr[h].y;
+        a.prev_orientation[2] = pr[h].z; a.prev_orientation[3] = pr[h].w;
+        a.sleep_timer = timer[h];
+        a.asleep = asleep[h];
+    }
+    std::vector<uint2> pab(P);
+    std::vector<float4> pn(P);
+    std::vector<float2> pmu(P);
+    std::vector<uint32_t> pnp(P);
+    size_t Q = (size_t)P * MAX_PTS;
+    std::vector<float4> qra(Q), qrb(Q), qlam(Q), qpen(Q), qroll(Q);
+    std::vector<int32_t> qm(Q);
+    if (P) {
+        CK(cudaMemcpyAsync(pab.data(), w.p_ab, P * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(pn.data(), w.p_n, P * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(pmu.data(), w.p_mu, P * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(pnp.data(), w.p_np, P * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qra.data(), w.q_ra, Q * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qrb.data(), w.q_rb, Q * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qlam.data(), w.q_lam, Q * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qpen.data(), w.q_pen, Q * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qroll.data(), w.q_roll, Q * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(qm.data(), w.q_matched, Q * 4, cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<float4> jll(J), jla(J), jpl(J), jpa(J), jlim(J);
+    if (J) {
+        CK(cudaMemcpyAsync(jll.data(), w.j_lam_l, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jla.data(), w.j_lam_a, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jpl.data(), w.j_pen_l, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jpa.data(), w.j_pen_a, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jlim.data(), w.j_lim, J * 16, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    W->pairs.resize(P);
+    W->points.assign(Q, AvbdPointState{});
+    for (uint32_t i = 0; i < P; i++) {
+        AvbdPairState& s = W->pairs[i];
+        s.a = pab[i].x; s.b = pab[i].y;
+        s.normal[0] = pn[i].x; s.normal[1] = pn[i].y; s.normal[2] = pn[i].z;
+        s.gap = pn[i].w;
+        s.mu[0] = pmu[i].x; s.mu[1] = pmu[i].y;
+        s.npoints = pnp[i];
+        for (int k = 0; k < MAX_PTS; k++) {
+            size_t d = (size_t)i * MAX_PTS + k;
+            AvbdPointState& q = W->points[d];
+            q.matched = -1;
+            if ((uint32_t)k >= pnp[i]) continue;
+            q.ra[0] = qra[d].x; q.ra[1] = qra[d].y; q.ra[2] = qra[d].z;
+            q.rb[0] = qrb[d].x; q.rb[1] = qrb[d].y; q.rb[2] = qrb[d].z;
+            q.stuck = qrb[d].w != 0.0f;
+            q.lam[0] = qlam[d].x; q.lam[1] = qlam[d].y; q.lam[2] = qlam[d].z;
+            q.pen[0] = qpen[d].x; q.pen[1] = qpen[d].y; q.pen[2] = qpen[d].z;
+            q.roll_lam[0] = qroll[d].x; q.roll_lam[1] = qroll[d].y; q.roll_lam[2] = qroll[d].z;
+            q.matched = qm[d];
+        }
+    }
+    for (uint32_t i = 0; i < J; i++) {
+        AvbdJointState& s = W->joints[i].st;
+        s.lam_l[0] = jll[i].x; s.lam_l[1] = jll[i].y; s.lam_l[2] = jll[i].z;
+        s.lam_a[0] = jla[i].x; s.lam_a[1] = jla[i].y; s.lam_a[2] = jla[i].z;
+        s.pen_l[0] = jpl[i].x; s.pen_l[1] = jpl[i].y; s.pen_l[2] = jpl[i].z;
+        s.pen_a[0] = jpa[i].x; s.pen_a[1] = jpa[i].y; s.pen_a[2] = jpa[i].z;
+        s.acc_lim = jlim[i].w;
+    }
+    W->host_valid = true;
+    return AVBD_OK;
+}
+
+static int ensure_device(AvbdWorld* W) {
+    if (W->dev_valid && !W->host_valid) return AVBD_OK;
+    if (W->dev_valid && W->host_valid) return AVBD_OK;
+    return upload_all(W);
+}
+// The host model is about to change: make it current and mark the device stale.
+static int host_edit(AvbdWorld* W) {
+    int rc = download_all(W);
+    W->dev_valid = false;
+    W->host_valid = true;
+    return rc;
+}
+
+// ---- substep driver ---------------------------------------------------------------
+// Enqueue one substep up to and including the colouring.
+static void enqueue_front(AvbdWorld* W) {
+    cudaStream_t st = W->st;
+    W->cur = 1 - W->cur;  // the previous generation becomes `old`
+    set_pair_ptrs(W);
+    const DW& w = W->w;
+    launch_begin_substep(w, st);
+    launch_wake_joint_motion(w, st);
+    launch_torque(w, st);
+    launch_broadphase(w, W->plan, st);
+    launch_ccd(w, st);
+    launch_discovery(w, W->scan_tmp, st);
+    launch_post_discovery(w, W->scan_tmp, st);
+    launch_colouring(w, W->scan_tmp, st);
+}
+static void enqueue_back(AvbdWorld* W, int ncol) {
+    const DW& w = W->w;
+    for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
+    launch_finish_substep(w, W->st);
+}
+
+static int read_ctr(AvbdWorld* W) {
+    CK(cudaMemcpyAsync(W->h_ctr, W->w.ctr, C_NUM * 4, cudaMemcpyDeviceToHost, W->st));
+    CK(cudaStreamSynchronize(W->st));
+    return AVBD_OK;
+}
+
+static int grow_candidates(AvbdWorld* W) {
+    // keep the (valid) previous generation: round-trip through the host model
+    W->host_valid = false;
+    int rc = download_all(W);
+    if (rc) return rc;
+    uint32_t cap = W->cand_cap * 2u;
+    rc = alloc_device(W, (uint32_t)W->bodies.size(), (uint32_t)W->joints.size(), cap);
+    if (rc) return rc;
+    W->dev_valid = false;
+    return upload_all(W);
+}
+
+static void accumulate(AvbdWorld* W) {
+    const uint32_t* c = W->h_ctr;
+    W->cum.steps += 1;
+    W->cum.pairs = c[C_PAIRS];
+    W->cum.points = c[C_POINTS];
+    W->cum.candidates = c[C_CAND];
+    W->cum.colours = c[C_NCOL];
+    W->cum.breakdowns = c[C_BREAKDOWN];
+    W->cum.ccd_hits = c[C_CCD];
+    W->cum.sleeping = c[C_SLEEP];
+    W->cum.timeouts = c[C_TIMEOUT] + c[C_CCD_LEFT];
+}
+
+// One substep through plain launches (the host reads the colour count).
+static int substep_plain(AvbdWorld* W) {
+    for (int attempt = 0; attempt < 8; attempt++) {
+        enqueue_front(W);
+        CK(cudaGetLastError());
+        int rc = read_ctr(W);
+        if (rc) return rc;
+        if (W->h_ctr[C_ERR] & E_CAND_OVERFLOW) {
+            // nothing after the broadphase ran: undo the buffer flip, grow, replay
+            W->cur = 1 - W->cur;
+            set_pair_ptrs(W);
+            CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, W->st));
+            rc = grow_candidates(W);
+            if (rc) return rc;
+            continue;
+        }
+        int ncol = (int)W->h_ctr[C_NCOL];
+        W->last_ncol = ncol;
+        enqueue_back(W, ncol);
+        CK(cudaGetLastError());
+        rc = read_ctr(W);
+        if (rc) return rc;
+        accumulate(W);
+        if (W->h_ctr[C_ERR] & E_COLOUR_OVERFLOW) return AVBD_ERR_CAPACITY;
+        return AVBD_OK;
+    }
+    return AVBD_ERR_CAPACITY;
+}
+
+extern "C" {
+
+int avbd_default_params(AvbdParams* p) {
+    if (!p) return AVBD_ERR_INVALID_ARG;
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -9.81f;
+    p->gravity[2] = 0.0f;
+    p->step_dt = 1.0f / 60.0f;
+    p->iterations = 10;
+    p->max_substeps = 4;
+    p->enable_sleep = 1;
+    p->enable_ccd = 1;
+    return AVBD_OK;
+}
+
+int avbd_world_create(const AvbdParams* params, int device, AvbdWorld** out) {
+    if (!params || !out) return AVBD_ERR_INVALID_ARG;
+    if (!(params->step_dt > 0.0f) || !std::isfinite(params->step_dt) || params->iterations < 0 ||
+        params->max_substeps < 1)
+        return AVBD_ERR_INVALID_ARG;
+    AvbdWorld* W = new AvbdWorld();
+    W->prm = *params;
+    W->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&W->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&W->h_ctr, C_NUM * 4) != cudaSuccess) {
+        delete W;
+        return AVBD_ERR_DEVICE;
+    }
+    W->scene_off = {0, 0};
+    *out = W;
+    return AVBD_OK;
+}
+
+int avbd_world_create_batch(const AvbdParams* params, int device, const AvbdBody* bodies, uint32_t n,
+                            const uint32_t* scene_offsets, uint32_t nscenes, AvbdWorld** out) {
+    if (!bodies || !scene_offsets || nscenes == 0 || scene_offsets[0] != 0 || scene_offsets[nscenes] != n)
+        return AVBD_ERR_INVALID_ARG;
+    for (uint32_t s = 0; s < nscenes; s++)
+        if (scene_offsets[s + 1] < scene_offsets[s]) return AVBD_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; i++)
+        if (!body_finite(bodies[i])) return AVBD_ERR_NONFINITE;
+    int rc = avbd_world_create(params, device, out);
+    if (rc) return rc;
+    AvbdWorld* W = *out;
+    W->scene_off.assign(scene_offsets, scene_offsets + nscenes + 1);
+    W->bodies.assign(bodies, bodies + n);
+    W->aux.resize(n);
+    for (uint32_t i = 0; i < n; i++) {
+        AvbdBodyAux& a = W->aux[i];
+        std::memcpy(a.prev_position, bodies[i].position, 12);
+        std::memcpy(a.prev_orientation, bodies[i].orientation, 16);
+        a.sleep_timer = 0.0f;
+        a.asleep = 0;
+    }
+    return AVBD_OK;
+}
+
+int avbd_world_destroy(AvbdWorld* W) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    free_graphs(W);
+    W->mem.release();
+    if (W->h_ctr) cudaFreeHost(W->h_ctr);
+    if (W->st) cudaStreamDestroy(W->st);
+    delete W;
+    return AVBD_OK;
+}
+
+int avbd_world_add_bodies(AvbdWorld* W, const AvbdBody* bodies, uint32_t n, uint32_t* first_handle) {
+    if (!W || (!bodies && n)) return AVBD_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; i++)
+        if (!body_finite(bodies[i])) return AVBD_ERR_NONFINITE;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    uint32_t first = (uint32_t)W->bodies.size();
+    for (uint32_t i = 0; i < n; i++) {
+        W->bodies.push_back(bodies[i]);
+        AvbdBodyAux a{};
+        std::memcpy(a.prev_position, bodies[i].position, 12);  // ensure_scratch (mod.rs:1193-1199)
+        std::memcpy(a.prev_orientation, bodies[i].orientation, 16);
+        W->aux.push_back(a);
+    }
+    W->scene_off.back() = (uint32_t)W->bodies.size();
+    if (first_handle) *first_handle = first;
+    return AVBD_OK;
+}
+
+int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle) {
+    if (!W || !d) return AVBD_ERR_INVALID_ARG;
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(d->local_anchor_a[k]) || !std::isfinite(d->local_anchor_b[k]) ||
+            !std::isfinite(d->local_axis_a[k]) || !std::isfinite(d->local_axis_b[k]))
+            return AVBD_ERR_JOINT_NONFINITE;
+    if (d->kind != AVBD_JOINT_BALL && d->kind != AVBD_JOINT_REVOLUTE) return AVBD_ERR_UNSUPPORTED;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    uint32_t n = (uint32_t)W->bodies.size();
+    // a new constraint wakes both members (mod.rs:1320-1321)
+    for (uint32_t h : {d->body_a, d->body_b})
+        if (h < n && W->aux[h].asleep) {
+            W->aux[h].asleep = 0;
+            W->aux[h].sleep_timer = 0.0f;
+            AvbdBody& b = W->bodies[h];
+            if (b.body_type == AVBD_BODY_DYNAMIC) {
+                bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
+                b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
+                shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, b.inertia);
+            }
+        }
+    if (d->body_a == d->body_b) return AVBD_ERR_JOINT_SELF;
+    if (d->body_a >= n || d->body_b >= n) return AVBD_ERR_JOINT_HANDLES;
+    // both members must live in the same scene
+    auto scene_of = [&](uint32_t h) {
+        return (uint32_t)(std::upper_bound(W->scene_off.begin(), W->scene_off.end(), h) - W->scene_off.begin()) - 1;
+    };
+    if (scene_of(d->body_a) != scene_of(d->body_b)) return AVBD_ERR_JOINT_HANDLES;
+    JointRec j{};
+    j.kind = d->kind;
+    j.a = d->body_a;
+    j.b = d->body_b;
+    std::memcpy(j.la, d->local_anchor_a, 12);
+    std::memcpy(j.lb, d->local_anchor_b, 12);
+    j.axa[0] = 1.0f; j.axb[0] = 1.0f;
+    if (d->kind == AVBD_JOINT_REVOLUTE) {  // joint.rs:1280-1294
+        const float* aa = d->local_axis_a;
+        const float* ab = d->local_axis_b;
+        float la2 = (aa[0] * aa[0] + aa[1] * aa[1]) + aa[2] * aa[2];
+        float lb2 = (ab[0] * ab[0] + ab[1] * ab[1]) + ab[2] * ab[2];
+        if (la2 < 1e-12f || lb2 < 1e-12f) return AVBD_ERR_JOINT_BAD_AXIS;
+        float ra = 1.0f / std::sqrt(la2), rb = 1.0f / std::sqrt(lb2);
+        for (int k = 0; k < 3; k++) {
+            j.axa[k] = aa[k] * ra;
+            j.axb[k] = ab[k] * rb;
+        }
+        j.ref = hinge_twist_host(W->bodies[j.a].orientation, W->bodies[j.b].orientation, j.axa);
+        j.has_lim = d->has_limit;
+        j.lo = d->limit_min;
+        j.hi = d->limit_max;
+    }
+    for (int k = 0; k < 3; k++) {
+        j.st.pen_l[k] = 1.0f;  // JOINT_PENALTY_INIT
+        j.st.pen_a[k] = 1.0f;
+    }
+    W->joints.push_back(j);
+    if (handle) *handle = (uint32_t)(W->joints.size() - 1);
+    return AVBD_OK;
+}
+
+int avbd_world_body_count(const AvbdWorld* W, uint32_t* n) {
+    if (!W || !n) return AVBD_ERR_INVALID_ARG;
+    *n = W->host_valid ? (uint32_t)W->bodies.size() : (uint32_t)W->w.N;
+    return AVBD_OK;
+}
+int avbd_world_scene_count(const AvbdWorld* W, uint32_t* n) {
+    if (!W || !n) return AVBD_ERR_INVALID_ARG;
+    *n = (uint32_t)W->scene_off.size() - 1;
+    return AVBD_OK;
+}
+
+int avbd_world_get_bodies(AvbdWorld* W, uint32_t first, uint32_t n, AvbdBody* out) {
+    if (!W || (!out && n)) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    if (W->host_valid) {
+        if ((size_t)first + n > W->bodies.size()) return AVBD_ERR_INVALID_ARG;
+        std::memcpy(out, W->bodies.data() + first, n * sizeof(AvbdBody));
+        return AVBD_OK;
+    }
+    if ((size_t)first + n > (size_t)W->w.N) return AVBD_ERR_INVALID_ARG;
+    if (n == 0) return AVBD_OK;
+    k_bodies_out<<<(n + 255) / 256, 256, 0, W->st>>>(W->w, W->d_stage, first, n);
+    CK(cudaMemcpyAsync(out, W->d_stage, n * sizeof(AvbdBody), cudaMemcpyDeviceToHost, W->st));
+    CK(cudaStreamSynchronize(W->st));
+    return AVBD_OK;
+}
+
+int avbd_world_set_bodies(AvbdWorld* W, uint32_t first, uint32_t n, const AvbdBody* in) {
+    if (!W || (!in && n)) return AVBD_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < n; i++)
+        if (!body_finite(in[i])) return AVBD_ERR_NONFINITE;
+    cudaSetDevice(W->device);
+    if (W->host_valid) {
+        if ((size_t)first + n > W->bodies.size()) return AVBD_ERR_INVALID_ARG;
+        for (uint32_t i = 0; i < n; i++) {
+            const AvbdBody& o = W->bodies[first + i];
+            if (o.shape != in[i].shape || o.body_type != in[i].body_type ||
+                std::memcmp(o.shape_params, in[i].shape_params, 12) != 0 || o.flags != in[i].flags)
+                W->dev_valid = false;  // static per-body data changed: full re-upload
+        }
+        std::memcpy(W->bodies.data() + first, in, n * sizeof(AvbdBody));
+        if (W->dev_valid) {
+            CK(cudaMemcpyAsync(W->d_stage, in, n * sizeof(AvbdBody), cudaMemcpyHostToDevice, W->st));
+            k_bodies_in<<<(n + 255) / 256, 256, 0, W->st>>>(W->w, W->d_stage, first, n);
+            CK(cudaStreamSynchronize(W->st));
+        }
+        return AVBD_OK;
+    }
+    if ((size_t)first + n > (size_t)W->w.N) return AVBD_ERR_INVALID_ARG;
+    if (n == 0) return AVBD_OK;
+    // device-resident: dynamic fields only (shape, type and flags are fixed
+    // after creation on this path)
+    CK(cudaMemcpyAsync(W->d_stage, in, n * sizeof(AvbdBody), cudaMemcpyHostToDevice, W->st));
+    k_bodies_in<<<(n + 255) / 256, 256, 0, W->st>>>(W->w, W->d_stage, first, n);
+    CK(cudaGetLastError());
+    return AVBD_OK;
+}
+
+int avbd_world_sync(AvbdWorld* W) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    CK(cudaStreamSynchronize(W->st));
+    return AVBD_OK;
+}
+
+static int begin_steps(AvbdWorld* W) {
+    cudaSetDevice(W->device);
+    if (W->host_valid && W->dev_valid) {
+        W->host_valid = false;
+        return AVBD_OK;
+    }
+    int rc = ensure_device(W);
+    if (rc) return rc;
+    W->host_valid = false;
+    return AVBD_OK;
+}
+
+int avbd_world_step_fixed(AvbdWorld* W, int32_t substeps) {
+    if (!W || substeps < 0) return AVBD_ERR_INVALID_ARG;
+    if (W->bodies.empty() && W->host_valid) return AVBD_OK;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    for (int i = 0; i < substeps; i++) {
+        rc = substep_plain(W);
+        if (rc) return rc;
+    }
+    return AVBD_OK;
+}
+
+int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    if (!std::isfinite(dt) || dt <= 0.0f) return AVBD_OK;
+    float sd = W->prm.step_dt;
+    W->time_debt = std::fmin(W->time_debt + dt, sd * (float)W->prm.max_substeps);
+    int n = 0;
+    while (W->time_debt >= sd && n < W->prm.max_substeps) {
+        W->time_debt -= sd;
+        n++;
+    }
+    return n ? avbd_world_step_fixed(W, n) : AVBD_OK;
+}
+
+// Graph replay: one captured substep per pair-buffer parity.  The primal is
+// captured for `graph_cols` colours; a substep that needs more colours stops
+// before its iterations (the colouring flags it) and is finished with plain
+// launches, then the graphs are re-captured wider.
+static int capture(AvbdWorld* W) {
+    free_graphs(W);
+    int base = W->cur;
+    for (int k = 0; k < 2; k++) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(W->st, cudaStreamCaptureModeThreadLocal));
+        W->w.max_cols = W->graph_cols;
+        enqueue_front(W);
+        enqueue_back(W, W->graph_cols);
+        W->w.max_cols = MAX_COLOURS;
+        CK(cudaStreamEndCapture(W->st, &g));
+        cudaError_t e = cudaGraphInstantiate(&W->gexec[W->cur], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            free_graphs(W);
+            W->cur = base;
+            set_pair_ptrs(W);
+            return AVBD_ERR_DEVICE;
+        }
+    }
+    // capture flipped the parity twice: back where we started
+    W->cur = base;
+    set_pair_ptrs(W);
+    return AVBD_OK;
+}
+
+int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
+    if (!W || substeps < 0) return AVBD_ERR_INVALID_ARG;
+    if (W->bodies.empty() && W->host_valid) return AVBD_OK;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    for (int i = 0; i < substeps; i++) {
+        if (!W->gexec[0] || W->last_ncol > W->graph_cols) {
+            if (W->last_ncol == 0) {
+                rc = substep_plain(W);  // learn the colour count first
+                if (rc) return rc;
+                continue;
+            }
+            W->graph_cols = W->last_ncol + 2;
+            rc = capture(W);
+            if (rc) return rc;
+        }
+        int next = 1 - W->cur;  // the parity this substep writes
+        CK(cudaGraphLaunch(W->gexec[next], W->st));
+        W->cur = next;
+        set_pair_ptrs(W);
+        rc = read_ctr(W);
+        if (rc) return rc;
+        if (W->h_ctr[C_ERR] & E_CAND_OVERFLOW) {
+            W->cur = 1 - W->cur;
+            set_pair_ptrs(W);
+            CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, W->st));
+            rc = grow_candidates(W);
+            if (rc) return rc;
+            W->host_valid = false;
+            rc = substep_plain(W);
+            if (rc) return rc;
+            continue;
+        }
+        int ncol = (int)W->h_ctr[C_NCOL];
+        W->last_ncol = ncol;
+        if (W->h_ctr[C_ERR] & E_COLOUR_RANGE) {
+            // the graph's iterations were skipped: finish this substep plainly
+            CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, W->st));
+            enqueue_back(W, ncol);
+            rc = read_ctr(W);
+            if (rc) return rc;
+        }
+        accumulate(W);
+    }
+    return AVBD_OK;
+}
+
+int avbd_world_get_counters(AvbdWorld* W, AvbdCounters* out) {
+    if (!W || !out) return AVBD_ERR_INVALID_ARG;
+    *out = W->cum;
+    return AVBD_OK;
+}
+
+int avbd_world_state_sizes(AvbdWorld* W, uint32_t* nb, uint32_t* np, uint32_t* nj) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = download_all(W);
+    if (rc) return rc;
+    if (nb) *nb = (uint32_t)W->bodies.size();
+    if (np) *np = (uint32_t)W->pairs.size();
+    if (nj) *nj = (uint32_t)W->joints.size();
+    return AVBD_OK;
+}
+
+int avbd_world_export_state(AvbdWorld* W, AvbdBody* bodies, AvbdBodyAux* aux, AvbdPairState* pairs,
+                            AvbdPointState* points, AvbdJointState* joints, uint32_t pair_capacity) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = download_all(W);
+    if (rc) return rc;
+    if ((pairs || points) && pair_capacity < W->pairs.size()) return AVBD_ERR_CAPACITY;
+    if (bodies) std::memcpy(bodies, W->bodies.data(), W->bodies.size() * sizeof(AvbdBody));
+    if (aux) std::memcpy(aux, W->aux.data(), W->aux.size() * sizeof(AvbdBodyAux));
+    if (pairs) std::memcpy(pairs, W->pairs.data(), W->pairs.size() * sizeof(AvbdPairState));
+    if (points) std::memcpy(points, W->points.data(), W->points.size() * sizeof(AvbdPointState));
+    if (joints)
+        for (size_t i = 0; i < W->joints.size(); i++) joints[i] = W->joints[i].st;
+    return AVBD_OK;
+}
+
+int avbd_world_import_state(AvbdWorld* W, const AvbdBody* bodies, const AvbdBodyAux* aux, const AvbdPairState* pairs,
+                            const AvbdPointState* points, uint32_t npairs, const AvbdJointState* joints) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    size_t n = W->bodies.size();
+    if (bodies) {
+        for (size_t i = 0; i < n; i++)
+            if (!body_finite(bodies[i])) return AVBD_ERR_NONFINITE;
+        std::memcpy(W->bodies.data(), bodies, n * sizeof(AvbdBody));
+    }
+    if (aux) std::memcpy(W->aux.data(), aux, n * sizeof(AvbdBodyAux));
+    if (pairs) {
+        if (npairs && !points) return AVBD_ERR_INVALID_ARG;
+        for (uint32_t i = 0; i < npairs; i++)
+            if (pairs[i].a >= n || pairs[i].b >= n || pairs[i].a >= pairs[i].b || pairs[i].npoints > MAX_PTS)
+                return AVBD_ERR_INVALID_ARG;
+        W->pairs.assign(pairs, pairs + npairs);
+        W->points.assign(points, points + (size_t)npairs * MAX_PTS);
+    }
+    if (joints)
+        for (size_t i = 0; i < W->joints.size(); i++) W->joints[i].st = joints[i];
+    W->time_debt = 0.0f;
+    return AVBD_OK;
+}
+
+int avbd_world_get_colours(AvbdWorld* W, int32_t* colours, uint32_t n) {
+    if (!W || !colours) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    if (!W->dev_valid || !W->w.colour) {
+        for (uint32_t i = 0; i < n; i++) colours[i] = -1;
+        return AVBD_OK;
+    }
+    if (n > (uint32_t)W->w.N) return AVBD_ERR_INVALID_ARG;
+    CK(cudaMemcpyAsync(colours, W->w.colour, n * 4, cudaMemcpyDeviceToHost, W->st));
+    CK(cudaStreamSynchronize(W->st));
+    return AVBD_OK;
+}
+
+// RigidBody::new_sphere / new_box / new_capsule / try_new_halfspace
+// (body.rs:346-376, :470-576, :873-889): default materials and mass triple.
+int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const float* position, float mass) {
+    if (!out || !params || !position) return AVBD_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    float rest = 0.3f, fric = 0.5f;
+    float sp[3] = {params[0], params[1], params[2]};
+    if (shape == AVBD_SHAPE_SPHERE) { rest = 0.5f; fric = 0.3f; }
+    else if (shape == AVBD_SHAPE_CAPSULE) { rest = 0.4f; fric = 0.4f; }
+    else if (shape == AVBD_SHAPE_HALFSPACE) {
+        if (mass > 0.0f && std::isfinite(mass)) return AVBD_ERR_INVALID_ARG;
+        float l = std::sqrt((sp[0] * sp[0] + sp[1] * sp[1]) + sp[2] * sp[2]);
+        float r = 1.0f / l;
+        if (!std::isfinite(r) || !(r > 0.0f)) return AVBD_ERR_INVALID_ARG;
+        for (float& v : sp) v *= r;
+        rest = 0.3f; fric = 0.6f;
+    } else if (shape != AVBD_SHAPE_BOX) {
+        return AVBD_ERR_UNSUPPORTED;
+    }
+    bool free_mass = mass > 0.0f && std::isfinite(mass);
+    std::memcpy(out->position, position, 12);
+    out->orientation[3] = 1.0f;
+    out->mass = free_mass ? mass : 0.0f;
+    out->inv_mass = free_mass ? 1.0f / mass : 0.0f;
+    shape_inertia(shape, sp, free_mass ? mass : 0.0f, out->inertia);
+    out->restitution = rest;
+    out->friction = fric;
+    out->friction_transverse = fric;
+    out->shape = shape;
+    std::memcpy(out->shape_params, sp, 12);
+    out->collision_layer = 1;
+    out->collision_mask = 0xffffffffu;
+    out->body_type = mass > 0.0f ? AVBD_BODY_DYNAMIC : AVBD_BODY_STATIC;
+    return AVBD_OK;
+}
+
+int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    if (primal_lanes != 1 && primal_lanes != 4 && primal_lanes != 8 && primal_lanes != 16 && primal_lanes != 32)
+        return AVBD_ERR_INVALID_ARG;
+    if (primal_block < 32 || primal_block > 1024 || primal_block % 32) return AVBD_ERR_INVALID_ARG;
+    W->tune.primal_lanes = primal_lanes;
+    W->tune.primal_block = primal_block;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
+int avbd_abi_version(void) { return AVBD_ABI_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// avbd_world.cuh — device-side layout of an AVBD world (flat multi-scene SoA)
+// and the solver constants of the reference (crates/physics/src/avbd/mod.rs:154-247,
+// crates/physics/src/constants.rs:26-79).
+#pragma once
+#include "../../include/ornis_avbd.h"
+#include "avbd_vec.cuh"
+
+namespace avbd {
+
+constexpr float ALPHA = 0.99f;
+constexpr float GAMMA = 0.999f;
+constexpr float BETA = 10000.0f;
+constexpr float BETA_ANG = 100.0f;
+constexpr float MARGIN = 0.01f;
+constexpr float PENALTY_MIN = 1.0f;
+constexpr float PENALTY_MAX = 1.0e10f;
+constexpr float PENALTY_INIT = 1.0f;
+constexpr float JOINT_PENALTY_INIT = 1.0f;
+constexpr float GEN_MARGIN = 0.05f;
+constexpr float EXPAND_SLOP = 0.005f;
+constexpr float POINT_MATCH_DIST = 0.03f;
+constexpr float LAMBDA_MATCH_DIST = 0.05f;
+constexpr float C_EPS = 1e-7f;
+constexpr float STICK_THRESH = 0.00001f;
+constexpr float SLEEP_LIN = 0.15f;
+constexpr float SLEEP_ANG = 0.15f;
+constexpr float HALF = 0.5f;
+constexpr float SLEEP_TIME = 0.5f;
+constexpr float WAKE_IMPACT_SPEED = 0.5f;
+constexpr float WAKE_PENETRATION = 0.01f;
+constexpr float LIMIT_SLOP_ANG = 0.005f;
+constexpr float LIM_PEN_MAX = 1e4f;
+constexpr float ROLL_PEN = 100.0f;
+constexpr float MIN_TOI_DISP_LENGTH = 1e-9f;
+constexpr float SPIN_REST_EPS = 1e-9f;
+constexpr float CCD_BOUNCE_SPEED = 1.0f;
+constexpr float DEGENERATE_LEN2 = 1e-12f;
+constexpr float NEAR_ZERO = 1e-9f;
+constexpr float SHAPE_TOUCH = 1e-3f;
+constexpr float AXIS_REST_LEN2 = 1e-16f;
+constexpr float CCD_TRAVEL_GATE_FRACTION = 0.5f;
+constexpr float DEGENERATE_EPS = 1e-12f;
+constexpr float FACE_AXIS_EPS = 1e-6f;
+constexpr float SPINE_ALIGNMENT_EPS = 1e-6f;
+constexpr float TANGENT_REF_AXIS_DOT = 0.9f;
+constexpr float JOINT_REST_ERROR = 0.005f;
+constexpr float PI_F = 3.14159265358979323846f;
+constexpr float TAU_F = 6.28318530717958647692f;
+constexpr int MAX_PTS = AVBD_MAX_POINTS;
+constexpr int MAX_COLOURS = 64;
+constexpr int CCD_ROUNDS = 8;
+
+// body info word: shape kind in bits 0-3, body type in bits 4-5, trigger bit 6
+__host__ __device__ __forceinline__ uint32_t info_shape(uint32_t i) { return i & 15u; }
+__host__ __device__ __forceinline__ uint32_t info_type(uint32_t i) { return (i >> 4) & 3u; }
+__host__ __device__ __forceinline__ bool info_trigger(uint32_t i) { return (i >> 6) & 1u; }
+
+// device counters (indices into DW::ctr)
+enum Ctr {
+    C_CAND = 0,       // broadphase candidates written this substep
+    C_PAIRS = 1,      // live pairs after discovery
+    C_ERR = 2,        // error bits (E_*)
+    C_BREAKDOWN = 3,  // cumulative LDL breakdowns
+    C_CCD = 4,        // cumulative TOI clamps
+    C_NCOL = 5,       // colours used this substep (max over scenes)
+    C_TIMEOUT = 6,    // cumulative bounded-wait give-ups
+    C_FAST = 7,       // fast (CCD) bodies this substep
+    C_POINTS = 8,     // live points
+    C_SLEEP = 9,      // bodies asleep
+    C_CCD_LEFT = 10,  // fast bodies left after the bounded CCD rounds
+    C_NUM = 16
+};
+enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
+
+// Everything a kernel needs, passed by value (pointers into one world's
+// device allocations).  Scene s owns bodies [scene_off[s], scene_off[s+1]).
+struct DW {
+    int N;  // bodies
+    int S;  // scenes
+    int J;  // joints
+    float dt;
+    V3 gravity;
+    int iterations;
+    int enable_sleep, enable_ccd;
+    uint32_t cand_cap, pair_cap;
+    int max_cols;  // colours the launched iteration covers (a CUDA graph fixes it at capture)
+
+    const uint32_t* scene_off;  // S+1
+    const uint32_t* scene_of;   // N
+    const uint32_t* plane_off;  // S+1: half-space bodies of each scene
+    const uint32_t* plane_list;
+
+    // bodies
+    float4 *pos, *rot, *vel, *angvel, *torque;
+    float4 *pos0, *rot0, *inertial, *inertial_rot, *prev_pos, *prev_rot;
+    float4 *inertia, *inertia_rest;
+    float4* mat;  // restitution, friction, rolling, torsion
+    float4* shp;  // shape params xyz, bound radius w
+    float *inv_mass, *inv_mass_rest, *mass, *friction_t, *sleep_timer;
+    uint32_t *info, *asleep;
+    uint2* filter;  // collision layer, mask
+    int32_t* colour;
+    int32_t* comp;  // joint component id (-1: no joint)
+
+    // joints (Ball / Revolute)
+    uint32_t* j_kind;
+    uint2* j_ab;
+    float4 *j_la, *j_lb, *j_axa, *j_axb;  // w of j_axa = reference twist
+    float4* j_lim;                         // lo, hi, has_limit, acc_lim
+    float4 *j_lam_l, *j_lam_a, *j_pen_l, *j_pen_a;
+    const uint32_t *jofs, *jlist;  // per-body joint adjacency (N+1, 2J)
+
+    // contact pairs: current generation (read by the solver) ...
+    uint2* p_ab;
+    float4* p_n;  // normal xyz, gap w
+    float2* p_mu;
+    uint32_t* p_np;
+    float4 *q_ra, *q_rb, *q_lam, *q_pen, *q_roll;  // q_rb.w = stuck
+    int32_t* q_matched;
+    uint32_t* offA;  // N+1: pairs whose A side is body h are [offA[h], offA[h+1])
+    uint32_t* offB;  // N+1: B-side incidence list
+    uint32_t* listB;
+    // ... and the previous generation (read by discovery for the warm merge)
+    uint2* o_ab;
+    float4* o_n;
+    uint32_t* o_np;
+    float4 *oq_ra, *oq_rb, *oq_lam, *oq_pen, *oq_roll;
+    uint32_t* o_offA;
+
+    // broadphase / discovery scratch
+    uint2* cand;       // candidate (a, b), a < b
+    uint8_t* keep;     // per candidate
+    uint32_t* cnt;     // per body counters (N+1)
+    uint32_t* cur;     // per body cursors
+    uint32_t* slot_c;  // final pair slot -> candidate index
+    float4 *aabb_lo, *aabb_hi;
+    uint32_t* sort_key;
+    uint32_t* sort_idx;
+
+    // CCD scratch
+    uint8_t* fast;
+    unsigned long long* ccd_best;
+    uint32_t* ccd_deps;
+    uint8_t* ccd_state;  // 0 pending, 1 final, 2 final+moved
+    uint8_t* ccd_recompute;
+
+    // wake / sleep scratch
+    uint8_t* flag;  // per body
+    uint32_t* comp_flag;
+
+    // colouring
+    uint32_t* col_cnt;   // MAX_COLOURS+1
+    uint32_t* col_list;  // N
+    uint32_t* ctr;       // counters
+};
+
+}  // namespace avbd

@@ -60,6 +60,9 @@ def lib():
         L.oracle_shape_inertia.argtypes = [C.c_uint32, vp, C.c_float, vp]
         L.oracle_colour_hash.restype = C.c_uint32
         L.oracle_colour_hash.argtypes = [C.c_uint32]
+        L.oracle_generate_pairs.argtypes = [vp]
+        L.oracle_gap_c0.restype = C.c_double
+        L.oracle_gap_c0.argtypes = [vp, C.c_uint32, C.c_uint32]
         L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
         _lib = L
     return _lib
@@ -149,6 +152,12 @@ class OracleWorld:
     def import_state(self, st):
         lib().oracle_import_state(self.h, abi.ptr(st["bodies"]), abi.ptr(st["aux"]), abi.ptr(st["pairs"]),
                                   abi.ptr(st["points"]), len(st["pairs"]), abi.ptr(st.get("joints")))
+
+    def generate_pairs(self):
+        lib().oracle_generate_pairs(self.h)
+
+    def gap_c0(self, pi, qi):
+        return lib().oracle_gap_c0(self.h, pi, qi)
 
     def colours(self):
         out = np.zeros(self.nbodies, dtype=np.int32)

@@ -1,0 +1,96 @@
+"""Host-only checks of the C ABI (no GPU needed): the library loads, every
+function include/ornis_avbd.h declares is exported, record layouts match,
+and the host-side constructors agree with the oracle's restatement of the
+reference constructors."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from ornis_gb300 import abi, scenes
+from ornis_gb300.avbd import LIB_PATH, bodies_array, body, lib
+
+import oracle_api as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names += re.findall(r"^\s*int\s+(avbd_\w+)\s*\(", txt, flags=re.M)
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib()
+    L = C.CDLL(LIB_PATH)
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_defaults():
+    assert lib().avbd_abi_version() == 1
+    p = abi.AvbdParams()
+    assert lib().avbd_default_params(C.byref(p)) == 0
+    assert abs(p.step_dt - 1 / 60) < 1e-9 and p.iterations == 10 and p.max_substeps == 4
+    assert tuple(p.gravity) == (0.0, np.float32(-9.81), 0.0)
+
+
+def test_record_sizes():
+    assert C.sizeof(abi.AvbdBody) == 136
+    assert C.sizeof(abi.AvbdPointState) == 68
+    assert abi.BODY_DTYPE.itemsize == 136
+
+
+def test_body_init_matches_oracle_constructors():
+    cases = [
+        (abi.SHAPE_BOX, [0.5, 0.25, 0.75], [1, 2, 3], 2.5),
+        (abi.SHAPE_SPHERE, [0.3], [0, 1, 0], 1.7),
+        (abi.SHAPE_CAPSULE, [0.3, 0.6], [0, 2, 0], 3.1),
+        (abi.SHAPE_BOX, [10, 1, 10], [0, -1, 0], 0.0),
+        (abi.SHAPE_HALFSPACE, [0, 2, 0], [0, 0, 0], 0.0),
+    ]
+    for shape, params, pos, mass in cases:
+        a = bodies_array([body(shape, params, pos, mass)])
+        b = O.bodies_to_array([O.body_new(shape, params, pos, mass)])
+        assert a.tobytes() == b.tobytes(), shape
+        p3 = list(params) + [0.0] * (3 - len(params))
+        if shape == abi.SHAPE_HALFSPACE:
+            m = scenes.halfspace(pos, params)
+        else:
+            m = scenes.make_bodies([shape], [p3], [pos], [mass])
+        assert m.tobytes() == a.tobytes(), shape
+
+
+def test_body_init_rejects_dynamic_halfspace():
+    b = abi.AvbdBody()
+    p = np.array([0, 1, 0], np.float32)
+    pos = np.zeros(3, np.float32)
+    assert lib().avbd_body_init(C.byref(b), abi.SHAPE_HALFSPACE, abi.ptr(p), abi.ptr(pos), 1.0) == \
+        abi.AVBD_ERR_INVALID_ARG
+
+
+def test_world_create_rejects_bad_params():
+    p = abi.default_params()
+    p.step_dt = 0.0
+    h = C.c_void_p()
+    assert lib().avbd_world_create(C.byref(p), 0, C.byref(h)) == abi.AVBD_ERR_INVALID_ARG
+
+
+def test_batched_scene_layout():
+    bodies, offs, counts = scenes.batched(64)
+    assert offs[0] == 0 and offs[-1] == len(bodies)
+    assert np.all(np.diff(offs) == counts + 5)
+    assert counts.min() >= 8 and counts.max() <= 1024
+    # every scene starts with its five static half-spaces
+    for s in range(64):
+        sc = bodies[offs[s]:offs[s + 1]]
+        assert np.all(sc["shape"][:5] == abi.SHAPE_HALFSPACE)
+        assert np.all(sc["body_type"][5:] == abi.BODY_DYNAMIC)
