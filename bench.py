@@ -1,0 +1,339 @@
+"""Benchmark of the GB300 AVBD step: body-steps/s on the batched workload.
+
+Workload (default): batched_4096 — 4096 independent scenes of log-uniform
+8..1024 bodies (boxes and spheres in a 20x20 bin), dt 1/120 s, 2 substeps,
+8 iterations, f32.  A "step" is one 1/60 s frame = 2 substeps of every
+scene.  body-steps/s = dynamic bodies x steps / seconds.
+
+  value        device time of K graph-replayed steps, state resident in HBM
+               (CUDA events on the world's stream).
+  e2e          the same steps through the C ABI with host buffers: every step
+               uploads all body records, steps, downloads all body records
+               (host wall clock around synchronised calls).
+  plain        the same scenes stepped one scene per launch sequence (one
+               world per scene), a bounded sample of scenes; the batched/plain
+               ratio is the batching speed-up.
+  roofline     the primal kernel: algorithmic bytes per launch (byte model in
+               ornis_gb300/roofline.py) / its CUDA-event time per launch,
+               against the measured HBM copy bandwidth.
+  cpu_baseline the oracle's Reference-mode step (the reference's own serial
+               algorithm restated in C++) on the host cores, a bounded sample
+               of the same scenes, one process per core.
+
+--impl reference times that CPU path alone (the reference itself is Rust and
+cannot be built here).  Under torchrun (N > 1) scenes are sharded across
+ranks (scene s -> rank s mod N), no data-path collective; rank 0 prints.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from ornis_gb300 import abi, scenes  # noqa: E402
+
+METRIC = "AVBD body-steps/s: batched vs one-scene launches @<=1e-5 err; adjoint steps/s"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.rows = []
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(n_gpus):
+    """torch.distributed only for the N>1 barrier and max-over-ranks timing."""
+    if n_gpus <= 1 or int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dist, rank, dist.get_world_size(), local
+
+
+def shard(bodies, offs, rank, world):
+    """Scenes s with s % world == rank, repacked with their own offsets."""
+    parts, new_offs = [], [0]
+    for s in range(rank, len(offs) - 1, world):
+        sc = bodies[offs[s]:offs[s + 1]]
+        parts.append(sc)
+        new_offs.append(new_offs[-1] + len(sc))
+    return np.concatenate(parts), np.asarray(new_offs, dtype=np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's Reference-mode step, one process per core.
+# ---------------------------------------------------------------------------
+def _cpu_scene_worker(args):
+    """Settle one scene (untimed), then time `steps` steps of the oracle."""
+    bodies, params_tuple, nsub, preroll, steps = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+
+    p = abi.default_params(step_dt=params_tuple[0], iterations=params_tuple[1])
+    w = O.OracleWorld(p, mode=O.REFERENCE)
+    w.add_bodies(bodies)
+    w.step_fixed(nsub * preroll)
+    t0 = time.perf_counter()
+    w.step_fixed(nsub * steps)
+    return time.perf_counter() - t0, scenes.dynamic_count(bodies) * steps
+
+
+def cpu_baseline(bodies, offs, params, nsub, preroll, steps=4, per_core=3):
+    """Body-steps/s of the oracle's Reference step on a seeded sample of scenes.
+
+    Each sampled scene settles for `preroll` steps (untimed, like the GPU run),
+    then `steps` steps are timed; scenes run one process per core and the rate
+    is sampled body-steps over the summed per-scene seconds divided by cores.
+    """
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    S = len(offs) - 1
+    rng = np.random.default_rng(12345)
+    chosen = [int(s) for s in rng.permutation(S)[: min(S, cores * per_core)]]
+    jobs = [(bodies[offs[s]:offs[s + 1]], (params.step_dt, params.iterations), nsub, preroll, steps) for s in chosen]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_scene_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    busy = sum(r[0] for r in res)
+    body_steps = sum(r[1] for r in res)
+    mean_n = float(np.mean([offs[s + 1] - offs[s] for s in chosen]))
+    return {
+        "value": body_steps / (busy / cores),
+        "unit": "body-steps/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{len(chosen)} of {S} scenes (seeded random, mean {mean_n:.0f} bodies incl. 5 planes), "
+                  f"each settled {preroll} steps untimed then {steps} steps x {nsub} substeps timed; "
+                  f"one process per core; rate = body-steps / (summed scene seconds / cores); wall {wall:.1f} s",
+    }
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    d = dist_init(args.gpus)
+    if d is not None and d[1] != 0:
+        return 0
+    bodies, offs, counts = scenes.batched(args.scenes)
+    params, nsub = scenes.params_for("batched_4096")
+    cb = cpu_baseline(bodies, offs, params, nsub, preroll=args.preroll, steps=max(1, args.steps // 5),
+                      per_core=args.cpu_per_core)
+    v = cb["value"]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
+            "config": {"workload": "batched_4096", "scenes": args.scenes, "dt": 1 / 120, "substeps": nsub,
+                       "iterations": params.iterations},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    from ornis_gb300 import roofline
+    from ornis_gb300.avbd import AvbdWorld
+
+    d = dist_init(args.gpus)
+    rank, world = (d[1], d[2]) if d else (0, 1)
+    device = d[3] if d else 0
+    bodies_all, offs_all, counts = scenes.batched(args.scenes)
+    params, nsub = scenes.params_for("batched_4096")
+    bodies, offs = shard(bodies_all, offs_all, rank, world) if world > 1 else (bodies_all, offs_all)
+    ndyn = scenes.dynamic_count(bodies)
+    w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
+    if args.lanes:
+        w.set_tuning(args.lanes, args.block)
+    # settle: bodies fall into their bins before the measured steps
+    for _ in range(args.preroll):
+        w.step_graph(nsub)
+    for _ in range(args.warmup):
+        w.step_graph(nsub)
+    w.sync()
+    # ---- timed region: K steps, device time -------------------------------
+    if d:
+        d[0].barrier()
+    with Clocks(device) as clk:
+        ms = w.step_timed(nsub * args.steps, use_graph=True)
+    if d:
+        import torch
+
+        t = torch.tensor([ms], device=f"cuda:{device}")
+        d[0].all_reduce(t, op=d[0].ReduceOp.MAX)
+        ms = float(t.item())
+        nd = torch.tensor([float(ndyn)], device=f"cuda:{device}")
+        d[0].all_reduce(nd)
+        ndyn_total = int(nd.item())
+    else:
+        ndyn_total = ndyn
+    value = ndyn_total * args.steps / (ms / 1e3)
+    nodes = w.graph_nodes()
+    # ---- e2e through the C ABI with host buffers ---------------------------
+    host = w.bodies()
+    h2d = d2h = host.nbytes
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        w.set_bodies(host)
+        w.step_graph(nsub)
+        host = w.bodies()
+    e2e_s = time.perf_counter() - t0
+    e2e = ndyn * args.e2e_steps / e2e_s
+    if d:
+        import torch
+
+        t = torch.tensor([e2e_s], device=f"cuda:{device}")
+        d[0].all_reduce(t, op=d[0].ReduceOp.MAX)
+        e2e = ndyn_total * args.e2e_steps / float(t.item())
+    # ---- per-phase profile: roofline of the primal kernel --------------------
+    phases, info = w.profile_substep()
+    roof = roofline.primal_roofline(phases, info, hbm_peak())
+    if rank != 0:
+        return 0
+    # ---- plain: one scene per launch sequence, bounded sample ----------------
+    plain = None
+    if args.plain_scenes > 0:
+        plain = plain_rate(bodies_all, offs_all, params, nsub, args)
+    cb = None
+    if args.cpu_per_core > 0 and world == 1:
+        cb = cpu_baseline(bodies_all, offs_all, params, nsub, preroll=args.preroll, steps=4,
+                          per_core=args.cpu_per_core)
+    c = w.counters()
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, no dataset)",
+        "config": {"workload": "batched_4096", "scenes": args.scenes, "dynamic_bodies": ndyn_total,
+                   "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations, "preroll_steps": args.preroll,
+                   "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
+                   "graph": True, "primal_lanes": args.lanes or 1},
+        "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "steps": args.e2e_steps},
+        "gpu_launches": int(nodes * nsub * args.steps),
+        "roofline": roof,
+        "cpu_baseline": cb,
+        "clocks": clk.summary(),
+        "plain_one_scene": plain,
+        "batched_over_plain": (value / plain["value"]) if plain else None,
+        "phases_ms_per_substep": phases,
+        "counters": {"pairs": c.pairs, "points": c.points, "colours": c.colours, "sleeping": c.sleeping,
+                     "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits, "ccd_left": c.timeouts},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def plain_rate(bodies, offs, params, nsub, args):
+    """Body-steps/s stepping scenes one world (one launch sequence) at a time."""
+    from ornis_gb300.avbd import AvbdWorld
+
+    S = len(offs) - 1
+    rng = np.random.default_rng(777)
+    pick = rng.choice(S, size=min(args.plain_scenes, S), replace=False)
+    worlds = [AvbdWorld(params, bodies=bodies[offs[s]:offs[s + 1]]) for s in pick]
+    for wd in worlds:
+        for _ in range(args.preroll):
+            wd.step_graph(nsub)
+    tot_ms = 0.0
+    body_steps = 0
+    for wd, s in zip(worlds, pick):
+        tot_ms += wd.step_timed(nsub * args.plain_steps, use_graph=False)
+        body_steps += scenes.dynamic_count(bodies[offs[s]:offs[s + 1]]) * args.plain_steps
+    for wd in worlds:
+        wd.close()
+    return {"value": body_steps / (tot_ms / 1e3), "unit": "body-steps/s", "scenes_sampled": int(len(pick)),
+            "steps": args.plain_steps, "how": "one world per scene, plain launches, scenes stepped one after another"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--preroll", type=int, default=60)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--plain-scenes", type=int, default=32)
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--cpu-per-core", type=int, default=3)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--block", type=int, default=128)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -266,6 +266,24 @@ int avbd_set_tuning(AvbdWorld* world, int primal_lanes, int primal_block);
 
 int avbd_abi_version(void);
 
+/* ---- measurement (no reference counterpart: the reference publishes no
+ * timing for this path) ---------------------------------------------------- */
+
+/* Advance `substeps` fixed substeps (CUDA-graph replay when use_graph != 0)
+ * and return their device time in *ms, from CUDA events recorded on the
+ * world's stream before the first and after the last substep. */
+int avbd_world_step_timed(AvbdWorld* world, int32_t substeps, int32_t use_graph, float* ms);
+
+/* Advance one substep through plain launches with a CUDA event between the
+ * phases.  ms[9]: wake+torque, broadphase, CCD, discovery, post-discovery,
+ * colouring, primal (all colours and iterations), dual (all iterations),
+ * BDF1+sleep.  info[5]: colours, primal launches, bodies swept per
+ * iteration, pairs, points. */
+int avbd_world_profile_substep(AvbdWorld* world, float* ms, uint32_t* info);
+
+/* Kernel nodes in one captured substep graph (0 before the first capture). */
+int avbd_world_graph_nodes(AvbdWorld* world, uint32_t* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,9 @@ def lib():
             "avbd_body_init": [C.POINTER(abi.AvbdBody), u32, vp, vp, C.c_float],
             "avbd_set_tuning": [vp, C.c_int, C.c_int],
             "avbd_abi_version": [],
+            "avbd_world_step_timed": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)],
+            "avbd_world_profile_substep": [vp, vp, vp],
+            "avbd_world_graph_nodes": [vp, C.POINTER(u32)],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -161,6 +164,26 @@ class AvbdWorld:
     def set_bodies(self, arr, first=0):
         arr = np.ascontiguousarray(arr, dtype=abi.BODY_DTYPE)
         _check(lib().avbd_world_set_bodies(self.h, first, len(arr), abi.ptr(arr)), "set_bodies")
+
+    def step_timed(self, substeps, use_graph=True):
+        """Device milliseconds of `substeps` substeps (CUDA events on the world's stream)."""
+        ms = C.c_float()
+        _check(lib().avbd_world_step_timed(self.h, int(substeps), int(use_graph), C.byref(ms)), "step_timed")
+        return ms.value
+
+    def profile_substep(self):
+        ms = np.zeros(9, np.float32)
+        info = np.zeros(5, np.uint32)
+        _check(lib().avbd_world_profile_substep(self.h, abi.ptr(ms), abi.ptr(info)), "profile_substep")
+        names = ["wake_torque", "broadphase", "ccd", "discovery", "post_discovery", "colouring", "primal", "dual",
+                 "finish"]
+        return dict(zip(names, map(float, ms))), dict(zip(["colours", "primal_launches", "swept", "pairs",
+                                                           "points"], map(int, info)))
+
+    def graph_nodes(self):
+        n = C.c_uint32()
+        _check(lib().avbd_world_graph_nodes(self.h, C.byref(n)), "graph_nodes")
+        return n.value
 
     def counters(self):
         c = abi.AvbdCounters()

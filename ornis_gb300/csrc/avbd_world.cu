@@ -133,6 +133,7 @@ struct AvbdWorld {
     // graphs: one captured substep per pair-buffer parity
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int graph_cols = 0;
+    size_t graph_nodes = 0;  // kernel nodes in one captured substep
     uint64_t steps = 0;
 };
 
@@ -941,6 +942,9 @@ static int capture(AvbdWorld* W) {
         enqueue_back(W, W->graph_cols);
         W->w.max_cols = MAX_COLOURS;
         CK(cudaStreamEndCapture(W->st, &g));
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        W->graph_nodes = nn;
         cudaError_t e = cudaGraphInstantiate(&W->gexec[W->cur], g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
@@ -1124,5 +1128,103 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
 }
 
 int avbd_abi_version(void) { return AVBD_ABI_VERSION; }
+
+// Device time of `substeps` substeps, bracketed by CUDA events on the world's
+// stream (graph replay when use_graph != 0).
+int avbd_world_step_timed(AvbdWorld* W, int32_t substeps, int32_t use_graph, float* ms) {
+    if (!W || !ms || substeps < 0) return AVBD_ERR_INVALID_ARG;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaStreamSynchronize(W->st));
+    CK(cudaEventRecord(e0, W->st));
+    rc = use_graph ? avbd_world_step_graph(W, substeps) : avbd_world_step_fixed(W, substeps);
+    CK(cudaEventRecord(e1, W->st));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+// One substep through plain launches with an event between phases:
+// ms[0] wake+torque, [1] broadphase, [2] CCD, [3] discovery, [4] wake+CSR+
+// targets+decay, [5] colouring, [6] primal (all colours, all iterations),
+// [7] dual (all iterations), [8] BDF1+sleep.  info[0] = colours,
+// info[1] = primal launches, info[2] = awake dynamic bodies swept,
+// info[3] = pairs, info[4] = points.
+int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
+    if (!W || !ms || !info) return AVBD_ERR_INVALID_ARG;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    cudaEvent_t ev[10];
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    cudaStream_t st = W->st;
+    CK(cudaStreamSynchronize(st));
+    W->cur = 1 - W->cur;
+    set_pair_ptrs(W);
+    const DW& w = W->w;
+    CK(cudaEventRecord(ev[0], st));
+    launch_begin_substep(w, st);
+    launch_wake_joint_motion(w, st);
+    launch_torque(w, st);
+    CK(cudaEventRecord(ev[1], st));
+    launch_broadphase(w, W->plan, st);
+    CK(cudaEventRecord(ev[2], st));
+    launch_ccd(w, st);
+    CK(cudaEventRecord(ev[3], st));
+    launch_discovery(w, W->scan_tmp, st);
+    CK(cudaEventRecord(ev[4], st));
+    launch_post_discovery(w, W->scan_tmp, st);
+    CK(cudaEventRecord(ev[5], st));
+    launch_colouring(w, W->scan_tmp, st);
+    CK(cudaEventRecord(ev[6], st));
+    rc = read_ctr(W);
+    if (rc) return rc;
+    for (int i = 0; i < 6; i++) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+    if (W->h_ctr[C_ERR]) return AVBD_ERR_CAPACITY;
+    int ncol = (int)W->h_ctr[C_NCOL];
+    uint32_t col_total = 0;
+    CK(cudaMemcpy(&col_total, w.col_cnt + MAX_COLOURS, 4, cudaMemcpyDeviceToHost));
+    float prim = 0.0f, dual = 0.0f;
+    for (int it = 0; it < w.iterations; it++) {
+        float t;
+        CK(cudaEventRecord(ev[6], st));
+        for (int c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, c, (uint32_t)w.N, st);
+        CK(cudaEventRecord(ev[7], st));
+        launch_dual(w, st);
+        CK(cudaEventRecord(ev[8], st));
+        CK(cudaEventSynchronize(ev[8]));
+        CK(cudaEventElapsedTime(&t, ev[6], ev[7]));
+        prim += t;
+        CK(cudaEventElapsedTime(&t, ev[7], ev[8]));
+        dual += t;
+    }
+    CK(cudaEventRecord(ev[8], st));
+    launch_finish_substep(w, st);
+    CK(cudaEventRecord(ev[9], st));
+    CK(cudaEventSynchronize(ev[9]));
+    ms[6] = prim;
+    ms[7] = dual;
+    CK(cudaEventElapsedTime(&ms[8], ev[8], ev[9]));
+    rc = read_ctr(W);
+    if (rc) return rc;
+    accumulate(W);
+    info[0] = (uint32_t)ncol;
+    info[1] = (uint32_t)(ncol * w.iterations);
+    info[2] = col_total;
+    info[3] = W->h_ctr[C_PAIRS];
+    info[4] = W->h_ctr[C_POINTS];
+    for (auto& e : ev) cudaEventDestroy(e);
+    return AVBD_OK;
+}
+
+int avbd_world_graph_nodes(AvbdWorld* W, uint32_t* n) {
+    if (!W || !n) return AVBD_ERR_INVALID_ARG;
+    *n = (uint32_t)W->graph_nodes;
+    return AVBD_OK;
+}
 
 }  // extern "C"

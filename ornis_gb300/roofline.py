@@ -1,0 +1,62 @@
+"""Algorithmic byte model of the AVBD iterations (v1) and the primal roofline.
+
+None of the AVBD kernels is a dense contraction, so the bound is HBM
+bandwidth.  Algorithmic bytes are what the math must move at least once per
+iteration, independent of how the kernels stage it:
+
+  primal, per iteration
+    swept body   128 B  (x,q 28 + x0,q0 28 + y,q~ 28 + inv_mass + inertia 16
+                         read; x,q 28 written)
+    contact point 48 B  (ra, rb, lambda, penalty read)
+    pair header   32 B  (normal, gap, mu, a, b)
+  dual, per iteration
+    contact point 76 B  (48 B read + lambda, penalty, stuck 28 B written)
+    body          56 B  per body referenced (x,q,x0,q0 of both sides, counted
+                        once per swept body)
+    pair header   32 B
+
+A launch of the primal kernel covers one colour; the roofline uses the sum
+over all colours of one iteration (the same ratio as per launch).
+"""
+
+PRIMAL_BODY_B = 128
+PRIMAL_POINT_B = 48
+PAIR_HEADER_B = 32
+DUAL_POINT_B = 76
+DUAL_BODY_B = 56
+
+
+def primal_bytes_per_iteration(swept, points, pairs):
+    return PRIMAL_BODY_B * swept + PRIMAL_POINT_B * points + PAIR_HEADER_B * pairs
+
+
+def dual_bytes_per_iteration(swept, points, pairs):
+    return DUAL_POINT_B * points + DUAL_BODY_B * swept + PAIR_HEADER_B * pairs
+
+
+def primal_roofline(phases_ms, info, peak):
+    """Roofline entry for the primal kernel from one profiled substep."""
+    peak_gbs, source = peak
+    iters = max(1, info["primal_launches"] // max(1, info["colours"]))
+    per_iter_ms = phases_ms["primal"] / iters
+    per_launch_ms = phases_ms["primal"] / max(1, info["primal_launches"])
+    b = primal_bytes_per_iteration(info["swept"], info["points"], info["pairs"])
+    achieved = b / (per_iter_ms / 1e3) / 1e9 if per_iter_ms > 0 else 0.0
+    dual_b = dual_bytes_per_iteration(info["swept"], info["points"], info["pairs"])
+    dual_ms = phases_ms["dual"] / iters
+    return {
+        "bound": "hbm",
+        "kernel": "k_primal_thread (one launch per colour)",
+        "achieved": achieved,
+        "peak": peak_gbs,
+        "unit": "GB/s",
+        "frac": achieved / peak_gbs,
+        "peak_source": f"{source} (MEASURED_PEAKS.json hbm_gbs)" if source == "measured" else "fallback 6.8 TB/s",
+        "traffic": None,
+        "bytes_per_launch": b / max(1, info["colours"]),
+        "launch_ms": per_launch_ms,
+        "model": "v1: 128 B/swept body + 48 B/point + 32 B/pair per iteration",
+        "dual": {"achieved": dual_b / (dual_ms / 1e3) / 1e9 if dual_ms > 0 else 0.0,
+                 "frac": (dual_b / (dual_ms / 1e3) / 1e9) / peak_gbs if dual_ms > 0 else 0.0,
+                 "launch_ms": dual_ms},
+    }
