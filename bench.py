@@ -212,14 +212,28 @@ def run_ours(args):
     bodies, offs = shard(bodies_all, offs_all, rank, world) if world > 1 else (bodies_all, offs_all)
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
-    if args.lanes:
-        w.set_tuning(args.lanes, args.block)
+    w.set_precision(not args.exact)
     # settle: bodies fall into their bins before the measured steps
     for _ in range(args.preroll):
         w.step_graph(nsub)
+    tuned = None
+    if args.lanes:
+        w.set_tuning(args.lanes, args.block)
+    elif args.autotune:
+        from ornis_gb300.tune import autotune
+
+        tuned = autotune(w, substeps_per_trial=nsub)
     for _ in range(args.warmup):
         w.step_graph(nsub)
     w.sync()
+    if args.profile_region:
+        # only the kernels of these steps are collected by `ncu --profile-from-start off`
+        from ornis_gb300.avbd import lib as _lib
+
+        _lib().avbd_profiler(1)
+        w.step_graph(nsub * args.profile_region)
+        w.sync()
+        _lib().avbd_profiler(0)
     # ---- timed region: K steps, device time -------------------------------
     if d:
         d[0].barrier()
@@ -275,7 +289,11 @@ def run_ours(args):
         "config": {"workload": "batched_4096", "scenes": args.scenes, "dynamic_bodies": ndyn_total,
                    "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations, "preroll_steps": args.preroll,
                    "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
-                   "graph": True, "primal_lanes": args.lanes or 1},
+                   "graph": True, "precision": "exact" if args.exact else "fast",
+                   "primal_launch": {"lanes": tuned[0][0], "block": tuned[0][1], "min_blocks_per_sm": tuned[0][2],
+                                     "by_work": tuned[0][3],
+                                     "trials_ms": [[list(c), round(m, 3)] for c, m in tuned[1]]}
+                   if tuned else {"lanes": args.lanes or 1, "block": args.block}},
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "steps": args.e2e_steps},
         "gpu_launches": int(nodes * nsub * args.steps),
@@ -285,7 +303,7 @@ def run_ours(args):
         "plain_one_scene": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "phases_ms_per_substep": phases,
-        "counters": {"pairs": c.pairs, "points": c.points, "colours": c.colours, "sleeping": c.sleeping,
+        "counters": {"candidates": c.candidates, "pairs": c.pairs, "points": c.points, "colours": c.colours, "sleeping": c.sleeping,
                      "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits, "ccd_left": c.timeouts},
     }
     print(json.dumps(line))
@@ -328,6 +346,10 @@ def main():
     ap.add_argument("--cpu-per-core", type=int, default=3)
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--exact", action="store_true", help="exact build of the iteration kernels")
+    ap.add_argument("--profile-region", type=int, default=0,
+                    help="steps bracketed by cudaProfilerStart/Stop before the timed region")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -264,6 +264,25 @@ int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const flo
  * sweeps on one CPU thread); picked by the autotuner in ornis_gb300/tune.py. */
 int avbd_set_tuning(AvbdWorld* world, int primal_lanes, int primal_block);
 
+/* Arithmetic of the iteration kernels: 0 (default) = exact build, the same
+ * f32 operation order as the reference (no contraction, IEEE divide and
+ * square root); 1 = fast build (contracted multiply-adds, approximate divide
+ * and square root), within the 1e-5 pose tolerance.  Pair sets, contact IDs
+ * and colours are computed exactly in both. */
+int avbd_set_precision(AvbdWorld* world, int fast);
+
+/* Register budget of the one-thread-per-body primal: built for 4, 6 or 8
+ * resident 128-thread blocks per SM.  Picked by the autotuner. */
+int avbd_set_occupancy(AvbdWorld* world, int min_blocks);
+
+/* Start (on != 0) or stop profiler collection (cudaProfilerStart/Stop). */
+int avbd_profiler(int on);
+
+/* Order of the bodies inside each colour's launch: 0 = ascending handle,
+ * 1 = by incident-pair count (less warp divergence).  Results do not depend
+ * on it: bodies of one colour are independent. */
+int avbd_set_work_order(AvbdWorld* world, int by_work);
+
 int avbd_abi_version(void);
 
 /* ---- measurement (no reference counterpart: the reference publishes no

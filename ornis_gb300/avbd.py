@@ -58,6 +58,10 @@ def lib():
             "avbd_world_get_colours": [vp, vp, u32],
             "avbd_body_init": [C.POINTER(abi.AvbdBody), u32, vp, vp, C.c_float],
             "avbd_set_tuning": [vp, C.c_int, C.c_int],
+            "avbd_set_precision": [vp, C.c_int],
+            "avbd_set_occupancy": [vp, C.c_int],
+            "avbd_profiler": [C.c_int],
+            "avbd_set_work_order": [vp, C.c_int],
             "avbd_abi_version": [],
             "avbd_world_step_timed": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)],
             "avbd_world_profile_substep": [vp, vp, vp],
@@ -189,6 +193,15 @@ class AvbdWorld:
         c = abi.AvbdCounters()
         _check(lib().avbd_world_get_counters(self.h, C.byref(c)), "get_counters")
         return c
+
+    def set_precision(self, fast):
+        _check(lib().avbd_set_precision(self.h, int(bool(fast))), "set_precision")
+
+    def set_work_order(self, by_work):
+        _check(lib().avbd_set_work_order(self.h, int(bool(by_work))), "set_work_order")
+
+    def set_occupancy(self, min_blocks):
+        _check(lib().avbd_set_occupancy(self.h, int(min_blocks)), "set_occupancy")
 
     def set_tuning(self, lanes, block):
         _check(lib().avbd_set_tuning(self.h, int(lanes), int(block)), "set_tuning")

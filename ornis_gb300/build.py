@@ -17,12 +17,16 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libornis_avbd.so")
 
+# (source, object, extra flags).  The iteration kernels are built twice:
+# exact (the default flags) and fast (contracted FMAs, approximate div/sqrt).
 SOURCES = [
-    "avbd_util.cu",
-    "avbd_phase_pre.cu",
-    "avbd_phase_disc.cu",
-    "avbd_phase_solve.cu",
-    "avbd_world.cu",
+    ("avbd_util.cu", "avbd_util.o", []),
+    ("avbd_phase_pre.cu", "avbd_phase_pre.o", []),
+    ("avbd_phase_disc.cu", "avbd_phase_disc.o", []),
+    ("avbd_phase_solve.cu", "avbd_phase_solve.o", []),
+    ("avbd_phase_solve.cu", "avbd_phase_solve_fast.o",
+     ["-DAVBD_SOLVE_FAST", "-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
+    ("avbd_world.cu", "avbd_world.o", []),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--extended-lambda", "-Xcompiler", "-fPIC",
@@ -54,13 +58,14 @@ def build(verbose=False, force=False):
     cc = nvcc()
     jobs = []
     objs = []
-    for src in SOURCES:
+    for src, obj, extra in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, obj)
         objs.append(o)
         if not force and _newer(o, [s] + headers):
             continue
-        jobs.append([cc] + ARCH + FLAGS + ["-c", s, "-o", o])
+        flags = [f for f in FLAGS if not (extra and f == "-fmad=false")]
+        jobs.append([cc] + ARCH + flags + extra + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -7,6 +7,12 @@
 namespace avbd {
 
 static inline unsigned nblk(size_t n, int b) { return (unsigned)((n + (size_t)b - 1) / (size_t)b); }
+// Grid for kernels whose trip count lives on the device (grid-stride loops):
+// enough resident blocks to fill the 152 SMs, never more than the capacity needs.
+static inline unsigned gsz(size_t cap, int b) {
+    unsigned g = nblk(cap, b);
+    return g < 152u * 16u ? g : 152u * 16u;
+}
 
 static __device__ __forceinline__ bool is_dynamic(const DW& w, uint32_t h) {
     return info_type(w.info[h]) == AVBD_BODY_DYNAMIC;
@@ -55,6 +61,24 @@ static __device__ __forceinline__ bool aborted_solve(const DW& w) {
 }
 static __device__ __forceinline__ uint32_t n_cand(const DW& w) { return min(w.ctr[C_CAND], w.cand_cap); }
 static __device__ __forceinline__ uint32_t n_pairs(const DW& w) { return w.offA[w.N]; }
+
+// Index of the previous-generation pair (a, b), or -1.  The old B-side list
+// of b (rebuilt every substep, untouched until this substep's incidence
+// rebuild) holds its pairs in ascending pair index, i.e. ascending a, so a
+// binary search finds (a, b) whatever the size of a's own A-side segment
+// (a half-space is the A side of every pair in its scene).
+static __device__ __forceinline__ int32_t find_old_pair(const DW& w, uint32_t a, uint32_t b) {
+    uint32_t lo = w.offB[b], hi = w.offB[b + 1];
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t p = w.listB[mid];
+        uint32_t v = w.o_ab[p].x;
+        if (v == a) return (int32_t)p;
+        if (v < a) lo = mid + 1;
+        else hi = mid;
+    }
+    return -1;
+}
 
 // sleep.rs:30-40 (Ball, Revolute)
 static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j) {

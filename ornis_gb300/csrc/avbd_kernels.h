@@ -13,7 +13,10 @@ namespace avbd {
 struct Tune {
     int primal_lanes = 1;        // lanes cooperating on one body in the primal (1, 4, 8, 16, 32)
     int primal_block = 128;      // threads per block of the primal kernel
+    int primal_minb = 4;         // resident blocks per SM the thread-per-body primal is built for
     int small_scene_max = 2048;  // scenes up to this many bodies use the one-CTA broadphase
+    int fast = 0;                // 1: the fast build of the iteration kernels
+    int sort_work = 0;           // 1: order each colour's bodies by incident-pair count
 };
 
 // exclusive scan of n uint32 values in place (out may alias in); tmp needs
@@ -25,6 +28,10 @@ void scan_exclusive(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, 
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, size_t n,
                       uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 size_t radix_hist_words(size_t n);
+// one stable 8-bit pass (digit = (key >> shift) & 255); hist keeps the scanned
+// digit-major table (digit d of tile t at hist[d * ntiles + t]); returns ntiles
+int radix_pass(const uint32_t* keys, const uint32_t* vals, uint32_t* okeys, uint32_t* ovals, size_t n, int shift,
+               uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st);
 
 // per substep phases
 void launch_begin_substep(const DW& w, cudaStream_t st);
@@ -40,12 +47,38 @@ void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st)
 void launch_ccd(const DW& w, cudaStream_t st);
 void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
 void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
-void launch_colouring(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
-void launch_iteration(const DW& w, const Tune& tune, int ncolours_hint, cudaStream_t st);
-void launch_finish_substep(const DW& w, cudaStream_t st);
+void launch_colouring(const DW& w, const Tune& tune, uint32_t* scan_tmp, cudaStream_t st);
 
 void launch_wake_apply(const DW& w, cudaStream_t st);
-void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st);
-void launch_dual(const DW& w, cudaStream_t st);
+// The iteration and finish kernels exist in two builds: `exact` reproduces
+// the CPU oracle bit for bit (thread-per-body primal), `fast` trades the last
+// bits for fewer instructions (contracted FMAs, approximate div/sqrt).
+#define AVBD_SOLVE_DECLS                                                                                    \
+    void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st);                   \
+    void launch_finish_substep(const DW& w, cudaStream_t st);                                             \
+    void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st); \
+    void launch_dual(const DW& w, cudaStream_t st);
+namespace exact {
+AVBD_SOLVE_DECLS
+}
+namespace fast {
+AVBD_SOLVE_DECLS
+}
+inline void launch_iteration(const DW& w, const Tune& t, int ncol, cudaStream_t st) {
+    if (t.fast) fast::launch_iteration(w, t, ncol, st);
+    else exact::launch_iteration(w, t, ncol, st);
+}
+inline void launch_finish_substep(const DW& w, const Tune& t, cudaStream_t st) {
+    if (t.fast) fast::launch_finish_substep(w, st);
+    else exact::launch_finish_substep(w, st);
+}
+inline void launch_primal_colour(const DW& w, const Tune& t, int c, uint32_t maxb, cudaStream_t st) {
+    if (t.fast) fast::launch_primal_colour(w, t, c, maxb, st);
+    else exact::launch_primal_colour(w, t, c, maxb, st);
+}
+inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
+    if (t.fast) fast::launch_dual(w, st);
+    else exact::launch_dual(w, st);
+}
 
 }  // namespace avbd

@@ -19,30 +19,26 @@ struct Disc {
     Dist d;
 };
 
-// discover_pair (rows.rs:432-555): prefilter, signed gap, frame, creation gate.
-static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b) {
-    Disc r;
+// discover_pair (rows.rs:432-555) in three parts: the prefilter and the
+// previous-generation lookup; the signed gap with witnesses; the contact
+// frame and the creation gate.
+static __device__ __forceinline__ bool discover_pre(const DW& w, uint32_t a, uint32_t b, Disc& r) {
     r.keep = false;
     r.exists = false;
     r.separated = false;
     r.old = -1;
-    if (!pair_allowed(w, a, b)) return r;
-    bool trig = info_trigger(w.info[a]) || info_trigger(w.info[b]);
-    if (!trig && jointed(w, a, b)) return r;
+    if (!pair_allowed(w, a, b)) return false;
+    if (info_trigger(w.info[a]) || info_trigger(w.info[b])) return false;  // triggers form no contact pair here
+    if (jointed(w, a, b)) return false;
     r.ra = w.shp[a].w;
     r.rb = w.shp[b].w;
-    Shape sa = shape_of(w, a), sb = shape_of(w, b);
-    if (len(sa.pos - sb.pos) > r.ra + r.rb + GEN_MARGIN) return r;
-    float sat = 0.0f;
-    r.d = shape_distance(sa, sb, &sat);
-    r.sgn = (sa.kind == AVBD_SHAPE_BOX && sb.kind == AVBD_SHAPE_BOX) ? sat : r.d.dist;
-    if (trig) return r;  // trigger overlaps form no contact pair
-    for (uint32_t p = w.o_offA[a]; p < w.o_offA[a + 1]; p++)
-        if (w.o_ab[p].y == b) {
-            r.old = (int32_t)p;
-            break;
-        }
+    if (len(ld3(w.pos[a]) - ld3(w.pos[b])) > r.ra + r.rb + GEN_MARGIN) return false;
+    r.old = find_old_pair(w, a, b);
     r.exists = r.old >= 0;
+    return true;
+}
+static __device__ __forceinline__ void discover_post(const DW& w, uint32_t a, uint32_t b, const Shape& sa,
+                                                     const Shape& sb, Disc& r) {
     V3 normal;
     if (sa.kind == AVBD_SHAPE_HALFSPACE) normal = -qrot(sa.rot, sa.p);
     else if (sb.kind == AVBD_SHAPE_HALFSPACE) normal = qrot(sb.rot, sb.p);
@@ -61,34 +57,73 @@ static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b
     r.normal = normal;
     float approach = fmaxf(dot(ld3(w.vel[b]) - ld3(w.vel[a]), normal), 0.0f);
     float reach = GEN_MARGIN + approach * w.dt;
-    if (r.sgn > reach && !r.exists) return r;
+    if (r.sgn > reach && !r.exists) return;
     r.separated = r.sgn > reach;
     r.keep = true;
+}
+static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b, bool need_witness) {
+    Disc r;
+    if (!discover_pre(w, a, b, r)) return r;
+    if (r.exists && !need_witness) {
+        // live pairs within the prefilter always survive (empty shells are
+        // kept, rows.rs:555-564): the filter pass needs no distance for them
+        r.keep = true;
+        return r;
+    }
+    Shape sa = shape_of(w, a), sb = shape_of(w, b);
+    bool boxes = sa.kind == AVBD_SHAPE_BOX && sb.kind == AVBD_SHAPE_BOX;
+    if (boxes && !r.exists && !need_witness) {
+        // The signed gap of a box pair is the SAT gap (rows.rs:498-510) and the
+        // creation reach is at most GEN_MARGIN + |v_b - v_a| dt: a new pair
+        // beyond that is rejected without the witness features.
+        V3 nsat;
+        float gap = separating_axis(sa.pos, sa.rot, sa.p, sb.pos, sb.rot, sb.p, nsat);
+        float bound = GEN_MARGIN + len(ld3(w.vel[b]) - ld3(w.vel[a])) * w.dt * 1.00001f + 1e-6f;
+        if (gap > bound) return r;
+    }
+    float sat = 0.0f;
+    r.d = shape_distance(sa, sb, &sat);
+    r.sgn = boxes ? sat : r.d.dist;
+    discover_post(w, a, b, sa, sb, r);
     return r;
 }
 
-__global__ void k_disc_filter(DW w) {
-    if (aborted(w)) return;
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cand(w)) return;
+static __device__ __forceinline__ void k_disc_filter_one(const DW& w, uint32_t c) {
     uint2 ab = w.cand[c];
-    Disc d = discover(w, ab.x, ab.y);
+    Disc d = discover(w, ab.x, ab.y, false);
     w.keep[c] = d.keep;
     if (d.keep) atomicAdd(&w.cnt[ab.x], 1u);
 }
-__global__ void k_place(DW w) {
+__global__ void k_disc_filter(DW w) {
     if (aborted(w)) return;
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cand(w) || !w.keep[c]) return;
+    const uint32_t n = n_cand(w);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        k_disc_filter_one(w, c);
+}
+
+static __device__ __forceinline__ void k_place_one(const DW& w, uint32_t c) {
+    if (!w.keep[c]) return;
     uint32_t a = w.cand[c].x;
     w.slot_c[w.offA[a] + atomicAdd(&w.cur[a], 1u)] = c;
 }
-// each body's A-side slots in ascending b: pairs end up in (a, b) order
+__global__ void k_place(DW w) {
+    if (aborted(w)) return;
+    const uint32_t n = n_cand(w);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        k_place_one(w, c);
+}
+
+// Each dynamic body's A-side slots in ascending b, so a swept body visits its
+// pairs in the reference's order.  The segments of static bodies
+// (half-spaces, floors: often long) are never read in sequence and are left
+// as placed.
 __global__ void k_sort_slots(DW w) {
     if (aborted(w)) return;
     uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= (uint32_t)w.N) return;
+    if (a == 0) w.ctr[C_PAIRS] = w.offA[w.N];
     uint32_t s0 = w.offA[a], s1 = w.offA[a + 1];
+    if (!is_dynamic(w, a)) return;
     for (uint32_t i = s0 + 1; i < s1; i++) {
         uint32_t c = w.slot_c[i];
         uint32_t bk = w.cand[c].y;
@@ -99,19 +134,60 @@ __global__ void k_sort_slots(DW w) {
         }
         w.slot_c[k] = c;
     }
-    if (a == 0) w.ctr[C_PAIRS] = w.offA[w.N];
 }
 
 // Manifold (rows.rs:571-715), wake vote (:716-744) and warm merge with the
 // previous generation (:809-931) for one surviving pair.
-__global__ void k_disc_build(DW w) {
+static __device__ __forceinline__ bool box_pair(const DW& w, uint2 ab) {
+    return info_shape(w.info[ab.x]) == AVBD_SHAPE_BOX && info_shape(w.info[ab.y]) == AVBD_SHAPE_BOX;
+}
+// Box-box witnesses are computed ahead by one warp per pair (the 15 SAT axes
+// and the 160 corner/edge tests spread over the lanes) into bd_pa / bd_pb;
+// the per-pair build below then reads them.
+static __device__ __forceinline__ void k_collect_boxes_one(const DW& w, uint32_t p) {
+    if (box_pair(w, w.cand[w.slot_c[p]])) w.boxlist[atomicAdd(&w.ctr[C_BOXPAIRS], 1u)] = p;
+}
+__global__ void k_collect_boxes(DW w) {
     if (aborted(w)) return;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        k_collect_boxes_one(w, p);
+}
+__global__ void k_box_witness(DW w) {
+    if (aborted(w)) return;
+    const uint32_t nbox = w.ctr[C_BOXPAIRS];
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = warp; i < nbox; i += nwarps) {
+        uint32_t p = w.boxlist[i];
+        uint2 ab = w.cand[w.slot_c[p]];
+        Shape sa = shape_of(w, ab.x), sb = shape_of(w, ab.y);
+        float sat;
+        Dist d = box_box_warp(sa.pos, sa.rot, sa.p, sb.pos, sb.rot, sb.p, &sat);
+        if ((threadIdx.x & 31) == 0) {
+            w.bd_pa[p] = st3(d.pa, d.dist);
+            w.bd_pb[p] = st3(d.pb, sat);
+        }
+    }
+}
+static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2 ab, const Disc& d);
+static __device__ __forceinline__ void k_disc_build_one(const DW& w, uint32_t p) {
     uint32_t c = w.slot_c[p];
     uint2 ab = w.cand[c];
+    if (box_pair(w, ab)) {
+        Disc r;
+        discover_pre(w, ab.x, ab.y, r);  // passed in the filter pass: same state, same result
+        float4 pa = w.bd_pa[p], pb = w.bd_pb[p];
+        r.d = Dist{pa.w, ld3(pa), ld3(pb)};
+        r.sgn = pb.w;
+        discover_post(w, ab.x, ab.y, shape_of(w, ab.x), shape_of(w, ab.y), r);
+        build_pair(w, p, ab, r);
+        return;
+    }
+    build_pair(w, p, ab, discover(w, ab.x, ab.y, true));
+}
+static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2 ab, const Disc& d) {
     uint32_t ia = ab.x, ib = ab.y;
-    Disc d = discover(w, ia, ib);
     V3 normal = d.normal;
     float sgn = d.sgn;
     float mu = fmaxf(fmaxf(w.mat[ia].y, w.mat[ib].y), 0.0f);
@@ -246,6 +322,13 @@ __global__ void k_disc_build(DW w) {
     }
     atomicAdd(&w.ctr[C_POINTS], (uint32_t)nf);
 }
+__global__ void k_disc_build(DW w) {
+    if (aborted(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        k_disc_build_one(w, p);
+}
+
 __global__ void k_clear_flags(DW w) {
     if (aborted(w)) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -254,15 +337,16 @@ __global__ void k_clear_flags(DW w) {
 
 void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
     unsigned g1 = nblk(w.N + 1, 256);
-    unsigned gc = nblk(w.cand_cap, 256);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cur, w.N + 1);
-    k_disc_filter<<<nblk(w.cand_cap, 128), 128, 0, st>>>(w);
+    k_disc_filter<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w);
     scan_exclusive(w.cnt, w.offA, w.N + 1, scan_tmp, st);
-    k_place<<<gc, 256, 0, st>>>(w);
+    k_place<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w);
     k_sort_slots<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_clear_flags<<<nblk(w.N, 256), 256, 0, st>>>(w);
-    k_disc_build<<<nblk(w.pair_cap, 128), 128, 0, st>>>(w);
+    k_collect_boxes<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
+    k_box_witness<<<gsz((size_t)w.pair_cap * 32, 128), 128, 0, st>>>(w);
+    k_disc_build<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
 }
 
 // ---- after discovery ----------------------------------------------------------
@@ -273,19 +357,27 @@ __global__ void k_external_wake(DW w) {
     if (h >= (uint32_t)w.N || !w.asleep[h]) return;
     if (len(ld3(w.vel[h])) > SLEEP_LIN || len(ld3(w.angvel[h])) > SLEEP_ANG) wake_body(w, h);
 }
-__global__ void k_countB(DW w) {
-    if (aborted(w)) return;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs(w)) return;
+static __device__ __forceinline__ void k_countB_one(const DW& w, uint32_t p) {
     atomicAdd(&w.cnt[w.p_ab[p].y], 1u);
 }
-__global__ void k_placeB(DW w) {
+__global__ void k_countB(DW w) {
     if (aborted(w)) return;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        k_countB_one(w, p);
+}
+
+static __device__ __forceinline__ void k_placeB_one(const DW& w, uint32_t p) {
     uint32_t b = w.p_ab[p].y;
     w.listB[w.offB[b] + atomicAdd(&w.cur[b], 1u)] = p;
 }
+__global__ void k_placeB(DW w) {
+    if (aborted(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        k_placeB_one(w, p);
+}
+
 __global__ void k_sortB(DW w) {
     if (aborted(w)) return;
     uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -329,19 +421,43 @@ __global__ void k_targets(DW w) {
         w.rot[h] = stq(qt);
     }
 }
-// Eq. 19 warmstart decay (mod.rs:1019-1040)
-__global__ void k_decay_points(DW w) {
+// Motion cache for the iterations: x - x0 and quat_diff_vec(q, q0) of every
+// body at the start of the sweep (the primal refreshes a body's entry when it
+// moves it).
+__global__ void k_motion_cache(DW w) {
     if (aborted(w)) return;
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    w.mdx[h] = st3(ld3(w.pos[h]) - ld3(w.pos0[h]), 0.0f);
+    w.mdr[h] = st3(quat_diff_vec(ldq(w.rot[h]), ldq(w.rot0[h])), 0.0f);
+}
+// Eq. 19 warmstart decay (mod.rs:1019-1040), then the point's step-start
+// normal violation C0 (joints_ext.rs:21-32), kept in lambda.w for the
+// iterations of this substep.
+static __device__ __forceinline__ void k_decay_points_one(const DW& w, uint32_t q) {
     uint32_t p = q / MAX_PTS, k = q % MAX_PTS;
-    if (p >= n_pairs(w) || k >= w.p_np[p]) return;
+    if (k >= w.p_np[p]) return;
     const float ag = ALPHA * GAMMA;
     float4 l = w.q_lam[q], r = w.q_roll[q], pn = w.q_pen[q];
-    w.q_lam[q] = make_float4(l.x * ag, l.y * ag, l.z * ag, 0.0f);
+    float4 n4 = w.p_n[p];
+    float c0 = 0.0f;
+    if (n4.w <= 0.0f) {
+        uint2 ab = w.p_ab[p];
+        bool sph = info_shape(w.info[ab.x]) == AVBD_SHAPE_SPHERE || info_shape(w.info[ab.y]) == AVBD_SHAPE_SPHERE;
+        c0 = gap_c0(sph, n4.w, ld3(n4), ld3(w.pos0[ab.x]), ldq(w.rot0[ab.x]), ld3(w.pos0[ab.y]), ldq(w.rot0[ab.y]),
+                    w.q_ra[q], w.q_rb[q]);
+    }
+    w.q_lam[q] = make_float4(l.x * ag, l.y * ag, l.z * ag, c0);
     w.q_roll[q] = make_float4(r.x * ag, r.y * ag, r.z * ag, 0.0f);
     w.q_pen[q] = make_float4(fclamp(pn.x * GAMMA, PENALTY_MIN, PENALTY_MAX),
                              fclamp(pn.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
                              fclamp(pn.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+}
+__global__ void k_decay_points(DW w) {
+    if (aborted(w)) return;
+    const uint32_t n = n_pairs(w) * MAX_PTS;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+        k_decay_points_one(w, q);
 }
 __global__ void k_decay_joints(DW w) {
     if (aborted(w)) return;
@@ -365,12 +481,13 @@ void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
     unsigned g1 = nblk(w.N + 1, 256);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cur, w.N + 1);
-    k_countB<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+    k_countB<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
     scan_exclusive(w.cnt, w.offB, w.N + 1, scan_tmp, st);
-    k_placeB<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+    k_placeB<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
     k_sortB<<<gb, 256, 0, st>>>(w);
     k_targets<<<gb, 256, 0, st>>>(w);
-    k_decay_points<<<nblk((size_t)w.pair_cap * MAX_PTS, 256), 256, 0, st>>>(w);
+    k_motion_cache<<<gb, 256, 0, st>>>(w);
+    k_decay_points<<<gsz((size_t)w.pair_cap * MAX_PTS, 256), 256, 0, st>>>(w);
     if (w.J) k_decay_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
 }
 
@@ -446,40 +563,42 @@ __global__ void __launch_bounds__(1024) k_colour(DW w) {
     if (maxc >= 0) atomicMax(&w.ctr[C_NCOL], (uint32_t)(maxc + 1));
     if (maxc + 1 > w.max_cols) atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_RANGE);
 }
-__global__ void k_colour_count(DW w) {
+// Colour lists: one stable 8-bit radix pass over (colour, body) puts the swept
+// bodies of each colour in ascending index order (coalesced body loads in
+// the primal); uncoloured bodies take digit 255 and sort last.
+__global__ void k_colour_keys(DW w, int by_work) {
     if (aborted(w)) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
     int c = w.colour[h];
-    if (c >= 0) atomicAdd(&w.col_cnt[c], 1u);
-}
-// col_cnt: [0, 64) colour starts, [64] total, [65, 129) scatter cursors
-__global__ void k_colour_scan(DW w) {
-    if (aborted(w)) return;
-    if (threadIdx.x != 0) return;
-    uint32_t run = 0;
-    for (int c = 0; c < MAX_COLOURS; c++) {
-        uint32_t v = w.col_cnt[c];
-        w.col_cnt[c] = run;
-        w.col_cnt[MAX_COLOURS + 1 + c] = run;
-        run += v;
+    uint32_t digit = c >= 0 ? (uint32_t)c : 255u;
+    uint32_t work = 0;
+    if (by_work) {
+        // incident pairs: bodies with similar work share a warp in the primal
+        work = (w.offA[h + 1] - w.offA[h]) + (w.offB[h + 1] - w.offB[h]);
+        work = min(work, 255u);
     }
-    w.col_cnt[MAX_COLOURS] = run;
+    w.col_key[h] = (digit << 8) | work;
+    w.col_val[h] = h;
 }
-__global__ void k_colour_scatter(DW w) {
+__global__ void k_colour_starts(DW w, int ntiles) {
     if (aborted(w)) return;
-    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N) return;
-    int c = w.colour[h];
-    if (c >= 0) w.col_list[atomicAdd(&w.col_cnt[MAX_COLOURS + 1 + c], 1u)] = h;
+    int c = threadIdx.x;
+    if (c <= MAX_COLOURS) w.col_cnt[c] = w.col_hist[(size_t)c * ntiles];
 }
-void launch_colouring(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
-    (void)scan_tmp;
-    k_zero_u32<<<1, 256, 0, st>>>(w.col_cnt, 2 * MAX_COLOURS + 2);
+void launch_colouring(const DW& w, const Tune& tune, uint32_t* scan_tmp, cudaStream_t st) {
     k_colour<<<w.S, 1024, 0, st>>>(w);
-    k_colour_count<<<nblk(w.N, 256), 256, 0, st>>>(w);
-    k_colour_scan<<<1, 32, 0, st>>>(w);
-    k_colour_scatter<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    k_colour_keys<<<nblk(w.N, 256), 256, 0, st>>>(w, tune.sort_work);
+    int ntiles;
+    if (tune.sort_work) {
+        // LSD: work byte, then colour byte (stable: index order within equal work)
+        radix_pass(w.col_key, w.col_val, w.col_key2, w.col_list, (size_t)w.N, 0, w.col_hist, scan_tmp, st);
+        ntiles = radix_pass(w.col_key2, w.col_list, w.col_key, w.col_val, (size_t)w.N, 8, w.col_hist, scan_tmp, st);
+        cudaMemcpyAsync(w.col_list, w.col_val, (size_t)w.N * 4, cudaMemcpyDeviceToDevice, st);
+    } else {
+        ntiles = radix_pass(w.col_key, w.col_val, w.col_key2, w.col_list, (size_t)w.N, 8, w.col_hist, scan_tmp, st);
+    }
+    k_colour_starts<<<1, 128, 0, st>>>(w, ntiles);
 }
 
 }  // namespace avbd

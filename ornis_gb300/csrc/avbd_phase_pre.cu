@@ -11,6 +11,8 @@ namespace avbd {
 
 __global__ void k_begin(DW w) {
     if (threadIdx.x == 0) {
+        w.ctr[C_CCD_PENDING] = 0;
+        w.ctr[C_BOXPAIRS] = 0;
         w.ctr[C_CAND] = 0;
         w.ctr[C_NCOL] = 0;
         w.ctr[C_FAST] = 0;
@@ -209,14 +211,33 @@ __global__ void k_sap_sweep(DW w, uint32_t n) {
         if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
     }
 }
-// Half-space bodies have an unbounded prefilter radius (rows.rs:290): every
-// other body of the scene is a candidate.
+// Half-space bodies have an unbounded prefilter radius (rows.rs:290), so the
+// reference narrowphases every (plane, body) pair.  A pair can only survive
+// discovery if it already exists (an empty shell is kept) or if the body can
+// come within the creation reach of the plane this substep; the body's
+// support distance is at least (x - p).n - bound_radius, its approach at most
+// |v_b| + |v_p| (twice that after a CCD bounce), and a CCD clamp moves it by at
+// most its travel.  Pairs outside that conservative reach are not emitted.
 __global__ void k_plane_cands(DW w) {
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
     if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) return;
     uint32_t s = w.scene_of[h];
-    for (uint32_t k = w.plane_off[s]; k < w.plane_off[s + 1]; k++) emit_candidate(w, w.plane_list[k], h);
+    V3 x = ld3(w.pos[h]);
+    float vh = len(ld3(w.vel[h]));
+    float travel = ccd_travel(w, h);
+    float rb = w.shp[h].w;
+    for (uint32_t k = w.plane_off[s]; k < w.plane_off[s + 1]; k++) {
+        uint32_t pl = w.plane_list[k];
+        if (find_old_pair(w, min(pl, h), max(pl, h)) < 0) {
+            float4 sp = w.shp[pl];
+            V3 n = qrot(ldq(w.rot[pl]), V3{sp.x, sp.y, sp.z});
+            float dlow = dot(x - ld3(w.pos[pl]), n) - rb;
+            float reach = GEN_MARGIN + 2.0f * (vh + len(ld3(w.vel[pl]))) * w.dt + travel;
+            if (dlow > reach + 1e-3f + 1e-5f * fabsf(dlow)) continue;
+        }
+        emit_candidate(w, pl, h);
+    }
 }
 
 void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st) {
@@ -280,15 +301,15 @@ __global__ void k_ccd_init(DW w) {
     w.ccd_deps[h] = 0;
     w.ccd_state[h] = 0;
     w.ccd_recompute[h] = 0;
-    if (w.fast[h]) atomicAdd(&w.ctr[C_FAST], 1u);
+    if (w.fast[h]) {
+        atomicAdd(&w.ctr[C_FAST], 1u);
+        atomicAdd(&w.ctr[C_CCD_PENDING], 1u);
+    }
 }
 // first = 1: every mover casts against its candidates at the step-top poses
 // and counts the earlier movers among its targets.  first = 0: only movers
 // flagged for a recast.
-__global__ void k_ccd_cast(DW w, int first) {
-    if (aborted(w)) return;
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cand(w)) return;
+static __device__ __forceinline__ void k_ccd_cast_one(const DW& w, int first, uint32_t c) {
     uint2 ab = w.cand[c];
     bool fa = w.fast[ab.x], fb = w.fast[ab.y];
     if (!fa && !fb) return;
@@ -306,6 +327,14 @@ __global__ void k_ccd_cast(DW w, int first) {
     }
     if (first && fa && fb && ccd_target(w, ab.x, ab.y)) atomicAdd(&w.ccd_deps[ab.y], 1u);
 }
+__global__ void k_ccd_cast(DW w, int first) {
+    if (aborted(w)) return;
+    if (w.ctr[C_FAST] == 0u || (!first && w.ctr[C_CCD_PENDING] == 0u)) return;
+    const uint32_t n = n_cand(w);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        k_ccd_cast_one(w, first, c);
+}
+
 static __device__ void ccd_apply(const DW& w, uint32_t h) {
     unsigned long long key = w.ccd_best[h];
     bool moved = false;
@@ -332,6 +361,7 @@ static __device__ void ccd_apply(const DW& w, uint32_t h) {
 }
 __global__ void k_ccd_finalize(DW w, int round, int last) {
     if (aborted(w)) return;
+    if (w.ctr[C_CCD_PENDING] == 0u) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N || !w.fast[h] || w.ccd_state[h] != 0) return;
     if (w.ccd_deps[h] != 0) {
@@ -340,11 +370,9 @@ __global__ void k_ccd_finalize(DW w, int round, int last) {
     }
     ccd_apply(w, h);
     w.ccd_recompute[h] = (uint8_t)(16 + round);  // "finalised in this round"
+    atomicSub(&w.ctr[C_CCD_PENDING], 1u);
 }
-__global__ void k_ccd_release(DW w, int round) {
-    if (aborted(w)) return;
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_cand(w)) return;
+static __device__ __forceinline__ void k_ccd_release_one(const DW& w, int round, uint32_t c) {
     uint2 ab = w.cand[c];
     if (!w.fast[ab.x] || !w.fast[ab.y]) return;
     if (w.ccd_recompute[ab.x] != (uint8_t)(16 + round)) return;
@@ -352,14 +380,24 @@ __global__ void k_ccd_release(DW w, int round) {
     atomicSub(&w.ccd_deps[ab.y], 1u);
     if (w.ccd_state[ab.x] == 2) w.ccd_recompute[ab.y] = 1;  // the earlier mover moved: recast
 }
+__global__ void k_ccd_release(DW w, int round) {
+    if (aborted(w)) return;
+    if (w.ctr[C_CCD_PENDING] == 0u) return;
+    const uint32_t n = n_cand(w);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+        k_ccd_release_one(w, round, c);
+}
+
 __global__ void k_ccd_reset(DW w) {
     if (aborted(w)) return;
+    if (w.ctr[C_CCD_PENDING] == 0u) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N || !w.fast[h]) return;
     if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_best[h] = ~0ull;
 }
 __global__ void k_ccd_clear_recast(DW w) {
     if (aborted(w)) return;
+    if (w.ctr[C_CCD_PENDING] == 0u) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N || !w.fast[h]) return;
     if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_recompute[h] = 0;
@@ -367,16 +405,15 @@ __global__ void k_ccd_clear_recast(DW w) {
 void launch_ccd(const DW& w, cudaStream_t st) {
     if (!w.enable_ccd) return;
     unsigned gb = nblk(w.N, 256);
-    unsigned gc = nblk(w.cand_cap, 256);
     k_ccd_init<<<gb, 256, 0, st>>>(w);
-    k_ccd_cast<<<gc, 256, 0, st>>>(w, 1);
+    k_ccd_cast<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, 1);
     for (int r = 0; r < CCD_ROUNDS; r++) {
         bool last = r == CCD_ROUNDS - 1;
         k_ccd_finalize<<<gb, 256, 0, st>>>(w, r, last ? 1 : 0);
         if (last) break;
-        k_ccd_release<<<gc, 256, 0, st>>>(w, r);
+        k_ccd_release<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, r);
         k_ccd_reset<<<gb, 256, 0, st>>>(w);
-        k_ccd_cast<<<gc, 256, 0, st>>>(w, 0);
+        k_ccd_cast<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, 0);
         k_ccd_clear_recast<<<gb, 256, 0, st>>>(w);
     }
 }

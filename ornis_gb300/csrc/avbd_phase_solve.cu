@@ -6,7 +6,19 @@
 // sleep, driver baseline), avbd/sleep.rs:140-175.
 #include "avbd_common.cuh"
 
+// This file is compiled twice: the exact build (-fmad=false, IEEE divide and
+// square root) reproduces the CPU oracle bit for bit with one thread per
+// body; the fast build (-DAVBD_SOLVE_FAST: contracted multiply-adds,
+// approximate divide and square root) stays within the 1e-5 pose tolerance
+// and is what the benchmark runs.  Discovery is exact in both.
+#ifdef AVBD_SOLVE_FAST
+#define AVBD_SOLVE_NS fast
+#else
+#define AVBD_SOLVE_NS exact
+#endif
+
 namespace avbd {
+namespace AVBD_SOLVE_NS {
 
 static __device__ __forceinline__ void load_ctx(const DW& w, uint32_t p, PairCtx& c) {
     uint2 ab = w.p_ab[p];
@@ -19,20 +31,20 @@ static __device__ __forceinline__ void load_ctx(const DW& w, uint32_t p, PairCtx
     c.np = w.p_np[p];
     c.pa = ld3(w.pos[c.a]);
     c.pb = ld3(w.pos[c.b]);
-    c.pa0 = ld3(w.pos0[c.a]);
-    c.pb0 = ld3(w.pos0[c.b]);
     c.qa = ldq(w.rot[c.a]);
     c.qb = ldq(w.rot[c.b]);
-    c.qa0 = ldq(w.rot0[c.a]);
-    c.qb0 = ldq(w.rot0[c.b]);
-    c.dxa = c.pa - c.pa0;
-    c.dxb = c.pb - c.pb0;
-    c.dra = quat_diff_vec(c.qa, c.qa0);
-    c.drb = quat_diff_vec(c.qb, c.qb0);
+    c.dxa = ld3(w.mdx[c.a]);
+    c.dxb = ld3(w.mdx[c.b]);
+    c.dra = ld3(w.mdr[c.a]);
+    c.drb = ld3(w.mdr[c.b]);
     c.sph_a = info_shape(w.info[c.a]) == AVBD_SHAPE_SPHERE;
     c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
     c.rad_a = w.shp[c.a].x;
     c.rad_b = w.shp[c.b].x;
+    if (c.gap <= 0.0f) {
+        c.t1 = tangent_t1(c.n);
+        c.t2 = cross(c.t1, c.n);
+    }
 }
 
 // Rows of point k of pair p for the body on side is_a (assembly.rs:99-252).
@@ -40,9 +52,10 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
                                                    Sys& s) {
     uint32_t q = p * MAX_PTS + k;
     float4 ra = w.q_ra[q], rb = w.q_rb[q];
+    float4 lam = w.q_lam[q];
     float sign = is_a ? 1.0f : -1.0f;
     bool touching = c.gap <= 0.0f;
-    float c0 = touching ? gap_c0(c, ra, rb) : 0.0f;
+    float c0 = touching ? lam.w : 0.0f;
     V3 rup, rlo;
     contact_levers(c, ra, rb, rup, rlo);
     float cn = row_c_levers(c, c.n, c0, rup, rlo);
@@ -63,14 +76,13 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
         }
         return;
     }
-    V3 t1 = tangent_t1(c.n);
-    V3 t2 = cross(t1, c.n);
+    const V3 t1 = c.t1, t2 = c.t2;
     V3 raf, rbf;
     friction_levers(c, rup, rlo, raf, rbf);
     V3 r_side_f = is_a ? raf : rbf;
     float ct1 = row_c_levers(c, t1, 0.0f, raf, rbf);
     float ct2 = row_c_levers(c, t2, 0.0f, raf, rbf);
-    float4 pen = w.q_pen[q], lam = w.q_lam[q];
+    float4 pen = w.q_pen[q];
     float f[3];
     contact_force(cn, pen, lam, ct1, ct2, c.mu, f);
     if (row_live(cn, f[0])) stamp_row(s, c.n, pen.x, f[0], r_side, sign);
@@ -196,8 +208,12 @@ static __device__ __forceinline__ void inertial_block(const DW& w, uint32_t h, S
 static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, const Sys& s) {
     float dx[6];
     if (solve_6x6(s, dx)) {
-        w.pos[h] = st3(ld3(w.pos[h]) + V3{dx[0], dx[1], dx[2]}, 0.0f);
-        w.rot[h] = stq(quat_integrate(ldq(w.rot[h]), V3{dx[3], dx[4], dx[5]}));
+        V3 p = ld3(w.pos[h]) + V3{dx[0], dx[1], dx[2]};
+        Q q = quat_integrate(ldq(w.rot[h]), V3{dx[3], dx[4], dx[5]});
+        w.pos[h] = st3(p, 0.0f);
+        w.rot[h] = stq(q);
+        w.mdx[h] = st3(p - ld3(w.pos0[h]), 0.0f);
+        w.mdr[h] = st3(quat_diff_vec(q, ldq(w.rot0[h])), 0.0f);
     } else {
         atomicAdd(&w.ctr[C_BREAKDOWN], 1u);  // breakdown: the body skips its update
     }
@@ -205,7 +221,8 @@ static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, cons
 
 // One thread per body: rows accumulate in the reference's order (pairs in
 // ascending index — B-side pairs precede A-side ones — then joints).
-__global__ void k_primal_thread(DW w, int colour) {
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_primal_thread(DW w, int colour) {
     if (aborted_solve(w)) return;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
@@ -273,18 +290,12 @@ __global__ void k_primal_lanes(DW w, int colour) {
 }
 
 // ---- dual (joints_ext.rs:464-573 contacts, :574-896 Ball/Revolute) ----
-__global__ void k_dual_points(DW w) {
-    if (aborted_solve(w)) return;
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t p = q / MAX_PTS, k = q % MAX_PTS;
-    if (p >= n_pairs(w) || k >= w.p_np[p]) return;
-    PairCtx c;
-    load_ctx(w, p, c);
+// One thread per pair: the pair context is built once for all its points.
+static __device__ __forceinline__ void dual_point(const DW& w, const PairCtx& c, V3 t1, V3 t2, uint32_t q) {
     float4 ra = w.q_ra[q], rb = w.q_rb[q];
-    V3 t1 = tangent_t1(c.n);
-    V3 t2 = cross(t1, c.n);
     bool touching = c.gap <= 0.0f;
-    float c0 = touching ? gap_c0(c, ra, rb) : 0.0f;
+    float4 pen = w.q_pen[q], lam = w.q_lam[q];
+    float c0 = touching ? lam.w : 0.0f;
     V3 raw, rbw;
     contact_levers(c, ra, rb, raw, rbw);
     float cn = row_c_levers(c, c.n, c0, raw, rbw);
@@ -292,7 +303,6 @@ __global__ void k_dual_points(DW w) {
     friction_levers(c, raw, rbw, raf, rbf);
     float ct1 = row_c_levers(c, t1, 0.0f, raf, rbf);
     float ct2 = row_c_levers(c, t2, 0.0f, raf, rbf);
-    float4 pen = w.q_pen[q], lam = w.q_lam[q];
     float f[3];
     contact_force(cn, pen, lam, ct1, ct2, c.mu, f);
     float bnd = fabsf(f[0]) * fmaxf(c.mu.x, c.mu.y);
@@ -330,6 +340,19 @@ __global__ void k_dual_points(DW w) {
             rls[li] = fclamp(ROLL_PEN * dot(wrel, rax[li]) + rls[li], -cap, cap);
         }
         w.q_roll[q] = make_float4(rls[0], rls[1], rls[2], 0.0f);
+    }
+}
+__global__ void k_dual_pairs(DW w) {
+    if (aborted_solve(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t np = w.p_np[p];
+        if (np == 0) continue;
+        PairCtx c;
+        load_ctx(w, p, c);
+        V3 t1 = tangent_t1(c.n);  // the grip flag of separated points needs the frame too
+        V3 t2 = cross(t1, c.n);
+        for (uint32_t k = 0; k < np; k++) dual_point(w, c, t1, t2, p * MAX_PTS + k);
     }
 }
 __global__ void k_dual_joints(DW w) {
@@ -396,7 +419,13 @@ __global__ void k_dual_joints(DW w) {
 void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
     int bs = tune.primal_block;
     switch (tune.primal_lanes) {
-        case 1: k_primal_thread<<<nblk(max_bodies, bs), bs, 0, st>>>(w, c); break;
+        case 1:
+            // occupancy variants of the thread-per-body kernel: 4, 6 or 8
+            // resident 128-thread blocks per SM (128, 80 or 64 registers)
+            if (tune.primal_minb >= 8) k_primal_thread<8><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            else if (tune.primal_minb >= 6) k_primal_thread<6><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            else k_primal_thread<4><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            break;
         case 4: k_primal_lanes<4><<<nblk((size_t)max_bodies * 4, bs), bs, 0, st>>>(w, c); break;
         case 8: k_primal_lanes<8><<<nblk((size_t)max_bodies * 8, bs), bs, 0, st>>>(w, c); break;
         case 16: k_primal_lanes<16><<<nblk((size_t)max_bodies * 16, bs), bs, 0, st>>>(w, c); break;
@@ -404,12 +433,12 @@ void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bod
     }
 }
 void launch_dual(const DW& w, cudaStream_t st) {
-    k_dual_points<<<nblk((size_t)w.pair_cap * MAX_PTS, 256), 256, 0, st>>>(w);
+    k_dual_pairs<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
     if (w.J) k_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
 }
 void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st) {
-    for (int c = 0; c < ncolours; c++) launch_primal_colour(w, tune, c, (uint32_t)w.N, st);
-    launch_dual(w, st);
+    for (int c = 0; c < ncolours; c++) AVBD_SOLVE_NS::launch_primal_colour(w, tune, c, (uint32_t)w.N, st);
+    AVBD_SOLVE_NS::launch_dual(w, st);
 }
 
 // ---- BDF1 + sleep + driver baseline (mod.rs:1060-1142) -------------------------
@@ -463,16 +492,20 @@ __global__ void k_support_joints(DW w) {
     w.flag[ab.x] |= 2;
     w.flag[ab.y] |= 2;
 }
-__global__ void k_support(DW w) {
-    if (aborted_solve(w)) return;
-    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs(w)) return;
+static __device__ __forceinline__ void k_support_one(const DW& w, uint32_t p) {
     if (w.p_n[p].w <= 0.0f && w.p_np[p] > 0) {
         uint2 ab = w.p_ab[p];
         w.flag[ab.x] |= 2;
         w.flag[ab.y] |= 2;
     }
 }
+__global__ void k_support(DW w) {
+    if (aborted_solve(w)) return;
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        k_support_one(w, p);
+}
+
 __global__ void k_sleep_timer(DW w) {
     if (aborted_solve(w)) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -532,7 +565,7 @@ void launch_finish_substep(const DW& w, cudaStream_t st) {
             k_ready_scatter<<<gb, 256, 0, st>>>(w);
             k_support_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
         }
-        k_support<<<nblk(w.pair_cap, 256), 256, 0, st>>>(w);
+        k_support<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
         k_sleep_timer<<<gb, 256, 0, st>>>(w);
         k_comp_clear<<<gb, 256, 0, st>>>(w);
         if (w.J) k_freeze_gather<<<gb, 256, 0, st>>>(w);
@@ -540,4 +573,5 @@ void launch_finish_substep(const DW& w, cudaStream_t st) {
     k_freeze_apply<<<gb, 256, 0, st>>>(w, w.enable_sleep);
 }
 
+}  // namespace AVBD_SOLVE_NS
 }  // namespace avbd

@@ -187,10 +187,11 @@ struct PairCtx {
     float gap;
     float2 mu;
     uint32_t a, b, np;
-    V3 pa, pb, pa0, pb0;
-    Q qa, qb, qa0, qb0;
+    V3 pa, pb;
+    Q qa, qb;
     V3 dxa, dxb;    // x - x0
     V3 dra, drb;    // quat_diff_vec(q, q0)
+    V3 t1, t2;      // friction frame (touching pairs)
     bool sph_a, sph_b;
     float rad_a, rad_b;
 };
@@ -209,11 +210,15 @@ static __device__ __forceinline__ void friction_levers(const PairCtx& c, V3 raw,
     raf = raw - c.n * (sep * HALF);
     rbf = rbw + c.n * (sep * HALF);
 }
-static __device__ __forceinline__ float gap_c0(const PairCtx& c, float4 ra, float4 rb) {  // joints_ext.rs:21-32
-    if (c.sph_a || c.sph_b) return c.gap + MARGIN;
-    V3 pa = c.pa0 + qrot(c.qa0, ld3(ra));
-    V3 pb = c.pb0 + qrot(c.qb0, ld3(rb));
-    return dot(c.n, pa - pb) + MARGIN;
+// Step-start normal violation of a point (joints_ext.rs:21-32).  It depends on
+// the step-start poses only, so it is evaluated once per substep and kept in
+// the w lane of the point's lambda record.
+static __device__ __forceinline__ float gap_c0(bool sphere_pair, float gap, V3 n, V3 pa0, Q qa0, V3 pb0, Q qb0,
+                                               float4 ra, float4 rb) {
+    if (sphere_pair) return gap + MARGIN;
+    V3 pa = pa0 + qrot(qa0, ld3(ra));
+    V3 pb = pb0 + qrot(qb0, ld3(rb));
+    return dot(n, pa - pb) + MARGIN;
 }
 
 }  // namespace avbd

@@ -134,6 +134,16 @@ __global__ void k_rs_scatter(const uint32_t* keys, const uint32_t* vals, uint32_
     }
 }
 
+int radix_pass(const uint32_t* keys, const uint32_t* vals, uint32_t* okeys, uint32_t* ovals, size_t n, int shift,
+               uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
+    int ntiles = (int)((n + RS_TILE - 1) / RS_TILE);
+    if (n == 0) return 0;
+    k_rs_hist<<<ntiles, RS_THREADS, 0, st>>>(keys, n, shift, hist, ntiles);
+    scan_exclusive(hist, hist, (size_t)256 * ntiles, scan_tmp, st);
+    k_rs_scatter<<<ntiles, RS_THREADS, 0, st>>>(keys, vals, okeys, ovals, n, shift, hist, ntiles);
+    return ntiles;
+}
+
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* keys_alt, uint32_t* vals_alt, size_t n,
                       uint32_t* hist, uint32_t* scan_tmp, cudaStream_t st) {
     if (n <= 1) return;

@@ -5,6 +5,7 @@
 // Host semantics mirror the reference's engine seam (crates/physics/src/
 // engine.rs:24-133, avbd/mod.rs:1211-1602): dense handles in insertion order,
 // the fixed-step accumulator of PhysicsEngine::step, JointError-style codes.
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -192,6 +193,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.inertial = m.get<float4>(N); w.inertial_rot = m.get<float4>(N);
     w.prev_pos = m.get<float4>(N); w.prev_rot = m.get<float4>(N);
     w.inertia = m.get<float4>(N); w.inertia_rest = m.get<float4>(N);
+    w.mdx = m.get<float4>(N); w.mdr = m.get<float4>(N);
     w.mat = m.get<float4>(N); w.shp = m.get<float4>(N);
     w.inv_mass = m.get<float>(N); w.inv_mass_rest = m.get<float>(N); w.mass = m.get<float>(N);
     w.friction_t = m.get<float>(N); w.sleep_timer = m.get<float>(N);
@@ -221,6 +223,9 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.cnt = m.get<uint32_t>(N + 1);
     w.cur = m.get<uint32_t>(N + 1);
     w.slot_c = m.get<uint32_t>(cand_cap);
+    w.boxlist = m.get<uint32_t>(cand_cap);
+    w.bd_pa = m.get<float4>(cand_cap);
+    w.bd_pb = m.get<float4>(cand_cap);
     w.aabb_lo = m.get<float4>(N); w.aabb_hi = m.get<float4>(N);
     // large-scene sort scratch
     uint32_t max_large = 0;
@@ -239,7 +244,8 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     W->plan.keys_alt = m.get<uint32_t>(max_large);
     W->plan.vals_alt = m.get<uint32_t>(max_large);
     W->plan.hist = m.get<uint32_t>(radix_hist_words(max_large));
-    size_t scan_words = std::max(scan_tmp_words((size_t)N + 1), scan_tmp_words(radix_hist_words(max_large)));
+    size_t scan_words = std::max({scan_tmp_words((size_t)N + 1), scan_tmp_words(radix_hist_words(max_large)),
+                                  scan_tmp_words(radix_hist_words(N))});
     W->scan_tmp = m.get<uint32_t>(scan_words + 16);
     W->plan.scan_tmp = W->scan_tmp;
     W->d_small = m.get<uint32_t>(small.size());
@@ -256,6 +262,10 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.comp_flag = m.get<uint32_t>(N);
     w.col_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
     w.col_list = m.get<uint32_t>(N);
+    w.col_key = m.get<uint32_t>(N);
+    w.col_key2 = m.get<uint32_t>(N);
+    w.col_val = m.get<uint32_t>(N);
+    w.col_hist = m.get<uint32_t>(radix_hist_words(N));
     w.ctr = m.get<uint32_t>(C_NUM);
     W->d_stage = m.get<AvbdBody>(N);
     for (void* p : m.ptrs)
@@ -451,6 +461,15 @@ static int upload_all(AvbdWorld* W) {
         }
     }
     for (uint32_t h = 0; h < N; h++) offA[h + 1] += offA[h];
+    // B-side incidence of the uploaded pairs (read by the next discovery's
+    // old-pair lookup): per body, pair indices ascending
+    std::vector<uint32_t> offB(N + 1, 0), listB(std::max<uint32_t>(P, 1));
+    for (uint32_t i = 0; i < P; i++) offB[pab[i].y + 1]++;
+    for (uint32_t h = 0; h < N; h++) offB[h + 1] += offB[h];
+    {
+        std::vector<uint32_t> cb(offB.begin(), offB.end() - 1);
+        for (uint32_t i = 0; i < P; i++) listB[cb[pab[i].y]++] = i;
+    }
     auto up = [&](void* dst, const void* src, size_t bytes) {
         if (bytes) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
@@ -482,6 +501,8 @@ static int upload_all(AvbdWorld* W) {
     up(w.q_lam, qlam.data(), qlam.size() * 16); up(w.q_pen, qpen.data(), qpen.size() * 16);
     up(w.q_roll, qroll.data(), qroll.size() * 16); up(w.q_matched, qm.data(), qm.size() * 4);
     up(w.offA, offA.data(), (N + 1) * 4);
+    up(w.offB, offB.data(), (N + 1) * 4);
+    up(w.listB, listB.data(), P * 4);
     up(W->d_stage, W->bodies.data(), N * sizeof(AvbdBody));
     k_bodies_in<<<(N + 255) / 256, 256, 0, st>>>(w, W->d_stage, 0, N);
     CK(cudaStreamSynchronize(st));
@@ -608,12 +629,12 @@ static void enqueue_front(AvbdWorld* W) {
     launch_ccd(w, st);
     launch_discovery(w, W->scan_tmp, st);
     launch_post_discovery(w, W->scan_tmp, st);
-    launch_colouring(w, W->scan_tmp, st);
+    launch_colouring(w, W->tune, W->scan_tmp, st);
 }
 static void enqueue_back(AvbdWorld* W, int ncol) {
     const DW& w = W->w;
     for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
-    launch_finish_substep(w, W->st);
+    launch_finish_substep(w, W->tune, W->st);
 }
 
 static int read_ctr(AvbdWorld* W) {
@@ -1116,11 +1137,34 @@ int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const flo
     return AVBD_OK;
 }
 
+int avbd_set_precision(AvbdWorld* W, int fast) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    W->tune.fast = fast ? 1 : 0;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
+int avbd_set_work_order(AvbdWorld* W, int by_work) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    W->tune.sort_work = by_work ? 1 : 0;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
+int avbd_set_occupancy(AvbdWorld* W, int min_blocks) {
+    if (!W || (min_blocks != 4 && min_blocks != 6 && min_blocks != 8)) return AVBD_ERR_INVALID_ARG;
+    W->tune.primal_minb = min_blocks;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
 int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
     if (!W) return AVBD_ERR_INVALID_ARG;
     if (primal_lanes != 1 && primal_lanes != 4 && primal_lanes != 8 && primal_lanes != 16 && primal_lanes != 32)
         return AVBD_ERR_INVALID_ARG;
     if (primal_block < 32 || primal_block > 1024 || primal_block % 32) return AVBD_ERR_INVALID_ARG;
+    // the thread-per-body primal is register-bounded for 128-thread blocks
+    if (primal_lanes == 1 && primal_block > 128) return AVBD_ERR_INVALID_ARG;
     W->tune.primal_lanes = primal_lanes;
     W->tune.primal_block = primal_block;
     free_graphs(W);
@@ -1128,6 +1172,13 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
 }
 
 int avbd_abi_version(void) { return AVBD_ABI_VERSION; }
+
+// Bracket a region for profilers started with collection off
+// (`ncu --profile-from-start off`).
+int avbd_profiler(int on) {
+    cudaError_t e = on ? cudaProfilerStart() : cudaProfilerStop();
+    return e == cudaSuccess ? AVBD_OK : AVBD_ERR_DEVICE;
+}
 
 // Device time of `substeps` substeps, bracketed by CUDA events on the world's
 // stream (graph replay when use_graph != 0).
@@ -1179,7 +1230,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     CK(cudaEventRecord(ev[4], st));
     launch_post_discovery(w, W->scan_tmp, st);
     CK(cudaEventRecord(ev[5], st));
-    launch_colouring(w, W->scan_tmp, st);
+    launch_colouring(w, W->tune, W->scan_tmp, st);
     CK(cudaEventRecord(ev[6], st));
     rc = read_ctr(W);
     if (rc) return rc;
@@ -1194,7 +1245,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
         CK(cudaEventRecord(ev[6], st));
         for (int c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, c, (uint32_t)w.N, st);
         CK(cudaEventRecord(ev[7], st));
-        launch_dual(w, st);
+        launch_dual(w, W->tune, st);
         CK(cudaEventRecord(ev[8], st));
         CK(cudaEventSynchronize(ev[8]));
         CK(cudaEventElapsedTime(&t, ev[6], ev[7]));
@@ -1203,7 +1254,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
         dual += t;
     }
     CK(cudaEventRecord(ev[8], st));
-    launch_finish_substep(w, st);
+    launch_finish_substep(w, W->tune, st);
     CK(cudaEventRecord(ev[9], st));
     CK(cudaEventSynchronize(ev[9]));
     ms[6] = prim;

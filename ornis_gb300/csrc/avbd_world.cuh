@@ -68,6 +68,8 @@ enum Ctr {
     C_POINTS = 8,     // live points
     C_SLEEP = 9,      // bodies asleep
     C_CCD_LEFT = 10,  // fast bodies left after the bounded CCD rounds
+    C_CCD_PENDING = 11,  // fast bodies not yet clamped this substep
+    C_BOXPAIRS = 12,     // box-box pairs handed to the warp-per-pair builder
     C_NUM = 16
 };
 enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
@@ -94,6 +96,7 @@ struct DW {
     float4 *pos, *rot, *vel, *angvel, *torque;
     float4 *pos0, *rot0, *inertial, *inertial_rot, *prev_pos, *prev_rot;
     float4 *inertia, *inertia_rest;
+    float4 *mdx, *mdr;  // cached x - x0 and quat_diff_vec(q, q0), refreshed whenever a pose changes in a substep
     float4* mat;  // restitution, friction, rolling, torsion
     float4* shp;  // shape params xyz, bound radius w
     float *inv_mass, *inv_mass_rest, *mass, *friction_t, *sleep_timer;
@@ -133,6 +136,8 @@ struct DW {
     uint32_t* cnt;     // per body counters (N+1)
     uint32_t* cur;     // per body cursors
     uint32_t* slot_c;  // final pair slot -> candidate index
+    uint32_t* boxlist; // box-box pair slots for the warp witness kernel
+    float4 *bd_pa, *bd_pb;  // box-box witnesses per pair slot: (pa, dist), (pb, SAT gap)
     float4 *aabb_lo, *aabb_hi;
     uint32_t* sort_key;
     uint32_t* sort_idx;
@@ -150,7 +155,8 @@ struct DW {
 
     // colouring
     uint32_t* col_cnt;   // MAX_COLOURS+1
-    uint32_t* col_list;  // N
+    uint32_t* col_list;  // N: swept bodies grouped by colour, ascending index within a colour
+    uint32_t *col_key, *col_key2, *col_val, *col_hist;
     uint32_t* ctr;       // counters
 };
 
