@@ -303,6 +303,30 @@ int avbd_world_profile_substep(AvbdWorld* world, float* ms, uint32_t* info);
 /* Kernel nodes in one captured substep graph (0 before the first capture). */
 int avbd_world_graph_nodes(AvbdWorld* world, uint32_t* n);
 
+/* ---- allocation-free stepping (no counterpart in the reference) ----------- */
+
+#define AVBD_STATIC_MAX_BODIES 128u      /* bodies per call */
+#define AVBD_STATIC_PAIR_CAP 2048u       /* broadphase candidates per substep */
+#define AVBD_STATIC_SCRATCH_BYTES 3481600u /* device array every GPU that loads the library holds */
+
+/* Step one scene of at most AVBD_STATIC_MAX_BODIES bodies (no joints) for
+ * `substeps` fixed substeps of params->step_dt, from host records `bodies`
+ * to host records `out` (out may equal bodies), without allocating: for
+ * callers that cannot call cudaMalloc (an engine that owns every device
+ * allocation through its own pools, a process whose device memory is capped
+ * or fully reserved).  All device scratch is one file-scope device array of
+ * AVBD_STATIC_SCRATCH_BYTES, resolved on the first call on each device with
+ * that device current (make that first call before any stream capture).
+ * The results equal an AvbdWorld created from the same bodies and advanced
+ * by avbd_world_step_fixed(substeps).  Each call starts fresh: no contact
+ * warm start carries over from an earlier call.  Calls share the array, so
+ * calls that overlap on the GPU (two host threads, two streams) race.
+ * Returns AVBD_ERR_CAPACITY for more than AVBD_STATIC_MAX_BODIES bodies or
+ * when a substep finds more than AVBD_STATIC_PAIR_CAP candidates (out is then
+ * not written), AVBD_ERR_NONFINITE for a non-finite body. */
+int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uint32_t n, int32_t substeps,
+                           AvbdBody* out);
+
 #ifdef __cplusplus
 }
 #endif

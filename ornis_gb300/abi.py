@@ -19,6 +19,11 @@ AVBD_ERR_JOINT_HANDLES = -11
 AVBD_ERR_JOINT_BAD_AXIS = -12
 AVBD_ERR_JOINT_NONFINITE = -13
 
+# limits of the allocation-free entry point (avbd_scene_step_static)
+STATIC_MAX_BODIES = 128
+STATIC_PAIR_CAP = 2048
+STATIC_SCRATCH_BYTES = 3481600
+
 SHAPE_SPHERE = 0
 SHAPE_BOX = 1
 SHAPE_CAPSULE = 2

@@ -66,6 +66,7 @@ def lib():
             "avbd_world_step_timed": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)],
             "avbd_world_profile_substep": [vp, vp, vp],
             "avbd_world_graph_nodes": [vp, C.POINTER(u32)],
+            "avbd_scene_step_static": [C.POINTER(abi.AvbdParams), vp, u32, C.c_int32, vp],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -95,6 +96,21 @@ def bodies_array(records):
     if records:
         C.memmove(arr.ctypes.data, (abi.AvbdBody * len(records))(*records), arr.nbytes)
     return arr
+
+
+def scene_step_static(params, bodies, substeps):
+    """Step one small scene without any device allocation (avbd_scene_step_static).
+
+    For callers that cannot call cudaMalloc: the library keeps one fixed
+    device array for this entry point (abi.STATIC_SCRATCH_BYTES per GPU) and
+    accepts at most abi.STATIC_MAX_BODIES bodies.  Returns the stepped body
+    records; the input array is not modified.
+    """
+    src = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+    out = np.empty_like(src)
+    rc = lib().avbd_scene_step_static(C.byref(params), src.ctypes.data, len(src), int(substeps), out.ctypes.data)
+    _check(rc, "avbd_scene_step_static")
+    return out
 
 
 class AvbdWorld:

@@ -27,6 +27,7 @@ SOURCES = [
     ("avbd_phase_solve.cu", "avbd_phase_solve_fast.o",
      ["-DAVBD_SOLVE_FAST", "-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
     ("avbd_world.cu", "avbd_world.o", []),
+    ("avbd_static.cu", "avbd_static.o", []),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--extended-lambda", "-Xcompiler", "-fPIC",
