@@ -1,30 +1,38 @@
 """Benchmark of the GB300 AVBD step: body-steps/s on the batched workload.
 
 Workload (default): batched_4096 — 4096 independent scenes of log-uniform
-8..1024 bodies (boxes and spheres in a 20x20 bin), dt 1/120 s, 2 substeps,
-8 iterations, f32.  A "step" is one 1/60 s frame = 2 substeps of every
-scene.  body-steps/s = dynamic bodies x steps / seconds.
+8..1024 bodies (boxes and spheres dropped into a 20x20 bin), dt 1/120 s,
+2 substeps, 8 iterations, f32, 240 steps.  A "step" is one 1/60 s frame =
+2 substeps of every scene.  body-steps/s = dynamic bodies x steps / seconds.
+Every rate below covers the same trajectory: K steps from the initial drop
+(K = --steps, default 240), so the cheap falling phase and the contact-heavy
+piles at the end weigh as they do in the workload.
 
-  value        device time of K graph-replayed steps, state resident in HBM
-               (CUDA events on the world's stream).
-  e2e          the same steps through the C ABI with host buffers: every step
-               uploads all body records, steps, downloads all body records
-               (host wall clock around synchronised calls).
-  plain        the same scenes stepped one scene per launch sequence (one
-               world per scene), a bounded sample of scenes; the batched/plain
-               ratio is the batching speed-up.
-  roofline     the primal kernel: algorithmic bytes per launch (byte model in
+  value        device time of the K graph-replayed steps, state resident in
+               HBM (CUDA events on the world's stream).
+  e2e          the same K steps through the C ABI with host buffers: every
+               step uploads all body records, steps, downloads all body
+               records (host wall clock around synchronised calls).
+  plain        a bounded sample of the same scenes, each stepped alone (one
+               world per scene, plain launches) over the same K steps; the
+               batched/plain ratio is the batching speed-up.
+  roofline     the primal kernel in one profiled substep at the end of the
+               trajectory: algorithmic bytes per launch (byte model in
                ornis_gb300/roofline.py) / its CUDA-event time per launch,
                against the measured HBM copy bandwidth.
   cpu_baseline the oracle's Reference-mode step (the reference's own serial
                algorithm restated in C++) on the host cores, a bounded sample
-               of the same scenes, one process per core.
+               of the same scenes over the same K steps, one process per core.
 
---impl reference times that CPU path alone (the reference itself is Rust and
+Warm-up steps run from the initial state and the world is then reset to it,
+so the timed trajectory starts at step 0.  The primal launch shape is
+autotuned at step --tune-at (piles formed), then the state is reset.
+--impl reference times the CPU path alone (the reference itself is Rust and
 cannot be built here).  Under torchrun (N > 1) scenes are sharded across
 ranks (scene s -> rank s mod N), no data-path collective; rank 0 prints.
 """
 import argparse
+import atexit
 import json
 import math
 import os
@@ -54,21 +62,30 @@ def hbm_peak():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling around the timed region.
+
+    The sampler starts before the warm-up steps (nvidia-smi needs a moment
+    before its first row) and every row carries its host arrival time;
+    `mark(t0, t1)` bounds the timed region and the summary keeps the rows
+    inside it.  When the region is shorter than a few sampling periods, the
+    rows within one period of its ends are kept too (stated in `window`).
+    """
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self, device=0):
         self.rows = []
         self.proc = None
         self.device = device
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -78,10 +95,19 @@ class Clocks:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
+
+    def wait_first(self, timeout=5.0):
+        end = time.perf_counter() + timeout
+        while self.proc and not self.rows and time.perf_counter() < end:
+            time.sleep(0.02)
+
+    def mark(self, t0, t1):
+        self.t0, self.t1 = t0, t1
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
+            time.sleep(2 * self.PERIOD_MS / 1e3)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -89,9 +115,20 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
+        rows = list(self.rows)
+        window = "timed region"
+        if self.t0 is not None:
+            inside = [r for t, r in rows if self.t0 <= t <= self.t1]
+            if len(inside) < 3:
+                pad = self.PERIOD_MS / 1e3
+                inside = [r for t, r in rows if self.t0 - pad <= t <= self.t1 + pad]
+                window = f"timed region +- {self.PERIOD_MS} ms ({(self.t1 - self.t0) * 1e3:.0f} ms long)"
+            rows = inside
+        else:
+            rows = [r for _, r in rows]
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in rows:
             try:
                 sm.append(float(r[1]))
                 mx = max(mx, float(r[2]))
@@ -101,7 +138,7 @@ class Clocks:
             except (ValueError, IndexError):
                 continue
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "window": window}
 
 
 def dist_init(n_gpus):
@@ -132,26 +169,27 @@ def shard(bodies, offs, rank, world):
 # CPU baseline: the oracle's Reference-mode step, one process per core.
 # ---------------------------------------------------------------------------
 def _cpu_scene_worker(args):
-    """Settle one scene (untimed), then time `steps` steps of the oracle."""
-    bodies, params_tuple, nsub, preroll, steps = args
+    """Step one scene `start` steps untimed, then time `steps` steps of the oracle."""
+    bodies, params_tuple, nsub, start, steps = args
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_api as O
 
     p = abi.default_params(step_dt=params_tuple[0], iterations=params_tuple[1])
     w = O.OracleWorld(p, mode=O.REFERENCE)
     w.add_bodies(bodies)
-    w.step_fixed(nsub * preroll)
+    if start:
+        w.step_fixed(nsub * start)
     t0 = time.perf_counter()
     w.step_fixed(nsub * steps)
     return time.perf_counter() - t0, scenes.dynamic_count(bodies) * steps
 
 
-def cpu_baseline(bodies, offs, params, nsub, preroll, steps=4, per_core=3):
+def cpu_baseline(bodies, offs, params, nsub, start, steps, per_core=3):
     """Body-steps/s of the oracle's Reference step on a seeded sample of scenes.
 
-    Each sampled scene settles for `preroll` steps (untimed, like the GPU run),
-    then `steps` steps are timed; scenes run one process per core and the rate
-    is sampled body-steps over the summed per-scene seconds divided by cores.
+    Each sampled scene runs steps [start, start + steps) of its trajectory;
+    scenes run one process per core and the rate is sampled body-steps over
+    the summed per-scene seconds divided by cores.
     """
     import multiprocessing as mp
 
@@ -159,7 +197,7 @@ def cpu_baseline(bodies, offs, params, nsub, preroll, steps=4, per_core=3):
     S = len(offs) - 1
     rng = np.random.default_rng(12345)
     chosen = [int(s) for s in rng.permutation(S)[: min(S, cores * per_core)]]
-    jobs = [(bodies[offs[s]:offs[s + 1]], (params.step_dt, params.iterations), nsub, preroll, steps) for s in chosen]
+    jobs = [(bodies[offs[s]:offs[s + 1]], (params.step_dt, params.iterations), nsub, start, steps) for s in chosen]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -174,8 +212,8 @@ def cpu_baseline(bodies, offs, params, nsub, preroll, steps=4, per_core=3):
         "cores": cores,
         "kind": "port",
         "sample": f"{len(chosen)} of {S} scenes (seeded random, mean {mean_n:.0f} bodies incl. 5 planes), "
-                  f"each settled {preroll} steps untimed then {steps} steps x {nsub} substeps timed; "
-                  f"one process per core; rate = body-steps / (summed scene seconds / cores); wall {wall:.1f} s",
+                  f"steps {start}..{start + steps} x {nsub} substeps timed per scene; one process per core; "
+                  f"rate = body-steps / (summed scene seconds / cores); wall {wall:.1f} s",
     }
 
 
@@ -186,8 +224,7 @@ def run_reference(args):
         return 0
     bodies, offs, counts = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
-    cb = cpu_baseline(bodies, offs, params, nsub, preroll=args.preroll, steps=max(1, args.steps // 5),
-                      per_core=args.cpu_per_core)
+    cb = cpu_baseline(bodies, offs, params, nsub, start=args.start, steps=args.steps, per_core=args.cpu_per_core)
     v = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -213,32 +250,42 @@ def run_ours(args):
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
     w.set_precision(not args.exact)
-    # settle: bodies fall into their bins before the measured steps
-    for _ in range(args.preroll):
-        w.step_graph(nsub)
+    s0 = w.export_state()  # the initial drop: no contacts yet
     tuned = None
-    if args.lanes:
+    if args.lanes is not None:
         w.set_tuning(args.lanes, args.block)
     elif args.autotune:
         from ornis_gb300.tune import autotune
 
-        tuned = autotune(w, substeps_per_trial=nsub)
+        w.step_graph(nsub * args.tune_at)  # piles formed: where the primal costs most
+        tuned = autotune(w, substeps_per_trial=2 * nsub)
+    clk = Clocks(device).__enter__()
+    atexit.register(clk.__exit__)
+    clk.wait_first()
     for _ in range(args.warmup):
         w.step_graph(nsub)
+    w.import_state(s0)
+    if args.start:
+        w.step_graph(nsub * args.start)
     w.sync()
     if args.profile_region:
-        # only the kernels of these steps are collected by `ncu --profile-from-start off`
+        # only the kernels of these steps are collected by `ncu --profile-from-start off`;
+        # they run from the state the timed region starts at, which is restored afterwards
         from ornis_gb300.avbd import lib as _lib
 
+        snap = w.export_state()
         _lib().avbd_profiler(1)
         w.step_graph(nsub * args.profile_region)
         w.sync()
         _lib().avbd_profiler(0)
+        w.import_state(snap)
     # ---- timed region: K steps, device time -------------------------------
     if d:
         d[0].barrier()
-    with Clocks(device) as clk:
-        ms = w.step_timed(nsub * args.steps, use_graph=True)
+    t0 = time.perf_counter()
+    ms = w.step_timed(nsub * args.steps, use_graph=True)
+    clk.mark(t0, time.perf_counter())
+    clk.__exit__()
     if d:
         import torch
 
@@ -252,50 +299,59 @@ def run_ours(args):
         ndyn_total = ndyn
     value = ndyn_total * args.steps / (ms / 1e3)
     nodes = w.graph_nodes()
-    # ---- e2e through the C ABI with host buffers ---------------------------
+    c = w.counters()
+    # ---- per-phase profile at the end of the trajectory: primal roofline ---
+    phases, info = w.profile_substep()
+    roof = roofline.primal_roofline(phases, info, hbm_peak())
+    roof["state"] = f"one profiled substep after step {args.start + args.steps}"
+    # ---- e2e through the C ABI with host buffers, same trajectory ----------
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    w.import_state(s0)
+    if args.start:
+        w.step_graph(nsub * args.start)
     host = w.bodies()
     h2d = d2h = host.nbytes
+    if d:
+        d[0].barrier()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         w.set_bodies(host)
         w.step_graph(nsub)
         host = w.bodies()
     e2e_s = time.perf_counter() - t0
-    e2e = ndyn * args.e2e_steps / e2e_s
+    e2e = ndyn * e2e_steps / e2e_s
     if d:
         import torch
 
         t = torch.tensor([e2e_s], device=f"cuda:{device}")
         d[0].all_reduce(t, op=d[0].ReduceOp.MAX)
-        e2e = ndyn_total * args.e2e_steps / float(t.item())
-    # ---- per-phase profile: roofline of the primal kernel --------------------
-    phases, info = w.profile_substep()
-    roof = roofline.primal_roofline(phases, info, hbm_peak())
+        e2e = ndyn_total * e2e_steps / float(t.item())
+    w.close()
     if rank != 0:
         return 0
-    # ---- plain: one scene per launch sequence, bounded sample ----------------
+    # ---- plain: one scene per world, same trajectory, bounded sample --------
     plain = None
     if args.plain_scenes > 0:
         plain = plain_rate(bodies_all, offs_all, params, nsub, args)
     cb = None
     if args.cpu_per_core > 0 and world == 1:
-        cb = cpu_baseline(bodies_all, offs_all, params, nsub, preroll=args.preroll, steps=4,
+        cb = cpu_baseline(bodies_all, offs_all, params, nsub, start=args.start, steps=args.steps,
                           per_core=args.cpu_per_core)
-    c = w.counters()
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, no dataset)",
         "config": {"workload": "batched_4096", "scenes": args.scenes, "dynamic_bodies": ndyn_total,
-                   "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations, "preroll_steps": args.preroll,
+                   "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations,
+                   "trajectory": f"steps {args.start}..{args.start + args.steps} from the initial drop",
                    "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
                    "graph": True, "precision": "exact" if args.exact else "fast",
                    "primal_launch": {"lanes": tuned[0][0], "block": tuned[0][1], "min_blocks_per_sm": tuned[0][2],
-                                     "by_work": tuned[0][3],
-                                     "trials_ms": [[list(c), round(m, 3)] for c, m in tuned[1]]}
-                   if tuned else {"lanes": args.lanes or 1, "block": args.block}},
+                                     "by_work": tuned[0][3], "tuned_at_step": args.tune_at,
+                                     "trials_ms": [[list(cd), round(m, 3)] for cd, m in tuned[1]]}
+                   if tuned else {"lanes": args.lanes if args.lanes is not None else 1, "block": args.block}},
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "steps": args.e2e_steps},
+                "steps": e2e_steps},
         "gpu_launches": int(nodes * nsub * args.steps),
         "roofline": roof,
         "cpu_baseline": cb,
@@ -303,48 +359,49 @@ def run_ours(args):
         "plain_one_scene": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "phases_ms_per_substep": phases,
-        "counters": {"candidates": c.candidates, "pairs": c.pairs, "points": c.points, "colours": c.colours, "sleeping": c.sleeping,
-                     "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits, "ccd_left": c.timeouts},
+        "counters_at_end": {"candidates": c.candidates, "pairs": c.pairs, "points": c.points, "colours": c.colours,
+                            "sleeping": c.sleeping, "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits,
+                            "ccd_left": c.timeouts},
     }
     print(json.dumps(line))
     return 0
 
 
 def plain_rate(bodies, offs, params, nsub, args):
-    """Body-steps/s stepping scenes one world (one launch sequence) at a time."""
+    """Body-steps/s stepping sampled scenes one world (one launch sequence) at a time."""
     from ornis_gb300.avbd import AvbdWorld
 
     S = len(offs) - 1
     rng = np.random.default_rng(777)
     pick = rng.choice(S, size=min(args.plain_scenes, S), replace=False)
-    worlds = [AvbdWorld(params, bodies=bodies[offs[s]:offs[s + 1]]) for s in pick]
-    for wd in worlds:
-        for _ in range(args.preroll):
-            wd.step_graph(nsub)
     tot_ms = 0.0
     body_steps = 0
-    for wd, s in zip(worlds, pick):
-        tot_ms += wd.step_timed(nsub * args.plain_steps, use_graph=False)
-        body_steps += scenes.dynamic_count(bodies[offs[s]:offs[s + 1]]) * args.plain_steps
-    for wd in worlds:
+    for s in pick:
+        sc = bodies[offs[s]:offs[s + 1]]
+        wd = AvbdWorld(params, bodies=sc)
+        if args.start:
+            wd.step_fixed(nsub * args.start)
+        tot_ms += wd.step_timed(nsub * args.steps, use_graph=False)
+        body_steps += scenes.dynamic_count(sc) * args.steps
         wd.close()
     return {"value": body_steps / (tot_ms / 1e3), "unit": "body-steps/s", "scenes_sampled": int(len(pick)),
-            "steps": args.plain_steps, "how": "one world per scene, plain launches, scenes stepped one after another"}
+            "steps": args.steps,
+            "how": "one world per scene, plain launches, each scene over the same steps, device time summed"}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=240)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
-    ap.add_argument("--preroll", type=int, default=60)
-    ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--plain-scenes", type=int, default=32)
-    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--start", type=int, default=0, help="untimed steps before the timed region")
+    ap.add_argument("--tune-at", type=int, default=150, help="step at which the primal launch is autotuned")
+    ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps")
+    ap.add_argument("--plain-scenes", type=int, default=16)
     ap.add_argument("--cpu-per-core", type=int, default=3)
-    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=None, help="fixed primal launch shape instead of autotuning")
     ap.add_argument("--block", type=int, default=128)
     ap.add_argument("--exact", action="store_true", help="exact build of the iteration kernels")
     ap.add_argument("--profile-region", type=int, default=0,

@@ -174,6 +174,32 @@ typedef struct AvbdCounters {
     uint64_t timeouts;     /* bounded device waits that gave up, cumulative   */
 } AvbdCounters;
 
+/* Contact transition of a body pair (ContactEvent / ContactEventKind,
+ * crates/physics/src/trigger.rs; emitted by avbd/mod.rs:1606-1669 and the
+ * CCD hit pass mod.rs:935-960, :1126-1136).  body_a < body_b.  Begin / End:
+ * the pair's deepest point crossed CONTACT_BEGIN_SLOP (5 mm) between two
+ * emitting substeps.  Hit: a pair that began touching, or a swept body's
+ * time-of-impact clamp, with a closing speed above CONTACT_HIT_THRESHOLD
+ * (1 m/s); point, normal (A toward B) and approach_speed are set for hits. */
+#define AVBD_CONTACT_BEGIN 0
+#define AVBD_CONTACT_END 1
+#define AVBD_CONTACT_HIT 2
+typedef struct AvbdContactEvent {
+    uint32_t body_a;
+    uint32_t body_b;
+    uint32_t kind;
+    float point[3];
+    float normal[3];
+    float approach_speed;
+} AvbdContactEvent;
+
+/* Trigger overlap transition (TriggerEvent, trigger.rs:20-36). */
+typedef struct AvbdTriggerEvent {
+    uint32_t body_a;
+    uint32_t body_b;
+    uint32_t entered; /* 1 = Entered, 0 = Exited */
+} AvbdTriggerEvent;
+
 typedef struct AvbdWorld AvbdWorld;
 
 /* ---- world lifecycle ----------------------------------------------------- */

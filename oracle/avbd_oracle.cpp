@@ -24,7 +24,9 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <set>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../include/ornis_avbd.h"
@@ -61,6 +63,8 @@ struct K {
     static constexpr float MIN_TOI_DISP_LENGTH = 1e-9f;
     static constexpr float SPIN_REST_EPS = 1e-9f;
     static constexpr float CCD_BOUNCE_SPEED = 1.0f;
+    static constexpr float CONTACT_BEGIN_SLOP = 0.005f;    // trigger.rs:68
+    static constexpr float CONTACT_HIT_THRESHOLD = 1.0f;   // trigger.rs:63
     static constexpr float DEGENERATE_LEN2 = 1e-12f;
     static constexpr float NEAR_ZERO = 1e-9f;
     static constexpr float SHAPE_TOUCH = 1e-3f;
@@ -728,6 +732,14 @@ template <class T> struct Engine {
     uint64_t ncolours = 0;
     // adjacency (same order as the pair vector) for the non-faithful sweep
     std::vector<std::vector<uint32_t>> adj_pairs, adj_joints;
+    // events (mod.rs:425-464 event state, :1606-1669 emit_events)
+    using Key = std::pair<uint32_t, uint32_t>;
+    std::set<Key> prev_touch, prev_trigger, trig_now;
+    std::vector<AvbdContactEvent> cev;
+    std::vector<AvbdTriggerEvent> tev;
+    std::vector<V3<T>> pre_vel;
+    std::vector<AvbdContactEvent> ccd_ev;  // this substep's swept hits (mod.rs:935-960)
+    int emit_period = 0;                   // 0: the last substep of each step call emits
 
     bool solvable(uint32_t h) const { return bodies[h].type == AVBD_BODY_DYNAMIC && bodies[h].inv_mass > T(0); }
 
@@ -1032,6 +1044,10 @@ template <class T> struct Engine {
             }
             return next;
         };
+        // trigger overlaps of this substep (rows.rs:802-807)
+        trig_now.clear();
+        for (auto& d : disc)
+            if (d.trigger && d.sgn <= T(0)) trig_now.insert({d.ia, d.ib});
         if (mode == REFERENCE) {
             std::vector<uint8_t> seen(pairs.size(), 0);
             for (auto& d : disc) {
@@ -1469,7 +1485,7 @@ template <class T> struct Engine {
             V3<T> dir = disp / L;
             bool have = false;
             T best_t = T(0);
-            V3<T> best_n{};
+            V3<T> best_n{}, best_p{};
             uint32_t best_h = 0;
             const Body<T>& mb = bodies[h];
             for (uint32_t o = 0; o < n; o++) {
@@ -1478,21 +1494,35 @@ template <class T> struct Engine {
                 ShapeRef<T> tgt = sref(bodies[o]);
                 T t = T(0);
                 bool hit = false;
-                V3<T> hn{};
+                V3<T> hn{}, hp{};
                 for (int it = 0; it < 24; it++) {
                     ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot};
                     Dist<T> d = shape_distance(mv, tgt);
                     if (d.dist <= C<T>(K::SHAPE_TOUCH)) {
-                        if (t > T(0)) { hit = true; hn = normalize_or(d.pa - d.pb, -dir); }
+                        if (t > T(0)) { hit = true; hn = normalize_or(d.pa - d.pb, -dir); hp = d.pb; }
                         break;
                     }
                     t += d.dist - C<T>(K::SHAPE_TOUCH) * C<T>(K::HALF);
                     if (t >= L) break;
                 }
-                if (hit && (!have || t < best_t)) { have = true; best_t = t; best_n = hn; best_h = o; }
+                if (hit && (!have || t < best_t)) { have = true; best_t = t; best_n = hn; best_p = hp; best_h = o; }
             }
             if (!have) continue;
             ccd_hits++;
+            {   // a swept impact is a hit event (mod.rs:946-960)
+                T approach = -dot(pre_vel[h] - pre_vel[best_h], best_n);
+                if (approach > C<T>(K::CONTACT_HIT_THRESHOLD)) {
+                    AvbdContactEvent e{};
+                    V3<T> nn = h < best_h ? -best_n : best_n;
+                    e.body_a = std::min(h, best_h);
+                    e.body_b = std::max(h, best_h);
+                    e.kind = AVBD_CONTACT_HIT;
+                    e.point[0] = (float)best_p.x; e.point[1] = (float)best_p.y; e.point[2] = (float)best_p.z;
+                    e.normal[0] = (float)nn.x; e.normal[1] = (float)nn.y; e.normal[2] = (float)nn.z;
+                    e.approach_speed = (float)approach;
+                    ccd_ev.push_back(e);
+                }
+            }
             T l2 = fmx(L, C<T>(K::MIN_TOI_DISP_LENGTH));
             T frac = fclamp(best_t / l2, T(0), T(1));
             T e = fmn(bodies[h].restitution, bodies[best_h].restitution);
@@ -1508,11 +1538,79 @@ template <class T> struct Engine {
         }
     }
 
-    // ---- one fixed substep (mod.rs:846-1143) ----
-    void step_inner() {
+    // ---- events (mod.rs:1606-1669) ----
+    void emit_events() {
+        // trigger transitions: symmetric difference in key order
+        {
+            auto i = trig_now.begin(), j = prev_trigger.begin();
+            while (i != trig_now.end() || j != prev_trigger.end()) {
+                if (j == prev_trigger.end() || (i != trig_now.end() && *i < *j)) {
+                    tev.push_back(AvbdTriggerEvent{i->first, i->second, 1u});
+                    ++i;
+                } else if (i == trig_now.end() || *j < *i) {
+                    tev.push_back(AvbdTriggerEvent{j->first, j->second, 0u});
+                    ++j;
+                } else {
+                    ++i;
+                    ++j;
+                }
+            }
+            prev_trigger = trig_now;
+        }
+        std::set<Key> touch_now;
+        std::vector<AvbdContactEvent> hits;
+        for (const Pair<T>& p : pairs) {
+            const Body<T>& a = bodies[p.a];
+            const Body<T>& b = bodies[p.b];
+            T deepest = T(0);
+            V3<T> witness = (a.pos + b.pos) * C<T>(K::HALF);
+            for (const Point<T>& pt : p.points) {
+                V3<T> pa = a.pos + qrot(a.rot, pt.ra);
+                V3<T> pb = b.pos + qrot(b.rot, pt.rb);
+                T gap = dot(p.n, pa - pb);
+                if (-gap > deepest) { deepest = -gap; witness = pa; }
+            }
+            if (deepest > C<T>(K::CONTACT_BEGIN_SLOP)) {
+                touch_now.insert({p.a, p.b});
+                if (!prev_touch.count({p.a, p.b})) {
+                    T approach = -dot(pre_vel[p.a] - pre_vel[p.b], p.n);
+                    if (approach > C<T>(K::CONTACT_HIT_THRESHOLD)) {
+                        AvbdContactEvent e{};
+                        e.body_a = p.a; e.body_b = p.b; e.kind = AVBD_CONTACT_HIT;
+                        e.point[0] = (float)witness.x; e.point[1] = (float)witness.y; e.point[2] = (float)witness.z;
+                        e.normal[0] = (float)-p.n.x; e.normal[1] = (float)-p.n.y; e.normal[2] = (float)-p.n.z;
+                        e.approach_speed = (float)approach;
+                        hits.push_back(e);
+                    }
+                }
+            }
+        }
+        auto i = touch_now.begin(), j = prev_touch.begin();
+        while (i != touch_now.end() || j != prev_touch.end()) {
+            AvbdContactEvent e{};
+            if (j == prev_touch.end() || (i != touch_now.end() && *i < *j)) {
+                e.body_a = i->first; e.body_b = i->second; e.kind = AVBD_CONTACT_BEGIN;
+                cev.push_back(e);
+                ++i;
+            } else if (i == touch_now.end() || *j < *i) {
+                e.body_a = j->first; e.body_b = j->second; e.kind = AVBD_CONTACT_END;
+                cev.push_back(e);
+                ++j;
+            } else {
+                ++i;
+                ++j;
+            }
+        }
+        for (auto& e : hits) cev.push_back(e);
+        prev_touch.swap(touch_now);
+    }
+
+    // ---- one fixed substep (mod.rs:846-1143); `emit`: the step's last substep ----
+    void step_inner(bool emit = true) {
         ensure_scratch();
         wake_joint_motion();
         uint32_t n = (uint32_t)bodies.size();
+        ccd_ev.clear();
         for (uint32_t h = 0; h < n; h++) {
             if (!solvable(h)) continue;
             Body<T>& b = bodies[h];
@@ -1525,6 +1623,8 @@ template <class T> struct Engine {
             b.torque = VZERO<T>();
             b.angvel = b.angvel + mat3_vec(inv, tq) * dt;
         }
+        pre_vel.resize(n);
+        for (uint32_t h = 0; h < n; h++) pre_vel[h] = bodies[h].vel;  // mod.rs:874-876
         if (prm.enable_ccd) ccd_pass();
         generate_pairs();
         wake_joint_motion();
@@ -1609,8 +1709,24 @@ template <class T> struct Engine {
             for (uint32_t h = 0; h < n; h++)
                 if (freeze[h] && !asleep[h]) sleep_body(h);
         }
+        {
+            size_t ev_start = cev.size();
+            if (emit) emit_events();
+            // swept impacts not already reported as hits this substep (mod.rs:1126-1136)
+            for (const AvbdContactEvent& e : ccd_ev) {
+                bool dup = false;
+                for (size_t i = ev_start; i < cev.size(); i++)
+                    if (cev[i].body_a == e.body_a && cev[i].body_b == e.body_b && cev[i].kind == AVBD_CONTACT_HIT)
+                        dup = true;
+                if (!dup) cev.push_back(e);
+            }
+        }
         for (uint32_t h = 0; h < n; h++) { prev_pos[h] = bodies[h].pos; prev_rot[h] = bodies[h].rot; }
         steps++;
+    }
+    void step_fixed(int nsub) {
+        for (int i = 0; i < nsub; i++)
+            step_inner(emit_period > 0 ? (i + 1) % emit_period == 0 : i == nsub - 1);
     }
 
     void step(float host_dt) {  // mod.rs:1212-1235
@@ -1621,7 +1737,7 @@ template <class T> struct Engine {
         while (time_debt >= sd && k < prm.max_substeps) {
             time_debt -= sd;
             k++;
-            step_inner();
+            step_inner(time_debt < sd || k == prm.max_substeps);
         }
     }
 
@@ -1759,8 +1875,32 @@ int oracle_step(OracleWorld* w, float dt) {
     return AVBD_OK;
 }
 int oracle_step_fixed(OracleWorld* w, int32_t nsub) {
-    DISPATCH(w, for (int i = 0; i < nsub; i++) E.step_inner());
+    DISPATCH(w, E.step_fixed(nsub));
     return AVBD_OK;
+}
+// Substeps per emitting step for step_fixed: 0 = only the last substep of a call.
+int oracle_set_emit_period(OracleWorld* w, int32_t period) {
+    DISPATCH(w, E.emit_period = period < 0 ? 0 : period);
+    return AVBD_OK;
+}
+// Move up to `cap` queued events out (oldest first); returns how many were moved.
+uint32_t oracle_drain_contact_events(OracleWorld* w, AvbdContactEvent* out, uint32_t cap) {
+    uint32_t n = 0;
+    DISPATCH(w, {
+        n = (uint32_t)std::min<size_t>(cap, E.cev.size());
+        std::copy(E.cev.begin(), E.cev.begin() + n, out);
+        E.cev.erase(E.cev.begin(), E.cev.begin() + n);
+    });
+    return n;
+}
+uint32_t oracle_drain_trigger_events(OracleWorld* w, AvbdTriggerEvent* out, uint32_t cap) {
+    uint32_t n = 0;
+    DISPATCH(w, {
+        n = (uint32_t)std::min<size_t>(cap, E.tev.size());
+        std::copy(E.tev.begin(), E.tev.begin() + n, out);
+        E.tev.erase(E.tev.begin(), E.tev.begin() + n);
+    });
+    return n;
 }
 uint32_t oracle_body_count(OracleWorld* w) {
     uint32_t n = 0;

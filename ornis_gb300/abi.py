@@ -164,11 +164,34 @@ def _dtype_of(struct):
     return dt
 
 
+class AvbdContactEvent(C.Structure):
+    _fields_ = [
+        ("body_a", C.c_uint32),
+        ("body_b", C.c_uint32),
+        ("kind", C.c_uint32),
+        ("point", C.c_float * 3),
+        ("normal", C.c_float * 3),
+        ("approach_speed", C.c_float),
+    ]
+
+
+class AvbdTriggerEvent(C.Structure):
+    _fields_ = [
+        ("body_a", C.c_uint32),
+        ("body_b", C.c_uint32),
+        ("entered", C.c_uint32),
+    ]
+
+
+CONTACT_BEGIN, CONTACT_END, CONTACT_HIT = 0, 1, 2
+
 BODY_DTYPE = _dtype_of(AvbdBody)
 AUX_DTYPE = _dtype_of(AvbdBodyAux)
 PAIR_DTYPE = _dtype_of(AvbdPairState)
 POINT_DTYPE = _dtype_of(AvbdPointState)
 JOINT_STATE_DTYPE = _dtype_of(AvbdJointState)
+CONTACT_EVENT_DTYPE = _dtype_of(AvbdContactEvent)
+TRIGGER_EVENT_DTYPE = _dtype_of(AvbdTriggerEvent)
 
 
 def ptr(arr, ctype=C.c_void_p):

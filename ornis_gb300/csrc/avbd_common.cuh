@@ -1,5 +1,8 @@
 // avbd_common.cuh — small device helpers shared by the pipeline phases.
 #pragma once
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
 #include "avbd_kernels.h"
 #include "avbd_rows.cuh"
 #include "avbd_shapes.cuh"
@@ -12,6 +15,33 @@ static inline unsigned nblk(size_t n, int b) { return (unsigned)((n + (size_t)b 
 static inline unsigned gsz(size_t cap, int b) {
     unsigned g = nblk(cap, b);
     return g < 152u * 16u ? g : 152u * 16u;
+}
+
+// Warp-aggregated counters: the lanes that call together share one atomic, so
+// a counter bumped by millions of threads (candidates, points) is not
+// serialised at one L2 address.  Call from the lanes that add, in any branch.
+static __device__ __forceinline__ uint32_t agg_inc(uint32_t* ctr) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(ctr, (uint32_t)g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+// Same for a per-key counter arr[key]: lanes with equal keys share one atomic
+// (a half-space is the A side of every candidate it has in its scene).
+static __device__ __forceinline__ uint32_t agg_inc_at(uint32_t* arr, uint32_t key) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group s = cg::labeled_partition(g, key);
+    uint32_t base = 0;
+    if (s.thread_rank() == 0) base = atomicAdd(&arr[key], (uint32_t)s.size());
+    return s.shfl(base, 0) + s.thread_rank();
+}
+static __device__ __forceinline__ void agg_add(uint32_t* ctr, uint32_t v) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t s = cg::reduce(g, v, cg::plus<uint32_t>());
+    if (g.thread_rank() == 0 && s) atomicAdd(ctr, s);
 }
 
 static __device__ __forceinline__ bool is_dynamic(const DW& w, uint32_t h) {

@@ -11,7 +11,8 @@
 namespace avbd {
 
 struct Tune {
-    int primal_lanes = 1;        // lanes cooperating on one body in the primal (1, 4, 8, 16, 32)
+    int primal_lanes = 1;        // lanes cooperating on one body in the primal (1, 4, 8, 16, 32);
+                                 // 0: split primal (per (pair, side) rows, then per-body sums and solve)
     int primal_block = 128;      // threads per block of the primal kernel
     int primal_minb = 4;         // resident blocks per SM the thread-per-body primal is built for
     int small_scene_max = 2048;  // scenes up to this many bodies use the one-CTA broadphase
@@ -57,7 +58,8 @@ void launch_wake_apply(const DW& w, cudaStream_t st);
     void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st);                   \
     void launch_finish_substep(const DW& w, cudaStream_t st);                                             \
     void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st); \
-    void launch_dual(const DW& w, cudaStream_t st);
+    void launch_dual(const DW& w, cudaStream_t st);                                                     \
+    void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st);
 namespace exact {
 AVBD_SOLVE_DECLS
 }
@@ -75,6 +77,10 @@ inline void launch_finish_substep(const DW& w, const Tune& t, cudaStream_t st) {
 inline void launch_primal_colour(const DW& w, const Tune& t, int c, uint32_t maxb, cudaStream_t st) {
     if (t.fast) fast::launch_primal_colour(w, t, c, maxb, st);
     else exact::launch_primal_colour(w, t, c, maxb, st);
+}
+inline void launch_solve_prep(const DW& w, const Tune& t, cudaStream_t st) {
+    if (t.fast) fast::launch_solve_prep(w, t, st);
+    else exact::launch_solve_prep(w, t, st);
 }
 inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
     if (t.fast) fast::launch_dual(w, st);

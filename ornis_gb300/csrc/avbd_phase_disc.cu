@@ -92,7 +92,7 @@ static __device__ __forceinline__ void k_disc_filter_one(const DW& w, uint32_t c
     uint2 ab = w.cand[c];
     Disc d = discover(w, ab.x, ab.y, false);
     w.keep[c] = d.keep;
-    if (d.keep) atomicAdd(&w.cnt[ab.x], 1u);
+    if (d.keep) agg_inc_at(w.cnt, ab.x);
 }
 __global__ void k_disc_filter(DW w) {
     if (aborted(w)) return;
@@ -104,7 +104,7 @@ __global__ void k_disc_filter(DW w) {
 static __device__ __forceinline__ void k_place_one(const DW& w, uint32_t c) {
     if (!w.keep[c]) return;
     uint32_t a = w.cand[c].x;
-    w.slot_c[w.offA[a] + atomicAdd(&w.cur[a], 1u)] = c;
+    w.slot_c[w.offA[a] + agg_inc_at(w.cur, a)] = c;
 }
 __global__ void k_place(DW w) {
     if (aborted(w)) return;
@@ -141,11 +141,12 @@ __global__ void k_sort_slots(DW w) {
 static __device__ __forceinline__ bool box_pair(const DW& w, uint2 ab) {
     return info_shape(w.info[ab.x]) == AVBD_SHAPE_BOX && info_shape(w.info[ab.y]) == AVBD_SHAPE_BOX;
 }
-// Box-box witnesses are computed ahead by one warp per pair (the 15 SAT axes
-// and the 160 corner/edge tests spread over the lanes) into bd_pa / bd_pb;
-// the per-pair build below then reads them.
+// Box-box witnesses are computed ahead, one thread per box pair, into bd_pa /
+// bd_pb; the per-pair build below then reads them.  Every box pair runs the
+// same fixed loops (15 SAT axes, 16 corner and 144 edge tests), so a warp of
+// box pairs stays converged and the kernel is ALU-bound with few loads.
 static __device__ __forceinline__ void k_collect_boxes_one(const DW& w, uint32_t p) {
-    if (box_pair(w, w.cand[w.slot_c[p]])) w.boxlist[atomicAdd(&w.ctr[C_BOXPAIRS], 1u)] = p;
+    if (box_pair(w, w.cand[w.slot_c[p]])) w.boxlist[agg_inc(&w.ctr[C_BOXPAIRS])] = p;
 }
 __global__ void k_collect_boxes(DW w) {
     if (aborted(w)) return;
@@ -156,18 +157,14 @@ __global__ void k_collect_boxes(DW w) {
 __global__ void k_box_witness(DW w) {
     if (aborted(w)) return;
     const uint32_t nbox = w.ctr[C_BOXPAIRS];
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = warp; i < nbox; i += nwarps) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbox; i += gridDim.x * blockDim.x) {
         uint32_t p = w.boxlist[i];
         uint2 ab = w.cand[w.slot_c[p]];
         Shape sa = shape_of(w, ab.x), sb = shape_of(w, ab.y);
         float sat;
-        Dist d = box_box_warp(sa.pos, sa.rot, sa.p, sb.pos, sb.rot, sb.p, &sat);
-        if ((threadIdx.x & 31) == 0) {
-            w.bd_pa[p] = st3(d.pa, d.dist);
-            w.bd_pb[p] = st3(d.pb, sat);
-        }
+        Dist d = box_box(sa.pos, sa.rot, sa.p, sb.pos, sb.rot, sb.p, &sat);
+        w.bd_pa[p] = st3(d.pa, d.dist);
+        w.bd_pb[p] = st3(d.pb, sat);
     }
 }
 static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2 ab, const Disc& d);
@@ -320,7 +317,7 @@ static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2
         }
         w.q_matched[q] = m;
     }
-    atomicAdd(&w.ctr[C_POINTS], (uint32_t)nf);
+    agg_add(&w.ctr[C_POINTS], (uint32_t)nf);
 }
 __global__ void k_disc_build(DW w) {
     if (aborted(w)) return;
@@ -345,7 +342,7 @@ void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
     k_sort_slots<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_clear_flags<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_collect_boxes<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
-    k_box_witness<<<gsz((size_t)w.pair_cap * 32, 128), 128, 0, st>>>(w);
+    k_box_witness<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
     k_disc_build<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
 }
 
@@ -392,6 +389,8 @@ __global__ void k_sortB(DW w) {
         }
         w.listB[k] = v;
     }
+    if (w.posB)
+        for (uint32_t i = s0; i < s1; i++) w.posB[w.listB[i]] = i;
 }
 // mod.rs:993-1018 (step-start pose, inertial target) and :1043-1049 (x <- y)
 __global__ void k_targets(DW w) {

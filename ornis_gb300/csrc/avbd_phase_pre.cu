@@ -129,7 +129,7 @@ __global__ void k_aabb(DW w) {
 
 static __device__ __forceinline__ void emit_candidate(const DW& w, uint32_t a, uint32_t b) {
     uint32_t lo = min(a, b), hi = max(a, b);
-    uint32_t slot = atomicAdd(&w.ctr[C_CAND], 1u);
+    uint32_t slot = agg_inc(&w.ctr[C_CAND]);
     if (slot < w.cand_cap) w.cand[slot] = make_uint2(lo, hi);
     else atomicOr(&w.ctr[C_ERR], (uint32_t)E_CAND_OVERFLOW);
 }
@@ -302,8 +302,8 @@ __global__ void k_ccd_init(DW w) {
     w.ccd_state[h] = 0;
     w.ccd_recompute[h] = 0;
     if (w.fast[h]) {
-        atomicAdd(&w.ctr[C_FAST], 1u);
-        atomicAdd(&w.ctr[C_CCD_PENDING], 1u);
+        agg_inc(&w.ctr[C_FAST]);
+        agg_inc(&w.ctr[C_CCD_PENDING]);
     }
 }
 // first = 1: every mover casts against its candidates at the step-top poses
@@ -354,7 +354,7 @@ static __device__ void ccd_apply(const DW& w, uint32_t h) {
         }
         wake_body(w, o);
         w.sleep_timer[h] = 0.0f;
-        atomicAdd(&w.ctr[C_CCD], 1u);
+        agg_inc(&w.ctr[C_CCD]);
         moved = true;
     }
     w.ccd_state[h] = moved ? 2 : 1;

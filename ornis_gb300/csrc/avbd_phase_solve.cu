@@ -289,6 +289,125 @@ __global__ void k_primal_lanes(DW w, int colour) {
     apply_solve(w, h, t);
 }
 
+// ---- split primal -------------------------------------------------------------------
+// Per colour, phase 1 (k_side_rows) computes for every (pair, side) whose body
+// has this colour the pair's rows for that body, summed over its points, and
+// stores the 27 numbers in the incidence slot of that body; phase 2
+// (k_side_solve) gives each body of the colour its inertial block plus its
+// slots in incidence order (B-side pairs ascending, then A-side pairs
+// ascending), then its joints, and solves.  Phase 1 has one thread per
+// (pair, side) instead of one per body: several times more threads and short
+// dependency chains, which is what the latency-bound per-body loop lacks once
+// bodies touch many others.  Rows are summed per pair before they join the
+// body's sum, so results equal the thread-per-body kernel's within rounding.
+// Slots: body h owns [offA[h] + offB[h], offA[h+1] + offB[h+1]), B sides first;
+// the A side of pair p is slot p + offB[a+1], the B side slot offA[b] + posB[p].
+constexpr int SIDE_BLOCK = 256;
+__global__ void k_side_count(DW w) {
+    if (aborted_solve(w)) return;
+    __shared__ uint32_t hist[MAX_COLOURS];
+    for (int c = threadIdx.x; c < MAX_COLOURS; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint2 ab = w.p_ab[p];
+        int ca = w.colour[ab.x], cb = w.colour[ab.y];
+        if (ca >= 0) atomicAdd(&hist[ca], 1u);
+        if (cb >= 0) atomicAdd(&hist[cb], 1u);
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < MAX_COLOURS; c += blockDim.x)
+        if (hist[c]) atomicAdd(&w.side_cnt[MAX_COLOURS + 1 + c], hist[c]);
+}
+// one thread: list starts from the per-colour totals; cursors start there
+__global__ void k_side_starts(DW w) {
+    if (aborted_solve(w) || threadIdx.x != 0) return;
+    uint32_t acc = 0;
+    for (int c = 0; c < MAX_COLOURS; c++) {
+        uint32_t t = w.side_cnt[MAX_COLOURS + 1 + c];
+        w.side_cnt[c] = acc;
+        w.side_cnt[MAX_COLOURS + 1 + c] = acc;
+        acc += t;
+    }
+    w.side_cnt[MAX_COLOURS] = acc;
+}
+// Entries are placed with block-aggregated reservations; their order inside a
+// colour is irrelevant (each entry writes its own slot).
+__global__ void k_side_place(DW w) {
+    if (aborted_solve(w)) return;
+    __shared__ uint32_t cnt[MAX_COLOURS], base[MAX_COLOURS];
+    const uint32_t n = n_pairs(w);
+    for (uint32_t p0 = blockIdx.x * blockDim.x; p0 < n; p0 += gridDim.x * blockDim.x) {
+        for (int c = threadIdx.x; c < MAX_COLOURS; c += blockDim.x) cnt[c] = 0;
+        __syncthreads();
+        uint32_t p = p0 + threadIdx.x;
+        int ca = -1, cb = -1;
+        if (p < n) {
+            uint2 ab = w.p_ab[p];
+            ca = w.colour[ab.x];
+            cb = w.colour[ab.y];
+        }
+        uint32_t ra = ca >= 0 ? atomicAdd(&cnt[ca], 1u) : 0u;
+        uint32_t rb = cb >= 0 ? atomicAdd(&cnt[cb], 1u) : 0u;
+        __syncthreads();
+        for (int c = threadIdx.x; c < MAX_COLOURS; c += blockDim.x)
+            base[c] = cnt[c] ? atomicAdd(&w.side_cnt[MAX_COLOURS + 1 + c], cnt[c]) : 0u;
+        __syncthreads();
+        if (ca >= 0) w.side_list[base[ca] + ra] = p * 2u + 1u;
+        if (cb >= 0) w.side_list[base[cb] + rb] = p * 2u;
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
+    if (aborted_solve(w)) return;
+    const uint32_t s0 = w.side_cnt[colour], s1 = w.side_cnt[colour + 1];
+    for (uint32_t i = s0 + blockIdx.x * blockDim.x + threadIdx.x; i < s1; i += gridDim.x * blockDim.x) {
+        uint32_t e = w.side_list[i];
+        uint32_t p = e >> 1;
+        bool side_a = (e & 1u) != 0u;
+        PairCtx c;
+        load_ctx(w, p, c);
+        Sys s;
+#pragma unroll
+        for (int k = 0; k < 21; k++) s.h[k] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) s.r[k] = 0.0f;
+        for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, side_a, s);
+        uint32_t slot = side_a ? p + w.offB[c.a + 1] : w.offA[c.b] + w.posB[p];
+        float4* o = w.contrib + (size_t)slot * 7;
+        o[0] = make_float4(s.h[0], s.h[1], s.h[2], s.h[3]);
+        o[1] = make_float4(s.h[4], s.h[5], s.h[6], s.h[7]);
+        o[2] = make_float4(s.h[8], s.h[9], s.h[10], s.h[11]);
+        o[3] = make_float4(s.h[12], s.h[13], s.h[14], s.h[15]);
+        o[4] = make_float4(s.h[16], s.h[17], s.h[18], s.h[19]);
+        o[5] = make_float4(s.h[20], s.r[0], s.r[1], s.r[2]);
+        o[6] = make_float4(s.r[3], s.r[4], s.r[5], 0.0f);
+    }
+}
+__global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
+    if (aborted_solve(w)) return;
+    const uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
+    for (uint32_t i = c0 + blockIdx.x * blockDim.x + threadIdx.x; i < c1; i += gridDim.x * blockDim.x) {
+        uint32_t h = w.col_list[i];
+        Sys s;
+        inertial_block(w, h, s);
+        const uint32_t k0 = w.offA[h] + w.offB[h], k1 = w.offA[h + 1] + w.offB[h + 1];
+        for (uint32_t k = k0; k < k1; k++) {
+            const float4* o = w.contrib + (size_t)k * 7;
+            float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];
+            s.h[0] += v0.x; s.h[1] += v0.y; s.h[2] += v0.z; s.h[3] += v0.w;
+            s.h[4] += v1.x; s.h[5] += v1.y; s.h[6] += v1.z; s.h[7] += v1.w;
+            s.h[8] += v2.x; s.h[9] += v2.y; s.h[10] += v2.z; s.h[11] += v2.w;
+            s.h[12] += v3.x; s.h[13] += v3.y; s.h[14] += v3.z; s.h[15] += v3.w;
+            s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
+            s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
+            s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
+        }
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+        apply_solve(w, h, s);
+    }
+}
+
 // ---- dual (joints_ext.rs:464-573 contacts, :574-896 Ball/Revolute) ----
 // One thread per pair: the pair context is built once for all its points.
 static __device__ __forceinline__ void dual_point(const DW& w, const PairCtx& c, V3 t1, V3 t2, uint32_t q) {
@@ -416,9 +535,20 @@ __global__ void k_dual_joints(DW w) {
     w.j_pen_a[j] = make_float4(pena[0], pena[1], pena[2], 0.0f);
 }
 
+void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st) {
+    if (tune.primal_lanes != 0) return;
+    k_zero_u32<<<1, 256, 0, st>>>(w.side_cnt, 2 * MAX_COLOURS + 2);
+    k_side_count<<<gsz(w.pair_cap, SIDE_BLOCK), SIDE_BLOCK, 0, st>>>(w);
+    k_side_starts<<<1, 32, 0, st>>>(w);
+    k_side_place<<<gsz(w.pair_cap, SIDE_BLOCK), SIDE_BLOCK, 0, st>>>(w);
+}
 void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
     int bs = tune.primal_block;
     switch (tune.primal_lanes) {
+        case 0:
+            k_side_rows<<<gsz((size_t)w.pair_cap * 2, 128), 128, 0, st>>>(w, c);
+            k_side_solve<<<gsz(max_bodies, 128), 128, 0, st>>>(w, c);
+            break;
         case 1:
             // occupancy variants of the thread-per-body kernel: 4, 6 or 8
             // resident 128-thread blocks per SM (128, 80 or 64 registers)
@@ -547,7 +677,7 @@ __global__ void k_freeze_apply(DW w, int sleep_on) {
             w.inertia[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             w.asleep[h] = 1;
         }
-        if (w.asleep[h]) atomicAdd(&w.ctr[C_SLEEP], 1u);
+        if (w.asleep[h]) agg_inc(&w.ctr[C_SLEEP]);
     }
     w.prev_pos[h] = w.pos[h];
     w.prev_rot[h] = w.rot[h];

@@ -218,6 +218,10 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     }
     w.offB = m.get<uint32_t>(N + 1);
     w.listB = m.get<uint32_t>(cand_cap);
+    w.posB = m.get<uint32_t>(cand_cap);
+    w.side_list = m.get<uint32_t>((size_t)cand_cap * 2);
+    w.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
+    w.contrib = W->tune.primal_lanes == 0 ? m.get<float4>((size_t)cand_cap * 2 * 7) : nullptr;
     w.cand = m.get<uint2>(cand_cap);
     w.keep = m.get<uint8_t>(cand_cap);
     w.cnt = m.get<uint32_t>(N + 1);
@@ -633,6 +637,7 @@ static void enqueue_front(AvbdWorld* W) {
 }
 static void enqueue_back(AvbdWorld* W, int ncol) {
     const DW& w = W->w;
+    launch_solve_prep(w, W->tune, W->st);
     for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
     launch_finish_substep(w, W->tune, W->st);
 }
@@ -1160,11 +1165,18 @@ int avbd_set_occupancy(AvbdWorld* W, int min_blocks) {
 
 int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
     if (!W) return AVBD_ERR_INVALID_ARG;
-    if (primal_lanes != 1 && primal_lanes != 4 && primal_lanes != 8 && primal_lanes != 16 && primal_lanes != 32)
+    if (primal_lanes != 0 && primal_lanes != 1 && primal_lanes != 4 && primal_lanes != 8 && primal_lanes != 16 &&
+        primal_lanes != 32)
         return AVBD_ERR_INVALID_ARG;
     if (primal_block < 32 || primal_block > 1024 || primal_block % 32) return AVBD_ERR_INVALID_ARG;
     // the thread-per-body primal is register-bounded for 128-thread blocks
     if (primal_lanes == 1 && primal_block > 128) return AVBD_ERR_INVALID_ARG;
+    if (primal_lanes == 0 && W->w.ctr && !W->w.contrib) {
+        // the split primal's per-incidence partial systems
+        cudaSetDevice(W->device);
+        W->w.contrib = W->mem.get<float4>((size_t)W->cand_cap * 2 * 7);
+        if (!W->w.contrib) return AVBD_ERR_DEVICE;
+    }
     W->tune.primal_lanes = primal_lanes;
     W->tune.primal_block = primal_block;
     free_graphs(W);
@@ -1231,6 +1243,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     launch_post_discovery(w, W->scan_tmp, st);
     CK(cudaEventRecord(ev[5], st));
     launch_colouring(w, W->tune, W->scan_tmp, st);
+    launch_solve_prep(w, W->tune, st);
     CK(cudaEventRecord(ev[6], st));
     rc = read_ctr(W);
     if (rc) return rc;

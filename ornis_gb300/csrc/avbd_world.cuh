@@ -123,6 +123,11 @@ struct DW {
     uint32_t* offA;  // N+1: pairs whose A side is body h are [offA[h], offA[h+1])
     uint32_t* offB;  // N+1: B-side incidence list
     uint32_t* listB;
+    uint32_t* posB;  // pair -> its index in listB
+    // split primal: per-colour (pair, side) work lists and per-incidence partial systems
+    uint32_t* side_list;  // 2*pair_cap entries: pair * 2 + (1 for the A side, 0 for the B side)
+    uint32_t* side_cnt;   // [0, MAX_COLOURS]: list starts; [MAX_COLOURS+1, 2*MAX_COLOURS+1]: cursors
+    float4* contrib;      // 7 float4 per incidence slot (21 Hessian + 6 rhs + pad)
     // ... and the previous generation (read by discovery for the warm merge)
     uint2* o_ab;
     float4* o_n;

@@ -64,6 +64,11 @@ def lib():
         L.oracle_gap_c0.restype = C.c_double
         L.oracle_gap_c0.argtypes = [vp, C.c_uint32, C.c_uint32]
         L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
+        L.oracle_set_emit_period.argtypes = [vp, C.c_int32]
+        L.oracle_drain_contact_events.restype = C.c_uint32
+        L.oracle_drain_contact_events.argtypes = [vp, vp, C.c_uint32]
+        L.oracle_drain_trigger_events.restype = C.c_uint32
+        L.oracle_drain_trigger_events.argtypes = [vp, vp, C.c_uint32]
         _lib = L
     return _lib
 
@@ -168,3 +173,16 @@ class OracleWorld:
         c = abi.AvbdCounters()
         lib().oracle_get_counters(self.h, C.byref(c))
         return c
+
+    def set_emit_period(self, period):
+        lib().oracle_set_emit_period(self.h, int(period))
+
+    def contact_events(self, cap=1 << 20):
+        out = np.zeros(cap, dtype=abi.CONTACT_EVENT_DTYPE)
+        n = lib().oracle_drain_contact_events(self.h, abi.ptr(out), cap)
+        return out[:n]
+
+    def trigger_events(self, cap=1 << 16):
+        out = np.zeros(cap, dtype=abi.TRIGGER_EVENT_DTYPE)
+        n = lib().oracle_drain_trigger_events(self.h, abi.ptr(out), cap)
+        return out[:n]

@@ -42,9 +42,9 @@ def test_graph_replay_equals_plain_launches():
     assert b.graph_nodes() > 0
 
 
-@pytest.mark.parametrize("lanes,fast", [(4, 0), (8, 0), (32, 0), (1, 1), (4, 1)])
+@pytest.mark.parametrize("lanes,fast", [(4, 0), (8, 0), (32, 0), (1, 1), (4, 1), (0, 0), (0, 1)])
 def test_lane_and_precision_variants_within_tolerance(lanes, fast):
-    """Lane-parallel primal and the fast build: different rounding, same integer outputs."""
+    """Lane-parallel and split primal, and the fast build: different rounding, same integer outputs."""
     rng = np.random.default_rng([2, 11])
     bodies = scenes.bin_scene(rng, 150)
     params = abi.default_params(step_dt=1.0 / 120.0, iterations=8)
