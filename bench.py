@@ -12,7 +12,8 @@ piles at the end weigh as they do in the workload.
                HBM (CUDA events on the world's stream).
   e2e          the same K steps through the C ABI with host buffers: every
                step uploads all body records, steps, downloads all body
-               records (host wall clock around synchronised calls).
+               records and drains the contact events (host wall clock
+               around synchronised calls).
   plain        a bounded sample of the same scenes, each stepped alone (one
                world per scene, plain launches) over the same K steps; the
                batched/plain ratio is the batching speed-up.
@@ -250,6 +251,7 @@ def run_ours(args):
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
     w.set_precision(not args.exact)
+    w.set_events(nsub)  # contact events every step, as the reference's step(dt) reports them
     s0 = w.export_state()  # the initial drop: no contacts yet
     tuned = None
     if args.lanes is not None:
@@ -298,11 +300,12 @@ def run_ours(args):
     else:
         ndyn_total = ndyn
     value = ndyn_total * args.steps / (ms / 1e3)
-    nodes = w.graph_nodes()
+    launches_per_step = w.graph_nodes() * (nsub - 1) + w.graph_nodes_emit()
     c = w.counters()
     # ---- per-phase profile at the end of the trajectory: primal roofline ---
     phases, info = w.profile_substep()
-    roof = roofline.primal_roofline(phases, info, hbm_peak())
+    split = (tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)) == 0
+    roof = roofline.primal_roofline(phases, info, hbm_peak(), split=split)
     roof["state"] = f"one profiled substep after step {args.start + args.steps}"
     # ---- e2e through the C ABI with host buffers, same trajectory ----------
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
@@ -310,7 +313,9 @@ def run_ours(args):
     if args.start:
         w.step_graph(nsub * args.start)
     host = w.bodies()
+    w.contact_events()
     h2d = d2h = host.nbytes
+    ev_bytes = 0
     if d:
         d[0].barrier()
     t0 = time.perf_counter()
@@ -318,7 +323,9 @@ def run_ours(args):
         w.set_bodies(host)
         w.step_graph(nsub)
         host = w.bodies()
+        ev_bytes += w.contact_events().nbytes
     e2e_s = time.perf_counter() - t0
+    d2h += ev_bytes // max(1, e2e_steps)
     e2e = ndyn * e2e_steps / e2e_s
     if d:
         import torch
@@ -352,7 +359,7 @@ def run_ours(args):
                    if tuned else {"lanes": args.lanes if args.lanes is not None else 1, "block": args.block}},
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "steps": e2e_steps},
-        "gpu_launches": int(nodes * nsub * args.steps),
+        "gpu_launches": int(launches_per_step * args.steps),
         "roofline": roof,
         "cpu_baseline": cb,
         "clocks": clk.summary(),

@@ -328,6 +328,32 @@ int avbd_world_profile_substep(AvbdWorld* world, float* ms, uint32_t* info);
 
 /* Kernel nodes in one captured substep graph (0 before the first capture). */
 int avbd_world_graph_nodes(AvbdWorld* world, uint32_t* n);
+/* ... and in the captured substep that also reports events. */
+int avbd_world_graph_nodes_emit(AvbdWorld* world, uint32_t* n);
+
+/* ---- events (PhysicsEngine::drain_contact_events / drain_trigger_events,
+ * engine.rs; emitted by avbd/mod.rs:1606-1669 and :1126-1136) ------------- */
+
+/* Which substeps report events.  As in the reference, avbd_world_step
+ * reports on the last substep of each call.  For fixed-step calls
+ * (avbd_world_step_fixed / _graph / _timed): period 0 (default) = the last
+ * substep of each call, k > 0 = every k-th substep of a call, -1 = no
+ * events at all (not even swept hits). */
+int avbd_set_events(AvbdWorld* world, int32_t period);
+
+/* Move every queued contact / trigger event into `out` (room for `cap`) and
+ * set *n to how many.  If more than `cap` are queued nothing is moved,
+ * *n = the number queued and AVBD_ERR_CAPACITY is returned.  Within one
+ * substep Begin / End come first, then hits of new touches, then swept
+ * hits; Begin / End and hits are ordered by (body_b, body_a) — the
+ * reference's set of events, in the reference's kinds-then-keys grouping
+ * but keyed on the higher handle first. */
+int avbd_world_drain_contact_events(AvbdWorld* world, AvbdContactEvent* out, uint32_t cap, uint32_t* n);
+int avbd_world_drain_trigger_events(AvbdWorld* world, AvbdTriggerEvent* out, uint32_t cap, uint32_t* n);
+
+/* counts[4]: contact events queued, trigger events queued, contact events
+ * dropped because the queue was full, trigger events dropped (cumulative). */
+int avbd_world_event_counts(AvbdWorld* world, uint32_t* counts);
 
 /* ---- allocation-free stepping (no counterpart in the reference) ----------- */
 

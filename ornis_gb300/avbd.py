@@ -67,6 +67,11 @@ def lib():
             "avbd_world_profile_substep": [vp, vp, vp],
             "avbd_world_graph_nodes": [vp, C.POINTER(u32)],
             "avbd_scene_step_static": [C.POINTER(abi.AvbdParams), vp, u32, C.c_int32, vp],
+            "avbd_world_graph_nodes_emit": [vp, C.POINTER(u32)],
+            "avbd_set_events": [vp, C.c_int32],
+            "avbd_world_drain_contact_events": [vp, vp, u32, C.POINTER(u32)],
+            "avbd_world_drain_trigger_events": [vp, vp, u32, C.POINTER(u32)],
+            "avbd_world_event_counts": [vp, vp],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -221,6 +226,40 @@ class AvbdWorld:
 
     def set_tuning(self, lanes, block):
         _check(lib().avbd_set_tuning(self.h, int(lanes), int(block)), "set_tuning")
+
+    def graph_nodes_emit(self):
+        n = C.c_uint32()
+        _check(lib().avbd_world_graph_nodes_emit(self.h, C.byref(n)), "graph_nodes_emit")
+        return n.value
+
+    # ---- events (PhysicsEngine::drain_contact_events / drain_trigger_events) ----
+    def set_events(self, period):
+        """0: events on the last substep of each call; k: every k substeps; -1: none."""
+        _check(lib().avbd_set_events(self.h, int(period)), "set_events")
+
+    def event_counts(self):
+        out = np.zeros(4, dtype=np.uint32)
+        _check(lib().avbd_world_event_counts(self.h, abi.ptr(out)), "event_counts")
+        return dict(contact=int(out[0]), trigger=int(out[1]), contact_dropped=int(out[2]),
+                    trigger_dropped=int(out[3]))
+
+    def _drain(self, fn, dtype):
+        n = C.c_uint32()
+        cap = 1024
+        while True:
+            out = np.zeros(cap, dtype=dtype)
+            rc = fn(self.h, abi.ptr(out), cap, C.byref(n))
+            if rc == abi.AVBD_ERR_CAPACITY:
+                cap = int(n.value)
+                continue
+            _check(rc, "drain events")
+            return out[: n.value]
+
+    def contact_events(self):
+        return self._drain(lib().avbd_world_drain_contact_events, abi.CONTACT_EVENT_DTYPE)
+
+    def trigger_events(self):
+        return self._drain(lib().avbd_world_drain_trigger_events, abi.TRIGGER_EVENT_DTYPE)
 
     def colours(self):
         n = self.body_count

@@ -26,6 +26,7 @@ SOURCES = [
     ("avbd_phase_solve.cu", "avbd_phase_solve.o", []),
     ("avbd_phase_solve.cu", "avbd_phase_solve_fast.o",
      ["-DAVBD_SOLVE_FAST", "-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
+    ("avbd_events.cu", "avbd_events.o", []),
     ("avbd_world.cu", "avbd_world.o", []),
     ("avbd_static.cu", "avbd_static.o", []),
 ]

@@ -46,11 +46,15 @@ struct BroadphasePlan {
 };
 void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st);
 void launch_ccd(const DW& w, cudaStream_t st);
-void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
+// triggers != 0: also collect this substep's trigger overlaps (an emitting substep)
+void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st, int triggers = 0);
 void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st);
 void launch_colouring(const DW& w, const Tune& tune, uint32_t* scan_tmp, cudaStream_t st);
 
 void launch_wake_apply(const DW& w, cudaStream_t st);
+// Contact events of this substep (emit: the step's emitting substep) and,
+// with triggers, trigger transitions; swept hits are collected every substep.
+void launch_events(const DW& w, int emit, int triggers, uint32_t* scan_tmp, cudaStream_t st);
 // The iteration and finish kernels exist in two builds: `exact` reproduces
 // the CPU oracle bit for bit (thread-per-body primal), `fast` trades the last
 // bits for fewer instructions (contracted FMAs, approximate div/sqrt).
@@ -58,7 +62,7 @@ void launch_wake_apply(const DW& w, cudaStream_t st);
     void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st);                   \
     void launch_finish_substep(const DW& w, cudaStream_t st);                                             \
     void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st); \
-    void launch_dual(const DW& w, cudaStream_t st);                                                     \
+    void launch_dual(const DW& w, const Tune& tune, cudaStream_t st);                                   \
     void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st);
 namespace exact {
 AVBD_SOLVE_DECLS
@@ -83,8 +87,8 @@ inline void launch_solve_prep(const DW& w, const Tune& t, cudaStream_t st) {
     else exact::launch_solve_prep(w, t, st);
 }
 inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
-    if (t.fast) fast::launch_dual(w, st);
-    else exact::launch_dual(w, st);
+    if (t.fast) fast::launch_dual(w, t, st);
+    else exact::launch_dual(w, t, st);
 }
 
 }  // namespace avbd

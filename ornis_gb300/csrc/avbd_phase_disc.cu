@@ -88,17 +88,37 @@ static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b
     return r;
 }
 
-static __device__ __forceinline__ void k_disc_filter_one(const DW& w, uint32_t c) {
+// A trigger pair overlaps when discover_pair would report it with a signed
+// gap <= 0 (rows.rs:432-520: no joint exclusion for triggers).
+static __device__ __noinline__ bool trigger_overlap(const DW& w, uint32_t a, uint32_t b) {
+    if (!pair_allowed(w, a, b)) return false;
+    if (len(ld3(w.pos[a]) - ld3(w.pos[b])) > w.shp[a].w + w.shp[b].w + GEN_MARGIN) return false;
+    Shape sa = shape_of(w, a), sb = shape_of(w, b);
+    float sat = 0.0f;
+    Dist d = shape_distance(sa, sb, &sat);
+    float sgn = (sa.kind == AVBD_SHAPE_BOX && sb.kind == AVBD_SHAPE_BOX) ? sat : d.dist;
+    return sgn <= 0.0f;
+}
+static __device__ __forceinline__ void k_disc_filter_one(const DW& w, uint32_t c, int triggers) {
     uint2 ab = w.cand[c];
+    if (triggers && (info_trigger(w.info[ab.x]) || info_trigger(w.info[ab.y]))) {
+        w.keep[c] = 0;
+        if (trigger_overlap(w, ab.x, ab.y)) {
+            uint32_t slot = agg_inc(&w.evs[EV_TRIG_NOW]);
+            if (slot < (uint32_t)TRIG_CAP) w.trig_now[slot] = ((unsigned long long)ab.y << 32) | ab.x;
+            else w.evs[EV_TRIG_OVF] = 1u;
+        }
+        return;
+    }
     Disc d = discover(w, ab.x, ab.y, false);
     w.keep[c] = d.keep;
     if (d.keep) agg_inc_at(w.cnt, ab.x);
 }
-__global__ void k_disc_filter(DW w) {
+__global__ void k_disc_filter(DW w, int triggers) {
     if (aborted(w)) return;
     const uint32_t n = n_cand(w);
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-        k_disc_filter_one(w, c);
+        k_disc_filter_one(w, c, triggers);
 }
 
 static __device__ __forceinline__ void k_place_one(const DW& w, uint32_t c) {
@@ -145,8 +165,14 @@ static __device__ __forceinline__ bool box_pair(const DW& w, uint2 ab) {
 // bd_pb; the per-pair build below then reads them.  Every box pair runs the
 // same fixed loops (15 SAT axes, 16 corner and 144 edge tests), so a warp of
 // box pairs stays converged and the kernel is ALU-bound with few loads.
+// Pairs are built class by class (box-box, one box, no box) so the lanes of
+// a warp run the same manifold code: corners of two boxes, of one, or none.
 static __device__ __forceinline__ void k_collect_boxes_one(const DW& w, uint32_t p) {
-    if (box_pair(w, w.cand[w.slot_c[p]])) w.boxlist[agg_inc(&w.ctr[C_BOXPAIRS])] = p;
+    uint2 ab = w.cand[w.slot_c[p]];
+    int boxes = (info_shape(w.info[ab.x]) == AVBD_SHAPE_BOX) + (info_shape(w.info[ab.y]) == AVBD_SHAPE_BOX);
+    if (boxes == 2) w.boxlist[agg_inc(&w.ctr[C_BOXPAIRS])] = p;
+    else if (boxes == 1) w.boxlist[w.pair_cap - 1u - agg_inc(&w.ctr[C_BOXONE])] = p;
+    else w.clist[agg_inc(&w.ctr[C_NOBOX])] = p;
 }
 __global__ void k_collect_boxes(DW w) {
     if (aborted(w)) return;
@@ -319,11 +345,14 @@ static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2
     }
     agg_add(&w.ctr[C_POINTS], (uint32_t)nf);
 }
-__global__ void k_disc_build(DW w) {
+// cls 0: box-box pairs, 1: one box, 2: no box
+__global__ void k_disc_build(DW w, int cls) {
     if (aborted(w)) return;
-    const uint32_t n = n_pairs(w);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+    const uint32_t n = w.ctr[cls == 0 ? C_BOXPAIRS : (cls == 1 ? C_BOXONE : C_NOBOX)];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t p = cls == 0 ? w.boxlist[i] : (cls == 1 ? w.boxlist[w.pair_cap - 1u - i] : w.clist[i]);
         k_disc_build_one(w, p);
+    }
 }
 
 __global__ void k_clear_flags(DW w) {
@@ -332,18 +361,18 @@ __global__ void k_clear_flags(DW w) {
     if (h < (uint32_t)w.N) w.flag[h] = 0;
 }
 
-void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {
+void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st, int triggers) {
     unsigned g1 = nblk(w.N + 1, 256);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cur, w.N + 1);
-    k_disc_filter<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w);
+    k_disc_filter<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, triggers && w.evs ? 1 : 0);
     scan_exclusive(w.cnt, w.offA, w.N + 1, scan_tmp, st);
     k_place<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w);
     k_sort_slots<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_clear_flags<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_collect_boxes<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
     k_box_witness<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
-    k_disc_build<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
+    for (int cls = 0; cls < 3; cls++) k_disc_build<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w, cls);
 }
 
 // ---- after discovery ----------------------------------------------------------

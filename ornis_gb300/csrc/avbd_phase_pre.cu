@@ -13,11 +13,15 @@ __global__ void k_begin(DW w) {
     if (threadIdx.x == 0) {
         w.ctr[C_CCD_PENDING] = 0;
         w.ctr[C_BOXPAIRS] = 0;
+        w.ctr[C_FCAND] = 0;
+        w.ctr[C_BOXONE] = 0;
+        w.ctr[C_NOBOX] = 0;
         w.ctr[C_CAND] = 0;
         w.ctr[C_NCOL] = 0;
         w.ctr[C_FAST] = 0;
         w.ctr[C_POINTS] = 0;
         w.ctr[C_SLEEP] = 0;
+        if (w.evs) w.evs[EV_TRIG_NOW] = 0;
     }
 }
 void launch_begin_substep(const DW& w, cudaStream_t st) { k_begin<<<1, 32, 0, st>>>(w); }
@@ -80,7 +84,9 @@ void launch_wake_apply(const DW& w, cudaStream_t st) { k_wake_apply<<<nblk(w.N, 
 // ---- torque -> angular velocity (mod.rs:855-871) ---------------------------
 __global__ void k_torque(DW w) {
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N || !solvable(w, h)) return;
+    if (h >= (uint32_t)w.N) return;
+    if (w.pre_vel) w.pre_vel[h] = w.vel[h];  // torque leaves the linear velocity as it is
+    if (!solvable(w, h)) return;
     float4 tq4 = w.torque[h];
     V3 in = ld3(w.inertia[h]);
     float iw[3][3], inv[3][3];
@@ -263,9 +269,10 @@ struct Cast {
     bool hit;
     float t;
     V3 normal;
+    V3 point;  // the target's witness at the hit
 };
 static __device__ __noinline__ Cast cast_one(const DW& w, uint32_t h, uint32_t o) {
-    Cast c{false, 0.0f, V0()};
+    Cast c{false, 0.0f, V0(), V0()};
     V3 disp = ld3(w.vel[h]) * w.dt;
     float L = len(disp);
     if (L < NEAR_ZERO) return c;
@@ -282,6 +289,7 @@ static __device__ __noinline__ Cast cast_one(const DW& w, uint32_t h, uint32_t o
                 c.hit = true;
                 c.t = t;
                 c.normal = normalize_or(d.pa - d.pb, -dir);
+                c.point = d.pb;
             }
             break;
         }
@@ -298,11 +306,12 @@ __global__ void k_ccd_init(DW w) {
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
     w.ccd_best[h] = ~0ull;
+    if (w.ccd_ev_o) w.ccd_ev_o[h] = -1;
     w.ccd_deps[h] = 0;
     w.ccd_state[h] = 0;
     w.ccd_recompute[h] = 0;
     if (w.fast[h]) {
-        agg_inc(&w.ctr[C_FAST]);
+        w.fbody[agg_inc(&w.ctr[C_FAST])] = h;
         agg_inc(&w.ctr[C_CCD_PENDING]);
     }
 }
@@ -325,14 +334,28 @@ static __device__ __forceinline__ void k_ccd_cast_one(const DW& w, int first, ui
             atomicMin(&w.ccd_best[h], key);
         }
     }
-    if (first && fa && fb && ccd_target(w, ab.x, ab.y)) atomicAdd(&w.ccd_deps[ab.y], 1u);
+}
+// Candidates with a fast body are listed once per substep (and the
+// dependency counts taken); every cast round then walks that list, so the
+// long cast loops fill whole warps instead of a few lanes of each.
+__global__ void k_ccd_collect(DW w) {
+    if (aborted(w)) return;
+    if (w.ctr[C_FAST] == 0u) return;
+    const uint32_t n = n_cand(w);
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        uint2 ab = w.cand[c];
+        bool fa = w.fast[ab.x], fb = w.fast[ab.y];
+        if (!fa && !fb) continue;
+        w.fcand[agg_inc(&w.ctr[C_FCAND])] = c;
+        if (fa && fb && ccd_target(w, ab.x, ab.y)) atomicAdd(&w.ccd_deps[ab.y], 1u);
+    }
 }
 __global__ void k_ccd_cast(DW w, int first) {
     if (aborted(w)) return;
     if (w.ctr[C_FAST] == 0u || (!first && w.ctr[C_CCD_PENDING] == 0u)) return;
-    const uint32_t n = n_cand(w);
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-        k_ccd_cast_one(w, first, c);
+    const uint32_t n = w.ctr[C_FCAND];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        k_ccd_cast_one(w, first, w.fcand[i]);
 }
 
 static __device__ void ccd_apply(const DW& w, uint32_t h) {
@@ -345,6 +368,15 @@ static __device__ void ccd_apply(const DW& w, uint32_t h) {
         float L = fmaxf(len(disp), MIN_TOI_DISP_LENGTH);
         float frac = fclamp(r.t / L, 0.0f, 1.0f);
         float e = fminf(w.mat[h].x, w.mat[o].x);
+        if (w.ccd_ev_o) {
+            // a swept impact is a hit event (mod.rs:946-960)
+            float approach = -dot(ld3(w.pre_vel[h]) - ld3(w.pre_vel[o]), r.normal);
+            if (approach > 1.0f) {
+                w.ccd_ev_o[h] = (int32_t)o;
+                w.ccd_ev_p[h] = st3(r.point, approach);
+                w.ccd_ev_n[h] = st3(h < o ? -r.normal : r.normal, 0.0f);
+            }
+        }
         w.pos[h] = st3(ld3(w.pos[h]) + disp * frac, 0.0f);
         V3 v = ld3(w.vel[h]);
         float vn = dot(v, r.normal);
@@ -362,8 +394,10 @@ static __device__ void ccd_apply(const DW& w, uint32_t h) {
 __global__ void k_ccd_finalize(DW w, int round, int last) {
     if (aborted(w)) return;
     if (w.ctr[C_CCD_PENDING] == 0u) return;
-    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N || !w.fast[h] || w.ccd_state[h] != 0) return;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.ctr[C_FAST]) return;
+    uint32_t h = w.fbody[i];
+    if (w.ccd_state[h] != 0) return;
     if (w.ccd_deps[h] != 0) {
         if (!last) return;
         atomicAdd(&w.ctr[C_CCD_LEFT], 1u);  // dependency chain longer than the bounded rounds
@@ -383,37 +417,40 @@ static __device__ __forceinline__ void k_ccd_release_one(const DW& w, int round,
 __global__ void k_ccd_release(DW w, int round) {
     if (aborted(w)) return;
     if (w.ctr[C_CCD_PENDING] == 0u) return;
-    const uint32_t n = n_cand(w);
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-        k_ccd_release_one(w, round, c);
+    const uint32_t n = w.ctr[C_FCAND];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        k_ccd_release_one(w, round, w.fcand[i]);
 }
 
 __global__ void k_ccd_reset(DW w) {
     if (aborted(w)) return;
     if (w.ctr[C_CCD_PENDING] == 0u) return;
-    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N || !w.fast[h]) return;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.ctr[C_FAST]) return;
+    uint32_t h = w.fbody[i];
     if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_best[h] = ~0ull;
 }
 __global__ void k_ccd_clear_recast(DW w) {
     if (aborted(w)) return;
     if (w.ctr[C_CCD_PENDING] == 0u) return;
-    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N || !w.fast[h]) return;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.ctr[C_FAST]) return;
+    uint32_t h = w.fbody[i];
     if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_recompute[h] = 0;
 }
 void launch_ccd(const DW& w, cudaStream_t st) {
     if (!w.enable_ccd) return;
     unsigned gb = nblk(w.N, 256);
     k_ccd_init<<<gb, 256, 0, st>>>(w);
-    k_ccd_cast<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, 1);
+    k_ccd_collect<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w);
+    k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 1);
     for (int r = 0; r < CCD_ROUNDS; r++) {
         bool last = r == CCD_ROUNDS - 1;
         k_ccd_finalize<<<gb, 256, 0, st>>>(w, r, last ? 1 : 0);
         if (last) break;
         k_ccd_release<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, r);
         k_ccd_reset<<<gb, 256, 0, st>>>(w);
-        k_ccd_cast<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, 0);
+        k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 0);
         k_ccd_clear_recast<<<gb, 256, 0, st>>>(w);
     }
 }

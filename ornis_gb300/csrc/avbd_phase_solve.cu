@@ -562,13 +562,13 @@ void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bod
         default: k_primal_lanes<32><<<nblk((size_t)max_bodies * 32, bs), bs, 0, st>>>(w, c); break;
     }
 }
-void launch_dual(const DW& w, cudaStream_t st) {
+void launch_dual(const DW& w, const Tune& tune, cudaStream_t st) {
     k_dual_pairs<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
     if (w.J) k_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
 }
 void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st) {
     for (int c = 0; c < ncolours; c++) AVBD_SOLVE_NS::launch_primal_colour(w, tune, c, (uint32_t)w.N, st);
-    AVBD_SOLVE_NS::launch_dual(w, st);
+    AVBD_SOLVE_NS::launch_dual(w, tune, st);
 }
 
 // ---- BDF1 + sleep + driver baseline (mod.rs:1060-1142) -------------------------

@@ -227,10 +227,13 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
     w.cur = cv.take<uint32_t>(N + 1);
     w.slot_c = cv.take<uint32_t>(PCAP);
     w.boxlist = cv.take<uint32_t>(PCAP);
+    w.clist = cv.take<uint32_t>(PCAP);
     w.bd_pa = cv.take<float4>(PCAP);
     w.bd_pb = cv.take<float4>(PCAP);
     w.sort_key = cv.take<uint32_t>(1);
     w.sort_idx = cv.take<uint32_t>(1);
+    w.fbody = cv.take<uint32_t>(N);
+    w.fcand = cv.take<uint32_t>(PCAP);
     w.fast = cv.take<uint8_t>(N);
     w.ccd_best = cv.take<unsigned long long>(N);
     w.ccd_deps = cv.take<uint32_t>(N);

@@ -128,13 +128,20 @@ struct AvbdWorld {
     uint32_t* scan_tmp = nullptr;
     AvbdBody* d_stage = nullptr;
     uint32_t* h_ctr = nullptr;  // pinned copy of the device counters
+    uint32_t ev_cap0 = 0;
     AvbdCounters cum{};
     float time_debt = 0.0f;
     int last_ncol = 0;
-    // graphs: one captured substep per pair-buffer parity
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    // graphs: one captured substep per pair-buffer parity, without and with events
+    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    // events: emitted on the last substep of each step call, or every
+    // ev_period substeps of a fixed-step call; -1 turns them off
+    int ev_period = 0;
+    bool has_trig = false;
+    Alloc evmem;  // the event queues: kept across reallocations of the world
     int graph_cols = 0;
-    size_t graph_nodes = 0;  // kernel nodes in one captured substep
+    size_t graph_nodes = 0;       // kernel nodes in one captured substep (no events)
+    size_t graph_nodes_emit = 0;  // ... in one that reports events
     uint64_t steps = 0;
 };
 
@@ -161,10 +168,11 @@ static void set_pair_ptrs(AvbdWorld* W) {
 
 static void free_graphs(AvbdWorld* W) {
     for (int i = 0; i < 2; i++)
-        if (W->gexec[i]) {
-            cudaGraphExecDestroy(W->gexec[i]);
-            W->gexec[i] = nullptr;
-        }
+        for (int e = 0; e < 2; e++)
+            if (W->gexec[i][e]) {
+                cudaGraphExecDestroy(W->gexec[i][e]);
+                W->gexec[i][e] = nullptr;
+            }
 }
 
 // Capacities: candidates are bounded by the sweep-and-prune overlaps plus the
@@ -172,6 +180,18 @@ static void free_graphs(AvbdWorld* W) {
 static uint32_t default_cand_cap(uint32_t n) { return 12u * n + 4096u; }
 
 static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap) {
+    // the previous touch set (handle keyed) survives a reallocation
+    std::vector<uint32_t> tof, tkeys;
+    if (W->w.toff && W->w.evs) {
+        uint32_t on = (uint32_t)W->w.N, par = 0;
+        tof.resize(on + 1);
+        cudaMemcpy(tof.data(), W->w.toff, (on + 1) * 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&par, W->w.evs + EV_PAR, 4, cudaMemcpyDeviceToHost);
+        tkeys.resize(tof[on]);
+        if (!tkeys.empty())
+            cudaMemcpy(tkeys.data(), (par & 1u) ? W->w.tk1 : W->w.tk0, tkeys.size() * 4, cudaMemcpyDeviceToHost);
+        tof.resize(N + 1, tof[on]);  // bodies added since: no touches
+    }
     W->mem.release();
     free_graphs(W);
     Alloc& m = W->mem;
@@ -228,6 +248,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.cur = m.get<uint32_t>(N + 1);
     w.slot_c = m.get<uint32_t>(cand_cap);
     w.boxlist = m.get<uint32_t>(cand_cap);
+    w.clist = m.get<uint32_t>(cand_cap);
     w.bd_pa = m.get<float4>(cand_cap);
     w.bd_pb = m.get<float4>(cand_cap);
     w.aabb_lo = m.get<float4>(N); w.aabb_hi = m.get<float4>(N);
@@ -257,6 +278,8 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
         cudaMemcpy(W->d_small, small.data(), small.size() * 4, cudaMemcpyHostToDevice);
     W->plan.small_scenes = W->d_small;
     W->plan.n_small = (int)small.size();
+    w.fbody = m.get<uint32_t>(N);
+    w.fcand = m.get<uint32_t>(cand_cap);
     w.fast = m.get<uint8_t>(N);
     w.ccd_best = m.get<unsigned long long>(N);
     w.ccd_deps = m.get<uint32_t>(N);
@@ -264,6 +287,45 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.ccd_recompute = m.get<uint8_t>(N);
     w.flag = m.get<uint8_t>(N);
     w.comp_flag = m.get<uint32_t>(N);
+    // events
+    w.pre_vel = m.get<float4>(N);
+    if (W->prm.enable_ccd) {
+        w.ccd_ev_o = m.get<int32_t>(N);
+        w.ccd_ev_p = m.get<float4>(N);
+        w.ccd_ev_n = m.get<float4>(N);
+    }
+    w.t_flag = m.get<uint8_t>(cand_cap);
+    w.t_wit = m.get<float4>(cand_cap);
+    w.toff = m.get<uint32_t>(N + 1);
+    w.tk0 = m.get<uint32_t>(cand_cap);
+    w.tk1 = m.get<uint32_t>(cand_cap);
+    w.ev_cbe = m.get<uint32_t>(N + 1);
+    w.ev_ch = m.get<uint32_t>(N + 1);
+    w.ev_cc = m.get<uint32_t>(N + 1);
+    w.ev_ct = m.get<uint32_t>(N + 1);
+    if (W->evmem.ptrs.empty()) {
+        W->evmem.get<uint32_t>(EV_NUM);
+        W->evmem.get<AvbdContactEvent>(std::max<uint32_t>(65536u, 2u * N));
+        W->evmem.get<AvbdTriggerEvent>(65536u);
+        W->evmem.get<unsigned long long>(TRIG_CAP);
+        W->evmem.get<unsigned long long>(TRIG_CAP);
+        W->ev_cap0 = std::max<uint32_t>(65536u, 2u * N);
+    }
+    if (W->evmem.ptrs.size() != 5) return AVBD_ERR_DEVICE;
+    w.evs = (uint32_t*)W->evmem.ptrs[0];
+    w.ev = (AvbdContactEvent*)W->evmem.ptrs[1];
+    w.ev_cap = W->ev_cap0;
+    w.tev = (AvbdTriggerEvent*)W->evmem.ptrs[2];
+    w.tev_cap = 65536u;
+    w.trig_now = (unsigned long long*)W->evmem.ptrs[3];
+    w.trig_prev = (unsigned long long*)W->evmem.ptrs[4];
+    if (!tof.empty()) {
+        uint32_t par = 0;
+        cudaMemcpy(&par, w.evs + EV_PAR, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(w.toff, tof.data(), (N + 1) * 4, cudaMemcpyHostToDevice);
+        if (!tkeys.empty())
+            cudaMemcpy((par & 1u) ? w.tk1 : w.tk0, tkeys.data(), tkeys.size() * 4, cudaMemcpyHostToDevice);
+    }
     w.col_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
     w.col_list = m.get<uint32_t>(N);
     w.col_key = m.get<uint32_t>(N);
@@ -369,8 +431,10 @@ static int upload_all(AvbdWorld* W) {
         }
     }
     plane_off[S] = (uint32_t)plane_list.size();
+    W->has_trig = false;
     for (uint32_t h = 0; h < N; h++) {
         const AvbdBody& b = W->bodies[h];
+        if (b.flags & AVBD_FLAG_TRIGGER) W->has_trig = true;
         info[h] = (b.shape & 15u) | ((b.body_type & 3u) << 4) | ((b.flags & AVBD_FLAG_TRIGGER) ? 64u : 0u);
         shp[h] = make_float4(b.shape_params[0], b.shape_params[1], b.shape_params[2], shape_bound(b.shape, b.shape_params));
         float in[3];
@@ -620,8 +684,9 @@ static int host_edit(AvbdWorld* W) {
 }
 
 // ---- substep driver ---------------------------------------------------------------
-// Enqueue one substep up to and including the colouring.
-static void enqueue_front(AvbdWorld* W) {
+// Enqueue one substep up to and including the colouring (emit: the
+// substep reports events, so discovery also collects trigger overlaps).
+static void enqueue_front(AvbdWorld* W, bool emit) {
     cudaStream_t st = W->st;
     W->cur = 1 - W->cur;  // the previous generation becomes `old`
     set_pair_ptrs(W);
@@ -631,15 +696,16 @@ static void enqueue_front(AvbdWorld* W) {
     launch_torque(w, st);
     launch_broadphase(w, W->plan, st);
     launch_ccd(w, st);
-    launch_discovery(w, W->scan_tmp, st);
+    launch_discovery(w, W->scan_tmp, st, emit && W->has_trig);
     launch_post_discovery(w, W->scan_tmp, st);
     launch_colouring(w, W->tune, W->scan_tmp, st);
 }
-static void enqueue_back(AvbdWorld* W, int ncol) {
+static void enqueue_back(AvbdWorld* W, int ncol, bool emit) {
     const DW& w = W->w;
     launch_solve_prep(w, W->tune, W->st);
     for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
     launch_finish_substep(w, W->tune, W->st);
+    if (W->ev_period >= 0) launch_events(w, emit, emit && W->has_trig, W->scan_tmp, W->st);
 }
 
 static int read_ctr(AvbdWorld* W) {
@@ -674,9 +740,9 @@ static void accumulate(AvbdWorld* W) {
 }
 
 // One substep through plain launches (the host reads the colour count).
-static int substep_plain(AvbdWorld* W) {
+static int substep_plain(AvbdWorld* W, bool emit) {
     for (int attempt = 0; attempt < 8; attempt++) {
-        enqueue_front(W);
+        enqueue_front(W, emit);
         CK(cudaGetLastError());
         int rc = read_ctr(W);
         if (rc) return rc;
@@ -691,7 +757,7 @@ static int substep_plain(AvbdWorld* W) {
         }
         int ncol = (int)W->h_ctr[C_NCOL];
         W->last_ncol = ncol;
-        enqueue_back(W, ncol);
+        enqueue_back(W, ncol, emit);
         CK(cudaGetLastError());
         rc = read_ctr(W);
         if (rc) return rc;
@@ -700,6 +766,26 @@ static int substep_plain(AvbdWorld* W) {
         return AVBD_OK;
     }
     return AVBD_ERR_CAPACITY;
+}
+
+template <class T>
+static int drain(AvbdWorld* W, int which, T* out, uint32_t cap, uint32_t* n) {
+    if (!W || !n || (cap && !out)) return AVBD_ERR_INVALID_ARG;
+    *n = 0;
+    if (!W->w.evs) return AVBD_OK;
+    cudaSetDevice(W->device);
+    const int idx = which == 0 ? EV_N : EV_TN;
+    uint32_t q = 0;
+    CK(cudaStreamSynchronize(W->st));
+    CK(cudaMemcpy(&q, W->w.evs + idx, 4, cudaMemcpyDeviceToHost));
+    *n = q;
+    if (q > cap) return AVBD_ERR_CAPACITY;  // nothing moved: call again with room for *n
+    if (q) {
+        const void* src = which == 0 ? (const void*)W->w.ev : (const void*)W->w.tev;
+        CK(cudaMemcpy(out, src, (size_t)q * sizeof(T), cudaMemcpyDeviceToHost));
+        CK(cudaMemset(W->w.evs + idx, 0, 4));
+    }
+    return AVBD_OK;
 }
 
 extern "C" {
@@ -764,6 +850,7 @@ int avbd_world_destroy(AvbdWorld* W) {
     cudaSetDevice(W->device);
     free_graphs(W);
     W->mem.release();
+    W->evmem.release();
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
     if (W->st) cudaStreamDestroy(W->st);
     delete W;
@@ -928,16 +1015,27 @@ static int begin_steps(AvbdWorld* W) {
     return AVBD_OK;
 }
 
+// Does substep i of an n-substep call report events?  The reference emits on
+// the last substep of each step (mod.rs:1226-1231); a fixed-step call is one
+// step unless an event period splits it.
+static bool emit_at(const AvbdWorld* W, int i, int n, bool last_only) {
+    if (W->ev_period < 0) return false;
+    if (W->ev_period > 0 && !last_only) return (i + 1) % W->ev_period == 0;
+    return i == n - 1;
+}
+static int step_plain_n(AvbdWorld* W, int32_t substeps, bool last_only) {
+    for (int i = 0; i < substeps; i++) {
+        int rc = substep_plain(W, emit_at(W, i, substeps, last_only));
+        if (rc) return rc;
+    }
+    return AVBD_OK;
+}
 int avbd_world_step_fixed(AvbdWorld* W, int32_t substeps) {
     if (!W || substeps < 0) return AVBD_ERR_INVALID_ARG;
     if (W->bodies.empty() && W->host_valid) return AVBD_OK;
     int rc = begin_steps(W);
     if (rc) return rc;
-    for (int i = 0; i < substeps; i++) {
-        rc = substep_plain(W);
-        if (rc) return rc;
-    }
-    return AVBD_OK;
+    return step_plain_n(W, substeps, false);
 }
 
 int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
@@ -950,7 +1048,10 @@ int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
         W->time_debt -= sd;
         n++;
     }
-    return n ? avbd_world_step_fixed(W, n) : AVBD_OK;
+    if (!n || (W->bodies.empty() && W->host_valid)) return AVBD_OK;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    return step_plain_n(W, n, true);
 }
 
 // Graph replay: one captured substep per pair-buffer parity.  The primal is
@@ -960,27 +1061,28 @@ int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
 static int capture(AvbdWorld* W) {
     free_graphs(W);
     int base = W->cur;
-    for (int k = 0; k < 2; k++) {
-        cudaGraph_t g;
-        CK(cudaStreamBeginCapture(W->st, cudaStreamCaptureModeThreadLocal));
-        W->w.max_cols = W->graph_cols;
-        enqueue_front(W);
-        enqueue_back(W, W->graph_cols);
-        W->w.max_cols = MAX_COLOURS;
-        CK(cudaStreamEndCapture(W->st, &g));
-        size_t nn = 0;
-        cudaGraphGetNodes(g, nullptr, &nn);
-        W->graph_nodes = nn;
-        cudaError_t e = cudaGraphInstantiate(&W->gexec[W->cur], g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            free_graphs(W);
-            W->cur = base;
-            set_pair_ptrs(W);
-            return AVBD_ERR_DEVICE;
+    for (int emit = 0; emit < 2; emit++)
+        for (int k = 0; k < 2; k++) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(W->st, cudaStreamCaptureModeThreadLocal));
+            W->w.max_cols = W->graph_cols;
+            enqueue_front(W, emit != 0);
+            enqueue_back(W, W->graph_cols, emit != 0);
+            W->w.max_cols = MAX_COLOURS;
+            CK(cudaStreamEndCapture(W->st, &g));
+            size_t nn = 0;
+            cudaGraphGetNodes(g, nullptr, &nn);
+            (emit ? W->graph_nodes_emit : W->graph_nodes) = nn;
+            cudaError_t e = cudaGraphInstantiate(&W->gexec[W->cur][emit], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                free_graphs(W);
+                W->cur = base;
+                set_pair_ptrs(W);
+                return AVBD_ERR_DEVICE;
+            }
         }
-    }
-    // capture flipped the parity twice: back where we started
+    // each capture flipped the parity: back where we started
     W->cur = base;
     set_pair_ptrs(W);
     return AVBD_OK;
@@ -992,9 +1094,10 @@ int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
     int rc = begin_steps(W);
     if (rc) return rc;
     for (int i = 0; i < substeps; i++) {
-        if (!W->gexec[0] || W->last_ncol > W->graph_cols) {
+        const bool emit = emit_at(W, i, substeps, false);
+        if (!W->gexec[0][0] || W->last_ncol > W->graph_cols) {
             if (W->last_ncol == 0) {
-                rc = substep_plain(W);  // learn the colour count first
+                rc = substep_plain(W, emit);  // learn the colour count first
                 if (rc) return rc;
                 continue;
             }
@@ -1003,7 +1106,7 @@ int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
             if (rc) return rc;
         }
         int next = 1 - W->cur;  // the parity this substep writes
-        CK(cudaGraphLaunch(W->gexec[next], W->st));
+        CK(cudaGraphLaunch(W->gexec[next][emit ? 1 : 0], W->st));
         W->cur = next;
         set_pair_ptrs(W);
         rc = read_ctr(W);
@@ -1015,7 +1118,7 @@ int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
             rc = grow_candidates(W);
             if (rc) return rc;
             W->host_valid = false;
-            rc = substep_plain(W);
+            rc = substep_plain(W, emit);
             if (rc) return rc;
             continue;
         }
@@ -1024,7 +1127,7 @@ int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
         if (W->h_ctr[C_ERR] & E_COLOUR_RANGE) {
             // the graph's iterations were skipped: finish this substep plainly
             CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, W->st));
-            enqueue_back(W, ncol);
+            enqueue_back(W, ncol, emit);
             rc = read_ctr(W);
             if (rc) return rc;
         }
@@ -1238,7 +1341,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     CK(cudaEventRecord(ev[2], st));
     launch_ccd(w, st);
     CK(cudaEventRecord(ev[3], st));
-    launch_discovery(w, W->scan_tmp, st);
+    launch_discovery(w, W->scan_tmp, st, W->ev_period >= 0 && W->has_trig);
     CK(cudaEventRecord(ev[4], st));
     launch_post_discovery(w, W->scan_tmp, st);
     CK(cudaEventRecord(ev[5], st));
@@ -1268,6 +1371,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     }
     CK(cudaEventRecord(ev[8], st));
     launch_finish_substep(w, W->tune, st);
+    if (W->ev_period >= 0) launch_events(w, 1, W->has_trig, W->scan_tmp, st);
     CK(cudaEventRecord(ev[9], st));
     CK(cudaEventSynchronize(ev[9]));
     ms[6] = prim;
@@ -1289,6 +1393,41 @@ int avbd_world_graph_nodes(AvbdWorld* W, uint32_t* n) {
     if (!W || !n) return AVBD_ERR_INVALID_ARG;
     *n = (uint32_t)W->graph_nodes;
     return AVBD_OK;
+}
+int avbd_world_graph_nodes_emit(AvbdWorld* W, uint32_t* n) {
+    if (!W || !n) return AVBD_ERR_INVALID_ARG;
+    *n = (uint32_t)W->graph_nodes_emit;
+    return AVBD_OK;
+}
+
+// ---- events ---------------------------------------------------------------------
+int avbd_set_events(AvbdWorld* W, int32_t period) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    W->ev_period = period < 0 ? -1 : period;
+    free_graphs(W);
+    return AVBD_OK;
+}
+// counts[4]: contact events queued, trigger events queued, contact events
+// dropped (queue full, cumulative), trigger events dropped
+int avbd_world_event_counts(AvbdWorld* W, uint32_t* counts) {
+    if (!W || !counts) return AVBD_ERR_INVALID_ARG;
+    std::memset(counts, 0, 16);
+    if (!W->w.evs) return AVBD_OK;
+    cudaSetDevice(W->device);
+    uint32_t e[EV_NUM];
+    CK(cudaStreamSynchronize(W->st));
+    CK(cudaMemcpy(e, W->w.evs, sizeof(e), cudaMemcpyDeviceToHost));
+    counts[0] = e[EV_N];
+    counts[1] = e[EV_TN];
+    counts[2] = e[EV_DROP];
+    counts[3] = e[EV_TDROP];
+    return AVBD_OK;
+}
+int avbd_world_drain_contact_events(AvbdWorld* W, AvbdContactEvent* out, uint32_t cap, uint32_t* n) {
+    return drain(W, 0, out, cap, n);
+}
+int avbd_world_drain_trigger_events(AvbdWorld* W, AvbdTriggerEvent* out, uint32_t cap, uint32_t* n) {
+    return drain(W, 1, out, cap, n);
 }
 
 }  // extern "C"

@@ -69,10 +69,27 @@ enum Ctr {
     C_SLEEP = 9,      // bodies asleep
     C_CCD_LEFT = 10,  // fast bodies left after the bounded CCD rounds
     C_CCD_PENDING = 11,  // fast bodies not yet clamped this substep
-    C_BOXPAIRS = 12,     // box-box pairs handed to the warp-per-pair builder
+    C_BOXPAIRS = 12,     // box-box pairs handed to the witness kernel
+    C_FCAND = 13,        // candidates with a fast (swept) body, this substep
+    C_BOXONE = 14,       // pairs with exactly one box (listed from the back of boxlist)
+    C_NOBOX = 15,        // pairs without a box (clist)
     C_NUM = 16
 };
 enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
+
+// event state words (indices into DW::evs)
+enum EvState {
+    EV_N = 0,          // contact events queued
+    EV_DROP = 1,       // contact events dropped (queue full), cumulative
+    EV_PAR = 2,        // which key buffer holds the previous touch set
+    EV_TN = 3,         // trigger events queued
+    EV_TDROP = 4,      // trigger events dropped, cumulative
+    EV_TRIG_NOW = 5,   // trigger overlaps found by this substep's discovery
+    EV_TRIG_PREV = 6,  // size of the previous trigger overlap set
+    EV_TRIG_OVF = 7,   // overlaps beyond TRIG_CAP were seen (set is then truncated)
+    EV_NUM = 16
+};
+constexpr int TRIG_CAP = 4096;  // trigger overlaps tracked per world
 
 // Everything a kernel needs, passed by value (pointers into one world's
 // device allocations).  Scene s owns bodies [scene_off[s], scene_off[s+1]).
@@ -141,13 +158,16 @@ struct DW {
     uint32_t* cnt;     // per body counters (N+1)
     uint32_t* cur;     // per body cursors
     uint32_t* slot_c;  // final pair slot -> candidate index
-    uint32_t* boxlist; // box-box pair slots for the warp witness kernel
+    uint32_t* boxlist; // box-box pair slots from the front, one-box pair slots from the back
+    uint32_t* clist;   // pair slots without a box
     float4 *bd_pa, *bd_pb;  // box-box witnesses per pair slot: (pa, dist), (pb, SAT gap)
     float4 *aabb_lo, *aabb_hi;
     uint32_t* sort_key;
     uint32_t* sort_idx;
 
     // CCD scratch
+    uint32_t* fbody;  // N: the fast bodies of this substep (C_FAST of them)
+    uint32_t* fcand;  // cand_cap: candidates with a fast body (C_FCAND of them)
     uint8_t* fast;
     unsigned long long* ccd_best;
     uint32_t* ccd_deps;
@@ -157,6 +177,23 @@ struct DW {
     // wake / sleep scratch
     uint8_t* flag;  // per body
     uint32_t* comp_flag;
+
+    // events (all null when the world keeps none)
+    float4* pre_vel;      // N: linear velocity at the substep start, after torque (mod.rs:874-876)
+    int32_t* ccd_ev_o;    // N: partner of this substep's swept-hit event, -1 none
+    float4* ccd_ev_p;     // N: hit point xyz, approach speed w
+    float4* ccd_ev_n;     // N: event normal (A toward B)
+    uint8_t* t_flag;      // pair_cap: touching (deepest point beyond the begin slop)
+    float4* t_wit;        // pair_cap: deepest point xyz, approach speed w
+    uint32_t* toff;       // N+1: previous touch set, CSR by the higher handle
+    uint32_t *tk0, *tk1;  // pair_cap each: its lower handles (ascending), alternating buffers
+    uint32_t *ev_cbe, *ev_ch, *ev_cc, *ev_ct;  // N+1 each: begin/end, hit, swept-hit, touch counts -> slots
+    uint32_t* evs;        // EV_* words
+    AvbdContactEvent* ev;
+    uint32_t ev_cap;
+    unsigned long long *trig_now, *trig_prev;  // TRIG_CAP each: (b << 32 | a) overlap keys
+    AvbdTriggerEvent* tev;
+    uint32_t tev_cap;
 
     // colouring
     uint32_t* col_cnt;   // MAX_COLOURS+1

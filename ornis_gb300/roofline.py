@@ -34,8 +34,12 @@ def dual_bytes_per_iteration(swept, points, pairs):
     return DUAL_POINT_B * points + DUAL_BODY_B * swept + PAIR_HEADER_B * pairs
 
 
-def primal_roofline(phases_ms, info, peak):
-    """Roofline entry for the primal kernel from one profiled substep."""
+def primal_roofline(phases_ms, info, peak, split=False):
+    """Roofline entry for the primal kernel from one profiled substep.
+
+    split: the primal ran as the split pair (k_side_rows + k_side_solve per
+    colour); its time is the pair's, its algorithmic bytes the same model.
+    """
     peak_gbs, source = peak
     iters = max(1, info["primal_launches"] // max(1, info["colours"]))
     per_iter_ms = phases_ms["primal"] / iters
@@ -46,7 +50,8 @@ def primal_roofline(phases_ms, info, peak):
     dual_ms = phases_ms["dual"] / iters
     return {
         "bound": "hbm",
-        "kernel": "k_primal_thread (one launch per colour)",
+        "kernel": ("k_side_rows + k_side_solve (one pair of launches per colour)" if split
+                   else "k_primal_thread (one launch per colour)"),
         "achieved": achieved,
         "peak": peak_gbs,
         "unit": "GB/s",
