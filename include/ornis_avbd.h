@@ -226,6 +226,14 @@ int avbd_world_destroy(AvbdWorld* world);
 int avbd_world_add_bodies(AvbdWorld* world, const AvbdBody* bodies, uint32_t n,
                           uint32_t* first_handle);
 
+/* PhysicsEngine::remove_body (engine.rs:40-43, avbd/mod.rs:1241-1300): the
+ * last body moves into the freed handle; pairs and joints of the removed
+ * body are dropped, the others renumbered; trigger pairs of the removed body
+ * report Exited, touches and queued contact events are cleared, every
+ * sleeping body wakes.  An invalid handle is a no-op.  One-scene worlds only
+ * (AVBD_ERR_UNSUPPORTED for a batch). */
+int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
+
 /* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529), Ball and Revolute. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 

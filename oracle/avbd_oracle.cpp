@@ -1741,6 +1741,59 @@ template <class T> struct Engine {
         }
     }
 
+    // PhysicsEngine::remove_body (mod.rs:1241-1300): the last body moves into
+    // the freed slot; pairs and joints of the removed body go, the others are
+    // renumbered; handle-keyed event state is cleared or remapped; every
+    // sleeper wakes.
+    void remove_body(uint32_t hi) {
+        if (hi >= bodies.size()) return;
+        uint32_t last = (uint32_t)bodies.size() - 1;
+        std::vector<Key> exited;
+        for (const Key& k : prev_trigger)
+            if (k.first == hi || k.second == hi) exited.push_back(k);
+        std::sort(exited.begin(), exited.end());
+        for (const Key& k : exited) tev.push_back(AvbdTriggerEvent{k.first, k.second, 0u});
+        bodies[hi] = bodies[last];
+        bodies.pop_back();
+        auto map = [&](uint32_t h) { return h == last ? hi : h; };
+        std::vector<Pair<T>> kept;
+        for (Pair<T>& p : pairs) {
+            if (p.a == hi || p.b == hi) continue;
+            p.a = map(p.a);
+            p.b = map(p.b);
+            kept.push_back(std::move(p));
+        }
+        pairs.swap(kept);
+        std::vector<Joint<T>> kj;
+        for (Joint<T>& j : joints) {
+            if (j.a == hi || j.b == hi) continue;
+            j.a = map(j.a);
+            j.b = map(j.b);
+            kj.push_back(j);
+        }
+        joints.swap(kj);
+        prev_touch.clear();
+        std::set<Key> remapped;
+        for (const Key& k : prev_trigger) {
+            if (k.first == hi || k.second == hi) continue;
+            uint32_t a = map(k.first), b = map(k.second);
+            remapped.insert({std::min(a, b), std::max(a, b)});
+        }
+        prev_trigger.swap(remapped);
+        cev.clear();
+        auto swap_remove = [&](auto& v) {
+            if (hi < v.size()) {
+                v[hi] = v.back();
+                v.pop_back();
+            }
+        };
+        swap_remove(sleep_timer);
+        swap_remove(asleep);
+        swap_remove(prev_pos);
+        swap_remove(prev_rot);
+        for (uint32_t h = 0; h < bodies.size(); h++) wake_body(h);
+    }
+
     int add_joint(const AvbdJointDesc& d, uint32_t& handle) {  // mod.rs:1310-1529
         for (int k = 0; k < 3; k++)
             if (!std::isfinite(d.local_anchor_a[k]) || !std::isfinite(d.local_anchor_b[k]) ||
@@ -1863,6 +1916,10 @@ int oracle_add_bodies(OracleWorld* w, const AvbdBody* b, uint32_t n) {
         using TT = std::remove_reference_t<decltype(E.dt)>;
         for (uint32_t i = 0; i < n; i++) E.bodies.push_back(from_desc<TT>(b[i]));
     });
+    return AVBD_OK;
+}
+int oracle_remove_body(OracleWorld* w, uint32_t handle) {
+    DISPATCH(w, E.remove_body(handle));
     return AVBD_OK;
 }
 int oracle_add_joint(OracleWorld* w, const AvbdJointDesc* d, uint32_t* handle) {

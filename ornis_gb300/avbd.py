@@ -43,6 +43,7 @@ def lib():
             "avbd_world_destroy": [vp],
             "avbd_world_add_bodies": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_add_joint": [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(u32)],
+            "avbd_world_remove_body": [vp, u32],
             "avbd_world_body_count": [vp, C.POINTER(u32)],
             "avbd_world_scene_count": [vp, C.POINTER(u32)],
             "avbd_world_get_bodies": [vp, u32, u32, vp],
@@ -154,6 +155,10 @@ class AvbdWorld:
         return self.add_bodies(bodies_array([rec]))
 
     # PhysicsEngine::add_joint
+    def remove_body(self, handle):
+        """PhysicsEngine::remove_body: the last body takes over the handle."""
+        _check(lib().avbd_world_remove_body(self.h, int(handle)), "remove_body")
+
     def add_joint(self, desc):
         hj = C.c_uint32()
         _check(lib().avbd_world_add_joint(self.h, C.byref(desc), C.byref(hj)), "add_joint")

@@ -41,6 +41,9 @@ static __device__ __forceinline__ void load_ctx(const DW& w, uint32_t p, PairCtx
     c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
     c.rad_a = w.shp[c.a].x;
     c.rad_b = w.shp[c.b].x;
+    float4 ma = w.mat[c.a], mb = w.mat[c.b];
+    c.mu_roll = fmaxf(ma.z, mb.z);
+    c.mu_spin = fmaxf(ma.w, mb.w);
     if (c.gap <= 0.0f) {
         c.t1 = tangent_t1(c.n);
         c.t2 = cross(c.t1, c.n);
@@ -88,7 +91,7 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
     if (row_live(cn, f[0])) stamp_row(s, c.n, pen.x, f[0], r_side, sign);
     if (row_live(ct1, f[1])) stamp_row(s, t1, pen.y, f[1], r_side_f, sign);
     if (row_live(ct2, f[2])) stamp_row(s, t2, pen.z, f[2], r_side_f, sign);
-    float mu_roll = fmaxf(w.mat[c.a].z, w.mat[c.b].z), mu_spin = fmaxf(w.mat[c.a].w, w.mat[c.b].w);
+    const float mu_roll = c.mu_roll, mu_spin = c.mu_spin;
     if (mu_roll > 0.0f || mu_spin > 0.0f) {
         V3 wrel = c.dra - c.drb;
         float4 rl = w.q_roll[q];
@@ -331,8 +334,11 @@ __global__ void k_side_starts(DW w) {
     }
     w.side_cnt[MAX_COLOURS] = acc;
 }
-// Entries are placed with block-aggregated reservations; their order inside a
-// colour is irrelevant (each entry writes its own slot).
+// Entries are placed with block-aggregated reservations, so a colour's list
+// keeps roughly the pair order (neighbouring entries share bodies and point
+// arrays: grouping entries by point count instead lost more in locality than
+// it won in convergence); the exact order is irrelevant (each entry writes
+// its own slot).
 __global__ void k_side_place(DW w) {
     if (aborted_solve(w)) return;
     __shared__ uint32_t cnt[MAX_COLOURS], base[MAX_COLOURS];
@@ -358,6 +364,7 @@ __global__ void k_side_place(DW w) {
         __syncthreads();
     }
 }
+
 __global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
     if (aborted_solve(w)) return;
     const uint32_t s0 = w.side_cnt[colour], s1 = w.side_cnt[colour + 1];
@@ -443,9 +450,10 @@ static __device__ __forceinline__ void dual_point(const DW& w, const PairCtx& c,
         }
     }
     w.q_lam[q] = nl;
-    w.q_pen[q] = np4;
-    w.q_rb[q] = make_float4(rb.x, rb.y, rb.z, stuck ? 1.0f : 0.0f);
-    float mu_roll = fmaxf(w.mat[c.a].z, w.mat[c.b].z), mu_spin = fmaxf(w.mat[c.a].w, w.mat[c.b].w);
+    // penalties and the grip flag change in few iterations: store only changes
+    if (np4.x != pen.x || np4.y != pen.y || np4.z != pen.z) w.q_pen[q] = np4;
+    if (stuck != (rb.w != 0.0f)) reinterpret_cast<float*>(&w.q_rb[q])[3] = stuck ? 1.0f : 0.0f;
+    const float mu_roll = c.mu_roll, mu_spin = c.mu_spin;
     if (touching && (mu_roll > 0.0f || mu_spin > 0.0f)) {
         V3 wrel = c.dra - c.drb;
         float lam_n = fabsf(nl.x);

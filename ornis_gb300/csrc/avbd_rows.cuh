@@ -194,6 +194,7 @@ struct PairCtx {
     V3 t1, t2;      // friction frame (touching pairs)
     bool sph_a, sph_b;
     float rad_a, rad_b;
+    float mu_roll, mu_spin;  // max of the two bodies' rolling / torsion friction
 };
 
 static __device__ __forceinline__ float row_c_levers(const PairCtx& c, V3 u, float c0, V3 raw, V3 rbw) {

@@ -204,11 +204,24 @@ static __device__ __forceinline__ void support_face(V3 pos, Q rot, V3 half, V3 d
     fpos = pos + qrot(rot, off);
 }
 
+// For a box with collapsed extents (a support face, edge or corner of the
+// penetration branch), corner i and corner i ^ bit coincide along a collapsed
+// axis, and so do edges whose corners coincide.  A repeated feature gives the
+// same squared distance as its first occurrence, which never strictly wins,
+// so only first occurrences are tested: the result is the full loop's.
+// Edge keep masks by collapse pattern (bit 4: x, 2: y, 1: z), kObbEdges order.
+static __constant__ const uint16_t kEdgeKeep[8] = {0xfff, 0xf55, 0x5f3, 0x51, 0x33f, 0x15, 0x103, 0x1};
+static __device__ __forceinline__ int collapsed(V3 h) {
+    return (h.x == 0.0f ? 4 : 0) | (h.y == 0.0f ? 2 : 0) | (h.z == 0.0f ? 1 : 0);
+}
+
 // distance_box.rs:99-129 — closest corner/face and edge/edge features.
 static __device__ __noinline__ Dist feature_distance(V3 apos, Q arot, V3 ha, V3 bpos, Q brot, V3 hb) {
     V3 ax, ay, az, bx, by, bz;
     obb_axes(ha, arot, ax, ay, az);
     obb_axes(hb, brot, bx, by, bz);
+    const int ma = collapsed(ha), mb = collapsed(hb);
+    const uint32_t ka = kEdgeKeep[ma], kb = kEdgeKeep[mb];
     Dist res{INFINITY, apos, bpos};
     float best = INFINITY;
     auto consider = [&](V3 x, V3 y) {
@@ -219,17 +232,21 @@ static __device__ __noinline__ Dist feature_distance(V3 apos, Q arot, V3 ha, V3 
         }
     };
     for (int i = 0; i < 8; i++) {
+        if (i & ma) continue;
         V3 c = obb_corner(apos, ax, ay, az, i);
         consider(c, point_obb_closest(c, bpos, hb, brot));
     }
     for (int i = 0; i < 8; i++) {
+        if (i & mb) continue;
         V3 c = obb_corner(bpos, bx, by, bz, i);
         consider(point_obb_closest(c, apos, ha, arot), c);
     }
     for (int i = 0; i < 12; i++) {
+        if (!((ka >> i) & 1u)) continue;
         V3 a0 = obb_corner(apos, ax, ay, az, kObbEdges[i][0]);
         V3 a1 = obb_corner(apos, ax, ay, az, kObbEdges[i][1]);
         for (int j = 0; j < 12; j++) {
+            if (!((kb >> j) & 1u)) continue;
             V3 b0 = obb_corner(bpos, bx, by, bz, kObbEdges[j][0]);
             V3 b1 = obb_corner(bpos, bx, by, bz, kObbEdges[j][1]);
             V3 x, y;
@@ -253,121 +270,6 @@ static __device__ __forceinline__ Dist box_box(V3 apos, Q arot, V3 ha, V3 bpos, 
     return r;
 }
 
-// ---- warp-cooperative box-box (one pair per warp) ----------------------------
-// The 15 SAT axes and the 160 feature tests of distance_box.rs:21-142 are
-// dealt over the 32 lanes; the reductions keep the sequential loops'
-// selection rule exactly: the first index reaching the extreme value wins
-// (strict comparisons), NaN and infinite candidates never win.
-static __device__ __forceinline__ float separating_axis_warp(V3 apos, Q arot, V3 ha, V3 bpos, Q brot, V3 hb,
-                                                             V3& nout) {
-    const int lane = threadIdx.x & 31;
-    V3 aa[3], bb[3];
-    mat3_cols(arot, aa);
-    mat3_cols(brot, bb);
-    float gap = -INFINITY;
-    V3 n = VY();
-    if (lane < 15) {
-        V3 ax;
-        if (lane < 3) ax = aa[lane];
-        else if (lane < 6) ax = bb[lane - 3];
-        else {
-            int i = (lane - 6) / 3, j = (lane - 6) % 3;
-            V3 c = cross(aa[i], bb[j]);
-            ax = len2(c) > DEGENERATE_EPS ? normalize(c) : V0();
-        }
-        if (!veq(ax, V0())) {
-            float ea = ha.x * fabsf(dot(ax, aa[0])) + ha.y * fabsf(dot(ax, aa[1])) + ha.z * fabsf(dot(ax, aa[2]));
-            float eb = hb.x * fabsf(dot(ax, bb[0])) + hb.y * fabsf(dot(ax, bb[1])) + hb.z * fabsf(dot(ax, bb[2]));
-            float proj = dot(bpos - apos, ax);
-            gap = fabsf(proj) - ea - eb;
-            n = proj >= 0.0f ? ax : -ax;
-        }
-    }
-    bool valid = gap > -INFINITY;  // false for NaN too
-    float bg = gap;
-    int bl = valid ? lane : 64;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        float og = __shfl_xor_sync(0xffffffffu, bg, o);
-        int ol = __shfl_xor_sync(0xffffffffu, bl, o);
-        bool better = ol < 64 && (bl == 64 || og > bg || (og == bg && ol < bl));
-        if (better) {
-            bg = og;
-            bl = ol;
-        }
-    }
-    if (bl == 64) {
-        nout = VY();
-        return -INFINITY;
-    }
-    nout = V3{__shfl_sync(0xffffffffu, n.x, bl), __shfl_sync(0xffffffffu, n.y, bl), __shfl_sync(0xffffffffu, n.z, bl)};
-    return bg;
-}
-
-static __device__ __forceinline__ Dist feature_distance_warp(V3 apos, Q arot, V3 ha, V3 bpos, Q brot, V3 hb) {
-    const int lane = threadIdx.x & 31;
-    V3 ax, ay, az, bx, by, bz;
-    obb_axes(ha, arot, ax, ay, az);
-    obb_axes(hb, brot, bx, by, bz);
-    float best = INFINITY;
-    int bt = 1 << 30;
-    V3 px = apos, py = bpos;
-    for (int t = lane; t < 160; t += 32) {
-        V3 x, y;
-        if (t < 8) {
-            x = obb_corner(apos, ax, ay, az, t);
-            y = point_obb_closest(x, bpos, hb, brot);
-        } else if (t < 16) {
-            y = obb_corner(bpos, bx, by, bz, t - 8);
-            x = point_obb_closest(y, apos, ha, arot);
-        } else {
-            int e = t - 16, i = e / 12, j = e % 12;
-            seg_seg_closest(obb_corner(apos, ax, ay, az, kObbEdges[i][0]), obb_corner(apos, ax, ay, az, kObbEdges[i][1]),
-                            obb_corner(bpos, bx, by, bz, kObbEdges[j][0]), obb_corner(bpos, bx, by, bz, kObbEdges[j][1]),
-                            x, y);
-        }
-        float sq = len2(y - x);
-        if (sq < best) {
-            best = sq;
-            bt = t;
-            px = x;
-            py = y;
-        }
-    }
-    float bs = best;
-    int bl = lane, btt = bt;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        float os = __shfl_xor_sync(0xffffffffu, bs, o);
-        int ot = __shfl_xor_sync(0xffffffffu, btt, o);
-        int ol = __shfl_xor_sync(0xffffffffu, bl, o);
-        if (os < bs || (os == bs && ot < btt)) {
-            bs = os;
-            btt = ot;
-            bl = ol;
-        }
-    }
-    if (!(bs < INFINITY)) return Dist{INFINITY, apos, bpos};
-    Dist r;
-    r.dist = sqrtf(bs);
-    r.pa = V3{__shfl_sync(0xffffffffu, px.x, bl), __shfl_sync(0xffffffffu, px.y, bl), __shfl_sync(0xffffffffu, px.z, bl)};
-    r.pb = V3{__shfl_sync(0xffffffffu, py.x, bl), __shfl_sync(0xffffffffu, py.y, bl), __shfl_sync(0xffffffffu, py.z, bl)};
-    return r;
-}
-
-// box_box (distance_box.rs:131-142) with every lane of the warp taking part.
-static __device__ __forceinline__ Dist box_box_warp(V3 apos, Q arot, V3 ha, V3 bpos, Q brot, V3 hb, float* sat_gap) {
-    V3 n;
-    float gap = separating_axis_warp(apos, arot, ha, bpos, brot, hb, n);
-    *sat_gap = gap;
-    if (gap > 0.0f) return feature_distance_warp(apos, arot, ha, bpos, brot, hb);
-    V3 fa, ea, fb, eb;
-    support_face(apos, arot, ha, n, fa, ea);
-    support_face(bpos, brot, hb, -n, fb, eb);
-    Dist r = feature_distance_warp(fa, arot, ea, fb, brot, eb);
-    r.dist = gap;
-    return r;
-}
 
 // distance_box.rs:146-190 — segment vs solid box, piecewise quadratic.
 static __device__ __noinline__ void segment_box(V3 start, V3 end, V3 lo, V3 hi, V3& opoint, V3& oclosest, float& osq) {

@@ -877,6 +877,94 @@ int avbd_world_add_bodies(AvbdWorld* W, const AvbdBody* bodies, uint32_t n, uint
     return AVBD_OK;
 }
 
+// PhysicsEngine::remove_body (mod.rs:1241-1300) on a one-scene world.
+int avbd_world_remove_body(AvbdWorld* W, uint32_t hi) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    if (W->scene_off.size() != 2) return AVBD_ERR_UNSUPPORTED;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    const uint32_t N = (uint32_t)W->bodies.size();
+    if (hi >= N) return AVBD_OK;  // invalid handles are a no-op
+    const uint32_t last = N - 1;
+    auto map = [&](uint32_t h) { return h == last ? hi : h; };
+    if (W->w.evs) {
+        // device event state: trigger pairs of the removed body exit, the
+        // others are renumbered; touches and queued contact events are cleared
+        const DW& w = W->w;
+        uint32_t e[EV_NUM];
+        CK(cudaStreamSynchronize(W->st));
+        CK(cudaMemcpy(e, w.evs, sizeof(e), cudaMemcpyDeviceToHost));
+        std::vector<unsigned long long> prev(e[EV_TRIG_PREV]), keep;
+        if (!prev.empty()) CK(cudaMemcpy(prev.data(), w.trig_prev, prev.size() * 8, cudaMemcpyDeviceToHost));
+        std::vector<AvbdTriggerEvent> exits;
+        for (unsigned long long k : prev) {
+            uint32_t a = (uint32_t)(k & 0xffffffffu), b = (uint32_t)(k >> 32);
+            if (a == hi || b == hi) {
+                exits.push_back(AvbdTriggerEvent{a, b, 0u});
+            } else {
+                uint32_t x = map(a), y = map(b);
+                keep.push_back(((unsigned long long)std::max(x, y) << 32) | std::min(x, y));
+            }
+        }
+        std::sort(keep.begin(), keep.end());
+        uint32_t q = e[EV_TN];
+        for (const AvbdTriggerEvent& t : exits) {
+            if (q < w.tev_cap) CK(cudaMemcpy(w.tev + q, &t, sizeof(t), cudaMemcpyHostToDevice));
+            else e[EV_TDROP]++;
+            q++;
+        }
+        e[EV_TN] = std::min(q, w.tev_cap);
+        e[EV_TRIG_PREV] = (uint32_t)keep.size();
+        e[EV_N] = 0;
+        if (!keep.empty()) CK(cudaMemcpy(w.trig_prev, keep.data(), keep.size() * 8, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(w.evs, e, sizeof(e), cudaMemcpyHostToDevice));
+        CK(cudaMemset(w.toff, 0, ((size_t)w.N + 1) * 4));
+    }
+    W->bodies[hi] = W->bodies[last];
+    W->bodies.pop_back();
+    W->aux[hi] = W->aux[last];
+    W->aux.pop_back();
+    // pairs: a pair renumbered out of (a < b) order is never matched again by
+    // the reference's discovery (it keeps (a, b) as they map): drop it now
+    std::vector<AvbdPairState> pairs;
+    std::vector<AvbdPointState> points;
+    for (size_t i = 0; i < W->pairs.size(); i++) {
+        AvbdPairState p = W->pairs[i];
+        if (p.a == hi || p.b == hi) continue;
+        p.a = map(p.a);
+        p.b = map(p.b);
+        if (p.a >= p.b) continue;
+        pairs.push_back(p);
+        for (int k = 0; k < MAX_PTS; k++) points.push_back(W->points[i * MAX_PTS + k]);
+    }
+    W->pairs.swap(pairs);
+    W->points.swap(points);
+    std::vector<JointRec> joints;
+    for (JointRec j : W->joints) {
+        if (j.a == hi || j.b == hi) continue;
+        j.a = map(j.a);
+        j.b = map(j.b);
+        joints.push_back(j);
+    }
+    W->joints.swap(joints);
+    // every sleeper wakes (mod.rs:1294-1296, body.rs:412-418)
+    for (uint32_t h = 0; h < last; h++) {
+        AvbdBodyAux& a = W->aux[h];
+        if (!a.asleep) continue;
+        a.asleep = 0;
+        a.sleep_timer = 0.0f;
+        AvbdBody& b = W->bodies[h];
+        if (b.body_type == AVBD_BODY_DYNAMIC) {
+            bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
+            b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
+            shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, b.inertia);
+        }
+    }
+    W->scene_off.back() = last;
+    return AVBD_OK;
+}
+
 int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle) {
     if (!W || !d) return AVBD_ERR_INVALID_ARG;
     for (int k = 0; k < 3; k++)

@@ -65,6 +65,7 @@ def lib():
         L.oracle_gap_c0.argtypes = [vp, C.c_uint32, C.c_uint32]
         L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
         L.oracle_set_emit_period.argtypes = [vp, C.c_int32]
+        L.oracle_remove_body.argtypes = [vp, C.c_uint32]
         L.oracle_drain_contact_events.restype = C.c_uint32
         L.oracle_drain_contact_events.argtypes = [vp, vp, C.c_uint32]
         L.oracle_drain_trigger_events.restype = C.c_uint32
@@ -173,6 +174,9 @@ class OracleWorld:
         c = abi.AvbdCounters()
         lib().oracle_get_counters(self.h, C.byref(c))
         return c
+
+    def remove_body(self, handle):
+        lib().oracle_remove_body(self.h, int(handle))
 
     def set_emit_period(self, period):
         lib().oracle_set_emit_period(self.h, int(period))

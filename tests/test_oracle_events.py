@@ -120,3 +120,21 @@ def test_event_order_is_key_order():
     assert kinds == [abi.CONTACT_BEGIN] * 4 + [abi.CONTACT_HIT] * 4
     keys = [(int(e["body_a"]), int(e["body_b"])) for e in ev[:4]]
     assert keys == sorted(keys) == [(0, 1), (0, 2), (0, 3), (0, 4)]
+
+
+def test_remove_body_swaps_last_and_reports_trigger_exit():
+    """PhysicsEngine::remove_body (avbd/mod.rs:1241-1300)."""
+    sensor = O.body_new(abi.SHAPE_SPHERE, [1.0], [0, 0, 0], 0.0)
+    sensor.flags = abi.FLAG_TRIGGER
+    inside = O.body_new(abi.SHAPE_SPHERE, [0.3], [0.2, 0, 0], 1.0)
+    other = O.body_new(abi.SHAPE_SPHERE, [0.3], [9, 0, 0], 2.0)
+    w = world([sensor, inside, other])
+    w.step(DT)
+    assert [int(e["entered"]) for e in w.trigger_events()] == [1]
+    w.remove_body(1)
+    ev = w.trigger_events()
+    assert len(ev) == 1 and ev[0]["entered"] == 0 and (ev[0]["body_a"], ev[0]["body_b"]) == (0, 1)
+    b = w.bodies()
+    assert len(b) == 2 and b["mass"][1] == 2.0  # the last body took handle 1
+    w.remove_body(7)  # invalid handle: no-op
+    assert w.nbodies == 2
