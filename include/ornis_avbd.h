@@ -317,6 +317,11 @@ int avbd_profiler(int on);
  * on it: bodies of one colour are independent. */
 int avbd_set_work_order(AvbdWorld* world, int by_work);
 
+/* Scenes of at most `small_scene_max` bodies (0..2048, default 2048) are
+ * swept by one CTA each; larger ones by the device-wide radix sort and
+ * sweep.  Both give the same candidate set.  No reference counterpart. */
+int avbd_set_broadphase(AvbdWorld* world, int small_scene_max);
+
 int avbd_abi_version(void);
 
 /* ---- measurement (no reference counterpart: the reference publishes no

@@ -70,6 +70,7 @@ def lib():
             "avbd_scene_step_static": [C.POINTER(abi.AvbdParams), vp, u32, C.c_int32, vp],
             "avbd_world_graph_nodes_emit": [vp, C.POINTER(u32)],
             "avbd_set_events": [vp, C.c_int32],
+            "avbd_set_broadphase": [vp, C.c_int],
             "avbd_world_drain_contact_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_drain_trigger_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_event_counts": [vp, vp],
@@ -228,6 +229,9 @@ class AvbdWorld:
 
     def set_occupancy(self, min_blocks):
         _check(lib().avbd_set_occupancy(self.h, int(min_blocks)), "set_occupancy")
+
+    def set_broadphase(self, small_scene_max):
+        _check(lib().avbd_set_broadphase(self.h, int(small_scene_max)), "set_broadphase")
 
     def set_tuning(self, lanes, block):
         _check(lib().avbd_set_tuning(self.h, int(lanes), int(block)), "set_tuning")

@@ -1374,6 +1374,17 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
     return AVBD_OK;
 }
 
+int avbd_set_broadphase(AvbdWorld* W, int small_scene_max) {
+    if (!W || small_scene_max < 0 || small_scene_max > 2048) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);  // the sweep plan is built with the device buffers
+    if (rc) return rc;
+    W->tune.small_scene_max = small_scene_max;
+    W->n_alloc = 0;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
 int avbd_abi_version(void) { return AVBD_ABI_VERSION; }
 
 // Bracket a region for profilers started with collection off

@@ -96,3 +96,25 @@ def test_free_run_matches_oracle_snapshot_scene():
     pe, _ = P.pose_errors(sg["bodies"], so["bodies"], 1 / 60)
     assert pe < 1e-4
     assert o.counters().sleeping == g.counters().sleeping
+
+
+def test_pyramid_210_600_steps_within_1e3():
+    """The 20-row, 210-cube pyramid (dt 1/60, 10 iterations) run freely for
+    600 steps: final poses within 1e-3 of the oracle's (the long-run bar for
+    stable stacks), and both against the f64 oracle."""
+    bodies = scenes.pyramid_210()
+    params = abi.default_params()
+    o = O.OracleWorld(params, mode=O.COLOURED)
+    o.add_bodies(bodies)
+    o64 = O.OracleWorld(params, mode=O.COLOURED, use_double=True)
+    o64.add_bodies(bodies)
+    g = AvbdWorld(params, bodies=bodies)
+    o.step_fixed(600)
+    o64.step_fixed(600)
+    g.step_graph(600)
+    ref, ref64, got = o.bodies(), o64.bodies(), g.bodies()
+    err, _ = P.pose_errors(got, ref, params.step_dt)
+    err64, _ = P.pose_errors(got, ref64, params.step_dt)
+    err_o64, _ = P.pose_errors(ref, ref64, params.step_dt)
+    print(f"pyramid 600 steps: gpu vs f32 oracle {err:.2e}, gpu vs f64 {err64:.2e}, f32 oracle vs f64 {err_o64:.2e}")
+    assert err <= 1e-3
