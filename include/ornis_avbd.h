@@ -54,6 +54,9 @@ extern "C" {
 #define AVBD_SHAPE_BOX 1       /* [hx, hy, hz] half extents                     */
 #define AVBD_SHAPE_CAPSULE 2   /* [radius, half_height, -], axis = local +Y     */
 #define AVBD_SHAPE_HALFSPACE 3 /* [nx, ny, nz] outward unit normal, body-local */
+#define AVBD_SHAPE_CYLINDER 4  /* [radius, half_height, -], axis = local +Y     */
+#define AVBD_SHAPE_CONE 5      /* [radius, half_height, -], apex at +half_height */
+#define AVBD_SHAPE_HULL 6      /* [hull index, -, -]: a hull of avbd_world_add_hull */
 
 #define AVBD_BODY_DYNAMIC 0   /* BodyType::Dynamic   */
 #define AVBD_BODY_STATIC 1    /* BodyType::Static    */
@@ -225,6 +228,16 @@ int avbd_world_destroy(AvbdWorld* world);
  * scene; the first new handle is written to *first_handle. */
 int avbd_world_add_bodies(AvbdWorld* world, const AvbdBody* bodies, uint32_t n,
                           uint32_t* first_handle);
+
+/* Register a convex hull (ConvexHull, collision/shape.rs:317-365) that
+ * bodies of shape AVBD_SHAPE_HULL name by index in shape_params[0]: the
+ * reference hull's centroid-relative vertices (3 floats each, support scans
+ * them in this order), its triangle faces (3 vertex indices each, used to
+ * re-seat contact witnesses; may be empty) and its body-frame inertia per
+ * unit mass (ConvexHull::try_inertia(1)), used when a sleeping body wakes.
+ * The hull's bodies carry their own mass and inertia in their records. */
+int avbd_world_add_hull(AvbdWorld* world, const float* verts, uint32_t nverts, const uint32_t* faces,
+                        uint32_t nfaces, const float* unit_inertia, uint32_t* hull_id);
 
 /* PhysicsEngine::remove_body (engine.rs:40-43, avbd/mod.rs:1241-1300): the
  * last body moves into the freed handle; pairs and joints of the removed

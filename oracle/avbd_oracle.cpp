@@ -20,9 +20,11 @@
 //               independent, so the order inside a colour is immaterial.
 // Scalar T = float (bit-level parity) or double (the f64 error column).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <limits>
 #include <set>
 #include <thread>
@@ -84,7 +86,31 @@ static constexpr int SPATIAL_DOF = 6;
 template <class T> static inline T C(float v) { return T(v); }
 
 // ---- shapes --------------------------------------------------------------------
+// ConvexHull (collision/shape.rs:317-365): centroid-relative vertices and the
+// triangle faces the reference builds for hulls of at most 64 vertices.
+template <class T> struct Hull {
+    std::vector<V3<T>> verts;
+    std::vector<uint32_t> faces;  // 3 indices per face
+    T bound = T(0), min_ext = T(0);
+    V3<T> unit_inertia{};  // body-frame inertia per unit mass (ConvexHull::try_inertia)
+};
+// bound (rows.rs:268-272: the longest vertex) and smallest extent
+// (shape.rs:1468-1479) of a hull
+template <class T> static void hull_measures(Hull<T>& h) {
+    T b = T(0);
+    V3<T> lo{std::numeric_limits<T>::infinity(), std::numeric_limits<T>::infinity(),
+             std::numeric_limits<T>::infinity()};
+    V3<T> hi = -lo;
+    for (const V3<T>& v : h.verts) {
+        b = std::fmax(b, len(v));
+        lo = {std::fmin(lo.x, v.x), std::fmin(lo.y, v.y), std::fmin(lo.z, v.z)};
+        hi = {std::fmax(hi.x, v.x), std::fmax(hi.y, v.y), std::fmax(hi.z, v.z)};
+    }
+    h.bound = b;
+    h.min_ext = h.verts.empty() ? T(0) : std::fmax(min_element(hi - lo), T(0));
+}
 template <class T> struct Body {
+    const Hull<T>* hull = nullptr;  // AVBD_SHAPE_HULL only
     V3<T> pos;
     Qt<T> rot;
     V3<T> vel, angvel, torque;
@@ -103,8 +129,9 @@ template <class T> struct ShapeRef {
     V3<T> sp;
     V3<T> pos;
     Qt<T> rot;
+    const Hull<T>* hull;
 };
-template <class T> static ShapeRef<T> sref(const Body<T>& b) { return {&b, b.shape, b.sp, b.pos, b.rot}; }
+template <class T> static ShapeRef<T> sref(const Body<T>& b) { return {&b, b.shape, b.sp, b.pos, b.rot, b.hull}; }
 
 template <class T> struct Dist {
     T dist;
@@ -130,6 +157,18 @@ template <class T> static V3<T> shape_inertia(uint32_t shape, V3<T> sp, T mass) 
             T r = sp.x, h = sp.y;
             T iy = C<T>(0.5f) * mass * r * r;
             T ixz = C<T>(0.25f) * mass * (r * r) + (mass / T(3)) * h * r + C<T>(0.25f) * mass * h * h;
+            return {ixz, iy, ixz};
+        }
+        case AVBD_SHAPE_CYLINDER: {  // shape.rs:780-790
+            T r = sp.x, h = sp.y;
+            T iy = C<T>(0.5f) * mass * r * r;
+            T ixz = mass * (T(3) * r * r + T(4) * h * h) / T(12);
+            return {ixz, iy, ixz};
+        }
+        case AVBD_SHAPE_CONE: {  // shape.rs:791-801
+            T r = sp.x, h = sp.y;
+            T iy = C<T>(0.3f) * mass * r * r;
+            T ixz = mass * (T(3) * r * r + T(8) * h * h) / T(20);
             return {ixz, iy, ixz};
         }
         default:
@@ -474,13 +513,15 @@ template <class T> static Dist<T> box_capsule(V3<T> apos, Qt<T> arot, V3<T> half
     return {distance, apos + qrot(arot, surface), apos + qrot(arot, core - normal * radius)};
 }
 
+#include "avbd_gjk.hpp"
+
 template <class T> static Dist<T> halfspace_distance(V3<T> hpos, Qt<T> hrot, V3<T> ln, const ShapeRef<T>& o, bool first) {  // :607-642
     if (o.shape == AVBD_SHAPE_HALFSPACE) {
         T inf = std::numeric_limits<T>::infinity();
         return first ? Dist<T>{inf, hpos, o.pos} : Dist<T>{inf, o.pos, hpos};
     }
     V3<T> n = qrot(hrot, ln);
-    V3<T> s = support(o.shape, o.sp, o.pos, o.rot, -n);
+    V3<T> s = support_any(o, -n);
     T dist = dot(s - hpos, n);
     Dist<T> d{dist, s - n * dist, s};
     if (first) return d;
@@ -492,6 +533,7 @@ template <class T> static Dist<T> shape_distance(const ShapeRef<T>& a, const Sha
     if (a.shape == AVBD_SHAPE_HALFSPACE) return halfspace_distance(a.pos, a.rot, a.sp, b, true);
     if (b.shape == AVBD_SHAPE_HALFSPACE) return halfspace_distance(b.pos, b.rot, b.sp, a, false);
     uint32_t sa = a.shape, sb = b.shape;
+    if (gjk_shape<T>(sa) || gjk_shape<T>(sb)) return gjk_pair_distance(a, b);  // distance.rs:811-817
     auto swap = [](Dist<T> d) { return Dist<T>{d.dist, d.pb, d.pa}; };
     if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_SPHERE) return sphere_sphere(a.pos, a.sp.x, b.pos, b.sp.x);
     if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_BOX) return sphere_obb(a.pos, a.sp.x, b.pos, b.rot, b.sp);
@@ -626,6 +668,9 @@ template <class T> static T bound_radius(const Body<T>& b) {  // rows.rs:253-292
         case AVBD_SHAPE_SPHERE: return b.sp.x;
         case AVBD_SHAPE_BOX: return len(b.sp);
         case AVBD_SHAPE_CAPSULE: return b.sp.y + b.sp.x;
+        case AVBD_SHAPE_CYLINDER:
+        case AVBD_SHAPE_CONE: return std::sqrt(b.sp.x * b.sp.x + b.sp.y * b.sp.y);
+        case AVBD_SHAPE_HULL: return b.hull ? b.hull->bound : T(0);
         default: return std::numeric_limits<T>::infinity();
     }
 }
@@ -634,6 +679,9 @@ template <class T> static T shape_min_dimension(const Body<T>& b) {  // rows.rs:
         case AVBD_SHAPE_SPHERE: return b.sp.x;
         case AVBD_SHAPE_BOX: return min_element(b.sp);
         case AVBD_SHAPE_CAPSULE: return b.sp.x;
+        case AVBD_SHAPE_CYLINDER: return fmn(b.sp.x, b.sp.y);
+        case AVBD_SHAPE_CONE: return C<T>(K::HALF) * fmn(b.sp.x, b.sp.y);
+        case AVBD_SHAPE_HULL: return C<T>(K::HALF) * (b.hull ? b.hull->min_ext : T(0));
         default: return std::numeric_limits<T>::infinity();
     }
 }
@@ -767,8 +815,17 @@ template <class T> struct Engine {
         if (b.type == AVBD_BODY_DYNAMIC) {
             T m = b.mass;
             b.inv_mass = (m > T(0)) ? T(1) / m : T(0);
-            b.inertia = shape_inertia(b.shape, b.sp, m);
+            b.inertia = b.shape == AVBD_SHAPE_HULL ? (b.hull && m > T(0) && std::isfinite(m) ? b.hull->unit_inertia * m
+                                                                                         : VZERO<T>())
+                                                   : shape_inertia(b.shape, b.sp, m);
         }
+    }
+    std::deque<Hull<T>> hulls;  // stable addresses: bodies point at them
+    void link_hull(Body<T>& b) {
+        b.hull = nullptr;
+        if (b.shape != AVBD_SHAPE_HULL) return;
+        double id = (double)b.sp.x;
+        if (id >= 0.0 && id < (double)hulls.size()) b.hull = &hulls[(size_t)id];
     }
 
     // ---- joints / sleep (avbd/sleep.rs) ----
@@ -1496,7 +1553,7 @@ template <class T> struct Engine {
                 bool hit = false;
                 V3<T> hn{}, hp{};
                 for (int it = 0; it < 24; it++) {
-                    ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot};
+                    ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot, mb.hull};
                     Dist<T> d = shape_distance(mv, tgt);
                     if (d.dist <= C<T>(K::SHAPE_TOUCH)) {
                         if (t > T(0)) { hit = true; hn = normalize_or(d.pa - d.pb, -dir); hp = d.pb; }
@@ -1914,9 +1971,49 @@ void oracle_set_faithful_scan(OracleWorld* w, int on) { DISPATCH(w, E.faithful_s
 int oracle_add_bodies(OracleWorld* w, const AvbdBody* b, uint32_t n) {
     DISPATCH(w, {
         using TT = std::remove_reference_t<decltype(E.dt)>;
-        for (uint32_t i = 0; i < n; i++) E.bodies.push_back(from_desc<TT>(b[i]));
+        for (uint32_t i = 0; i < n; i++) {
+            E.bodies.push_back(from_desc<TT>(b[i]));
+            E.link_hull(E.bodies.back());
+        }
     });
     return AVBD_OK;
+}
+// A convex hull (centroid-relative vertices, triangle faces as 3 indices,
+// body-frame inertia per unit mass); bodies of shape AVBD_SHAPE_HULL name it
+// by index in shape_params[0].  Returns the index.
+uint32_t oracle_add_hull(OracleWorld* w, const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf,
+                         const float* unit_inertia) {
+    uint32_t id = 0;
+    DISPATCH(w, {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        Hull<TT> h;
+        for (uint32_t i = 0; i < nv; i++) h.verts.push_back({TT(verts[3 * i]), TT(verts[3 * i + 1]), TT(verts[3 * i + 2])});
+        h.faces.assign(faces, faces + 3 * nf);
+        h.unit_inertia = {TT(unit_inertia[0]), TT(unit_inertia[1]), TT(unit_inertia[2])};
+        hull_measures(h);
+        id = (uint32_t)E.hulls.size();
+        E.hulls.push_back(std::move(h));
+    });
+    return id;
+}
+// Test hooks: the raw GJK/EPA query (gjk.rs:589-638) and the full
+// shape_distance between bodies ia and ib.  out = dist, normal[3] (GJK only),
+// pa[3], pb[3].
+void oracle_convex_distance(OracleWorld* w, uint32_t ia, uint32_t ib, float* out) {
+    DISPATCH(w, {
+        auto g = convex_distance(sref(E.bodies[ia]), sref(E.bodies[ib]));
+        float v[10] = {(float)g.dist, (float)g.normal.x, (float)g.normal.y, (float)g.normal.z, (float)g.pa.x,
+                       (float)g.pa.y, (float)g.pa.z, (float)g.pb.x, (float)g.pb.y, (float)g.pb.z};
+        std::memcpy(out, v, sizeof(v));
+    });
+}
+void oracle_shape_distance(OracleWorld* w, uint32_t ia, uint32_t ib, float* out) {
+    DISPATCH(w, {
+        auto d = shape_distance(sref(E.bodies[ia]), sref(E.bodies[ib]));
+        float v[10] = {(float)d.dist, 0.0f, 0.0f, 0.0f, (float)d.pa.x, (float)d.pa.y, (float)d.pa.z,
+                       (float)d.pb.x, (float)d.pb.y, (float)d.pb.z};
+        std::memcpy(out, v, sizeof(v));
+    });
 }
 int oracle_remove_body(OracleWorld* w, uint32_t handle) {
     DISPATCH(w, E.remove_body(handle));
@@ -1983,7 +2080,10 @@ int oracle_set_bodies(OracleWorld* w, const AvbdBody* in, uint32_t n) {
     DISPATCH(w, {
         using TT = std::remove_reference_t<decltype(E.dt)>;
         if (n != E.bodies.size()) return AVBD_ERR_INVALID_ARG;
-        for (uint32_t i = 0; i < n; i++) E.bodies[i] = from_desc<TT>(in[i]);
+        for (uint32_t i = 0; i < n; i++) {
+            E.bodies[i] = from_desc<TT>(in[i]);
+            E.link_hull(E.bodies[i]);
+        }
     });
     return AVBD_OK;
 }
@@ -2058,7 +2158,10 @@ int oracle_import_state(OracleWorld* w, const AvbdBody* bodies, const AvbdBodyAu
         E.ensure_scratch();
         size_t n = E.bodies.size();
         for (size_t i = 0; i < n; i++) {
-            if (bodies) E.bodies[i] = from_desc<TT>(bodies[i]);
+            if (bodies) {
+                E.bodies[i] = from_desc<TT>(bodies[i]);
+                E.link_hull(E.bodies[i]);
+            }
             if (aux) {
                 E.prev_pos[i] = {TT(aux[i].prev_position[0]), TT(aux[i].prev_position[1]), TT(aux[i].prev_position[2])};
                 E.prev_rot[i] = {TT(aux[i].prev_orientation[0]), TT(aux[i].prev_orientation[1]),
@@ -2177,7 +2280,8 @@ int oracle_body_new(uint32_t shape, const float* params, const float* position, 
     float rest = 0.3f, fric = 0.5f;
     float sp[3] = {params[0], params[1], params[2]};
     if (shape == AVBD_SHAPE_SPHERE) { rest = 0.5f; fric = 0.3f; }
-    else if (shape == AVBD_SHAPE_CAPSULE) { rest = 0.4f; fric = 0.4f; }
+    else if (shape == AVBD_SHAPE_CAPSULE || shape == AVBD_SHAPE_CYLINDER) { rest = 0.4f; fric = 0.4f; }  // body.rs:580-591
+    else if (shape == AVBD_SHAPE_CONE) { rest = 0.3f; fric = 0.5f; }  // body.rs:596-607
     else if (shape == AVBD_SHAPE_HALFSPACE) {
         if (mass > 0.0f && std::isfinite(mass)) return AVBD_ERR_INVALID_ARG;
         V3<float> nn = normalize_or(V3<float>{sp[0], sp[1], sp[2]}, VZERO<float>());

@@ -28,6 +28,9 @@ SHAPE_SPHERE = 0
 SHAPE_BOX = 1
 SHAPE_CAPSULE = 2
 SHAPE_HALFSPACE = 3
+SHAPE_CYLINDER = 4
+SHAPE_CONE = 5
+SHAPE_HULL = 6
 
 BODY_DYNAMIC = 0
 BODY_STATIC = 1

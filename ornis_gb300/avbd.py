@@ -44,6 +44,7 @@ def lib():
             "avbd_world_add_bodies": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_add_joint": [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(u32)],
             "avbd_world_remove_body": [vp, u32],
+            "avbd_world_add_hull": [vp, vp, u32, vp, u32, vp, C.POINTER(u32)],
             "avbd_world_body_count": [vp, C.POINTER(u32)],
             "avbd_world_scene_count": [vp, C.POINTER(u32)],
             "avbd_world_get_bodies": [vp, u32, u32, vp],
@@ -156,6 +157,16 @@ class AvbdWorld:
         return self.add_bodies(bodies_array([rec]))
 
     # PhysicsEngine::add_joint
+    def add_hull(self, verts, faces=(), unit_inertia=(1.0, 1.0, 1.0)):
+        """Register a convex hull; bodies of shape SHAPE_HULL name it by index."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float32).reshape(-1))
+        f = np.ascontiguousarray(np.asarray(faces, dtype=np.uint32).reshape(-1))
+        ui = np.ascontiguousarray(np.asarray(unit_inertia, dtype=np.float32))
+        out = C.c_uint32()
+        _check(lib().avbd_world_add_hull(self.h, abi.ptr(v), len(v) // 3, abi.ptr(f) if len(f) else None,
+                                         len(f) // 3, abi.ptr(ui), C.byref(out)), "add_hull")
+        return out.value
+
     def remove_body(self, handle):
         """PhysicsEngine::remove_body: the last body takes over the handle."""
         _check(lib().avbd_world_remove_body(self.h, int(handle)), "remove_body")

@@ -55,7 +55,13 @@ static __device__ __forceinline__ bool solvable(const DW& w, uint32_t h) {
 static __device__ __forceinline__ bool solved(const DW& w, uint32_t h) { return solvable(w, h) && !w.asleep[h]; }
 static __device__ __forceinline__ Shape shape_of(const DW& w, uint32_t h) {
     float4 sp = w.shp[h];
-    return Shape{info_shape(w.info[h]), V3{sp.x, sp.y, sp.z}, ld3(w.pos[h]), ldq(w.rot[h])};
+    uint32_t kind = info_shape(w.info[h]);
+    const HullDesc* hull = nullptr;
+    if (kind == AVBD_SHAPE_HULL) {
+        uint32_t id = (uint32_t)sp.x;
+        hull = id < w.nhulls ? &w.hulls[id] : nullptr;
+    }
+    return Shape{kind, V3{sp.x, sp.y, sp.z}, ld3(w.pos[h]), ldq(w.rot[h]), hull};
 }
 // rows.rs:366-368
 static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uint32_t b) {

@@ -114,7 +114,7 @@ static __device__ __forceinline__ void k_disc_filter_one(const DW& w, uint32_t c
     w.keep[c] = d.keep;
     if (d.keep) agg_inc_at(w.cnt, ab.x);
 }
-__global__ void k_disc_filter(DW w, int triggers) {
+__global__ void __launch_bounds__(128, 4) k_disc_filter(DW w, int triggers) {
     if (aborted(w)) return;
     const uint32_t n = n_cand(w);
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
@@ -346,7 +346,7 @@ static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2
     agg_add(&w.ctr[C_POINTS], (uint32_t)nf);
 }
 // cls 0: box-box pairs, 1: one box, 2: no box
-__global__ void k_disc_build(DW w, int cls) {
+__global__ void __launch_bounds__(128, 4) k_disc_build(DW w, int cls) {
     if (aborted(w)) return;
     const uint32_t n = w.ctr[cls == 0 ? C_BOXPAIRS : (cls == 1 ? C_BOXONE : C_NOBOX)];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -100,10 +100,17 @@ __global__ void k_torque(DW w) {
 void launch_torque(const DW& w, cudaStream_t st) { k_torque<<<nblk(w.N, 256), 256, 0, st>>>(w); }
 
 // ---- broadphase ---------------------------------------------------------------
-static __device__ __forceinline__ float min_dim(uint32_t kind, float4 sp) {  // rows.rs:373-403
+// shape_min_dimension (rows.rs:373-403)
+static __device__ __forceinline__ float min_dim(const DW& w, uint32_t kind, float4 sp) {
     if (kind == AVBD_SHAPE_SPHERE) return sp.x;
     if (kind == AVBD_SHAPE_BOX) return fminf(sp.x, fminf(sp.y, sp.z));
     if (kind == AVBD_SHAPE_CAPSULE) return sp.x;
+    if (kind == AVBD_SHAPE_CYLINDER) return fminf(sp.x, sp.y);
+    if (kind == AVBD_SHAPE_CONE) return HALF * fminf(sp.x, sp.y);
+    if (kind == AVBD_SHAPE_HULL) {
+        uint32_t id = (uint32_t)sp.x;
+        return HALF * (id < w.nhulls ? w.hulls[id].min_ext : 0.0f);
+    }
     return INFINITY;
 }
 // CCD mover gate (mod.rs:882-895): returns the step travel |v h| of a body
@@ -112,7 +119,7 @@ static __device__ __forceinline__ float ccd_travel(const DW& w, uint32_t h) {
     if (!w.enable_ccd || !solvable(w, h) || w.asleep[h] || info_trigger(w.info[h])) return 0.0f;
     V3 disp = ld3(w.vel[h]) * w.dt;
     float l = len(disp);
-    if (l <= CCD_TRAVEL_GATE_FRACTION * min_dim(info_shape(w.info[h]), w.shp[h])) return 0.0f;
+    if (l <= CCD_TRAVEL_GATE_FRACTION * min_dim(w, info_shape(w.info[h]), w.shp[h])) return 0.0f;
     if (l < NEAR_ZERO) return 0.0f;
     return l;
 }

@@ -1,5 +1,6 @@
 // avbd_shapes.cuh — narrowphase geometry on the device: signed surface
-// distance with witness points for sphere / box / capsule / half-space pairs.
+// distance with witness points for sphere / box / capsule / half-space pairs
+// (analytic) and cylinder / cone / convex-hull pairs (GJK / EPA, avbd_gjk.cuh).
 //
 // Semantics follow the reference's analytic oracles one for one (citations to
 // crates/physics/src/collision/): the pair set, the contact normal and the
@@ -7,6 +8,8 @@
 // reference bit for bit on identical input (this translation unit is built
 // with -fmad=false; see avbd_vec.cuh for the operation order).
 #pragma once
+#include <cfloat>
+
 #include "avbd_world.cuh"
 
 namespace avbd {
@@ -20,6 +23,7 @@ struct Shape {
     V3 p;  // params
     V3 pos;
     Q rot;
+    const HullDesc* hull;  // AVBD_SHAPE_HULL only
 };
 
 static __device__ __forceinline__ V3 point_segment_closest(V3 p, V3 a, V3 b) {  // distance.rs:63-71
@@ -382,10 +386,12 @@ static __device__ __noinline__ Dist box_capsule(V3 apos, Q arot, V3 half, V3 bpo
     return {distance, apos + qrot(arot, surface), apos + qrot(arot, core - normal * radius)};
 }
 
+#include "avbd_gjk.cuh"
+
 static __device__ __forceinline__ Dist halfspace_distance(const Shape& h, const Shape& o, bool first) {  // distance.rs:607-642
     if (o.kind == AVBD_SHAPE_HALFSPACE) return first ? Dist{INFINITY, h.pos, o.pos} : Dist{INFINITY, o.pos, h.pos};
     V3 n = qrot(h.rot, h.p);
-    V3 s = support(o, -n);
+    V3 s = support_any(o, -n);
     float dist = dot(s - h.pos, n);
     Dist d{dist, s - n * dist, s};
     if (first) return d;
@@ -398,6 +404,7 @@ static __device__ __noinline__ Dist shape_distance(const Shape& a, const Shape& 
     if (a.kind == AVBD_SHAPE_HALFSPACE) return halfspace_distance(a, b, true);
     if (b.kind == AVBD_SHAPE_HALFSPACE) return halfspace_distance(b, a, false);
     uint32_t sa = a.kind, sb = b.kind;
+    if (gjk_shape(sa) || gjk_shape(sb)) return gjk_pair_distance(a, b);  // distance.rs:811-817
     if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_SPHERE) return sphere_sphere(a.pos, a.p.x, b.pos, b.p.x);
     if (sa == AVBD_SHAPE_SPHERE && sb == AVBD_SHAPE_BOX) return sphere_obb(a.pos, a.p.x, b.pos, b.rot, b.p);
     if (sa == AVBD_SHAPE_BOX && sb == AVBD_SHAPE_SPHERE) {

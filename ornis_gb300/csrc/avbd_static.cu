@@ -80,6 +80,8 @@ float bound_of(const AvbdBody& b) {  // rows.rs:253-292
         case AVBD_SHAPE_SPHERE: return p[0];
         case AVBD_SHAPE_BOX: return std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
         case AVBD_SHAPE_CAPSULE: return p[1] + p[0];
+        case AVBD_SHAPE_CYLINDER:
+        case AVBD_SHAPE_CONE: return std::sqrt(p[0] * p[0] + p[1] * p[1]);
         default: return INFINITY;
     }
 }
@@ -100,6 +102,13 @@ void inertia_of(const AvbdBody& b, float m, float out[3]) {  // collision/shape.
         float ixz = 0.25f * m * (r * r) + (m / 3.0f) * h * r + 0.25f * m * h * h;
         out[0] = ixz;
         out[1] = 0.5f * m * r * r;
+        out[2] = ixz;
+    } else if (b.shape == AVBD_SHAPE_CYLINDER || b.shape == AVBD_SHAPE_CONE) {
+        float r = sp[0], h = sp[1];
+        bool cyl = b.shape == AVBD_SHAPE_CYLINDER;
+        float ixz = m * (3.0f * r * r + (cyl ? 4.0f : 8.0f) * h * h) / (cyl ? 12.0f : 20.0f);
+        out[0] = ixz;
+        out[1] = (cyl ? 0.5f : 0.3f) * m * r * r;
         out[2] = ixz;
     }
 }
@@ -151,6 +160,7 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
         for (int k = 0; k < 16; k++)
             if (!std::isfinite(f[k])) return AVBD_ERR_NONFINITE;
         if (!std::isfinite(bodies[i].mass) || !std::isfinite(bodies[i].inv_mass)) return AVBD_ERR_NONFINITE;
+        if (bodies[i].shape == AVBD_SHAPE_HULL) return AVBD_ERR_UNSUPPORTED;  // hull tables live in worlds
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return AVBD_ERR_DEVICE;

@@ -56,11 +56,25 @@ struct PairBuf {
     uint32_t* offA;
 };
 
-float shape_bound(uint32_t shape, const float* p) {  // rows.rs:253-292
+// A convex hull as the host keeps it (ConvexHull, collision/shape.rs:317-365).
+struct HostHull {
+    std::vector<float4> v;
+    std::vector<uint32_t> f;
+    float unit_inertia[3];
+    float bound, min_ext;
+};
+
+float shape_bound(uint32_t shape, const float* p, const std::vector<HostHull>& hulls) {  // rows.rs:253-292
     switch (shape) {
         case AVBD_SHAPE_SPHERE: return p[0];
         case AVBD_SHAPE_BOX: return std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
         case AVBD_SHAPE_CAPSULE: return p[1] + p[0];
+        case AVBD_SHAPE_CYLINDER:
+        case AVBD_SHAPE_CONE: return std::sqrt(p[0] * p[0] + p[1] * p[1]);
+        case AVBD_SHAPE_HULL: {
+            size_t id = (size_t)p[0];
+            return id < hulls.size() ? hulls[id].bound : 0.0f;
+        }
         default: return INFINITY;
     }
 }
@@ -85,7 +99,25 @@ void shape_inertia(uint32_t shape, const float* sp, float mass, float out[3]) {
         out[0] = ixz;
         out[1] = iy;
         out[2] = ixz;
+    } else if (shape == AVBD_SHAPE_CYLINDER || shape == AVBD_SHAPE_CONE) {  // shape.rs:780-801
+        float r = sp[0], h = sp[1];
+        bool cyl = shape == AVBD_SHAPE_CYLINDER;
+        float iy = (cyl ? 0.5f : 0.3f) * mass * r * r;
+        float ixz = mass * (3.0f * r * r + (cyl ? 4.0f : 8.0f) * h * h) / (cyl ? 12.0f : 20.0f);
+        out[0] = ixz;
+        out[1] = iy;
+        out[2] = ixz;
     }
+}
+// rest inertia of a body: its shape's, or the hull's per-unit-mass inertia times the mass
+static void rest_inertia(const AvbdBody& b, float mass, const std::vector<HostHull>& hulls, float out[3]) {
+    if (b.shape != AVBD_SHAPE_HULL) {
+        shape_inertia(b.shape, b.shape_params, mass, out);
+        return;
+    }
+    size_t id = (size_t)b.shape_params[0];
+    for (int k = 0; k < 3; k++)
+        out[k] = (id < hulls.size() && mass > 0.0f && std::isfinite(mass)) ? hulls[id].unit_inertia[k] * mass : 0.0f;
 }
 float hinge_twist_host(const float qa[4], const float qb[4], const float ax[3]) {  // sequential_impulse/joints.rs:38-48
     // q = conj(qa) * qb (Hamilton product, avbd/rows.rs:91-98 order)
@@ -139,6 +171,8 @@ struct AvbdWorld {
     int ev_period = 0;
     bool has_trig = false;
     Alloc evmem;  // the event queues: kept across reallocations of the world
+    std::vector<HostHull> hulls;
+    Alloc hullmem;
     int graph_cols = 0;
     size_t graph_nodes = 0;       // kernel nodes in one captured substep (no events)
     size_t graph_nodes_emit = 0;  // ... in one that reports events
@@ -416,6 +450,37 @@ static int upload_all(AvbdWorld* W) {
     }
     DW& w = W->w;
     cudaStream_t st = W->st;
+    // convex hull tables (rebuilt on every full upload: hulls are few and small)
+    W->hullmem.release();
+    w.hulls = nullptr;
+    w.nhulls = 0;
+    if (!W->hulls.empty()) {
+        size_t nv = 0, nf = 0;
+        for (const HostHull& h : W->hulls) {
+            nv += h.v.size();
+            nf += h.f.size();
+        }
+        float4* dv = W->hullmem.get<float4>(nv);
+        uint32_t* df = W->hullmem.get<uint32_t>(nf);
+        HullDesc* dd = W->hullmem.get<HullDesc>(W->hulls.size());
+        if (!dv || !df || !dd) return AVBD_ERR_DEVICE;
+        std::vector<HullDesc> desc;
+        size_t ov = 0, of = 0;
+        for (const HostHull& h : W->hulls) {
+            if (!h.v.empty()) CK(cudaMemcpy(dv + ov, h.v.data(), h.v.size() * 16, cudaMemcpyHostToDevice));
+            if (!h.f.empty()) CK(cudaMemcpy(df + of, h.f.data(), h.f.size() * 4, cudaMemcpyHostToDevice));
+            desc.push_back(HullDesc{dv + ov, df + of, (uint32_t)h.v.size(), (uint32_t)(h.f.size() / 3), h.bound,
+                                    h.min_ext});
+            ov += h.v.size();
+            of += h.f.size();
+        }
+        CK(cudaMemcpy(dd, desc.data(), desc.size() * sizeof(HullDesc), cudaMemcpyHostToDevice));
+        w.hulls = dd;
+        w.nhulls = (uint32_t)desc.size();
+    }
+    for (uint32_t h = 0; h < N; h++)
+        if (W->bodies[h].shape == AVBD_SHAPE_HULL && !((size_t)W->bodies[h].shape_params[0] < W->hulls.size()))
+            return AVBD_ERR_INVALID_ARG;  // names a hull that was never added
     // static per-body data
     std::vector<uint32_t> scene_of(N), info(N);
     std::vector<float4> shp(N), inertia_rest(N);
@@ -436,10 +501,11 @@ static int upload_all(AvbdWorld* W) {
         const AvbdBody& b = W->bodies[h];
         if (b.flags & AVBD_FLAG_TRIGGER) W->has_trig = true;
         info[h] = (b.shape & 15u) | ((b.body_type & 3u) << 4) | ((b.flags & AVBD_FLAG_TRIGGER) ? 64u : 0u);
-        shp[h] = make_float4(b.shape_params[0], b.shape_params[1], b.shape_params[2], shape_bound(b.shape, b.shape_params));
+        shp[h] = make_float4(b.shape_params[0], b.shape_params[1], b.shape_params[2],
+                             shape_bound(b.shape, b.shape_params, W->hulls));
         float in[3];
         bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
-        shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, in);
+        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, in);
         inertia_rest[h] = make_float4(in[0], in[1], in[2], 0.0f);
         inv_rest[h] = free_mass ? 1.0f / b.mass : 0.0f;
         const AvbdBodyAux& a = W->aux[h];
@@ -851,6 +917,7 @@ int avbd_world_destroy(AvbdWorld* W) {
     free_graphs(W);
     W->mem.release();
     W->evmem.release();
+    W->hullmem.release();
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
     if (W->st) cudaStreamDestroy(W->st);
     delete W;
@@ -874,6 +941,42 @@ int avbd_world_add_bodies(AvbdWorld* W, const AvbdBody* bodies, uint32_t n, uint
     }
     W->scene_off.back() = (uint32_t)W->bodies.size();
     if (first_handle) *first_handle = first;
+    return AVBD_OK;
+}
+
+// A convex hull shared by bodies of shape AVBD_SHAPE_HULL (ConvexHull,
+// collision/shape.rs:317-365): the reference's centroid-relative vertices and
+// triangle faces, and its inertia per unit mass (ConvexHull::try_inertia).
+int avbd_world_add_hull(AvbdWorld* W, const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf,
+                        const float* unit_inertia, uint32_t* hull_id) {
+    if (!W || !unit_inertia || (nv && !verts) || (nf && !faces)) return AVBD_ERR_INVALID_ARG;
+    HostHull h;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    h.bound = 0.0f;
+    for (uint32_t i = 0; i < nv; i++) {
+        const float* p = verts + 3 * i;
+        if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2])) return AVBD_ERR_NONFINITE;
+        h.v.push_back(make_float4(p[0], p[1], p[2], 0.0f));
+        h.bound = std::fmax(h.bound, std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]));
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::fmin(lo[k], p[k]);
+            hi[k] = std::fmax(hi[k], p[k]);
+        }
+    }
+    h.min_ext = nv ? std::fmax(std::fmin(hi[0] - lo[0], std::fmin(hi[1] - lo[1], hi[2] - lo[2])), 0.0f) : 0.0f;
+    for (uint32_t i = 0; i < 3 * nf; i++) {
+        if (faces[i] >= nv) return AVBD_ERR_INVALID_ARG;
+        h.f.push_back(faces[i]);
+    }
+    for (int k = 0; k < 3; k++) {
+        if (!std::isfinite(unit_inertia[k])) return AVBD_ERR_NONFINITE;
+        h.unit_inertia[k] = unit_inertia[k];
+    }
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);  // the device tables are rebuilt at the next upload
+    if (rc) return rc;
+    if (hull_id) *hull_id = (uint32_t)W->hulls.size();
+    W->hulls.push_back(std::move(h));
     return AVBD_OK;
 }
 
@@ -958,7 +1061,7 @@ int avbd_world_remove_body(AvbdWorld* W, uint32_t hi) {
         if (b.body_type == AVBD_BODY_DYNAMIC) {
             bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
             b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
-            shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, b.inertia);
+            rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
         }
     }
     W->scene_off.back() = last;
@@ -985,7 +1088,7 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
             if (b.body_type == AVBD_BODY_DYNAMIC) {
                 bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
                 b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
-                shape_inertia(b.shape, b.shape_params, free_mass ? b.mass : 0.0f, b.inertia);
+                rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
             }
         }
     if (d->body_a == d->body_b) return AVBD_ERR_JOINT_SELF;
@@ -1305,7 +1408,8 @@ int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const flo
     float rest = 0.3f, fric = 0.5f;
     float sp[3] = {params[0], params[1], params[2]};
     if (shape == AVBD_SHAPE_SPHERE) { rest = 0.5f; fric = 0.3f; }
-    else if (shape == AVBD_SHAPE_CAPSULE) { rest = 0.4f; fric = 0.4f; }
+    else if (shape == AVBD_SHAPE_CAPSULE || shape == AVBD_SHAPE_CYLINDER) { rest = 0.4f; fric = 0.4f; }
+    else if (shape == AVBD_SHAPE_CONE) { rest = 0.3f; fric = 0.5f; }
     else if (shape == AVBD_SHAPE_HALFSPACE) {
         if (mass > 0.0f && std::isfinite(mass)) return AVBD_ERR_INVALID_ARG;
         float l = std::sqrt((sp[0] * sp[0] + sp[1] * sp[1]) + sp[2] * sp[2]);
@@ -1313,8 +1417,8 @@ int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const flo
         if (!std::isfinite(r) || !(r > 0.0f)) return AVBD_ERR_INVALID_ARG;
         for (float& v : sp) v *= r;
         rest = 0.3f; fric = 0.6f;
-    } else if (shape != AVBD_SHAPE_BOX) {
-        return AVBD_ERR_UNSUPPORTED;
+    } else if (shape != AVBD_SHAPE_BOX && shape != AVBD_SHAPE_CYLINDER && shape != AVBD_SHAPE_CONE) {
+        return AVBD_ERR_UNSUPPORTED;  // hulls: fill the record with the hull's mass properties
     }
     bool free_mass = mass > 0.0f && std::isfinite(mass);
     std::memcpy(out->position, position, 12);

@@ -91,6 +91,15 @@ enum EvState {
 };
 constexpr int TRIG_CAP = 4096;  // trigger overlaps tracked per world
 
+// A convex hull on the device (ConvexHull, collision/shape.rs:317-365):
+// centroid-relative vertices and the reference's triangle faces.
+struct HullDesc {
+    const float4* v;     // nv vertices
+    const uint32_t* f;   // 3 * nf vertex indices
+    uint32_t nv, nf;
+    float bound, min_ext;  // longest vertex (rows.rs:268-272), smallest extent (shape.rs:1468-1479)
+};
+
 // Everything a kernel needs, passed by value (pointers into one world's
 // device allocations).  Scene s owns bodies [scene_off[s], scene_off[s+1]).
 struct DW {
@@ -108,6 +117,8 @@ struct DW {
     const uint32_t* scene_of;   // N
     const uint32_t* plane_off;  // S+1: half-space bodies of each scene
     const uint32_t* plane_list;
+    const HullDesc* hulls;  // convex hulls named by AVBD_SHAPE_HULL bodies (shape_params[0])
+    uint32_t nhulls;
 
     // bodies
     float4 *pos, *rot, *vel, *angvel, *torque;

@@ -27,8 +27,10 @@ from . import abi
 
 F = np.float32
 
-RESTITUTION = {abi.SHAPE_BOX: 0.3, abi.SHAPE_SPHERE: 0.5, abi.SHAPE_CAPSULE: 0.4, abi.SHAPE_HALFSPACE: 0.3}
-FRICTION = {abi.SHAPE_BOX: 0.5, abi.SHAPE_SPHERE: 0.3, abi.SHAPE_CAPSULE: 0.4, abi.SHAPE_HALFSPACE: 0.6}
+RESTITUTION = {abi.SHAPE_BOX: 0.3, abi.SHAPE_SPHERE: 0.5, abi.SHAPE_CAPSULE: 0.4, abi.SHAPE_HALFSPACE: 0.3,
+               abi.SHAPE_CYLINDER: 0.4, abi.SHAPE_CONE: 0.3, abi.SHAPE_HULL: 0.3}
+FRICTION = {abi.SHAPE_BOX: 0.5, abi.SHAPE_SPHERE: 0.3, abi.SHAPE_CAPSULE: 0.4, abi.SHAPE_HALFSPACE: 0.6,
+            abi.SHAPE_CYLINDER: 0.4, abi.SHAPE_CONE: 0.5, abi.SHAPE_HULL: 0.5}
 
 
 def _inertia(shape, p, m):
@@ -54,6 +56,13 @@ def _inertia(shape, p, m):
     out[cap, 0] = ixz
     out[cap, 1] = iy
     out[cap, 2] = ixz
+    for kind, axial, tr2, th2, div in ((abi.SHAPE_CYLINDER, 0.5, 3.0, 4.0, 12.0), (abi.SHAPE_CONE, 0.3, 3.0, 8.0, 20.0)):
+        sel = (shape == kind) & pos
+        r, h, mc = p[sel, 0], p[sel, 1], m[sel]
+        ixz = mc * (F(tr2) * r * r + F(th2) * h * h) / F(div)
+        out[sel, 0] = ixz
+        out[sel, 1] = F(axial) * mc * r * r
+        out[sel, 2] = ixz
     return out
 
 

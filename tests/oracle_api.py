@@ -66,6 +66,10 @@ def lib():
         L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
         L.oracle_set_emit_period.argtypes = [vp, C.c_int32]
         L.oracle_remove_body.argtypes = [vp, C.c_uint32]
+        L.oracle_add_hull.restype = C.c_uint32
+        L.oracle_add_hull.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32, vp]
+        L.oracle_convex_distance.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
+        L.oracle_shape_distance.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
         L.oracle_drain_contact_events.restype = C.c_uint32
         L.oracle_drain_contact_events.argtypes = [vp, vp, C.c_uint32]
         L.oracle_drain_trigger_events.restype = C.c_uint32
@@ -174,6 +178,23 @@ class OracleWorld:
         c = abi.AvbdCounters()
         lib().oracle_get_counters(self.h, C.byref(c))
         return c
+
+    def add_hull(self, verts, faces=(), unit_inertia=(1.0, 1.0, 1.0)):
+        v = f32(np.asarray(verts).reshape(-1))
+        fc = np.ascontiguousarray(np.asarray(faces, dtype=np.uint32).reshape(-1))
+        ui = f32(unit_inertia)
+        return lib().oracle_add_hull(self.h, abi.ptr(v), len(v) // 3, abi.ptr(fc) if len(fc) else None,
+                                     len(fc) // 3, abi.ptr(ui))
+
+    def convex_distance(self, ia, ib):
+        out = np.zeros(10, dtype=np.float32)
+        lib().oracle_convex_distance(self.h, ia, ib, abi.ptr(out))
+        return float(out[0]), out[1:4].copy(), out[4:7].copy(), out[7:10].copy()
+
+    def shape_distance(self, ia, ib):
+        out = np.zeros(10, dtype=np.float32)
+        lib().oracle_shape_distance(self.h, ia, ib, abi.ptr(out))
+        return float(out[0]), out[4:7].copy(), out[7:10].copy()
 
     def remove_body(self, handle):
         lib().oracle_remove_body(self.h, int(handle))

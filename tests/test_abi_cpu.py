@@ -56,6 +56,8 @@ def test_body_init_matches_oracle_constructors():
         (abi.SHAPE_CAPSULE, [0.3, 0.6], [0, 2, 0], 3.1),
         (abi.SHAPE_BOX, [10, 1, 10], [0, -1, 0], 0.0),
         (abi.SHAPE_HALFSPACE, [0, 2, 0], [0, 0, 0], 0.0),
+        (abi.SHAPE_CYLINDER, [0.4, 0.7], [1, 1, 1], 2.0),
+        (abi.SHAPE_CONE, [0.5, 0.3], [2, 1, 0], 1.3),
     ]
     for shape, params, pos, mass in cases:
         a = bodies_array([body(shape, params, pos, mass)])
