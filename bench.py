@@ -156,6 +156,19 @@ def dist_init(n_gpus):
     return dist, rank, dist.get_world_size(), local
 
 
+def workload(args):
+    """(bodies, scene offsets, joints, params, substeps) of the chosen workload."""
+    if args.workload == "ragdoll_8192":
+        # 8192 ragdolls of 15 capsules in two scenes of 3000 and 5192
+        counts = (3000, 5192) if args.scenes == 4096 else (args.scenes // 3, args.scenes - args.scenes // 3)
+        bodies, offs, joints = scenes.ragdolls(counts)
+        params, nsub = scenes.params_for("ragdoll_8192")
+        return bodies, offs, joints, params, nsub
+    bodies, offs, _ = scenes.batched(args.scenes)
+    params, nsub = scenes.params_for("batched_4096")
+    return bodies, offs, [], params, nsub
+
+
 def shard(bodies, offs, rank, world):
     """Scenes s with s % world == rank, repacked with their own offsets."""
     parts, new_offs = [], [0]
@@ -245,11 +258,14 @@ def run_ours(args):
     d = dist_init(args.gpus)
     rank, world = (d[1], d[2]) if d else (0, 1)
     device = d[3] if d else 0
-    bodies_all, offs_all, counts = scenes.batched(args.scenes)
-    params, nsub = scenes.params_for("batched_4096")
+    bodies_all, offs_all, joints_all, params, nsub = workload(args)
+    if world > 1 and joints_all:
+        raise SystemExit("the articulated workload runs on one GPU (two scenes)")
     bodies, offs = shard(bodies_all, offs_all, rank, world) if world > 1 else (bodies_all, offs_all)
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
+    for j in joints_all:
+        w.add_joint(j)
     w.set_precision(not args.exact)
     w.set_events(nsub)  # contact events every step, as the reference's step(dt) reports them
     s0 = w.export_state()  # the initial drop: no contacts yet
@@ -338,17 +354,21 @@ def run_ours(args):
         return 0
     # ---- plain: one scene per world, same trajectory, bounded sample --------
     plain = None
-    if args.plain_scenes > 0:
+    # the one-scene and CPU comparisons belong to the batched workload (the
+    # ragdoll scenes are 45k and 78k bodies: the oracle's all-pairs discovery
+    # does not finish a step in bounded time)
+    if args.plain_scenes > 0 and not joints_all:
         plain = plain_rate(bodies_all, offs_all, params, nsub, args)
     cb = None
-    if args.cpu_per_core > 0 and world == 1:
+    if args.cpu_per_core > 0 and world == 1 and not joints_all:
         cb = cpu_baseline(bodies_all, offs_all, params, nsub, start=args.start, steps=args.steps,
                           per_core=args.cpu_per_core)
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, no dataset)",
-        "config": {"workload": "batched_4096", "scenes": args.scenes, "dynamic_bodies": ndyn_total,
+        "config": {"workload": args.workload, "scenes": len(offs_all) - 1, "dynamic_bodies": ndyn_total,
+                   "joints": len(joints_all),
                    "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations,
                    "trajectory": f"steps {args.start}..{args.start + args.steps} from the initial drop",
                    "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
@@ -403,6 +423,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--workload", default="batched_4096", choices=["batched_4096", "ragdoll_8192"],
+                    help="ragdoll_8192: 8192 15-capsule ragdolls with ball/hinge joints in two scenes")
     ap.add_argument("--start", type=int, default=0, help="untimed steps before the timed region")
     ap.add_argument("--tune-at", type=int, default=150, help="step at which the primal launch is autotuned")
     ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps")

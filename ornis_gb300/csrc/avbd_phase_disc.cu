@@ -449,15 +449,23 @@ __global__ void k_targets(DW w) {
         w.rot[h] = stq(qt);
     }
 }
-// Motion cache for the iterations: x - x0 and quat_diff_vec(q, q0) of every
-// body at the start of the sweep (the primal refreshes a body's entry when it
-// moves it).
+// Contact record of every body for the iterations (pose, x - x0,
+// quat_diff_vec(q, q0), shape word and first parameter in one 64-byte line),
+// taken at the start of the sweep; the primal refreshes a body's record when
+// it moves it.
 __global__ void k_motion_cache(DW w) {
     if (aborted(w)) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
-    w.mdx[h] = st3(ld3(w.pos[h]) - ld3(w.pos0[h]), 0.0f);
-    w.mdr[h] = st3(quat_diff_vec(ldq(w.rot[h]), ldq(w.rot0[h])), 0.0f);
+    V3 p = ld3(w.pos[h]);
+    Q q = ldq(w.rot[h]);
+    V3 dx = p - ld3(w.pos0[h]);
+    V3 dr = quat_diff_vec(q, ldq(w.rot0[h]));
+    float4* k = w.kin + (size_t)h * 4;
+    k[0] = st3(p, w.shp[h].x);
+    k[1] = stq(q);
+    k[2] = st3(dx, __uint_as_float(w.info[h]));
+    k[3] = st3(dr, 0.0f);
 }
 // Eq. 19 warmstart decay (mod.rs:1019-1040), then the point's step-start
 // normal violation C0 (joints_ext.rs:21-32), kept in lambda.w for the
@@ -537,13 +545,85 @@ static __device__ __forceinline__ bool prio_gt(uint32_t la, uint32_t lb) {  // s
     uint32_t ha = colour_hash(la), hb = colour_hash(lb);
     return ha != hb ? ha > hb : la > lb;
 }
-__global__ void __launch_bounds__(1024) k_colour(DW w) {
+// The colour a pending body takes once every higher-priority neighbour has
+// one (the smallest colour none of them uses), or -2 while one is pending.
+static __device__ __forceinline__ int jp_pick(const DW& w, volatile int32_t* col, uint32_t h, uint32_t b0) {
+    bool ready = true;
+    unsigned long long used = 0ull;
+    uint32_t lh = h - b0;
+    auto visit = [&](uint32_t o) {
+        int32_t c = col[o];
+        if (c == -2) {
+            if (prio_gt(o - b0, lh)) ready = false;
+        } else if (c >= 0) {
+            used |= 1ull << c;
+        }
+    };
+    for (uint32_t p = w.offA[h]; p < w.offA[h + 1] && ready; p++)
+        if (w.p_np[p]) visit(w.p_ab[p].y);
+    for (uint32_t k = w.offB[h]; k < w.offB[h + 1] && ready; k++) {
+        uint32_t p = w.listB[k];
+        if (w.p_np[p]) visit(w.p_ab[p].x);
+    }
+    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1] && ready; k++) {
+        uint2 ab = w.j_ab[w.jlist[k]];
+        visit(ab.x == h ? ab.y : ab.x);
+    }
+    if (!ready) return -2;
+    int c = __ffsll((long long)~used) - 1;
+    if (c < 0) {
+        atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_OVERFLOW);
+        c = MAX_COLOURS - 1;
+    }
+    return c;
+}
+// Scenes above the one-CTA limit: Jones-Plassmann rounds over the whole
+// device (a body's colour depends only on its higher-priority neighbours', so
+// the rounds give the same colours as the one-CTA loop); the per-scene CTA
+// pass afterwards finishes any body still pending.
+static __device__ __forceinline__ bool large_scene(const DW& w, uint32_t h, uint32_t small_max, uint32_t& b0) {
+    uint32_t s = w.scene_of[h];
+    b0 = w.scene_off[s];
+    return w.scene_off[s + 1] - b0 > small_max;
+}
+__global__ void k_colour_init_large(DW w, uint32_t small_max) {
+    if (aborted(w)) return;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < (uint32_t)w.N; h += gridDim.x * blockDim.x) {
+        uint32_t b0;
+        if (large_scene(w, h, small_max, b0)) w.colour[h] = solved(w, h) ? -2 : -1;
+    }
+}
+__global__ void k_colour_round(DW w, uint32_t small_max) {
+    if (aborted(w)) return;
+    __shared__ int bmax;
+    if (threadIdx.x == 0) bmax = -1;
+    __syncthreads();
+    volatile int32_t* col = w.colour;
+    int maxc = -1;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < (uint32_t)w.N; h += gridDim.x * blockDim.x) {
+        uint32_t b0;
+        if (col[h] != -2 || !large_scene(w, h, small_max, b0)) continue;
+        int c = jp_pick(w, col, h, b0);
+        if (c >= 0) {
+            col[h] = c;
+            maxc = max(maxc, c);
+        }
+    }
+    if (maxc >= 0) atomicMax(&bmax, maxc);
+    __syncthreads();
+    if (threadIdx.x == 0 && bmax >= 0) {
+        atomicMax(&w.ctr[C_NCOL], (uint32_t)(bmax + 1));
+        if (bmax + 1 > w.max_cols) atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_RANGE);
+    }
+}
+__global__ void __launch_bounds__(1024) k_colour(DW w, uint32_t small_max) {
     if (aborted(w)) return;
     __shared__ int pending;
     uint32_t s = blockIdx.x;
     uint32_t b0 = w.scene_off[s], b1 = w.scene_off[s + 1];
     volatile int32_t* col = w.colour;
-    for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) col[h] = solved(w, h) ? -2 : -1;
+    if (b1 - b0 <= small_max)  // large scenes arrive partly coloured by the device-wide rounds
+        for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) col[h] = solved(w, h) ? -2 : -1;
     __syncthreads();
     int maxc = -1;
     for (uint32_t round = 0; round <= (b1 - b0) + 1; round++) {
@@ -551,35 +631,10 @@ __global__ void __launch_bounds__(1024) k_colour(DW w) {
         __syncthreads();
         for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) {
             if (col[h] != -2) continue;
-            bool ready = true;
-            unsigned long long used = 0ull;
-            uint32_t lh = h - b0;
-            auto visit = [&](uint32_t o) {
-                int32_t c = col[o];
-                if (c == -2) {
-                    if (prio_gt(o - b0, lh)) ready = false;
-                } else if (c >= 0) {
-                    used |= 1ull << c;
-                }
-            };
-            for (uint32_t p = w.offA[h]; p < w.offA[h + 1] && ready; p++)
-                if (w.p_np[p]) visit(w.p_ab[p].y);
-            for (uint32_t k = w.offB[h]; k < w.offB[h + 1] && ready; k++) {
-                uint32_t p = w.listB[k];
-                if (w.p_np[p]) visit(w.p_ab[p].x);
-            }
-            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1] && ready; k++) {
-                uint2 ab = w.j_ab[w.jlist[k]];
-                visit(ab.x == h ? ab.y : ab.x);
-            }
-            if (!ready) {
+            int c = jp_pick(w, col, h, b0);
+            if (c < 0) {
                 pending = 1;
                 continue;
-            }
-            int c = __ffsll((long long)~used) - 1;
-            if (c < 0) {
-                atomicOr(&w.ctr[C_ERR], (uint32_t)E_COLOUR_OVERFLOW);
-                c = MAX_COLOURS - 1;
             }
             col[h] = c;
             maxc = max(maxc, c);
@@ -615,7 +670,12 @@ __global__ void k_colour_starts(DW w, int ntiles) {
     if (c <= MAX_COLOURS) w.col_cnt[c] = w.col_hist[(size_t)c * ntiles];
 }
 void launch_colouring(const DW& w, const Tune& tune, uint32_t* scan_tmp, cudaStream_t st) {
-    k_colour<<<w.S, 1024, 0, st>>>(w);
+    const uint32_t small_max = (uint32_t)tune.small_scene_max;
+    if (w.n_large_scenes) {
+        k_colour_init_large<<<gsz(w.N, 256), 256, 0, st>>>(w, small_max);
+        for (int r = 0; r < COLOUR_ROUNDS; r++) k_colour_round<<<gsz(w.N, 256), 256, 0, st>>>(w, small_max);
+    }
+    k_colour<<<w.S, 1024, 0, st>>>(w, small_max);
     k_colour_keys<<<nblk(w.N, 256), 256, 0, st>>>(w, tune.sort_work);
     int ntiles;
     if (tune.sort_work) {

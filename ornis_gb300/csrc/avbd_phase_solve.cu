@@ -29,18 +29,22 @@ static __device__ __forceinline__ void load_ctx(const DW& w, uint32_t p, PairCtx
     c.gap = n4.w;
     c.mu = w.p_mu[p];
     c.np = w.p_np[p];
-    c.pa = ld3(w.pos[c.a]);
-    c.pb = ld3(w.pos[c.b]);
-    c.qa = ldq(w.rot[c.a]);
-    c.qb = ldq(w.rot[c.b]);
-    c.dxa = ld3(w.mdx[c.a]);
-    c.dxb = ld3(w.mdx[c.b]);
-    c.dra = ld3(w.mdr[c.a]);
-    c.drb = ld3(w.mdr[c.b]);
-    c.sph_a = info_shape(w.info[c.a]) == AVBD_SHAPE_SPHERE;
-    c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
-    c.rad_a = w.shp[c.a].x;
-    c.rad_b = w.shp[c.b].x;
+    const float4* ka = w.kin + (size_t)c.a * 4;
+    const float4* kb = w.kin + (size_t)c.b * 4;
+    float4 a0 = ka[0], a1 = ka[1], a2 = ka[2], a3 = ka[3];
+    float4 b0 = kb[0], b1 = kb[1], b2 = kb[2], b3 = kb[3];
+    c.pa = ld3(a0);
+    c.pb = ld3(b0);
+    c.qa = ldq(a1);
+    c.qb = ldq(b1);
+    c.dxa = ld3(a2);
+    c.dxb = ld3(b2);
+    c.dra = ld3(a3);
+    c.drb = ld3(b3);
+    c.sph_a = info_shape(__float_as_uint(a2.w)) == AVBD_SHAPE_SPHERE;
+    c.sph_b = info_shape(__float_as_uint(b2.w)) == AVBD_SHAPE_SPHERE;
+    c.rad_a = a0.w;
+    c.rad_b = b0.w;
     float4 ma = w.mat[c.a], mb = w.mat[c.b];
     c.mu_roll = fmaxf(ma.z, mb.z);
     c.mu_spin = fmaxf(ma.w, mb.w);
@@ -213,10 +217,15 @@ static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, cons
     if (solve_6x6(s, dx)) {
         V3 p = ld3(w.pos[h]) + V3{dx[0], dx[1], dx[2]};
         Q q = quat_integrate(ldq(w.rot[h]), V3{dx[3], dx[4], dx[5]});
+        V3 dx = p - ld3(w.pos0[h]);
+        V3 dr = quat_diff_vec(q, ldq(w.rot0[h]));
         w.pos[h] = st3(p, 0.0f);
         w.rot[h] = stq(q);
-        w.mdx[h] = st3(p - ld3(w.pos0[h]), 0.0f);
-        w.mdr[h] = st3(quat_diff_vec(q, ldq(w.rot0[h])), 0.0f);
+        float4* k = w.kin + (size_t)h * 4;
+        k[0] = st3(p, w.shp[h].x);
+        k[1] = stq(q);
+        k[2] = st3(dx, __uint_as_float(w.info[h]));
+        k[3] = st3(dr, 0.0f);
     } else {
         atomicAdd(&w.ctr[C_BREAKDOWN], 1u);  // breakdown: the body skips its update
     }

@@ -191,7 +191,7 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
     w.plane_off = plane_off;
     w.plane_list = plane_list;
     float4** f4[] = {&w.pos, &w.rot, &w.vel, &w.angvel, &w.torque, &w.pos0, &w.rot0, &w.inertial, &w.inertial_rot,
-                     &w.prev_pos, &w.prev_rot, &w.inertia, &w.inertia_rest, &w.mdx, &w.mdr, &w.mat, &w.shp,
+                     &w.prev_pos, &w.prev_rot, &w.inertia, &w.inertia_rest, &w.mat, &w.shp,
                      &w.aabb_lo, &w.aabb_hi};
     for (float4** p : f4) *p = cv.take<float4>(N);
     float** f1[] = {&w.inv_mass, &w.inv_mass_rest, &w.mass, &w.friction_t, &w.sleep_timer};
@@ -242,6 +242,7 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
     w.bd_pb = cv.take<float4>(PCAP);
     w.sort_key = cv.take<uint32_t>(1);
     w.sort_idx = cv.take<uint32_t>(1);
+    w.kin = cv.take<float4>((size_t)N * 4);
     w.fbody = cv.take<uint32_t>(N);
     w.fcand = cv.take<uint32_t>(PCAP);
     w.fast = cv.take<uint8_t>(N);

@@ -247,7 +247,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.inertial = m.get<float4>(N); w.inertial_rot = m.get<float4>(N);
     w.prev_pos = m.get<float4>(N); w.prev_rot = m.get<float4>(N);
     w.inertia = m.get<float4>(N); w.inertia_rest = m.get<float4>(N);
-    w.mdx = m.get<float4>(N); w.mdr = m.get<float4>(N);
+    w.kin = m.get<float4>((size_t)N * 4);
     w.mat = m.get<float4>(N); w.shp = m.get<float4>(N);
     w.inv_mass = m.get<float>(N); w.inv_mass_rest = m.get<float>(N); w.mass = m.get<float>(N);
     w.friction_t = m.get<float>(N); w.sleep_timer = m.get<float>(N);
@@ -298,6 +298,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
             max_large = std::max(max_large, n);
         }
     }
+    w.n_large_scenes = (int)W->plan.large.size();
     w.sort_key = m.get<uint32_t>(max_large);
     w.sort_idx = m.get<uint32_t>(max_large);
     W->plan.keys_alt = m.get<uint32_t>(max_large);

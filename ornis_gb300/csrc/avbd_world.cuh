@@ -49,6 +49,7 @@ constexpr float TAU_F = 6.28318530717958647692f;
 constexpr int MAX_PTS = AVBD_MAX_POINTS;
 constexpr int MAX_COLOURS = 64;
 constexpr int CCD_ROUNDS = 8;
+constexpr int COLOUR_ROUNDS = 24;  // device-wide colouring rounds for scenes above the one-CTA limit
 
 // body info word: shape kind in bits 0-3, body type in bits 4-5, trigger bit 6
 __host__ __device__ __forceinline__ uint32_t info_shape(uint32_t i) { return i & 15u; }
@@ -112,6 +113,7 @@ struct DW {
     int enable_sleep, enable_ccd;
     uint32_t cand_cap, pair_cap;
     int max_cols;  // colours the launched iteration covers (a CUDA graph fixes it at capture)
+    int n_large_scenes;  // host: scenes above the one-CTA sweep and colouring limit
 
     const uint32_t* scene_off;  // S+1
     const uint32_t* scene_of;   // N
@@ -124,7 +126,11 @@ struct DW {
     float4 *pos, *rot, *vel, *angvel, *torque;
     float4 *pos0, *rot0, *inertial, *inertial_rot, *prev_pos, *prev_rot;
     float4 *inertia, *inertia_rest;
-    float4 *mdx, *mdr;  // cached x - x0 and quat_diff_vec(q, q0), refreshed whenever a pose changes in a substep
+    // what a contact row reads of a body, packed in one 64-byte record (4 float4
+    // per body), refreshed whenever a pose changes during the iterations of a
+    // substep: (x, first shape parameter), q, (x - x0, info word bits),
+    // (quat_diff_vec(q, q0), 0)
+    float4* kin;
     float4* mat;  // restitution, friction, rolling, torsion
     float4* shp;  // shape params xyz, bound radius w
     float *inv_mass, *inv_mass_rest, *mass, *friction_t, *sleep_timer;

@@ -206,8 +206,97 @@ def params_for(workload):
     """Solver parameters of a workload (gravity -9.81 y, reference constants)."""
     if workload == "batched_4096":
         return abi.default_params(step_dt=1.0 / 120.0, iterations=8), 2
+    if workload == "ragdoll_8192":
+        return abi.default_params(step_dt=1.0 / 120.0, iterations=12), 2
     return abi.default_params(step_dt=1.0 / 60.0, iterations=10), 1
 
 
 def dynamic_count(bodies):
     return int(np.count_nonzero(bodies["body_type"] == abi.BODY_DYNAMIC))
+
+
+# ---- articulated ragdolls ---------------------------------------------------------
+# 15 capsule links; (parent, hinge?) per link; hinges bend about local x with
+# limits, the rest are ball joints.  Links hang along -y from their parent's
+# bottom end, arms and legs offset sideways from the trunk.
+_RAGDOLL = [
+    # name, parent, joint kind, x offset from parent bottom, limit
+    ("pelvis", -1, None, 0.0, None),
+    ("spine", 0, "ball", 0.0, None),
+    ("chest", 1, "ball", 0.0, None),
+    ("head", 2, "ball", 0.0, None),
+    ("l_upper_arm", 2, "ball", -0.35, None),
+    ("l_forearm", 4, "hinge", 0.0, (0.0, 2.5)),
+    ("l_hand", 5, "ball", 0.0, None),
+    ("r_upper_arm", 2, "ball", 0.35, None),
+    ("r_forearm", 7, "hinge", 0.0, (0.0, 2.5)),
+    ("r_hand", 8, "ball", 0.0, None),
+    ("l_thigh", 0, "ball", -0.15, None),
+    ("l_shin", 10, "hinge", 0.0, (-2.5, 0.0)),
+    ("l_foot", 11, "ball", 0.0, None),
+    ("r_thigh", 0, "ball", 0.15, None),
+    ("r_shin", 13, "hinge", 0.0, (-2.5, 0.0)),
+]
+
+
+def _rotate(q, v):
+    """q (xyzw) applied to v, numpy float64."""
+    x, y, z, w = q
+    t = 2.0 * np.cross([x, y, z], v)
+    return v + w * t + np.cross([x, y, z], t)
+
+
+def ragdolls(counts=(3000, 5192), seed=4, density=1000.0):
+    """Scenes of 15-capsule ragdolls dropped onto a ground plane.
+
+    Capsule radii U[0.05, 0.12], lengths U[0.15, 0.45] (half_height =
+    length / 2), mass = density x volume; drop height U[1, 3], random root
+    orientation; ragdolls on a 2.5 m grid.  Returns (bodies, scene_offsets,
+    joints) with joints as AvbdJointDesc records in global handles.
+    """
+    rng = np.random.default_rng(seed)
+    parts, offs, joints = [], [0], []
+    base = 0
+    for count in counts:
+        side = int(math.ceil(math.sqrt(count)))
+        recs = [halfspace([0, 0, 0], [0, 1, 0])]
+        nb = 1
+        for k in range(count):
+            r = rng.uniform(0.05, 0.12, len(_RAGDOLL))
+            hh = rng.uniform(0.15, 0.45, len(_RAGDOLL)) / 2.0
+            q = random_quats(rng, 1)[0].astype(np.float64)
+            drop = rng.uniform(1.0, 3.0)
+            root = np.array([(k % side - side / 2) * 2.5, 0.0, (k // side - side / 2) * 2.5])
+            # upright layout in the ragdoll frame: link i's top end meets its
+            # parent's bottom end (plus the sideways offset)
+            top = np.zeros((len(_RAGDOLL), 3))
+            centre = np.zeros((len(_RAGDOLL), 3))
+            for i, (_, parent, _, dx, _) in enumerate(_RAGDOLL):
+                if parent < 0:
+                    top[i] = [0.0, 0.0, 0.0]
+                else:
+                    pb = centre[parent] - [0.0, hh[parent] + r[parent], 0.0]
+                    top[i] = pb + [dx, 0.0, 0.0]
+                centre[i] = top[i] - [0.0, hh[i] + r[i], 0.0]
+            lowest = (centre[:, 1] - hh - r).min()
+            first = base + nb
+            for i in range(len(_RAGDOLL)):
+                p = root + _rotate(q, centre[i]) + [0.0, drop - lowest, 0.0]
+                vol = math.pi * r[i] ** 2 * (2 * hh[i]) + 4.0 / 3.0 * math.pi * r[i] ** 3
+                b = make_bodies([abi.SHAPE_CAPSULE], [[r[i], hh[i], 0.0]], [p.astype(F)], [density * vol],
+                                q[None, :].astype(F))
+                recs.append(b)
+            for i, (_, parent, kind, dx, lim) in enumerate(_RAGDOLL):
+                if parent < 0:
+                    continue
+                # anchors in each link's frame: the child's top, the parent's bottom (+ offset)
+                la = [dx, -(hh[parent] + r[parent]), 0.0]
+                lb = [0.0, hh[i] + r[i], 0.0]
+                jk = abi.JOINT_REVOLUTE if kind == "hinge" else abi.JOINT_BALL
+                joints.append(abi.joint_desc(jk, first + parent, first + i, la, lb, (1, 0, 0), (1, 0, 0), lim))
+            nb += len(_RAGDOLL)
+        sc = np.concatenate(recs)
+        parts.append(sc)
+        base += len(sc)
+        offs.append(base)
+    return np.concatenate(parts), np.asarray(offs, dtype=np.uint32), joints

@@ -65,7 +65,7 @@ def step_from_oracle_state(o, g, nsub=1):
     return o.export_state(), g.export_state()
 
 
-def compare_states(so, sg, dt, o=None, g=None):
+def compare_states(so, sg, dt, o=None, g=None, rtol=POSE_RTOL):
     """Assert the parity bars; returns (pose_err, vel_err)."""
     ro, io = pair_table(so)
     rg, ig = pair_table(sg)
@@ -76,6 +76,6 @@ def compare_states(so, sg, dt, o=None, g=None):
         co, cg = o.colours(), g.colours()
         assert np.array_equal(co, cg), f"colours differ at {np.nonzero(co != cg)[0][:10]}"
     pe, ve = pose_errors(sg["bodies"], so["bodies"], dt)
-    assert pe <= POSE_RTOL, f"pose error {pe:.3e} > {POSE_RTOL}"
-    assert ve <= POSE_RTOL, f"velocity error (x dt) {ve:.3e} > {POSE_RTOL}"
+    assert pe <= rtol, f"pose error {pe:.3e} > {rtol}"
+    assert ve <= rtol, f"velocity error (x dt) {ve:.3e} > {rtol}"
     return pe, ve
