@@ -405,6 +405,31 @@ int avbd_world_event_counts(AvbdWorld* world, uint32_t* counts);
 int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uint32_t n, int32_t substeps,
                            AvbdBody* out);
 
+/* ---- differentiable rollouts (no counterpart in the reference: its AVBD
+ * engine has no adjoint; the interface shape follows the forward/backward
+ * pair the Rust side wraps as one Function-style type) ------------------- */
+
+/* Advance the world `steps` steps of `substeps` fixed substeps (as
+ * avbd_world_step_graph) and keep a device checkpoint of the full step
+ * state every `checkpoint_every` steps, for avbd_adjoint_backward.  Worlds
+ * with joints or with rolling / torsion friction return
+ * AVBD_ERR_UNSUPPORTED.  A new forward replaces the previous recording. */
+int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int32_t checkpoint_every);
+
+/* Reverse-mode gradient of a scalar loss of the recorded rollout's final
+ * state.  grad_final: dLoss/d(final state), 13 floats per body (position 3,
+ * orientation x y z w, velocity 3, angular velocity 3).  Writes
+ * grad_initial (the same layout, dLoss/d(initial state)) and, when not
+ * null, grad_friction: one float per scene, dLoss/d(mu) for a friction
+ * coefficient mu that every body of the scene shares (pair friction is the
+ * larger of the two bodies', so it moves with mu).  The contact set, the
+ * contact frames (normal, friction basis, local anchors) and the colouring
+ * are held at the values of the recorded rollout; the step-start gap stays a
+ * function of the step-start poses.  Each segment between checkpoints is
+ * recomputed from its checkpoint.  The world is left at the end of the
+ * recorded rollout. */
+int avbd_adjoint_backward(AvbdWorld* world, const float* grad_final, float* grad_initial, float* grad_friction);
+
 #ifdef __cplusplus
 }
 #endif

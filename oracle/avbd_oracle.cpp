@@ -18,7 +18,8 @@
 //               in hash-priority order (identical to the Jones-Plassmann
 //               colouring the GPU computes).  Within a colour bodies are
 //               independent, so the order inside a colour is immaterial.
-// Scalar T = float (bit-level parity) or double (the f64 error column).
+// Scalar T = float (bit-level parity), double (the f64 error column) or Dual
+// (f64 forward-mode derivatives for the adjoint checks, avbd_dual.hpp).
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -32,6 +33,7 @@
 #include <vector>
 
 #include "../include/ornis_avbd.h"
+#include "avbd_dual.hpp"  // before the templates that call std:: math on T
 #include "avbd_math.hpp"
 
 namespace orc {
@@ -765,6 +767,12 @@ template <class T> struct Engine {
     int mode = REFERENCE;
     int threads = 1;
     bool faithful_scan = false;  // true: solve_body scans every pair/joint (the reference's O(P) scan)
+    // Dual numbers only: hold each step's contact frames (normal, gap, local
+    // anchors) fixed in the derivative, the device adjoint's convention; the
+    // step-start gap keeps the derivative of n.(witness_a - witness_b) with
+    // the witnesses carried by the bodies.
+    bool freeze_frames = false;
+    int freeze_bits = 7;
     V3<T> gravity;
     T dt;
     std::vector<Body<T>> bodies;
@@ -1155,6 +1163,22 @@ template <class T> struct Engine {
             pairs = std::move(next);
         }
         for (auto& w : wake) { wake_body(w.first); wake_body(w.second); }
+        if (freeze_frames)
+            for (auto& p : pairs) {
+                if (freeze_bits & 1) p.n = {no_tangent(p.n.x), no_tangent(p.n.y), no_tangent(p.n.z)};
+                p.gap = no_tangent(p.gap);
+                if (freeze_bits & 8)
+                    for (auto& pt : p.points)
+                        for (int k = 0; k < 3; k++) { pt.lam[k] = no_tangent(pt.lam[k]); pt.pen[k] = no_tangent(pt.pen[k]); }
+                if (freeze_bits & 16)
+                    for (auto& pt : p.points)
+                        for (int k = 0; k < 3; k++) pt.pen[k] = no_tangent(pt.pen[k]);
+                if (freeze_bits & 4)
+                for (auto& pt : p.points) {
+                    pt.ra = {no_tangent(pt.ra.x), no_tangent(pt.ra.y), no_tangent(pt.ra.z)};
+                    pt.rb = {no_tangent(pt.rb.x), no_tangent(pt.rb.y), no_tangent(pt.rb.z)};
+                }
+            }
     }
 
     // ---- contact rows (rows.rs:947-1060, joints_ext.rs:21-32) ----
@@ -1167,7 +1191,14 @@ template <class T> struct Engine {
     T gap_c0(const Pair<T>& p, const Point<T>& pt) const {
         const Body<T>& a = bodies[p.a];
         const Body<T>& b = bodies[p.b];
-        if (a.shape == AVBD_SHAPE_SPHERE || b.shape == AVBD_SHAPE_SPHERE) return p.gap + C<T>(K::MARGIN);
+        if (a.shape == AVBD_SHAPE_SPHERE || b.shape == AVBD_SHAPE_SPHERE) {
+            if (!freeze_frames) return p.gap + C<T>(K::MARGIN);
+            // value from the narrowphase gap, derivative from the witnesses
+            // (a sphere's witness is its centre minus radius along the normal)
+            V3<T> wa = a.shape == AVBD_SHAPE_SPHERE ? pos0[p.a] - p.n * a.sp.x : pos0[p.a] + qrot(rot0[p.a], pt.ra);
+            V3<T> wb = b.shape == AVBD_SHAPE_SPHERE ? pos0[p.b] + p.n * b.sp.x : pos0[p.b] + qrot(rot0[p.b], pt.rb);
+            return value_with_tangent(p.gap + C<T>(K::MARGIN), dot(p.n, wa - wb));
+        }
         V3<T> pa = pos0[p.a] + qrot(rot0[p.a], pt.ra);
         V3<T> pb = pos0[p.b] + qrot(rot0[p.b], pt.rb);
         return dot(p.n, pa - pb) + C<T>(K::MARGIN);
@@ -1933,22 +1964,25 @@ template <class T> struct Oracle : OracleBase {
 using namespace orc;
 
 struct OracleWorld {
-    int dbl;
+    int dbl;  // 0 f32, 1 f64, 2 f64 dual numbers
     Engine<float>* f;
     Engine<double>* d;
+    Engine<Dual>* g;
 };
 
-#define DISPATCH(w, ...)                                 \
-    do {                                                 \
-        if ((w)->dbl) { auto& E = *(w)->d; __VA_ARGS__; } \
-        else { auto& E = *(w)->f; __VA_ARGS__; }          \
+#define DISPATCH(w, ...)                                      \
+    do {                                                      \
+        if ((w)->dbl == 2) { auto& E = *(w)->g; __VA_ARGS__; } \
+        else if ((w)->dbl) { auto& E = *(w)->d; __VA_ARGS__; } \
+        else { auto& E = *(w)->f; __VA_ARGS__; }               \
     } while (0)
 
 extern "C" {
 
-// mode: 0 = Reference, 1 = Coloured.  use_double: 0 = f32, 1 = f64.
+// mode: 0 = Reference, 1 = Coloured.  use_double: 0 = f32, 1 = f64, 2 = f64
+// dual numbers (forward-mode derivatives).
 OracleWorld* oracle_world_create(const AvbdParams* p, int mode, int use_double, int threads) {
-    OracleWorld* w = new OracleWorld{use_double, nullptr, nullptr};
+    OracleWorld* w = new OracleWorld{use_double, nullptr, nullptr, nullptr};
     auto init = [&](auto& E) {
         using TT = std::remove_reference_t<decltype(E.dt)>;
         E.prm = *p;
@@ -1957,7 +1991,8 @@ OracleWorld* oracle_world_create(const AvbdParams* p, int mode, int use_double, 
         E.gravity = {TT(p->gravity[0]), TT(p->gravity[1]), TT(p->gravity[2])};
         E.dt = TT(p->step_dt);
     };
-    if (use_double) { w->d = new Engine<double>(); init(*w->d); }
+    if (use_double == 2) { w->g = new Engine<Dual>(); init(*w->g); }
+    else if (use_double) { w->d = new Engine<double>(); init(*w->d); }
     else { w->f = new Engine<float>(); init(*w->f); }
     return w;
 }
@@ -1965,6 +2000,7 @@ void oracle_world_destroy(OracleWorld* w) {
     if (!w) return;
     delete w->f;
     delete w->d;
+    delete w->g;
     delete w;
 }
 void oracle_set_faithful_scan(OracleWorld* w, int on) { DISPATCH(w, E.faithful_scan = on != 0); }
@@ -2074,6 +2110,47 @@ int oracle_get_state13(OracleWorld* w, double* out) {
                         double(b.angvel.x), double(b.angvel.y), double(b.angvel.z)};
         std::memcpy(out + 13 * i, v, sizeof(v));
     });
+    return AVBD_OK;
+}
+// ---- dual-number worlds (use_double = 2): forward-mode derivatives ----------
+int oracle_dual_dirs() { return DUAL_DIRS; }
+// Seed d(field[comp] of body)/d(direction dir) = value.  field: 0 position,
+// 1 rotation (x, y, z, w), 2 velocity, 3 angular velocity, 4 friction (both
+// friction coefficients; comp ignored).
+int oracle_dual_seed(OracleWorld* w, uint32_t body, int field, int comp, int dir, double value) {
+    if (!w || w->dbl != 2 || dir < 0 || dir >= DUAL_DIRS || body >= w->g->bodies.size()) return AVBD_ERR_INVALID_ARG;
+    auto& b = w->g->bodies[body];
+    Dual* f = nullptr;
+    switch (field) {
+        case 0: f = comp == 0 ? &b.pos.x : comp == 1 ? &b.pos.y : &b.pos.z; break;
+        case 1: f = comp == 0 ? &b.rot.x : comp == 1 ? &b.rot.y : comp == 2 ? &b.rot.z : &b.rot.w; break;
+        case 2: f = comp == 0 ? &b.vel.x : comp == 1 ? &b.vel.y : &b.vel.z; break;
+        case 3: f = comp == 0 ? &b.angvel.x : comp == 1 ? &b.angvel.y : &b.angvel.z; break;
+        case 4:
+            b.friction.d[dir] = value;
+            b.friction_t.d[dir] = value;
+            return AVBD_OK;
+        default: return AVBD_ERR_INVALID_ARG;
+    }
+    f->d[dir] = value;
+    return AVBD_OK;
+}
+int oracle_dual_freeze_frames(OracleWorld* w, int on) {
+    if (!w || w->dbl != 2) return AVBD_ERR_INVALID_ARG;
+    w->g->freeze_frames = on != 0;
+    w->g->freeze_bits = on;
+    return AVBD_OK;
+}
+// Tangents of the 13 state numbers of every body: out[(13 * body + k) * DUAL_DIRS + dir].
+int oracle_dual_tangents(OracleWorld* w, double* out) {
+    if (!w || w->dbl != 2) return AVBD_ERR_INVALID_ARG;
+    for (size_t i = 0; i < w->g->bodies.size(); i++) {
+        auto& b = w->g->bodies[i];
+        const Dual* v[13] = {&b.pos.x, &b.pos.y, &b.pos.z, &b.rot.x, &b.rot.y, &b.rot.z, &b.rot.w,
+                             &b.vel.x, &b.vel.y, &b.vel.z, &b.angvel.x, &b.angvel.y, &b.angvel.z};
+        for (int k = 0; k < 13; k++)
+            for (int d = 0; d < DUAL_DIRS; d++) out[(13 * i + k) * DUAL_DIRS + d] = v[k]->d[d];
+    }
     return AVBD_OK;
 }
 int oracle_set_bodies(OracleWorld* w, const AvbdBody* in, uint32_t n) {

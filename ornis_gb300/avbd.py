@@ -75,6 +75,8 @@ def lib():
             "avbd_world_drain_contact_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_drain_trigger_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_event_counts": [vp, vp],
+            "avbd_adjoint_forward": [vp, C.c_int32, C.c_int32, C.c_int32],
+            "avbd_adjoint_backward": [vp, vp, vp, vp],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -307,3 +309,41 @@ class AvbdWorld:
         _check(lib().avbd_world_import_state(self.h, abi.ptr(st["bodies"]), abi.ptr(st["aux"]),
                                              abi.ptr(st["pairs"]), abi.ptr(st["points"]), len(st["pairs"]),
                                              abi.ptr(st.get("joints"))), "import_state")
+
+    # ---- differentiable rollouts ----
+    def adjoint_forward(self, steps, substeps=1, checkpoint_every=10):
+        """Advance `steps` steps, recording checkpoints for adjoint_backward."""
+        _check(lib().avbd_adjoint_forward(self.h, int(steps), int(substeps), int(checkpoint_every)),
+               "adjoint_forward")
+
+    def adjoint_backward(self, grad_final):
+        """dLoss/d(initial state) (bodies x 13) and dLoss/d(scene friction)
+        (scenes) from dLoss/d(final state) (bodies x 13: position, quaternion
+        x y z w, velocity, angular velocity)."""
+        g = np.ascontiguousarray(grad_final, dtype=np.float32).reshape(-1, 13)
+        n = self.body_count
+        if g.shape[0] != n:
+            raise ValueError("grad_final must have one row of 13 per body")
+        out = np.zeros((n, 13), dtype=np.float32)
+        ns = C.c_uint32()
+        _check(lib().avbd_world_scene_count(self.h, C.byref(ns)), "scene_count")
+        mu = np.zeros(ns.value, dtype=np.float32)
+        _check(lib().avbd_adjoint_backward(self.h, abi.ptr(g), abi.ptr(out), abi.ptr(mu)), "adjoint_backward")
+        return out, mu
+
+
+class Rollout:
+    """A differentiable rollout as a forward/backward pair over one world:
+    forward() advances and records, backward(dloss_dfinal) returns the
+    gradients of the initial state and of each scene's friction."""
+
+    def __init__(self, world, steps, substeps=1, checkpoint_every=10):
+        self.world = world
+        self.steps, self.substeps, self.every = steps, substeps, checkpoint_every
+
+    def forward(self):
+        self.world.adjoint_forward(self.steps, self.substeps, self.every)
+        return self.world.bodies()
+
+    def backward(self, grad_final):
+        return self.world.adjoint_backward(grad_final)

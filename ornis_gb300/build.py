@@ -29,6 +29,7 @@ SOURCES = [
     ("avbd_events.cu", "avbd_events.o", []),
     ("avbd_world.cu", "avbd_world.o", []),
     ("avbd_static.cu", "avbd_static.o", []),
+    ("avbd_adjoint.cu", "avbd_adjoint.o", []),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--extended-lambda", "-Xcompiler", "-fPIC",

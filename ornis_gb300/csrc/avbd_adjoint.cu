@@ -1,0 +1,599 @@
+// avbd_adjoint.cu — reverse-mode (adjoint) kernels of one AVBD substep.
+//
+// The forward substep (crates/physics/src/avbd/mod.rs:980-1078: targets and
+// warmstart decay, the primal/dual iterations of avbd/assembly.rs and
+// avbd/joints_ext.rs, BDF1) is reversed with the contact set, the contact
+// frames (normal, friction basis, local anchors) and the colouring held at
+// the values the forward computed.  The step-start gap C0 stays a function
+// of the step-start poses (joints_ext.rs:21-32, with the witnesses carried
+// by the bodies for sphere pairs), the warm lambda / penalty state flows
+// across substeps through the point inheritance of the discovery merge, and
+// every clamp, cone and liveness test keeps the branch the forward took.
+//
+// Order of one substep's reverse:
+//   k_adj_bdf          BDF1 velocities and the quaternion renormalisation
+//   per iteration, last first:
+//     k_adj_dual       the dual update of every point (pair order)
+//     k_adj_body       per colour, last first: one body's block solve
+//   k_adj_c0           C0 and the warmstart decay
+//   k_adj_start        the inertial targets -> previous substep's state
+//   k_adj_inherit      point adjoints -> the previous generation's points
+//   k_adj_mu_scene     friction adjoint summed per scene
+// A body's update x1 = x + d, q1 = integrate(q, d_ang), d = -H^-1 r, has the
+// adjoint  s_bar = -(d(r + H d)/ds)^T H^-1 d_bar  for every input s; each
+// stamped row contributes through its force, penalty and lever.
+#include "avbd_common.cuh"
+#include "avbd_adjoint.cuh"
+
+namespace avbd {
+
+static __device__ __forceinline__ size_t pslice(const DW& w, int s) { return (size_t)s * (size_t)w.N; }
+
+// Pose slice in which body o is seen by a body of colour c during iteration
+// it: bodies of lower colours have already moved in this iteration.
+static __device__ __forceinline__ int seen_slice(const AdjFrame& f, uint32_t o, int c, int it) {
+    int co = f.colour[o];
+    return (co >= 0 && co < c) ? it + 1 : it;
+}
+
+static __device__ __forceinline__ void adj_ctx(const DW& w, const AdjFrame& f, uint32_t p, int sa, int sb, PairCtx& c,
+                                               Q& qa0, Q& qb0) {
+    uint2 ab = f.p_ab[p];
+    float4 n4 = f.p_n[p];
+    c.a = ab.x;
+    c.b = ab.y;
+    c.n = ld3(n4);
+    c.gap = n4.w;
+    c.mu = f.p_mu[p];
+    c.np = f.p_np[p];
+    c.pa = ld3(f.it_pos[pslice(w, sa) + c.a]);
+    c.qa = ldq(f.it_rot[pslice(w, sa) + c.a]);
+    c.pb = ld3(f.it_pos[pslice(w, sb) + c.b]);
+    c.qb = ldq(f.it_rot[pslice(w, sb) + c.b]);
+    qa0 = ldq(f.rot0[c.a]);
+    qb0 = ldq(f.rot0[c.b]);
+    c.dxa = c.pa - ld3(f.pos0[c.a]);
+    c.dxb = c.pb - ld3(f.pos0[c.b]);
+    c.dra = quat_diff_vec(c.qa, qa0);
+    c.drb = quat_diff_vec(c.qb, qb0);
+    c.sph_a = info_shape(w.info[c.a]) == AVBD_SHAPE_SPHERE;
+    c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
+    c.rad_a = w.shp[c.a].x;
+    c.rad_b = w.shp[c.b].x;
+    c.mu_roll = 0.0f;
+    c.mu_spin = 0.0f;
+    c.t1 = tangent_t1(c.n);
+    c.t2 = cross(c.t1, c.n);
+}
+
+// Separated-point damper gate and stiffness (assembly.rs:113-175); false when
+// the point stamps nothing.
+static __device__ __forceinline__ bool damper(const DW& w, const AdjFrame& f, const PairCtx& c, float cn, float& pen_d) {
+    float approach = fmaxf(dot(ld3(f.vel[c.b]) - ld3(f.vel[c.a]), c.n), 0.0f);
+    if (c.gap - approach * w.dt > 0.0f) return false;
+    if (fabsf(cn) < C_EPS) return false;
+    float npts = (float)max(c.np, 1u);
+    float ka = is_dynamic(w, c.a) ? f.inv_mass[c.a] : 0.0f;
+    float kb = is_dynamic(w, c.b) ? f.inv_mass[c.b] : 0.0f;
+    float m_red = ka + kb > NEAR_ZERO ? 1.0f / (ka + kb) : 0.0f;
+    if (!(m_red > 0.0f)) return false;
+    pen_d = fminf(2.0f * m_red / (w.dt * w.dt) / npts, PENALTY_MAX);
+    return true;
+}
+
+// The rows of one point for the body on side is_a (the forward stamp_point
+// without rolling friction).
+static __device__ __forceinline__ void adj_stamp_point(const DW& w, const AdjFrame& f, const PairCtx& c, uint32_t q,
+                                                       bool is_a, float4 lam, float4 pen, Sys& s) {
+    float4 ra = f.q_ra[q], rb = f.q_rb[q];
+    float sign = is_a ? 1.0f : -1.0f;
+    bool touching = c.gap <= 0.0f;
+    float c0 = touching ? lam.w : 0.0f;
+    V3 rup, rlo;
+    contact_levers(c, ra, rb, rup, rlo);
+    float cn = row_c_levers(c, c.n, c0, rup, rlo);
+    V3 r_side = is_a ? rup : rlo;
+    if (!touching) {
+        float pen_d;
+        if (damper(w, f, c, cn, pen_d)) stamp_row(s, c.n, pen_d, fminf(pen_d * cn, 0.0f), r_side, sign);
+        return;
+    }
+    V3 raf, rbf;
+    friction_levers(c, rup, rlo, raf, rbf);
+    V3 r_side_f = is_a ? raf : rbf;
+    float ct1 = row_c_levers(c, c.t1, 0.0f, raf, rbf);
+    float ct2 = row_c_levers(c, c.t2, 0.0f, raf, rbf);
+    float fo[3];
+    contact_force(cn, pen, lam, ct1, ct2, c.mu, fo);
+    if (row_live(cn, fo[0])) stamp_row(s, c.n, pen.x, fo[0], r_side, sign);
+    if (row_live(ct1, fo[1])) stamp_row(s, c.t1, pen.y, fo[1], r_side_f, sign);
+    if (row_live(ct2, fo[2])) stamp_row(s, c.t2, pen.z, fo[2], r_side_f, sign);
+}
+
+// One stamped row J = [s a; r x (s a)] with H += pen J J^T, rhs += f J: the
+// seeds of s_bar = -d/ds [w.(rhs + H d)] for its force, penalty and lever.
+static __device__ __forceinline__ void row_bwd(V3 axis, float pen, float fo, V3 r, float sign, const float w6[6],
+                                               const float d6[6], float& gf, float& gpen, V3& gr) {
+    V3 nn = sign * axis;
+    V3 t = cross(r, nn);
+    V3 wl{w6[0], w6[1], w6[2]}, wa{w6[3], w6[4], w6[5]};
+    V3 dl{d6[0], d6[1], d6[2]}, da{d6[3], d6[4], d6[5]};
+    float a = dot(nn, wl) + dot(t, wa);
+    float dd = dot(nn, dl) + dot(t, da);
+    gf -= a;
+    gpen -= a * dd;
+    V3 gja = -(wa * fo + (wa * dd + da * a) * pen);
+    gr = gr + cross(nn, gja);
+}
+
+// friction_levers (rows.rs:987-996): sep = n.((pa + raw) - (pb + rbw)),
+// raf = raw - n sep/2, rbf = rbw + n sep/2.
+static __device__ __forceinline__ void friction_levers_bwd(const PairCtx& c, V3 graf, V3 grbf, V3& graw, V3& grbw,
+                                                           PairGrad& pg) {
+    float gsep = HALF * dot(c.n, grbf - graf);
+    graw = graw + graf + c.n * gsep;
+    grbw = grbw + grbf - c.n * gsep;
+    pg.xa = pg.xa + c.n * gsep;
+    pg.xb = pg.xb - c.n * gsep;
+}
+// contact_levers (rows.rs:963-973): a non-sphere lever is the anchor rotated
+// by the body; a sphere's is fixed by the (frozen) normal.
+static __device__ __forceinline__ void contact_levers_bwd(const PairCtx& c, float4 ra, float4 rb, V3 graw, V3 grbw,
+                                                          PairGrad& pg) {
+    V3 dummy = V0();
+    if (!c.sph_a) qrot_bwd(c.qa, ld3(ra), graw, pg.qa, dummy);
+    if (!c.sph_b) qrot_bwd(c.qb, ld3(rb), grbw, pg.qb, dummy);
+}
+
+// Adjoint of one point's rows in a block solve of the body on side is_a.
+static __device__ __forceinline__ void adj_point_bwd(const DW& w, const AdjFrame& f, const PairCtx& c, Q qa0, Q qb0,
+                                                     uint32_t q, bool is_a, float4 lam, float4 pen, const float w6[6],
+                                                     const float d6[6], PairGrad& pg, float4& glam, float4& gpen,
+                                                     float2& gmu) {
+    float4 ra = f.q_ra[q], rb = f.q_rb[q];
+    float sign = is_a ? 1.0f : -1.0f;
+    bool touching = c.gap <= 0.0f;
+    float c0 = touching ? lam.w : 0.0f;
+    V3 rup, rlo;
+    contact_levers(c, ra, rb, rup, rlo);
+    float cn = row_c_levers(c, c.n, c0, rup, rlo);
+    V3 graw = V0(), grbw = V0();
+    float gcn = 0.0f, gc0 = 0.0f;
+    if (!touching) {
+        float pen_d;
+        if (!damper(w, f, c, cn, pen_d)) return;
+        float fd = fminf(pen_d * cn, 0.0f);
+        float gf = 0.0f, gp = 0.0f;
+        V3 gr = V0();
+        row_bwd(c.n, pen_d, fd, is_a ? rup : rlo, sign, w6, d6, gf, gp, gr);
+        if (pen_d * cn < 0.0f) gcn += pen_d * gf;
+        if (is_a) graw = graw + gr;
+        else grbw = grbw + gr;
+    } else {
+        V3 raf, rbf;
+        friction_levers(c, rup, rlo, raf, rbf);
+        float ct1 = row_c_levers(c, c.t1, 0.0f, raf, rbf);
+        float ct2 = row_c_levers(c, c.t2, 0.0f, raf, rbf);
+        float fo[3];
+        contact_force(cn, pen, lam, ct1, ct2, c.mu, fo);
+        float gf[3] = {0.0f, 0.0f, 0.0f};
+        V3 gr = V0(), grf = V0();
+        if (row_live(cn, fo[0])) row_bwd(c.n, pen.x, fo[0], is_a ? rup : rlo, sign, w6, d6, gf[0], gpen.x, gr);
+        if (row_live(ct1, fo[1])) row_bwd(c.t1, pen.y, fo[1], is_a ? raf : rbf, sign, w6, d6, gf[1], gpen.y, grf);
+        if (row_live(ct2, fo[2])) row_bwd(c.t2, pen.z, fo[2], is_a ? raf : rbf, sign, w6, d6, gf[2], gpen.z, grf);
+        float gct1 = 0.0f, gct2 = 0.0f;
+        contact_force_bwd(cn, pen, lam, ct1, ct2, c.mu, gf, gcn, gpen, glam, gct1, gct2, gmu);
+        V3 graf = is_a ? grf : V0(), grbf = is_a ? V0() : grf;
+        float unused = 0.0f;
+        row_c_bwd(c, qa0, qb0, c.t1, raf, rbf, gct1, unused, graf, grbf, pg);
+        row_c_bwd(c, qa0, qb0, c.t2, raf, rbf, gct2, unused, graf, grbf, pg);
+        friction_levers_bwd(c, graf, grbf, graw, grbw, pg);
+        if (is_a) graw = graw + gr;
+        else grbw = grbw + gr;
+    }
+    row_c_bwd(c, qa0, qb0, c.n, rup, rlo, gcn, gc0, graw, grbw, pg);
+    contact_levers_bwd(c, ra, rb, graw, grbw, pg);
+    glam.w += gc0;
+}
+
+// inertial block (assembly.rs:74-96) with the frame's masses and targets
+static __device__ __forceinline__ void adj_inertial(const DW& w, const AdjFrame& f, uint32_t h, V3 x, Q q, Sys& s) {
+    float dt2 = w.dt * w.dt;
+    float im = is_dynamic(w, h) ? f.inv_mass[h] : 0.0f;
+    float m_dt2 = 1.0f / im / dt2;
+    float iw[3][3];
+    world_inertia(ld3(f.inertia[h]), q, iw);
+    for (int i = 0; i < 21; i++) s.h[i] = 0.0f;
+    s.h[tri(0, 0)] = m_dt2;
+    s.h[tri(1, 1)] = m_dt2;
+    s.h[tri(2, 2)] = m_dt2;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b <= a; b++) s.h[tri(3 + a, 3 + b)] = iw[a][b] / dt2;
+    V3 rl = m_dt2 * (x - ld3(f.inertial[h]));
+    s.r[0] = rl.x;
+    s.r[1] = rl.y;
+    s.r[2] = rl.z;
+    V3 ra = mat3_vec(iw, quat_diff_vec(q, ldq(f.inertial_rot[h]))) / dt2;
+    s.r[3] = ra.x;
+    s.r[4] = ra.y;
+    s.r[5] = ra.z;
+}
+
+static __device__ __forceinline__ float4* slot_of(const AdjFrame& f, const AdjState& A, uint32_t p, bool side_a,
+                                                  uint2 ab) {
+    uint32_t k = side_a ? p + f.offB[ab.x + 1] : f.offA[ab.y] + f.posB[p];
+    return A.slot + (size_t)k * 4;
+}
+static __device__ __forceinline__ void slot_add(float4* s, V3 x, Q q, V3 x0, Q q0) {
+    float4 a = s[0], b = s[1], c = s[2], d = s[3];
+    s[0] = make_float4(a.x + x.x, a.y + x.y, a.z + x.z, 0.0f);
+    s[1] = make_float4(b.x + q.x, b.y + q.y, b.z + q.z, b.w + q.w);
+    s[2] = make_float4(c.x + x0.x, c.y + x0.y, c.z + x0.z, 0.0f);
+    s[3] = make_float4(d.x + q0.x, d.y + q0.y, d.z + q0.z, d.w + q0.w);
+}
+static __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// ---- BDF1 (mod.rs:1060-1078) --------------------------------------------------
+__global__ void k_adj_bdf(DW w, AdjFrame f, AdjState A, int iters) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    A.ay[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    A.aqt[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (f.colour[h] < 0) {  // not swept: its pose and velocities pass through the substep
+        A.ax0[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.aq0[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+    }
+    float dt = w.dt;
+    V3 xk = ld3(f.it_pos[pslice(w, iters) + h]);
+    Q qk = ldq(f.it_rot[pslice(w, iters) + h]);
+    Q q0 = ldq(f.rot0[h]);
+    (void)xk;
+    V3 gv = ld3(A.av[h]), gw = ld3(A.aw[h]);
+    if (f.asleep_end[h]) gv = gw = V0();  // frozen at the end of the substep: velocities zeroed
+    V3 gx = ld3(A.ax[h]) + gv / dt;
+    V3 gx0 = -(gv / dt);
+    Q gq = qnormalize_bwd(qk, ldq(A.aq[h]));
+    Q gq0 = Q0();
+    V3 spin = quat_diff_vec(qk, q0);
+    if (len(spin) >= SPIN_REST_EPS) quat_diff_vec_bwd(qk, q0, gw / dt, gq, gq0);
+    A.ax[h] = st3(gx, 0.0f);
+    A.aq[h] = stq(gq);
+    A.ax0[h] = st3(gx0, 0.0f);
+    A.aq0[h] = stq(gq0);
+    A.av[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    A.aw[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// ---- dual update (joints_ext.rs:464-573), one thread per pair ------------------
+__global__ void k_adj_dual(DW w, AdjFrame f, AdjState A, int it) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npairs; p += gridDim.x * blockDim.x) {
+        uint32_t np = f.p_np[p];
+        if (np == 0) continue;
+        PairCtx c;
+        Q qa0, qb0;
+        adj_ctx(w, f, p, it + 1, it + 1, c, qa0, qb0);
+        if (c.gap > 0.0f) continue;  // separated points keep lambda and penalty
+        PairGrad pg;
+        pair_grad_zero(pg);
+        float2 gmu = make_float2(0.0f, 0.0f);
+        for (uint32_t k = 0; k < np; k++) {
+            uint32_t q = p * MAX_PTS + k;
+            size_t qi = (size_t)it * f.qstride + q;
+            float4 lam = f.it_lam[qi], pen = f.it_pen[qi];
+            float4 gl = A.alam[q], gp = A.apen[q];
+            float4 ra = f.q_ra[q], rb = f.q_rb[q];
+            float c0 = lam.w;
+            V3 raw, rbw;
+            contact_levers(c, ra, rb, raw, rbw);
+            float cn = row_c_levers(c, c.n, c0, raw, rbw);
+            V3 raf, rbf;
+            friction_levers(c, raw, rbw, raf, rbf);
+            float ct1 = row_c_levers(c, c.t1, 0.0f, raf, rbf);
+            float ct2 = row_c_levers(c, c.t2, 0.0f, raf, rbf);
+            float fo[3];
+            contact_force(cn, pen, lam, ct1, ct2, c.mu, fo);
+            float fu0 = pen.y * ct1 + lam.y, fu1 = pen.z * ct2 + lam.z;
+            float b1 = fabsf(fo[0]) * c.mu.x, b2 = fabsf(fo[0]) * c.mu.y;
+            float s_ell = (b1 > 0.0f && b2 > 0.0f) ? (fu0 / b1) * (fu0 / b1) + (fu1 / b2) * (fu1 / b2) : INFINITY;
+            float4 glo = make_float4(0.0f, 0.0f, 0.0f, gl.w), gpo = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float gf[3] = {0.0f, 0.0f, 0.0f};
+            float gcn = 0.0f, gct1 = 0.0f, gct2 = 0.0f;
+            if (fabsf(cn) >= C_EPS) {
+                gf[0] += gl.x;
+                if (fo[0] < 0.0f) {
+                    if (pen.x + BETA * fabsf(cn) < PENALTY_MAX) {
+                        gpo.x += gp.x;
+                        gcn += BETA * copysignf(1.0f, cn) * gp.x;
+                    }
+                } else {
+                    gpo.x += gp.x;
+                }
+            } else {
+                glo.x += gl.x;
+                gpo.x += gp.x;
+            }
+            gf[1] += gl.y;
+            gf[2] += gl.z;
+            float cts[2] = {ct1, ct2}, pts[2] = {pen.y, pen.z}, gps[2] = {gp.y, gp.z};
+            float gpt[2] = {0.0f, 0.0f}, gct[2] = {0.0f, 0.0f};
+            for (int k2 = 0; k2 < 2; k2++) {
+                if (s_ell <= 1.0f && fabsf(cts[k2]) >= C_EPS) {
+                    if (pts[k2] + BETA * fabsf(cts[k2]) < PENALTY_MAX) {
+                        gpt[k2] += gps[k2];
+                        gct[k2] += BETA * copysignf(1.0f, cts[k2]) * gps[k2];
+                    }
+                } else {
+                    gpt[k2] += gps[k2];
+                }
+            }
+            gpo.y += gpt[0];
+            gpo.z += gpt[1];
+            gct1 += gct[0];
+            gct2 += gct[1];
+            contact_force_bwd(cn, pen, lam, ct1, ct2, c.mu, gf, gcn, gpo, glo, gct1, gct2, gmu);
+            V3 graw = V0(), grbw = V0(), graf = V0(), grbf = V0();
+            float gc0 = 0.0f, unused = 0.0f;
+            row_c_bwd(c, qa0, qb0, c.t1, raf, rbf, gct1, unused, graf, grbf, pg);
+            row_c_bwd(c, qa0, qb0, c.t2, raf, rbf, gct2, unused, graf, grbf, pg);
+            friction_levers_bwd(c, graf, grbf, graw, grbw, pg);
+            row_c_bwd(c, qa0, qb0, c.n, raw, rbw, gcn, gc0, graw, grbw, pg);
+            contact_levers_bwd(c, ra, rb, graw, grbw, pg);
+            glo.w += gc0;
+            A.alam[q] = glo;
+            A.apen[q] = gpo;
+        }
+        uint2 ab = make_uint2(c.a, c.b);
+        slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
+        slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
+        float2 m = A.amu[p];
+        A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
+    }
+}
+
+// ---- primal block solve of one colour (assembly.rs:73-903) --------------------
+__global__ void __launch_bounds__(128) k_adj_body(DW w, AdjFrame f, AdjState A, int it, int colour) {
+    const uint32_t c0 = f.col_cnt[colour], c1 = f.col_cnt[colour + 1];
+    for (uint32_t i = c0 + blockIdx.x * blockDim.x + threadIdx.x; i < c1; i += gridDim.x * blockDim.x) {
+        uint32_t h = f.col_list[i];
+        // the body's pose adjoint: its own plus what partners left in its slots
+        V3 gx = ld3(A.ax[h]);
+        Q gq = ldq(A.aq[h]);
+        const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
+        for (uint32_t k = k0; k < k1; k++) {
+            float4* s = A.slot + (size_t)k * 4;
+            gx = gx + ld3(s[0]);
+            gq = qadd(gq, ldq(s[1]));
+            s[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            s[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+        V3 x = ld3(f.it_pos[pslice(w, it) + h]);
+        Q q = ldq(f.it_rot[pslice(w, it) + h]);
+        const size_t qoff = (size_t)it * f.qstride;
+        Sys s;
+        adj_inertial(w, f, h, x, q, s);
+        auto each_point = [&](auto&& fn) {
+            for (uint32_t k = f.offB[h]; k < f.offB[h + 1]; k++) {
+                uint32_t p = f.listB[k];
+                uint2 ab = f.p_ab[p];
+                PairCtx c;
+                Q qa0, qb0;
+                adj_ctx(w, f, p, seen_slice(f, ab.x, colour, it), it, c, qa0, qb0);
+                for (uint32_t j = 0; j < c.np; j++) fn(c, qa0, qb0, p, p * MAX_PTS + j, false);
+            }
+            for (uint32_t p = f.offA[h]; p < f.offA[h + 1]; p++) {
+                uint2 ab = f.p_ab[p];
+                PairCtx c;
+                Q qa0, qb0;
+                adj_ctx(w, f, p, it, seen_slice(f, ab.y, colour, it), c, qa0, qb0);
+                for (uint32_t j = 0; j < c.np; j++) fn(c, qa0, qb0, p, p * MAX_PTS + j, true);
+            }
+        };
+        each_point([&](const PairCtx& c, Q, Q, uint32_t, uint32_t q, bool is_a) {
+            adj_stamp_point(w, f, c, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], s);
+        });
+        float d6[6];
+        if (!solve_6x6(s, d6)) {  // breakdown: the forward skipped the update
+            A.ax[h] = st3(gx, 0.0f);
+            A.aq[h] = stq(gq);
+            continue;
+        }
+        V3 dang{d6[3], d6[4], d6[5]};
+        Q gqb = Q0();
+        V3 gdang = V0();
+        quat_integrate_bwd(q, dang, gq, gqb, gdang);
+        Sys s2 = s;
+        s2.r[0] = -gx.x;
+        s2.r[1] = -gx.y;
+        s2.r[2] = -gx.z;
+        s2.r[3] = -gdang.x;
+        s2.r[4] = -gdang.y;
+        s2.r[5] = -gdang.z;
+        float w6[6];
+        solve_6x6(s2, w6);  // w = H^-1 d_bar
+        V3 gxb = gx;
+        // inertial rows
+        {
+            float dt2 = w.dt * w.dt;
+            float im = is_dynamic(w, h) ? f.inv_mass[h] : 0.0f;
+            float m_dt2 = 1.0f / im / dt2;
+            V3 wl{w6[0], w6[1], w6[2]}, wa{w6[3], w6[4], w6[5]};
+            gxb = gxb - wl * m_dt2;
+            float4 ay = A.ay[h];
+            A.ay[h] = make_float4(ay.x + wl.x * m_dt2, ay.y + wl.y * m_dt2, ay.z + wl.z * m_dt2, 0.0f);
+            Q qt = ldq(f.inertial_rot[h]);
+            V3 inr = ld3(f.inertia[h]);
+            float iw[3][3];
+            world_inertia(inr, q, iw);
+            V3 th = quat_diff_vec(q, qt);
+            V3 gth = mat3_vec(iw, wa) * (-1.0f / dt2);
+            Q gqt = Q0();
+            quat_diff_vec_bwd(q, qt, gth, gqb, gqt);
+            world_inertia_bwd(inr, q, wa, th + dang, -1.0f / dt2, gqb);
+            A.aqt[h] = f4add(A.aqt[h], stq(gqt));
+        }
+        V3 gx0 = V0();
+        Q gq0 = Q0();
+        each_point([&](const PairCtx& c, Q qa0, Q qb0, uint32_t p, uint32_t q, bool is_a) {
+            PairGrad pg;
+            pair_grad_zero(pg);
+            float4 glam = make_float4(0.0f, 0.0f, 0.0f, 0.0f), gpen = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float2 gmu = make_float2(0.0f, 0.0f);
+            adj_point_bwd(w, f, c, qa0, qb0, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], w6, d6, pg, glam, gpen,
+                          gmu);
+            uint2 ab = make_uint2(c.a, c.b);
+            if (is_a) {
+                gxb = gxb + pg.xa;
+                gqb = qadd(gqb, pg.qa);
+                gx0 = gx0 + pg.xa0;
+                gq0 = qadd(gq0, pg.qa0);
+                slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
+            } else {
+                gxb = gxb + pg.xb;
+                gqb = qadd(gqb, pg.qb);
+                gx0 = gx0 + pg.xb0;
+                gq0 = qadd(gq0, pg.qb0);
+                slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
+            }
+            A.alam[q] = f4add(A.alam[q], glam);
+            A.apen[q] = f4add(A.apen[q], gpen);
+            float2 m = A.amu[p];
+            A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
+        });
+        A.ax0[h] = f4add(A.ax0[h], st3(gx0, 0.0f));
+        A.aq0[h] = f4add(A.aq0[h], stq(gq0));
+        A.ax[h] = st3(gxb, 0.0f);
+        A.aq[h] = stq(gqb);
+    }
+}
+
+// ---- C0 and the warmstart decay (joints_ext.rs:21-32, mod.rs:1019-1040) -------
+__global__ void k_adj_c0(DW w, AdjFrame f, AdjState A) {
+    const float ag = ALPHA * GAMMA;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npairs; p += gridDim.x * blockDim.x) {
+        uint32_t np = f.p_np[p];
+        if (np == 0) continue;
+        uint2 ab = f.p_ab[p];
+        float4 n4 = f.p_n[p];
+        V3 n = ld3(n4);
+        bool touching = n4.w <= 0.0f;
+        bool sa = info_shape(w.info[ab.x]) == AVBD_SHAPE_SPHERE, sb = info_shape(w.info[ab.y]) == AVBD_SHAPE_SPHERE;
+        Q qa0 = ldq(f.rot0[ab.x]), qb0 = ldq(f.rot0[ab.y]);
+        PairGrad pg;
+        pair_grad_zero(pg);
+        for (uint32_t k = 0; k < np; k++) {
+            uint32_t q = p * MAX_PTS + k;
+            float4 gl = A.alam[q], gp = A.apen[q];
+            if (touching && gl.w != 0.0f) {
+                // C0 = n.(w_a - w_b) + margin with the witnesses carried by the bodies
+                V3 g = n * gl.w;
+                V3 dummy = V0();
+                pg.xa0 = pg.xa0 + g;
+                if (!sa) qrot_bwd(qa0, ld3(f.q_ra[q]), g, pg.qa0, dummy);
+                pg.xb0 = pg.xb0 - g;
+                if (!sb) qrot_bwd(qb0, ld3(f.q_rb[q]), -g, pg.qb0, dummy);
+            }
+            float4 pen0 = f.it_pen[q];  // slice 0: after the decay clamp
+            auto keep = [](float v) { return v > PENALTY_MIN && v < PENALTY_MAX; };
+            A.alam[q] = make_float4(gl.x * ag, gl.y * ag, gl.z * ag, 0.0f);
+            A.apen[q] = make_float4(keep(pen0.x) ? gp.x * GAMMA : 0.0f, keep(pen0.y) ? gp.y * GAMMA : 0.0f,
+                                    keep(pen0.z) ? gp.z * GAMMA : 0.0f, 0.0f);
+        }
+        slot_add(slot_of(f, A, p, true, ab), V0(), Q0(), pg.xa0, pg.qa0);
+        slot_add(slot_of(f, A, p, false, ab), V0(), Q0(), pg.xb0, pg.qb0);
+    }
+}
+
+// ---- inertial targets (mod.rs:993-1018) -> the previous substep's state --------
+__global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    V3 gx = ld3(A.ax[h]), gx0 = ld3(A.ax0[h]);
+    Q gq = ldq(A.aq[h]), gq0 = ldq(A.aq0[h]);
+    const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
+    for (uint32_t k = k0; k < k1; k++) {
+        const float4* s = A.slot + (size_t)k * 4;
+        gx = gx + ld3(s[0]);
+        gq = qadd(gq, ldq(s[1]));
+        gx0 = gx0 + ld3(s[2]);
+        gq0 = qadd(gq0, ldq(s[3]));
+    }
+    if (f.colour[h] >= 0) {
+        // the iterations started from the targets: x = y = x0 + v dt + g dt^2,
+        // q = qt = integrate(q0, w dt)
+        float dt = w.dt;
+        V3 gy = ld3(A.ay[h]) + gx;
+        Q gqt = qadd(ldq(A.aqt[h]), gq);
+        gx0 = gx0 + gy;
+        V3 gwd = V0();
+        quat_integrate_bwd(ldq(f.rot0[h]), ld3(f.angvel[h]) * dt, gqt, gq0, gwd);
+        A.av[h] = st3(gy * dt, 0.0f);
+        A.aw[h] = st3(gwd * dt, 0.0f);
+        A.ax[h] = st3(gx0, 0.0f);
+        A.aq[h] = stq(gq0);
+    } else {
+        A.ax[h] = st3(gx + gx0, 0.0f);
+        A.aq[h] = stq(qadd(gq, gq0));
+    }
+}
+
+// ---- warm-state inheritance of the discovery merge (rows.rs:831-904) -----------
+// One thread per new pair: all new points that inherit from one old pair
+// belong to the same new pair, so the sums need no atomics.
+__global__ void k_adj_inherit(DW w, AdjFrame f, AdjState A) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npairs; p += gridDim.x * blockDim.x) {
+        int32_t o = f.p_old[p];
+        if (o < 0) continue;
+        uint32_t np = f.p_np[p];
+        for (uint32_t k = 0; k < np; k++) {
+            uint32_t q = p * MAX_PTS + k;
+            int32_t m = f.q_matched[q];
+            if (m < 0) continue;
+            size_t oq = (size_t)o * MAX_PTS + (uint32_t)m;
+            A.alam_old[oq] = f4add(A.alam_old[oq], A.alam[q]);
+            A.apen_old[oq] = f4add(A.apen_old[oq], A.apen[q]);
+        }
+    }
+}
+
+// ---- friction coefficient adjoint per scene (pair mu = max of the bodies') -----
+__global__ void k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (uint32_t)w.S) return;
+    uint32_t b0 = w.scene_off[s], b1 = w.scene_off[s + 1];
+    // pairs are ordered by their A body: binary search the scene's range
+    auto lower = [&](uint32_t key) {
+        uint32_t lo = 0, hi = f.npairs;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (f.p_ab[mid].x < key) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    uint32_t p0 = lower(b0), p1 = lower(b1);
+    float acc = 0.0f;
+    for (uint32_t p = p0; p < p1; p++) {
+        float2 m = A.amu[p];
+        acc += m.x + m.y;
+    }
+    A.ascene_mu[s] += acc;
+}
+
+void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st) {
+    unsigned gb = nblk(w.N, 256);
+    unsigned gp = f.npairs ? nblk(f.npairs, 128) : 1u;
+    k_adj_bdf<<<gb, 256, 0, st>>>(w, f, A, iters);
+    for (int it = iters - 1; it >= 0; it--) {
+        k_adj_dual<<<gp, 128, 0, st>>>(w, f, A, it);
+        for (int c = (int)f.ncol - 1; c >= 0; c--) k_adj_body<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
+    }
+    k_adj_c0<<<gp, 128, 0, st>>>(w, f, A);
+    k_adj_start<<<gb, 256, 0, st>>>(w, f, A);
+    k_adj_inherit<<<gp, 128, 0, st>>>(w, f, A);
+    k_adj_mu_scene<<<nblk(w.S, 128), 128, 0, st>>>(w, f, A);
+}
+
+}  // namespace avbd

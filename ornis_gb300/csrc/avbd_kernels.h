@@ -91,4 +91,7 @@ inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
     else exact::launch_dual(w, t, st);
 }
 
+// reverse of one recomputed substep (avbd_adjoint.cu)
+void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st);
+
 }  // namespace avbd

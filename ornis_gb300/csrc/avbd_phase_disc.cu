@@ -308,6 +308,7 @@ static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2
     w.p_n[p] = st3(normal, sgn);
     w.p_mu[p] = make_float2(mu, mu);
     w.p_np[p] = (uint32_t)nf;
+    if (w.p_old) w.p_old[p] = d.exists ? d.old : -1;
     bool touching = sgn <= 0.0f;
     bool smooth = ka == AVBD_SHAPE_SPHERE || kb == AVBD_SHAPE_SPHERE;
     uint32_t onp = d.exists ? w.o_np[d.old] : 0u;

@@ -19,7 +19,7 @@ struct Sys {
 };
 static __host__ __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
-static __device__ __forceinline__ Q quat_integrate(Q q, V3 v) {  // rows.rs:110-119
+static __host__ __device__ __forceinline__ Q quat_integrate(Q q, V3 v) {  // rows.rs:110-119
     float theta = len(v);
     if (theta < NEAR_ZERO) return q;
     float s, c;
@@ -28,7 +28,7 @@ static __device__ __forceinline__ Q quat_integrate(Q q, V3 v) {  // rows.rs:110-
     Q dq = qmul(Q{v.x * k, v.y * k, v.z * k, c}, q);
     return qnormalize(dq);
 }
-static __device__ __forceinline__ V3 quat_diff_vec(Q a, Q b) {  // rows.rs:128-146
+static __host__ __device__ __forceinline__ V3 quat_diff_vec(Q a, Q b) {  // rows.rs:128-146
     Q r = qmul(a, Q{-b.x, -b.y, -b.z, b.w});
     V3 xyz{r.x, r.y, r.z};
     if (r.w < 0.0f) xyz = -xyz;
@@ -36,24 +36,24 @@ static __device__ __forceinline__ V3 quat_diff_vec(Q a, Q b) {  // rows.rs:128-1
     if (s < NEAR_ZERO) return V0();
     return xyz * (2.0f * asinf(s) / s);
 }
-static __device__ __forceinline__ float rem_euclid(float x, float m) {
+static __host__ __device__ __forceinline__ float rem_euclid(float x, float m) {
     float r = fmodf(x, m);
     return r < 0.0f ? r + fabsf(m) : r;
 }
-static __device__ __forceinline__ float wrap_pi(float x) { return rem_euclid(x + PI_F, TAU_F) - PI_F; }
-static __device__ __forceinline__ float hinge_twist(Q qa, Q qb, V3 axis) {  // sequential_impulse/joints.rs:38-48
+static __host__ __device__ __forceinline__ float wrap_pi(float x) { return rem_euclid(x + PI_F, TAU_F) - PI_F; }
+static __host__ __device__ __forceinline__ float hinge_twist(Q qa, Q qb, V3 axis) {  // sequential_impulse/joints.rs:38-48
     Q q = qmul(conj(qa), qb);
     float t = 2.0f * atan2f(dot(V3{q.x, q.y, q.z}, axis), q.w);
     return rem_euclid(t + PI_F, TAU_F) - PI_F;
 }
-static __device__ __forceinline__ int warm_limit_state(float v, float lo, float hi, float slop, float force) {  // rows.rs:156-183
+static __host__ __device__ __forceinline__ int warm_limit_state(float v, float lo, float hi, float slop, float force) {  // rows.rs:156-183
     if (v <= lo + slop) return 1;
     if (v >= hi - slop) return 0;
     if (force < 0.0f) return 1;
     if (force > 0.0f) return 0;
     return -1;
 }
-static __device__ __forceinline__ float regularized_limit(float value, float initial, float bound, bool lower) {
+static __host__ __device__ __forceinline__ float regularized_limit(float value, float initial, float bound, bool lower) {
     float old = initial - bound;
     float viol = lower ? fminf(old, 0.0f) : fmaxf(old, 0.0f);
     return value - bound - ALPHA * viol;
@@ -62,14 +62,14 @@ static __host__ __device__ __forceinline__ V3 tangent_t1(V3 n) {  // math.rs:152
     V3 axis = fabsf(n.x) < TANGENT_REF_AXIS_DOT ? VX() : VY();
     return normalize_or(cross(n, axis), VZ());
 }
-static __device__ __forceinline__ void world_inertia(V3 inertia, Q rot, float m[3][3]) {  // rows.rs:194-207
+static __host__ __device__ __forceinline__ void world_inertia(V3 inertia, Q rot, float m[3][3]) {  // rows.rs:194-207
     V3 c[3];
     mat3_cols(rot, c);
     for (int a = 0; a < 3; a++)
         for (int b = 0; b < 3; b++)
             m[a][b] = c[0][a] * inertia.x * c[0][b] + c[1][a] * inertia.y * c[1][b] + c[2][a] * inertia.z * c[2][b];
 }
-static __device__ __forceinline__ void inverse_symmetric(const float m[3][3], V3 diag, float o[3][3]) {  // rows.rs:211-241
+static __host__ __device__ __forceinline__ void inverse_symmetric(const float m[3][3], V3 diag, float o[3][3]) {  // rows.rs:211-241
     float a = m[0][0], b = m[0][1], c = m[0][2], d = m[1][1], e = m[1][2], f = m[2][2];
     float det = a * (d * f - e * e) - b * (b * f - c * e) + c * (b * e - c * d);
     if (fabsf(det) < DEGENERATE_LEN2) {
@@ -85,14 +85,14 @@ static __device__ __forceinline__ void inverse_symmetric(const float m[3][3], V3
     o[1][0] = (c * e - b * f) * id; o[1][1] = (a * f - c * c) * id; o[1][2] = (b * c - a * e) * id;
     o[2][0] = (b * e - c * d) * id; o[2][1] = (b * c - a * e) * id; o[2][2] = (a * d - b * b) * id;
 }
-static __device__ __forceinline__ V3 mat3_vec(const float m[3][3], V3 v) {
+static __host__ __device__ __forceinline__ V3 mat3_vec(const float m[3][3], V3 v) {
     return {m[0][0] * v.x + m[0][1] * v.y + m[0][2] * v.z, m[1][0] * v.x + m[1][1] * v.y + m[1][2] * v.z,
             m[2][0] * v.x + m[2][1] * v.y + m[2][2] * v.z};
 }
-static __device__ __forceinline__ bool row_live(float c, float f) { return fabsf(c) >= C_EPS || f != 0.0f; }
+static __host__ __device__ __forceinline__ bool row_live(float c, float f) { return fabsf(c) >= C_EPS || f != 0.0f; }
 
 // stamp_row (rows.rs:1064-1092) restricted to the lower triangle.
-static __device__ __forceinline__ void stamp_row(Sys& s, V3 axis, float pen, float f, V3 r, float sign) {
+static __host__ __device__ __forceinline__ void stamp_row(Sys& s, V3 axis, float pen, float f, V3 r, float sign) {
     V3 nn = sign * axis;
     V3 t = cross(r, nn);
     float n3[3] = {nn.x, nn.y, nn.z}, t3[3] = {t.x, t.y, t.z};
@@ -110,7 +110,7 @@ static __device__ __forceinline__ void stamp_row(Sys& s, V3 axis, float pen, flo
     s.r[3] += f * t.x; s.r[4] += f * t.y; s.r[5] += f * t.z;
 }
 // Pure angular row (assembly.rs:637-647 and the limit rows).
-static __device__ __forceinline__ void stamp_angular(Sys& s, V3 g, float pen, float f) {
+static __host__ __device__ __forceinline__ void stamp_angular(Sys& s, V3 g, float pen, float f) {
     float g3[3] = {g.x, g.y, g.z};
 #pragma unroll
     for (int x = 0; x < 3; x++)
@@ -121,7 +121,7 @@ static __device__ __forceinline__ void stamp_angular(Sys& s, V3 g, float pen, fl
 
 // Dense LDL^T without pivoting (assembly.rs:25-69).  Returns false on a
 // breakdown pivot (<= 1e-12); the body then skips its update.
-static __device__ __forceinline__ bool solve_6x6(const Sys& s, float x[6]) {
+static __host__ __device__ __forceinline__ bool solve_6x6(const Sys& s, float x[6]) {
     float l[6][6];
     float d[6];
 #pragma unroll
@@ -162,7 +162,7 @@ static __device__ __forceinline__ bool solve_6x6(const Sys& s, float x[6]) {
 }
 
 // contact_force (rows.rs:1032-1060): push-only normal, elliptical cone.
-static __device__ __forceinline__ void contact_force(float cn, float4 pen, float4 lam, float ct0, float ct1, float2 mu,
+static __host__ __device__ __forceinline__ void contact_force(float cn, float4 pen, float4 lam, float ct0, float ct1, float2 mu,
                                               float f[3]) {
     float fnc = fminf(pen.x * cn + lam.x, 0.0f);
     float fr0 = pen.y * ct0 + lam.y, fr1 = pen.z * ct1 + lam.z;
@@ -197,16 +197,16 @@ struct PairCtx {
     float mu_roll, mu_spin;  // max of the two bodies' rolling / torsion friction
 };
 
-static __device__ __forceinline__ float row_c_levers(const PairCtx& c, V3 u, float c0, V3 raw, V3 rbw) {
+static __host__ __device__ __forceinline__ float row_c_levers(const PairCtx& c, V3 u, float c0, V3 raw, V3 rbw) {
     V3 da = c.dxa + u * dot(cross(raw, u), c.dra);
     V3 db = c.dxb + u * dot(cross(rbw, u), c.drb);
     return c0 * (1.0f - ALPHA) + dot(u, da - db);
 }
-static __device__ __forceinline__ void contact_levers(const PairCtx& c, float4 ra, float4 rb, V3& raw, V3& rbw) {  // :963-973
+static __host__ __device__ __forceinline__ void contact_levers(const PairCtx& c, float4 ra, float4 rb, V3& raw, V3& rbw) {  // :963-973
     raw = c.sph_a ? -c.n * c.rad_a : qrot(c.qa, ld3(ra));
     rbw = c.sph_b ? c.n * c.rad_b : qrot(c.qb, ld3(rb));
 }
-static __device__ __forceinline__ void friction_levers(const PairCtx& c, V3 raw, V3 rbw, V3& raf, V3& rbf) {  // :987-996
+static __host__ __device__ __forceinline__ void friction_levers(const PairCtx& c, V3 raw, V3 rbw, V3& raf, V3& rbf) {  // :987-996
     float sep = dot((c.pa + raw) - (c.pb + rbw), c.n);
     raf = raw - c.n * (sep * HALF);
     rbf = rbw + c.n * (sep * HALF);
@@ -214,7 +214,7 @@ static __device__ __forceinline__ void friction_levers(const PairCtx& c, V3 raw,
 // Step-start normal violation of a point (joints_ext.rs:21-32).  It depends on
 // the step-start poses only, so it is evaluated once per substep and kept in
 // the w lane of the point's lambda record.
-static __device__ __forceinline__ float gap_c0(bool sphere_pair, float gap, V3 n, V3 pa0, Q qa0, V3 pb0, Q qb0,
+static __host__ __device__ __forceinline__ float gap_c0(bool sphere_pair, float gap, V3 n, V3 pa0, Q qa0, V3 pb0, Q qb0,
                                                float4 ra, float4 rb) {
     if (sphere_pair) return gap + MARGIN;
     V3 pa = pa0 + qrot(qa0, ld3(ra));

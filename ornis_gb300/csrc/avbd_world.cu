@@ -53,6 +53,7 @@ struct PairBuf {
     uint32_t* np;
     float4 *ra, *rb, *lam, *pen, *roll;
     int32_t* matched;
+    int32_t* old;  // previous-generation pair index (-1 new)
     uint32_t* offA;
 };
 
@@ -135,6 +136,11 @@ float hinge_twist_host(const float qa[4], const float qb[4], const float ax[3]) 
 
 }  // namespace
 
+namespace {
+struct AdjTape;
+void adj_free(AdjTape* t);
+}  // namespace
+
 struct AvbdWorld {
     AvbdParams prm;
     int device = 0;
@@ -177,6 +183,7 @@ struct AvbdWorld {
     size_t graph_nodes = 0;       // kernel nodes in one captured substep (no events)
     size_t graph_nodes_emit = 0;  // ... in one that reports events
     uint64_t steps = 0;
+    AdjTape* adj = nullptr;  // checkpoints of the last differentiable rollout
 };
 
 #define CK(x)                                    \
@@ -194,6 +201,7 @@ static void set_pair_ptrs(AvbdWorld* W) {
     DW& w = W->w;
     w.p_ab = c.ab; w.p_n = c.n; w.p_mu = c.mu; w.p_np = c.np;
     w.q_ra = c.ra; w.q_rb = c.rb; w.q_lam = c.lam; w.q_pen = c.pen; w.q_roll = c.roll; w.q_matched = c.matched;
+    w.p_old = c.old;
     w.offA = c.offA;
     w.o_ab = o.ab; w.o_n = o.n; w.o_np = o.np;
     w.oq_ra = o.ra; w.oq_rb = o.rb; w.oq_lam = o.lam; w.oq_pen = o.pen; w.oq_roll = o.roll;
@@ -268,6 +276,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
         size_t q = (size_t)cand_cap * MAX_PTS;
         p.ra = m.get<float4>(q); p.rb = m.get<float4>(q); p.lam = m.get<float4>(q); p.pen = m.get<float4>(q);
         p.roll = m.get<float4>(q); p.matched = m.get<int32_t>(q);
+        p.old = m.get<int32_t>(cand_cap);
         p.offA = m.get<uint32_t>(N + 1);
     }
     w.offB = m.get<uint32_t>(N + 1);
@@ -835,6 +844,258 @@ static int substep_plain(AvbdWorld* W, bool emit) {
     return AVBD_ERR_CAPACITY;
 }
 
+// ---- differentiable rollouts ----------------------------------------------------
+// The forward records a device checkpoint of the whole step state every
+// `every` steps.  The backward walks the segments last to first: it restores
+// a segment's checkpoint, recomputes the segment with plain launches while
+// copying each substep's frozen contact set, colouring and iterates into a
+// frame, then runs the adjoint kernels over the frames in reverse.
+namespace {
+
+struct Snap {
+    Alloc mem;
+    int cur = 0;
+    uint32_t P = 0;
+    float4 *pos, *rot, *vel, *angvel, *torque, *prev_pos, *prev_rot, *inertia;
+    float *inv_mass, *sleep_timer;
+    uint32_t *asleep, *info;
+    PairBuf pb{};
+    uint32_t *offB, *listB, *posB;  // B-side incidence: the next discovery finds old pairs through it
+    float4 *jll, *jla, *jpl, *jpa, *jlim;
+};
+
+struct AdjTape {
+    int steps = 0, substeps = 0, every = 0;
+    uint32_t N = 0, J = 0, S = 0, max_pairs = 0;
+    std::vector<Snap*> ckpt;  // segment starts
+    Snap* fin = nullptr;      // the state after the rollout
+    Alloc fmem, smem;         // frames; adjoint state
+    uint32_t pcap = 0;        // pairs a frame holds
+    int nframes = 0;
+    std::vector<AdjFrame> frames;
+    AdjState A{};
+};
+
+void snap_free(Snap* s) {
+    if (!s) return;
+    s->mem.release();
+    delete s;
+}
+void adj_free(AdjTape* t) {
+    if (!t) return;
+    for (Snap* s : t->ckpt) snap_free(s);
+    snap_free(t->fin);
+    t->fmem.release();
+    t->smem.release();
+    delete t;
+}
+
+#define D2D(dst, src, bytes) CK(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st))
+
+int snap_take(AvbdWorld* W, Snap** out) {
+    DW& w = W->w;
+    cudaStream_t st = W->st;
+    const size_t N = (size_t)w.N, J = (size_t)w.J;
+    uint32_t P = 0;
+    CK(cudaMemcpyAsync(&P, w.offA + N, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    Snap* s = new Snap();
+    Alloc& m = s->mem;
+    s->cur = W->cur;
+    s->P = P;
+    const size_t Q = (size_t)P * MAX_PTS;
+    s->pos = m.get<float4>(N); s->rot = m.get<float4>(N); s->vel = m.get<float4>(N); s->angvel = m.get<float4>(N);
+    s->torque = m.get<float4>(N); s->prev_pos = m.get<float4>(N); s->prev_rot = m.get<float4>(N);
+    s->inertia = m.get<float4>(N);
+    s->inv_mass = m.get<float>(N); s->sleep_timer = m.get<float>(N);
+    s->asleep = m.get<uint32_t>(N); s->info = m.get<uint32_t>(N);
+    PairBuf& b = s->pb;
+    b.ab = m.get<uint2>(P); b.n = m.get<float4>(P); b.mu = m.get<float2>(P); b.np = m.get<uint32_t>(P);
+    b.old = m.get<int32_t>(P);
+    b.ra = m.get<float4>(Q); b.rb = m.get<float4>(Q); b.lam = m.get<float4>(Q); b.pen = m.get<float4>(Q);
+    b.roll = m.get<float4>(Q); b.matched = m.get<int32_t>(Q);
+    b.offA = m.get<uint32_t>(N + 1);
+    s->offB = m.get<uint32_t>(N + 1); s->listB = m.get<uint32_t>(P); s->posB = m.get<uint32_t>(P);
+    s->jll = m.get<float4>(J); s->jla = m.get<float4>(J); s->jpl = m.get<float4>(J); s->jpa = m.get<float4>(J);
+    s->jlim = m.get<float4>(J);
+    if (!s->jlim || !b.offA) {
+        snap_free(s);
+        return AVBD_ERR_DEVICE;
+    }
+    D2D(s->pos, w.pos, N * 16); D2D(s->rot, w.rot, N * 16); D2D(s->vel, w.vel, N * 16);
+    D2D(s->angvel, w.angvel, N * 16); D2D(s->torque, w.torque, N * 16); D2D(s->prev_pos, w.prev_pos, N * 16);
+    D2D(s->prev_rot, w.prev_rot, N * 16); D2D(s->inertia, w.inertia, N * 16);
+    D2D(s->inv_mass, w.inv_mass, N * 4); D2D(s->sleep_timer, w.sleep_timer, N * 4);
+    D2D(s->asleep, w.asleep, N * 4); D2D(s->info, w.info, N * 4);
+    if (P) {
+        D2D(b.ab, w.p_ab, P * 8); D2D(b.n, w.p_n, P * 16); D2D(b.mu, w.p_mu, P * 8); D2D(b.np, w.p_np, P * 4);
+        D2D(b.old, w.p_old, P * 4);
+        D2D(b.ra, w.q_ra, Q * 16); D2D(b.rb, w.q_rb, Q * 16); D2D(b.lam, w.q_lam, Q * 16);
+        D2D(b.pen, w.q_pen, Q * 16); D2D(b.roll, w.q_roll, Q * 16); D2D(b.matched, w.q_matched, Q * 4);
+    }
+    D2D(b.offA, w.offA, (N + 1) * 4);
+    D2D(s->offB, w.offB, (N + 1) * 4);
+    if (P) {
+        D2D(s->listB, w.listB, P * 4);
+        D2D(s->posB, w.posB, P * 4);
+    }
+    if (J) {
+        D2D(s->jll, w.j_lam_l, J * 16); D2D(s->jla, w.j_lam_a, J * 16); D2D(s->jpl, w.j_pen_l, J * 16);
+        D2D(s->jpa, w.j_pen_a, J * 16); D2D(s->jlim, w.j_lim, J * 16);
+    }
+    *out = s;
+    return AVBD_OK;
+}
+
+int snap_restore(AvbdWorld* W, const Snap* s) {
+    W->cur = s->cur;
+    set_pair_ptrs(W);
+    DW& w = W->w;
+    cudaStream_t st = W->st;
+    const size_t N = (size_t)w.N, J = (size_t)w.J, P = s->P, Q = P * MAX_PTS;
+    const PairBuf& b = s->pb;
+    D2D(w.pos, s->pos, N * 16); D2D(w.rot, s->rot, N * 16); D2D(w.vel, s->vel, N * 16);
+    D2D(w.angvel, s->angvel, N * 16); D2D(w.torque, s->torque, N * 16); D2D(w.prev_pos, s->prev_pos, N * 16);
+    D2D(w.prev_rot, s->prev_rot, N * 16); D2D(w.inertia, s->inertia, N * 16);
+    D2D(w.inv_mass, s->inv_mass, N * 4); D2D(w.sleep_timer, s->sleep_timer, N * 4);
+    D2D(w.asleep, s->asleep, N * 4); D2D(w.info, s->info, N * 4);
+    if (P) {
+        D2D(w.p_ab, b.ab, P * 8); D2D(w.p_n, b.n, P * 16); D2D(w.p_mu, b.mu, P * 8); D2D(w.p_np, b.np, P * 4);
+        D2D(w.p_old, b.old, P * 4);
+        D2D(w.q_ra, b.ra, Q * 16); D2D(w.q_rb, b.rb, Q * 16); D2D(w.q_lam, b.lam, Q * 16);
+        D2D(w.q_pen, b.pen, Q * 16); D2D(w.q_roll, b.roll, Q * 16); D2D(w.q_matched, b.matched, Q * 4);
+    }
+    D2D(w.offA, b.offA, (N + 1) * 4);
+    D2D(w.offB, s->offB, (N + 1) * 4);
+    if (P) {
+        D2D(w.listB, s->listB, P * 4);
+        D2D(w.posB, s->posB, P * 4);
+    }
+    if (J) {
+        D2D(w.j_lam_l, s->jll, J * 16); D2D(w.j_lam_a, s->jla, J * 16); D2D(w.j_pen_l, s->jpl, J * 16);
+        D2D(w.j_pen_a, s->jpa, J * 16); D2D(w.j_lim, s->jlim, J * 16);
+    }
+    W->host_valid = false;
+    W->dev_valid = true;
+    return AVBD_OK;
+}
+
+// Frames for `n` substeps of up to `pcap` pairs, and the adjoint state.
+int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
+    if (t->nframes >= n && t->pcap >= pcap) return AVBD_OK;
+    t->fmem.release();
+    t->smem.release();
+    t->frames.assign(n, AdjFrame{});
+    t->nframes = n;
+    t->pcap = pcap;
+    const size_t N = (size_t)W->w.N, Pc = pcap, Qc = Pc * MAX_PTS;
+    const int K = W->w.iterations;
+    Alloc& m = t->fmem;
+    for (AdjFrame& f : t->frames) {
+        f.qstride = Qc;
+        f.pos0 = m.get<float4>(N); f.rot0 = m.get<float4>(N); f.inertial = m.get<float4>(N);
+        f.inertial_rot = m.get<float4>(N); f.vel = m.get<float4>(N); f.angvel = m.get<float4>(N);
+        f.inertia = m.get<float4>(N); f.inv_mass = m.get<float>(N); f.asleep_end = m.get<uint32_t>(N);
+        f.it_pos = m.get<float4>(N * (K + 1)); f.it_rot = m.get<float4>(N * (K + 1));
+        f.colour = m.get<int32_t>(N); f.col_cnt = m.get<uint32_t>(MAX_COLOURS + 1); f.col_list = m.get<uint32_t>(N);
+        f.offA = m.get<uint32_t>(N + 1); f.offB = m.get<uint32_t>(N + 1);
+        f.listB = m.get<uint32_t>(Pc); f.posB = m.get<uint32_t>(Pc);
+        f.p_ab = m.get<uint2>(Pc); f.p_n = m.get<float4>(Pc); f.p_mu = m.get<float2>(Pc);
+        f.p_np = m.get<uint32_t>(Pc); f.p_old = m.get<int32_t>(Pc);
+        f.q_ra = m.get<float4>(Qc); f.q_rb = m.get<float4>(Qc); f.q_matched = m.get<int32_t>(Qc);
+        f.it_lam = m.get<float4>(Qc * (K + 1)); f.it_pen = m.get<float4>(Qc * (K + 1));
+        if (!f.it_pen) return AVBD_ERR_DEVICE;
+    }
+    Alloc& a = t->smem;
+    AdjState& A = t->A;
+    A.ax = a.get<float4>(N); A.aq = a.get<float4>(N); A.av = a.get<float4>(N); A.aw = a.get<float4>(N);
+    A.ax0 = a.get<float4>(N); A.aq0 = a.get<float4>(N); A.ay = a.get<float4>(N); A.aqt = a.get<float4>(N);
+    A.slot = a.get<float4>(Pc * 2 * 4);
+    A.alam = a.get<float4>(Qc); A.apen = a.get<float4>(Qc);
+    A.alam_old = a.get<float4>(Qc); A.apen_old = a.get<float4>(Qc);
+    A.amu = a.get<float2>(Pc);
+    A.ascene_mu = a.get<float>(W->w.S);
+    return A.ascene_mu ? AVBD_OK : AVBD_ERR_DEVICE;
+}
+
+// One substep with plain launches, its frame filled on the way.
+int adj_substep(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
+    cudaStream_t st = W->st;
+    for (int attempt = 0;; attempt++) {
+        if (attempt == 8) return AVBD_ERR_CAPACITY;
+        enqueue_front(W, false);
+        CK(cudaGetLastError());
+        int rc = read_ctr(W);
+        if (rc) return rc;
+        if (!(W->h_ctr[C_ERR] & E_CAND_OVERFLOW)) break;
+        W->cur = 1 - W->cur;
+        set_pair_ptrs(W);
+        CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, st));
+        rc = grow_candidates(W);
+        if (rc) return rc;
+    }
+    const DW& w = W->w;
+    const uint32_t P = W->h_ctr[C_PAIRS], ncol = W->h_ctr[C_NCOL];
+    if (P > t->pcap) return AVBD_ERR_CAPACITY;
+    W->last_ncol = (int)ncol;
+    f.npairs = P;
+    f.ncol = ncol;
+    const size_t N = (size_t)w.N, Q = (size_t)P * MAX_PTS;
+    D2D(f.pos0, w.pos0, N * 16); D2D(f.rot0, w.rot0, N * 16); D2D(f.inertial, w.inertial, N * 16);
+    D2D(f.inertial_rot, w.inertial_rot, N * 16); D2D(f.vel, w.vel, N * 16); D2D(f.angvel, w.angvel, N * 16);
+    D2D(f.inertia, w.inertia, N * 16); D2D(f.inv_mass, w.inv_mass, N * 4);
+    D2D(f.colour, w.colour, N * 4); D2D(f.col_cnt, w.col_cnt, (MAX_COLOURS + 1) * 4); D2D(f.col_list, w.col_list, N * 4);
+    D2D(f.offA, w.offA, (N + 1) * 4); D2D(f.offB, w.offB, (N + 1) * 4);
+    D2D(f.it_pos, w.pos, N * 16); D2D(f.it_rot, w.rot, N * 16);
+    if (P) {
+        D2D(f.listB, w.listB, P * 4); D2D(f.posB, w.posB, P * 4);
+        D2D(f.p_ab, w.p_ab, P * 8); D2D(f.p_n, w.p_n, P * 16); D2D(f.p_mu, w.p_mu, P * 8);
+        D2D(f.p_np, w.p_np, P * 4); D2D(f.p_old, w.p_old, P * 4);
+        D2D(f.q_ra, w.q_ra, Q * 16); D2D(f.q_rb, w.q_rb, Q * 16); D2D(f.q_matched, w.q_matched, Q * 4);
+        D2D(f.it_lam, w.q_lam, Q * 16); D2D(f.it_pen, w.q_pen, Q * 16);
+    }
+    launch_solve_prep(w, W->tune, st);
+    for (int it = 0; it < w.iterations; it++) {
+        for (uint32_t c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, (int)c, (uint32_t)w.N, st);
+        D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
+        D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);
+        launch_dual(w, W->tune, st);
+        if (P) {
+            D2D(f.it_lam + (it + 1) * f.qstride, w.q_lam, Q * 16);
+            D2D(f.it_pen + (it + 1) * f.qstride, w.q_pen, Q * 16);
+        }
+    }
+    launch_finish_substep(w, W->tune, st);
+    D2D(f.asleep_end, w.asleep, N * 4);
+    CK(cudaGetLastError());
+    int rc = read_ctr(W);
+    if (rc) return rc;
+    accumulate(W);
+    if (W->h_ctr[C_ERR] & E_COLOUR_OVERFLOW) return AVBD_ERR_CAPACITY;
+    return AVBD_OK;
+}
+
+int adj_reverse(AvbdWorld* W, AdjTape* t, const AdjFrame& f) {
+    cudaStream_t st = W->st;
+    AdjState& A = t->A;
+    const size_t Qc = (size_t)t->pcap * MAX_PTS;
+    if (f.npairs) {
+        CK(cudaMemsetAsync(A.slot, 0, (size_t)f.npairs * 2 * 4 * 16, st));
+        CK(cudaMemsetAsync(A.amu, 0, (size_t)f.npairs * 8, st));
+    }
+    CK(cudaMemsetAsync(A.alam_old, 0, Qc * 16, st));
+    CK(cudaMemsetAsync(A.apen_old, 0, Qc * 16, st));
+    launch_adjoint_substep(W->w, f, A, W->w.iterations, st);
+    CK(cudaGetLastError());
+    std::swap(A.alam, A.alam_old);
+    std::swap(A.apen, A.apen_old);
+    return AVBD_OK;
+}
+
+#undef D2D
+
+}  // namespace
+
 template <class T>
 static int drain(AvbdWorld* W, int which, T* out, uint32_t cap, uint32_t* n) {
     if (!W || !n || (cap && !out)) return AVBD_ERR_INVALID_ARG;
@@ -916,6 +1177,7 @@ int avbd_world_destroy(AvbdWorld* W) {
     if (!W) return AVBD_ERR_INVALID_ARG;
     cudaSetDevice(W->device);
     free_graphs(W);
+    adj_free(W->adj);
     W->mem.release();
     W->evmem.release();
     W->hullmem.release();
@@ -1632,6 +1894,103 @@ int avbd_world_drain_contact_events(AvbdWorld* W, AvbdContactEvent* out, uint32_
 }
 int avbd_world_drain_trigger_events(AvbdWorld* W, AvbdTriggerEvent* out, uint32_t cap, uint32_t* n) {
     return drain(W, 1, out, cap, n);
+}
+
+int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t every) {
+    if (!W || steps <= 0 || substeps <= 0 || every <= 0) return AVBD_ERR_INVALID_ARG;
+    if (!W->joints.empty()) return AVBD_ERR_UNSUPPORTED;  // contact rows only
+    for (const AvbdBody& b : W->bodies)
+        if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f) return AVBD_ERR_UNSUPPORTED;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    adj_free(W->adj);
+    AdjTape* t = W->adj = new AdjTape();
+    t->steps = steps;
+    t->substeps = substeps;
+    t->every = every;
+    t->N = (uint32_t)W->w.N;
+    t->J = (uint32_t)W->w.J;
+    t->S = (uint32_t)W->w.S;
+    for (int s = 0; s < steps; s++) {
+        if (s % every == 0) {
+            Snap* sn = nullptr;
+            rc = snap_take(W, &sn);
+            if (rc) return rc;
+            t->ckpt.push_back(sn);
+        }
+        for (int k = 0; k < substeps; k++) {
+            rc = avbd_world_step_graph(W, 1);
+            if (rc) return rc;
+            t->max_pairs = std::max(t->max_pairs, W->h_ctr[C_PAIRS]);
+        }
+    }
+    return snap_take(W, &t->fin);
+}
+
+int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_initial, float* grad_friction) {
+    if (!W || !W->adj || !grad_final || !grad_initial) return AVBD_ERR_INVALID_ARG;
+    AdjTape* t = W->adj;
+    if ((uint32_t)W->w.N != t->N || (uint32_t)W->w.J != t->J || (uint32_t)W->w.S != t->S) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    cudaStream_t st = W->st;
+    const int per_seg = t->every * t->substeps;
+    uint32_t pmax = t->max_pairs;  // point inheritance also indexes the checkpoints' generations
+    for (const Snap* s : t->ckpt) pmax = std::max(pmax, s->P);
+    int rc = adj_storage(W, t, per_seg, pmax + 64);
+    if (rc) return rc;
+    const size_t N = t->N;
+    AdjState& A = t->A;
+    {
+        std::vector<float4> x(N), q(N), v(N), w(N);
+        for (size_t h = 0; h < N; h++) {
+            const float* g = grad_final + 13 * h;
+            x[h] = make_float4(g[0], g[1], g[2], 0.0f);
+            q[h] = make_float4(g[3], g[4], g[5], g[6]);
+            v[h] = make_float4(g[7], g[8], g[9], 0.0f);
+            w[h] = make_float4(g[10], g[11], g[12], 0.0f);
+        }
+        CK(cudaMemcpyAsync(A.ax, x.data(), N * 16, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(A.aq, q.data(), N * 16, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(A.av, v.data(), N * 16, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(A.aw, w.data(), N * 16, cudaMemcpyHostToDevice, st));
+        const size_t Qc = (size_t)t->pcap * MAX_PTS;
+        CK(cudaMemsetAsync(A.alam, 0, Qc * 16, st));
+        CK(cudaMemsetAsync(A.apen, 0, Qc * 16, st));
+        CK(cudaMemsetAsync(A.ascene_mu, 0, t->S * 4, st));
+        CK(cudaStreamSynchronize(st));  // the staging vectors go out of scope
+    }
+    const int nseg = (int)t->ckpt.size();
+    for (int seg = nseg - 1; seg >= 0; seg--) {
+        rc = snap_restore(W, t->ckpt[seg]);
+        if (rc) return rc;
+        const int nsteps = std::min(t->every, t->steps - seg * t->every);
+        const int nsub = nsteps * t->substeps;
+        for (int k = 0; k < nsub; k++) {
+            rc = adj_substep(W, t, t->frames[k]);
+            if (rc) return rc;
+        }
+        for (int k = nsub - 1; k >= 0; k--) {
+            rc = adj_reverse(W, t, t->frames[k]);
+            if (rc) return rc;
+        }
+    }
+    {
+        std::vector<float4> x(N), q(N), v(N), w(N);
+        CK(cudaMemcpyAsync(x.data(), A.ax, N * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(q.data(), A.aq, N * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(v.data(), A.av, N * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(w.data(), A.aw, N * 16, cudaMemcpyDeviceToHost, st));
+        if (grad_friction) CK(cudaMemcpyAsync(grad_friction, A.ascene_mu, t->S * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (size_t h = 0; h < N; h++) {
+            float* g = grad_initial + 13 * h;
+            g[0] = x[h].x; g[1] = x[h].y; g[2] = x[h].z;
+            g[3] = q[h].x; g[4] = q[h].y; g[5] = q[h].z; g[6] = q[h].w;
+            g[7] = v[h].x; g[8] = v[h].y; g[9] = v[h].z;
+            g[10] = w[h].x; g[11] = w[h].y; g[12] = w[h].z;
+        }
+    }
+    return snap_restore(W, t->fin);
 }
 
 }  // extern "C"

@@ -154,6 +154,7 @@ struct DW {
     uint32_t* p_np;
     float4 *q_ra, *q_rb, *q_lam, *q_pen, *q_roll;  // q_rb.w = stuck
     int32_t* q_matched;
+    int32_t* p_old;  // previous-generation index of each pair, -1 when new (read by the adjoint)
     uint32_t* offA;  // N+1: pairs whose A side is body h are [offA[h], offA[h+1])
     uint32_t* offB;  // N+1: B-side incidence list
     uint32_t* listB;
@@ -217,6 +218,48 @@ struct DW {
     uint32_t* col_list;  // N: swept bodies grouped by colour, ascending index within a colour
     uint32_t *col_key, *col_key2, *col_val, *col_hist;
     uint32_t* ctr;       // counters
+};
+
+// One recomputed substep as the adjoint kernels read it: the frozen contact
+// set and colouring, the step-start and target poses, and the iterates.
+// Pose slice 0 is the pose the iterations start from, slice i+1 the pose
+// after the primal sweep of iteration i; point slice 0 is the warm state
+// after the decay (lambda.w = the step-start gap C0), slice i+1 the state
+// after the dual update of iteration i.
+struct AdjFrame {
+    uint32_t npairs, ncol;
+    size_t qstride;  // point entries per point slice
+    // bodies
+    float4 *pos0, *rot0, *inertial, *inertial_rot, *vel, *angvel, *inertia;
+    float* inv_mass;
+    uint32_t* asleep_end;  // asleep after the substep's sleep pass
+    float4 *it_pos, *it_rot;  // (iterations + 1) slices of N
+    int32_t* colour;
+    uint32_t *col_cnt, *col_list;
+    uint32_t *offA, *offB, *listB, *posB;
+    // pairs and points
+    uint2* p_ab;
+    float4* p_n;
+    float2* p_mu;
+    uint32_t* p_np;
+    int32_t* p_old;
+    float4 *q_ra, *q_rb;
+    int32_t* q_matched;
+    float4 *it_lam, *it_pen;  // (iterations + 1) slices of qstride
+};
+// Adjoint state.  Body adjoints are of the state between substeps (pose,
+// velocities) plus per-substep accumulators; every (pair, side) incidence
+// slot holds 4 float4 (pose adjoint pending for the body, step-start pose
+// adjoint) so that contributions to a body from its partners are summed in
+// a fixed order.
+struct AdjState {
+    float4 *ax, *aq, *av, *aw;
+    float4 *ax0, *aq0, *ay, *aqt;
+    float4* slot;
+    float4 *alam, *apen;          // points of the current generation (alam.w: adjoint of C0)
+    float4 *alam_old, *apen_old;  // points of the previous generation
+    float2* amu;                  // per pair
+    float* ascene_mu;             // per scene: friction coefficient adjoint
 };
 
 }  // namespace avbd

@@ -17,6 +17,10 @@ ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "libavbd_oracle.so")
 
 REFERENCE = 0
 COLOURED = 1
+DUAL = 2  # use_double value of an f64 dual-number (forward-mode) world
+
+# fields of OracleWorld.seed
+F_POS, F_ROT, F_VEL, F_ANGVEL, F_FRICTION = 0, 1, 2, 3, 4
 
 _lib = None
 
@@ -74,6 +78,9 @@ def lib():
         L.oracle_drain_contact_events.argtypes = [vp, vp, C.c_uint32]
         L.oracle_drain_trigger_events.restype = C.c_uint32
         L.oracle_drain_trigger_events.argtypes = [vp, vp, C.c_uint32]
+        L.oracle_dual_seed.argtypes = [vp, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.oracle_dual_freeze_frames.argtypes = [vp, C.c_int]
+        L.oracle_dual_tangents.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -211,3 +218,18 @@ class OracleWorld:
         out = np.zeros(cap, dtype=abi.TRIGGER_EVENT_DTYPE)
         n = lib().oracle_drain_trigger_events(self.h, abi.ptr(out), cap)
         return out[:n]
+
+    # ---- dual-number worlds (use_double=DUAL) ----
+    def seed(self, body, field, comp, direction, value=1.0):
+        """d(field[comp] of body)/d(direction) = value in the initial state."""
+        assert lib().oracle_dual_seed(self.h, int(body), int(field), int(comp), int(direction), float(value)) == 0
+
+    def freeze_frames(self, on=True):
+        assert lib().oracle_dual_freeze_frames(self.h, int(on)) == 0
+
+    def tangents(self):
+        """(bodies, 13, directions): derivatives of pos, quat, vel, angvel."""
+        nd = lib().oracle_dual_dirs()
+        out = np.zeros((self.nbodies, 13, nd), dtype=np.float64)
+        assert lib().oracle_dual_tangents(self.h, abi.ptr(out)) == 0
+        return out
