@@ -359,6 +359,9 @@ def run_ours(args):
     # does not finish a step in bounded time)
     if args.plain_scenes > 0 and not joints_all:
         plain = plain_rate(bodies_all, offs_all, params, nsub, args)
+    adj = None
+    if args.adjoint_scenes > 0 and world == 1 and not joints_all:
+        adj = adjoint_rate(args)
     cb = None
     if args.cpu_per_core > 0 and world == 1 and not joints_all:
         cb = cpu_baseline(bodies_all, offs_all, params, nsub, start=args.start, steps=args.steps,
@@ -385,6 +388,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "plain_one_scene": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
+        "adjoint": adj,
         "phases_ms_per_substep": phases,
         "counters_at_end": {"candidates": c.candidates, "pairs": c.pairs, "points": c.points, "colours": c.colours,
                             "sleeping": c.sleeping, "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits,
@@ -392,6 +396,53 @@ def run_ours(args):
     }
     print(json.dumps(line))
     return 0
+
+
+def adjoint_rate(args):
+    """The differentiable batch (diff_1024): recorded forward with checkpoints,
+    then the reverse sweep, against the plain graph-replayed forward."""
+    from ornis_gb300.avbd import AvbdWorld
+
+    bodies, offs, ball, tower = scenes.diff_towers(nscenes=args.adjoint_scenes)
+    params, nsub = scenes.params_for("diff_1024")
+    steps, every = args.adjoint_steps, 10
+    ndyn = scenes.dynamic_count(bodies)
+    w = AvbdWorld(params, bodies=bodies, scene_offsets=offs)
+    w.set_precision(True)
+    w.set_events(-1)
+    s0 = w.export_state()
+    w.step_graph(nsub * 3)  # warm-up: graphs captured
+    w.import_state(s0)
+    w.sync()
+    t0 = time.perf_counter()
+    fwd_dev_ms = w.step_timed(nsub * steps, use_graph=True)
+    fwd_s = time.perf_counter() - t0
+    w.import_state(s0)
+    w.sync()
+    t0 = time.perf_counter()
+    w.adjoint_forward(steps, nsub, every)
+    rec_s = time.perf_counter() - t0
+    end = w.bodies()
+    g = np.zeros((len(bodies), 13), dtype=np.float32)
+    g[tower, 0:3] = 2.0 * end["position"][tower]
+    loss = float(np.sum(end["position"][tower].astype(np.float64) ** 2))
+    t0 = time.perf_counter()
+    g0, gmu = w.adjoint_backward(g)
+    bwd_s = time.perf_counter() - t0
+    rec_ms, rev_ms = w.adjoint_timing()
+    w.close()
+    gv = g0[ball, 7:10]
+    return {"workload": "diff_1024", "scenes": int(len(offs) - 1), "dynamic_bodies": ndyn, "steps": steps,
+            "checkpoint_every": every, "dt": 1 / 60, "iterations": params.iterations, "precision": "fast",
+            "forward_ms_per_step": 1e3 * fwd_s / steps, "forward_device_ms_per_step": fwd_dev_ms / steps,
+            "record_ms_per_step": 1e3 * rec_s / steps, "backward_ms_per_step": 1e3 * bwd_s / steps,
+            "adjoint_steps_per_s": steps / bwd_s, "adjoint_body_steps_per_s": ndyn * steps / bwd_s,
+            "backward_over_forward": bwd_s / fwd_s, "loss": loss,
+            "backward_split_ms_per_step": {"recompute": rec_ms / steps, "reverse": rev_ms / steps},
+            "grad_ball_velocity_mean": [float(x) for x in gv.mean(axis=0)],
+            "grad_friction_mean": float(np.mean(gmu)),
+            "how": "wall time with the host waiting; backward = per-segment recompute from the checkpoint "
+                   "plus the reverse sweep; forward = the same rollout by CUDA-graph replay"}
 
 
 def plain_rate(bodies, offs, params, nsub, args):
@@ -436,6 +487,8 @@ def main():
     ap.add_argument("--profile-region", type=int, default=0,
                     help="steps bracketed by cudaProfilerStart/Stop before the timed region")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
+    ap.add_argument("--adjoint-scenes", type=int, default=1024, help="differentiable batch size (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=120)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

@@ -413,7 +413,10 @@ int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uin
  * avbd_world_step_graph) and keep a device checkpoint of the full step
  * state every `checkpoint_every` steps, for avbd_adjoint_backward.  Worlds
  * with joints or with rolling / torsion friction return
- * AVBD_ERR_UNSUPPORTED.  A new forward replaces the previous recording. */
+ * AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
+ * (avbd_set_tuning lanes 0), which the world keeps afterwards; retuning the
+ * world before the backward invalidates the recording.  A new forward
+ * replaces the previous recording. */
 int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int32_t checkpoint_every);
 
 /* Reverse-mode gradient of a scalar loss of the recorded rollout's final
@@ -429,6 +432,10 @@ int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int3
  * recomputed from its checkpoint.  The world is left at the end of the
  * recorded rollout. */
 int avbd_adjoint_backward(AvbdWorld* world, const float* grad_final, float* grad_initial, float* grad_friction);
+
+/* Device time of the last avbd_adjoint_backward: ms[0] the segment
+ * recomputes (restores included), ms[1] the reverse sweeps. */
+int avbd_adjoint_timing(AvbdWorld* world, float* ms);
 
 #ifdef __cplusplus
 }

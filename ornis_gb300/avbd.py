@@ -77,6 +77,7 @@ def lib():
             "avbd_world_event_counts": [vp, vp],
             "avbd_adjoint_forward": [vp, C.c_int32, C.c_int32, C.c_int32],
             "avbd_adjoint_backward": [vp, vp, vp, vp],
+            "avbd_adjoint_timing": [vp, vp],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -330,6 +331,13 @@ class AvbdWorld:
         mu = np.zeros(ns.value, dtype=np.float32)
         _check(lib().avbd_adjoint_backward(self.h, abi.ptr(g), abi.ptr(out), abi.ptr(mu)), "adjoint_backward")
         return out, mu
+
+
+    def adjoint_timing(self):
+        """(recompute ms, reverse ms) of the last adjoint_backward, device time."""
+        ms = np.zeros(2, dtype=np.float32)
+        _check(lib().avbd_adjoint_timing(self.h, abi.ptr(ms)), "adjoint_timing")
+        return float(ms[0]), float(ms[1])
 
 
 class Rollout:

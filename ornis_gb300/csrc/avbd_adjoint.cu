@@ -14,7 +14,9 @@
 //   k_adj_bdf          BDF1 velocities and the quaternion renormalisation
 //   per iteration, last first:
 //     k_adj_dual       the dual update of every point (pair order)
-//     k_adj_body       per colour, last first: one body's block solve
+//     per colour, last first:
+//       k_adj_solve    each body's block solve (thread per body)
+//       k_adj_sides    its contact rows (thread per pair side)
 //   k_adj_c0           C0 and the warmstart decay
 //   k_adj_start        the inertial targets -> previous substep's state
 //   k_adj_inherit      point adjoints -> the previous generation's points
@@ -79,35 +81,6 @@ static __device__ __forceinline__ bool damper(const DW& w, const AdjFrame& f, co
     if (!(m_red > 0.0f)) return false;
     pen_d = fminf(2.0f * m_red / (w.dt * w.dt) / npts, PENALTY_MAX);
     return true;
-}
-
-// The rows of one point for the body on side is_a (the forward stamp_point
-// without rolling friction).
-static __device__ __forceinline__ void adj_stamp_point(const DW& w, const AdjFrame& f, const PairCtx& c, uint32_t q,
-                                                       bool is_a, float4 lam, float4 pen, Sys& s) {
-    float4 ra = f.q_ra[q], rb = f.q_rb[q];
-    float sign = is_a ? 1.0f : -1.0f;
-    bool touching = c.gap <= 0.0f;
-    float c0 = touching ? lam.w : 0.0f;
-    V3 rup, rlo;
-    contact_levers(c, ra, rb, rup, rlo);
-    float cn = row_c_levers(c, c.n, c0, rup, rlo);
-    V3 r_side = is_a ? rup : rlo;
-    if (!touching) {
-        float pen_d;
-        if (damper(w, f, c, cn, pen_d)) stamp_row(s, c.n, pen_d, fminf(pen_d * cn, 0.0f), r_side, sign);
-        return;
-    }
-    V3 raf, rbf;
-    friction_levers(c, rup, rlo, raf, rbf);
-    V3 r_side_f = is_a ? raf : rbf;
-    float ct1 = row_c_levers(c, c.t1, 0.0f, raf, rbf);
-    float ct2 = row_c_levers(c, c.t2, 0.0f, raf, rbf);
-    float fo[3];
-    contact_force(cn, pen, lam, ct1, ct2, c.mu, fo);
-    if (row_live(cn, fo[0])) stamp_row(s, c.n, pen.x, fo[0], r_side, sign);
-    if (row_live(ct1, fo[1])) stamp_row(s, c.t1, pen.y, fo[1], r_side_f, sign);
-    if (row_live(ct2, fo[2])) stamp_row(s, c.t2, pen.z, fo[2], r_side_f, sign);
 }
 
 // One stamped row J = [s a; r x (s a)] with H += pen J J^T, rhs += f J: the
@@ -268,7 +241,7 @@ __global__ void k_adj_bdf(DW w, AdjFrame f, AdjState A, int iters) {
 }
 
 // ---- dual update (joints_ext.rs:464-573), one thread per pair ------------------
-__global__ void k_adj_dual(DW w, AdjFrame f, AdjState A, int it) {
+__global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState A, int it) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npairs; p += gridDim.x * blockDim.x) {
         uint32_t np = f.p_np[p];
         if (np == 0) continue;
@@ -354,50 +327,48 @@ __global__ void k_adj_dual(DW w, AdjFrame f, AdjState A, int it) {
 }
 
 // ---- primal block solve of one colour (assembly.rs:73-903) --------------------
-__global__ void __launch_bounds__(128) k_adj_body(DW w, AdjFrame f, AdjState A, int it, int colour) {
+// Two passes per colour, like the forward's split primal.  k_adj_solve (one
+// thread per body) rebuilds the body's system from its inertial block and
+// the per-incidence row sums the recompute kept, solves for the step d and
+// for w = H^-1 d_bar, and takes the inertial rows' adjoint; k_adj_sides (one
+// thread per (pair, side)) takes the adjoint of that side's contact rows and
+// leaves the results in the incidence slots of both bodies of the pair.
+__global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A, int it, int colour) {
     const uint32_t c0 = f.col_cnt[colour], c1 = f.col_cnt[colour + 1];
     for (uint32_t i = c0 + blockIdx.x * blockDim.x + threadIdx.x; i < c1; i += gridDim.x * blockDim.x) {
         uint32_t h = f.col_list[i];
-        // the body's pose adjoint: its own plus what partners left in its slots
         V3 gx = ld3(A.ax[h]);
         Q gq = ldq(A.aq[h]);
         const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
         for (uint32_t k = k0; k < k1; k++) {
-            float4* s = A.slot + (size_t)k * 4;
-            gx = gx + ld3(s[0]);
-            gq = qadd(gq, ldq(s[1]));
-            s[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            s[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float4* sl = A.slot + (size_t)k * 4;
+            gx = gx + ld3(sl[0]);
+            gq = qadd(gq, ldq(sl[1]));
+            sl[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            sl[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         V3 x = ld3(f.it_pos[pslice(w, it) + h]);
         Q q = ldq(f.it_rot[pslice(w, it) + h]);
-        const size_t qoff = (size_t)it * f.qstride;
         Sys s;
         adj_inertial(w, f, h, x, q, s);
-        auto each_point = [&](auto&& fn) {
-            for (uint32_t k = f.offB[h]; k < f.offB[h + 1]; k++) {
-                uint32_t p = f.listB[k];
-                uint2 ab = f.p_ab[p];
-                PairCtx c;
-                Q qa0, qb0;
-                adj_ctx(w, f, p, seen_slice(f, ab.x, colour, it), it, c, qa0, qb0);
-                for (uint32_t j = 0; j < c.np; j++) fn(c, qa0, qb0, p, p * MAX_PTS + j, false);
-            }
-            for (uint32_t p = f.offA[h]; p < f.offA[h + 1]; p++) {
-                uint2 ab = f.p_ab[p];
-                PairCtx c;
-                Q qa0, qb0;
-                adj_ctx(w, f, p, it, seen_slice(f, ab.y, colour, it), c, qa0, qb0);
-                for (uint32_t j = 0; j < c.np; j++) fn(c, qa0, qb0, p, p * MAX_PTS + j, true);
-            }
-        };
-        each_point([&](const PairCtx& c, Q, Q, uint32_t, uint32_t q, bool is_a) {
-            adj_stamp_point(w, f, c, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], s);
-        });
+        const float4* cb = f.it_contrib + (size_t)it * f.cstride;
+        for (uint32_t k = k0; k < k1; k++) {  // incidence order, as the forward sums them
+            const float4* o = cb + (size_t)k * 7;
+            float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];
+            s.h[0] += v0.x; s.h[1] += v0.y; s.h[2] += v0.z; s.h[3] += v0.w;
+            s.h[4] += v1.x; s.h[5] += v1.y; s.h[6] += v1.z; s.h[7] += v1.w;
+            s.h[8] += v2.x; s.h[9] += v2.y; s.h[10] += v2.z; s.h[11] += v2.w;
+            s.h[12] += v3.x; s.h[13] += v3.y; s.h[14] += v3.z; s.h[15] += v3.w;
+            s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
+            s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
+            s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
+        }
+        float4* wd = A.wd + (size_t)h * 3;
         float d6[6];
         if (!solve_6x6(s, d6)) {  // breakdown: the forward skipped the update
             A.ax[h] = st3(gx, 0.0f);
             A.aq[h] = stq(gq);
+            wd[0] = wd[1] = wd[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             continue;
         }
         V3 dang{d6[3], d6[4], d6[5]};
@@ -413,59 +384,65 @@ __global__ void __launch_bounds__(128) k_adj_body(DW w, AdjFrame f, AdjState A, 
         s2.r[5] = -gdang.z;
         float w6[6];
         solve_6x6(s2, w6);  // w = H^-1 d_bar
-        V3 gxb = gx;
-        // inertial rows
-        {
-            float dt2 = w.dt * w.dt;
-            float im = is_dynamic(w, h) ? f.inv_mass[h] : 0.0f;
-            float m_dt2 = 1.0f / im / dt2;
-            V3 wl{w6[0], w6[1], w6[2]}, wa{w6[3], w6[4], w6[5]};
-            gxb = gxb - wl * m_dt2;
-            float4 ay = A.ay[h];
-            A.ay[h] = make_float4(ay.x + wl.x * m_dt2, ay.y + wl.y * m_dt2, ay.z + wl.z * m_dt2, 0.0f);
-            Q qt = ldq(f.inertial_rot[h]);
-            V3 inr = ld3(f.inertia[h]);
-            float iw[3][3];
-            world_inertia(inr, q, iw);
-            V3 th = quat_diff_vec(q, qt);
-            V3 gth = mat3_vec(iw, wa) * (-1.0f / dt2);
-            Q gqt = Q0();
-            quat_diff_vec_bwd(q, qt, gth, gqb, gqt);
-            world_inertia_bwd(inr, q, wa, th + dang, -1.0f / dt2, gqb);
-            A.aqt[h] = f4add(A.aqt[h], stq(gqt));
-        }
-        V3 gx0 = V0();
-        Q gq0 = Q0();
-        each_point([&](const PairCtx& c, Q qa0, Q qb0, uint32_t p, uint32_t q, bool is_a) {
-            PairGrad pg;
-            pair_grad_zero(pg);
-            float4 glam = make_float4(0.0f, 0.0f, 0.0f, 0.0f), gpen = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            float2 gmu = make_float2(0.0f, 0.0f);
-            adj_point_bwd(w, f, c, qa0, qb0, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], w6, d6, pg, glam, gpen,
-                          gmu);
-            uint2 ab = make_uint2(c.a, c.b);
-            if (is_a) {
-                gxb = gxb + pg.xa;
-                gqb = qadd(gqb, pg.qa);
-                gx0 = gx0 + pg.xa0;
-                gq0 = qadd(gq0, pg.qa0);
-                slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
-            } else {
-                gxb = gxb + pg.xb;
-                gqb = qadd(gqb, pg.qb);
-                gx0 = gx0 + pg.xb0;
-                gq0 = qadd(gq0, pg.qb0);
-                slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
-            }
-            A.alam[q] = f4add(A.alam[q], glam);
-            A.apen[q] = f4add(A.apen[q], gpen);
-            float2 m = A.amu[p];
-            A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
-        });
-        A.ax0[h] = f4add(A.ax0[h], st3(gx0, 0.0f));
-        A.aq0[h] = f4add(A.aq0[h], stq(gq0));
+        // inertial rows: -d/ds [w.(rhs + H d)] of the mass and inertia blocks
+        float dt2 = w.dt * w.dt;
+        float m_dt2 = 1.0f / f.inv_mass[h] / dt2;
+        V3 wl{w6[0], w6[1], w6[2]}, wa{w6[3], w6[4], w6[5]};
+        V3 gxb = gx - wl * m_dt2;
+        float4 ay = A.ay[h];
+        A.ay[h] = make_float4(ay.x + wl.x * m_dt2, ay.y + wl.y * m_dt2, ay.z + wl.z * m_dt2, 0.0f);
+        Q qt = ldq(f.inertial_rot[h]);
+        V3 inr = ld3(f.inertia[h]);
+        float iw[3][3];
+        world_inertia(inr, q, iw);
+        V3 th = quat_diff_vec(q, qt);
+        V3 gth = mat3_vec(iw, wa) * (-1.0f / dt2);
+        Q gqt = Q0();
+        quat_diff_vec_bwd(q, qt, gth, gqb, gqt);
+        world_inertia_bwd(inr, q, wa, th + dang, -1.0f / dt2, gqb);
+        A.aqt[h] = f4add(A.aqt[h], stq(gqt));
         A.ax[h] = st3(gxb, 0.0f);
         A.aq[h] = stq(gqb);
+        wd[0] = make_float4(w6[0], w6[1], w6[2], w6[3]);
+        wd[1] = make_float4(w6[4], w6[5], d6[0], d6[1]);
+        wd[2] = make_float4(d6[2], d6[3], d6[4], d6[5]);
+    }
+}
+
+__global__ void __launch_bounds__(128, 3) k_adj_sides(DW w, AdjFrame f, AdjState A, int it, int colour) {
+    const uint32_t s0 = f.side_cnt[colour], s1 = f.side_cnt[colour + 1];
+    const size_t qoff = (size_t)it * f.qstride;
+    for (uint32_t i = s0 + blockIdx.x * blockDim.x + threadIdx.x; i < s1; i += gridDim.x * blockDim.x) {
+        uint32_t e = f.side_list[i];
+        uint32_t p = e >> 1;
+        bool is_a = (e & 1u) != 0u;
+        uint2 ab = f.p_ab[p];
+        uint32_t h = is_a ? ab.x : ab.y;
+        const float4* wd = A.wd + (size_t)h * 3;
+        float4 x0 = wd[0], x1 = wd[1], x2 = wd[2];
+        const float w6[6] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y};
+        const float d6[6] = {x1.z, x1.w, x2.x, x2.y, x2.z, x2.w};
+        PairCtx c;
+        Q qa0, qb0;
+        if (is_a) adj_ctx(w, f, p, it, seen_slice(f, ab.y, colour, it), c, qa0, qb0);
+        else adj_ctx(w, f, p, seen_slice(f, ab.x, colour, it), it, c, qa0, qb0);
+        PairGrad pg;
+        pair_grad_zero(pg);
+        float2 gmu = make_float2(0.0f, 0.0f);
+        for (uint32_t k = 0; k < c.np; k++) {
+            uint32_t q = p * MAX_PTS + k;
+            float4 glam = make_float4(0.0f, 0.0f, 0.0f, 0.0f), gpen = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            adj_point_bwd(w, f, c, qa0, qb0, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], w6, d6, pg, glam, gpen,
+                          gmu);
+            A.alam[q] = f4add(A.alam[q], glam);
+            A.apen[q] = f4add(A.apen[q], gpen);
+        }
+        // the body's own adjoint (of its pose before this update) and its
+        // partner's both wait in the slots until the next gather
+        slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
+        slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
+        float2 m = A.amu[p];
+        A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
     }
 }
 
@@ -585,10 +562,14 @@ __global__ void k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
 void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st) {
     unsigned gb = nblk(w.N, 256);
     unsigned gp = f.npairs ? nblk(f.npairs, 128) : 1u;
+    unsigned gp2 = f.npairs ? nblk((size_t)f.npairs * 2, 128) : 1u;
     k_adj_bdf<<<gb, 256, 0, st>>>(w, f, A, iters);
     for (int it = iters - 1; it >= 0; it--) {
         k_adj_dual<<<gp, 128, 0, st>>>(w, f, A, it);
-        for (int c = (int)f.ncol - 1; c >= 0; c--) k_adj_body<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
+        for (int c = (int)f.ncol - 1; c >= 0; c--) {
+            k_adj_solve<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
+            k_adj_sides<<<gp2, 128, 0, st>>>(w, f, A, it, c);
+        }
     }
     k_adj_c0<<<gp, 128, 0, st>>>(w, f, A);
     k_adj_start<<<gb, 256, 0, st>>>(w, f, A);

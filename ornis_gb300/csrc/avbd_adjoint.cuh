@@ -120,58 +120,6 @@ static __host__ __device__ __forceinline__ void world_inertia_bwd(V3 inertia, Q 
     mat3_cols_bwd(q, gc, gq);
 }
 
-// Dense LDL^T of the 6x6 system, then two solves: x = -H^-1 r (the forward
-// step) and y = H^-1 g.  Returns false on a breakdown pivot, as solve_6x6.
-static __host__ __device__ __forceinline__ bool solve2_6x6(const Sys& s, const float g[6], float x[6], float y6[6]) {
-    float l[6][6];
-    float d[6];
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-#pragma unroll
-        for (int j = 0; j <= i; j++) {
-            float v = s.h[tri(i, j)];
-#pragma unroll
-            for (int k = 0; k < j; k++) v -= l[i][k] * d[k] * l[j][k];
-            if (i == j) {
-                if (v <= DEGENERATE_LEN2) return false;
-                d[i] = v;
-                l[i][i] = 1.0f;
-            } else {
-                l[i][j] = v / d[j];
-            }
-        }
-    }
-    float ya[6], yb[6];
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-        float va = -s.r[i], vb = g[i];
-#pragma unroll
-        for (int k = 0; k < i; k++) {
-            va -= l[i][k] * ya[k];
-            vb -= l[i][k] * yb[k];
-        }
-        ya[i] = va;
-        yb[i] = vb;
-    }
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-        ya[i] /= d[i];
-        yb[i] /= d[i];
-    }
-#pragma unroll
-    for (int i = 5; i >= 0; i--) {
-        float va = ya[i], vb = yb[i];
-#pragma unroll
-        for (int k = i + 1; k < 6; k++) {
-            va -= l[k][i] * x[k];
-            vb -= l[k][i] * y6[k];
-        }
-        x[i] = va;
-        y6[i] = vb;
-    }
-    return true;
-}
-
 // contact_force (rows.rs:1032-1060) adjoint.  gf: adjoints of the three
 // force components; adds to gcn, gpen, glam, gct0/gct1, gmu.
 static __host__ __device__ __forceinline__ void contact_force_bwd(float cn, float4 pen, float4 lam, float ct0, float ct1,

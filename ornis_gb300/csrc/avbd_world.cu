@@ -874,6 +874,7 @@ struct AdjTape {
     int nframes = 0;
     std::vector<AdjFrame> frames;
     AdjState A{};
+    float ms_recompute = 0.0f, ms_reverse = 0.0f;  // device time of the last backward
 };
 
 void snap_free(Snap* s) {
@@ -1004,7 +1005,10 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
         f.p_np = m.get<uint32_t>(Pc); f.p_old = m.get<int32_t>(Pc);
         f.q_ra = m.get<float4>(Qc); f.q_rb = m.get<float4>(Qc); f.q_matched = m.get<int32_t>(Qc);
         f.it_lam = m.get<float4>(Qc * (K + 1)); f.it_pen = m.get<float4>(Qc * (K + 1));
-        if (!f.it_pen) return AVBD_ERR_DEVICE;
+        f.side_list = m.get<uint32_t>(Pc * 2); f.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
+        f.cstride = Pc * 2 * 7;
+        f.it_contrib = m.get<float4>(f.cstride * K);
+        if (!f.it_contrib) return AVBD_ERR_DEVICE;
     }
     Alloc& a = t->smem;
     AdjState& A = t->A;
@@ -1015,7 +1019,8 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
     A.alam_old = a.get<float4>(Qc); A.apen_old = a.get<float4>(Qc);
     A.amu = a.get<float2>(Pc);
     A.ascene_mu = a.get<float>(W->w.S);
-    return A.ascene_mu ? AVBD_OK : AVBD_ERR_DEVICE;
+    A.wd = a.get<float4>(N * 3);
+    return A.wd ? AVBD_OK : AVBD_ERR_DEVICE;
 }
 
 // One substep with plain launches, its frame filled on the way.
@@ -1055,8 +1060,11 @@ int adj_substep(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
         D2D(f.it_lam, w.q_lam, Q * 16); D2D(f.it_pen, w.q_pen, Q * 16);
     }
     launch_solve_prep(w, W->tune, st);
+    D2D(f.side_cnt, w.side_cnt, (2 * MAX_COLOURS + 2) * 4);
+    if (P) D2D(f.side_list, w.side_list, P * 2 * 4);
     for (int it = 0; it < w.iterations; it++) {
         for (uint32_t c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, (int)c, (uint32_t)w.N, st);
+        if (P) D2D(f.it_contrib + it * f.cstride, w.contrib, (size_t)P * 2 * 7 * 16);
         D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
         D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);
         launch_dual(w, W->tune, st);
@@ -1903,6 +1911,11 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
         if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f) return AVBD_ERR_UNSUPPORTED;
     int rc = begin_steps(W);
     if (rc) return rc;
+    if (W->tune.primal_lanes != 0) {
+        // the reverse sweep reuses the split primal's per-incidence row sums
+        rc = avbd_set_tuning(W, 0, W->tune.primal_block);
+        if (rc) return rc;
+    }
     adj_free(W->adj);
     AdjTape* t = W->adj = new AdjTape();
     t->steps = steps;
@@ -1927,10 +1940,18 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
     return snap_take(W, &t->fin);
 }
 
+int avbd_adjoint_timing(AvbdWorld* W, float* ms) {
+    if (!W || !ms || !W->adj) return AVBD_ERR_INVALID_ARG;
+    ms[0] = W->adj->ms_recompute;
+    ms[1] = W->adj->ms_reverse;
+    return AVBD_OK;
+}
+
 int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_initial, float* grad_friction) {
     if (!W || !W->adj || !grad_final || !grad_initial) return AVBD_ERR_INVALID_ARG;
     AdjTape* t = W->adj;
     if ((uint32_t)W->w.N != t->N || (uint32_t)W->w.J != t->J || (uint32_t)W->w.S != t->S) return AVBD_ERR_INVALID_ARG;
+    if (W->tune.primal_lanes != 0) return AVBD_ERR_INVALID_ARG;  // retuned since the forward
     cudaSetDevice(W->device);
     cudaStream_t st = W->st;
     const int per_seg = t->every * t->substeps;
@@ -1960,20 +1981,27 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         CK(cudaStreamSynchronize(st));  // the staging vectors go out of scope
     }
     const int nseg = (int)t->ckpt.size();
-    for (int seg = nseg - 1; seg >= 0; seg--) {
+    cudaEvent_t ev[3];
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    t->ms_recompute = t->ms_reverse = 0.0f;
+    for (int seg = nseg - 1; seg >= 0 && !rc; seg--) {
+        CK(cudaEventRecord(ev[0], st));
         rc = snap_restore(W, t->ckpt[seg]);
-        if (rc) return rc;
         const int nsteps = std::min(t->every, t->steps - seg * t->every);
         const int nsub = nsteps * t->substeps;
-        for (int k = 0; k < nsub; k++) {
-            rc = adj_substep(W, t, t->frames[k]);
-            if (rc) return rc;
-        }
-        for (int k = nsub - 1; k >= 0; k--) {
-            rc = adj_reverse(W, t, t->frames[k]);
-            if (rc) return rc;
-        }
+        for (int k = 0; k < nsub && !rc; k++) rc = adj_substep(W, t, t->frames[k]);
+        CK(cudaEventRecord(ev[1], st));
+        for (int k = nsub - 1; k >= 0 && !rc; k--) rc = adj_reverse(W, t, t->frames[k]);
+        CK(cudaEventRecord(ev[2], st));
+        CK(cudaEventSynchronize(ev[2]));
+        float a = 0.0f, b = 0.0f;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        t->ms_recompute += a;
+        t->ms_reverse += b;
     }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
     {
         std::vector<float4> x(N), q(N), v(N), w(N);
         CK(cudaMemcpyAsync(x.data(), A.ax, N * 16, cudaMemcpyDeviceToHost, st));

@@ -246,6 +246,11 @@ struct AdjFrame {
     float4 *q_ra, *q_rb;
     int32_t* q_matched;
     float4 *it_lam, *it_pen;  // (iterations + 1) slices of qstride
+    // split primal: per-colour side lists and, per iteration, the 7 float4
+    // row sums of every incidence slot
+    uint32_t *side_list, *side_cnt;
+    float4* it_contrib;  // iterations slices of cstride
+    size_t cstride;
 };
 // Adjoint state.  Body adjoints are of the state between substeps (pose,
 // velocities) plus per-substep accumulators; every (pair, side) incidence
@@ -260,6 +265,7 @@ struct AdjState {
     float4 *alam_old, *apen_old;  // points of the previous generation
     float2* amu;                  // per pair
     float* ascene_mu;             // per scene: friction coefficient adjoint
+    float4* wd;                   // 3 per body: w = H^-1 d_bar and the step d of its last reversed solve
 };
 
 }  // namespace avbd

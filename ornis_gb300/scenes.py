@@ -18,6 +18,15 @@ Workloads (sizes as named by the benchmark configuration):
                    dropped into a 20x20 bin (ground + 4 wall half-spaces) from
                    a jittered column grid; dt 1/120, 2 substeps, 8 iterations;
                    seed 2.
+  diff_1024        1024 scenes of a 32-box tower (unit cubes, friction 0.6) on
+                   a ground plane hit by a ball (r 0.5, mass 5) whose initial
+                   velocity is N((10,0,0), I) per scene (seed 3); every body of
+                   a scene shares the friction coefficient 0.6; dt 1/60, 10
+                   iterations, 120 steps, a checkpoint every 10 steps; the loss
+                   is the sum of squared final tower-body positions.
+  ragdoll_8192     2 scenes of 3000 and 5192 ragdolls of 15 capsules with
+                   ball and limited hinge joints (seed 4); dt 1/120, 2
+                   substeps, 12 iterations.
 """
 import math
 
@@ -200,6 +209,29 @@ def batched(nscenes=4096, seed=2, lo=8, hi=1024):
         parts.append(sc)
         offs.append(offs[-1] + len(sc))
     return np.concatenate(parts), np.asarray(offs, dtype=np.uint32), counts
+
+
+def diff_towers(nscenes=1024, seed=3, height=32, mu=0.6):
+    """The differentiable batch: per scene a ground plane, `height` stacked
+    unit cubes and a ball 2 m in front of the tower's base.  Returns
+    (bodies, scene_offsets, ball_index, tower_mask)."""
+    rng = np.random.default_rng(seed)
+    per = height + 2
+    kinds = [abi.SHAPE_BOX] * height + [abi.SHAPE_SPHERE]
+    params = [[0.5, 0.5, 0.5]] * height + [[0.5, 0.0, 0.0]]
+    mass = [1.0] * height + [5.0]
+    pos = [[0.0, 0.5 + i, 0.0] for i in range(height)] + [[-2.5, 1.0, 0.0]]
+    scene = np.concatenate([halfspace([0, 0, 0], [0, 1, 0]), make_bodies(kinds, params, pos, mass)])
+    scene["friction"] = mu
+    scene["friction_transverse"] = mu
+    bodies = np.tile(scene, nscenes)
+    ball = np.arange(nscenes) * per + per - 1
+    bodies["velocity"][ball] = (rng.normal(size=(nscenes, 3)) + np.array([10.0, 0.0, 0.0])).astype(F)
+    offs = (np.arange(nscenes + 1) * per).astype(np.uint32)
+    tower = np.zeros(len(bodies), dtype=bool)
+    for k in range(height):
+        tower[np.arange(nscenes) * per + 1 + k] = True
+    return bodies, offs, ball, tower
 
 
 def params_for(workload):

@@ -35,9 +35,17 @@ def roll(mu=0.6, v=2.0):
 
 
 def stack(mu=0.6, n=3, v=1.0):
+    """A box stack sheared at its base.  The boxes start 1 mm into their
+    supports, offset 5 cm and turned 0.02 rad per level, so that no contact
+    sits on a selection threshold (touching at exactly zero gap, or a corner
+    at the edge of the manifold patch): there the f32 and f64 rollouts would
+    pick different contact points and differentiate different functions."""
     bs = [O.body_new(abi.SHAPE_HALFSPACE, [0, 1, 0], [0, 0, 0], 0.0)]
     for i in range(n):
-        bs.append(O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0.5 + i, 0], 1.0))
+        b = O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0.05 * i, 0.499 + 0.999 * i, -0.03 * i], 1.0)
+        yaw = 0.02 * (i + 1)
+        b.orientation[:] = [0.0, np.sin(yaw / 2), 0.0, np.cos(yaw / 2)]
+        bs.append(b)
     bs[1].velocity[0] = v
     return _finish(bs, mu)
 
