@@ -414,7 +414,8 @@ int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uin
  * state every `checkpoint_every` steps, for avbd_adjoint_backward.  Worlds
  * with joints or with rolling / torsion friction return
  * AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
- * (avbd_set_tuning lanes 0), which the world keeps afterwards; retuning the
+ * (avbd_set_tuning lanes 0) and orders every body's contact pairs (the
+ * static bodies' too), which the world keeps afterwards; retuning the
  * world before the backward invalidates the recording.  A new forward
  * replaces the previous recording. */
 int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int32_t checkpoint_every);

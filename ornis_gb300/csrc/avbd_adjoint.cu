@@ -13,10 +13,10 @@
 // Order of one substep's reverse:
 //   k_adj_bdf          BDF1 velocities and the quaternion renormalisation
 //   per iteration, last first:
-//     k_adj_dual       the dual update of every point (pair order)
+//     k_adj_dual       the dual update of every point (4 lanes per pair)
 //     per colour, last first:
 //       k_adj_solve    each body's block solve (thread per body)
-//       k_adj_sides    its contact rows (thread per pair side)
+//       k_adj_sides    its contact rows (4 lanes per pair side)
 //   k_adj_c0           C0 and the warmstart decay
 //   k_adj_start        the inertial targets -> previous substep's state
 //   k_adj_inherit      point adjoints -> the previous generation's points
@@ -204,6 +204,21 @@ static __device__ __forceinline__ void slot_add(float4* s, V3 x, Q q, V3 x0, Q q
     s[2] = make_float4(c.x + x0.x, c.y + x0.y, c.z + x0.z, 0.0f);
     s[3] = make_float4(d.x + q0.x, d.y + q0.y, d.z + q0.z, d.w + q0.w);
 }
+// Sum a PairGrad and a float2 over the ADJ_LANES lanes of a group.
+constexpr int ADJ_LANES = 4;
+static __device__ __forceinline__ float lsum(float v) {
+#pragma unroll
+    for (int o = ADJ_LANES / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, ADJ_LANES);
+    return v;
+}
+static __device__ __forceinline__ V3 lsum(V3 v) { return {lsum(v.x), lsum(v.y), lsum(v.z)}; }
+static __device__ __forceinline__ Q lsum(Q v) { return {lsum(v.x), lsum(v.y), lsum(v.z), lsum(v.w)}; }
+static __device__ __forceinline__ void lsum(PairGrad& g, float2& m) {
+    g.xa = lsum(g.xa); g.xb = lsum(g.xb); g.xa0 = lsum(g.xa0); g.xb0 = lsum(g.xb0);
+    g.qa = lsum(g.qa); g.qb = lsum(g.qb); g.qa0 = lsum(g.qa0); g.qb0 = lsum(g.qb0);
+    m.x = lsum(m.x);
+    m.y = lsum(m.y);
+}
 static __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
@@ -240,19 +255,22 @@ __global__ void k_adj_bdf(DW w, AdjFrame f, AdjState A, int iters) {
     A.aw[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-// ---- dual update (joints_ext.rs:464-573), one thread per pair ------------------
+// ---- dual update (joints_ext.rs:464-573), ADJ_LANES lanes per pair -------------
+// Lane l of a pair's group takes points l, l + ADJ_LANES, ...; the pose and
+// friction adjoints are summed over the group before lane 0 stores them.
 __global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState A, int it) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < f.npairs; p += gridDim.x * blockDim.x) {
-        uint32_t np = f.p_np[p];
-        if (np == 0) continue;
-        PairCtx c;
-        Q qa0, qb0;
+    const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t p = gid / ADJ_LANES;
+    const int lane = (int)(threadIdx.x % ADJ_LANES);
+    const bool active = p < f.npairs && f.p_np[p] != 0 && f.p_n[p].w <= 0.0f;  // separated points keep lambda
+    PairGrad pg;
+    pair_grad_zero(pg);
+    float2 gmu = make_float2(0.0f, 0.0f);
+    PairCtx c;
+    Q qa0 = Q0(), qb0 = Q0();
+    if (active) {
         adj_ctx(w, f, p, it + 1, it + 1, c, qa0, qb0);
-        if (c.gap > 0.0f) continue;  // separated points keep lambda and penalty
-        PairGrad pg;
-        pair_grad_zero(pg);
-        float2 gmu = make_float2(0.0f, 0.0f);
-        for (uint32_t k = 0; k < np; k++) {
+        for (uint32_t k = lane; k < c.np; k += ADJ_LANES) {
             uint32_t q = p * MAX_PTS + k;
             size_t qi = (size_t)it * f.qstride + q;
             float4 lam = f.it_lam[qi], pen = f.it_pen[qi];
@@ -318,12 +336,14 @@ __global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState 
             A.alam[q] = glo;
             A.apen[q] = gpo;
         }
-        uint2 ab = make_uint2(c.a, c.b);
-        slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
-        slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
-        float2 m = A.amu[p];
-        A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
     }
+    lsum(pg, gmu);
+    if (!active || lane != 0) return;
+    uint2 ab = make_uint2(c.a, c.b);
+    slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
+    slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
+    float2 m = A.amu[p];
+    A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
 }
 
 // ---- primal block solve of one colour (assembly.rs:73-903) --------------------
@@ -412,11 +432,19 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
 __global__ void __launch_bounds__(128, 3) k_adj_sides(DW w, AdjFrame f, AdjState A, int it, int colour) {
     const uint32_t s0 = f.side_cnt[colour], s1 = f.side_cnt[colour + 1];
     const size_t qoff = (size_t)it * f.qstride;
-    for (uint32_t i = s0 + blockIdx.x * blockDim.x + threadIdx.x; i < s1; i += gridDim.x * blockDim.x) {
+    const uint32_t i = s0 + (blockIdx.x * blockDim.x + threadIdx.x) / ADJ_LANES;
+    const int lane = (int)(threadIdx.x % ADJ_LANES);
+    const bool active = i < s1;
+    PairGrad pg;
+    pair_grad_zero(pg);
+    float2 gmu = make_float2(0.0f, 0.0f);
+    uint32_t p = 0;
+    uint2 ab = make_uint2(0u, 0u);
+    if (active) {
         uint32_t e = f.side_list[i];
-        uint32_t p = e >> 1;
+        p = e >> 1;
         bool is_a = (e & 1u) != 0u;
-        uint2 ab = f.p_ab[p];
+        ab = f.p_ab[p];
         uint32_t h = is_a ? ab.x : ab.y;
         const float4* wd = A.wd + (size_t)h * 3;
         float4 x0 = wd[0], x1 = wd[1], x2 = wd[2];
@@ -426,10 +454,7 @@ __global__ void __launch_bounds__(128, 3) k_adj_sides(DW w, AdjFrame f, AdjState
         Q qa0, qb0;
         if (is_a) adj_ctx(w, f, p, it, seen_slice(f, ab.y, colour, it), c, qa0, qb0);
         else adj_ctx(w, f, p, seen_slice(f, ab.x, colour, it), it, c, qa0, qb0);
-        PairGrad pg;
-        pair_grad_zero(pg);
-        float2 gmu = make_float2(0.0f, 0.0f);
-        for (uint32_t k = 0; k < c.np; k++) {
+        for (uint32_t k = lane; k < c.np; k += ADJ_LANES) {
             uint32_t q = p * MAX_PTS + k;
             float4 glam = make_float4(0.0f, 0.0f, 0.0f, 0.0f), gpen = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             adj_point_bwd(w, f, c, qa0, qb0, q, is_a, f.it_lam[qoff + q], f.it_pen[qoff + q], w6, d6, pg, glam, gpen,
@@ -437,13 +462,15 @@ __global__ void __launch_bounds__(128, 3) k_adj_sides(DW w, AdjFrame f, AdjState
             A.alam[q] = f4add(A.alam[q], glam);
             A.apen[q] = f4add(A.apen[q], gpen);
         }
-        // the body's own adjoint (of its pose before this update) and its
-        // partner's both wait in the slots until the next gather
-        slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
-        slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
-        float2 m = A.amu[p];
-        A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
     }
+    lsum(pg, gmu);
+    if (!active || lane != 0) return;
+    // the body's own adjoint (of its pose before this update) and its
+    // partner's both wait in the slots until the next gather
+    slot_add(slot_of(f, A, p, true, ab), pg.xa, pg.qa, pg.xa0, pg.qa0);
+    slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
+    float2 m = A.amu[p];
+    A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
 }
 
 // ---- C0 and the warmstart decay (joints_ext.rs:21-32, mod.rs:1019-1040) -------
@@ -562,10 +589,11 @@ __global__ void k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
 void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st) {
     unsigned gb = nblk(w.N, 256);
     unsigned gp = f.npairs ? nblk(f.npairs, 128) : 1u;
-    unsigned gp2 = f.npairs ? nblk((size_t)f.npairs * 2, 128) : 1u;
+    unsigned gpl = f.npairs ? nblk((size_t)f.npairs * ADJ_LANES, 128) : 1u;
+    unsigned gp2 = f.npairs ? nblk((size_t)f.npairs * 2 * ADJ_LANES, 128) : 1u;
     k_adj_bdf<<<gb, 256, 0, st>>>(w, f, A, iters);
     for (int it = iters - 1; it >= 0; it--) {
-        k_adj_dual<<<gp, 128, 0, st>>>(w, f, A, it);
+        k_adj_dual<<<gpl, 128, 0, st>>>(w, f, A, it);
         for (int c = (int)f.ncol - 1; c >= 0; c--) {
             k_adj_solve<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
             k_adj_sides<<<gp2, 128, 0, st>>>(w, f, A, it, c);

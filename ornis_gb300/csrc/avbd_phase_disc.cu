@@ -136,14 +136,16 @@ __global__ void k_place(DW w) {
 // Each dynamic body's A-side slots in ascending b, so a swept body visits its
 // pairs in the reference's order.  The segments of static bodies
 // (half-spaces, floors: often long) are never read in sequence and are left
-// as placed.
+// as placed, unless the world keeps a differentiable rollout: its adjoint
+// carries point state across checkpoints by pair index, so every segment is
+// put in one order.
 __global__ void k_sort_slots(DW w) {
     if (aborted(w)) return;
     uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= (uint32_t)w.N) return;
     if (a == 0) w.ctr[C_PAIRS] = w.offA[w.N];
     uint32_t s0 = w.offA[a], s1 = w.offA[a + 1];
-    if (!is_dynamic(w, a)) return;
+    if (!is_dynamic(w, a) && !w.sort_static) return;
     for (uint32_t i = s0 + 1; i < s1; i++) {
         uint32_t c = w.slot_c[i];
         uint32_t bk = w.cand[c].y;

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -184,6 +185,7 @@ struct AvbdWorld {
     size_t graph_nodes_emit = 0;  // ... in one that reports events
     uint64_t steps = 0;
     AdjTape* adj = nullptr;  // checkpoints of the last differentiable rollout
+    uint64_t mem_gen = 0;    // bumped whenever the device arrays are (re)allocated
 };
 
 #define CK(x)                                    \
@@ -222,6 +224,7 @@ static void free_graphs(AvbdWorld* W) {
 static uint32_t default_cand_cap(uint32_t n) { return 12u * n + 4096u; }
 
 static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap) {
+    W->mem_gen++;
     // the previous touch set (handle keyed) survives a reallocation
     std::vector<uint32_t> tof, tkeys;
     if (W->w.toff && W->w.evs) {
@@ -238,7 +241,9 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     free_graphs(W);
     Alloc& m = W->mem;
     DW& w = W->w;
+    const int sort_static = w.sort_static;  // a setting of the world, not of the allocation
     w = DW{};
+    w.sort_static = sort_static;
     uint32_t S = (uint32_t)W->scene_off.size() - 1;
     w.N = (int)N;
     w.S = (int)S;
@@ -873,6 +878,9 @@ struct AdjTape {
     uint32_t pcap = 0;        // pairs a frame holds
     int nframes = 0;
     std::vector<AdjFrame> frames;
+    std::vector<std::array<cudaGraphExec_t, 2>> rg;  // recording graphs per frame and parity
+    int rg_cols = 0;
+    uint64_t rg_key = 0;  // the world allocation (mem_gen) the graphs were captured against
     AdjState A{};
     float ms_recompute = 0.0f, ms_reverse = 0.0f;  // device time of the last backward
 };
@@ -882,8 +890,10 @@ void snap_free(Snap* s) {
     s->mem.release();
     delete s;
 }
+void adj_free_graphs(AdjTape* t);
 void adj_free(AdjTape* t) {
     if (!t) return;
+    adj_free_graphs(t);
     for (Snap* s : t->ckpt) snap_free(s);
     snap_free(t->fin);
     t->fmem.release();
@@ -984,6 +994,7 @@ int snap_restore(AvbdWorld* W, const Snap* s) {
 // Frames for `n` substeps of up to `pcap` pairs, and the adjoint state.
 int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
     if (t->nframes >= n && t->pcap >= pcap) return AVBD_OK;
+    adj_free_graphs(t);  // they copy into the frames
     t->fmem.release();
     t->smem.release();
     t->frames.assign(n, AdjFrame{});
@@ -1024,8 +1035,130 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
 }
 
 // One substep with plain launches, its frame filled on the way.
-int adj_substep(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
+// What the reverse reads of a substep, copied right after its front (the
+// copies cover the frame's capacity, so that a captured graph replays them).
+int adj_copy_front(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
     cudaStream_t st = W->st;
+    const DW& w = W->w;
+    const size_t N = (size_t)w.N, P = std::min<size_t>(t->pcap, W->cand_cap), Q = P * MAX_PTS;
+    D2D(f.pos0, w.pos0, N * 16); D2D(f.rot0, w.rot0, N * 16); D2D(f.inertial, w.inertial, N * 16);
+    D2D(f.inertial_rot, w.inertial_rot, N * 16); D2D(f.vel, w.vel, N * 16); D2D(f.angvel, w.angvel, N * 16);
+    D2D(f.inertia, w.inertia, N * 16); D2D(f.inv_mass, w.inv_mass, N * 4);
+    D2D(f.colour, w.colour, N * 4); D2D(f.col_cnt, w.col_cnt, (MAX_COLOURS + 1) * 4); D2D(f.col_list, w.col_list, N * 4);
+    D2D(f.offA, w.offA, (N + 1) * 4); D2D(f.offB, w.offB, (N + 1) * 4);
+    D2D(f.it_pos, w.pos, N * 16); D2D(f.it_rot, w.rot, N * 16);
+    D2D(f.listB, w.listB, P * 4); D2D(f.posB, w.posB, P * 4);
+    D2D(f.p_ab, w.p_ab, P * 8); D2D(f.p_n, w.p_n, P * 16); D2D(f.p_mu, w.p_mu, P * 8);
+    D2D(f.p_np, w.p_np, P * 4); D2D(f.p_old, w.p_old, P * 4);
+    D2D(f.q_ra, w.q_ra, Q * 16); D2D(f.q_rb, w.q_rb, Q * 16); D2D(f.q_matched, w.q_matched, Q * 4);
+    D2D(f.it_lam, w.q_lam, Q * 16); D2D(f.it_pen, w.q_pen, Q * 16);
+    return AVBD_OK;
+}
+// The iterations and the finish of a substep for `cover` colours, with the
+// split primal's row sums and every iterate copied into the frame.
+int adj_back(AvbdWorld* W, AdjTape* t, AdjFrame& f, int cover) {
+    cudaStream_t st = W->st;
+    const DW& w = W->w;
+    const size_t N = (size_t)w.N, P = std::min<size_t>(t->pcap, W->cand_cap), Q = P * MAX_PTS;
+    launch_solve_prep(w, W->tune, st);
+    D2D(f.side_cnt, w.side_cnt, (2 * MAX_COLOURS + 2) * 4);
+    D2D(f.side_list, w.side_list, P * 2 * 4);
+    for (int it = 0; it < w.iterations; it++) {
+        for (int c = 0; c < cover; c++) launch_primal_colour(w, W->tune, c, (uint32_t)w.N, st);
+        D2D(f.it_contrib + it * f.cstride, w.contrib, P * 2 * 7 * 16);
+        D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
+        D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);
+        launch_dual(w, W->tune, st);
+        D2D(f.it_lam + (it + 1) * f.qstride, w.q_lam, Q * 16);
+        D2D(f.it_pen + (it + 1) * f.qstride, w.q_pen, Q * 16);
+    }
+    launch_finish_substep(w, W->tune, st);
+    D2D(f.asleep_end, w.asleep, N * 4);
+    return AVBD_OK;
+}
+
+uint64_t adj_graph_key(const AvbdWorld* W) { return W->mem_gen; }
+
+void adj_free_graphs(AdjTape* t) {
+    for (auto& g : t->rg)
+        for (auto& e : g)
+            if (e) {
+                cudaGraphExecDestroy(e);
+                e = nullptr;
+            }
+    t->rg.clear();
+}
+
+// One captured recording substep per frame and pair-buffer parity.  The
+// primal is captured for rg_cols colours; a substep that needs more is
+// finished with plain launches.
+int adj_capture(AvbdWorld* W, AdjTape* t) {
+    adj_free_graphs(t);
+    const int base = W->cur;
+    t->rg_cols = std::max(W->graph_cols, std::max(W->last_ncol + 2, 4));
+    t->rg.assign(t->frames.size(), {nullptr, nullptr});
+    for (size_t k = 0; k < t->frames.size(); k++)
+        for (int par = 0; par < 2; par++) {
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(W->st, cudaStreamCaptureModeThreadLocal));
+            W->w.max_cols = t->rg_cols;
+            enqueue_front(W, false);
+            adj_copy_front(W, t, t->frames[k]);
+            adj_back(W, t, t->frames[k], t->rg_cols);
+            W->w.max_cols = MAX_COLOURS;
+            CK(cudaStreamEndCapture(W->st, &g));
+            cudaError_t e = cudaGraphInstantiate(&t->rg[k][W->cur], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                adj_free_graphs(t);
+                W->cur = base;
+                set_pair_ptrs(W);
+                return AVBD_ERR_DEVICE;
+            }
+        }
+    W->cur = base;  // each capture flipped the parity twice per frame
+    set_pair_ptrs(W);
+    t->rg_key = adj_graph_key(W);
+    return AVBD_OK;
+}
+
+// Substep k of the segment being recomputed, its frame filled on the way:
+// by graph replay when the recording graphs match the world, else plainly.
+int adj_substep(AvbdWorld* W, AdjTape* t, int k) {
+    cudaStream_t st = W->st;
+    AdjFrame& f = t->frames[k];
+    if (!t->rg.empty() && t->rg_key == adj_graph_key(W)) {
+        const int next = 1 - W->cur;
+        CK(cudaGraphLaunch(t->rg[k][next], st));
+        W->cur = next;
+        set_pair_ptrs(W);
+        int rc = read_ctr(W);
+        if (rc) return rc;
+        if (!(W->h_ctr[C_ERR] & E_CAND_OVERFLOW)) {
+            const uint32_t P = W->h_ctr[C_PAIRS], ncol = W->h_ctr[C_NCOL];
+            if (P > t->pcap) return AVBD_ERR_CAPACITY;
+            if (W->h_ctr[C_ERR] & E_COLOUR_RANGE) {
+                // the graph's iterations were skipped: finish this substep plainly
+                CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, st));
+                adj_back(W, t, f, (int)ncol);
+                rc = read_ctr(W);
+                if (rc) return rc;
+            }
+            W->last_ncol = (int)ncol;
+            f.npairs = P;
+            f.ncol = ncol;
+            accumulate(W);
+            if (W->h_ctr[C_ERR] & E_COLOUR_OVERFLOW) return AVBD_ERR_CAPACITY;
+            return AVBD_OK;
+        }
+        // candidate overflow: nothing after the broadphase ran; undo the flip
+        // and record this substep plainly after growing
+        W->cur = 1 - W->cur;
+        set_pair_ptrs(W);
+        CK(cudaMemsetAsync(W->w.ctr + C_ERR, 0, 4, st));
+        rc = grow_candidates(W);
+        if (rc) return rc;
+    }
     for (int attempt = 0;; attempt++) {
         if (attempt == 8) return AVBD_ERR_CAPACITY;
         enqueue_front(W, false);
@@ -1039,42 +1172,13 @@ int adj_substep(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
         rc = grow_candidates(W);
         if (rc) return rc;
     }
-    const DW& w = W->w;
     const uint32_t P = W->h_ctr[C_PAIRS], ncol = W->h_ctr[C_NCOL];
     if (P > t->pcap) return AVBD_ERR_CAPACITY;
     W->last_ncol = (int)ncol;
     f.npairs = P;
     f.ncol = ncol;
-    const size_t N = (size_t)w.N, Q = (size_t)P * MAX_PTS;
-    D2D(f.pos0, w.pos0, N * 16); D2D(f.rot0, w.rot0, N * 16); D2D(f.inertial, w.inertial, N * 16);
-    D2D(f.inertial_rot, w.inertial_rot, N * 16); D2D(f.vel, w.vel, N * 16); D2D(f.angvel, w.angvel, N * 16);
-    D2D(f.inertia, w.inertia, N * 16); D2D(f.inv_mass, w.inv_mass, N * 4);
-    D2D(f.colour, w.colour, N * 4); D2D(f.col_cnt, w.col_cnt, (MAX_COLOURS + 1) * 4); D2D(f.col_list, w.col_list, N * 4);
-    D2D(f.offA, w.offA, (N + 1) * 4); D2D(f.offB, w.offB, (N + 1) * 4);
-    D2D(f.it_pos, w.pos, N * 16); D2D(f.it_rot, w.rot, N * 16);
-    if (P) {
-        D2D(f.listB, w.listB, P * 4); D2D(f.posB, w.posB, P * 4);
-        D2D(f.p_ab, w.p_ab, P * 8); D2D(f.p_n, w.p_n, P * 16); D2D(f.p_mu, w.p_mu, P * 8);
-        D2D(f.p_np, w.p_np, P * 4); D2D(f.p_old, w.p_old, P * 4);
-        D2D(f.q_ra, w.q_ra, Q * 16); D2D(f.q_rb, w.q_rb, Q * 16); D2D(f.q_matched, w.q_matched, Q * 4);
-        D2D(f.it_lam, w.q_lam, Q * 16); D2D(f.it_pen, w.q_pen, Q * 16);
-    }
-    launch_solve_prep(w, W->tune, st);
-    D2D(f.side_cnt, w.side_cnt, (2 * MAX_COLOURS + 2) * 4);
-    if (P) D2D(f.side_list, w.side_list, P * 2 * 4);
-    for (int it = 0; it < w.iterations; it++) {
-        for (uint32_t c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, (int)c, (uint32_t)w.N, st);
-        if (P) D2D(f.it_contrib + it * f.cstride, w.contrib, (size_t)P * 2 * 7 * 16);
-        D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
-        D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);
-        launch_dual(w, W->tune, st);
-        if (P) {
-            D2D(f.it_lam + (it + 1) * f.qstride, w.q_lam, Q * 16);
-            D2D(f.it_pen + (it + 1) * f.qstride, w.q_pen, Q * 16);
-        }
-    }
-    launch_finish_substep(w, W->tune, st);
-    D2D(f.asleep_end, w.asleep, N * 4);
+    adj_copy_front(W, t, f);
+    adj_back(W, t, f, (int)ncol);
     CK(cudaGetLastError());
     int rc = read_ctr(W);
     if (rc) return rc;
@@ -1742,6 +1846,7 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
         cudaSetDevice(W->device);
         W->w.contrib = W->mem.get<float4>((size_t)W->cand_cap * 2 * 7);
         if (!W->w.contrib) return AVBD_ERR_DEVICE;
+        W->mem_gen++;
     }
     W->tune.primal_lanes = primal_lanes;
     W->tune.primal_block = primal_block;
@@ -1916,6 +2021,11 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
         rc = avbd_set_tuning(W, 0, W->tune.primal_block);
         if (rc) return rc;
     }
+    if (!W->w.sort_static) {
+        // one pair order for every run: point state crosses checkpoints by index
+        W->w.sort_static = 1;
+        free_graphs(W);
+    }
     adj_free(W->adj);
     AdjTape* t = W->adj = new AdjTape();
     t->steps = steps;
@@ -1959,6 +2069,10 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
     for (const Snap* s : t->ckpt) pmax = std::max(pmax, s->P);
     int rc = adj_storage(W, t, per_seg, pmax + 64);
     if (rc) return rc;
+    if (t->rg.empty() || t->rg_key != adj_graph_key(W)) {
+        rc = adj_capture(W, t);
+        if (rc) return rc;
+    }
     const size_t N = t->N;
     AdjState& A = t->A;
     {
@@ -1989,7 +2103,7 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         rc = snap_restore(W, t->ckpt[seg]);
         const int nsteps = std::min(t->every, t->steps - seg * t->every);
         const int nsub = nsteps * t->substeps;
-        for (int k = 0; k < nsub && !rc; k++) rc = adj_substep(W, t, t->frames[k]);
+        for (int k = 0; k < nsub && !rc; k++) rc = adj_substep(W, t, k);
         CK(cudaEventRecord(ev[1], st));
         for (int k = nsub - 1; k >= 0 && !rc; k--) rc = adj_reverse(W, t, t->frames[k]);
         CK(cudaEventRecord(ev[2], st));

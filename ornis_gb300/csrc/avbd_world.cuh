@@ -114,6 +114,7 @@ struct DW {
     uint32_t cand_cap, pair_cap;
     int max_cols;  // colours the launched iteration covers (a CUDA graph fixes it at capture)
     int n_large_scenes;  // host: scenes above the one-CTA sweep and colouring limit
+    int sort_static;     // also order static bodies' pair segments (differentiable rollouts)
 
     const uint32_t* scene_off;  // S+1
     const uint32_t* scene_of;   // N

@@ -86,6 +86,30 @@ def test_checkpoint_spacing_does_not_change_gradients():
         np.testing.assert_array_equal(x[1], y[1])
 
 
+def test_tower_batch_gradients_are_reproducible():
+    """Colliding towers (the differentiable workload, 16 scenes): repeated
+    backward passes and any checkpoint spacing give the same gradients bit
+    for bit (point state crosses checkpoints by pair index, so the pair order
+    must not depend on the run)."""
+    bodies, offs, ball, tower = scenes.diff_towers(nscenes=16)
+    params, nsub = scenes.params_for("diff_1024")
+    res = []
+    for every in (1, 9, 40):
+        w = AvbdWorld(params, bodies=bodies, scene_offsets=offs)
+        w.set_precision(True)
+        w.adjoint_forward(40, nsub, every)
+        end = w.bodies()
+        g = np.zeros((len(bodies), 13), dtype=np.float32)
+        g[tower, 0:3] = 2.0 * end["position"][tower]
+        a, b = w.adjoint_backward(g), w.adjoint_backward(g)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+        res.append(a)
+    for r in res[1:]:
+        np.testing.assert_array_equal(res[0][0], r[0])
+        np.testing.assert_array_equal(res[0][1], r[1])
+
+
 def test_batch_gradients_equal_scenes_alone():
     parts = [S.tower(seed=1), S.slide(), S.pile(n=10, seed=3), S.roll()]
     arr = np.concatenate(parts)
