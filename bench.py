@@ -362,6 +362,9 @@ def run_ours(args):
     adj = None
     if args.adjoint_scenes > 0 and world == 1 and not joints_all:
         adj = adjoint_rate(args)
+    rag = None
+    if args.ragdoll_adjoint_steps > 0 and world == 1:
+        rag = ragdoll_adjoint_rate(args)
     cb = None
     if args.cpu_per_core > 0 and world == 1 and not joints_all:
         cb = cpu_baseline(bodies_all, offs_all, params, nsub, start=args.start, steps=args.steps,
@@ -389,6 +392,7 @@ def run_ours(args):
         "plain_one_scene": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "adjoint": adj,
+        "adjoint_articulated": rag,
         "phases_ms_per_substep": phases,
         "counters_at_end": {"candidates": c.candidates, "pairs": c.pairs, "points": c.points, "colours": c.colours,
                             "sleeping": c.sleeping, "breakdowns": c.breakdowns, "ccd_hits": c.ccd_hits,
@@ -452,6 +456,73 @@ def adjoint_rate(args):
                    "of the two primal launches (the rollout itself runs the split primal)"}
 
 
+RAGDOLL_STIFFNESS = 2.0e4  # N/m (anchor rows), N m/rad (hinge rows)
+
+
+def ragdoll_adjoint_rate(args):
+    """The articulated batch (8192 ragdolls in scenes of 3000 and 5192) with
+    joints of finite stiffness: recorded forward with checkpoints, then the
+    reverse sweep for d(final centre-of-mass height of each scene)/d(joint
+    stiffness), against the plain graph-replayed forward."""
+    from ornis_gb300.avbd import AvbdWorld
+
+    bodies, offs, joints = scenes.ragdolls()
+    params, nsub = scenes.params_for("ragdoll_8192")
+    steps, every = args.ragdoll_adjoint_steps, 10
+    ndyn = scenes.dynamic_count(bodies)
+    w = AvbdWorld(params, bodies=bodies, scene_offsets=offs)
+    for j in joints:
+        w.add_joint(j)
+    w.set_joint_stiffness(RAGDOLL_STIFFNESS)
+    w.set_precision(True)
+    w.set_events(-1)
+    s0 = w.export_state()
+    fwd = {}
+    for lanes in (1, 0):
+        w.set_tuning(lanes, 128)
+        w.step_graph(nsub * 3)
+        w.import_state(s0)
+        w.sync()
+        t0 = time.perf_counter()
+        dev_ms = w.step_timed(nsub * steps, use_graph=True)
+        fwd[lanes] = (time.perf_counter() - t0, dev_ms)
+        w.import_state(s0)
+    best = min(fwd, key=lambda k: fwd[k][0])
+    fwd_s, fwd_dev_ms = fwd[best]
+    w.sync()
+    t0 = time.perf_counter()
+    w.adjoint_forward(steps, nsub, every)
+    rec_s = time.perf_counter() - t0
+    end = w.bodies()
+    dyn = end["inv_mass"] > 0
+    mass = np.where(dyn, 1.0 / np.where(dyn, end["inv_mass"], 1.0), 0.0)
+    g = np.zeros((len(bodies), 13), dtype=np.float32)
+    com = []
+    for s in range(len(offs) - 1):
+        a, b = offs[s], offs[s + 1]
+        m = mass[a:b]
+        g[a:b, 1] = m / m.sum()
+        com.append(float(np.sum(m * end["position"][a:b, 1]) / m.sum()))
+    t0 = time.perf_counter()
+    w.adjoint_backward(g)
+    bwd_s = time.perf_counter() - t0
+    gk = w.adjoint_grad_joint_stiffness()
+    rec_ms, rev_ms = w.adjoint_timing()
+    w.close()
+    return {"workload": "ragdoll_8192", "scenes": int(len(offs) - 1), "dynamic_bodies": ndyn, "joints": len(joints),
+            "joint_stiffness": RAGDOLL_STIFFNESS, "steps": steps, "checkpoint_every": every, "dt": 1 / 120,
+            "substeps": nsub, "iterations": params.iterations, "precision": "fast",
+            "forward_ms_per_step": 1e3 * fwd_s / steps, "forward_device_ms_per_step": fwd_dev_ms / steps,
+            "forward_ms_per_step_by_primal": {"thread": 1e3 * fwd[1][0] / steps, "split": 1e3 * fwd[0][0] / steps},
+            "record_ms_per_step": 1e3 * rec_s / steps, "backward_ms_per_step": 1e3 * bwd_s / steps,
+            "adjoint_steps_per_s": steps / bwd_s, "adjoint_body_steps_per_s": ndyn * steps / bwd_s,
+            "backward_over_forward": bwd_s / fwd_s,
+            "backward_split_ms_per_step": {"recompute": rec_ms / steps, "reverse": rev_ms / steps},
+            "com_height": com, "grad_com_height_wrt_stiffness": [float(x) for x in gk],
+            "how": "as the differentiable batch: wall time with the host waiting; loss per scene = final "
+                   "centre-of-mass height of its dynamic bodies"}
+
+
 def plain_rate(bodies, offs, params, nsub, args):
     """Body-steps/s stepping sampled scenes one world (one launch sequence) at a time."""
     from ornis_gb300.avbd import AvbdWorld
@@ -496,14 +567,21 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--adjoint-scenes", type=int, default=1024, help="differentiable batch size (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=120)
+    ap.add_argument("--ragdoll-adjoint-steps", type=int, default=240,
+                    help="steps of the articulated forward+adjoint measurement (0: skip)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="print only the differentiable-batch measurement (for profiling)")
+    ap.add_argument("--ragdoll-adjoint-only", action="store_true",
+                    help="print only the articulated forward+adjoint measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     if args.adjoint_only:
         print(json.dumps(adjoint_rate(args)))
+        return 0
+    if args.ragdoll_adjoint_only:
+        print(json.dumps(ragdoll_adjoint_rate(args)))
         return 0
     return run_ours(args)
 

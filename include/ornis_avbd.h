@@ -381,6 +381,14 @@ int avbd_world_drain_trigger_events(AvbdWorld* world, AvbdTriggerEvent* out, uin
  * dropped because the queue was full, trigger events dropped (cumulative). */
 int avbd_world_event_counts(AvbdWorld* world, uint32_t* counts);
 
+/* Finite joint stiffness k (N/m for the anchor rows, N m/rad for the hinge
+ * alignment rows; 0, the default, keeps the reference's hard joints,
+ * mod.rs:176-181).  With k > 0 those rows are springs of stiffness k
+ * (penalty k, lambda zero: the AVBD treatment of a finite-stiffness
+ * constraint); the hinge limit row stays hard.  No counterpart in the reference: the
+ * articulated workload's gradient is taken with respect to k. */
+int avbd_set_joint_stiffness(AvbdWorld* world, float k);
+
 /* ---- allocation-free stepping (no counterpart in the reference) ----------- */
 
 #define AVBD_STATIC_MAX_BODIES 128u      /* bodies per call */
@@ -412,8 +420,7 @@ int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uin
 /* Advance the world `steps` steps of `substeps` fixed substeps (as
  * avbd_world_step_graph) and keep a device checkpoint of the full step
  * state every `checkpoint_every` steps, for avbd_adjoint_backward.  Worlds
- * with joints or with rolling / torsion friction return
- * AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
+ * with rolling / torsion friction return AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
  * (avbd_set_tuning lanes 0) and orders every body's contact pairs (the
  * static bodies' too), which the world keeps afterwards; retuning the
  * world before the backward invalidates the recording.  A new forward
@@ -433,6 +440,12 @@ int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int3
  * recomputed from its checkpoint.  The world is left at the end of the
  * recorded rollout. */
 int avbd_adjoint_backward(AvbdWorld* world, const float* grad_final, float* grad_initial, float* grad_friction);
+
+/* dLoss/d(joint stiffness) of the last avbd_adjoint_backward, one float per
+ * scene (the contributions of the scene's joints; their sum is the gradient
+ * for the world's one stiffness, avbd_set_joint_stiffness).  Zero for hard
+ * joints (stiffness 0). */
+int avbd_adjoint_grad_joint_stiffness(AvbdWorld* world, float* per_scene);
 
 /* Device time of the last avbd_adjoint_backward: ms[0] the segment
  * recomputes (restores included), ms[1] the reverse sweeps. */

@@ -19,64 +19,69 @@ namespace orc {
 
 constexpr int DUAL_DIRS = 8;
 
-struct Dual {
-    double v = 0.0;
+// V: the value type.  DualT<double> differentiates the f64 step; DualT<float>
+// keeps f32 values computed in the f32 engine's operation order (so its
+// trajectory is the f32 one bit for bit) with f64 tangents.
+template <class V> struct DualT {
+    V v = V(0);
     double d[DUAL_DIRS] = {};
 
-    Dual() = default;
+    DualT() = default;
     template <class A, class = std::enable_if_t<std::is_arithmetic<A>::value>>
-    Dual(A a) : v(double(a)) {}
+    DualT(A a) : v(V(a)) {}
 
-    explicit operator double() const { return v; }
+    explicit operator double() const { return double(v); }
     explicit operator float() const { return float(v); }
 
-    Dual& operator+=(const Dual& o) { return *this = *this + o; }
-    Dual& operator-=(const Dual& o) { return *this = *this - o; }
-    Dual& operator*=(const Dual& o) { return *this = *this * o; }
-    Dual& operator/=(const Dual& o) { return *this = *this / o; }
+    DualT& operator+=(const DualT& o) { return *this = *this + o; }
+    DualT& operator-=(const DualT& o) { return *this = *this - o; }
+    DualT& operator*=(const DualT& o) { return *this = *this * o; }
+    DualT& operator/=(const DualT& o) { return *this = *this / o; }
 
-    friend Dual operator+(const Dual& a, const Dual& b) {
-        Dual r;
+    friend DualT operator+(const DualT& a, const DualT& b) {
+        DualT r;
         r.v = a.v + b.v;
         for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = a.d[i] + b.d[i];
         return r;
     }
-    friend Dual operator-(const Dual& a, const Dual& b) {
-        Dual r;
+    friend DualT operator-(const DualT& a, const DualT& b) {
+        DualT r;
         r.v = a.v - b.v;
         for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = a.d[i] - b.d[i];
         return r;
     }
-    friend Dual operator-(const Dual& a) {
-        Dual r;
+    friend DualT operator-(const DualT& a) {
+        DualT r;
         r.v = -a.v;
         for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = -a.d[i];
         return r;
     }
-    friend Dual operator*(const Dual& a, const Dual& b) {
-        Dual r;
+    friend DualT operator*(const DualT& a, const DualT& b) {
+        DualT r;
         r.v = a.v * b.v;
-        for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+        for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = a.d[i] * double(b.v) + double(a.v) * b.d[i];
         return r;
     }
-    friend Dual operator/(const Dual& a, const Dual& b) {
-        Dual r;
+    friend DualT operator/(const DualT& a, const DualT& b) {
+        DualT r;
         r.v = a.v / b.v;
-        double ib = 1.0 / b.v;
-        for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+        double ib = 1.0 / double(b.v), q = double(a.v) * ib;
+        for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = (a.d[i] - q * b.d[i]) * ib;
         return r;
     }
-    friend bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
-    friend bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
-    friend bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
-    friend bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
-    friend bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
-    friend bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
+    friend bool operator<(const DualT& a, const DualT& b) { return a.v < b.v; }
+    friend bool operator<=(const DualT& a, const DualT& b) { return a.v <= b.v; }
+    friend bool operator>(const DualT& a, const DualT& b) { return a.v > b.v; }
+    friend bool operator>=(const DualT& a, const DualT& b) { return a.v >= b.v; }
+    friend bool operator==(const DualT& a, const DualT& b) { return a.v == b.v; }
+    friend bool operator!=(const DualT& a, const DualT& b) { return a.v != b.v; }
 };
+using Dual = DualT<double>;
+using DualF = DualT<float>;
 
 // f(a) with f' given: the chain rule on every direction
-inline Dual dual_apply(const Dual& a, double fv, double dfv) {
-    Dual r;
+template <class V> inline DualT<V> dual_apply(const DualT<V>& a, V fv, double dfv) {
+    DualT<V> r;
     r.v = fv;
     for (int i = 0; i < DUAL_DIRS; i++) r.d[i] = dfv * a.d[i];
     return r;
@@ -85,61 +90,73 @@ inline Dual dual_apply(const Dual& a, double fv, double dfv) {
 // The value with the tangents dropped (a quantity held fixed by the
 // derivative), and a value carrying another expression's tangents.
 template <class T> inline T no_tangent(const T& x) { return x; }
-inline Dual no_tangent(const Dual& x) { return Dual(x.v); }
+template <class V> inline DualT<V> no_tangent(const DualT<V>& x) { return DualT<V>(x.v); }
 template <class T> inline T value_with_tangent(const T& value, const T&) { return value; }
-inline Dual value_with_tangent(const Dual& value, const Dual& tangent_of) {
-    Dual r = tangent_of;
+template <class V> inline DualT<V> value_with_tangent(const DualT<V>& value, const DualT<V>& tangent_of) {
+    DualT<V> r = tangent_of;
     r.v = value.v;
     return r;
 }
 template <class T> struct is_dual : std::false_type {};
-template <> struct is_dual<Dual> : std::true_type {};
+template <class V> struct is_dual<DualT<V>> : std::true_type {};
 
 }  // namespace orc
 
 namespace std {
-inline orc::Dual sqrt(const orc::Dual& a) {
-    double s = std::sqrt(a.v);
-    return orc::dual_apply(a, s, s > 0.0 ? 0.5 / s : 0.0);
+template <class V> inline orc::DualT<V> sqrt(const orc::DualT<V>& a) {
+    V s = std::sqrt(a.v);
+    return orc::dual_apply(a, s, s > V(0) ? 0.5 / double(s) : 0.0);
 }
-inline orc::Dual fabs(const orc::Dual& a) { return orc::dual_apply(a, std::fabs(a.v), a.v < 0.0 ? -1.0 : 1.0); }
-inline orc::Dual abs(const orc::Dual& a) { return fabs(a); }
-inline orc::Dual fmin(const orc::Dual& a, const orc::Dual& b) { return (b.v < a.v || std::isnan(a.v)) ? b : a; }
-inline orc::Dual fmax(const orc::Dual& a, const orc::Dual& b) { return (b.v > a.v || std::isnan(a.v)) ? b : a; }
-inline orc::Dual copysign(const orc::Dual& a, const orc::Dual& b) {
+template <class V> inline orc::DualT<V> fabs(const orc::DualT<V>& a) {
+    return orc::dual_apply(a, std::fabs(a.v), a.v < V(0) ? -1.0 : 1.0);
+}
+template <class V> inline orc::DualT<V> abs(const orc::DualT<V>& a) { return fabs(a); }
+template <class V> inline orc::DualT<V> fmin(const orc::DualT<V>& a, const orc::DualT<V>& b) {
+    return (b.v < a.v || std::isnan(a.v)) ? b : a;
+}
+template <class V> inline orc::DualT<V> fmax(const orc::DualT<V>& a, const orc::DualT<V>& b) {
+    return (b.v > a.v || std::isnan(a.v)) ? b : a;
+}
+template <class V> inline orc::DualT<V> copysign(const orc::DualT<V>& a, const orc::DualT<V>& b) {
     bool flip = std::signbit(a.v) != std::signbit(b.v);
     return flip ? -a : a;
 }
-inline orc::Dual fmod(const orc::Dual& x, const orc::Dual& m) {
-    double q = std::trunc(x.v / m.v);
-    orc::Dual r = x - orc::Dual(q) * m;
+template <class V> inline orc::DualT<V> fmod(const orc::DualT<V>& x, const orc::DualT<V>& m) {
+    double q = std::trunc(double(x.v) / double(m.v));
+    orc::DualT<V> r;
     r.v = std::fmod(x.v, m.v);
+    for (int i = 0; i < orc::DUAL_DIRS; i++) r.d[i] = x.d[i] - q * m.d[i];
     return r;
 }
-inline orc::Dual sin(const orc::Dual& a) { return orc::dual_apply(a, std::sin(a.v), std::cos(a.v)); }
-inline orc::Dual cos(const orc::Dual& a) { return orc::dual_apply(a, std::cos(a.v), -std::sin(a.v)); }
-inline orc::Dual asin(const orc::Dual& a) {
-    double c = 1.0 - a.v * a.v;
+template <class V> inline orc::DualT<V> sin(const orc::DualT<V>& a) {
+    return orc::dual_apply(a, std::sin(a.v), std::cos(double(a.v)));
+}
+template <class V> inline orc::DualT<V> cos(const orc::DualT<V>& a) {
+    return orc::dual_apply(a, std::cos(a.v), -std::sin(double(a.v)));
+}
+template <class V> inline orc::DualT<V> asin(const orc::DualT<V>& a) {
+    double c = 1.0 - double(a.v) * double(a.v);
     return orc::dual_apply(a, std::asin(a.v), c > 0.0 ? 1.0 / std::sqrt(c) : 0.0);
 }
-inline orc::Dual atan2(const orc::Dual& y, const orc::Dual& x) {
-    orc::Dual r;
+template <class V> inline orc::DualT<V> atan2(const orc::DualT<V>& y, const orc::DualT<V>& x) {
+    orc::DualT<V> r;
     r.v = std::atan2(y.v, x.v);
-    double r2 = x.v * x.v + y.v * y.v;
+    double xv = double(x.v), yv = double(y.v);
+    double r2 = xv * xv + yv * yv;
     double k = r2 > 0.0 ? 1.0 / r2 : 0.0;
-    for (int i = 0; i < orc::DUAL_DIRS; i++) r.d[i] = (x.v * y.d[i] - y.v * x.d[i]) * k;
+    for (int i = 0; i < orc::DUAL_DIRS; i++) r.d[i] = (xv * y.d[i] - yv * x.d[i]) * k;
     return r;
 }
-inline bool isfinite(const orc::Dual& a) { return std::isfinite(a.v); }
-inline bool isnan(const orc::Dual& a) { return std::isnan(a.v); }
-inline bool signbit(const orc::Dual& a) { return std::signbit(a.v); }
+template <class V> inline bool isfinite(const orc::DualT<V>& a) { return std::isfinite(a.v); }
+template <class V> inline bool isnan(const orc::DualT<V>& a) { return std::isnan(a.v); }
+template <class V> inline bool signbit(const orc::DualT<V>& a) { return std::signbit(a.v); }
 
-template <> class numeric_limits<orc::Dual> {
+template <class V> class numeric_limits<orc::DualT<V>> {
 public:
     static constexpr bool is_specialized = true;
-    static orc::Dual infinity() { return orc::Dual(std::numeric_limits<double>::infinity()); }
-    static orc::Dual max() { return orc::Dual(std::numeric_limits<double>::max()); }
-    static orc::Dual lowest() { return orc::Dual(std::numeric_limits<double>::lowest()); }
-    static orc::Dual epsilon() { return orc::Dual(std::numeric_limits<double>::epsilon()); }
+    static orc::DualT<V> infinity() { return orc::DualT<V>(std::numeric_limits<V>::infinity()); }
+    static orc::DualT<V> max() { return orc::DualT<V>(std::numeric_limits<V>::max()); }
+    static orc::DualT<V> lowest() { return orc::DualT<V>(std::numeric_limits<V>::lowest()); }
+    static orc::DualT<V> epsilon() { return orc::DualT<V>(std::numeric_limits<V>::epsilon()); }
 };
 }  // namespace std

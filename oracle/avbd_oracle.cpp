@@ -560,6 +560,7 @@ template <class T> struct Point {
     bool stuck;
     T roll_lam[3];
     int32_t matched;
+    bool kept;  // anchors kept from a stuck point of the previous substep
 };
 template <class T> struct Pair {
     uint32_t a, b;
@@ -767,12 +768,18 @@ template <class T> struct Engine {
     int mode = REFERENCE;
     int threads = 1;
     bool faithful_scan = false;  // true: solve_body scans every pair/joint (the reference's O(P) scan)
+    // true: a pair's rows are summed on their own before they join the body's
+    // system (the device's split primal, whose rounding this reproduces)
+    bool split_sums = false;
     // Dual numbers only: hold each step's contact frames (normal, gap, local
     // anchors) fixed in the derivative, the device adjoint's convention; the
     // step-start gap keeps the derivative of n.(witness_a - witness_b) with
     // the witnesses carried by the bodies.
     bool freeze_frames = false;
     int freeze_bits = 7;
+    // Finite joint stiffness (0: the reference's hard joints).  A soft joint
+    // row is a spring of that stiffness: penalty = stiffness, lambda = 0.
+    T joint_k = T(0);
     V3<T> gravity;
     T dt;
     std::vector<Body<T>> bodies;
@@ -1094,7 +1101,7 @@ template <class T> struct Engine {
                 Point<T> p{};
                 if (m >= 0) {
                     const Point<T>& o = old.points[m];
-                    if (o.stuck && touching && !smooth) { p.ra = o.ra; p.rb = o.rb; }
+                    if (o.stuck && touching && !smooth) { p.ra = o.ra; p.rb = o.rb; p.kept = true; }
                     else { p.ra = f.first; p.rb = f.second; }
                     for (int k = 0; k < 3; k++) { p.lam[k] = o.lam[k]; p.pen[k] = o.pen[k]; p.roll_lam[k] = o.roll_lam[k]; }
                     p.stuck = o.stuck;
@@ -1178,6 +1185,24 @@ template <class T> struct Engine {
                     pt.ra = {no_tangent(pt.ra.x), no_tangent(pt.ra.y), no_tangent(pt.ra.z)};
                     pt.rb = {no_tangent(pt.rb.x), no_tangent(pt.rb.y), no_tangent(pt.rb.z)};
                 }
+                if (freeze_bits & 4)
+                    for (auto& pt : p.points) {
+                        if (pt.kept) continue;
+                        // a capsule's witness anchor rolls with the body: segment
+                        // point + s R0^T n (s = -r on side A, +r on side B)
+                        const Body<T>& A = bodies[p.a];
+                        const Body<T>& B = bodies[p.b];
+                        if (B.shape == AVBD_SHAPE_CAPSULE && A.shape != AVBD_SHAPE_BOX) {
+                            V3<T> t = qrot(conj(B.rot), p.n) * B.sp.x;
+                            pt.rb = {value_with_tangent(pt.rb.x, t.x), value_with_tangent(pt.rb.y, t.y),
+                                     value_with_tangent(pt.rb.z, t.z)};
+                        }
+                        if (A.shape == AVBD_SHAPE_CAPSULE && B.shape != AVBD_SHAPE_BOX) {
+                            V3<T> t = qrot(conj(A.rot), p.n) * (-A.sp.x);
+                            pt.ra = {value_with_tangent(pt.ra.x, t.x), value_with_tangent(pt.ra.y, t.y),
+                                     value_with_tangent(pt.ra.z, t.z)};
+                        }
+                    }
             }
     }
 
@@ -1386,6 +1411,17 @@ template <class T> struct Engine {
                 if (pairs[pi].a == h || pairs[pi].b == h) stamp_contacts_for(h, pi, lhs, rhs);
             for (const Joint<T>& j : joints)
                 if (j.a == h || j.b == h) stamp_joint_for(h, j, lhs, rhs);
+        } else if (split_sums) {
+            for (uint32_t pi : adj_pairs[h]) {
+                T lp[6][6] = {};
+                T rp[6] = {};
+                stamp_contacts_for(h, pi, lp, rp);
+                for (int i = 0; i < 6; i++) {
+                    for (int k = 0; k < 6; k++) lhs[i][k] += lp[i][k];
+                    rhs[i] += rp[i];
+                }
+            }
+            for (uint32_t ji : adj_joints[h]) stamp_joint_for(h, joints[ji], lhs, rhs);
         } else {
             for (uint32_t pi : adj_pairs[h]) stamp_contacts_for(h, pi, lhs, rhs);
             for (uint32_t ji : adj_joints[h]) stamp_joint_for(h, joints[ji], lhs, rhs);
@@ -1469,9 +1505,13 @@ template <class T> struct Engine {
             V3<T> live = pa - pb, c0v = pa0 - pb0;
             for (int k = 0; k < 3; k++) {
                 T c = live[k] - C<T>(K::ALPHA) * c0v[k];
-                if (std::fabs(c) >= C<T>(K::C_EPS)) {
-                    j.lam_l[k] += j.pen_l[k] * c;
-                    j.pen_l[k] = fmn(j.pen_l[k] + C<T>(K::BETA) * std::fabs(c), C<T>(K::PENALTY_MAX));
+                if (joint_k > T(0)) {
+                    j.pen_l[k] = joint_k;
+                } else if (std::fabs(c) >= C<T>(K::C_EPS)) {
+                    {
+                        j.lam_l[k] += j.pen_l[k] * c;
+                        j.pen_l[k] = fmn(j.pen_l[k] + C<T>(K::BETA) * std::fabs(c), C<T>(K::PENALTY_MAX));
+                    }
                 }
             }
             if (j.kind == AVBD_JOINT_REVOLUTE) {
@@ -1482,6 +1522,10 @@ template <class T> struct Engine {
                 V3<T> ts[2] = {t1, t2};
                 for (int li = 0; li < 2; li++) {
                     T c = dot(ts[li], axa - axb) - C<T>(K::ALPHA) * dot(ts[li], axa0 - axb0);
+                    if (joint_k > T(0)) {
+                        j.pen_a[li] = joint_k;
+                        continue;
+                    }
                     if (std::fabs(c) < C<T>(K::C_EPS)) continue;
                     j.lam_a[li] = j.pen_a[li] * c + j.lam_a[li];
                     j.pen_a[li] = fmn(j.pen_a[li] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::PENALTY_MAX));
@@ -1614,6 +1658,10 @@ template <class T> struct Engine {
             T l2 = fmx(L, C<T>(K::MIN_TOI_DISP_LENGTH));
             T frac = fclamp(best_t / l2, T(0), T(1));
             T e = fmn(bodies[h].restitution, bodies[best_h].restitution);
+            if (freeze_frames) {  // the time of impact and its normal held fixed, as a contact frame
+                frac = no_tangent(frac);
+                best_n = {no_tangent(best_n.x), no_tangent(best_n.y), no_tangent(best_n.z)};
+            }
             Body<T>& b = bodies[h];
             b.pos = b.pos + disp * frac;
             T vn = dot(b.vel, best_n);
@@ -1743,6 +1791,10 @@ template <class T> struct Engine {
                 j.lam_a[k] *= ag;
                 j.pen_l[k] = fclamp(j.pen_l[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
                 j.pen_a[k] = fclamp(j.pen_a[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
+                if (joint_k > T(0)) {  // soft rows: anchors and hinge alignment (not the limit)
+                    j.pen_l[k] = joint_k;
+                    if (k < 2) j.pen_a[k] = joint_k;
+                }
             }
         for (uint32_t h = 0; h < n; h++) {
             if (!solvable(h) || asleep[h]) continue;
@@ -1964,25 +2016,34 @@ template <class T> struct Oracle : OracleBase {
 using namespace orc;
 
 struct OracleWorld {
-    int dbl;  // 0 f32, 1 f64, 2 f64 dual numbers
+    int dbl;  // 0 f32, 1 f64, 2 f64 dual numbers, 3 dual numbers with f32 values
     Engine<float>* f;
     Engine<double>* d;
     Engine<Dual>* g;
+    Engine<DualF>* gf;
 };
 
-#define DISPATCH(w, ...)                                      \
-    do {                                                      \
-        if ((w)->dbl == 2) { auto& E = *(w)->g; __VA_ARGS__; } \
+#define DISPATCH(w, ...)                                       \
+    do {                                                       \
+        if ((w)->dbl == 3) { auto& E = *(w)->gf; __VA_ARGS__; } \
+        else if ((w)->dbl == 2) { auto& E = *(w)->g; __VA_ARGS__; } \
         else if ((w)->dbl) { auto& E = *(w)->d; __VA_ARGS__; } \
-        else { auto& E = *(w)->f; __VA_ARGS__; }               \
+        else { auto& E = *(w)->f; __VA_ARGS__; }                \
+    } while (0)
+// the dual-number engines only
+#define DISPATCH_DUAL(w, ...)                                  \
+    do {                                                       \
+        if ((w)->dbl == 3) { auto& E = *(w)->gf; __VA_ARGS__; } \
+        else { auto& E = *(w)->g; __VA_ARGS__; }                \
     } while (0)
 
 extern "C" {
 
 // mode: 0 = Reference, 1 = Coloured.  use_double: 0 = f32, 1 = f64, 2 = f64
-// dual numbers (forward-mode derivatives).
+// dual numbers (forward-mode derivatives), 3 = dual numbers whose values are
+// the f32 engine's (its trajectory bit for bit) with f64 tangents.
 OracleWorld* oracle_world_create(const AvbdParams* p, int mode, int use_double, int threads) {
-    OracleWorld* w = new OracleWorld{use_double, nullptr, nullptr, nullptr};
+    OracleWorld* w = new OracleWorld{use_double, nullptr, nullptr, nullptr, nullptr};
     auto init = [&](auto& E) {
         using TT = std::remove_reference_t<decltype(E.dt)>;
         E.prm = *p;
@@ -1991,7 +2052,8 @@ OracleWorld* oracle_world_create(const AvbdParams* p, int mode, int use_double, 
         E.gravity = {TT(p->gravity[0]), TT(p->gravity[1]), TT(p->gravity[2])};
         E.dt = TT(p->step_dt);
     };
-    if (use_double == 2) { w->g = new Engine<Dual>(); init(*w->g); }
+    if (use_double == 3) { w->gf = new Engine<DualF>(); init(*w->gf); }
+    else if (use_double == 2) { w->g = new Engine<Dual>(); init(*w->g); }
     else if (use_double) { w->d = new Engine<double>(); init(*w->d); }
     else { w->f = new Engine<float>(); init(*w->f); }
     return w;
@@ -2001,9 +2063,11 @@ void oracle_world_destroy(OracleWorld* w) {
     delete w->f;
     delete w->d;
     delete w->g;
+    delete w->gf;
     delete w;
 }
 void oracle_set_faithful_scan(OracleWorld* w, int on) { DISPATCH(w, E.faithful_scan = on != 0); }
+void oracle_set_split_sums(OracleWorld* w, int on) { DISPATCH(w, E.split_sums = on != 0); }
 int oracle_add_bodies(OracleWorld* w, const AvbdBody* b, uint32_t n) {
     DISPATCH(w, {
         using TT = std::remove_reference_t<decltype(E.dt)>;
@@ -2112,45 +2176,72 @@ int oracle_get_state13(OracleWorld* w, double* out) {
     });
     return AVBD_OK;
 }
-// ---- dual-number worlds (use_double = 2): forward-mode derivatives ----------
+// ---- dual-number worlds (use_double = 2 or 3): forward-mode derivatives -------
+static bool is_dual_world(const OracleWorld* w) { return w && (w->dbl == 2 || w->dbl == 3); }
 int oracle_dual_dirs() { return DUAL_DIRS; }
 // Seed d(field[comp] of body)/d(direction dir) = value.  field: 0 position,
 // 1 rotation (x, y, z, w), 2 velocity, 3 angular velocity, 4 friction (both
 // friction coefficients; comp ignored).
 int oracle_dual_seed(OracleWorld* w, uint32_t body, int field, int comp, int dir, double value) {
-    if (!w || w->dbl != 2 || dir < 0 || dir >= DUAL_DIRS || body >= w->g->bodies.size()) return AVBD_ERR_INVALID_ARG;
-    auto& b = w->g->bodies[body];
-    Dual* f = nullptr;
-    switch (field) {
-        case 0: f = comp == 0 ? &b.pos.x : comp == 1 ? &b.pos.y : &b.pos.z; break;
-        case 1: f = comp == 0 ? &b.rot.x : comp == 1 ? &b.rot.y : comp == 2 ? &b.rot.z : &b.rot.w; break;
-        case 2: f = comp == 0 ? &b.vel.x : comp == 1 ? &b.vel.y : &b.vel.z; break;
-        case 3: f = comp == 0 ? &b.angvel.x : comp == 1 ? &b.angvel.y : &b.angvel.z; break;
-        case 4:
-            b.friction.d[dir] = value;
-            b.friction_t.d[dir] = value;
-            return AVBD_OK;
-        default: return AVBD_ERR_INVALID_ARG;
-    }
-    f->d[dir] = value;
+    if (!is_dual_world(w) || dir < 0 || dir >= DUAL_DIRS) return AVBD_ERR_INVALID_ARG;
+    int rc = AVBD_OK;
+    DISPATCH_DUAL(w, {
+        if (body >= E.bodies.size()) {
+            rc = AVBD_ERR_INVALID_ARG;
+        } else {
+            auto& b = E.bodies[body];
+            double* f = nullptr;
+            switch (field) {
+                case 0: f = comp == 0 ? b.pos.x.d : comp == 1 ? b.pos.y.d : b.pos.z.d; break;
+                case 1: f = comp == 0 ? b.rot.x.d : comp == 1 ? b.rot.y.d : comp == 2 ? b.rot.z.d : b.rot.w.d; break;
+                case 2: f = comp == 0 ? b.vel.x.d : comp == 1 ? b.vel.y.d : b.vel.z.d; break;
+                case 3: f = comp == 0 ? b.angvel.x.d : comp == 1 ? b.angvel.y.d : b.angvel.z.d; break;
+                case 4:
+                    b.friction.d[dir] = value;
+                    b.friction_t.d[dir] = value;
+                    break;
+                default: rc = AVBD_ERR_INVALID_ARG;
+            }
+            if (f) f[dir] = value;
+        }
+    });
+    return rc;
+}
+// Finite joint stiffness (0: hard joints, the reference's).
+int oracle_set_joint_stiffness(OracleWorld* w, float k) {
+    if (!w || !(k >= 0.0f)) return AVBD_ERR_INVALID_ARG;
+    DISPATCH(w, {
+        using TT = std::remove_reference_t<decltype(E.dt)>;
+        E.joint_k = TT(k);
+    });
+    return AVBD_OK;
+}
+// d(joint stiffness)/d(direction dir) = value (dual worlds).
+int oracle_dual_seed_joint_stiffness(OracleWorld* w, int dir, double value) {
+    if (!is_dual_world(w) || dir < 0 || dir >= DUAL_DIRS) return AVBD_ERR_INVALID_ARG;
+    DISPATCH_DUAL(w, E.joint_k.d[dir] = value);
     return AVBD_OK;
 }
 int oracle_dual_freeze_frames(OracleWorld* w, int on) {
-    if (!w || w->dbl != 2) return AVBD_ERR_INVALID_ARG;
-    w->g->freeze_frames = on != 0;
-    w->g->freeze_bits = on;
+    if (!is_dual_world(w)) return AVBD_ERR_INVALID_ARG;
+    DISPATCH_DUAL(w, {
+        E.freeze_frames = on != 0;
+        E.freeze_bits = on;
+    });
     return AVBD_OK;
 }
 // Tangents of the 13 state numbers of every body: out[(13 * body + k) * DUAL_DIRS + dir].
 int oracle_dual_tangents(OracleWorld* w, double* out) {
-    if (!w || w->dbl != 2) return AVBD_ERR_INVALID_ARG;
-    for (size_t i = 0; i < w->g->bodies.size(); i++) {
-        auto& b = w->g->bodies[i];
-        const Dual* v[13] = {&b.pos.x, &b.pos.y, &b.pos.z, &b.rot.x, &b.rot.y, &b.rot.z, &b.rot.w,
-                             &b.vel.x, &b.vel.y, &b.vel.z, &b.angvel.x, &b.angvel.y, &b.angvel.z};
-        for (int k = 0; k < 13; k++)
-            for (int d = 0; d < DUAL_DIRS; d++) out[(13 * i + k) * DUAL_DIRS + d] = v[k]->d[d];
-    }
+    if (!is_dual_world(w)) return AVBD_ERR_INVALID_ARG;
+    DISPATCH_DUAL(w, {
+        for (size_t i = 0; i < E.bodies.size(); i++) {
+            auto& b = E.bodies[i];
+            const double* v[13] = {b.pos.x.d, b.pos.y.d, b.pos.z.d, b.rot.x.d, b.rot.y.d, b.rot.z.d, b.rot.w.d,
+                                   b.vel.x.d, b.vel.y.d, b.vel.z.d, b.angvel.x.d, b.angvel.y.d, b.angvel.z.d};
+            for (int k = 0; k < 13; k++)
+                for (int d = 0; d < DUAL_DIRS; d++) out[(13 * i + k) * DUAL_DIRS + d] = v[k][d];
+        }
+    });
     return AVBD_OK;
 }
 int oracle_set_bodies(OracleWorld* w, const AvbdBody* in, uint32_t n) {

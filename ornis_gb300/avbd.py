@@ -78,6 +78,8 @@ def lib():
             "avbd_adjoint_forward": [vp, C.c_int32, C.c_int32, C.c_int32],
             "avbd_adjoint_backward": [vp, vp, vp, vp],
             "avbd_adjoint_timing": [vp, vp],
+            "avbd_set_joint_stiffness": [vp, C.c_float],
+            "avbd_adjoint_grad_joint_stiffness": [vp, vp],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -244,6 +246,10 @@ class AvbdWorld:
     def set_occupancy(self, min_blocks):
         _check(lib().avbd_set_occupancy(self.h, int(min_blocks)), "set_occupancy")
 
+    def set_joint_stiffness(self, k):
+        """Finite joint stiffness (0: hard joints, the reference's)."""
+        _check(lib().avbd_set_joint_stiffness(self.h, float(k)), "set_joint_stiffness")
+
     def set_broadphase(self, small_scene_max):
         _check(lib().avbd_set_broadphase(self.h, int(small_scene_max)), "set_broadphase")
 
@@ -332,6 +338,14 @@ class AvbdWorld:
         _check(lib().avbd_adjoint_backward(self.h, abi.ptr(g), abi.ptr(out), abi.ptr(mu)), "adjoint_backward")
         return out, mu
 
+
+    def adjoint_grad_joint_stiffness(self):
+        """dLoss/d(joint stiffness) per scene from the last adjoint_backward."""
+        ns = C.c_uint32()
+        _check(lib().avbd_world_scene_count(self.h, C.byref(ns)), "scene_count")
+        out = np.zeros(ns.value, dtype=np.float32)
+        _check(lib().avbd_adjoint_grad_joint_stiffness(self.h, abi.ptr(out)), "adjoint_grad_joint_stiffness")
+        return out
 
     def adjoint_timing(self):
         """(recompute ms, reverse ms) of the last adjoint_backward, device time."""

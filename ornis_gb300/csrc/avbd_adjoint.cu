@@ -13,11 +13,12 @@
 // Order of one substep's reverse:
 //   k_adj_bdf          BDF1 velocities and the quaternion renormalisation
 //   per iteration, last first:
-//     k_adj_dual       the dual update of every point (4 lanes per pair)
+//     k_adj_dual       the dual update of every point (4 lanes per pair);
+//                      k_adj_dual_joints that of every joint
 //     per colour, last first:
 //       k_adj_solve    each body's block solve (thread per body)
 //       k_adj_sides    its contact rows (4 lanes per pair side)
-//   k_adj_c0           C0 and the warmstart decay
+//   k_adj_c0           C0 and the warmstart decay (k_adj_decay_joints: joints')
 //   k_adj_start        the inertial targets -> previous substep's state
 //   k_adj_inherit      point adjoints -> the previous generation's points
 //   k_adj_mu_scene     friction adjoint summed per scene
@@ -58,8 +59,11 @@ static __device__ __forceinline__ void adj_ctx(const DW& w, const AdjFrame& f, u
     c.dxb = c.pb - ld3(f.pos0[c.b]);
     c.dra = quat_diff_vec(c.qa, qa0);
     c.drb = quat_diff_vec(c.qb, qb0);
-    c.sph_a = info_shape(w.info[c.a]) == AVBD_SHAPE_SPHERE;
-    c.sph_b = info_shape(w.info[c.b]) == AVBD_SHAPE_SPHERE;
+    const uint32_t sha = info_shape(w.info[c.a]), shb = info_shape(w.info[c.b]);
+    c.sph_a = sha == AVBD_SHAPE_SPHERE;
+    c.sph_b = shb == AVBD_SHAPE_SPHERE;
+    c.roll_a = sha == AVBD_SHAPE_CAPSULE && shb != AVBD_SHAPE_BOX;
+    c.roll_b = shb == AVBD_SHAPE_CAPSULE && sha != AVBD_SHAPE_BOX;
     c.rad_a = w.shp[c.a].x;
     c.rad_b = w.shp[c.b].x;
     c.mu_roll = 0.0f;
@@ -109,13 +113,33 @@ static __device__ __forceinline__ void friction_levers_bwd(const PairCtx& c, V3 
     pg.xa = pg.xa + c.n * gsep;
     pg.xb = pg.xb - c.n * gsep;
 }
+// A capsule's witness anchor (taken this substep, not kept from a stuck
+// point, and not a box corner's projection) is the closest point of its
+// rounded surface: segment point + s R0^T n in the body frame (s = -r on
+// side A, +r on side B).  Held fixed as a material point instead, its
+// lever would not roll with the body, and the linearised iteration of a
+// capsule resting on its cap grows without bound; the anchor adjoint g
+// therefore reaches the step-start orientation q0.
+static __device__ __forceinline__ void rolling_anchor_bwd(Q q0, V3 n, float s, V3 g, Q& gq0) {
+    Q gc = Q0();
+    V3 dummy = V0();
+    qrot_bwd(conj(q0), n, g * s, gc, dummy);
+    gq0.x -= gc.x;
+    gq0.y -= gc.y;
+    gq0.z -= gc.z;
+    gq0.w += gc.w;
+}
 // contact_levers (rows.rs:963-973): a non-sphere lever is the anchor rotated
 // by the body; a sphere's is fixed by the (frozen) normal.
-static __device__ __forceinline__ void contact_levers_bwd(const PairCtx& c, float4 ra, float4 rb, V3 graw, V3 grbw,
-                                                          PairGrad& pg) {
-    V3 dummy = V0();
-    if (!c.sph_a) qrot_bwd(c.qa, ld3(ra), graw, pg.qa, dummy);
-    if (!c.sph_b) qrot_bwd(c.qb, ld3(rb), grbw, pg.qb, dummy);
+static __device__ __forceinline__ void contact_levers_bwd(const PairCtx& c, Q qa0, Q qb0, float4 ra, float4 rb,
+                                                          V3 graw, V3 grbw, PairGrad& pg) {
+    V3 gla = V0(), glb = V0();
+    if (!c.sph_a) qrot_bwd(c.qa, ld3(ra), graw, pg.qa, gla);
+    if (!c.sph_b) qrot_bwd(c.qb, ld3(rb), grbw, pg.qb, glb);
+    if (ra.w == 0.0f) {
+        if (c.roll_a) rolling_anchor_bwd(qa0, c.n, -c.rad_a, gla, pg.qa0);
+        if (c.roll_b) rolling_anchor_bwd(qb0, c.n, c.rad_b, glb, pg.qb0);
+    }
 }
 
 // Adjoint of one point's rows in a block solve of the body on side is_a.
@@ -165,7 +189,7 @@ static __device__ __forceinline__ void adj_point_bwd(const DW& w, const AdjFrame
         else grbw = grbw + gr;
     }
     row_c_bwd(c, qa0, qb0, c.n, rup, rlo, gcn, gc0, graw, grbw, pg);
-    contact_levers_bwd(c, ra, rb, graw, grbw, pg);
+    contact_levers_bwd(c, qa0, qb0, ra, rb, graw, grbw, pg);
     glam.w += gc0;
 }
 
@@ -221,6 +245,72 @@ static __device__ __forceinline__ void lsum(PairGrad& g, float2& m) {
 }
 static __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// ---- joints ----------------------------------------------------------------
+static __device__ __forceinline__ const float4* jslice(const DW& w, const AdjFrame& f, int s) {
+    return f.it_joint + (size_t)s * 5 * (size_t)w.J;
+}
+static __device__ __forceinline__ JDef jdef(const DW& w, uint32_t j) {
+    JDef d;
+    float4 axa = w.j_axa[j];
+    d.la = ld3(w.j_la[j]);
+    d.lb = ld3(w.j_lb[j]);
+    d.axa_l = ld3(axa);
+    d.axb_l = ld3(w.j_axb[j]);
+    d.ref = axa.w;
+    d.revolute = w.j_kind[j] == AVBD_JOINT_REVOLUTE;
+    d.lim = w.j_lim[j];
+    return d;
+}
+static __device__ __forceinline__ JState jstate(const DW& w, const AdjFrame& f, uint32_t j, int s) {
+    const float4* b = jslice(w, f, s);
+    const size_t J = (size_t)w.J;
+    JState st;
+    st.laml = b[j];
+    st.penl = b[J + j];
+    st.lama = b[2 * J + j];
+    st.pena = b[3 * J + j];
+    st.acc = b[4 * J + j].w;
+    return st;
+}
+static __device__ __forceinline__ JPose jpose(const DW& w, const AdjFrame& f, uint2 ab, int sa, int sb) {
+    JPose p;
+    p.xa = ld3(f.it_pos[pslice(w, sa) + ab.x]);
+    p.qa = ldq(f.it_rot[pslice(w, sa) + ab.x]);
+    p.xb = ld3(f.it_pos[pslice(w, sb) + ab.y]);
+    p.qb = ldq(f.it_rot[pslice(w, sb) + ab.y]);
+    p.xa0 = ld3(f.pos0[ab.x]);
+    p.qa0 = ldq(f.rot0[ab.x]);
+    p.xb0 = ld3(f.pos0[ab.y]);
+    p.qb0 = ldq(f.rot0[ab.y]);
+    return p;
+}
+static __device__ __forceinline__ JState ajs_load(const AdjState& A, uint32_t j) {
+    const float4* g = A.ajs + (size_t)j * 5;
+    JState st;
+    st.laml = g[0];
+    st.penl = g[1];
+    st.lama = g[2];
+    st.pena = g[3];
+    st.acc = g[4].w;
+    return st;
+}
+static __device__ __forceinline__ void ajs_store(const AdjState& A, uint32_t j, const JState& st) {
+    float4* g = A.ajs + (size_t)j * 5;
+    g[0] = st.laml;
+    g[1] = st.penl;
+    g[2] = st.lama;
+    g[3] = st.pena;
+    g[4] = make_float4(0.0f, 0.0f, 0.0f, st.acc);
+}
+static __device__ __forceinline__ JState jstate_add(JState a, const JState& b) {
+    a.laml = f4add(a.laml, b.laml);
+    a.penl = f4add(a.penl, b.penl);
+    a.lama = f4add(a.lama, b.lama);
+    a.pena = f4add(a.pena, b.pena);
+    a.acc += b.acc;
+    return a;
 }
 
 // ---- BDF1 (mod.rs:1060-1078) --------------------------------------------------
@@ -331,7 +421,7 @@ __global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState 
             row_c_bwd(c, qa0, qb0, c.t2, raf, rbf, gct2, unused, graf, grbf, pg);
             friction_levers_bwd(c, graf, grbf, graw, grbw, pg);
             row_c_bwd(c, qa0, qb0, c.n, raw, rbw, gcn, gc0, graw, grbw, pg);
-            contact_levers_bwd(c, ra, rb, graw, grbw, pg);
+            contact_levers_bwd(c, qa0, qb0, ra, rb, graw, grbw, pg);
             glo.w += gc0;
             A.alam[q] = glo;
             A.apen[q] = gpo;
@@ -367,6 +457,15 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
             sl[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             sl[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
+        const uint32_t j0 = w.J ? w.jofs[h] : 0u, j1 = w.J ? w.jofs[h + 1] : 0u;
+        for (uint32_t k = j0; k < j1; k++) {
+            uint32_t j = w.jlist[k];
+            float4* sl = A.jslot + ((size_t)j * 2 + (w.j_ab[j].x == h ? 0u : 1u)) * 4;
+            gx = gx + ld3(sl[0]);
+            gq = qadd(gq, ldq(sl[1]));
+            sl[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            sl[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
         V3 x = ld3(f.it_pos[pslice(w, it) + h]);
         Q q = ldq(f.it_rot[pslice(w, it) + h]);
         Sys s;
@@ -382,6 +481,14 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
             s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
             s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
             s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
+        }
+        for (uint32_t k = j0; k < j1; k++) {  // joints after the contact rows, as the forward
+            uint32_t j = w.jlist[k];
+            uint2 ab = w.j_ab[j];
+            bool is_a = ab.x == h;
+            JPose jp = is_a ? jpose(w, f, ab, it, seen_slice(f, ab.y, colour, it))
+                            : jpose(w, f, ab, seen_slice(f, ab.x, colour, it), it);
+            joint_stamp(jdef(w, j), jp, jstate(w, f, j, it), is_a, s);
         }
         float4* wd = A.wd + (size_t)h * 3;
         float d6[6];
@@ -421,6 +528,32 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
         quat_diff_vec_bwd(q, qt, gth, gqb, gqt);
         world_inertia_bwd(inr, q, wa, th + dang, -1.0f / dt2, gqb);
         A.aqt[h] = f4add(A.aqt[h], stq(gqt));
+        for (uint32_t k = j0; k < j1; k++) {
+            uint32_t j = w.jlist[k];
+            uint2 ab = w.j_ab[j];
+            bool is_a = ab.x == h;
+            JPose jp = is_a ? jpose(w, f, ab, it, seen_slice(f, ab.y, colour, it))
+                            : jpose(w, f, ab, seen_slice(f, ab.x, colour, it), it);
+            PairGrad pg;
+            pair_grad_zero(pg);
+            JState gs;
+            jstate_zero(gs);
+            joint_stamp_bwd(jdef(w, j), jp, jstate(w, f, j, it), is_a, w6, d6, pg, gs);
+            ajs_store(A, j, jstate_add(ajs_load(A, j), gs));
+            float4* own = A.jslot + ((size_t)j * 2 + (is_a ? 0u : 1u)) * 4;
+            float4* other = A.jslot + ((size_t)j * 2 + (is_a ? 1u : 0u)) * 4;
+            if (is_a) {
+                gxb = gxb + pg.xa;
+                gqb = qadd(gqb, pg.qa);
+                slot_add(own, V0(), Q0(), pg.xa0, pg.qa0);
+                slot_add(other, pg.xb, pg.qb, pg.xb0, pg.qb0);
+            } else {
+                gxb = gxb + pg.xb;
+                gqb = qadd(gqb, pg.qb);
+                slot_add(own, V0(), Q0(), pg.xb0, pg.qb0);
+                slot_add(other, pg.xa, pg.qa, pg.xa0, pg.qa0);
+            }
+        }
         A.ax[h] = st3(gxb, 0.0f);
         A.aq[h] = stq(gqb);
         wd[0] = make_float4(w6[0], w6[1], w6[2], w6[3]);
@@ -471,6 +604,47 @@ __global__ void __launch_bounds__(128, 3) k_adj_sides(DW w, AdjFrame f, AdjState
     slot_add(slot_of(f, A, p, false, ab), pg.xb, pg.qb, pg.xb0, pg.qb0);
     float2 m = A.amu[p];
     A.amu[p] = make_float2(m.x + gmu.x, m.y + gmu.y);
+}
+
+// ---- joint dual update (joints_ext.rs:574-896), one thread per joint -----------
+__global__ void k_adj_dual_joints(DW w, AdjFrame f, AdjState A, int it) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    uint2 ab = w.j_ab[j];
+    PairGrad pg;
+    pair_grad_zero(pg);
+    JState gin;
+    float gk = 0.0f;
+    joint_dual_bwd(jdef(w, j), jpose(w, f, ab, it + 1, it + 1), jstate(w, f, j, it), w.joint_k, ajs_load(A, j), gin,
+                   pg, gk);
+    ajs_store(A, j, gin);
+    A.ajk[j] += gk;
+    slot_add(A.jslot + (size_t)j * 8, pg.xa, pg.qa, pg.xa0, pg.qa0);
+    slot_add(A.jslot + (size_t)j * 8 + 4, pg.xb, pg.qb, pg.xb0, pg.qb0);
+}
+// joint warmstart decay (mod.rs:1019-1040): lambda * alpha gamma; penalty
+// clamp(p gamma), or the stiffness for the rows of a soft joint
+__global__ void k_adj_decay_joints(DW w, AdjFrame f, AdjState A) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (uint32_t)w.J) return;
+    const float ag = ALPHA * GAMMA, K = w.joint_k;
+    JState g = ajs_load(A, j), s0 = jstate(w, f, j, 0);
+    float gk = 0.0f;
+    auto pen_bwd = [&](float after, float gp, bool soft) {
+        if (soft && K > 0.0f) {
+            gk += gp;
+            return 0.0f;
+        }
+        return (after > PENALTY_MIN && after < PENALTY_MAX) ? gp * GAMMA : 0.0f;
+    };
+    g.laml = make_float4(g.laml.x * ag, g.laml.y * ag, g.laml.z * ag, 0.0f);
+    g.lama = make_float4(g.lama.x * ag, g.lama.y * ag, g.lama.z * ag, 0.0f);
+    g.penl = make_float4(pen_bwd(s0.penl.x, g.penl.x, true), pen_bwd(s0.penl.y, g.penl.y, true),
+                         pen_bwd(s0.penl.z, g.penl.z, true), 0.0f);
+    g.pena = make_float4(pen_bwd(s0.pena.x, g.pena.x, true), pen_bwd(s0.pena.y, g.pena.y, true),
+                         pen_bwd(s0.pena.z, g.pena.z, false), 0.0f);
+    ajs_store(A, j, g);
+    A.ajk[j] += gk;
 }
 
 // ---- C0 and the warmstart decay (joints_ext.rs:21-32, mod.rs:1019-1040) -------
@@ -524,6 +698,15 @@ __global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
         gx0 = gx0 + ld3(s[2]);
         gq0 = qadd(gq0, ldq(s[3]));
     }
+    if (w.J)
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
+            uint32_t j = w.jlist[k];
+            const float4* s = A.jslot + ((size_t)j * 2 + (w.j_ab[j].x == h ? 0u : 1u)) * 4;
+            gx = gx + ld3(s[0]);
+            gq = qadd(gq, ldq(s[1]));
+            gx0 = gx0 + ld3(s[2]);
+            gq0 = qadd(gq0, ldq(s[3]));
+        }
     if (f.colour[h] >= 0) {
         // the iterations started from the targets: x = y = x0 + v dt + g dt^2,
         // q = qt = integrate(q0, w dt)
@@ -533,7 +716,16 @@ __global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
         gx0 = gx0 + gy;
         V3 gwd = V0();
         quat_integrate_bwd(ldq(f.rot0[h]), ld3(f.angvel[h]) * dt, gqt, gq0, gwd);
-        A.av[h] = st3(gy * dt, 0.0f);
+        V3 gv = gy * dt;
+        if (f.ccd && f.ccd[2 * h + 1].y != 0.0f) {
+            // a swept impact moved the body before the targets: x' = x + v dt
+            // frac, v' = (I - bounce n n^T) v, time of impact and normal held
+            // fixed like a contact frame
+            float4 nb = f.ccd[2 * h];
+            V3 n = ld3(nb);
+            gv = gv - n * (nb.w * dot(n, gv)) + gx0 * f.ccd[2 * h + 1].x;
+        }
+        A.av[h] = st3(gv, 0.0f);
         A.aw[h] = st3(gwd * dt, 0.0f);
         A.ax[h] = st3(gx0, 0.0f);
         A.aq[h] = stq(gq0);
@@ -563,9 +755,10 @@ __global__ void k_adj_inherit(DW w, AdjFrame f, AdjState A) {
 }
 
 // ---- friction coefficient adjoint per scene (pair mu = max of the bodies') -----
-__global__ void k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= (uint32_t)w.S) return;
+// One block per scene; the block's fixed-shape tree sum keeps the result the
+// same from run to run.
+__global__ void __launch_bounds__(256) k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
+    const uint32_t s = blockIdx.x;
     uint32_t b0 = w.scene_off[s], b1 = w.scene_off[s + 1];
     // pairs are ordered by their A body: binary search the scene's range
     auto lower = [&](uint32_t key) {
@@ -579,11 +772,18 @@ __global__ void k_adj_mu_scene(DW w, AdjFrame f, AdjState A) {
     };
     uint32_t p0 = lower(b0), p1 = lower(b1);
     float acc = 0.0f;
-    for (uint32_t p = p0; p < p1; p++) {
+    for (uint32_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
         float2 m = A.amu[p];
         acc += m.x + m.y;
     }
-    A.ascene_mu[s] += acc;
+    __shared__ float part[256];
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    for (uint32_t k = blockDim.x >> 1; k > 0; k >>= 1) {
+        if (threadIdx.x < k) part[threadIdx.x] += part[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.ascene_mu[s] += part[0];
 }
 
 void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st) {
@@ -594,15 +794,17 @@ void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, i
     k_adj_bdf<<<gb, 256, 0, st>>>(w, f, A, iters);
     for (int it = iters - 1; it >= 0; it--) {
         k_adj_dual<<<gpl, 128, 0, st>>>(w, f, A, it);
+        if (w.J) k_adj_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w, f, A, it);
         for (int c = (int)f.ncol - 1; c >= 0; c--) {
             k_adj_solve<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
             k_adj_sides<<<gp2, 128, 0, st>>>(w, f, A, it, c);
         }
     }
     k_adj_c0<<<gp, 128, 0, st>>>(w, f, A);
+    if (w.J) k_adj_decay_joints<<<nblk(w.J, 128), 128, 0, st>>>(w, f, A);
     k_adj_start<<<gb, 256, 0, st>>>(w, f, A);
     k_adj_inherit<<<gp, 128, 0, st>>>(w, f, A);
-    k_adj_mu_scene<<<nblk(w.S, 128), 128, 0, st>>>(w, f, A);
+    if (w.S > 0) k_adj_mu_scene<<<(unsigned)w.S, 256, 0, st>>>(w, f, A);
 }
 
 }  // namespace avbd

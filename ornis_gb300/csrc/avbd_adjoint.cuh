@@ -210,3 +210,460 @@ static __host__ __device__ __forceinline__ void row_c_bwd(const PairCtx& c, cons
 }
 
 }  // namespace avbd
+
+// ---- joints (assembly.rs:255-881 rows, joints_ext.rs:574-896 dual) ------------------
+namespace avbd {
+
+// One joint as a reversed body update sees it: its definition, the poses of
+// both bodies (current and step start) and its warm state.
+struct JDef {
+    V3 la, lb, axa_l, axb_l;
+    float ref;     // reference twist of the hinge
+    bool revolute;
+    float4 lim;    // lo, hi, has_limit (w unused)
+};
+struct JPose {
+    V3 xa, xb, xa0, xb0;
+    Q qa, qb, qa0, qb0;
+};
+struct JState {
+    float4 laml, penl, lama, pena;
+    float acc;  // the limit's accumulated force (j_lim.w)
+};
+AVBD_HD void jstate_zero(JState& s) {
+    s.laml = s.penl = s.lama = s.pena = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    s.acc = 0.0f;
+}
+static __host__ __device__ __forceinline__ float f4get(const float4& v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+static __host__ __device__ __forceinline__ void f4add_at(float4& v, int k, float a) {
+    if (k == 0) v.x += a;
+    else if (k == 1) v.y += a;
+    else if (k == 2) v.z += a;
+    else v.w += a;
+}
+
+// hinge_twist (sequential_impulse/joints.rs:38-48): 2 atan2(q.xyz . axis, q.w)
+// of q = conj(qa) (x) qb, wrapped (the wrap is the identity almost everywhere).
+static __host__ __device__ __forceinline__ void hinge_twist_bwd(Q qa, Q qb, V3 axis, float g, Q& gqa, Q& gqb) {
+    Q q = qmul(conj(qa), qb);
+    float s = dot(V3{q.x, q.y, q.z}, axis), w = q.w;
+    float r2 = s * s + w * w;
+    if (!(r2 > 0.0f)) return;
+    float k = 2.0f * g / r2;
+    Q gq{axis.x * w * k, axis.y * w * k, axis.z * w * k, -s * k};
+    Q gca = Q0();
+    qmul_bwd(conj(qa), qb, gq, gca, gqb);
+    gqa = qadd(gqa, conj(gca));
+}
+// tangent_t1 (math.rs:152-160): normalize(n x r) with r = X or Y by |n.x|;
+// adds the adjoint of n.
+static __host__ __device__ __forceinline__ void tangent_t1_bwd(V3 n, V3 gt, V3& gn) {
+    V3 axis = fabsf(n.x) < TANGENT_REF_AXIS_DOT ? VX() : VY();
+    V3 u = cross(n, axis);
+    float l = len(u);
+    if (!(l > 0.0f)) return;
+    V3 t = u / l;
+    V3 gu = (gt - t * dot(t, gt)) / l;
+    gn = gn + cross(axis, gu);
+}
+
+// Adjoint of one stamped row for the solve's -d/ds [w.(rhs + H d)]
+// (stamp_row and stamp_angular; see row_bwd in avbd_adjoint.cu).
+static __host__ __device__ __forceinline__ void jrow_lin_bwd(V3 axis, float pen, float f, V3 r, float sign,
+                                                             const float w6[6], const float d6[6], float& gf,
+                                                             float& gpen, V3& gr) {
+    V3 nn = sign * axis;
+    V3 t = cross(r, nn);
+    V3 wl{w6[0], w6[1], w6[2]}, wa{w6[3], w6[4], w6[5]};
+    V3 dl{d6[0], d6[1], d6[2]}, da{d6[3], d6[4], d6[5]};
+    float a = dot(nn, wl) + dot(t, wa);
+    float dd = dot(nn, dl) + dot(t, da);
+    gf -= a;
+    gpen -= a * dd;
+    V3 gja = -(wa * f + (wa * dd + da * a) * pen);
+    gr = gr + cross(nn, gja);
+}
+static __host__ __device__ __forceinline__ void jrow_ang_bwd(V3 g, float pen, float f, const float w6[6],
+                                                             const float d6[6], float& gf, float& gpen, V3& gg) {
+    V3 wa{w6[3], w6[4], w6[5]}, da{d6[3], d6[4], d6[5]};
+    float a = dot(g, wa), dd = dot(g, da);
+    gf -= a;
+    gpen -= a * dd;
+    gg = gg - (wa * f + (wa * dd + da * a) * pen);
+}
+
+// The hinge frame of a joint at its step-start pose: t1, t2 from axa0.
+static __host__ __device__ __forceinline__ void hinge_frame(V3 axa0, V3& t1, V3& t2) {
+    t1 = tangent_t1(axa0);
+    t2 = cross(t1, axa0);
+}
+// adjoint of (t1, t2) -> axa0
+static __host__ __device__ __forceinline__ void hinge_frame_bwd(V3 axa0, V3 t1, V3 gt1, V3 gt2, V3& gaxa0) {
+    // t2 = t1 x axa0
+    gt1 = gt1 + cross(axa0, gt2);
+    gaxa0 = gaxa0 + cross(gt2, t1);
+    tangent_t1_bwd(axa0, gt1, gaxa0);
+}
+
+// The joint rows of one body (the forward stamp_joint of avbd_phase_solve.cu).
+static __host__ __device__ __forceinline__ void joint_stamp(const JDef& d, const JPose& p, const JState& s, bool is_a,
+                                                            Sys& sys) {
+    float sign = is_a ? 1.0f : -1.0f;
+    V3 pa = p.xa + qrot(p.qa, d.la), pb = p.xb + qrot(p.qb, d.lb);
+    V3 pa0 = p.xa0 + qrot(p.qa0, d.la), pb0 = p.xb0 + qrot(p.qb0, d.lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    V3 lever = is_a ? qrot(p.qa, d.la) : qrot(p.qb, d.lb);
+    float fl[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < 3; k++) {
+        V3 axis = V0();
+        axis[k] = 1.0f;
+        float cc = live[k] - ALPHA * c0v[k];
+        float f = f4get(s.penl, k) * cc + f4get(s.laml, k);
+        if (!row_live(cc, f)) continue;
+        stamp_row(sys, axis, f4get(s.penl, k), f, lever, sign);
+        fl[k] = f;
+    }
+    {
+        V3 r = is_a ? qrot(p.qa, d.la) : -qrot(p.qb, d.lb);
+        float rf = dot(r, V3{fl[0], fl[1], fl[2]});
+        for (int y = 0; y < 3; y++) {
+            V3 col = r * fl[y];
+            col[y] -= rf;
+            sys.h[tri(3 + y, 3 + y)] += len(col);
+        }
+    }
+    if (!d.revolute) return;
+    V3 axa = qrot(p.qa, d.axa_l), axb = qrot(p.qb, d.axb_l);
+    V3 axa0 = qrot(p.qa0, d.axa_l), axb0 = qrot(p.qb0, d.axb_l);
+    V3 t1, t2;
+    hinge_frame(axa0, t1, t2);
+    V3 ts[2] = {t1, t2};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        float f = f4get(s.pena, li) * cc + f4get(s.lama, li);
+        if (!row_live(cc, f)) continue;
+        stamp_angular(sys, is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]), f4get(s.pena, li), f);
+    }
+    if (d.lim.z != 0.0f) {
+        V3 wa = normalize_or(axa, VZ());
+        float angle = wrap_pi(hinge_twist(p.qa, p.qb, d.axa_l) - d.ref);
+        int stt = warm_limit_state(angle, d.lim.x, d.lim.y, LIMIT_SLOP_ANG, s.acc);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float initial = wrap_pi(hinge_twist(p.qa0, p.qb0, d.axa_l) - d.ref);
+            float cc = regularized_limit(angle, initial, lower ? d.lim.x : d.lim.y, lower);
+            float f_raw = s.pena.z * cc + s.acc;
+            float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+            if (row_live(cc, f)) stamp_angular(sys, is_a ? -wa : wa, s.pena.z, f);
+        }
+    }
+}
+
+// Adjoint of joint_stamp for the body on side is_a, given w = H^-1 d_bar and
+// the step d of that body: adds the adjoints of both bodies' poses (g) and
+// of the joint's warm state (gs).
+static __host__ __device__ __forceinline__ void joint_stamp_bwd(const JDef& d, const JPose& p, const JState& s,
+                                                                bool is_a, const float w6[6], const float d6[6],
+                                                                PairGrad& g, JState& gs) {
+    float sign = is_a ? 1.0f : -1.0f;
+    V3 pa = p.xa + qrot(p.qa, d.la), pb = p.xb + qrot(p.qb, d.lb);
+    V3 pa0 = p.xa0 + qrot(p.qa0, d.la), pb0 = p.xb0 + qrot(p.qb0, d.lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    V3 lever = is_a ? qrot(p.qa, d.la) : qrot(p.qb, d.lb);
+    V3 glive = V0(), gc0v = V0(), glever = V0();
+    float fl[3] = {0.0f, 0.0f, 0.0f}, cs[3] = {0.0f, 0.0f, 0.0f};
+    bool liv[3] = {false, false, false};
+    float gfl[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < 3; k++) {
+        float cc = live[k] - ALPHA * c0v[k];
+        float f = f4get(s.penl, k) * cc + f4get(s.laml, k);
+        cs[k] = cc;
+        if (!row_live(cc, f)) continue;
+        liv[k] = true;
+        fl[k] = f;
+        V3 axis = V0();
+        axis[k] = 1.0f;
+        float gpen = 0.0f;
+        jrow_lin_bwd(axis, f4get(s.penl, k), f, lever, sign, w6, d6, gfl[k], gpen, glever);
+        f4add_at(gs.penl, k, gpen);
+    }
+    {
+        // geometric stiffness: H[3+y][3+y] += |col_y|, col_y = r fl_y - (r.fl) e_y
+        V3 r = is_a ? qrot(p.qa, d.la) : -qrot(p.qb, d.lb);
+        V3 flv{fl[0], fl[1], fl[2]};
+        float rf = dot(r, flv);
+        V3 gr = V0(), gflv = V0();
+        for (int y = 0; y < 3; y++) {
+            V3 col = r * fl[y];
+            col[y] -= rf;
+            float l = len(col);
+            if (!(l > 0.0f)) continue;
+            float c = -w6[3 + y] * d6[3 + y];
+            V3 gcol = col * (c / l);
+            // col[x] = r_x fl_y - rf delta_xy
+            gr = gr + gcol * fl[y] - flv * gcol[y];
+            gflv[y] += dot(gcol, r);
+            gflv = gflv - r * gcol[y];
+        }
+        for (int k = 0; k < 3; k++) gfl[k] += gflv[k];
+        V3 dummy = V0();
+        if (is_a) qrot_bwd(p.qa, d.la, gr, g.qa, dummy);
+        else qrot_bwd(p.qb, d.lb, -gr, g.qb, dummy);
+    }
+    for (int k = 0; k < 3; k++) {
+        if (!liv[k]) continue;
+        // f = pen c + lambda, c = live_k - alpha c0v_k
+        float gc = f4get(s.penl, k) * gfl[k];
+        f4add_at(gs.penl, k, cs[k] * gfl[k]);
+        f4add_at(gs.laml, k, gfl[k]);
+        glive[k] += gc;
+        gc0v[k] -= ALPHA * gc;
+    }
+    {
+        V3 dummy = V0();
+        if (is_a) qrot_bwd(p.qa, d.la, glever, g.qa, dummy);
+        else qrot_bwd(p.qb, d.lb, glever, g.qb, dummy);
+        g.xa = g.xa + glive;
+        qrot_bwd(p.qa, d.la, glive, g.qa, dummy);
+        g.xb = g.xb - glive;
+        qrot_bwd(p.qb, d.lb, -glive, g.qb, dummy);
+        g.xa0 = g.xa0 + gc0v;
+        qrot_bwd(p.qa0, d.la, gc0v, g.qa0, dummy);
+        g.xb0 = g.xb0 - gc0v;
+        qrot_bwd(p.qb0, d.lb, -gc0v, g.qb0, dummy);
+    }
+    if (!d.revolute) return;
+    V3 axa = qrot(p.qa, d.axa_l), axb = qrot(p.qb, d.axb_l);
+    V3 axa0 = qrot(p.qa0, d.axa_l), axb0 = qrot(p.qb0, d.axb_l);
+    V3 t1, t2;
+    hinge_frame(axa0, t1, t2);
+    V3 ts[2] = {t1, t2};
+    V3 gaxa = V0(), gaxb = V0(), gaxa0 = V0(), gaxb0 = V0(), gts[2] = {V0(), V0()};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        float pen = f4get(s.pena, li);
+        float f = pen * cc + f4get(s.lama, li);
+        if (!row_live(cc, f)) continue;
+        V3 gv = is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]);
+        float gf = 0.0f, gpen = 0.0f;
+        V3 ggv = V0();
+        jrow_ang_bwd(gv, pen, f, w6, d6, gf, gpen, ggv);
+        if (is_a) {
+            gaxa = gaxa + cross(ts[li], ggv);
+            gts[li] = gts[li] + cross(ggv, axa);
+        } else {
+            gaxb = gaxb - cross(ts[li], ggv);
+            gts[li] = gts[li] - cross(ggv, axb);
+        }
+        float gc = pen * gf;
+        f4add_at(gs.pena, li, gpen + cc * gf);
+        f4add_at(gs.lama, li, gf);
+        gts[li] = gts[li] + ((axa - axb) - (axa0 - axb0) * ALPHA) * gc;
+        gaxa = gaxa + ts[li] * gc;
+        gaxb = gaxb - ts[li] * gc;
+        gaxa0 = gaxa0 - ts[li] * (ALPHA * gc);
+        gaxb0 = gaxb0 + ts[li] * (ALPHA * gc);
+    }
+    if (d.lim.z != 0.0f) {
+        V3 wa = normalize_or(axa, VZ());
+        float angle = wrap_pi(hinge_twist(p.qa, p.qb, d.axa_l) - d.ref);
+        int stt = warm_limit_state(angle, d.lim.x, d.lim.y, LIMIT_SLOP_ANG, s.acc);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float bound = lower ? d.lim.x : d.lim.y;
+            float initial = wrap_pi(hinge_twist(p.qa0, p.qb0, d.axa_l) - d.ref);
+            float cc = regularized_limit(angle, initial, bound, lower);
+            float f_raw = s.pena.z * cc + s.acc;
+            float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+            if (row_live(cc, f)) {
+                float gf = 0.0f, gpen = 0.0f;
+                V3 gwv = V0();
+                jrow_ang_bwd(is_a ? -wa : wa, s.pena.z, f, w6, d6, gf, gpen, gwv);
+                gs.pena.z += gpen;
+                V3 gwa = is_a ? -gwv : gwv;
+                float la = len(axa);
+                if (la > 0.0f) gaxa = gaxa + (gwa - wa * dot(wa, gwa)) / la;
+                bool pass = lower ? f_raw < 0.0f : f_raw > 0.0f;
+                if (pass) {
+                    float gc = s.pena.z * gf;
+                    gs.pena.z += cc * gf;
+                    gs.acc += gf;
+                    float old = initial - bound;
+                    bool active = lower ? old < 0.0f : old > 0.0f;
+                    hinge_twist_bwd(p.qa, p.qb, d.axa_l, gc, g.qa, g.qb);
+                    if (active) hinge_twist_bwd(p.qa0, p.qb0, d.axa_l, -ALPHA * gc, g.qa0, g.qb0);
+                }
+            }
+        }
+    }
+    hinge_frame_bwd(axa0, t1, gts[0], gts[1], gaxa0);
+    V3 dummy = V0();
+    qrot_bwd(p.qa, d.axa_l, gaxa, g.qa, dummy);
+    qrot_bwd(p.qb, d.axb_l, gaxb, g.qb, dummy);
+    qrot_bwd(p.qa0, d.axa_l, gaxa0, g.qa0, dummy);
+    qrot_bwd(p.qb0, d.axb_l, gaxb0, g.qb0, dummy);
+}
+
+// The joint dual update (k_dual_joints) with finite stiffness K (0: hard).
+static __host__ __device__ __forceinline__ void joint_dual(const JDef& d, const JPose& p, const JState& in, float K,
+                                                           JState& out) {
+    out = in;
+    V3 pa = p.xa + qrot(p.qa, d.la), pb = p.xb + qrot(p.qb, d.lb);
+    V3 pa0 = p.xa0 + qrot(p.qa0, d.la), pb0 = p.xb0 + qrot(p.qb0, d.lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    for (int k = 0; k < 3; k++) {
+        float cc = live[k] - ALPHA * c0v[k];
+        float pen = f4get(in.penl, k);
+        if (K > 0.0f) {
+            f4add_at(out.penl, k, K - pen);
+            continue;
+        }
+        if (fabsf(cc) < C_EPS) continue;
+        f4add_at(out.laml, k, pen * cc);
+        f4add_at(out.penl, k, fminf(pen + BETA * fabsf(cc), PENALTY_MAX) - pen);
+    }
+    if (!d.revolute) return;
+    V3 axa = qrot(p.qa, d.axa_l), axb = qrot(p.qb, d.axb_l);
+    V3 axa0 = qrot(p.qa0, d.axa_l), axb0 = qrot(p.qb0, d.axb_l);
+    V3 t1, t2;
+    hinge_frame(axa0, t1, t2);
+    V3 ts[2] = {t1, t2};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        float pen = f4get(in.pena, li);
+        if (K > 0.0f) {
+            f4add_at(out.pena, li, K - pen);
+            continue;
+        }
+        if (fabsf(cc) < C_EPS) continue;
+        f4add_at(out.lama, li, pen * cc);
+        f4add_at(out.pena, li, fminf(pen + BETA_ANG * fabsf(cc), PENALTY_MAX) - pen);
+    }
+    if (d.lim.z != 0.0f) {
+        float angle = wrap_pi(hinge_twist(p.qa, p.qb, d.axa_l) - d.ref);
+        int stt = warm_limit_state(angle, d.lim.x, d.lim.y, LIMIT_SLOP_ANG, in.acc);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float initial = wrap_pi(hinge_twist(p.qa0, p.qb0, d.axa_l) - d.ref);
+            float cc = regularized_limit(angle, initial, lower ? d.lim.x : d.lim.y, lower);
+            if (fabsf(cc) >= C_EPS) {
+                float f = in.pena.z * cc + in.acc;
+                out.acc = lower ? fminf(f, 0.0f) : fmaxf(f, 0.0f);
+                out.pena.z = fminf(in.pena.z + BETA_ANG * fabsf(cc), LIM_PEN_MAX);
+            }
+        } else {
+            out.acc = 0.0f;
+        }
+    }
+}
+
+// Adjoint of joint_dual: gout (adjoint of the state after) -> gin (before),
+// the poses (g) and the stiffness (gK).
+static __host__ __device__ __forceinline__ void joint_dual_bwd(const JDef& d, const JPose& p, const JState& in, float K,
+                                                               const JState& gout, JState& gin, PairGrad& g,
+                                                               float& gK) {
+    gin = gout;
+    V3 pa = p.xa + qrot(p.qa, d.la), pb = p.xb + qrot(p.qb, d.lb);
+    V3 pa0 = p.xa0 + qrot(p.qa0, d.la), pb0 = p.xb0 + qrot(p.qb0, d.lb);
+    V3 live = pa - pb, c0v = pa0 - pb0;
+    V3 glive = V0(), gc0v = V0();
+    for (int k = 0; k < 3; k++) {
+        float cc = live[k] - ALPHA * c0v[k];
+        float pen = f4get(in.penl, k);
+        float gl = f4get(gout.laml, k), gp = f4get(gout.penl, k);
+        if (K > 0.0f) {  // penalty := K (the pass-through copied into gin is undone)
+            f4add_at(gin.penl, k, -gp);
+            gK += gp;
+            continue;
+        }
+        if (fabsf(cc) < C_EPS) continue;
+        float gc = 0.0f;
+        if (!(pen + BETA * fabsf(cc) < PENALTY_MAX)) f4add_at(gin.penl, k, -gp);
+        else gc += BETA * copysignf(1.0f, cc) * gp;
+        f4add_at(gin.penl, k, cc * gl);  // lambda += pen c
+        gc += pen * gl;
+        glive[k] += gc;
+        gc0v[k] -= ALPHA * gc;
+    }
+    {
+        V3 dummy = V0();
+        g.xa = g.xa + glive;
+        qrot_bwd(p.qa, d.la, glive, g.qa, dummy);
+        g.xb = g.xb - glive;
+        qrot_bwd(p.qb, d.lb, -glive, g.qb, dummy);
+        g.xa0 = g.xa0 + gc0v;
+        qrot_bwd(p.qa0, d.la, gc0v, g.qa0, dummy);
+        g.xb0 = g.xb0 - gc0v;
+        qrot_bwd(p.qb0, d.lb, -gc0v, g.qb0, dummy);
+    }
+    if (!d.revolute) return;
+    V3 axa = qrot(p.qa, d.axa_l), axb = qrot(p.qb, d.axb_l);
+    V3 axa0 = qrot(p.qa0, d.axa_l), axb0 = qrot(p.qb0, d.axb_l);
+    V3 t1, t2;
+    hinge_frame(axa0, t1, t2);
+    V3 ts[2] = {t1, t2};
+    V3 gaxa = V0(), gaxb = V0(), gaxa0 = V0(), gaxb0 = V0(), gts[2] = {V0(), V0()};
+    for (int li = 0; li < 2; li++) {
+        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        float pen = f4get(in.pena, li);
+        float gl = f4get(gout.lama, li), gp = f4get(gout.pena, li);
+        if (K > 0.0f) {
+            f4add_at(gin.pena, li, -gp);
+            gK += gp;
+            continue;
+        }
+        if (fabsf(cc) < C_EPS) continue;
+        float gc = 0.0f;
+        if (!(pen + BETA_ANG * fabsf(cc) < PENALTY_MAX)) f4add_at(gin.pena, li, -gp);
+        else gc += BETA_ANG * copysignf(1.0f, cc) * gp;
+        f4add_at(gin.pena, li, cc * gl);
+        gc += pen * gl;
+        gts[li] = gts[li] + ((axa - axb) - (axa0 - axb0) * ALPHA) * gc;
+        gaxa = gaxa + ts[li] * gc;
+        gaxb = gaxb - ts[li] * gc;
+        gaxa0 = gaxa0 - ts[li] * (ALPHA * gc);
+        gaxb0 = gaxb0 + ts[li] * (ALPHA * gc);
+    }
+    if (d.lim.z != 0.0f) {
+        float angle = wrap_pi(hinge_twist(p.qa, p.qb, d.axa_l) - d.ref);
+        int stt = warm_limit_state(angle, d.lim.x, d.lim.y, LIMIT_SLOP_ANG, in.acc);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            float bound = lower ? d.lim.x : d.lim.y;
+            float initial = wrap_pi(hinge_twist(p.qa0, p.qb0, d.axa_l) - d.ref);
+            float cc = regularized_limit(angle, initial, bound, lower);
+            if (fabsf(cc) >= C_EPS) {
+                float gacc = gout.acc, gp = gout.pena.z;
+                gin.acc = 0.0f;  // overwritten
+                gin.pena.z = 0.0f;
+                float gc = 0.0f;
+                float f = in.pena.z * cc + in.acc;
+                if (lower ? f < 0.0f : f > 0.0f) {
+                    gin.pena.z += cc * gacc;
+                    gin.acc += gacc;
+                    gc += in.pena.z * gacc;
+                }
+                if (in.pena.z + BETA_ANG * fabsf(cc) < LIM_PEN_MAX) {
+                    gin.pena.z += gp;
+                    gc += BETA_ANG * copysignf(1.0f, cc) * gp;
+                }
+                float old = initial - bound;
+                bool active = lower ? old < 0.0f : old > 0.0f;
+                hinge_twist_bwd(p.qa, p.qb, d.axa_l, gc, g.qa, g.qb);
+                if (active) hinge_twist_bwd(p.qa0, p.qb0, d.axa_l, -ALPHA * gc, g.qa0, g.qb0);
+            }
+        } else {
+            gin.acc = 0.0f;
+        }
+    }
+    hinge_frame_bwd(axa0, t1, gts[0], gts[1], gaxa0);
+    V3 dummy = V0();
+    qrot_bwd(p.qa, d.axa_l, gaxa, g.qa, dummy);
+    qrot_bwd(p.qb, d.axb_l, gaxb, g.qb, dummy);
+    qrot_bwd(p.qa0, d.axa_l, gaxa0, g.qa0, dummy);
+    qrot_bwd(p.qb0, d.axb_l, gaxb0, g.qb0, dummy);
+}
+
+}  // namespace avbd

@@ -138,14 +138,24 @@ __global__ void k_place(DW w) {
 // (half-spaces, floors: often long) are never read in sequence and are left
 // as placed, unless the world keeps a differentiable rollout: its adjoint
 // carries point state across checkpoints by pair index, so every segment is
-// put in one order.
+// put in one order.  A thread sorts a short segment by insertion; a long
+// static one (a floor under thousands of bodies) is listed for the chunk
+// sort below.
+constexpr uint32_t SORT_SHORT = 64;
+constexpr uint32_t SORT_CHUNK = 1024;
 __global__ void k_sort_slots(DW w) {
     if (aborted(w)) return;
     uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= (uint32_t)w.N) return;
     if (a == 0) w.ctr[C_PAIRS] = w.offA[w.N];
     uint32_t s0 = w.offA[a], s1 = w.offA[a + 1];
-    if (!is_dynamic(w, a) && !w.sort_static) return;
+    if (!is_dynamic(w, a)) {
+        if (!w.sort_static) return;
+        if (s1 - s0 > SORT_SHORT) {
+            w.long_seg[atomicAdd(&w.ctr[C_LONGSEG], 1u)] = a;
+            return;
+        }
+    }
     for (uint32_t i = s0 + 1; i < s1; i++) {
         uint32_t c = w.slot_c[i];
         uint32_t bk = w.cand[c].y;
@@ -327,8 +337,8 @@ static __device__ __forceinline__ void build_pair(const DW& w, uint32_t p, uint2
         if (m >= 0) {
             uint32_t oq = (uint32_t)d.old * MAX_PTS + m;
             float4 ora = w.oq_ra[oq], orb = w.oq_rb[oq];
-            if (orb.w != 0.0f && touching && !smooth) {  // stuck: anchors stay frozen
-                w.q_ra[q] = make_float4(ora.x, ora.y, ora.z, 0.0f);
+            if (orb.w != 0.0f && touching && !smooth) {  // stuck: anchors stay frozen (q_ra.w = 1: kept)
+                w.q_ra[q] = make_float4(ora.x, ora.y, ora.z, 1.0f);
                 w.q_rb[q] = orb;
             } else {
                 w.q_ra[q] = st3(fra[k], 0.0f);
@@ -364,6 +374,73 @@ __global__ void k_clear_flags(DW w) {
     if (h < (uint32_t)w.N) w.flag[h] = 0;
 }
 
+// Long static segments, in (b, candidate) order: every chunk of SORT_CHUNK
+// slots is sorted in shared memory (bitonic network), then each slot's final
+// place is its place in its chunk plus, for every other chunk, the number of
+// smaller keys there (binary search).  Keys are unique (one candidate per
+// slot), so the places are a permutation of the segment.
+__global__ void __launch_bounds__(512) k_sort_long_chunks(DW w) {
+    if (aborted(w)) return;
+    const uint32_t nl = w.ctr[C_LONGSEG];
+    __shared__ unsigned long long key[SORT_CHUNK];
+    for (uint32_t l = 0; l < nl; l++) {
+        const uint32_t a = w.long_seg[l];
+        const uint32_t s0 = w.offA[a], s1 = w.offA[a + 1];
+        const uint32_t nch = (s1 - s0 + SORT_CHUNK - 1) / SORT_CHUNK;
+        for (uint32_t ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+            const uint32_t c0 = s0 + ch * SORT_CHUNK, len = min(SORT_CHUNK, s1 - c0);
+            for (uint32_t i = threadIdx.x; i < SORT_CHUNK; i += blockDim.x) {
+                unsigned long long k = ~0ull;
+                if (i < len) {
+                    uint32_t c = w.slot_c[c0 + i];
+                    k = ((unsigned long long)w.cand[c].y << 32) | c;
+                }
+                key[i] = k;
+            }
+            __syncthreads();
+            for (uint32_t k = 2; k <= SORT_CHUNK; k <<= 1)
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t t = threadIdx.x; t < SORT_CHUNK / 2; t += blockDim.x) {
+                        uint32_t i = 2 * t - (t & (j - 1));  // t with a zero bit inserted at j
+                        unsigned long long x = key[i], y = key[i + j];
+                        if ((x > y) == ((i & k) == 0)) {
+                            key[i] = y;
+                            key[i + j] = x;
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) w.seg_key[c0 + i] = key[i];
+            __syncthreads();
+        }
+    }
+}
+__global__ void k_sort_long_rank(DW w) {
+    if (aborted(w)) return;
+    const uint32_t nl = w.ctr[C_LONGSEG];
+    for (uint32_t l = 0; l < nl; l++) {
+        const uint32_t a = w.long_seg[l];
+        const uint32_t s0 = w.offA[a], n = w.offA[a + 1] - s0;
+        const unsigned long long* sk = w.seg_key + s0;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            const unsigned long long k = sk[i];
+            const uint32_t own = i / SORT_CHUNK;
+            uint32_t place = i - own * SORT_CHUNK;
+            for (uint32_t lo = 0, ch = 0; lo < n; lo += SORT_CHUNK, ch++) {
+                if (ch == own) continue;
+                uint32_t b0 = lo, b1 = min(lo + SORT_CHUNK, n);
+                while (b0 < b1) {
+                    uint32_t m = (b0 + b1) >> 1;
+                    if (sk[m] < k) b0 = m + 1;
+                    else b1 = m;
+                }
+                place += b0 - lo;
+            }
+            w.slot_c[s0 + place] = (uint32_t)(k & 0xffffffffull);
+        }
+    }
+}
+
 void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st, int triggers) {
     unsigned g1 = nblk(w.N + 1, 256);
     k_zero_u32<<<g1, 256, 0, st>>>(w.cnt, w.N + 1);
@@ -372,6 +449,10 @@ void launch_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st, int trig
     scan_exclusive(w.cnt, w.offA, w.N + 1, scan_tmp, st);
     k_place<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w);
     k_sort_slots<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    if (w.sort_static) {
+        k_sort_long_chunks<<<2 * 152, 512, 0, st>>>(w);
+        k_sort_long_rank<<<4 * 152, 256, 0, st>>>(w);
+    }
     k_clear_flags<<<nblk(w.N, 256), 256, 0, st>>>(w);
     k_collect_boxes<<<gsz(w.pair_cap, 256), 256, 0, st>>>(w);
     k_box_witness<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
@@ -506,10 +587,18 @@ __global__ void k_decay_joints(DW w) {
     float4 a = w.j_lam_l[j], b = w.j_lam_a[j], c = w.j_pen_l[j], d = w.j_pen_a[j];
     w.j_lam_l[j] = make_float4(a.x * ag, a.y * ag, a.z * ag, 0.0f);
     w.j_lam_a[j] = make_float4(b.x * ag, b.y * ag, b.z * ag, 0.0f);
-    w.j_pen_l[j] = make_float4(fclamp(c.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(c.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
-                               fclamp(c.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
-    w.j_pen_a[j] = make_float4(fclamp(d.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(d.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
-                               fclamp(d.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+    float4 pl = make_float4(fclamp(c.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(c.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                            fclamp(c.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+    float4 pa = make_float4(fclamp(d.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(d.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
+                            fclamp(d.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
+    const float K = w.joint_k;
+    if (K > 0.0f) {  // soft rows (anchors and hinge alignment, not the limit) are springs of stiffness K
+        pl = make_float4(K, K, K, 0.0f);
+        pa.x = K;
+        pa.y = K;
+    }
+    w.j_pen_l[j] = pl;
+    w.j_pen_a[j] = pa;
 }
 
 void launch_post_discovery(const DW& w, uint32_t* scan_tmp, cudaStream_t st) {

@@ -16,6 +16,7 @@ __global__ void k_begin(DW w) {
         w.ctr[C_FCAND] = 0;
         w.ctr[C_BOXONE] = 0;
         w.ctr[C_NOBOX] = 0;
+        w.ctr[C_LONGSEG] = 0;
         w.ctr[C_CAND] = 0;
         w.ctr[C_NCOL] = 0;
         w.ctr[C_FAST] = 0;
@@ -317,6 +318,7 @@ __global__ void k_ccd_init(DW w) {
     w.ccd_deps[h] = 0;
     w.ccd_state[h] = 0;
     w.ccd_recompute[h] = 0;
+    if (w.sort_static) w.ccd_rec[2 * h + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (w.fast[h]) {
         w.fbody[agg_inc(&w.ctr[C_FAST])] = h;
         agg_inc(&w.ctr[C_CCD_PENDING]);
@@ -387,9 +389,14 @@ static __device__ void ccd_apply(const DW& w, uint32_t h) {
         w.pos[h] = st3(ld3(w.pos[h]) + disp * frac, 0.0f);
         V3 v = ld3(w.vel[h]);
         float vn = dot(v, r.normal);
+        float bounce = 0.0f;
         if (vn < 0.0f) {
-            float bounce = vn < -CCD_BOUNCE_SPEED ? 1.0f + e : 1.0f;
+            bounce = vn < -CCD_BOUNCE_SPEED ? 1.0f + e : 1.0f;
             w.vel[h] = st3(v - r.normal * (bounce * vn), 0.0f);
+        }
+        if (w.sort_static) {
+            w.ccd_rec[2 * h] = st3(r.normal, bounce);
+            w.ccd_rec[2 * h + 1] = make_float4(frac * w.dt, 1.0f, 0.0f, 0.0f);
         }
         wake_body(w, o);
         w.sleep_timer[h] = 0.0f;

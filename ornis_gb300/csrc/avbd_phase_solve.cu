@@ -504,9 +504,14 @@ __global__ void k_dual_joints(DW w) {
     V3 live = pa - pb, c0v = pa0 - pb0;
     float4 ll = w.j_lam_l[j], pl = w.j_pen_l[j];
     float laml[3] = {ll.x, ll.y, ll.z}, penl[3] = {pl.x, pl.y, pl.z};
+    // a soft joint (finite stiffness K) is a spring: penalty K, lambda zero;
+    // a hard one is the reference's dual ascent
+    const float K = w.joint_k;
     for (int k = 0; k < 3; k++) {
         float cc = live[k] - ALPHA * c0v[k];
-        if (fabsf(cc) >= C_EPS) {
+        if (K > 0.0f) {
+            penl[k] = K;
+        } else if (fabsf(cc) >= C_EPS) {
             laml[k] += penl[k] * cc;
             penl[k] = fminf(penl[k] + BETA * fabsf(cc), PENALTY_MAX);
         }
@@ -525,6 +530,10 @@ __global__ void k_dual_joints(DW w) {
     float lama[3] = {la4.x, la4.y, la4.z}, pena[3] = {pa4.x, pa4.y, pa4.z};
     for (int li = 0; li < 2; li++) {
         float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+        if (K > 0.0f) {
+            pena[li] = K;
+            continue;
+        }
         if (fabsf(cc) < C_EPS) continue;
         lama[li] = pena[li] * cc + lama[li];
         pena[li] = fminf(pena[li] + BETA_ANG * fabsf(cc), PENALTY_MAX);

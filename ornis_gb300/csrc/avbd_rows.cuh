@@ -195,6 +195,7 @@ struct PairCtx {
     bool sph_a, sph_b;
     float rad_a, rad_b;
     float mu_roll, mu_spin;  // max of the two bodies' rolling / torsion friction
+    bool roll_a, roll_b;     // adjoint: the side's witness anchor rolls (a capsule not against a box)
 };
 
 static __host__ __device__ __forceinline__ float row_c_levers(const PairCtx& c, V3 u, float c0, V3 raw, V3 rbw) {

@@ -241,9 +241,11 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     free_graphs(W);
     Alloc& m = W->mem;
     DW& w = W->w;
-    const int sort_static = w.sort_static;  // a setting of the world, not of the allocation
+    const int sort_static = w.sort_static;  // settings of the world, not of the allocation
+    const float joint_k = w.joint_k;
     w = DW{};
     w.sort_static = sort_static;
+    w.joint_k = joint_k;
     uint32_t S = (uint32_t)W->scene_off.size() - 1;
     w.N = (int)N;
     w.S = (int)S;
@@ -295,6 +297,8 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.cnt = m.get<uint32_t>(N + 1);
     w.cur = m.get<uint32_t>(N + 1);
     w.slot_c = m.get<uint32_t>(cand_cap);
+    w.long_seg = m.get<uint32_t>(N);
+    w.seg_key = m.get<unsigned long long>(cand_cap);
     w.boxlist = m.get<uint32_t>(cand_cap);
     w.clist = m.get<uint32_t>(cand_cap);
     w.bd_pa = m.get<float4>(cand_cap);
@@ -334,6 +338,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.ccd_deps = m.get<uint32_t>(N);
     w.ccd_state = m.get<uint8_t>(N);
     w.ccd_recompute = m.get<uint8_t>(N);
+    w.ccd_rec = W->prm.enable_ccd ? m.get<float4>(2 * N) : nullptr;
     w.flag = m.get<uint8_t>(N);
     w.comp_flag = m.get<uint32_t>(N);
     // events
@@ -883,6 +888,7 @@ struct AdjTape {
     uint64_t rg_key = 0;  // the world allocation (mem_gen) the graphs were captured against
     AdjState A{};
     float ms_recompute = 0.0f, ms_reverse = 0.0f;  // device time of the last backward
+    std::vector<float> gk_scene;  // joint stiffness adjoint per scene, last backward
 };
 
 void snap_free(Snap* s) {
@@ -1019,7 +1025,9 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
         f.side_list = m.get<uint32_t>(Pc * 2); f.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
         f.cstride = Pc * 2 * 7;
         f.it_contrib = m.get<float4>(f.cstride * K);
-        if (!f.it_contrib) return AVBD_ERR_DEVICE;
+        f.it_joint = m.get<float4>((size_t)(K + 1) * 5 * W->w.J);
+        f.ccd = W->w.ccd_rec ? m.get<float4>(N * 2) : nullptr;
+        if (!f.it_contrib || !f.it_joint || (W->w.ccd_rec && !f.ccd)) return AVBD_ERR_DEVICE;
     }
     Alloc& a = t->smem;
     AdjState& A = t->A;
@@ -1031,10 +1039,25 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
     A.amu = a.get<float2>(Pc);
     A.ascene_mu = a.get<float>(W->w.S);
     A.wd = a.get<float4>(N * 3);
-    return A.wd ? AVBD_OK : AVBD_ERR_DEVICE;
+    const size_t J = (size_t)W->w.J;
+    A.jslot = a.get<float4>(J * 2 * 4);
+    A.ajs = a.get<float4>(J * 5);
+    A.ajk = a.get<float>(J);
+    return (A.wd && A.ajk) ? AVBD_OK : AVBD_ERR_DEVICE;
 }
 
 // One substep with plain launches, its frame filled on the way.
+// The joints' warm state into pose slice s of a frame.
+int adj_copy_joints(AvbdWorld* W, AdjFrame& f, int slice) {
+    cudaStream_t st = W->st;
+    const DW& w = W->w;
+    const size_t J = (size_t)w.J;
+    if (!J) return AVBD_OK;
+    float4* b = f.it_joint + (size_t)slice * 5 * J;
+    D2D(b, w.j_lam_l, J * 16); D2D(b + J, w.j_pen_l, J * 16); D2D(b + 2 * J, w.j_lam_a, J * 16);
+    D2D(b + 3 * J, w.j_pen_a, J * 16); D2D(b + 4 * J, w.j_lim, J * 16);
+    return AVBD_OK;
+}
 // What the reverse reads of a substep, copied right after its front (the
 // copies cover the frame's capacity, so that a captured graph replays them).
 int adj_copy_front(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
@@ -1052,6 +1075,8 @@ int adj_copy_front(AvbdWorld* W, AdjTape* t, AdjFrame& f) {
     D2D(f.p_np, w.p_np, P * 4); D2D(f.p_old, w.p_old, P * 4);
     D2D(f.q_ra, w.q_ra, Q * 16); D2D(f.q_rb, w.q_rb, Q * 16); D2D(f.q_matched, w.q_matched, Q * 4);
     D2D(f.it_lam, w.q_lam, Q * 16); D2D(f.it_pen, w.q_pen, Q * 16);
+    if (f.ccd) D2D(f.ccd, w.ccd_rec, N * 32);
+    adj_copy_joints(W, f, 0);
     return AVBD_OK;
 }
 // The iterations and the finish of a substep for `cover` colours, with the
@@ -1071,6 +1096,7 @@ int adj_back(AvbdWorld* W, AdjTape* t, AdjFrame& f, int cover) {
         launch_dual(w, W->tune, st);
         D2D(f.it_lam + (it + 1) * f.qstride, w.q_lam, Q * 16);
         D2D(f.it_pen + (it + 1) * f.qstride, w.q_pen, Q * 16);
+        adj_copy_joints(W, f, it + 1);
     }
     launch_finish_substep(w, W->tune, st);
     D2D(f.asleep_end, w.asleep, N * 4);
@@ -1197,6 +1223,7 @@ int adj_reverse(AvbdWorld* W, AdjTape* t, const AdjFrame& f) {
     }
     CK(cudaMemsetAsync(A.alam_old, 0, Qc * 16, st));
     CK(cudaMemsetAsync(A.apen_old, 0, Qc * 16, st));
+    if (W->w.J) CK(cudaMemsetAsync(A.jslot, 0, (size_t)W->w.J * 2 * 4 * 16, st));
     launch_adjoint_substep(W->w, f, A, W->w.iterations, st);
     CK(cudaGetLastError());
     std::swap(A.alam, A.alam_old);
@@ -1854,6 +1881,13 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
     return AVBD_OK;
 }
 
+int avbd_set_joint_stiffness(AvbdWorld* W, float k) {
+    if (!W || !std::isfinite(k) || k < 0.0f) return AVBD_ERR_INVALID_ARG;
+    W->w.joint_k = k;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
 int avbd_set_broadphase(AvbdWorld* W, int small_scene_max) {
     if (!W || small_scene_max < 0 || small_scene_max > 2048) return AVBD_ERR_INVALID_ARG;
     cudaSetDevice(W->device);
@@ -2011,7 +2045,6 @@ int avbd_world_drain_trigger_events(AvbdWorld* W, AvbdTriggerEvent* out, uint32_
 
 int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t every) {
     if (!W || steps <= 0 || substeps <= 0 || every <= 0) return AVBD_ERR_INVALID_ARG;
-    if (!W->joints.empty()) return AVBD_ERR_UNSUPPORTED;  // contact rows only
     for (const AvbdBody& b : W->bodies)
         if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f) return AVBD_ERR_UNSUPPORTED;
     int rc = begin_steps(W);
@@ -2048,6 +2081,12 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
         }
     }
     return snap_take(W, &t->fin);
+}
+
+int avbd_adjoint_grad_joint_stiffness(AvbdWorld* W, float* per_scene) {
+    if (!W || !per_scene || !W->adj || W->adj->gk_scene.empty()) return AVBD_ERR_INVALID_ARG;
+    std::copy(W->adj->gk_scene.begin(), W->adj->gk_scene.end(), per_scene);
+    return AVBD_OK;
 }
 
 int avbd_adjoint_timing(AvbdWorld* W, float* ms) {
@@ -2092,6 +2131,10 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         CK(cudaMemsetAsync(A.alam, 0, Qc * 16, st));
         CK(cudaMemsetAsync(A.apen, 0, Qc * 16, st));
         CK(cudaMemsetAsync(A.ascene_mu, 0, t->S * 4, st));
+        if (t->J) {
+            CK(cudaMemsetAsync(A.ajs, 0, (size_t)t->J * 5 * 16, st));
+            CK(cudaMemsetAsync(A.ajk, 0, (size_t)t->J * 4, st));
+        }
         CK(cudaStreamSynchronize(st));  // the staging vectors go out of scope
     }
     const int nseg = (int)t->ckpt.size();
@@ -2123,7 +2166,16 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         CK(cudaMemcpyAsync(v.data(), A.av, N * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(w.data(), A.aw, N * 16, cudaMemcpyDeviceToHost, st));
         if (grad_friction) CK(cudaMemcpyAsync(grad_friction, A.ascene_mu, t->S * 4, cudaMemcpyDeviceToHost, st));
+        std::vector<float> gk(t->J);
+        if (t->J) CK(cudaMemcpyAsync(gk.data(), A.ajk, (size_t)t->J * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        // the stiffness adjoint per scene: a joint belongs to its first body's scene
+        t->gk_scene.assign(t->S, 0.0f);
+        for (size_t j = 0; j < gk.size() && j < W->joints.size(); j++) {
+            uint32_t a = W->joints[j].a;
+            size_t sc = std::upper_bound(W->scene_off.begin(), W->scene_off.end(), a) - W->scene_off.begin() - 1;
+            if (sc < t->gk_scene.size()) t->gk_scene[sc] += gk[j];
+        }
         for (size_t h = 0; h < N; h++) {
             float* g = grad_initial + 13 * h;
             g[0] = x[h].x; g[1] = x[h].y; g[2] = x[h].z;

@@ -74,7 +74,8 @@ enum Ctr {
     C_FCAND = 13,        // candidates with a fast (swept) body, this substep
     C_BOXONE = 14,       // pairs with exactly one box (listed from the back of boxlist)
     C_NOBOX = 15,        // pairs without a box (clist)
-    C_NUM = 16
+    C_LONGSEG = 16,      // long static pair segments put in order by the chunk sort
+    C_NUM = 17
 };
 enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
 
@@ -115,6 +116,7 @@ struct DW {
     int max_cols;  // colours the launched iteration covers (a CUDA graph fixes it at capture)
     int n_large_scenes;  // host: scenes above the one-CTA sweep and colouring limit
     int sort_static;     // also order static bodies' pair segments (differentiable rollouts)
+    float joint_k;       // finite joint stiffness (0: hard joints, the reference's)
 
     const uint32_t* scene_off;  // S+1
     const uint32_t* scene_of;   // N
@@ -177,6 +179,8 @@ struct DW {
     uint32_t* cnt;     // per body counters (N+1)
     uint32_t* cur;     // per body cursors
     uint32_t* slot_c;  // final pair slot -> candidate index
+    uint32_t* long_seg;            // N: static bodies with a long pair segment (C_LONGSEG of them)
+    unsigned long long* seg_key;  // cand_cap: (b, candidate) keys of those segments, sorted per chunk
     uint32_t* boxlist; // box-box pair slots from the front, one-box pair slots from the back
     uint32_t* clist;   // pair slots without a box
     float4 *bd_pa, *bd_pb;  // box-box witnesses per pair slot: (pa, dist), (pb, SAT gap)
@@ -199,6 +203,10 @@ struct DW {
 
     // events (all null when the world keeps none)
     float4* pre_vel;      // N: linear velocity at the substep start, after torque (mod.rs:874-876)
+    // differentiable rollouts: per body, the swept impact applied this
+    // substep as [2h] = (normal, velocity factor: 0 kept, else the bounce)
+    // and [2h + 1] = (fraction of the sweep x dt, 1 when applied, 0, 0)
+    float4* ccd_rec;
     int32_t* ccd_ev_o;    // N: partner of this substep's swept-hit event, -1 none
     float4* ccd_ev_p;     // N: hit point xyz, approach speed w
     float4* ccd_ev_n;     // N: event normal (A toward B)
@@ -252,6 +260,10 @@ struct AdjFrame {
     uint32_t *side_list, *side_cnt;
     float4* it_contrib;  // iterations slices of cstride
     size_t cstride;
+    // joints: per slice (iterations + 1), 5 arrays of J float4: lambda and
+    // penalty of the anchor rows, of the hinge rows, and the limit record
+    float4* it_joint;
+    float4* ccd;  // 2N: the swept impacts of the substep (null without CCD)
 };
 // Adjoint state.  Body adjoints are of the state between substeps (pose,
 // velocities) plus per-substep accumulators; every (pair, side) incidence
@@ -267,6 +279,9 @@ struct AdjState {
     float2* amu;                  // per pair
     float* ascene_mu;             // per scene: friction coefficient adjoint
     float4* wd;                   // 3 per body: w = H^-1 d_bar and the step d of its last reversed solve
+    float4* jslot;                // 4 per (joint, side): as slot, for joint partners
+    float4* ajs;                  // 5 per joint: adjoint of its warm state (lambda, penalty, limit force in .w)
+    float* ajk;                   // per joint: adjoint of the joint stiffness, summed over the rollout
 };
 
 }  // namespace avbd

@@ -73,5 +73,58 @@ def pile(n=12, seed=1, mu=0.5):
     return arr
 
 
+def capsule_rest(mu=0.5, tilt=0.05, v=0.4):
+    """A capsule lying on the ground plane, tilted slightly about its
+    horizontal axis so one end cap touches first, sliding and turning: its
+    one witness point moves over the rounded caps (rolling anchors)."""
+    g = O.body_new(abi.SHAPE_HALFSPACE, [0, 1, 0], [0, 0, 0], 0.0)
+    c = O.body_new(abi.SHAPE_CAPSULE, [0.1, 0.2, 0.0], [0, 0.1 + 0.2 * np.sin(tilt) - 0.002, 0], 13.0)
+    # capsule axis (local y) turned to lie along x, then tilted by `tilt` about z
+    ang = np.pi / 2 - tilt
+    c.orientation[:] = [0.0, 0.0, np.sin(ang / 2), np.cos(ang / 2)]
+    c.velocity[0] = v
+    c.velocity[2] = 0.1
+    c.angular_velocity[1] = 0.5
+    return _finish([g, c], mu)
+
+
+def carpet(n=36, r=0.2, spacing=0.5, seed=2, mu=0.5):
+    """n x n spheres resting 1 mm into one ground plane with small random
+    velocities: the plane's pair segment holds n^2 slots (over 1024 for the
+    default, i.e. several chunks of the long-segment sort)."""
+    rng = np.random.default_rng(seed)
+    bs = [O.body_new(abi.SHAPE_HALFSPACE, [0, 1, 0], [0, 0, 0], 0.0)]
+    for i in range(n):
+        for k in range(n):
+            b = O.body_new(abi.SHAPE_SPHERE, [r], [spacing * i, r - 0.001, spacing * k], 1.0)
+            b.velocity[0], b.velocity[2] = 0.4 * rng.standard_normal(2)
+            bs.append(b)
+    return _finish(bs, mu)
+
+
 def dynamic_mask(arr):
     return arr["inv_mass"] > 0
+
+
+def pendulum(links=4, kind_hinge=(2,), limit=(-0.6, 0.6), v=1.5, mu=0.5, offset=0.05):
+    """A chain of capsules hanging from a static anchor, swinging without
+    contacts: ball joints, with the links in kind_hinge joined by a limited
+    hinge.  Returns (bodies, joint descriptors)."""
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 5, 0], 0.0)
+    bs = [anchor]
+    for i in range(links):
+        b = O.body_new(abi.SHAPE_CAPSULE, [0.08, 0.2], [offset * i, 5 - 0.5 * (i + 1), 0.4 * offset * i], 1.0)
+        bs.append(b)
+    bs[-1].velocity[0] = v
+    bs[-1].velocity[2] = 0.4
+    arr = _finish(bs, mu)
+    joints = []
+    for i in range(links):
+        a, b = i, i + 1
+        la = [0, -0.1, 0] if i == 0 else [0, -0.25, 0]
+        lb = [0, 0.25, 0]
+        if i in kind_hinge:
+            joints.append(abi.joint_desc(abi.JOINT_REVOLUTE, a, b, la, lb, (0, 0, 1), (0, 0, 1), limit=limit))
+        else:
+            joints.append(abi.joint_desc(abi.JOINT_BALL, a, b, la, lb))
+    return arr, joints

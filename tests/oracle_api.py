@@ -18,6 +18,7 @@ ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "libavbd_oracle.so")
 REFERENCE = 0
 COLOURED = 1
 DUAL = 2  # use_double value of an f64 dual-number (forward-mode) world
+DUAL_F32 = 3  # dual numbers whose values follow the f32 world bit for bit
 
 # fields of OracleWorld.seed
 F_POS, F_ROT, F_VEL, F_ANGVEL, F_FRICTION = 0, 1, 2, 3, 4
@@ -40,6 +41,7 @@ def lib():
         L.oracle_world_create.argtypes = [C.POINTER(abi.AvbdParams), C.c_int, C.c_int, C.c_int]
         L.oracle_world_destroy.argtypes = [vp]
         L.oracle_set_faithful_scan.argtypes = [vp, C.c_int]
+        L.oracle_set_split_sums.argtypes = [vp, C.c_int]
         L.oracle_add_bodies.argtypes = [vp, vp, C.c_uint32]
         L.oracle_add_joint.argtypes = [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(C.c_uint32)]
         L.oracle_step.argtypes = [vp, C.c_float]
@@ -81,6 +83,8 @@ def lib():
         L.oracle_dual_seed.argtypes = [vp, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_double]
         L.oracle_dual_freeze_frames.argtypes = [vp, C.c_int]
         L.oracle_dual_tangents.argtypes = [vp, vp]
+        L.oracle_set_joint_stiffness.argtypes = [vp, C.c_float]
+        L.oracle_dual_seed_joint_stiffness.argtypes = [vp, C.c_int, C.c_double]
         _lib = L
     return _lib
 
@@ -119,6 +123,11 @@ class OracleWorld:
 
     def faithful_scan(self, on=True):
         lib().oracle_set_faithful_scan(self.h, int(on))
+
+    def split_sums(self, on=True):
+        """Sum each pair's rows before they join the body's system (the
+        device's split primal launch)."""
+        lib().oracle_set_split_sums(self.h, int(on))
 
     def add_bodies(self, arr):
         arr = np.ascontiguousarray(arr)
@@ -223,6 +232,12 @@ class OracleWorld:
     def seed(self, body, field, comp, direction, value=1.0):
         """d(field[comp] of body)/d(direction) = value in the initial state."""
         assert lib().oracle_dual_seed(self.h, int(body), int(field), int(comp), int(direction), float(value)) == 0
+
+    def set_joint_stiffness(self, k):
+        assert lib().oracle_set_joint_stiffness(self.h, float(k)) == 0
+
+    def seed_joint_stiffness(self, direction, value=1.0):
+        assert lib().oracle_dual_seed_joint_stiffness(self.h, int(direction), float(value)) == 0
 
     def freeze_frames(self, on=True):
         assert lib().oracle_dual_freeze_frames(self.h, int(on)) == 0
