@@ -316,6 +316,7 @@ static __device__ __forceinline__ JState jstate_add(JState a, const JState& b) {
 // ---- BDF1 (mod.rs:1060-1078) --------------------------------------------------
 __global__ void k_adj_bdf(DW w, AdjFrame f, AdjState A, int iters) {
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h == 0) *A.nlong = 0u;
     if (h >= (uint32_t)w.N) return;
     A.ay[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     A.aqt[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -443,6 +444,9 @@ __global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState 
 // for w = H^-1 d_bar, and takes the inertial rows' adjoint; k_adj_sides (one
 // thread per (pair, side)) takes the adjoint of that side's contact rows and
 // leaves the results in the incidence slots of both bodies of the pair.
+// JOINTS = false: a world without joints (the joint code would cost it
+// registers and occupancy).
+template <bool JOINTS>
 __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A, int it, int colour) {
     const uint32_t c0 = f.col_cnt[colour], c1 = f.col_cnt[colour + 1];
     for (uint32_t i = c0 + blockIdx.x * blockDim.x + threadIdx.x; i < c1; i += gridDim.x * blockDim.x) {
@@ -457,7 +461,7 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
             sl[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             sl[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
-        const uint32_t j0 = w.J ? w.jofs[h] : 0u, j1 = w.J ? w.jofs[h + 1] : 0u;
+        const uint32_t j0 = JOINTS ? w.jofs[h] : 0u, j1 = JOINTS ? w.jofs[h + 1] : 0u;
         for (uint32_t k = j0; k < j1; k++) {
             uint32_t j = w.jlist[k];
             float4* sl = A.jslot + ((size_t)j * 2 + (w.j_ab[j].x == h ? 0u : 1u)) * 4;
@@ -528,37 +532,41 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
         quat_diff_vec_bwd(q, qt, gth, gqb, gqt);
         world_inertia_bwd(inr, q, wa, th + dang, -1.0f / dt2, gqb);
         A.aqt[h] = f4add(A.aqt[h], stq(gqt));
-        for (uint32_t k = j0; k < j1; k++) {
-            uint32_t j = w.jlist[k];
-            uint2 ab = w.j_ab[j];
-            bool is_a = ab.x == h;
-            JPose jp = is_a ? jpose(w, f, ab, it, seen_slice(f, ab.y, colour, it))
-                            : jpose(w, f, ab, seen_slice(f, ab.x, colour, it), it);
-            PairGrad pg;
-            pair_grad_zero(pg);
-            JState gs;
-            jstate_zero(gs);
-            joint_stamp_bwd(jdef(w, j), jp, jstate(w, f, j, it), is_a, w6, d6, pg, gs);
-            ajs_store(A, j, jstate_add(ajs_load(A, j), gs));
-            float4* own = A.jslot + ((size_t)j * 2 + (is_a ? 0u : 1u)) * 4;
-            float4* other = A.jslot + ((size_t)j * 2 + (is_a ? 1u : 0u)) * 4;
-            if (is_a) {
-                gxb = gxb + pg.xa;
-                gqb = qadd(gqb, pg.qa);
-                slot_add(own, V0(), Q0(), pg.xa0, pg.qa0);
-                slot_add(other, pg.xb, pg.qb, pg.xb0, pg.qb0);
-            } else {
-                gxb = gxb + pg.xb;
-                gqb = qadd(gqb, pg.qb);
-                slot_add(own, V0(), Q0(), pg.xb0, pg.qb0);
-                slot_add(other, pg.xa, pg.qa, pg.xa0, pg.qa0);
-            }
-        }
         A.ax[h] = st3(gxb, 0.0f);
         A.aq[h] = stq(gqb);
         wd[0] = make_float4(w6[0], w6[1], w6[2], w6[3]);
         wd[1] = make_float4(w6[4], w6[5], d6[0], d6[1]);
         wd[2] = make_float4(d6[2], d6[3], d6[4], d6[5]);
+    }
+}
+
+// The joint rows of the colour's bodies, one thread per (joint, side): the
+// adjoint of the side's stamp with that body's w and d.  Both bodies'
+// results go to the joint's slots; the side's own pose adjoint is gathered
+// with the rest of its slots before the body's previous update.  The two
+// bodies of a joint never share a colour, so one launch writes each joint's
+// state adjoint once.
+__global__ void __launch_bounds__(128) k_adj_joint_sides(DW w, AdjFrame f, AdjState A, int it, int colour) {
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < 2u * (uint32_t)w.J; e += gridDim.x * blockDim.x) {
+        const uint32_t j = e >> 1;
+        const bool is_a = (e & 1u) == 0u;
+        const uint2 ab = w.j_ab[j];
+        const uint32_t h = is_a ? ab.x : ab.y;
+        if (f.colour[h] != colour) continue;
+        const float4* wd = A.wd + (size_t)h * 3;
+        const float4 x0 = wd[0], x1 = wd[1], x2 = wd[2];
+        const float w6[6] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y};
+        const float d6[6] = {x1.z, x1.w, x2.x, x2.y, x2.z, x2.w};
+        JPose jp = is_a ? jpose(w, f, ab, it, seen_slice(f, ab.y, colour, it))
+                        : jpose(w, f, ab, seen_slice(f, ab.x, colour, it), it);
+        PairGrad pg;
+        pair_grad_zero(pg);
+        JState gs;
+        jstate_zero(gs);
+        joint_stamp_bwd(jdef(w, j), jp, jstate(w, f, j, it), is_a, w6, d6, pg, gs);
+        ajs_store(A, j, jstate_add(ajs_load(A, j), gs));
+        slot_add(A.jslot + ((size_t)j * 2) * 4, pg.xa, pg.qa, pg.xa0, pg.qa0);
+        slot_add(A.jslot + ((size_t)j * 2 + 1u) * 4, pg.xb, pg.qb, pg.xb0, pg.qb0);
     }
 }
 
@@ -685,19 +693,18 @@ __global__ void k_adj_c0(DW w, AdjFrame f, AdjState A) {
 }
 
 // ---- inertial targets (mod.rs:993-1018) -> the previous substep's state --------
-__global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
-    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= (uint32_t)w.N) return;
-    V3 gx = ld3(A.ax[h]), gx0 = ld3(A.ax0[h]);
-    Q gq = ldq(A.aq[h]), gq0 = ldq(A.aq0[h]);
-    const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
-    for (uint32_t k = k0; k < k1; k++) {
-        const float4* s = A.slot + (size_t)k * 4;
-        gx = gx + ld3(s[0]);
-        gq = qadd(gq, ldq(s[1]));
-        gx0 = gx0 + ld3(s[2]);
-        gq0 = qadd(gq0, ldq(s[3]));
-    }
+// The start of the substep: the pose adjoints gathered from every incidence
+// slot are taken back through the targets (and a swept impact) to the
+// previous substep's state.  A thread gathers up to START_SHORT slots; a
+// body with more (a floor under many bodies) is listed for k_adj_start_long,
+// whose block sums them in a fixed-shape tree.
+constexpr uint32_t START_SHORT = 32;
+static __device__ __forceinline__ void start_finish(const DW& w, const AdjFrame& f, const AdjState& A, uint32_t h,
+                                                    V3 gx, Q gq, V3 gx0, Q gq0) {
+    gx = gx + ld3(A.ax[h]);
+    gq = qadd(gq, ldq(A.aq[h]));
+    gx0 = gx0 + ld3(A.ax0[h]);
+    gq0 = qadd(gq0, ldq(A.aq0[h]));
     if (w.J)
         for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
             uint32_t j = w.jlist[k];
@@ -732,6 +739,54 @@ __global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
     } else {
         A.ax[h] = st3(gx + gx0, 0.0f);
         A.aq[h] = stq(qadd(gq, gq0));
+    }
+}
+__global__ void k_adj_start(DW w, AdjFrame f, AdjState A) {
+    uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= (uint32_t)w.N) return;
+    const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
+    if (k1 - k0 > START_SHORT) {
+        A.long_list[atomicAdd(A.nlong, 1u)] = h;
+        return;
+    }
+    V3 gx = V0(), gx0 = V0();
+    Q gq = Q0(), gq0 = Q0();
+    for (uint32_t k = k0; k < k1; k++) {
+        const float4* s = A.slot + (size_t)k * 4;
+        gx = gx + ld3(s[0]);
+        gq = qadd(gq, ldq(s[1]));
+        gx0 = gx0 + ld3(s[2]);
+        gq0 = qadd(gq0, ldq(s[3]));
+    }
+    start_finish(w, f, A, h, gx, gq, gx0, gq0);
+}
+__global__ void __launch_bounds__(256) k_adj_start_long(DW w, AdjFrame f, AdjState A) {
+    __shared__ float4 part[4][256];
+    const uint32_t nl = *A.nlong;
+    for (uint32_t l = blockIdx.x; l < nl; l += gridDim.x) {
+        const uint32_t h = A.long_list[l];
+        const uint32_t k0 = f.offA[h] + f.offB[h], k1 = f.offA[h + 1] + f.offB[h + 1];
+        float4 s0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), s1 = s0, s2 = s0, s3 = s0;
+        for (uint32_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+            const float4* s = A.slot + (size_t)k * 4;
+            s0 = f4add(s0, s[0]);
+            s1 = f4add(s1, s[1]);
+            s2 = f4add(s2, s[2]);
+            s3 = f4add(s3, s[3]);
+        }
+        part[0][threadIdx.x] = s0;
+        part[1][threadIdx.x] = s1;
+        part[2][threadIdx.x] = s2;
+        part[3][threadIdx.x] = s3;
+        __syncthreads();
+        for (uint32_t m = blockDim.x >> 1; m > 0; m >>= 1) {
+            if (threadIdx.x < m)
+                for (int c = 0; c < 4; c++) part[c][threadIdx.x] = f4add(part[c][threadIdx.x], part[c][threadIdx.x + m]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            start_finish(w, f, A, h, ld3(part[0][0]), ldq(part[1][0]), ld3(part[2][0]), ldq(part[3][0]));
+        __syncthreads();
     }
 }
 
@@ -796,13 +851,16 @@ void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, i
         k_adj_dual<<<gpl, 128, 0, st>>>(w, f, A, it);
         if (w.J) k_adj_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w, f, A, it);
         for (int c = (int)f.ncol - 1; c >= 0; c--) {
-            k_adj_solve<<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
+            if (w.J) k_adj_solve<true><<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
+            else k_adj_solve<false><<<nblk(w.N, 128), 128, 0, st>>>(w, f, A, it, c);
             k_adj_sides<<<gp2, 128, 0, st>>>(w, f, A, it, c);
+            if (w.J) k_adj_joint_sides<<<nblk(2 * (size_t)w.J, 128), 128, 0, st>>>(w, f, A, it, c);
         }
     }
     k_adj_c0<<<gp, 128, 0, st>>>(w, f, A);
     if (w.J) k_adj_decay_joints<<<nblk(w.J, 128), 128, 0, st>>>(w, f, A);
     k_adj_start<<<gb, 256, 0, st>>>(w, f, A);
+    k_adj_start_long<<<152, 256, 0, st>>>(w, f, A);
     k_adj_inherit<<<gp, 128, 0, st>>>(w, f, A);
     if (w.S > 0) k_adj_mu_scene<<<(unsigned)w.S, 256, 0, st>>>(w, f, A);
 }

@@ -390,6 +390,7 @@ __global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
         for (int k = 0; k < 6; k++) s.r[k] = 0.0f;
         for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, side_a, s);
         uint32_t slot = side_a ? p + w.offB[c.a + 1] : w.offA[c.b] + w.posB[p];
+        if (slot >= w.contrib_slots) continue;  // a recording frame too small: the host reports it
         float4* o = w.contrib + (size_t)slot * 7;
         o[0] = make_float4(s.h[0], s.h[1], s.h[2], s.h[3]);
         o[1] = make_float4(s.h[4], s.h[5], s.h[6], s.h[7]);
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
         uint32_t h = w.col_list[i];
         Sys s;
         inertial_block(w, h, s);
-        const uint32_t k0 = w.offA[h] + w.offB[h], k1 = w.offA[h + 1] + w.offB[h + 1];
+        const uint32_t k0 = w.offA[h] + w.offB[h], k1 = min(w.offA[h + 1] + w.offB[h + 1], w.contrib_slots);
         for (uint32_t k = k0; k < k1; k++) {
             const float4* o = w.contrib + (size_t)k * 7;
             float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];

@@ -185,7 +185,7 @@ struct AvbdWorld {
     size_t graph_nodes_emit = 0;  // ... in one that reports events
     uint64_t steps = 0;
     AdjTape* adj = nullptr;  // checkpoints of the last differentiable rollout
-    uint64_t mem_gen = 0;    // bumped whenever the device arrays are (re)allocated
+    uint64_t mem_gen = 0;    // bumped whenever the device arrays are (re)allocated or a launch setting changes
 };
 
 #define CK(x)                                    \
@@ -210,13 +210,16 @@ static void set_pair_ptrs(AvbdWorld* W) {
     w.o_offA = o.offA;
 }
 
-static void free_graphs(AvbdWorld* W) {
+// settings_changed: something a captured launch holds by value changed, so
+// the recording graphs of a differentiable rollout are stale too.
+static void free_graphs(AvbdWorld* W, bool settings_changed = true) {
     for (int i = 0; i < 2; i++)
         for (int e = 0; e < 2; e++)
             if (W->gexec[i][e]) {
                 cudaGraphExecDestroy(W->gexec[i][e]);
                 W->gexec[i][e] = nullptr;
             }
+    if (settings_changed) W->mem_gen++;
 }
 
 // Capacities: candidates are bounded by the sweep-and-prune overlaps plus the
@@ -292,6 +295,7 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.side_list = m.get<uint32_t>((size_t)cand_cap * 2);
     w.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
     w.contrib = W->tune.primal_lanes == 0 ? m.get<float4>((size_t)cand_cap * 2 * 7) : nullptr;
+    w.contrib_slots = w.contrib ? (uint32_t)(cand_cap * 2) : 0u;
     w.cand = m.get<uint2>(cand_cap);
     w.keep = m.get<uint8_t>(cand_cap);
     w.cnt = m.get<uint32_t>(N + 1);
@@ -1043,7 +1047,9 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
     A.jslot = a.get<float4>(J * 2 * 4);
     A.ajs = a.get<float4>(J * 5);
     A.ajk = a.get<float>(J);
-    return (A.wd && A.ajk) ? AVBD_OK : AVBD_ERR_DEVICE;
+    A.nlong = a.get<uint32_t>(1);
+    A.long_list = a.get<uint32_t>(N);
+    return (A.wd && A.ajk && A.long_list) ? AVBD_OK : AVBD_ERR_DEVICE;
 }
 
 // One substep with plain launches, its frame filled on the way.
@@ -1089,8 +1095,11 @@ int adj_back(AvbdWorld* W, AdjTape* t, AdjFrame& f, int cover) {
     D2D(f.side_cnt, w.side_cnt, (2 * MAX_COLOURS + 2) * 4);
     D2D(f.side_list, w.side_list, P * 2 * 4);
     for (int it = 0; it < w.iterations; it++) {
-        for (int c = 0; c < cover; c++) launch_primal_colour(w, W->tune, c, (uint32_t)w.N, st);
-        D2D(f.it_contrib + it * f.cstride, w.contrib, P * 2 * 7 * 16);
+        // the split primal writes this iteration's row sums straight into the frame
+        DW wi = w;
+        wi.contrib = f.it_contrib + it * f.cstride;
+        wi.contrib_slots = (uint32_t)(2 * P);
+        for (int c = 0; c < cover; c++) launch_primal_colour(wi, W->tune, c, (uint32_t)w.N, st);
         D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
         D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);
         launch_dual(w, W->tune, st);
@@ -1652,7 +1661,7 @@ int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
 // before its iterations (the colouring flags it) and is finished with plain
 // launches, then the graphs are re-captured wider.
 static int capture(AvbdWorld* W) {
-    free_graphs(W);
+    free_graphs(W, false);
     int base = W->cur;
     for (int emit = 0; emit < 2; emit++)
         for (int k = 0; k < 2; k++) {
@@ -1669,7 +1678,7 @@ static int capture(AvbdWorld* W) {
             cudaError_t e = cudaGraphInstantiate(&W->gexec[W->cur][emit], g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) {
-                free_graphs(W);
+                free_graphs(W, false);
                 W->cur = base;
                 set_pair_ptrs(W);
                 return AVBD_ERR_DEVICE;
@@ -1873,6 +1882,7 @@ int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
         cudaSetDevice(W->device);
         W->w.contrib = W->mem.get<float4>((size_t)W->cand_cap * 2 * 7);
         if (!W->w.contrib) return AVBD_ERR_DEVICE;
+        W->w.contrib_slots = (uint32_t)(W->cand_cap * 2);
         W->mem_gen++;
     }
     W->tune.primal_lanes = primal_lanes;
@@ -2059,8 +2069,20 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
         W->w.sort_static = 1;
         free_graphs(W);
     }
-    adj_free(W->adj);
-    AdjTape* t = W->adj = new AdjTape();
+    AdjTape* t = W->adj;
+    if (t && t->N == (uint32_t)W->w.N && t->J == (uint32_t)W->w.J && t->S == (uint32_t)W->w.S) {
+        // the same world again: keep the frames, the adjoint state and the
+        // recording graphs (still valid while the world's generation holds)
+        for (Snap* s : t->ckpt) snap_free(s);
+        t->ckpt.clear();
+        snap_free(t->fin);
+        t->fin = nullptr;
+        t->max_pairs = 0;
+        t->gk_scene.clear();
+    } else {
+        adj_free(t);
+        t = W->adj = new AdjTape();
+    }
     t->steps = steps;
     t->substeps = substeps;
     t->every = every;

@@ -166,6 +166,7 @@ struct DW {
     uint32_t* side_list;  // 2*pair_cap entries: pair * 2 + (1 for the A side, 0 for the B side)
     uint32_t* side_cnt;   // [0, MAX_COLOURS]: list starts; [MAX_COLOURS+1, 2*MAX_COLOURS+1]: cursors
     float4* contrib;      // 7 float4 per incidence slot (21 Hessian + 6 rhs + pad)
+    uint32_t contrib_slots;  // incidence slots contrib holds
     // ... and the previous generation (read by discovery for the warm merge)
     uint2* o_ab;
     float4* o_n;
@@ -282,6 +283,8 @@ struct AdjState {
     float4* jslot;                // 4 per (joint, side): as slot, for joint partners
     float4* ajs;                  // 5 per joint: adjoint of its warm state (lambda, penalty, limit force in .w)
     float* ajk;                   // per joint: adjoint of the joint stiffness, summed over the rollout
+    uint32_t* nlong;              // bodies whose incidence slots a block gathers (a floor under many bodies)
+    uint32_t* long_list;          // N: those bodies
 };
 
 }  // namespace avbd
