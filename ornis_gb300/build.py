@@ -29,7 +29,9 @@ SOURCES = [
     ("avbd_events.cu", "avbd_events.o", []),
     ("avbd_world.cu", "avbd_world.o", []),
     ("avbd_static.cu", "avbd_static.o", []),
-    ("avbd_adjoint.cu", "avbd_adjoint.o", []),
+    # the reverse sweep: contracted FMAs, approximate div/sqrt (its gradients
+    # are checked to 5e-3; it repeats bit for bit run to run on one build)
+    ("avbd_adjoint.cu", "avbd_adjoint.o", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--extended-lambda", "-Xcompiler", "-fPIC",
