@@ -451,6 +451,15 @@ int avbd_adjoint_grad_joint_stiffness(AvbdWorld* world, float* per_scene);
  * recomputes (restores included), ms[1] the reverse sweeps. */
 int avbd_adjoint_timing(AvbdWorld* world, float* ms);
 
+/* Magnitude of the adjoint along the last avbd_adjoint_backward: for each
+ * substep s of the rollout (in forward order, steps x substeps of them), the
+ * largest |component| of the body adjoints (position, orientation, velocity,
+ * angular velocity) of the state at the start of substep s, and the first
+ * body holding it; a non-finite adjoint reads as infinity.  Fills up to cap
+ * entries and sets *n to the substep count.  A diagnostic for gradients that
+ * grow without bound along a trajectory. */
+int avbd_adjoint_trace(AvbdWorld* world, float* max_abs, uint32_t* body, int32_t cap, int32_t* n);
+
 #ifdef __cplusplus
 }
 #endif

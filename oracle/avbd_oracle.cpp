@@ -1206,6 +1206,17 @@ template <class T> struct Engine {
             }
     }
 
+    // Hinge twist of a joint.  Under frozen frames the angle is held fixed
+    // once the hinge axes part by more than 120 degrees (cos^2(swing/2) < 1/4),
+    // where the twist stops being defined and its derivative has no bound.
+    T twist(Qt<T> qa, Qt<T> qb, V3<T> axis) const {
+        T t = hinge_twist(qa, qb, axis);
+        if (!freeze_frames) return t;
+        Qt<T> q = qmul(conj(qa), qb);
+        T s = dot(V3<T>{q.x, q.y, q.z}, axis);
+        return s * s + q.w * q.w < T(0.25) ? no_tangent(t) : t;
+    }
+
     // ---- contact rows (rows.rs:947-1060, joints_ext.rs:21-32) ----
     V3<T> lever_a(const Body<T>& a, V3<T> n, const Point<T>& pt) const {
         return a.shape == AVBD_SHAPE_SPHERE ? -n * a.sp.x : qrot(a.rot, pt.ra);
@@ -1377,11 +1388,11 @@ template <class T> struct Engine {
                 stamp_angular(lhs, rhs, g, j.pen_a[li], f);
             }
             if (j.has_lim) {
-                T angle = wrap_pi(hinge_twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+                T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
                 int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
                 if (st >= 0) {
                     bool lower = st == 1;
-                    T initial = wrap_pi(hinge_twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                    T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
                     T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
                     T f_raw = j.pen_a[2] * c + j.acc_lim;
                     T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
@@ -1531,11 +1542,11 @@ template <class T> struct Engine {
                     j.pen_a[li] = fmn(j.pen_a[li] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::PENALTY_MAX));
                 }
                 if (j.has_lim) {
-                    T angle = wrap_pi(hinge_twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+                    T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
                     int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
                     if (st >= 0) {
                         bool lower = st == 1;
-                        T initial = wrap_pi(hinge_twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                        T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
                         T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
                         if (std::fabs(c) >= C<T>(K::C_EPS)) {
                             T f = j.pen_a[2] * c + j.acc_lim;

@@ -78,6 +78,7 @@ def lib():
             "avbd_adjoint_forward": [vp, C.c_int32, C.c_int32, C.c_int32],
             "avbd_adjoint_backward": [vp, vp, vp, vp],
             "avbd_adjoint_timing": [vp, vp],
+            "avbd_adjoint_trace": [vp, vp, vp, C.c_int32, C.POINTER(C.c_int32)],
             "avbd_set_joint_stiffness": [vp, C.c_float],
             "avbd_adjoint_grad_joint_stiffness": [vp, vp],
         }
@@ -346,6 +347,16 @@ class AvbdWorld:
         out = np.zeros(ns.value, dtype=np.float32)
         _check(lib().avbd_adjoint_grad_joint_stiffness(self.h, abi.ptr(out)), "adjoint_grad_joint_stiffness")
         return out
+
+    def adjoint_trace(self):
+        """Per substep of the last rollout (forward order): the largest body
+        adjoint magnitude of the substep's start state and the body holding it."""
+        n = C.c_int32()
+        _check(lib().avbd_adjoint_trace(self.h, None, None, 0, C.byref(n)), "adjoint_trace")
+        mx = np.zeros(n.value, dtype=np.float32)
+        body = np.zeros(n.value, dtype=np.uint32)
+        _check(lib().avbd_adjoint_trace(self.h, abi.ptr(mx), abi.ptr(body), n.value, C.byref(n)), "adjoint_trace")
+        return mx, body
 
     def adjoint_timing(self):
         """(recompute ms, reverse ms) of the last adjoint_backward, device time."""

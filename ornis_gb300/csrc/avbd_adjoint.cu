@@ -809,6 +809,46 @@ __global__ void __launch_bounds__(256) k_adj_mu_scene(DW w, AdjFrame f, AdjState
     if (threadIdx.x == 0) A.ascene_mu[s] += part[0];
 }
 
+// The largest magnitude among the body adjoints (pose, orientation,
+// velocities) after a reversed substep, and the first body holding it; a
+// non-finite component counts as infinite.  One block, fixed reduction order.
+__global__ void __launch_bounds__(256) k_adj_trace(DW w, AdjState A, uint2* out) {
+    __shared__ float mv[256];
+    __shared__ uint32_t mb[256];
+    float best = -1.0f;
+    uint32_t bh = 0xffffffffu;
+    for (uint32_t h = threadIdx.x; h < (uint32_t)w.N; h += blockDim.x) {
+        const float4 v[4] = {A.ax[h], A.aq[h], A.av[h], A.aw[h]};
+        float m = 0.0f;
+        for (int i = 0; i < 4; i++) {
+            const float c[4] = {v[i].x, v[i].y, v[i].z, v[i].w};
+            for (int k = 0; k < 4; k++) m = isfinite(c[k]) ? fmaxf(m, fabsf(c[k])) : INFINITY;
+        }
+        if (m > best) {
+            best = m;
+            bh = h;
+        }
+    }
+    mv[threadIdx.x] = best;
+    mb[threadIdx.x] = bh;
+    __syncthreads();
+    for (uint32_t s = blockDim.x >> 1; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            float o = mv[threadIdx.x + s];
+            uint32_t ob = mb[threadIdx.x + s];
+            if (o > mv[threadIdx.x] || (o == mv[threadIdx.x] && ob < mb[threadIdx.x])) {
+                mv[threadIdx.x] = o;
+                mb[threadIdx.x] = ob;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = make_uint2(__float_as_uint(fmaxf(mv[0], 0.0f)), mb[0]);
+}
+void launch_adjoint_trace(const DW& w, const AdjState& A, uint2* out, cudaStream_t st) {
+    k_adj_trace<<<1, 256, 0, st>>>(w, A, out);
+}
+
 void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st) {
     unsigned gb = nblk(w.N, 256);
     unsigned gp = f.npairs ? nblk(f.npairs, 128) : 1u;

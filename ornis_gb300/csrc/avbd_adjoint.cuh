@@ -246,11 +246,16 @@ static __host__ __device__ __forceinline__ void f4add_at(float4& v, int k, float
 
 // hinge_twist (sequential_impulse/joints.rs:38-48): 2 atan2(q.xyz . axis, q.w)
 // of q = conj(qa) (x) qb, wrapped (the wrap is the identity almost everywhere).
+// r2 = s^2 + w^2 = cos^2(swing / 2) of q's swing-twist split: as the hinge
+// axes part by a half turn the twist angle loses its meaning and its
+// derivative 2/r2 has no bound.  Past a swing of 120 degrees (r2 < 1/4) the
+// angle is held fixed, as a contact frame is.
+constexpr float TWIST_HELD_R2 = 0.25f;
 static __host__ __device__ __forceinline__ void hinge_twist_bwd(Q qa, Q qb, V3 axis, float g, Q& gqa, Q& gqb) {
     Q q = qmul(conj(qa), qb);
     float s = dot(V3{q.x, q.y, q.z}, axis), w = q.w;
     float r2 = s * s + w * w;
-    if (!(r2 > 0.0f)) return;
+    if (!(r2 >= TWIST_HELD_R2)) return;
     float k = 2.0f * g / r2;
     Q gq{axis.x * w * k, axis.y * w * k, axis.z * w * k, -s * k};
     Q gca = Q0();

@@ -93,5 +93,6 @@ inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
 
 // reverse of one recomputed substep (avbd_adjoint.cu)
 void launch_adjoint_substep(const DW& w, const AdjFrame& f, const AdjState& A, int iters, cudaStream_t st);
+void launch_adjoint_trace(const DW& w, const AdjState& A, uint2* out, cudaStream_t st);
 
 }  // namespace avbd

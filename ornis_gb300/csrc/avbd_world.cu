@@ -893,6 +893,9 @@ struct AdjTape {
     AdjState A{};
     float ms_recompute = 0.0f, ms_reverse = 0.0f;  // device time of the last backward
     std::vector<float> gk_scene;  // joint stiffness adjoint per scene, last backward
+    uint2* d_trace = nullptr;     // per substep of the rollout: (max |body adjoint| bits, body)
+    int trace_cap = 0;
+    std::vector<uint2> trace;
 };
 
 void snap_free(Snap* s) {
@@ -908,6 +911,7 @@ void adj_free(AdjTape* t) {
     snap_free(t->fin);
     t->fmem.release();
     t->smem.release();
+    if (t->d_trace) cudaFree(t->d_trace);
     delete t;
 }
 
@@ -2109,6 +2113,18 @@ int avbd_adjoint_grad_joint_stiffness(AvbdWorld* W, float* per_scene) {
     return AVBD_OK;
 }
 
+int avbd_adjoint_trace(AvbdWorld* W, float* max_abs, uint32_t* body, int32_t cap, int32_t* n) {
+    if (!W || !n || !W->adj || (cap > 0 && (!max_abs || !body))) return AVBD_ERR_INVALID_ARG;
+    const std::vector<uint2>& tr = W->adj->trace;
+    *n = (int32_t)tr.size();
+    for (int32_t i = 0; i < cap && i < (int32_t)tr.size(); i++) {
+        uint32_t bits = tr[i].x;
+        std::memcpy(&max_abs[i], &bits, 4);
+        body[i] = tr[i].y;
+    }
+    return AVBD_OK;
+}
+
 int avbd_adjoint_timing(AvbdWorld* W, float* ms) {
     if (!W || !ms || !W->adj) return AVBD_ERR_INVALID_ARG;
     ms[0] = W->adj->ms_recompute;
@@ -2158,6 +2174,14 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         CK(cudaStreamSynchronize(st));  // the staging vectors go out of scope
     }
     const int nseg = (int)t->ckpt.size();
+    const int total = t->steps * t->substeps;
+    if (t->trace_cap < total) {
+        if (t->d_trace) cudaFree(t->d_trace);
+        t->d_trace = nullptr;
+        t->trace_cap = 0;
+        CK(cudaMalloc(&t->d_trace, (size_t)total * sizeof(uint2)));
+        t->trace_cap = total;
+    }
     cudaEvent_t ev[3];
     for (auto& e : ev) CK(cudaEventCreate(&e));
     t->ms_recompute = t->ms_reverse = 0.0f;
@@ -2168,7 +2192,10 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         const int nsub = nsteps * t->substeps;
         for (int k = 0; k < nsub && !rc; k++) rc = adj_substep(W, t, k);
         CK(cudaEventRecord(ev[1], st));
-        for (int k = nsub - 1; k >= 0 && !rc; k--) rc = adj_reverse(W, t, t->frames[k]);
+        for (int k = nsub - 1; k >= 0 && !rc; k--) {
+            rc = adj_reverse(W, t, t->frames[k]);
+            if (!rc) launch_adjoint_trace(W->w, t->A, t->d_trace + seg * t->every * t->substeps + k, st);
+        }
         CK(cudaEventRecord(ev[2], st));
         CK(cudaEventSynchronize(ev[2]));
         float a = 0.0f, b = 0.0f;
@@ -2179,6 +2206,8 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
     }
     for (auto& e : ev) cudaEventDestroy(e);
     if (rc) return rc;
+    t->trace.resize((size_t)total);
+    CK(cudaMemcpyAsync(t->trace.data(), t->d_trace, (size_t)total * sizeof(uint2), cudaMemcpyDeviceToHost, st));
     {
         std::vector<float4> x(N), q(N), v(N), w(N);
         CK(cudaMemcpyAsync(x.data(), A.ax, N * 16, cudaMemcpyDeviceToHost, st));

@@ -109,6 +109,21 @@ def test_long_floor_segment_keeps_one_order():
     np.testing.assert_allclose(rec, p.bodies()["position"], atol=1e-5)
 
 
+def test_adjoint_trace_covers_every_substep():
+    """The adjoint-magnitude trace has one entry per substep of the rollout,
+    finite on a bounded scene, the bodies named being in range."""
+    arr = S.tower()
+    wts = loss_weights(arr, seed=3)
+    w = AvbdWorld(abi.default_params(), bodies=arr)
+    r = Rollout(w, 20, 1, 7)
+    r.forward()
+    r.backward(wts.astype(np.float32))
+    mx, body = w.adjoint_trace()
+    assert len(mx) == 20 and len(body) == 20
+    assert np.all(np.isfinite(mx)) and np.all(mx > 0)
+    assert np.all(body < len(arr))
+
+
 def test_tower_batch_gradients_are_reproducible():
     """Colliding towers (the differentiable workload, 16 scenes): repeated
     backward passes and any checkpoint spacing give the same gradients bit
