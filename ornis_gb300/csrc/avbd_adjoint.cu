@@ -193,6 +193,29 @@ static __device__ __forceinline__ void adj_point_bwd(const DW& w, const AdjFrame
     glam.w += gc0;
 }
 
+// inertial block (assembly.rs:74-96) with the frame's masses and targets
+static __device__ __forceinline__ void adj_inertial(const DW& w, const AdjFrame& f, uint32_t h, V3 x, Q q, Sys& s) {
+    float dt2 = w.dt * w.dt;
+    float im = is_dynamic(w, h) ? f.inv_mass[h] : 0.0f;
+    float m_dt2 = 1.0f / im / dt2;
+    float iw[3][3];
+    world_inertia(ld3(f.inertia[h]), q, iw);
+    for (int i = 0; i < 21; i++) s.h[i] = 0.0f;
+    s.h[tri(0, 0)] = m_dt2;
+    s.h[tri(1, 1)] = m_dt2;
+    s.h[tri(2, 2)] = m_dt2;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b <= a; b++) s.h[tri(3 + a, 3 + b)] = iw[a][b] / dt2;
+    V3 rl = m_dt2 * (x - ld3(f.inertial[h]));
+    s.r[0] = rl.x;
+    s.r[1] = rl.y;
+    s.r[2] = rl.z;
+    V3 ra = mat3_vec(iw, quat_diff_vec(q, ldq(f.inertial_rot[h]))) / dt2;
+    s.r[3] = ra.x;
+    s.r[4] = ra.y;
+    s.r[5] = ra.z;
+}
+
 static __device__ __forceinline__ float4* slot_of(const AdjFrame& f, const AdjState& A, uint32_t p, bool side_a,
                                                   uint2 ab) {
     uint32_t k = side_a ? p + f.offB[ab.x + 1] : f.offA[ab.y] + f.posB[p];
@@ -415,10 +438,10 @@ __global__ void __launch_bounds__(128, 3) k_adj_dual(DW w, AdjFrame f, AdjState 
 }
 
 // ---- primal block solve of one colour (assembly.rs:73-903) --------------------
-// Passes per colour, like the forward's split primal.  k_adj_solve (one
-// thread per body) loads the system the recompute recorded before the
-// body's solve, solves for the step d and for w = H^-1 d_bar, and takes the
-// inertial rows' adjoint; k_adj_sides (one
+// Two passes per colour, like the forward's split primal.  k_adj_solve (one
+// thread per body) rebuilds the body's system from its inertial block and
+// the per-incidence row sums the recompute kept, solves for the step d and
+// for w = H^-1 d_bar, and takes the inertial rows' adjoint; k_adj_sides (one
 // thread per (pair, side)) takes the adjoint of that side's contact rows and
 // leaves the results in the incidence slots of both bodies of the pair.
 // JOINTS = false: a world without joints (the joint code would cost it
@@ -447,20 +470,29 @@ __global__ void __launch_bounds__(128) k_adj_solve(DW w, AdjFrame f, AdjState A,
             sl[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             sl[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
+        V3 x = ld3(f.it_pos[pslice(w, it) + h]);
         Q q = ldq(f.it_rot[pslice(w, it) + h]);
-        // the system the forward solved (inertial block, contact rows in
-        // incidence order, joint rows), recorded before its solve
         Sys s;
-        {
-            const float4* o = f.it_sys + ((size_t)it * (size_t)w.N + h) * 7;
+        adj_inertial(w, f, h, x, q, s);
+        const float4* cb = f.it_contrib + (size_t)it * f.cstride;
+        for (uint32_t k = k0; k < k1; k++) {  // incidence order, as the forward sums them
+            const float4* o = cb + (size_t)k * 7;
             float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];
-            s.h[0] = v0.x; s.h[1] = v0.y; s.h[2] = v0.z; s.h[3] = v0.w;
-            s.h[4] = v1.x; s.h[5] = v1.y; s.h[6] = v1.z; s.h[7] = v1.w;
-            s.h[8] = v2.x; s.h[9] = v2.y; s.h[10] = v2.z; s.h[11] = v2.w;
-            s.h[12] = v3.x; s.h[13] = v3.y; s.h[14] = v3.z; s.h[15] = v3.w;
-            s.h[16] = v4.x; s.h[17] = v4.y; s.h[18] = v4.z; s.h[19] = v4.w;
-            s.h[20] = v5.x; s.r[0] = v5.y; s.r[1] = v5.z; s.r[2] = v5.w;
-            s.r[3] = v6.x; s.r[4] = v6.y; s.r[5] = v6.z;
+            s.h[0] += v0.x; s.h[1] += v0.y; s.h[2] += v0.z; s.h[3] += v0.w;
+            s.h[4] += v1.x; s.h[5] += v1.y; s.h[6] += v1.z; s.h[7] += v1.w;
+            s.h[8] += v2.x; s.h[9] += v2.y; s.h[10] += v2.z; s.h[11] += v2.w;
+            s.h[12] += v3.x; s.h[13] += v3.y; s.h[14] += v3.z; s.h[15] += v3.w;
+            s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
+            s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
+            s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
+        }
+        for (uint32_t k = j0; k < j1; k++) {  // joints after the contact rows, as the forward
+            uint32_t j = w.jlist[k];
+            uint2 ab = w.j_ab[j];
+            bool is_a = ab.x == h;
+            JPose jp = is_a ? jpose(w, f, ab, it, seen_slice(f, ab.y, colour, it))
+                            : jpose(w, f, ab, seen_slice(f, ab.x, colour, it), it);
+            joint_stamp(jdef(w, j), jp, jstate(w, f, j, it), is_a, s);
         }
         float4* wd = A.wd + (size_t)h * 3;
         float d6[6];

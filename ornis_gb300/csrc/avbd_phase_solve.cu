@@ -421,16 +421,6 @@ __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
             s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
         }
         for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
-        if (w.sys_rec) {
-            float4* o = w.sys_rec + (size_t)h * 7;
-            o[0] = make_float4(s.h[0], s.h[1], s.h[2], s.h[3]);
-            o[1] = make_float4(s.h[4], s.h[5], s.h[6], s.h[7]);
-            o[2] = make_float4(s.h[8], s.h[9], s.h[10], s.h[11]);
-            o[3] = make_float4(s.h[12], s.h[13], s.h[14], s.h[15]);
-            o[4] = make_float4(s.h[16], s.h[17], s.h[18], s.h[19]);
-            o[5] = make_float4(s.h[20], s.r[0], s.r[1], s.r[2]);
-            o[6] = make_float4(s.r[3], s.r[4], s.r[5], 0.0f);
-        }
         apply_solve(w, h, s);
     }
 }

@@ -1031,10 +1031,11 @@ int adj_storage(AvbdWorld* W, AdjTape* t, int n, uint32_t pcap) {
         f.q_ra = m.get<float4>(Qc); f.q_rb = m.get<float4>(Qc); f.q_matched = m.get<int32_t>(Qc);
         f.it_lam = m.get<float4>(Qc * (K + 1)); f.it_pen = m.get<float4>(Qc * (K + 1));
         f.side_list = m.get<uint32_t>(Pc * 2); f.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
-        f.it_sys = m.get<float4>(N * 7 * K);
+        f.cstride = Pc * 2 * 7;
+        f.it_contrib = m.get<float4>(f.cstride * K);
         f.it_joint = m.get<float4>((size_t)(K + 1) * 5 * W->w.J);
         f.ccd = W->w.ccd_rec ? m.get<float4>(N * 2) : nullptr;
-        if (!f.it_sys || !f.it_joint || (W->w.ccd_rec && !f.ccd)) return AVBD_ERR_DEVICE;
+        if (!f.it_contrib || !f.it_joint || (W->w.ccd_rec && !f.ccd)) return AVBD_ERR_DEVICE;
     }
     Alloc& a = t->smem;
     AdjState& A = t->A;
@@ -1098,9 +1099,10 @@ int adj_back(AvbdWorld* W, AdjTape* t, AdjFrame& f, int cover) {
     D2D(f.side_cnt, w.side_cnt, (2 * MAX_COLOURS + 2) * 4);
     D2D(f.side_list, w.side_list, P * 2 * 4);
     for (int it = 0; it < w.iterations; it++) {
-        // the split primal writes each body's assembled system into the frame
+        // the split primal writes this iteration's row sums straight into the frame
         DW wi = w;
-        wi.sys_rec = f.it_sys + (size_t)it * N * 7;
+        wi.contrib = f.it_contrib + it * f.cstride;
+        wi.contrib_slots = (uint32_t)(2 * P);
         for (int c = 0; c < cover; c++) launch_primal_colour(wi, W->tune, c, (uint32_t)w.N, st);
         D2D(f.it_pos + (it + 1) * N, w.pos, N * 16);
         D2D(f.it_rot + (it + 1) * N, w.rot, N * 16);

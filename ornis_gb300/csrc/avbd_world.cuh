@@ -166,7 +166,6 @@ struct DW {
     uint32_t* side_list;  // 2*pair_cap entries: pair * 2 + (1 for the A side, 0 for the B side)
     uint32_t* side_cnt;   // [0, MAX_COLOURS]: list starts; [MAX_COLOURS+1, 2*MAX_COLOURS+1]: cursors
     float4* contrib;      // 7 float4 per incidence slot (21 Hessian + 6 rhs + pad)
-    float4* sys_rec;      // recording a differentiable rollout: 7 float4 per body, its system before the solve
     uint32_t contrib_slots;  // incidence slots contrib holds
     // ... and the previous generation (read by discovery for the warm merge)
     uint2* o_ab;
@@ -260,7 +259,8 @@ struct AdjFrame {
     // split primal: per-colour side lists and, per iteration, the 7 float4
     // row sums of every incidence slot
     uint32_t *side_list, *side_cnt;
-    float4* it_sys;  // iterations slices of N x 7: each body's assembled system before its solve
+    float4* it_contrib;  // iterations slices of cstride
+    size_t cstride;
     // joints: per slice (iterations + 1), 5 arrays of J float4: lambda and
     // penalty of the anchor rows, of the hinge rows, and the limit record
     float4* it_joint;
