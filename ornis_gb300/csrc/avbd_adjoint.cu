@@ -113,22 +113,6 @@ static __device__ __forceinline__ void friction_levers_bwd(const PairCtx& c, V3 
     pg.xa = pg.xa + c.n * gsep;
     pg.xb = pg.xb - c.n * gsep;
 }
-// A capsule's witness anchor (taken this substep, not kept from a stuck
-// point, and not a box corner's projection) is the closest point of its
-// rounded surface: segment point + s R0^T n in the body frame (s = -r on
-// side A, +r on side B).  Held fixed as a material point instead, its
-// lever would not roll with the body, and the linearised iteration of a
-// capsule resting on its cap grows without bound; the anchor adjoint g
-// therefore reaches the step-start orientation q0.
-static __device__ __forceinline__ void rolling_anchor_bwd(Q q0, V3 n, float s, V3 g, Q& gq0) {
-    Q gc = Q0();
-    V3 dummy = V0();
-    qrot_bwd(conj(q0), n, g * s, gc, dummy);
-    gq0.x -= gc.x;
-    gq0.y -= gc.y;
-    gq0.z -= gc.z;
-    gq0.w += gc.w;
-}
 // contact_levers (rows.rs:963-973): a non-sphere lever is the anchor rotated
 // by the body; a sphere's is fixed by the (frozen) normal.
 static __device__ __forceinline__ void contact_levers_bwd(const PairCtx& c, Q qa0, Q qb0, float4 ra, float4 rb,

@@ -244,6 +244,23 @@ static __host__ __device__ __forceinline__ void f4add_at(float4& v, int k, float
     else v.w += a;
 }
 
+// A capsule's witness anchor (taken this substep, not kept from a stuck
+// point, and not a box corner's projection) is the closest point of its
+// rounded surface: segment point + s R0^T n in the body frame (s = -r on
+// side A, +r on side B).  Held fixed as a material point instead, its
+// lever would not roll with the body, and the linearised iteration of a
+// capsule resting on its cap grows without bound; the anchor adjoint g
+// therefore reaches the step-start orientation q0.
+static __host__ __device__ __forceinline__ void rolling_anchor_bwd(Q q0, V3 n, float s, V3 g, Q& gq0) {
+    Q gc = Q0();
+    V3 dummy = V0();
+    qrot_bwd(conj(q0), n, g * s, gc, dummy);
+    gq0.x -= gc.x;
+    gq0.y -= gc.y;
+    gq0.z -= gc.z;
+    gq0.w += gc.w;
+}
+
 // hinge_twist (sequential_impulse/joints.rs:38-48): 2 atan2(q.xyz . axis, q.w)
 // of q = conj(qa) (x) qb, wrapped (the wrap is the identity almost everywhere).
 // r2 = s^2 + w^2 = cos^2(swing / 2) of q's swing-twist split: as the hinge
