@@ -402,6 +402,12 @@ def run_ours(args):
     return 0
 
 
+def finite(x):
+    """A JSON-safe float: None for NaN and infinities."""
+    x = float(x)
+    return x if math.isfinite(x) else None
+
+
 def adjoint_rate(args):
     """The differentiable batch (diff_1024): recorded forward with checkpoints,
     then the reverse sweep, against the plain graph-replayed forward."""
@@ -443,6 +449,7 @@ def adjoint_rate(args):
         bwd_s = time.perf_counter() - t0
         first_s = bwd_s if first_s is None else first_s
     rec_ms, rev_ms = w.adjoint_timing()
+    amax, _ = w.adjoint_trace()
     w.close()
     gv = g0[ball, 7:10]
     return {"workload": "diff_1024", "scenes": int(len(offs) - 1), "dynamic_bodies": ndyn, "steps": steps,
@@ -454,8 +461,9 @@ def adjoint_rate(args):
             "adjoint_steps_per_s": steps / bwd_s, "adjoint_body_steps_per_s": ndyn * steps / bwd_s,
             "backward_over_forward": bwd_s / fwd_s, "loss": loss,
             "backward_split_ms_per_step": {"recompute": rec_ms / steps, "reverse": rev_ms / steps},
-            "grad_ball_velocity_mean": [float(x) for x in gv.mean(axis=0)],
-            "grad_friction_mean": float(np.mean(gmu)),
+            "grad_ball_velocity_mean": [finite(x) for x in gv.mean(axis=0)],
+            "grad_friction_mean": finite(np.mean(gmu)),
+            "adjoint_max_abs": finite(np.max(amax)) if len(amax) else None,
             "how": "wall time with the host waiting; backward = per-segment recompute from the checkpoint "
                    "plus the reverse sweep; forward = the same rollout by CUDA-graph replay with the faster "
                    "of the two primal launches (the rollout itself runs the split primal); the second of two "
@@ -519,6 +527,7 @@ def ragdoll_adjoint_rate(args):
         first_s = bwd_s if first_s is None else first_s
     gk = w.adjoint_grad_joint_stiffness()
     rec_ms, rev_ms = w.adjoint_timing()
+    amax, _ = w.adjoint_trace()
     w.close()
     return {"workload": "ragdoll_8192" if args.ragdoll_counts == "3000,5192" else f"ragdolls_{args.ragdoll_counts}",
             "scenes": int(len(offs) - 1), "dynamic_bodies": ndyn, "joints": len(joints),
@@ -531,7 +540,8 @@ def ragdoll_adjoint_rate(args):
             "adjoint_steps_per_s": steps / bwd_s, "adjoint_body_steps_per_s": ndyn * steps / bwd_s,
             "backward_over_forward": bwd_s / fwd_s,
             "backward_split_ms_per_step": {"recompute": rec_ms / steps, "reverse": rev_ms / steps},
-            "com_height": com, "grad_com_height_wrt_stiffness": [float(x) for x in gk],
+            "com_height": com, "grad_com_height_wrt_stiffness": [finite(x) for x in gk],
+            "adjoint_max_abs": finite(np.max(amax)) if len(amax) else None,
             "how": "as the differentiable batch: wall time with the host waiting; loss per scene = final "
                    "centre-of-mass height of its dynamic bodies"}
 
