@@ -95,3 +95,55 @@ def test_dual_values_equal_f64_run():
     a = run(arr, True, steps=20).state13()
     d = run(arr, O.DUAL, steps=20, seeds=[(1, O.F_POS, 0, 0)]).state13()
     np.testing.assert_array_equal(a, d)
+
+
+def _world(arr, use_double, joints=(), k=0.0, seeds=(), freeze=0, params=None):
+    w = O.OracleWorld(params or abi.default_params(), mode=O.COLOURED, use_double=use_double)
+    w.add_bodies(arr)
+    for j in joints:
+        assert w.add_joint(j)[0] == 0
+    w.set_joint_stiffness(k)
+    for s in seeds:
+        w.seed(*s)
+    if freeze:
+        w.freeze_frames(freeze)
+    return w
+
+
+def _swept_sphere():
+    """A small fast sphere crossing a thin wall within one step: a swept
+    impact (time of impact clamp and bounce) every time it reaches it."""
+    g = O.body_new(abi.SHAPE_HALFSPACE, [0, 1, 0], [0, 0, 0], 0.0)
+    wall = O.body_new(abi.SHAPE_BOX, [0.05, 1.0, 1.0], [2.0, 1.0, 0.0], 0.0)
+    ball = O.body_new(abi.SHAPE_SPHERE, [0.05], [0.0, 0.5, 0.1], 1.0)
+    ball.velocity[0] = 45.0
+    ball.restitution = 0.5
+    return S._finish([g, wall, ball], 0.4)
+
+
+@pytest.mark.parametrize("case", ["capsule_rest", "ragdoll", "swept"])
+def test_frozen_conventions_change_no_value(case):
+    """The frozen-frame conventions of the dual world (rolling capsule
+    anchors, the hinge twist held past a 120-degree swing, the swept
+    impact's time of impact, normal and bounce) drop tangents only: its
+    trajectory is the f64 world's bit for bit."""
+    joints, k, steps = (), 0.0, 60
+    if case == "capsule_rest":
+        arr = S.capsule_rest()
+    elif case == "ragdoll":
+        from ornis_gb300 import scenes
+        arr, _, joints = scenes.ragdolls(counts=(1,), seed=4)
+        k, steps = 2e4, 90
+    else:
+        arr = _swept_sphere()
+    b = len(arr) - 1
+    seeds = [(b, O.F_VEL, 0, 0), (b, O.F_ANGVEL, 1, 1), (1, O.F_POS, 1, 2)]
+    plain = _world(arr, True, joints, k)
+    dual = _world(arr, O.DUAL, joints, k, seeds=seeds, freeze=7)
+    for _ in range(steps):
+        plain.step_fixed(1)
+        dual.step_fixed(1)
+    np.testing.assert_array_equal(plain.state13(), dual.state13())
+    assert np.all(np.isfinite(dual.tangents()))
+    if case == "swept":
+        assert dual.counters().ccd_hits > 0
