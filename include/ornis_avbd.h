@@ -424,7 +424,8 @@ int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uin
  * (avbd_set_tuning lanes 0) and orders every body's contact pairs (the
  * static bodies' too), which the world keeps afterwards; retuning the
  * world before the backward invalidates the recording.  A new forward
- * replaces the previous recording. */
+ * replaces the previous recording and, on the same world, keeps its frame
+ * storage and recording graphs. */
 int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int32_t checkpoint_every);
 
 /* Reverse-mode gradient of a scalar loss of the recorded rollout's final
@@ -434,9 +435,13 @@ int avbd_adjoint_forward(AvbdWorld* world, int32_t steps, int32_t substeps, int3
  * null, grad_friction: one float per scene, dLoss/d(mu) for a friction
  * coefficient mu that every body of the scene shares (pair friction is the
  * larger of the two bodies', so it moves with mu).  The contact set, the
- * contact frames (normal, friction basis, local anchors) and the colouring
- * are held at the values of the recorded rollout; the step-start gap stays a
- * function of the step-start poses.  Each segment between checkpoints is
+ * contact frames (normal, friction basis, local anchors; a capsule's
+ * witness anchor rolls with the body) and the colouring are held at the
+ * values of the recorded rollout, and so are a swept impact's time of
+ * impact, normal and bounce, and a hinge's twist angle once its axes part
+ * by more than 120 degrees; the step-start gap stays a function of the
+ * step-start poses.  Joint rows are differentiated (see
+ * avbd_adjoint_grad_joint_stiffness).  Each segment between checkpoints is
  * recomputed from its checkpoint.  The world is left at the end of the
  * recorded rollout. */
 int avbd_adjoint_backward(AvbdWorld* world, const float* grad_final, float* grad_initial, float* grad_friction);

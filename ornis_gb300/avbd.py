@@ -368,7 +368,9 @@ class AvbdWorld:
 class Rollout:
     """A differentiable rollout as a forward/backward pair over one world:
     forward() advances and records, backward(dloss_dfinal) returns the
-    gradients of the initial state and of each scene's friction."""
+    gradients of the initial state and of each scene's friction; the joint
+    stiffness gradient per scene follows from
+    world.adjoint_grad_joint_stiffness()."""
 
     def __init__(self, world, steps, substeps=1, checkpoint_every=10):
         self.world = world
