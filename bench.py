@@ -156,6 +156,24 @@ def dist_init(n_gpus):
     return dist, rank, dist.get_world_size(), local
 
 
+def combine_ranks(dist, device, worst=(), total=()):
+    """The job-wide view of per-rank numbers: the max over ranks of each of
+    `worst` (times) and the sum of each of `total` (counts).  `device` is
+    where the collective's tensor lives ("cuda:<n>" under NCCL, "cpu" under
+    gloo)."""
+    import torch
+
+    out = []
+    for vals, op in ((worst, dist.ReduceOp.MAX), (total, dist.ReduceOp.SUM)):
+        if not vals:
+            out.append([])
+            continue
+        t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=op)
+        out.append([float(x) for x in t.cpu().tolist()])
+    return out[0], out[1]
+
+
 def workload(args):
     """(bodies, scene offsets, joints, params, substeps) of the chosen workload."""
     if args.workload == "ragdoll_8192":
@@ -305,14 +323,8 @@ def run_ours(args):
     clk.mark(t0, time.perf_counter())
     clk.__exit__()
     if d:
-        import torch
-
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        d[0].all_reduce(t, op=d[0].ReduceOp.MAX)
-        ms = float(t.item())
-        nd = torch.tensor([float(ndyn)], device=f"cuda:{device}")
-        d[0].all_reduce(nd)
-        ndyn_total = int(nd.item())
+        (ms,), (nd,) = combine_ranks(d[0], f"cuda:{device}", worst=[ms], total=[ndyn])
+        ndyn_total = int(nd)
     else:
         ndyn_total = ndyn
     value = ndyn_total * args.steps / (ms / 1e3)
@@ -344,11 +356,8 @@ def run_ours(args):
     d2h += ev_bytes // max(1, e2e_steps)
     e2e = ndyn * e2e_steps / e2e_s
     if d:
-        import torch
-
-        t = torch.tensor([e2e_s], device=f"cuda:{device}")
-        d[0].all_reduce(t, op=d[0].ReduceOp.MAX)
-        e2e = ndyn_total * e2e_steps / float(t.item())
+        (e2e_max,), _ = combine_ranks(d[0], f"cuda:{device}", worst=[e2e_s])
+        e2e = ndyn_total * e2e_steps / e2e_max
     w.close()
     if rank != 0:
         return 0

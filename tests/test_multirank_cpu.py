@@ -1,0 +1,79 @@
+"""The multi-GPU bench path's host logic on the CPU, with two gloo ranks.
+
+Scenes are independent, so ranks shard them with no exchange: rank r takes
+the scenes s with s mod N == r (bench.shard).  The job-wide numbers are the
+max over ranks of the times and the sum of the bodies (bench.combine_ranks,
+the same code the bench runs under NCCL)."""
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+NSCENES = 12
+WORLD = 2
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, port, q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+
+    import bench
+    from ornis_gb300 import scenes
+
+    dist.init_process_group("gloo", rank=rank, world_size=WORLD)
+    try:
+        bodies, offs, _ = scenes.batched(NSCENES)
+        mine, my_offs = bench.shard(bodies, offs, rank, WORLD)
+        ndyn = scenes.dynamic_count(mine)
+        seconds = 1.5 + rank  # rank 1 is the slower one
+        worst, total = bench.combine_ranks(dist, "cpu", worst=[seconds], total=[ndyn, len(my_offs) - 1])
+        dist.barrier()
+        q.put((rank, mine, my_offs, worst, total))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_scenes_and_combine_timing():
+    import torch.multiprocessing as mp
+
+    from ornis_gb300 import scenes
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, port, q)) for r in range(WORLD)]
+    for p in procs:
+        p.start()
+    got = {}
+    try:
+        for _ in range(WORLD):
+            rank, mine, my_offs, worst, total = q.get(timeout=120)
+            got[rank] = (mine, my_offs, worst, total)
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.kill()
+    assert all(p.exitcode == 0 for p in procs)
+
+    bodies, offs, _ = scenes.batched(NSCENES)
+    # every scene exactly once, on rank s mod N, in order
+    for s in range(NSCENES):
+        mine, my_offs, _, _ = got[s % WORLD]
+        k = s // WORLD
+        np.testing.assert_array_equal(mine[my_offs[k]:my_offs[k + 1]], bodies[offs[s]:offs[s + 1]])
+    for r in range(WORLD):
+        _, _, worst, total = got[r]
+        assert worst == [1.5 + WORLD - 1]  # the slowest rank's time, on every rank
+        assert total == [float(scenes.dynamic_count(bodies)), float(NSCENES)]
