@@ -249,6 +249,58 @@ def cpu_baseline(bodies, offs, params, nsub, start, steps, per_core=3):
     }
 
 
+def _cpu_adjoint_worker(args):
+    """One tower scene's gradients by the f64 dual-number oracle: the ball's
+    initial velocity (3 directions) and the scene friction (1), frozen
+    frames, `steps` steps timed (values and derivatives in one pass)."""
+    bodies, ball, params_tuple, nsub, steps = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+
+    p = abi.default_params(step_dt=params_tuple[0], iterations=params_tuple[1])
+    w = O.OracleWorld(p, mode=O.REFERENCE, use_double=O.DUAL)
+    w.add_bodies(bodies)
+    for c in range(3):
+        w.seed(ball, O.F_VEL, c, c)
+    for i in range(len(bodies)):
+        w.seed(i, O.F_FRICTION, 0, 3)
+    w.freeze_frames(7)
+    t0 = time.perf_counter()
+    w.step_fixed(nsub * steps)
+    w.tangents()
+    return time.perf_counter() - t0, steps
+
+
+def adjoint_cpu_baseline(bodies, offs, ball, params, nsub, steps, per_core=1):
+    """Scene-steps/s of the differentiable batch's gradients on the host
+    cores: the dual-number oracle (forward mode, the four directions the
+    workload asks for) on a seeded sample of scenes, one process per core."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    S = len(offs) - 1
+    rng = np.random.default_rng(54321)
+    chosen = [int(s) for s in rng.permutation(S)[: min(S, cores * per_core)]]
+    jobs = [(bodies[offs[s]:offs[s + 1]], int(ball[s] - offs[s]), (params.step_dt, params.iterations), nsub, steps)
+            for s in chosen]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_adjoint_worker, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    busy = sum(r[0] for r in res)
+    scene_steps = sum(r[1] for r in res)
+    return {
+        "value": scene_steps / (busy / cores),
+        "unit": "gradient scene-steps/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{len(chosen)} of {S} scenes (seeded random), {steps} steps each by the f64 dual-number "
+                  f"oracle (reference order, frozen frames; ball velocity and friction directions); one "
+                  f"process per core; rate = scene-steps / (summed scene seconds / cores); wall {wall:.1f} s",
+    }
+
+
 # ---------------------------------------------------------------------------
 def run_reference(args):
     d = dist_init(args.gpus)
@@ -461,6 +513,9 @@ def adjoint_rate(args):
     amax, _ = w.adjoint_trace()
     w.close()
     gv = g0[ball, 7:10]
+    cpu = None
+    if args.adjoint_cpu_per_core > 0:
+        cpu = adjoint_cpu_baseline(bodies, offs, ball, params, nsub, steps, per_core=args.adjoint_cpu_per_core)
     return {"workload": "diff_1024", "scenes": int(len(offs) - 1), "dynamic_bodies": ndyn, "steps": steps,
             "checkpoint_every": every, "dt": 1 / 60, "iterations": params.iterations, "precision": "fast",
             "forward_ms_per_step": 1e3 * fwd_s / steps, "forward_device_ms_per_step": fwd_dev_ms / steps,
@@ -473,6 +528,8 @@ def adjoint_rate(args):
             "grad_ball_velocity_mean": [finite(x) for x in gv.mean(axis=0)],
             "grad_friction_mean": finite(np.mean(gmu)),
             "adjoint_max_abs": finite(np.max(amax)) if len(amax) else None,
+            "gradient_scene_steps_per_s": (len(offs) - 1) * steps / (rec_s + bwd_s),
+            "cpu_baseline": cpu,
             "how": "wall time with the host waiting; backward = per-segment recompute from the checkpoint "
                    "plus the reverse sweep; forward = the same rollout by CUDA-graph replay with the faster "
                    "of the two primal launches (the rollout itself runs the split primal); the second of two "
@@ -599,6 +656,8 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--adjoint-scenes", type=int, default=1024, help="differentiable batch size (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=120)
+    ap.add_argument("--adjoint-cpu-per-core", type=int, default=1,
+                    help="differentiable-batch scenes per host core for the dual-number CPU baseline (0: skip)")
     ap.add_argument("--ragdoll-adjoint-steps", type=int, default=240,
                     help="steps of the articulated forward+adjoint measurement (0: skip)")
     ap.add_argument("--adjoint-only", action="store_true",
