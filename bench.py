@@ -4,12 +4,15 @@ Workload (default): batched_4096 — 4096 independent scenes of log-uniform
 8..1024 bodies (boxes and spheres dropped into a 20x20 bin), dt 1/120 s,
 2 substeps, 8 iterations, f32, 240 steps.  A "step" is one 1/60 s frame =
 2 substeps of every scene.  body-steps/s = dynamic bodies x steps / seconds.
-Every rate below covers the same trajectory: K steps from the initial drop
-(K = --steps, default 240), so the cheap falling phase and the contact-heavy
-piles at the end weigh as they do in the workload.
+Every rate below covers the same steps of the workload's 240-step
+trajectory: all 240 by default; with --steps K < 240, K steps spread evenly
+over the trajectory (step i of the sample is trajectory step
+floor((i + 1/2) 240 / K); the steps between them run untimed), so the cheap
+falling phase and the contact-heavy piles at the end weigh as they do in the
+workload; --start S times the contiguous window [S, S + K) instead.
 
   value        device time of the K graph-replayed steps, state resident in
-               HBM (CUDA events on the world's stream).
+               HBM (CUDA events on the world's stream around each timed step).
   e2e          the same K steps through the C ABI with host buffers: every
                step uploads all body records, steps, downloads all body
                records and drains the contact events (host wall clock
@@ -24,6 +27,11 @@ piles at the end weigh as they do in the workload.
   cpu_baseline the oracle's Reference-mode step (the reference's own serial
                algorithm restated in C++) on the host cores, a bounded sample
                of the same scenes over the same K steps, one process per core.
+  parity       part of the oracle leg: sampled scenes of the batch at the end
+               of the trajectory, each stepped from the device's state by the
+               oracle (Coloured order, f32 and f64) while the device steps the
+               whole batch in the benchmarked configuration; integer outputs
+               compared exactly, poses relative to max(1, |x|).
 
 Warm-up steps run from the initial state and the world is then reset to it,
 so the timed trajectory starts at step 0.  The primal launch shape is
@@ -197,31 +205,72 @@ def shard(bodies, offs, rank, world):
     return np.concatenate(parts), np.asarray(new_offs, dtype=np.uint32)
 
 
+TRAJECTORY_STEPS = 240  # the batched and articulated workloads' trajectories
+
+
+def timed_steps(args, total=TRAJECTORY_STEPS):
+    """Trajectory steps the timed region covers (the state before each)."""
+    if args.start is not None:
+        return list(range(args.start, args.start + args.steps))
+    if args.steps >= total:
+        return list(range(args.steps))
+    return [int((i + 0.5) * total / args.steps) for i in range(args.steps)]
+
+
+def describe_steps(steps):
+    if steps == list(range(steps[0], steps[0] + len(steps))):
+        return f"steps {steps[0]}..{steps[0] + len(steps)} from the initial drop"
+    stride = steps[1] - steps[0] if len(steps) > 1 else 0
+    return (f"{len(steps)} single steps spread over the {TRAJECTORY_STEPS}-step trajectory (steps {steps[0]}, "
+            f"{steps[0] + stride}, ..., {steps[-1]}; the steps between them run untimed)")
+
+
+def run_sampled(step_untimed, step_timed, steps):
+    """Advance through `steps` (sorted trajectory indices): untimed steps up to
+    each, then one timed step; returns the summed timed quantity.  A
+    contiguous window is timed by one call."""
+    if steps == list(range(steps[0], steps[0] + len(steps))):
+        if steps[0]:
+            step_untimed(steps[0])
+        return step_timed(len(steps))
+    total, cur = 0.0, 0
+    for t in steps:
+        if t > cur:
+            step_untimed(t - cur)
+        total += step_timed(1)
+        cur = t + 1
+    return total
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle's Reference-mode step, one process per core.
 # ---------------------------------------------------------------------------
 def _cpu_scene_worker(args):
-    """Step one scene `start` steps untimed, then time `steps` steps of the oracle."""
-    bodies, params_tuple, nsub, start, steps = args
+    """Step one scene through the trajectory, timing the oracle on the sampled steps."""
+    bodies, params_tuple, nsub, steps = args
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_api as O
 
     p = abi.default_params(step_dt=params_tuple[0], iterations=params_tuple[1])
     w = O.OracleWorld(p, mode=O.REFERENCE)
     w.add_bodies(bodies)
-    if start:
-        w.step_fixed(nsub * start)
-    t0 = time.perf_counter()
-    w.step_fixed(nsub * steps)
-    return time.perf_counter() - t0, scenes.dynamic_count(bodies) * steps
+
+    def timed(k):
+        t0 = time.perf_counter()
+        w.step_fixed(nsub * k)
+        return time.perf_counter() - t0
+
+    secs = run_sampled(lambda k: w.step_fixed(nsub * k), timed, steps)
+    return secs, scenes.dynamic_count(bodies) * len(steps)
 
 
-def cpu_baseline(bodies, offs, params, nsub, start, steps, per_core=3):
+def cpu_baseline(bodies, offs, params, nsub, steps, per_core=3):
     """Body-steps/s of the oracle's Reference step on a seeded sample of scenes.
 
-    Each sampled scene runs steps [start, start + steps) of its trajectory;
-    scenes run one process per core and the rate is sampled body-steps over
-    the summed per-scene seconds divided by cores.
+    Each sampled scene runs its trajectory and is timed on `steps` (the
+    trajectory steps the device is timed on); scenes run one process per
+    core and the rate is sampled body-steps over the summed per-scene seconds
+    divided by cores.  The spread of the per-scene rates is reported too.
     """
     import multiprocessing as mp
 
@@ -229,7 +278,7 @@ def cpu_baseline(bodies, offs, params, nsub, start, steps, per_core=3):
     S = len(offs) - 1
     rng = np.random.default_rng(12345)
     chosen = [int(s) for s in rng.permutation(S)[: min(S, cores * per_core)]]
-    jobs = [(bodies[offs[s]:offs[s + 1]], (params.step_dt, params.iterations), nsub, start, steps) for s in chosen]
+    jobs = [(bodies[offs[s]:offs[s + 1]], (params.step_dt, params.iterations), nsub, steps) for s in chosen]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -238,13 +287,17 @@ def cpu_baseline(bodies, offs, params, nsub, start, steps, per_core=3):
     busy = sum(r[0] for r in res)
     body_steps = sum(r[1] for r in res)
     mean_n = float(np.mean([offs[s + 1] - offs[s] for s in chosen]))
+    # the sample's own spread: the rate of each half of the sampled scenes
+    halves = [res[0::2], res[1::2]]
+    half_rates = [sum(r[1] for r in h) / (sum(r[0] for r in h) / cores) for h in halves if h]
     return {
         "value": body_steps / (busy / cores),
         "unit": "body-steps/s",
         "cores": cores,
         "kind": "port",
+        "half_sample_rates": half_rates,
         "sample": f"{len(chosen)} of {S} scenes (seeded random, mean {mean_n:.0f} bodies incl. 5 planes), "
-                  f"steps {start}..{start + steps} x {nsub} substeps timed per scene; one process per core; "
+                  f"timed on {describe_steps(steps)} x {nsub} substeps per scene; one process per core; "
                   f"rate = body-steps / (summed scene seconds / cores); wall {wall:.1f} s",
     }
 
@@ -296,9 +349,71 @@ def adjoint_cpu_baseline(bodies, offs, ball, params, nsub, steps, per_core=1):
         "cores": cores,
         "kind": "port",
         "sample": f"{len(chosen)} of {S} scenes (seeded random), {steps} steps each by the f64 dual-number "
-                  f"oracle (reference order, frozen frames; ball velocity and friction directions); one "
+                  f"oracle (reference order, frozen frames; ball velocity and friction directions seeded: 4 of "
+                  f"the 8 tangents the dual type always carries, so the host does about twice the tangent "
+                  f"arithmetic the 4 directions need, in f64 where the device computes in f32); one "
                   f"process per core; rate = scene-steps / (summed scene seconds / cores); wall {wall:.1f} s",
     }
+
+
+def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
+    """Part of the oracle leg: per-step parity of the benchmarked world
+    against the oracle on a seeded sample of its scenes, at the world's
+    current state.  Each step, every sampled scene's state is exported from
+    the device and loaded into an f32 and an f64 oracle world (Coloured
+    order; rows summed per pair when the device runs the split launch); the
+    device steps the whole batch in the benchmarked configuration and the
+    oracles step their scene.  Integer outputs (pair sets, points per pair,
+    contact IDs, colours) are compared exactly; poses relative to
+    max(1, |x|), velocities x dt."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+    import parity as P
+
+    S = len(offs) - 1
+    rng = np.random.default_rng(2468)
+    sizes = np.diff(offs)
+    # half the sample from the largest scenes (the deepest piles), half random
+    big = [int(x) for x in np.argsort(-sizes, kind="stable")[: nscenes // 2]]
+    rest = [int(x) for x in rng.permutation(S) if int(x) not in big][: nscenes - len(big)]
+    chosen = big + rest
+    worst = {"f32": 0.0, "f64": 0.0, "f32_oracle_vs_f64": 0.0, "vel_f32": 0.0}
+    same = True
+    st = w.export_state()
+    for _ in range(steps):
+        ors = []
+        for sc in chosen:
+            sub = P.scene_state(st, offs, sc)
+            pair = []
+            for dbl in (False, True):
+                o = O.OracleWorld(params, mode=O.COLOURED, use_double=dbl)
+                o.split_sums(split)
+                o.add_bodies(sub["bodies"])
+                o.import_state(sub)
+                o.step_fixed(nsub)
+                pair.append(o)
+            ors.append(pair)
+        w.step_graph(nsub)
+        st = w.export_state()
+        cols = w.colours()
+        for sc, (o32, o64) in zip(chosen, ors):
+            sg = P.scene_state(st, offs, sc)
+            a0, a1 = int(offs[sc]), int(offs[sc + 1])
+            ok, pe, ve = P.scene_step_errors(o32.export_state(), sg, o32.colours(), cols[a0:a1], params.step_dt)
+            same &= ok
+            worst["f32"] = max(worst["f32"], pe)
+            worst["vel_f32"] = max(worst["vel_f32"], ve)
+            s64 = o64.export_state()
+            worst["f64"] = max(worst["f64"], P.pose_errors(sg["bodies"], s64["bodies"], params.step_dt)[0])
+            worst["f32_oracle_vs_f64"] = max(worst["f32_oracle_vs_f64"],
+                                             P.pose_errors(o32.export_state()["bodies"], s64["bodies"],
+                                                           params.step_dt)[0])
+    return {"max_pose_rel_err": worst["f32"], "max_vel_err_x_dt": worst["vel_f32"], "vs_f64": worst["f64"],
+            "oracle_f32_vs_f64": worst["f32_oracle_vs_f64"], "integers_identical": bool(same),
+            "bar": P.POSE_RTOL, "scenes": chosen, "bodies": [int(sizes[c]) for c in chosen], "steps": steps,
+            "how": "per step from the device's state: the device steps the whole batch (benchmarked launch "
+                   "shape, precision and graph replay), f32 and f64 oracles (Coloured order, per-pair row "
+                   "sums) step each sampled scene; pose error relative to max(1, |x|)"}
 
 
 # ---------------------------------------------------------------------------
@@ -308,13 +423,14 @@ def run_reference(args):
         return 0
     bodies, offs, counts = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
-    cb = cpu_baseline(bodies, offs, params, nsub, start=args.start, steps=args.steps, per_core=args.cpu_per_core)
+    steps = timed_steps(args)
+    cb = cpu_baseline(bodies, offs, params, nsub, steps, per_core=args.cpu_per_core)
     v = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes)",
             "config": {"workload": "batched_4096", "scenes": args.scenes, "dt": 1 / 120, "substeps": nsub,
-                       "iterations": params.iterations},
+                       "iterations": params.iterations, "trajectory": describe_steps(steps)},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -347,16 +463,17 @@ def run_ours(args):
 
         w.step_graph(nsub * args.tune_at)  # piles formed: where the primal costs most
         tuned = autotune(w, substeps_per_trial=2 * nsub)
+    steps = timed_steps(args)
     clk = Clocks(device).__enter__()
     atexit.register(clk.__exit__)
     clk.wait_first()
     for _ in range(args.warmup):
         w.step_graph(nsub)
     w.import_state(s0)
-    if args.start:
-        w.step_graph(nsub * args.start)
-    w.sync()
     if args.profile_region:
+        if steps[0]:
+            w.step_graph(nsub * steps[0])
+        w.sync()
         # only the kernels of these steps are collected by `ncu --profile-from-start off`;
         # they run from the state the timed region starts at, which is restored afterwards
         from ornis_gb300.avbd import lib as _lib
@@ -367,11 +484,13 @@ def run_ours(args):
         w.sync()
         _lib().avbd_profiler(0)
         w.import_state(snap)
-    # ---- timed region: K steps, device time -------------------------------
+        w.import_state(s0)
+    w.sync()
+    # ---- timed region: K steps of the trajectory, device time --------------
     if d:
         d[0].barrier()
     t0 = time.perf_counter()
-    ms = w.step_timed(nsub * args.steps, use_graph=True)
+    ms = run_sampled(lambda k: w.step_graph(nsub * k), lambda k: w.step_timed(nsub * k, use_graph=True), steps)
     clk.mark(t0, time.perf_counter())
     clk.__exit__()
     if d:
@@ -382,34 +501,47 @@ def run_ours(args):
     value = ndyn_total * args.steps / (ms / 1e3)
     launches_per_step = w.graph_nodes() * (nsub - 1) + w.graph_nodes_emit()
     c = w.counters()
+    # ---- parity of the benchmarked configuration at the end of the trajectory
+    par = None
+    if args.parity_scenes > 0 and not joints_all:
+        lanes = tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)
+        par = oracle_parity(w, offs, params, nsub, nscenes=args.parity_scenes, steps=args.parity_steps,
+                            split=lanes == 0)
     # ---- per-phase profile at the end of the trajectory: primal roofline ---
     phases, info = w.profile_substep()
     split = (tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)) == 0
     roof = roofline.primal_roofline(phases, info, hbm_peak(), split=split)
-    roof["state"] = f"one profiled substep after step {args.start + args.steps}"
-    # ---- e2e through the C ABI with host buffers, same trajectory ----------
-    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    roof["state"] = "one profiled substep at the end of the trajectory"
+    # ---- e2e through the C ABI with host buffers, same trajectory steps ----
+    e2e_steps = steps if args.e2e_steps is None else timed_steps(argparse.Namespace(
+        start=args.start, steps=args.e2e_steps))
     w.import_state(s0)
-    if args.start:
-        w.step_graph(nsub * args.start)
-    host = w.bodies()
     w.contact_events()
-    h2d = d2h = host.nbytes
-    ev_bytes = 0
+    io = {"host": None, "ev": 0}
+
+    def e2e_untimed(k):
+        w.step_graph(nsub * k)
+        w.contact_events()
+
+    def e2e_timed(k):
+        io["host"] = w.bodies()  # the state the caller holds (untimed)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            w.set_bodies(io["host"])
+            w.step_graph(nsub)
+            io["host"] = w.bodies()
+            io["ev"] += w.contact_events().nbytes
+        return time.perf_counter() - t0
+
     if d:
         d[0].barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        w.set_bodies(host)
-        w.step_graph(nsub)
-        host = w.bodies()
-        ev_bytes += w.contact_events().nbytes
-    e2e_s = time.perf_counter() - t0
-    d2h += ev_bytes // max(1, e2e_steps)
-    e2e = ndyn * e2e_steps / e2e_s
+    e2e_s = run_sampled(e2e_untimed, e2e_timed, e2e_steps)
+    h2d = d2h = io["host"].nbytes
+    d2h += io["ev"] // max(1, len(e2e_steps))
+    e2e = ndyn * len(e2e_steps) / e2e_s
     if d:
         (e2e_max,), _ = combine_ranks(d[0], f"cuda:{device}", worst=[e2e_s])
-        e2e = ndyn_total * e2e_steps / e2e_max
+        e2e = ndyn_total * len(e2e_steps) / e2e_max
     w.close()
     if rank != 0:
         return 0
@@ -428,8 +560,7 @@ def run_ours(args):
         rag = ragdoll_adjoint_rate(args)
     cb = None
     if args.cpu_per_core > 0 and world == 1 and not joints_all:
-        cb = cpu_baseline(bodies_all, offs_all, params, nsub, start=args.start, steps=args.steps,
-                          per_core=args.cpu_per_core)
+        cb = cpu_baseline(bodies_all, offs_all, params, nsub, steps, per_core=args.cpu_per_core)
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -437,7 +568,7 @@ def run_ours(args):
         "config": {"workload": args.workload, "scenes": len(offs_all) - 1, "dynamic_bodies": ndyn_total,
                    "joints": len(joints_all),
                    "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations,
-                   "trajectory": f"steps {args.start}..{args.start + args.steps} from the initial drop",
+                   "trajectory": describe_steps(steps),
                    "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
                    "graph": True, "precision": "exact" if args.exact else "fast",
                    "primal_launch": {"lanes": tuned[0][0], "block": tuned[0][1], "min_blocks_per_sm": tuned[0][2],
@@ -445,10 +576,11 @@ def run_ours(args):
                                      "trials_ms": [[list(cd), round(m, 3)] for cd, m in tuned[1]]}
                    if tuned else {"lanes": args.lanes if args.lanes is not None else 1, "block": args.block}},
         "e2e": {"value": e2e, "unit": "body-steps/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "steps": e2e_steps},
+                "steps": len(e2e_steps)},
         "gpu_launches": int(launches_per_step * args.steps),
         "roofline": roof,
         "cpu_baseline": cb,
+        "parity": par,
         "clocks": clk.summary(),
         "plain_one_scene": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
@@ -621,17 +753,18 @@ def plain_rate(bodies, offs, params, nsub, args):
     pick = rng.choice(S, size=min(args.plain_scenes, S), replace=False)
     tot_ms = 0.0
     body_steps = 0
+    steps = timed_steps(args)
     for s in pick:
         sc = bodies[offs[s]:offs[s + 1]]
         wd = AvbdWorld(params, bodies=sc)
-        if args.start:
-            wd.step_fixed(nsub * args.start)
-        tot_ms += wd.step_timed(nsub * args.steps, use_graph=False)
-        body_steps += scenes.dynamic_count(sc) * args.steps
+        tot_ms += run_sampled(lambda k: wd.step_fixed(nsub * k), lambda k: wd.step_timed(nsub * k, use_graph=False),
+                              steps)
+        body_steps += scenes.dynamic_count(sc) * len(steps)
         wd.close()
     return {"value": body_steps / (tot_ms / 1e3), "unit": "body-steps/s", "scenes_sampled": int(len(pick)),
-            "steps": args.steps,
-            "how": "one world per scene, plain launches, each scene over the same steps, device time summed"}
+            "steps": len(steps),
+            "how": "one world per scene, plain launches, each scene over the same trajectory steps, device time "
+                   "summed"}
 
 
 def main():
@@ -643,7 +776,12 @@ def main():
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--workload", default="batched_4096", choices=["batched_4096", "ragdoll_8192"],
                     help="ragdoll_8192: 8192 15-capsule ragdolls with ball/hinge joints in two scenes")
-    ap.add_argument("--start", type=int, default=0, help="untimed steps before the timed region")
+    ap.add_argument("--start", type=int, default=None,
+                    help="time the contiguous window [start, start + steps) instead of steps spread over the "
+                         "trajectory")
+    ap.add_argument("--parity-scenes", type=int, default=8,
+                    help="scenes of the oracle parity check at the end of the trajectory (0: skip)")
+    ap.add_argument("--parity-steps", type=int, default=3)
     ap.add_argument("--tune-at", type=int, default=150, help="step at which the primal launch is autotuned")
     ap.add_argument("--e2e-steps", type=int, default=None, help="default: --steps")
     ap.add_argument("--plain-scenes", type=int, default=16)

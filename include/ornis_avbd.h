@@ -243,8 +243,11 @@ int avbd_world_add_hull(AvbdWorld* world, const float* verts, uint32_t nverts, c
  * last body moves into the freed handle; pairs and joints of the removed
  * body are dropped, the others renumbered; trigger pairs of the removed body
  * report Exited, touches and queued contact events are cleared, every
- * sleeping body wakes.  An invalid handle is a no-op.  One-scene worlds only
- * (AVBD_ERR_UNSUPPORTED for a batch). */
+ * sleeping body wakes.  A pair whose two handles change order under the
+ * renumbering is dropped at once: the reference keeps it until its next
+ * discovery drops it (it never matches again), so stepping is the same, but
+ * an export taken right after the removal lacks it.  An invalid handle is a
+ * no-op.  One-scene worlds only (AVBD_ERR_UNSUPPORTED for a batch). */
 int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
 
 /* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529), Ball and Revolute. */
@@ -401,15 +404,20 @@ int avbd_set_joint_stiffness(AvbdWorld* world, float k);
  * callers that cannot call cudaMalloc (an engine that owns every device
  * allocation through its own pools, a process whose device memory is capped
  * or fully reserved).  All device scratch is one file-scope device array of
- * AVBD_STATIC_SCRATCH_BYTES, resolved on the first call on each device with
- * that device current (make that first call before any stream capture).
- * The results equal an AvbdWorld created from the same bodies and advanced
- * by avbd_world_step_fixed(substeps).  Each call starts fresh: no contact
- * warm start carries over from an earlier call.  Calls share the array, so
- * calls that overlap on the GPU (two host threads, two streams) race.
- * Returns AVBD_ERR_CAPACITY for more than AVBD_STATIC_MAX_BODIES bodies or
- * when a substep finds more than AVBD_STATIC_PAIR_CAP candidates (out is then
- * not written), AVBD_ERR_NONFINITE for a non-finite body. */
+ * AVBD_STATIC_SCRATCH_BYTES on the caller's current device; its address is
+ * looked up on every call.  The first call on a device loads the library's
+ * device code and with it the array (CUDA's lazy module loading): make that
+ * first call before any stream capture and before the caller reserves or
+ * caps device memory, or run with CUDA_MODULE_LOADING=EAGER.  Later calls
+ * allocate nothing.  The results equal an AvbdWorld created from the same
+ * bodies and advanced by avbd_world_step_fixed(substeps).  Each call starts
+ * fresh: no contact warm start carries over from an earlier call.  Calls
+ * share the array, so calls that overlap on the GPU (two host threads, two
+ * streams) race.  Returns AVBD_ERR_CAPACITY for more than
+ * AVBD_STATIC_MAX_BODIES bodies, when a substep finds more than
+ * AVBD_STATIC_PAIR_CAP candidates, or when a substep needs more than 64
+ * colours; out is then not written.  AVBD_ERR_NONFINITE for a non-finite
+ * body. */
 int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uint32_t n, int32_t substeps,
                            AvbdBody* out);
 

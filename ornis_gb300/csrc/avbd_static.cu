@@ -19,11 +19,17 @@
 // must start at zero is cleared at the start of the call), so two calls that
 // overlap on the GPU — from two host threads, or on two streams — race on
 // the array and must not be issued.
+//
+// The first call on a device is where the CUDA runtime loads this library's
+// device code (lazy module loading, the default): loading places the array
+// and the kernels in device memory.  A caller that reserves or caps device
+// memory must therefore make one call on each device before it does so (or
+// run with CUDA_MODULE_LOADING=EAGER, which loads everything when the
+// context is created); the calls after that allocate nothing.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "avbd_kernels.h"
 
@@ -39,25 +45,19 @@ constexpr size_t STATIC_BYTES = AVBD_STATIC_SCRATCH_BYTES;
 
 // The scratch of the allocation-free entry point.  In host code this name is
 // only a host-side stand-in: its device address comes from
-// cudaGetSymbolAddress, taken once per device by static_base() below.
+// cudaGetSymbolAddress (static_base() below).
 static __device__ __align__(256) unsigned char g_scene_scratch[STATIC_BYTES];
 
 namespace {
 
-std::mutex g_mu;
-void* g_base[64] = {nullptr};  // device address of g_scene_scratch, per device ordinal
-
-// First call on a device: resolve the array's device address with that
-// device current (the caller's current device).
-int static_base(int dev, unsigned char** out) {
-    if (dev < 0 || dev >= 64) return AVBD_ERR_DEVICE;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_base[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_scene_scratch) != cudaSuccess || !p) return AVBD_ERR_DEVICE;
-        g_base[dev] = p;
-    }
-    *out = (unsigned char*)g_base[dev];
+// The array's device address on the caller's current device.  It is looked
+// up on every call (a table lookup once the module is loaded), so a context
+// that was reset and re-created (cudaDeviceReset) gets the new address and
+// never a stale one; the first lookup on a device loads the module.
+int static_base(unsigned char** out) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scene_scratch) != cudaSuccess || !p) return AVBD_ERR_DEVICE;
+    *out = (unsigned char*)p;
     return AVBD_OK;
 }
 
@@ -162,10 +162,8 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
         if (!std::isfinite(bodies[i].mass) || !std::isfinite(bodies[i].inv_mass)) return AVBD_ERR_NONFINITE;
         if (bodies[i].shape == AVBD_SHAPE_HULL) return AVBD_ERR_UNSUPPORTED;  // hull tables live in worlds
     }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return AVBD_ERR_DEVICE;
     unsigned char* base = nullptr;
-    int rc = static_base(dev, &base);
+    int rc = static_base(&base);
     if (rc) return rc;
     const uint32_t N = n, S = 1;
     cudaStream_t st = cudaStreamPerThread;
@@ -333,10 +331,14 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
         for (int it = 0; it < w.iterations; it++) launch_iteration(w, tune, ncol, st);
         launch_finish_substep(w, tune, st);
     }
+    if (colour_overflow) {
+        // more colours than a launch covers: out is left untouched
+        return cudaStreamSynchronize(st) == cudaSuccess ? AVBD_ERR_CAPACITY : AVBD_ERR_DEVICE;
+    }
     k_static_out<<<1, MAXB, 0, st>>>(w, stage, N);
     if (cudaGetLastError() != cudaSuccess) return AVBD_ERR_DEVICE;
     if (cudaMemcpyAsync(out, stage, sizeof(AvbdBody) * N, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return AVBD_ERR_DEVICE;
-    return colour_overflow ? AVBD_ERR_CAPACITY : AVBD_OK;
+    return AVBD_OK;
 }

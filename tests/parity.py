@@ -79,3 +79,28 @@ def compare_states(so, sg, dt, o=None, g=None, rtol=POSE_RTOL):
     assert pe <= rtol, f"pose error {pe:.3e} > {rtol}"
     assert ve <= rtol, f"velocity error (x dt) {ve:.3e} > {rtol}"
     return pe, ve
+
+
+def scene_state(st, offs, s):
+    """Scene s of a multi-scene state with scene-local handles (what a
+    one-scene world of that scene would export).  Contact IDs are point slots
+    within a pair, so they need no renumbering."""
+    a0, a1 = int(offs[s]), int(offs[s + 1])
+    pairs = st["pairs"]
+    m = (pairs["a"] >= a0) & (pairs["a"] < a1)
+    sp = pairs[m].copy()
+    sp["a"] -= a0
+    sp["b"] -= a0
+    pts = st["points"].reshape(-1, abi.MAX_POINTS)[m].reshape(-1).copy()
+    return dict(bodies=st["bodies"][a0:a1].copy(), aux=st["aux"][a0:a1].copy(), pairs=sp, points=pts,
+                joints=np.zeros(0, dtype=abi.JOINT_STATE_DTYPE))
+
+
+def scene_step_errors(so, sg, co, cg, dt):
+    """Per-step comparison of one scene without asserting: (integers identical,
+    pose error, velocity error x dt)."""
+    ro, io = pair_table(so)
+    rg, ig = pair_table(sg)
+    same = ro.shape == rg.shape and np.array_equal(ro, rg) and np.array_equal(io, ig) and np.array_equal(co, cg)
+    pe, ve = pose_errors(sg["bodies"], so["bodies"], dt)
+    return bool(same), pe, ve

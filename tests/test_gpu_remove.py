@@ -24,6 +24,18 @@ def test_remove_body_then_step_matches_oracle():
         g.remove_body(h)
         assert g.body_count == o.nbodies
         np.testing.assert_array_equal(g.bodies()["mass"], o.bodies()["mass"])
+        # the state right after the removal: the reference keeps a renumbered
+        # pair whose (a, b) order flipped until its next discovery drops it;
+        # the device drops it at once (its pair list is kept in (a, b) order).
+        # Everything else is the same state.
+        so, sg = o.export_state(), g.export_state()
+        keep = so["pairs"]["a"] < so["pairs"]["b"]
+        so = dict(so, pairs=so["pairs"][keep],
+                  points=so["points"].reshape(-1, abi.MAX_POINTS)[keep].reshape(-1))
+        ro, io = P.pair_table(so)
+        rg, ig = P.pair_table(sg)
+        assert np.array_equal(ro, rg) and np.array_equal(io, ig)
+        assert P.pose_errors(sg["bodies"], so["bodies"], params.step_dt) == (0.0, 0.0)
         # the first step after a removal runs from each side's own state: the
         # reference keeps renumbered pairs whose (a, b) order flipped until its
         # next discovery drops them, the device drops them at once

@@ -1,17 +1,25 @@
-"""The allocation-free entry point (avbd_scene_step_static) against a world.
+"""The allocation-free entry point (avbd_scene_step_static) against a world
+and against the CPU oracle.
 
-Callers that cannot allocate device memory step a small scene through one
-fixed device array; the results must match an AvbdWorld stepped from the same
-bodies.  Two calls in a row: the second, on a different and smaller scene,
-also shows that nothing left in the shared array by the first leaks into it.
-This file is collected last, so it runs both alone and after every other test.
+Callers that cannot allocate device memory (an engine that hands out device
+memory only from its own pools, a process whose device memory is capped or
+already reserved) step a small scene through one fixed device array; the
+results must match an AvbdWorld stepped from the same bodies and the oracle
+(Coloured order, the order the device sweeps in).  Two calls in a row: the
+second, on a different and smaller scene, also shows that nothing left in the
+shared array by the first leaks into it, and that it allocates no device
+memory (the device's free memory is the same before and after it).  This
+file is collected last, so it runs both alone and after every other test.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
 from ornis_gb300 import abi, scenes
-from ornis_gb300.avbd import AvbdError, AvbdWorld, scene_step_static
+from ornis_gb300.avbd import AvbdError, AvbdWorld, lib, scene_step_static
 
+import oracle_api as O
 import parity as P
 
 pytestmark = pytest.mark.gpu
@@ -27,6 +35,22 @@ def world_result(params, bodies, substeps):
     return out
 
 
+def oracle_result(params, bodies, substeps):
+    o = O.OracleWorld(params, mode=O.COLOURED)
+    o.add_bodies(bodies)
+    o.step_fixed(substeps)
+    return o.bodies()
+
+
+def device_free_bytes():
+    """cudaMemGetInfo's free bytes, from the CUDA runtime the library uses."""
+    lib()  # the library (and with it libcudart) is loaded
+    rt = C.CDLL("libcudart.so.13")
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
 def assert_close(got, ref, dt):
     pe, ve = P.pose_errors(got, ref, dt)
     assert pe <= P.POSE_RTOL, f"pose error {pe:.3e} > {P.POSE_RTOL}"
@@ -40,12 +64,17 @@ def test_static_step_matches_world_on_two_calls():
     assert len(first) <= abi.STATIC_MAX_BODIES
 
     got1 = scene_step_static(params, first, SUBSTEPS)
+    free_before = device_free_bytes()
     got2 = scene_step_static(params, second, SUBSTEPS)
+    free_after = device_free_bytes()
+    assert free_after == free_before, f"the second call changed free device memory by {free_before - free_after} B"
     ref1 = world_result(params, first, SUBSTEPS)
     ref2 = world_result(params, second, SUBSTEPS)
 
     assert_close(got1, ref1, params.step_dt)
     assert_close(got2, ref2, params.step_dt)
+    assert_close(got1, oracle_result(params, first, SUBSTEPS), params.step_dt)
+    assert_close(got2, oracle_result(params, second, SUBSTEPS), params.step_dt)
     # the scenes moved (a no-op would not be a test)
     assert np.abs(got1["position"] - first["position"]).max() > 1e-3
     # records other than the state pass through unchanged
