@@ -357,14 +357,15 @@ def adjoint_cpu_baseline(bodies, offs, ball, params, nsub, steps, per_core=1):
 
 
 def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
-    """Part of the oracle leg: per-step parity of the benchmarked world
+    """Part of the oracle leg: per-substep parity of the benchmarked world
     against the oracle on a seeded sample of its scenes, at the world's
-    current state.  Each step, every sampled scene's state is exported from
-    the device and loaded into an f32 and an f64 oracle world (Coloured
-    order; rows summed per pair when the device runs the split launch); the
-    device steps the whole batch in the benchmarked configuration and the
-    oracles step their scene.  Integer outputs (pair sets, points per pair,
-    contact IDs, colours) are compared exactly; poses relative to
+    current state, for `steps` steps.  Before every substep, each sampled
+    scene's state is exported from the device and loaded into an f32 and an
+    f64 oracle world (Coloured order; rows summed per pair when the device
+    runs the split or per-scene launch); the device steps the whole batch one
+    substep (the reference's step_inner) in the benchmarked configuration
+    and the oracles step their scene.  Integer outputs (pair sets, points per
+    pair, contact IDs, colours) are compared exactly; poses relative to
     max(1, |x|), velocities x dt."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_api as O
@@ -380,7 +381,7 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
     worst = {"f32": 0.0, "f64": 0.0, "f32_oracle_vs_f64": 0.0, "vel_f32": 0.0}
     same = True
     st = w.export_state()
-    for _ in range(steps):
+    for _ in range(steps * nsub):
         ors = []
         for sc in chosen:
             sub = P.scene_state(st, offs, sc)
@@ -390,10 +391,10 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
                 o.split_sums(split)
                 o.add_bodies(sub["bodies"])
                 o.import_state(sub)
-                o.step_fixed(nsub)
+                o.step_fixed(1)
                 pair.append(o)
             ors.append(pair)
-        w.step_graph(nsub)
+        w.step_graph(1)
         st = w.export_state()
         cols = w.colours()
         for sc, (o32, o64) in zip(chosen, ors):
@@ -410,8 +411,9 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
                                                            params.step_dt)[0])
     return {"max_pose_rel_err": worst["f32"], "max_vel_err_x_dt": worst["vel_f32"], "vs_f64": worst["f64"],
             "oracle_f32_vs_f64": worst["f32_oracle_vs_f64"], "integers_identical": bool(same),
-            "bar": P.POSE_RTOL, "scenes": chosen, "bodies": [int(sizes[c]) for c in chosen], "steps": steps,
-            "how": "per step from the device's state: the device steps the whole batch (benchmarked launch "
+            "bar": P.POSE_RTOL, "scenes": chosen, "bodies": [int(sizes[c]) for c in chosen],
+            "substeps": steps * nsub,
+            "how": "per substep from the device's state: the device steps the whole batch (benchmarked launch "
                    "shape, precision and graph replay), f32 and f64 oracles (Coloured order, per-pair row "
                    "sums) step each sampled scene; pose error relative to max(1, |x|)"}
 
@@ -506,11 +508,13 @@ def run_ours(args):
     if args.parity_scenes > 0 and not joints_all:
         lanes = tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)
         par = oracle_parity(w, offs, params, nsub, nscenes=args.parity_scenes, steps=args.parity_steps,
-                            split=lanes == 0)
+                            split=lanes <= 0)
     # ---- per-phase profile at the end of the trajectory: primal roofline ---
     phases, info = w.profile_substep()
-    split = (tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)) == 0
-    roof = roofline.primal_roofline(phases, info, hbm_peak(), split=split)
+    lanes = tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)
+    kind = "scene" if info["primal_launches"] == 1 and lanes < 0 else (
+        "split" if lanes <= 0 else ("thread" if lanes == 1 else "lanes"))
+    roof = roofline.primal_roofline(phases, info, hbm_peak(), kind=kind, iterations=params.iterations)
     roof["state"] = "one profiled substep at the end of the trajectory"
     # ---- e2e through the C ABI with host buffers, same trajectory steps ----
     e2e_steps = steps if args.e2e_steps is None else timed_steps(argparse.Namespace(

@@ -310,8 +310,15 @@ int avbd_world_get_colours(AvbdWorld* world, int32_t* colours, uint32_t n);
 int avbd_body_init(AvbdBody* out, uint32_t shape, const float* params, const float* position, float mass);
 
 /* Launch shape of the primal kernel: lanes cooperating on one body (1, 4, 8,
- * 16 or 32) and threads per block.  No reference counterpart (the reference
- * sweeps on one CPU thread); picked by the autotuner in ornis_gb300/tune.py. */
+ * 16 or 32) and threads per block; 0 = the split launch (per colour, one
+ * thread per (pair, side) for the rows, then one per body for the sums and
+ * the solve); AVBD_PRIMAL_SCENES = the per-scene solve (one block takes a
+ * scene through every iteration of a substep — all colours' primal and the
+ * dual — in one launch per substep; block 128, 256 or 512; the split
+ * arithmetic; a world with a scene above 2048 bodies runs the split launches
+ * instead).  No reference counterpart (the reference sweeps on one CPU
+ * thread); picked by the autotuner in ornis_gb300/tune.py. */
+#define AVBD_PRIMAL_SCENES (-1)
 int avbd_set_tuning(AvbdWorld* world, int primal_lanes, int primal_block);
 
 /* Arithmetic of the iteration kernels: 0 (default) = exact build, the same

@@ -15,6 +15,8 @@
 #include <limits>
 #include <type_traits>
 
+#include "avbd_crmath.hpp"
+
 namespace orc {
 
 constexpr int DUAL_DIRS = 8;
@@ -129,18 +131,18 @@ template <class V> inline orc::DualT<V> fmod(const orc::DualT<V>& x, const orc::
     return r;
 }
 template <class V> inline orc::DualT<V> sin(const orc::DualT<V>& a) {
-    return orc::dual_apply(a, std::sin(a.v), std::cos(double(a.v)));
+    return orc::dual_apply(a, orc::osin(a.v), std::cos(double(a.v)));
 }
 template <class V> inline orc::DualT<V> cos(const orc::DualT<V>& a) {
-    return orc::dual_apply(a, std::cos(a.v), -std::sin(double(a.v)));
+    return orc::dual_apply(a, orc::ocos(a.v), -std::sin(double(a.v)));
 }
 template <class V> inline orc::DualT<V> asin(const orc::DualT<V>& a) {
     double c = 1.0 - double(a.v) * double(a.v);
-    return orc::dual_apply(a, std::asin(a.v), c > 0.0 ? 1.0 / std::sqrt(c) : 0.0);
+    return orc::dual_apply(a, orc::oasin(a.v), c > 0.0 ? 1.0 / std::sqrt(c) : 0.0);
 }
 template <class V> inline orc::DualT<V> atan2(const orc::DualT<V>& y, const orc::DualT<V>& x) {
     orc::DualT<V> r;
-    r.v = std::atan2(y.v, x.v);
+    r.v = orc::oatan2(y.v, x.v);
     double xv = double(x.v), yv = double(y.v);
     double r2 = xv * xv + yv * yv;
     double k = r2 > 0.0 ? 1.0 / r2 : 0.0;

@@ -38,6 +38,13 @@
 
 namespace orc {
 
+// sin, cos, asin, atan2 of the step: correctly rounded for f32 (the platform
+// libm's results, avbd_crmath.hpp), std's for f64, the dual rules for duals
+template <class V> inline DualT<V> osin(const DualT<V>& a) { return std::sin(a); }
+template <class V> inline DualT<V> ocos(const DualT<V>& a) { return std::cos(a); }
+template <class V> inline DualT<V> oasin(const DualT<V>& a) { return std::asin(a); }
+template <class V> inline DualT<V> oatan2(const DualT<V>& y, const DualT<V>& x) { return std::atan2(y, x); }
+
 // ---- constants (avbd/mod.rs:154-247, constants.rs:26-79) -------------------
 struct K {
     static constexpr float ALPHA = 0.99f;
@@ -593,7 +600,7 @@ template <class T> static Qt<T> quat_integrate(Qt<T> q, V3<T> v) {  // :110-119
     T theta = len(v);
     if (theta < C<T>(K::NEAR_ZERO)) return q;
     T hth = C<T>(K::HALF) * theta;
-    T s = std::sin(hth), c = std::cos(hth);
+    T s = osin(hth), c = ocos(hth);
     T k = s / theta;
     Qt<T> dq = qmul(Qt<T>{v.x * k, v.y * k, v.z * k, c}, q);
     return qnormalize(dq);
@@ -604,7 +611,7 @@ template <class T> static V3<T> quat_diff_vec(Qt<T> a, Qt<T> b) {  // :128-146
     if (r.w < T(0)) xyz = -xyz;
     T s = fmn(len(xyz), T(1));
     if (s < C<T>(K::NEAR_ZERO)) return VZERO<T>();
-    return xyz * (T(2) * std::asin(s) / s);
+    return xyz * (T(2) * oasin(s) / s);
 }
 template <class T> static T rem_euclid(T x, T m) {
     T r = std::fmod(x, m);
@@ -612,7 +619,7 @@ template <class T> static T rem_euclid(T x, T m) {
 }
 template <class T> static T wrap_pi(T x) { return rem_euclid(x + C<T>(K::PI), C<T>(K::TAU)) - C<T>(K::PI); }
 template <class T> static T quat_twist(Qt<T> q, V3<T> axis) {  // sequential_impulse/joints.rs:44-48
-    T t = T(2) * std::atan2(dot(V3<T>{q.x, q.y, q.z}, axis), q.w);
+    T t = T(2) * oatan2(dot(V3<T>{q.x, q.y, q.z}, axis), q.w);
     return rem_euclid(t + C<T>(K::PI), C<T>(K::TAU)) - C<T>(K::PI);
 }
 template <class T> static T hinge_twist(Qt<T> qa, Qt<T> qb, V3<T> axis) { return quat_twist(qmul(conj(qa), qb), axis); }

@@ -43,6 +43,9 @@ JOINT_REVOLUTE = 1
 
 MAX_POINTS = 8
 
+# avbd_set_tuning lanes value of the per-scene solve (one block per scene)
+PRIMAL_SCENES = -1
+
 F3 = C.c_float * 3
 F4 = C.c_float * 4
 

@@ -12,8 +12,11 @@ namespace avbd {
 
 struct Tune {
     int primal_lanes = 1;        // lanes cooperating on one body in the primal (1, 4, 8, 16, 32);
-                                 // 0: split primal (per (pair, side) rows, then per-body sums and solve)
-    int primal_block = 128;      // threads per block of the primal kernel
+                                 // 0: split primal (per (pair, side) rows, then per-body sums and solve);
+                                 // -1: per-scene solve (one block takes a scene through all
+                                 // iterations; split arithmetic; worlds with a scene above
+                                 // SCENE_MAX_BODIES run the split launches instead)
+    int primal_block = 128;      // threads per block of the primal kernel (per-scene solve: 128, 256, 512)
     int primal_minb = 4;         // resident blocks per SM the thread-per-body primal is built for
     int small_scene_max = 2048;  // scenes up to this many bodies use the one-CTA broadphase
     int fast = 0;                // 1: the fast build of the iteration kernels
@@ -63,7 +66,8 @@ void launch_events(const DW& w, int emit, int triggers, uint32_t* scan_tmp, cuda
     void launch_finish_substep(const DW& w, cudaStream_t st);                                             \
     void launch_primal_colour(const DW& w, const Tune& tune, int colour, uint32_t max_bodies, cudaStream_t st); \
     void launch_dual(const DW& w, const Tune& tune, cudaStream_t st);                                   \
-    void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st);
+    void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st);                               \
+    void launch_scene_solve(const DW& w, const Tune& tune, cudaStream_t st);
 namespace exact {
 AVBD_SOLVE_DECLS
 }
@@ -85,6 +89,15 @@ inline void launch_primal_colour(const DW& w, const Tune& t, int c, uint32_t max
 inline void launch_solve_prep(const DW& w, const Tune& t, cudaStream_t st) {
     if (t.fast) fast::launch_solve_prep(w, t, st);
     else exact::launch_solve_prep(w, t, st);
+}
+// every iteration of the substep by the per-scene solve (one launch)
+inline void launch_scene_solve(const DW& w, const Tune& t, cudaStream_t st) {
+    if (t.fast) fast::launch_scene_solve(w, t, st);
+    else exact::launch_scene_solve(w, t, st);
+}
+// the per-scene solve runs when chosen and every scene fits a block
+inline bool use_scene_solve(const DW& w, const Tune& t) {
+    return t.primal_lanes < 0 && w.max_scene <= (uint32_t)SCENE_MAX_BODIES;
 }
 inline void launch_dual(const DW& w, const Tune& t, cudaStream_t st) {
     if (t.fast) fast::launch_dual(w, t, st);

@@ -374,6 +374,34 @@ __global__ void k_side_place(DW w) {
     }
 }
 
+// The rows of pair p for its body on side side_a, summed over the pair's
+// points in point order: 21 Hessian + 6 rhs numbers as 7 float4 at o.
+static __device__ __forceinline__ void side_rows(const DW& w, uint32_t p, bool side_a, PairCtx& c, float4* o) {
+    Sys s;
+#pragma unroll
+    for (int k = 0; k < 21; k++) s.h[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) s.r[k] = 0.0f;
+    for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, side_a, s);
+    o[0] = make_float4(s.h[0], s.h[1], s.h[2], s.h[3]);
+    o[1] = make_float4(s.h[4], s.h[5], s.h[6], s.h[7]);
+    o[2] = make_float4(s.h[8], s.h[9], s.h[10], s.h[11]);
+    o[3] = make_float4(s.h[12], s.h[13], s.h[14], s.h[15]);
+    o[4] = make_float4(s.h[16], s.h[17], s.h[18], s.h[19]);
+    o[5] = make_float4(s.h[20], s.r[0], s.r[1], s.r[2]);
+    o[6] = make_float4(s.r[3], s.r[4], s.r[5], 0.0f);
+}
+// Add one incidence slot's 7 float4 to a body's system (k_side_solve's order).
+static __device__ __forceinline__ void add_slot(Sys& s, const float4* o) {
+    float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];
+    s.h[0] += v0.x; s.h[1] += v0.y; s.h[2] += v0.z; s.h[3] += v0.w;
+    s.h[4] += v1.x; s.h[5] += v1.y; s.h[6] += v1.z; s.h[7] += v1.w;
+    s.h[8] += v2.x; s.h[9] += v2.y; s.h[10] += v2.z; s.h[11] += v2.w;
+    s.h[12] += v3.x; s.h[13] += v3.y; s.h[14] += v3.z; s.h[15] += v3.w;
+    s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
+    s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
+    s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
+}
 __global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
     if (aborted_solve(w)) return;
     const uint32_t s0 = w.side_cnt[colour], s1 = w.side_cnt[colour + 1];
@@ -383,22 +411,9 @@ __global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
         bool side_a = (e & 1u) != 0u;
         PairCtx c;
         load_ctx(w, p, c);
-        Sys s;
-#pragma unroll
-        for (int k = 0; k < 21; k++) s.h[k] = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 6; k++) s.r[k] = 0.0f;
-        for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, side_a, s);
         uint32_t slot = side_a ? p + w.offB[c.a + 1] : w.offA[c.b] + w.posB[p];
         if (slot >= w.contrib_slots) continue;  // a recording frame too small: the host reports it
-        float4* o = w.contrib + (size_t)slot * 7;
-        o[0] = make_float4(s.h[0], s.h[1], s.h[2], s.h[3]);
-        o[1] = make_float4(s.h[4], s.h[5], s.h[6], s.h[7]);
-        o[2] = make_float4(s.h[8], s.h[9], s.h[10], s.h[11]);
-        o[3] = make_float4(s.h[12], s.h[13], s.h[14], s.h[15]);
-        o[4] = make_float4(s.h[16], s.h[17], s.h[18], s.h[19]);
-        o[5] = make_float4(s.h[20], s.r[0], s.r[1], s.r[2]);
-        o[6] = make_float4(s.r[3], s.r[4], s.r[5], 0.0f);
+        side_rows(w, p, side_a, c, w.contrib + (size_t)slot * 7);
     }
 }
 __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
@@ -409,17 +424,7 @@ __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
         Sys s;
         inertial_block(w, h, s);
         const uint32_t k0 = w.offA[h] + w.offB[h], k1 = min(w.offA[h + 1] + w.offB[h + 1], w.contrib_slots);
-        for (uint32_t k = k0; k < k1; k++) {
-            const float4* o = w.contrib + (size_t)k * 7;
-            float4 v0 = o[0], v1 = o[1], v2 = o[2], v3 = o[3], v4 = o[4], v5 = o[5], v6 = o[6];
-            s.h[0] += v0.x; s.h[1] += v0.y; s.h[2] += v0.z; s.h[3] += v0.w;
-            s.h[4] += v1.x; s.h[5] += v1.y; s.h[6] += v1.z; s.h[7] += v1.w;
-            s.h[8] += v2.x; s.h[9] += v2.y; s.h[10] += v2.z; s.h[11] += v2.w;
-            s.h[12] += v3.x; s.h[13] += v3.y; s.h[14] += v3.z; s.h[15] += v3.w;
-            s.h[16] += v4.x; s.h[17] += v4.y; s.h[18] += v4.z; s.h[19] += v4.w;
-            s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
-            s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
-        }
+        for (uint32_t k = k0; k < k1; k++) add_slot(s, w.contrib + (size_t)k * 7);
         for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
         apply_solve(w, h, s);
     }
@@ -479,23 +484,21 @@ static __device__ __forceinline__ void dual_point(const DW& w, const PairCtx& c,
         w.q_roll[q] = make_float4(rls[0], rls[1], rls[2], 0.0f);
     }
 }
+static __device__ __forceinline__ void dual_pair(const DW& w, uint32_t p) {
+    uint32_t np = w.p_np[p];
+    if (np == 0) return;
+    PairCtx c;
+    load_ctx(w, p, c);
+    V3 t1 = tangent_t1(c.n);  // the grip flag of separated points needs the frame too
+    V3 t2 = cross(t1, c.n);
+    for (uint32_t k = 0; k < np; k++) dual_point(w, c, t1, t2, p * MAX_PTS + k);
+}
 __global__ void k_dual_pairs(DW w) {
     if (aborted_solve(w)) return;
     const uint32_t n = n_pairs(w);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        uint32_t np = w.p_np[p];
-        if (np == 0) continue;
-        PairCtx c;
-        load_ctx(w, p, c);
-        V3 t1 = tangent_t1(c.n);  // the grip flag of separated points needs the frame too
-        V3 t2 = cross(t1, c.n);
-        for (uint32_t k = 0; k < np; k++) dual_point(w, c, t1, t2, p * MAX_PTS + k);
-    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) dual_pair(w, p);
 }
-__global__ void k_dual_joints(DW w) {
-    if (aborted_solve(w)) return;
-    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= (uint32_t)w.J) return;
+static __device__ void dual_joint(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
@@ -561,9 +564,213 @@ __global__ void k_dual_joints(DW w) {
     w.j_lam_a[j] = make_float4(lama[0], lama[1], lama[2], 0.0f);
     w.j_pen_a[j] = make_float4(pena[0], pena[1], pena[2], 0.0f);
 }
+__global__ void k_dual_joints(DW w) {
+    if (aborted_solve(w)) return;
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < (uint32_t)w.J) dual_joint(w, j);
+}
 
+// ---- per-scene solve: one block walks a scene through every iteration ---------
+// Scenes never interact, so a block can take one scene through all
+// iterations of a substep — every colour's primal, then the scene's dual —
+// with block barriers between the phases and no wait on any other block.
+// The scene's data (its bodies' motion records, pairs and points) is touched
+// iterations x (colours + 1) times within one block, so after the first
+// touch it is served from L2 instead of being streamed from HBM once per
+// launch.  Blocks take scenes from a queue in descending size order (the
+// longest first), so the largest scenes do not finish last.
+//
+// Arithmetic is the split primal's: per (pair, side) the pair's rows summed
+// over its points (one thread per item, staged in shared memory), then per
+// body the inertial block, its items in incidence order and its joints, and
+// the 6x6 solve (one owner thread per body); the dual per pair and per joint.
+// Bodies of one colour share no pair or joint, so the order in which a
+// colour's bodies are visited cannot change a result.
+
+// In-place exclusive scan of a[0..n) (n <= SCENE_MAX_BODIES) by the block;
+// a[n] receives the total.  Needs 32 words of scratch.
+template <int BS>
+static __device__ __forceinline__ void block_scan(uint32_t* a, uint32_t n, uint32_t* warp_tot) {
+    const uint32_t per = (n + BS - 1) / BS;
+    const uint32_t t = threadIdx.x, i0 = min(n, t * per), i1 = min(n, i0 + per);
+    uint32_t sum = 0;
+    for (uint32_t i = i0; i < i1; i++) sum += a[i];
+    const uint32_t lane = t & 31u, wid = t >> 5;
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += v;
+    }
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t v = lane < BS / 32 ? warp_tot[lane] : 0u, x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane < BS / 32) warp_tot[lane] = x - v;  // exclusive warp offsets
+        if (lane == BS / 32 - 1) a[n] = x;          // the total (a[n] is past every thread's chunk)
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[wid] + inc - sum;
+    for (uint32_t i = i0; i < i1; i++) {
+        uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
+}
+
+template <int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
+    if (aborted_solve(w)) return;
+    __shared__ uint32_t s_list[SCENE_MAX_BODIES];      // swept bodies grouped by colour
+    __shared__ uint32_t s_pref[SCENE_MAX_BODIES + 1];  // item offset of each list entry
+    __shared__ uint32_t s_cstart[MAX_COLOURS + 1];
+    __shared__ uint32_t s_cur[MAX_COLOURS];
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_scene;
+    __shared__ int s_ncol;
+    extern __shared__ float4 s_rows[];  // BS items x 7 float4
+    const uint32_t tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_scene = atomicAdd(&w.ctr[C_SCENE_Q], 1u);
+        __syncthreads();
+        const uint32_t q = s_scene;
+        if (q >= (uint32_t)w.S) return;
+        const uint32_t sc = w.scene_order[q];
+        const uint32_t b0 = w.scene_off[sc], b1 = w.scene_off[sc + 1];
+        // colour lists of the scene's swept bodies
+        for (uint32_t c = tid; c < MAX_COLOURS; c += BS) s_cur[c] = 0;
+        if (tid == 0) s_ncol = 0;
+        __syncthreads();
+        for (uint32_t h = b0 + tid; h < b1; h += BS) {
+            int c = w.colour[h];
+            if (c >= 0 && c < MAX_COLOURS) {
+                atomicAdd(&s_cur[c], 1u);
+                atomicMax(&s_ncol, c + 1);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t acc = 0;
+            for (int c = 0; c < s_ncol; c++) {
+                s_cstart[c] = acc;
+                acc += s_cur[c];
+                s_cur[c] = s_cstart[c];
+            }
+            s_cstart[s_ncol] = acc;
+        }
+        __syncthreads();
+        const int ncol = s_ncol;
+        const uint32_t nlist = s_cstart[ncol];
+        for (uint32_t h = b0 + tid; h < b1; h += BS) {
+            int c = w.colour[h];
+            if (c >= 0 && c < MAX_COLOURS) s_list[atomicAdd(&s_cur[c], 1u)] = h;
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < nlist; i += BS) {
+            uint32_t h = s_list[i];
+            s_pref[i] = (w.offA[h + 1] - w.offA[h]) + (w.offB[h + 1] - w.offB[h]);
+        }
+        __syncthreads();
+        block_scan<BS>(s_pref, nlist, s_warp);
+        const uint32_t p0 = w.offA[b0], p1 = w.offA[b1];
+        for (int it = 0; it < w.iterations; it++) {
+            for (int c = 0; c < ncol; c++) {
+                const uint32_t hi = s_cstart[c + 1];
+                for (uint32_t i0 = s_cstart[c]; i0 < hi;) {
+                    // a group: the next (up to) BS bodies of the colour, one
+                    // owner thread each; their items are computed BS per round
+                    const uint32_t base = s_pref[i0];
+                    const uint32_t i1 = min(hi, i0 + BS);
+                    const uint32_t nb = i1 - i0, nitems = s_pref[i1] - base;
+                    Sys s;
+                    uint32_t h = 0, my0 = 0, my1 = 0;
+                    if (tid < nb) {
+                        h = s_list[i0 + tid];
+                        inertial_block(w, h, s);
+                        my0 = s_pref[i0 + tid] - base;
+                        my1 = s_pref[i0 + tid + 1] - base;
+                    }
+                    for (uint32_t r0 = 0; r0 < nitems; r0 += BS) {
+                        const uint32_t g = r0 + tid;
+                        if (g < nitems) {
+                            // the body of item g: the last entry starting at or before it
+                            int lo = (int)i0, up = (int)i1 - 1;
+                            while (lo < up) {
+                                int m = (lo + up + 1) >> 1;
+                                if (s_pref[m] - base <= g) lo = m;
+                                else up = m - 1;
+                            }
+                            const uint32_t hb = s_list[lo], k = g - (s_pref[lo] - base);
+                            const uint32_t nB = w.offB[hb + 1] - w.offB[hb];
+                            const bool side_a = k >= nB;
+                            const uint32_t p = side_a ? w.offA[hb] + (k - nB) : w.listB[w.offB[hb] + k];
+                            PairCtx cx;
+                            load_ctx(w, p, cx);
+                            side_rows(w, p, side_a, cx, s_rows + (size_t)tid * 7);
+                        }
+                        __syncthreads();
+                        if (tid < nb) {
+                            const uint32_t e1 = min(my1, r0 + BS);
+                            for (uint32_t e = max(my0, r0); e < e1; e++) add_slot(s, s_rows + (size_t)(e - r0) * 7);
+                        }
+                        __syncthreads();
+                    }
+                    if (tid < nb) {
+                        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+                        apply_solve(w, h, s);
+                    }
+                    i0 = i1;
+                }
+                __syncthreads();  // this colour's poses before the next colour reads them
+            }
+            for (uint32_t p = p0 + tid; p < p1; p += BS) dual_pair(w, p);
+            if (w.J)
+                for (uint32_t h = b0 + tid; h < b1; h += BS)
+                    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
+                        uint32_t j = w.jlist[k];
+                        if (w.j_ab[j].x == h) dual_joint(w, j);
+                    }
+            __syncthreads();
+        }
+    }
+}
+
+template <int BS, int MINB>
+static void scene_solve_launch(const DW& w, cudaStream_t st) {
+    const size_t smem = (size_t)BS * 7 * sizeof(float4);
+    static int grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device ordinal
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int& g = grid[dev & 7];
+    if (!g) {
+        cudaFuncSetAttribute(k_scene_solve<BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_solve<BS, MINB>, BS, smem);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        g = max(1, per_sm) * max(1, sms);
+    }
+    k_scene_solve<BS, MINB><<<min(g, max(1, w.S)), BS, smem, st>>>(w);
+}
+void launch_scene_solve(const DW& w, const Tune& tune, cudaStream_t st) {
+    cudaMemsetAsync(w.ctr + C_SCENE_Q, 0, sizeof(uint32_t), st);
+    switch (tune.primal_block) {
+        case 128: scene_solve_launch<128, 4>(w, st); break;
+        case 512: scene_solve_launch<512, 1>(w, st); break;
+        default: scene_solve_launch<256, 2>(w, st); break;
+    }
+}
+
+// The per-scene solve's fallback for a world with a scene above its limit is
+// the split launch.
+static inline int launch_lanes(const Tune& tune) { return tune.primal_lanes < 0 ? 0 : tune.primal_lanes; }
 void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st) {
-    if (tune.primal_lanes != 0) return;
+    if (launch_lanes(tune) != 0) return;
     k_zero_u32<<<1, 256, 0, st>>>(w.side_cnt, 2 * MAX_COLOURS + 2);
     k_side_count<<<gsz(w.pair_cap, SIDE_BLOCK), SIDE_BLOCK, 0, st>>>(w);
     k_side_starts<<<1, 32, 0, st>>>(w);
@@ -571,7 +778,7 @@ void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st) {
 }
 void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
     int bs = tune.primal_block;
-    switch (tune.primal_lanes) {
+    switch (launch_lanes(tune)) {
         case 0:
             k_side_rows<<<gsz((size_t)w.pair_cap * 2, 128), 128, 0, st>>>(w, c);
             k_side_solve<<<gsz(max_bodies, 128), 128, 0, st>>>(w, c);

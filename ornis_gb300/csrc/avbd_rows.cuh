@@ -7,6 +7,7 @@
 // crates/physics/src/avbd/assembly.rs:25-69 (solve_6x6),
 // crates/physics/src/avbd/joints_ext.rs:21-32 (gap_c0).
 #pragma once
+#include "avbd_crmath.cuh"
 #include "avbd_world.cuh"
 
 namespace avbd {
@@ -19,11 +20,13 @@ struct Sys {
 };
 static __host__ __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// sin, cos, asin and atan2 are the correctly rounded ones (avbd_crmath.cuh):
+// the reference's libm results, identical on every device and host.
 static __host__ __device__ __forceinline__ Q quat_integrate(Q q, V3 v) {  // rows.rs:110-119
     float theta = len(v);
     if (theta < NEAR_ZERO) return q;
     float s, c;
-    sincosf(HALF * theta, &s, &c);
+    crm::sincosf(HALF * theta, &s, &c);
     float k = s / theta;
     Q dq = qmul(Q{v.x * k, v.y * k, v.z * k, c}, q);
     return qnormalize(dq);
@@ -34,7 +37,7 @@ static __host__ __device__ __forceinline__ V3 quat_diff_vec(Q a, Q b) {  // rows
     if (r.w < 0.0f) xyz = -xyz;
     float s = fminf(len(xyz), 1.0f);
     if (s < NEAR_ZERO) return V0();
-    return xyz * (2.0f * asinf(s) / s);
+    return xyz * (2.0f * crm::asinf(s) / s);
 }
 static __host__ __device__ __forceinline__ float rem_euclid(float x, float m) {
     float r = fmodf(x, m);
@@ -43,7 +46,7 @@ static __host__ __device__ __forceinline__ float rem_euclid(float x, float m) {
 static __host__ __device__ __forceinline__ float wrap_pi(float x) { return rem_euclid(x + PI_F, TAU_F) - PI_F; }
 static __host__ __device__ __forceinline__ float hinge_twist(Q qa, Q qb, V3 axis) {  // sequential_impulse/joints.rs:38-48
     Q q = qmul(conj(qa), qb);
-    float t = 2.0f * atan2f(dot(V3{q.x, q.y, q.z}, axis), q.w);
+    float t = 2.0f * crm::atan2f(dot(V3{q.x, q.y, q.z}, axis), q.w);
     return rem_euclid(t + PI_F, TAU_F) - PI_F;
 }
 static __host__ __device__ __forceinline__ int warm_limit_state(float v, float lo, float hi, float slop, float force) {  // rows.rs:156-183

@@ -16,6 +16,7 @@
 #include <numeric>
 #include <vector>
 
+#include "avbd_crmath.cuh"
 #include "avbd_kernels.h"
 
 using namespace avbd;
@@ -128,7 +129,7 @@ float hinge_twist_host(const float qa[4], const float qb[4], const float ax[3]) 
     float y = a3 * qb[1] - a0 * qb[2] + a1 * qb[3] + a2 * qb[0];
     float z = a3 * qb[2] + a0 * qb[1] - a1 * qb[0] + a2 * qb[3];
     float w = a3 * qb[3] - a0 * qb[0] - a1 * qb[1] - a2 * qb[2];
-    float t = 2.0f * std::atan2((x * ax[0] + y * ax[1]) + z * ax[2], w);
+    float t = 2.0f * avbd::crm::atan2f((x * ax[0] + y * ax[1]) + z * ax[2], w);
     const float PI = 3.14159265358979323846f, TAU = 6.28318530717958647692f;
     float r = std::fmod(t + PI, TAU);
     if (r < 0.0f) r += std::fabs(TAU);
@@ -294,7 +295,14 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.posB = m.get<uint32_t>(cand_cap);
     w.side_list = m.get<uint32_t>((size_t)cand_cap * 2);
     w.side_cnt = m.get<uint32_t>(2 * MAX_COLOURS + 2);
-    w.contrib = W->tune.primal_lanes == 0 ? m.get<float4>((size_t)cand_cap * 2 * 7) : nullptr;
+    // the split primal's per-incidence partial systems (the per-scene solve
+    // falls back to the split launches when a scene is above its limit)
+    uint32_t max_scene = 0;
+    for (uint32_t s = 0; s < S; s++) max_scene = std::max(max_scene, W->scene_off[s + 1] - W->scene_off[s]);
+    w.max_scene = max_scene;
+    const bool need_contrib = W->tune.primal_lanes == 0 ||
+                              (W->tune.primal_lanes < 0 && max_scene > (uint32_t)SCENE_MAX_BODIES);
+    w.contrib = need_contrib ? m.get<float4>((size_t)cand_cap * 2 * 7) : nullptr;
     w.contrib_slots = w.contrib ? (uint32_t)(cand_cap * 2) : 0u;
     w.cand = m.get<uint2>(cand_cap);
     w.keep = m.get<uint8_t>(cand_cap);
@@ -333,6 +341,17 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     W->d_small = m.get<uint32_t>(small.size());
     if (!small.empty())
         cudaMemcpy(W->d_small, small.data(), small.size() * 4, cudaMemcpyHostToDevice);
+    {
+        // the per-scene solve's queue: largest scenes first (ties by index)
+        std::vector<uint32_t> order(S);
+        for (uint32_t s = 0; s < S; s++) order[s] = s;
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+            return W->scene_off[a + 1] - W->scene_off[a] > W->scene_off[b + 1] - W->scene_off[b];
+        });
+        uint32_t* d = m.get<uint32_t>(S);
+        if (S) cudaMemcpy(d, order.data(), S * 4, cudaMemcpyHostToDevice);
+        w.scene_order = d;
+    }
     W->plan.small_scenes = W->d_small;
     W->plan.n_small = (int)small.size();
     w.fbody = m.get<uint32_t>(N);
@@ -792,8 +811,12 @@ static void enqueue_front(AvbdWorld* W, bool emit) {
 }
 static void enqueue_back(AvbdWorld* W, int ncol, bool emit) {
     const DW& w = W->w;
-    launch_solve_prep(w, W->tune, W->st);
-    for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
+    if (use_scene_solve(w, W->tune)) {
+        launch_scene_solve(w, W->tune, W->st);
+    } else {
+        launch_solve_prep(w, W->tune, W->st);
+        for (int it = 0; it < w.iterations; it++) launch_iteration(w, W->tune, ncol, W->st);
+    }
     launch_finish_substep(w, W->tune, W->st);
     if (W->ev_period >= 0) launch_events(w, emit, emit && W->has_trig, W->scan_tmp, W->st);
 }
@@ -1671,7 +1694,8 @@ static int capture(AvbdWorld* W) {
         for (int k = 0; k < 2; k++) {
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(W->st, cudaStreamCaptureModeThreadLocal));
-            W->w.max_cols = W->graph_cols;
+            // the per-scene solve walks as many colours as each scene has
+            W->w.max_cols = use_scene_solve(W->w, W->tune) ? MAX_COLOURS : W->graph_cols;
             enqueue_front(W, emit != 0);
             enqueue_back(W, W->graph_cols, emit != 0);
             W->w.max_cols = MAX_COLOURS;
@@ -1875,13 +1899,17 @@ int avbd_set_occupancy(AvbdWorld* W, int min_blocks) {
 
 int avbd_set_tuning(AvbdWorld* W, int primal_lanes, int primal_block) {
     if (!W) return AVBD_ERR_INVALID_ARG;
-    if (primal_lanes != 0 && primal_lanes != 1 && primal_lanes != 4 && primal_lanes != 8 && primal_lanes != 16 &&
-        primal_lanes != 32)
+    if (primal_lanes != AVBD_PRIMAL_SCENES && primal_lanes != 0 && primal_lanes != 1 && primal_lanes != 4 &&
+        primal_lanes != 8 && primal_lanes != 16 && primal_lanes != 32)
         return AVBD_ERR_INVALID_ARG;
     if (primal_block < 32 || primal_block > 1024 || primal_block % 32) return AVBD_ERR_INVALID_ARG;
     // the thread-per-body primal is register-bounded for 128-thread blocks
     if (primal_lanes == 1 && primal_block > 128) return AVBD_ERR_INVALID_ARG;
-    if (primal_lanes == 0 && W->w.ctr && !W->w.contrib) {
+    if (primal_lanes == AVBD_PRIMAL_SCENES && primal_block != 128 && primal_block != 256 && primal_block != 512)
+        return AVBD_ERR_INVALID_ARG;
+    const bool need_contrib = primal_lanes == 0 ||
+                              (primal_lanes < 0 && W->w.max_scene > (uint32_t)SCENE_MAX_BODIES);
+    if (need_contrib && W->w.ctr && !W->w.contrib) {
         // the split primal's per-incidence partial systems
         cudaSetDevice(W->device);
         W->w.contrib = W->mem.get<float4>((size_t)W->cand_cap * 2 * 7);
@@ -1973,7 +2001,8 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     launch_post_discovery(w, W->scan_tmp, st);
     CK(cudaEventRecord(ev[5], st));
     launch_colouring(w, W->tune, W->scan_tmp, st);
-    launch_solve_prep(w, W->tune, st);
+    const bool scene_solve = use_scene_solve(w, W->tune);
+    if (!scene_solve) launch_solve_prep(w, W->tune, st);
     CK(cudaEventRecord(ev[6], st));
     rc = read_ctr(W);
     if (rc) return rc;
@@ -1983,7 +2012,15 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     uint32_t col_total = 0;
     CK(cudaMemcpy(&col_total, w.col_cnt + MAX_COLOURS, 4, cudaMemcpyDeviceToHost));
     float prim = 0.0f, dual = 0.0f;
-    for (int it = 0; it < w.iterations; it++) {
+    if (scene_solve) {
+        // primal and dual of every iteration in one launch: reported as primal
+        CK(cudaEventRecord(ev[6], st));
+        launch_scene_solve(w, W->tune, st);
+        CK(cudaEventRecord(ev[7], st));
+        CK(cudaEventSynchronize(ev[7]));
+        CK(cudaEventElapsedTime(&prim, ev[6], ev[7]));
+    }
+    for (int it = 0; it < (scene_solve ? 0 : w.iterations); it++) {
         float t;
         CK(cudaEventRecord(ev[6], st));
         for (int c = 0; c < ncol; c++) launch_primal_colour(w, W->tune, c, (uint32_t)w.N, st);
@@ -2008,7 +2045,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     if (rc) return rc;
     accumulate(W);
     info[0] = (uint32_t)ncol;
-    info[1] = (uint32_t)(ncol * w.iterations);
+    info[1] = scene_solve ? 1u : (uint32_t)(ncol * w.iterations);
     info[2] = col_total;
     info[3] = W->h_ctr[C_PAIRS];
     info[4] = W->h_ctr[C_POINTS];

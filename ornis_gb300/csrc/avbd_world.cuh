@@ -50,6 +50,7 @@ constexpr int MAX_PTS = AVBD_MAX_POINTS;
 constexpr int MAX_COLOURS = 64;
 constexpr int CCD_ROUNDS = 8;
 constexpr int COLOUR_ROUNDS = 24;  // device-wide colouring rounds for scenes above the one-CTA limit
+constexpr int SCENE_MAX_BODIES = 2048;  // scenes up to this size are solved by one block each (k_scene_solve)
 
 // body info word: shape kind in bits 0-3, body type in bits 4-5, trigger bit 6
 __host__ __device__ __forceinline__ uint32_t info_shape(uint32_t i) { return i & 15u; }
@@ -75,7 +76,8 @@ enum Ctr {
     C_BOXONE = 14,       // pairs with exactly one box (listed from the back of boxlist)
     C_NOBOX = 15,        // pairs without a box (clist)
     C_LONGSEG = 16,      // long static pair segments put in order by the chunk sort
-    C_NUM = 17
+    C_SCENE_Q = 17,      // next entry of scene_order a block of the per-scene solve takes
+    C_NUM = 18
 };
 enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
 
@@ -120,6 +122,8 @@ struct DW {
 
     const uint32_t* scene_off;  // S+1
     const uint32_t* scene_of;   // N
+    const uint32_t* scene_order;  // S: scenes by descending body count (the per-scene solve's queue)
+    uint32_t max_scene;           // bodies of the largest scene
     const uint32_t* plane_off;  // S+1: half-space bodies of each scene
     const uint32_t* plane_list;
     const HullDesc* hulls;  // convex hulls named by AVBD_SHAPE_HULL bodies (shape_params[0])

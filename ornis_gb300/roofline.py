@@ -15,8 +15,12 @@ iteration, independent of how the kernels stage it:
                         once per swept body)
     pair header   32 B
 
-A launch of the primal kernel covers one colour; the roofline uses the sum
-over all colours of one iteration (the same ratio as per launch).
+A launch of the per-colour primal kernels covers one colour; their roofline
+uses the sum over all colours of one iteration (the same ratio as per
+launch).  The per-scene solve is one launch per substep covering every
+iteration's primal and dual: its algorithmic bytes are iterations x (primal
++ dual bytes per iteration).  It keeps a scene's data on chip and in L2
+across the iterations, so its DRAM traffic is below these bytes.
 """
 
 PRIMAL_BODY_B = 128
@@ -34,13 +38,35 @@ def dual_bytes_per_iteration(swept, points, pairs):
     return DUAL_POINT_B * points + DUAL_BODY_B * swept + PAIR_HEADER_B * pairs
 
 
-def primal_roofline(phases_ms, info, peak, split=False):
+KERNELS = {
+    "thread": "k_primal_thread (one launch per colour)",
+    "lanes": "k_primal_lanes (one launch per colour)",
+    "split": "k_side_rows + k_side_solve (one pair of launches per colour)",
+    "scene": "k_scene_solve (one launch per substep: every iteration's primal and dual, a block per scene)",
+}
+
+
+def primal_roofline(phases_ms, info, peak, kind="thread", iterations=1):
     """Roofline entry for the primal kernel from one profiled substep.
 
-    split: the primal ran as the split pair (k_side_rows + k_side_solve per
-    colour); its time is the pair's, its algorithmic bytes the same model.
+    kind: the launch that ran ("thread", "lanes", "split" — the pair of
+    kernels per colour, its time is the pair's — or "scene", the per-scene
+    solve, one launch covering every iteration's primal and dual).
     """
     peak_gbs, source = peak
+    if kind == "scene":
+        b = iterations * (primal_bytes_per_iteration(info["swept"], info["points"], info["pairs"]) +
+                          dual_bytes_per_iteration(info["swept"], info["points"], info["pairs"]))
+        ms = phases_ms["primal"]
+        achieved = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        return {
+            "bound": "hbm", "kernel": KERNELS[kind], "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+            "frac": achieved / peak_gbs,
+            "peak_source": f"{source} (MEASURED_PEAKS.json hbm_gbs)" if source == "measured" else "fallback 6.8 TB/s",
+            "traffic": None, "bytes_per_launch": b, "launch_ms": ms,
+            "model": "v1: per iteration 128 B/swept body + 48 B/point + 32 B/pair (primal) + 56 B/swept body + "
+                     "76 B/point + 32 B/pair (dual), times the iterations of the launch",
+        }
     iters = max(1, info["primal_launches"] // max(1, info["colours"]))
     per_iter_ms = phases_ms["primal"] / iters
     per_launch_ms = phases_ms["primal"] / max(1, info["primal_launches"])
@@ -50,8 +76,7 @@ def primal_roofline(phases_ms, info, peak, split=False):
     dual_ms = phases_ms["dual"] / iters
     return {
         "bound": "hbm",
-        "kernel": ("k_side_rows + k_side_solve (one pair of launches per colour)" if split
-                   else "k_primal_thread (one launch per colour)"),
+        "kernel": KERNELS[kind],
         "achieved": achieved,
         "peak": peak_gbs,
         "unit": "GB/s",

@@ -4,12 +4,19 @@ The batched workload (4096 scenes, dt 1/120, 2 substeps, 8 iterations) run
 as the benchmark runs it — fast build, launch shape picked by the autotuner
 at step 150, CUDA-graph replay, events every step — to step 200, where the
 piles have formed (millions of contact pairs, several colours).  From there,
-for 10 steps, sampled scenes of the batch are exported from the device each
-step and stepped by the oracle (Coloured order; rows summed per pair when
-the split launch runs, as it sums them) while the device steps the whole
-batch.  Per step: pair sets, points per pair, contact IDs and colours
+for 10 steps (20 substeps, the reference's step_inner each), sampled scenes
+of the batch are exported from the device before every substep and stepped
+by the oracle (Coloured order; rows summed per pair when the split or
+per-scene launch runs, as they sum them) while the device steps the whole
+batch.  Per substep: pair sets, points per pair, contact IDs and colours
 identical; poses within 1e-5 relative (scale max(1, |x|)), velocities the
 same times dt.
+
+The comparison restarts from the device's state every substep because the
+fast build's last bits differ from the oracle's: a pose 1 ulp away can move
+a box corner across the manifold's slop in the next discovery (seen at these
+piles: one point count in a 2,762-pair scene after two substeps), which is a
+different input, not a different algorithm.
 """
 import numpy as np
 import pytest
@@ -40,17 +47,17 @@ def test_batched_piles_bench_configuration_per_step():
     st = w.export_state()
     assert len(st["pairs"]) > 1_000_000  # the piles the benchmark times
     worst = 0.0
-    for _ in range(10):
+    for _ in range(10 * nsub):
         ors = []
         for sc in chosen:
             sub = P.scene_state(st, offs, sc)
             o = O.OracleWorld(params, mode=O.COLOURED)
-            o.split_sums(lanes == 0)
+            o.split_sums(lanes <= 0)
             o.add_bodies(sub["bodies"])
             o.import_state(sub)
-            o.step_fixed(nsub)
+            o.step_fixed(1)
             ors.append(o)
-        w.step_graph(nsub)
+        w.step_graph(1)
         st = w.export_state()
         cols = w.colours()
         for sc, o in zip(chosen, ors):
