@@ -323,9 +323,13 @@ int avbd_set_tuning(AvbdWorld* world, int primal_lanes, int primal_block);
 
 /* Arithmetic of the iteration kernels: 0 (default) = exact build, the same
  * f32 operation order as the reference (no contraction, IEEE divide and
- * square root); 1 = fast build (contracted multiply-adds, approximate divide
- * and square root), within the 1e-5 pose tolerance.  Pair sets, contact IDs
- * and colours are computed exactly in both. */
+ * square root, correctly rounded sin / cos / asin / atan2): from identical
+ * state it reproduces the CPU restatement bit for bit; 1 = fast build
+ * (contracted multiply-adds, approximate divide and square root), a few
+ * percent faster but not bit-faithful: the stiff contact and joint rows
+ * amplify its last-bit differences to 1e-5 .. 3e-4 per step in settled piles
+ * and ragdolls.  Discovery (pair sets, contact IDs, colours) is exact in
+ * both. */
 int avbd_set_precision(AvbdWorld* world, int fast);
 
 /* Register budget of the one-thread-per-body primal: built for 4, 6 or 8

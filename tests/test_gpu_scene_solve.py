@@ -3,10 +3,12 @@ a substep: all colours' primal and the dual in one launch) against the split
 launches and the oracle.
 
 It computes the split launches' arithmetic (rows summed per pair, then per
-body the inertial block, the pairs in incidence order and the joints), so it
-must equal them bit for bit, in both builds, through plain launches and
-graph replay, for every block size; and it must meet the parity bars against
-the oracle (Coloured order, per-pair row sums) from identical state.
+body the inertial block, the pairs in incidence order and the joints), so in
+the exact build it must equal them bit for bit, through plain launches and
+graph replay, for every block size, and equal the oracle (Coloured order,
+per-pair row sums) bit for bit from identical state.  The fast build lets
+the compiler contract multiply-adds where it likes, which can differ between
+the two kernels, so there both are held to the parity bars instead.
 """
 import numpy as np
 import pytest
@@ -36,7 +38,7 @@ def run(bodies, offs, params, nsub, lanes, block, fast, graph, steps, joints=())
     return out, c
 
 
-@pytest.mark.parametrize("block,fast,graph", [(128, 0, 0), (256, 1, 1), (512, 0, 1), (256, 0, 0)])
+@pytest.mark.parametrize("block,fast,graph", [(128, 0, 0), (256, 0, 1), (512, 0, 1), (256, 0, 0)])
 def test_scene_solve_equals_split_launches(block, fast, graph):
     # scenes up to 600 bodies: colours with more items than a block's round
     bodies, offs, _ = scenes.batched(12, seed=21, lo=8, hi=600)
@@ -99,3 +101,5 @@ def test_scene_solve_per_step_against_oracle(fast):
         so, sg = P.step_from_oracle_state(o, g)
         worst = max(worst, P.compare_states(so, sg, params.step_dt, o, g)[0])
     print(f"per-scene solve, fast={fast}: worst per-step pose error {worst:.2e}")
+    if not fast:
+        assert worst == 0.0  # correctly rounded sin / asin on both sides: the same arithmetic
