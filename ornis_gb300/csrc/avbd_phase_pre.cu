@@ -22,6 +22,7 @@ __global__ void k_begin(DW w) {
         w.ctr[C_FAST] = 0;
         w.ctr[C_POINTS] = 0;
         w.ctr[C_SLEEP] = 0;
+        w.ctr[C_CCD_HITS] = 0;
         if (w.evs) w.evs[EV_TRIG_NOW] = 0;
     }
 }
@@ -309,11 +310,34 @@ static __device__ __noinline__ Cast cast_one(const DW& w, uint32_t h, uint32_t o
 static __device__ __forceinline__ bool ccd_target(const DW& w, uint32_t h, uint32_t o) {
     return !info_trigger(w.info[o]) && pair_allowed(w, h, o) && !jointed(w, h, o);
 }
+// Whether the sweep of h along its step displacement can bring it within
+// touching distance of o: its bounding sphere swept along the segment
+// against o's bounding sphere (or o's plane).  When it cannot, cast_one
+// returns no hit (every distance it evaluates exceeds SHAPE_TOUCH), so the
+// cast is skipped; the slack covers the float rounding of both tests.
+static __device__ __forceinline__ bool sweep_may_touch(const DW& w, uint32_t h, uint32_t o) {
+    const V3 p0 = ld3(w.pos[h]), d = ld3(w.vel[h]) * w.dt, c = ld3(w.pos[o]);
+    const float rh = w.shp[h].w;
+    const float slack = 4.0f * SHAPE_TOUCH + 1e-4f * (len(p0) + len(c) + len(d));
+    if (!isfinite(rh)) return true;
+    if (info_shape(w.info[o]) == AVBD_SHAPE_HALFSPACE) {
+        const float4 sp = w.shp[o];
+        const V3 n = qrot(ldq(w.rot[o]), V3{sp.x, sp.y, sp.z});
+        const float d0 = dot(p0 - c, n), d1 = d0 + dot(d, n);
+        return fminf(d0, d1) - rh <= slack;
+    }
+    const float ro = w.shp[o].w;
+    if (!isfinite(ro)) return true;
+    const float dd = dot(d, d);
+    const float sp = dd > 0.0f ? fclamp(dot(c - p0, d) / dd, 0.0f, 1.0f) : 0.0f;
+    return len(c - (p0 + d * sp)) - rh - ro <= slack;
+}
 __global__ void k_ccd_init(DW w) {
     if (aborted(w)) return;
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
     w.ccd_best[h] = ~0ull;
+    if (w.ccd_win) w.ccd_win[h] = ~0u;
     if (w.ccd_ev_o) w.ccd_ev_o[h] = -1;
     w.ccd_deps[h] = 0;
     w.ccd_state[h] = 0;
@@ -326,8 +350,12 @@ __global__ void k_ccd_init(DW w) {
 }
 // first = 1: every mover casts against its candidates at the step-top poses
 // and counts the earlier movers among its targets.  first = 0: only movers
-// flagged for a recast.
-static __device__ __forceinline__ void k_ccd_cast_one(const DW& w, int first, uint32_t c) {
+// flagged for a recast.  Every hit is recorded (tag = the cast round) so
+// that the apply can take the winner's time, normal and witness instead of
+// casting again: the winner's inputs do not change between its cast and its
+// apply (a mover applies once its earlier movers are final and it has recast
+// against any that moved; later movers wait for it).
+static __device__ __forceinline__ void k_ccd_cast_one(const DW& w, int first, uint32_t c, uint32_t tag) {
     uint2 ab = w.cand[c];
     bool fa = w.fast[ab.x], fb = w.fast[ab.y];
     if (!fa && !fb) return;
@@ -336,11 +364,21 @@ static __device__ __forceinline__ void k_ccd_cast_one(const DW& w, int first, ui
         if (!(k ? fb : fa)) continue;
         if (!first && !(w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1)) continue;
         if (!ccd_target(w, h, o)) continue;
+        if (!sweep_may_touch(w, h, o)) continue;
         Cast r = cast_one(w, h, o);
         if (r.hit) {
             // earliest time wins; equal times keep the lower handle (distance.rs:886-890)
             unsigned long long key = ((unsigned long long)__float_as_uint(r.t) << 32) | o;
             atomicMin(&w.ccd_best[h], key);
+            if (w.ccd_hit) {
+                uint32_t k = agg_inc(&w.ctr[C_CCD_HITS]);
+                if (k < w.ccd_hit_cap) {
+                    float4* rec = w.ccd_hit + (size_t)k * 3;
+                    rec[0] = make_float4(r.t, __uint_as_float(o), __uint_as_float(h), __uint_as_float(tag));
+                    rec[1] = st3(r.normal, 0.0f);
+                    rec[2] = st3(r.point, 0.0f);
+                }
+            }
         }
     }
 }
@@ -359,20 +397,42 @@ __global__ void k_ccd_collect(DW w) {
         if (fa && fb && ccd_target(w, ab.x, ab.y)) atomicAdd(&w.ccd_deps[ab.y], 1u);
     }
 }
-__global__ void k_ccd_cast(DW w, int first) {
+__global__ void k_ccd_cast(DW w, int first, uint32_t tag) {
     if (aborted(w)) return;
     if (w.ctr[C_FAST] == 0u || (!first && w.ctr[C_CCD_PENDING] == 0u)) return;
     const uint32_t n = w.ctr[C_FCAND];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        k_ccd_cast_one(w, first, w.fcand[i]);
+        k_ccd_cast_one(w, first, w.fcand[i], tag);
+}
+// The record of each mover's winning cast of round `tag` (the one whose key
+// equals the mover's best; keys are unique per mover).
+__global__ void k_ccd_pick(DW w, uint32_t tag) {
+    if (aborted(w) || !w.ccd_hit) return;
+    if (w.ctr[C_FAST] == 0u || w.ctr[C_CCD_PENDING] == 0u) return;
+    const uint32_t n = min(w.ctr[C_CCD_HITS], w.ccd_hit_cap);
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        float4 r0 = w.ccd_hit[(size_t)k * 3];
+        if (__float_as_uint(r0.w) != tag) continue;
+        uint32_t o = __float_as_uint(r0.y), h = __float_as_uint(r0.z);
+        unsigned long long key = ((unsigned long long)__float_as_uint(r0.x) << 32) | o;
+        if (w.ccd_best[h] == key) w.ccd_win[h] = k;
+    }
 }
 
-static __device__ void ccd_apply(const DW& w, uint32_t h) {
+// recorded: the winner's record may be used (its cast saw the final poses)
+static __device__ void ccd_apply(const DW& w, uint32_t h, bool recorded) {
     unsigned long long key = w.ccd_best[h];
     bool moved = false;
     if (key != ~0ull) {
         uint32_t o = (uint32_t)(key & 0xffffffffu);
-        Cast r = cast_one(w, h, o);  // the winning cast again: same inputs, same t and normal
+        Cast r;
+        const uint32_t k = recorded && w.ccd_win ? w.ccd_win[h] : ~0u;
+        if (k != ~0u) {
+            const float4* rec = w.ccd_hit + (size_t)k * 3;
+            r = Cast{true, rec[0].x, ld3(rec[1]), ld3(rec[2])};
+        } else {
+            r = cast_one(w, h, o);  // the winning cast again: same inputs, same t and normal
+        }
         V3 disp = ld3(w.vel[h]) * w.dt;
         float L = fmaxf(len(disp), MIN_TOI_DISP_LENGTH);
         float frac = fclamp(r.t / L, 0.0f, 1.0f);
@@ -412,11 +472,12 @@ __global__ void k_ccd_finalize(DW w, int round, int last) {
     if (i >= w.ctr[C_FAST]) return;
     uint32_t h = w.fbody[i];
     if (w.ccd_state[h] != 0) return;
-    if (w.ccd_deps[h] != 0) {
+    const bool waiting = w.ccd_deps[h] != 0;
+    if (waiting) {
         if (!last) return;
         atomicAdd(&w.ctr[C_CCD_LEFT], 1u);  // dependency chain longer than the bounded rounds
     }
-    ccd_apply(w, h);
+    ccd_apply(w, h, !waiting);
     w.ccd_recompute[h] = (uint8_t)(16 + round);  // "finalised in this round"
     atomicSub(&w.ctr[C_CCD_PENDING], 1u);
 }
@@ -442,7 +503,10 @@ __global__ void k_ccd_reset(DW w) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.ctr[C_FAST]) return;
     uint32_t h = w.fbody[i];
-    if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) w.ccd_best[h] = ~0ull;
+    if (w.ccd_state[h] == 0 && w.ccd_deps[h] == 0 && w.ccd_recompute[h] == 1) {
+        w.ccd_best[h] = ~0ull;
+        if (w.ccd_win) w.ccd_win[h] = ~0u;
+    }
 }
 __global__ void k_ccd_clear_recast(DW w) {
     if (aborted(w)) return;
@@ -457,14 +521,17 @@ void launch_ccd(const DW& w, cudaStream_t st) {
     unsigned gb = nblk(w.N, 256);
     k_ccd_init<<<gb, 256, 0, st>>>(w);
     k_ccd_collect<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w);
-    k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 1);
+    const unsigned gh = w.ccd_hit ? gsz(w.ccd_hit_cap, 256) : 0u;
+    k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 1, 0u);
+    if (gh) k_ccd_pick<<<gh, 256, 0, st>>>(w, 0u);
     for (int r = 0; r < CCD_ROUNDS; r++) {
         bool last = r == CCD_ROUNDS - 1;
         k_ccd_finalize<<<gb, 256, 0, st>>>(w, r, last ? 1 : 0);
         if (last) break;
         k_ccd_release<<<gsz(w.cand_cap, 256), 256, 0, st>>>(w, r);
         k_ccd_reset<<<gb, 256, 0, st>>>(w);
-        k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 0);
+        k_ccd_cast<<<gsz(w.cand_cap, 128), 128, 0, st>>>(w, 0, (uint32_t)(r + 1));
+        if (gh) k_ccd_pick<<<gh, 256, 0, st>>>(w, (uint32_t)(r + 1));
         k_ccd_clear_recast<<<gb, 256, 0, st>>>(w);
     }
 }

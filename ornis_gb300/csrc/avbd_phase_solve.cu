@@ -402,18 +402,59 @@ static __device__ __forceinline__ void add_slot(Sys& s, const float4* o) {
     s.h[20] += v5.x; s.r[0] += v5.y; s.r[1] += v5.z; s.r[2] += v5.w;
     s.r[3] += v6.x; s.r[4] += v6.y; s.r[5] += v6.z;
 }
-__global__ void __launch_bounds__(128) k_side_rows(DW w, int colour) {
+// Work lists are taken in chunks of one block (128 entries) whose entries are
+// handed to the block's threads grouped by a small work class (the entry's
+// loop length), so that the lanes of a warp run loops of the same length
+// instead of idling behind the longest one.  The chunk keeps the list's
+// locality; each entry writes only its own outputs, so which thread takes
+// it changes no result.
+constexpr int CHUNK = 128;
+// Counting sort of the chunk's entries by class (0..MAX_PTS) into ent[].
+// Every thread of the block calls it; returns the entries in the chunk.
+static __device__ __forceinline__ uint32_t chunk_sort(uint32_t* cnt, uint32_t* ent, bool has, uint32_t e,
+                                                      uint32_t cls, uint32_t n) {
+    if (threadIdx.x <= MAX_PTS) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    if (has) atomicAdd(&cnt[cls], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k <= MAX_PTS; k++) {
+            uint32_t c = cnt[k];
+            cnt[k] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    if (has) ent[atomicAdd(&cnt[cls], 1u)] = e;
+    __syncthreads();
+    return n;
+}
+__global__ void __launch_bounds__(CHUNK) k_side_rows(DW w, int colour) {
     if (aborted_solve(w)) return;
+    __shared__ uint32_t s_cnt[MAX_PTS + 1], s_ent[CHUNK];
     const uint32_t s0 = w.side_cnt[colour], s1 = w.side_cnt[colour + 1];
-    for (uint32_t i = s0 + blockIdx.x * blockDim.x + threadIdx.x; i < s1; i += gridDim.x * blockDim.x) {
-        uint32_t e = w.side_list[i];
-        uint32_t p = e >> 1;
-        bool side_a = (e & 1u) != 0u;
-        PairCtx c;
-        load_ctx(w, p, c);
-        uint32_t slot = side_a ? p + w.offB[c.a + 1] : w.offA[c.b] + w.posB[p];
-        if (slot >= w.contrib_slots) continue;  // a recording frame too small: the host reports it
-        side_rows(w, p, side_a, c, w.contrib + (size_t)slot * 7);
+    for (uint32_t base = s0 + blockIdx.x * CHUNK; base < s1; base += gridDim.x * CHUNK) {
+        const uint32_t i = base + threadIdx.x;
+        const bool has = i < s1;
+        uint32_t e = 0, cls = 0;
+        if (has) {
+            e = w.side_list[i];
+            uint32_t p = e >> 1;
+            cls = w.p_n[p].w <= 0.0f ? w.p_np[p] : 0u;  // separated pairs stamp at most a damper row
+        }
+        const uint32_t n = chunk_sort(s_cnt, s_ent, has, e, cls, min((uint32_t)CHUNK, s1 - base));
+        if (threadIdx.x < n) {
+            e = s_ent[threadIdx.x];
+            uint32_t p = e >> 1;
+            bool side_a = (e & 1u) != 0u;
+            PairCtx c;
+            load_ctx(w, p, c);
+            uint32_t slot = side_a ? p + w.offB[c.a + 1] : w.offA[c.b] + w.posB[p];
+            // a recording frame too small: the host reports it
+            if (slot < w.contrib_slots) side_rows(w, p, side_a, c, w.contrib + (size_t)slot * 7);
+        }
+        __syncthreads();  // the chunk's entries are read before the next chunk is sorted
     }
 }
 __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
@@ -493,10 +534,18 @@ static __device__ __forceinline__ void dual_pair(const DW& w, uint32_t p) {
     V3 t2 = cross(t1, c.n);
     for (uint32_t k = 0; k < np; k++) dual_point(w, c, t1, t2, p * MAX_PTS + k);
 }
-__global__ void k_dual_pairs(DW w) {
+__global__ void __launch_bounds__(CHUNK) k_dual_pairs(DW w) {
     if (aborted_solve(w)) return;
-    const uint32_t n = n_pairs(w);
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) dual_pair(w, p);
+    __shared__ uint32_t s_cnt[MAX_PTS + 1], s_ent[CHUNK];
+    const uint32_t np = n_pairs(w);
+    for (uint32_t base = blockIdx.x * CHUNK; base < np; base += gridDim.x * CHUNK) {
+        const uint32_t p = base + threadIdx.x;
+        const bool has = p < np;
+        const uint32_t cls = has ? min(w.p_np[p], (uint32_t)MAX_PTS) : 0u;
+        const uint32_t n = chunk_sort(s_cnt, s_ent, has, p, cls, min((uint32_t)CHUNK, np - base));
+        if (threadIdx.x < n) dual_pair(w, s_ent[threadIdx.x]);
+        __syncthreads();
+    }
 }
 static __device__ void dual_joint(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];

@@ -361,6 +361,11 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.ccd_deps = m.get<uint32_t>(N);
     w.ccd_state = m.get<uint8_t>(N);
     w.ccd_recompute = m.get<uint8_t>(N);
+    if (W->prm.enable_ccd) {
+        w.ccd_hit_cap = std::max(4096u, cand_cap / 4u);
+        w.ccd_hit = m.get<float4>((size_t)w.ccd_hit_cap * 3);
+        w.ccd_win = m.get<uint32_t>(N);
+    }
     w.ccd_rec = W->prm.enable_ccd ? m.get<float4>(2 * N) : nullptr;
     w.flag = m.get<uint8_t>(N);
     w.comp_flag = m.get<uint32_t>(N);

@@ -77,7 +77,8 @@ enum Ctr {
     C_NOBOX = 15,        // pairs without a box (clist)
     C_LONGSEG = 16,      // long static pair segments put in order by the chunk sort
     C_SCENE_Q = 17,      // next entry of scene_order a block of the per-scene solve takes
-    C_NUM = 18
+    C_CCD_HITS = 18,     // swept-cast hits recorded this substep (ccd_hit)
+    C_NUM = 19
 };
 enum ErrBits { E_CAND_OVERFLOW = 1, E_COLOUR_OVERFLOW = 2, E_TIMEOUT = 4, E_COLOUR_RANGE = 8 };
 
@@ -201,6 +202,13 @@ struct DW {
     uint32_t* ccd_deps;
     uint8_t* ccd_state;  // 0 pending, 1 final, 2 final+moved
     uint8_t* ccd_recompute;
+    // the hits of this substep's casts, 3 float4 each: (t, other, body, cast
+    // round as float bits), normal, target witness; ccd_win[h] = the record
+    // of h's winning cast, or ~0 (then the apply recomputes it).  Null: the
+    // apply always recomputes.
+    float4* ccd_hit;
+    uint32_t ccd_hit_cap;
+    uint32_t* ccd_win;
 
     // wake / sleep scratch
     uint8_t* flag;  // per body

@@ -53,8 +53,8 @@ def test_scene_solve_equals_split_launches(block, fast, graph):
 def test_scene_solve_with_joints_equals_split_launches():
     bodies, offs, joints = scenes.ragdolls((3, 5), seed=6)
     params, nsub = scenes.params_for("ragdoll_8192")
-    ref, _ = run(bodies, offs, params, nsub, 0, 128, 1, 1, 50, joints)
-    got, _ = run(bodies, offs, params, nsub, SCENES, 256, 1, 1, 50, joints)
+    ref, _ = run(bodies, offs, params, nsub, 0, 128, 0, 1, 50, joints)
+    got, _ = run(bodies, offs, params, nsub, SCENES, 256, 0, 1, 50, joints)
     assert got.tobytes() == ref.tobytes()
 
 
