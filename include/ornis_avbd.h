@@ -253,6 +253,18 @@ int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
 /* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529), Ball and Revolute. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 
+/* PhysicsEngine::remove_joint (engine.rs, avbd/mod.rs:1531-1540): both
+ * bodies of the joint wake, the joint and its warm state go, and the handles
+ * of later joints move down by one (the reference's Vec::retain).  An invalid
+ * handle is a no-op. */
+int avbd_world_remove_joint(AvbdWorld* world, uint32_t handle);
+
+/* PhysicsEngine::wake_body (engine.rs:109, avbd/mod.rs:1599-1601): a sleeping
+ * body wakes with its mass and inertia restored and its sleep timer reset
+ * (mod.rs:833-842, body.rs:412-418); awake bodies and invalid handles are
+ * untouched. */
+int avbd_world_wake_body(AvbdWorld* world, uint32_t handle);
+
 int avbd_world_body_count(const AvbdWorld* world, uint32_t* n);
 int avbd_world_scene_count(const AvbdWorld* world, uint32_t* n);
 

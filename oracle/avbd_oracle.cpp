@@ -2137,6 +2137,22 @@ int oracle_remove_body(OracleWorld* w, uint32_t handle) {
     DISPATCH(w, E.remove_body(handle));
     return AVBD_OK;
 }
+// PhysicsEngine::remove_joint (mod.rs:1531-1540): wake both, then retain.
+int oracle_remove_joint(OracleWorld* w, uint32_t handle) {
+    DISPATCH(w, {
+        if (handle < E.joints.size()) {
+            E.wake_body(E.joints[handle].a);
+            E.wake_body(E.joints[handle].b);
+            E.joints.erase(E.joints.begin() + handle);
+        }
+    });
+    return AVBD_OK;
+}
+// PhysicsEngine::wake_body (mod.rs:1599-1601)
+int oracle_wake_body(OracleWorld* w, uint32_t handle) {
+    DISPATCH(w, E.wake_body(handle));
+    return AVBD_OK;
+}
 int oracle_add_joint(OracleWorld* w, const AvbdJointDesc* d, uint32_t* handle) {
     int rc = 0;
     DISPATCH(w, rc = E.add_joint(*d, *handle));

@@ -44,6 +44,8 @@ def lib():
             "avbd_world_add_bodies": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_add_joint": [vp, C.POINTER(abi.AvbdJointDesc), C.POINTER(u32)],
             "avbd_world_remove_body": [vp, u32],
+            "avbd_world_remove_joint": [vp, u32],
+            "avbd_world_wake_body": [vp, u32],
             "avbd_world_add_hull": [vp, vp, u32, vp, u32, vp, C.POINTER(u32)],
             "avbd_world_body_count": [vp, C.POINTER(u32)],
             "avbd_world_scene_count": [vp, C.POINTER(u32)],
@@ -176,6 +178,14 @@ class AvbdWorld:
     def remove_body(self, handle):
         """PhysicsEngine::remove_body: the last body takes over the handle."""
         _check(lib().avbd_world_remove_body(self.h, int(handle)), "remove_body")
+
+    def remove_joint(self, handle):
+        """PhysicsEngine::remove_joint: both bodies wake; later joint handles move down one."""
+        _check(lib().avbd_world_remove_joint(self.h, int(handle)), "remove_joint")
+
+    def wake_body(self, handle):
+        """PhysicsEngine::wake_body: a sleeping body wakes (mass and inertia restored)."""
+        _check(lib().avbd_world_wake_body(self.h, int(handle)), "wake_body")
 
     def add_joint(self, desc):
         hj = C.c_uint32()

@@ -1424,6 +1424,21 @@ int avbd_world_add_hull(AvbdWorld* W, const float* verts, uint32_t nv, const uin
 }
 
 // PhysicsEngine::remove_body (mod.rs:1241-1300) on a one-scene world.
+// AvbdEngine::wake_body (mod.rs:833-842) with RigidBody::wake_restore
+// (body.rs:412-418) on the host model: a sleeper's mass and inertia return.
+static void wake_host(AvbdWorld* W, uint32_t h) {
+    AvbdBodyAux& a = W->aux[h];
+    if (!a.asleep) return;
+    a.asleep = 0;
+    a.sleep_timer = 0.0f;
+    AvbdBody& b = W->bodies[h];
+    if (b.body_type == AVBD_BODY_DYNAMIC) {
+        bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
+        b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
+        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
+    }
+}
+
 int avbd_world_remove_body(AvbdWorld* W, uint32_t hi) {
     if (!W) return AVBD_ERR_INVALID_ARG;
     if (W->scene_off.size() != 2) return AVBD_ERR_UNSUPPORTED;
@@ -1495,19 +1510,31 @@ int avbd_world_remove_body(AvbdWorld* W, uint32_t hi) {
     }
     W->joints.swap(joints);
     // every sleeper wakes (mod.rs:1294-1296, body.rs:412-418)
-    for (uint32_t h = 0; h < last; h++) {
-        AvbdBodyAux& a = W->aux[h];
-        if (!a.asleep) continue;
-        a.asleep = 0;
-        a.sleep_timer = 0.0f;
-        AvbdBody& b = W->bodies[h];
-        if (b.body_type == AVBD_BODY_DYNAMIC) {
-            bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
-            b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
-            rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
-        }
-    }
+    for (uint32_t h = 0; h < last; h++) wake_host(W, h);
     W->scene_off.back() = last;
+    return AVBD_OK;
+}
+
+int avbd_world_remove_joint(AvbdWorld* W, uint32_t handle) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    if (handle >= W->joints.size()) return AVBD_OK;  // invalid handles are a no-op (mod.rs:1532)
+    // both members wake, then the joint goes and later handles move down one
+    // (mod.rs:1531-1540, retain_joints mod.rs:766-784)
+    wake_host(W, W->joints[handle].a);
+    wake_host(W, W->joints[handle].b);
+    W->joints.erase(W->joints.begin() + handle);
+    return AVBD_OK;
+}
+
+int avbd_world_wake_body(AvbdWorld* W, uint32_t handle) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);
+    if (rc) return rc;
+    if (handle < W->bodies.size()) wake_host(W, handle);  // mod.rs:1599-1601, :833-842
     return AVBD_OK;
 }
 

@@ -72,6 +72,8 @@ def lib():
         L.oracle_body_new.argtypes = [C.c_uint32, vp, vp, C.c_float, C.POINTER(abi.AvbdBody)]
         L.oracle_set_emit_period.argtypes = [vp, C.c_int32]
         L.oracle_remove_body.argtypes = [vp, C.c_uint32]
+        L.oracle_remove_joint.argtypes = [vp, C.c_uint32]
+        L.oracle_wake_body.argtypes = [vp, C.c_uint32]
         L.oracle_add_hull.restype = C.c_uint32
         L.oracle_add_hull.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32, vp]
         L.oracle_convex_distance.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
@@ -214,6 +216,12 @@ class OracleWorld:
 
     def remove_body(self, handle):
         lib().oracle_remove_body(self.h, int(handle))
+
+    def remove_joint(self, handle):
+        lib().oracle_remove_joint(self.h, int(handle))
+
+    def wake_body(self, handle):
+        lib().oracle_wake_body(self.h, int(handle))
 
     def set_emit_period(self, period):
         lib().oracle_set_emit_period(self.h, int(period))
