@@ -1699,6 +1699,7 @@ int avbd_world_step_fixed(AvbdWorld* W, int32_t substeps) {
     return step_plain_n(W, substeps, false);
 }
 
+static int step_graph_n(AvbdWorld* W, int32_t substeps, bool last_only);
 int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
     if (!W) return AVBD_ERR_INVALID_ARG;
     if (!std::isfinite(dt) || dt <= 0.0f) return AVBD_OK;
@@ -1712,7 +1713,10 @@ int avbd_world_step(AvbdWorld* W, float dt) {  // mod.rs:1212-1235
     if (!n || (W->bodies.empty() && W->host_valid)) return AVBD_OK;
     int rc = begin_steps(W);
     if (rc) return rc;
-    return step_plain_n(W, n, true);
+    // CUDA-graph replay of each substep (identical results to plain launches,
+    // one launch per substep instead of a few hundred); events on the last
+    // substep of the call, as the reference reports them
+    return step_graph_n(W, n, true);
 }
 
 // Graph replay: one captured substep per pair-buffer parity.  The primal is
@@ -1750,13 +1754,10 @@ static int capture(AvbdWorld* W) {
     return AVBD_OK;
 }
 
-int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
-    if (!W || substeps < 0) return AVBD_ERR_INVALID_ARG;
-    if (W->bodies.empty() && W->host_valid) return AVBD_OK;
-    int rc = begin_steps(W);
-    if (rc) return rc;
+static int step_graph_n(AvbdWorld* W, int32_t substeps, bool last_only) {
+    int rc = AVBD_OK;
     for (int i = 0; i < substeps; i++) {
-        const bool emit = emit_at(W, i, substeps, false);
+        const bool emit = emit_at(W, i, substeps, last_only);
         if (!W->gexec[0][0] || W->last_ncol > W->graph_cols) {
             if (W->last_ncol == 0) {
                 rc = substep_plain(W, emit);  // learn the colour count first
@@ -1796,6 +1797,13 @@ int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
         accumulate(W);
     }
     return AVBD_OK;
+}
+int avbd_world_step_graph(AvbdWorld* W, int32_t substeps) {
+    if (!W || substeps < 0) return AVBD_ERR_INVALID_ARG;
+    if (W->bodies.empty() && W->host_valid) return AVBD_OK;
+    int rc = begin_steps(W);
+    if (rc) return rc;
+    return step_graph_n(W, substeps, false);
 }
 
 int avbd_world_get_counters(AvbdWorld* W, AvbdCounters* out) {
