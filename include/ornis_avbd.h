@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define AVBD_ABI_VERSION 1
+#define AVBD_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 #define AVBD_OK 0
@@ -46,7 +46,8 @@ extern "C" {
 #define AVBD_ERR_JOINT_SELF (-10)    /* JointError::SelfJoint                  */
 #define AVBD_ERR_JOINT_HANDLES (-11) /* JointError::InvalidHandles             */
 #define AVBD_ERR_JOINT_BAD_AXIS (-12)/* JointError::BadAxis                    */
-#define AVBD_ERR_JOINT_NONFINITE (-13)
+#define AVBD_ERR_JOINT_NONFINITE (-13) /* JointError::NonFinite (motor fields)   */
+#define AVBD_ERR_JOINT_BAD_BOUNDS (-14)/* JointError::BadBounds (limits, rope)     */
 
 /* ---- enums --------------------------------------------------------------- */
 /* Shape variants on the path (collision/shape.rs); shape_params meaning:     */
@@ -64,8 +65,18 @@ extern "C" {
 
 #define AVBD_FLAG_TRIGGER 1u /* RigidBody::is_trigger */
 
-#define AVBD_JOINT_BALL 0     /* JointKind::Ball     (joint.rs:209+) */
-#define AVBD_JOINT_REVOLUTE 1 /* JointKind::Revolute (optional limit) */
+#define AVBD_JOINT_BALL 0      /* JointKind::Ball      (joint.rs:209+)               */
+#define AVBD_JOINT_REVOLUTE 1  /* JointKind::Revolute  (optional limit and motor)    */
+#define AVBD_JOINT_PRISMATIC 2 /* JointKind::Prismatic (optional limit and motor)    */
+#define AVBD_JOINT_FIXED 3     /* JointKind::Fixed     (weld)                        */
+#define AVBD_JOINT_DISTANCE 4  /* JointKind::Distance  (rod of the assembly length)  */
+#define AVBD_JOINT_ROPE 5      /* JointKind::Rope      (max_distance)                */
+#define AVBD_JOINT_SIXDOF 6    /* JointKind::SixDof    (axis_config per axis)        */
+
+/* SixDof per-axis configuration (AxisConfig, joint.rs) */
+#define AVBD_AXIS_FREE 0
+#define AVBD_AXIS_LOCKED 1
+#define AVBD_AXIS_LIMITED 2
 
 /* ---- plain-old-data records --------------------------------------------- */
 
@@ -93,18 +104,26 @@ typedef struct AvbdBody {
     uint32_t flags;
 } AvbdBody;
 
-/* Joint specification (JointKind::Ball / ::Revolute, joint.rs:209-260). */
+/* Joint specification (JointKind, joint.rs:209-330).  Fields a kind does not
+ * use are ignored. */
 typedef struct AvbdJointDesc {
     uint32_t kind;
     uint32_t body_a;
     uint32_t body_b;
     float local_anchor_a[3];
     float local_anchor_b[3];
-    float local_axis_a[3]; /* revolute only */
-    float local_axis_b[3]; /* revolute only */
-    int32_t has_limit;     /* revolute only: RevoluteLimit present */
+    float local_axis_a[3]; /* revolute hinge / prismatic slide axis */
+    float local_axis_b[3];
+    int32_t has_limit;     /* revolute (rad) / prismatic (m): RevoluteLimit / PrismaticLimit */
     float limit_min;
     float limit_max;
+    int32_t has_motor;     /* revolute / prismatic velocity motor (RevoluteMotor / PrismaticMotor) */
+    float motor_speed;     /* target_speed (rad/s or m/s) */
+    float motor_max;       /* max_torque / max_force */
+    float max_distance;    /* rope */
+    uint32_t axis_config[6]; /* sixdof: linear x y z, angular x y z in body A's assembly frame */
+    float axis_min[6];       /* sixdof limited axes: travel window */
+    float axis_max[6];
 } AvbdJointDesc;
 
 /* Solver parameters.  avbd_default_params() fills the reference's constants
@@ -160,7 +179,9 @@ typedef struct AvbdJointState {
     float lam_a[3];
     float pen_l[3];
     float pen_a[3];
-    float acc_lim;
+    float acc_lim;   /* revolute limit accumulator */
+    float lim_dual;  /* prismatic limit force */
+    float sacc[6];   /* sixdof limited-axis forces: linear x y z, angular x y z */
 } AvbdJointState;
 
 /* Per-step observability counters (the reference exposes sleeping_count(),
@@ -250,7 +271,14 @@ int avbd_world_add_hull(AvbdWorld* world, const float* verts, uint32_t nverts, c
  * no-op.  One-scene worlds only (AVBD_ERR_UNSUPPORTED for a batch). */
 int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
 
-/* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529), Ball and Revolute. */
+/* PhysicsEngine::add_joint (avbd/mod.rs:1310-1529) with the admission
+ * checks of validate_joint (migration.rs:160-330): non-finite anchors or
+ * axes -> AVBD_ERR_JOINT_BAD_AXIS, inverted or non-finite limits and a rope
+ * length <= 0 -> AVBD_ERR_JOINT_BAD_BOUNDS, non-finite motor fields ->
+ * AVBD_ERR_JOINT_NONFINITE, then both bodies wake, then self / invalid
+ * handles; a degenerate hinge or slide axis -> AVBD_ERR_JOINT_BAD_AXIS.
+ * Kinds: Ball, Revolute (limit, velocity motor), Prismatic (limit, velocity
+ * motor), Fixed, Distance, Rope, SixDof. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 
 /* PhysicsEngine::remove_joint (engine.rs, avbd/mod.rs:1531-1540): both

@@ -69,6 +69,8 @@ struct K {
     static constexpr float WAKE_IMPACT_SPEED = 0.5f;
     static constexpr float WAKE_PENETRATION = 0.01f;
     static constexpr float LIMIT_SLOP_ANG = 0.005f;
+    static constexpr float LIMIT_SLOP_LIN = 0.002f;      // mod.rs:222
+    static constexpr float MIN_EFFECTIVE_MASS = 1e-10f;  // constants.rs:16
     static constexpr float LIM_PEN_MAX = 1e4f;
     static constexpr float ROLL_PEN = 100.0f;
     static constexpr float MIN_TOI_DISP_LENGTH = 1e-9f;
@@ -576,13 +578,23 @@ template <class T> struct Pair {
     T gap;
     std::vector<Point<T>> points;
 };
-template <class T> struct Joint {
+template <class T> struct Joint {  // AvbdJoint (avbd/mod.rs:327-402)
     uint32_t a, b, kind;
     V3<T> la, lb, ax_a, ax_b;
+    // revolute reference twist, prismatic reference length, distance rest
+    // length, rope maximum
     T ref_val;
     bool has_lim;
     T lo, hi;
-    T acc_lim;
+    T acc_lim;   // revolute limit accumulator
+    T lim_dual;  // prismatic limit force
+    bool has_mot;
+    T mot_speed, mot_max;
+    Qt<T> q_ref;  // fixed / sixdof: qa^-1 qb at assembly
+    V3<T> dref;   // fixed / sixdof: anchor separation in A's frame at assembly
+    uint32_t six_cfg[6];
+    T six_min[6], six_max[6];
+    T sacc[6];
     T lam_l[3], lam_a[3], pen_l[3], pen_a[3];
 };
 
@@ -851,15 +863,141 @@ template <class T> struct Engine {
     }
 
     // ---- joints / sleep (avbd/sleep.rs) ----
-    T joint_rest_error(const Joint<T>& j) const {
+    T joint_rest_error(const Joint<T>& j) const {  // sleep.rs:30-105
         const Body<T>& a = bodies[j.a];
         const Body<T>& b = bodies[j.b];
         V3<T> delta = (b.pos + qrot(b.rot, j.lb)) - (a.pos + qrot(a.rot, j.la));
-        if (j.kind == AVBD_JOINT_BALL) return len(delta);
         V3<T> axis = qrot(a.rot, j.ax_a);
-        return fmx(len(delta), len(axis - qrot(b.rot, j.ax_b)));
+        switch (j.kind) {
+            case AVBD_JOINT_BALL: return len(delta);
+            case AVBD_JOINT_REVOLUTE: return fmx(len(delta), len(axis - qrot(b.rot, j.ax_b)));
+            case AVBD_JOINT_FIXED:
+                return fmx(len(delta - qrot(a.rot, j.dref)), len(quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref)));
+            case AVBD_JOINT_DISTANCE: return std::fabs(len(delta) - j.ref_val);
+            case AVBD_JOINT_ROPE: return fmx(len(delta) - j.ref_val, T(0));
+            case AVBD_JOINT_PRISMATIC: {
+                V3<T> perp = delta - axis * dot(delta, axis);
+                T e = len(perp);
+                if (j.has_lim) {
+                    T value = dot(delta, axis) - j.ref_val;
+                    e = fmx(e, fmx(j.lo - value, value - j.hi));
+                }
+                return fmx(e, len(axis - qrot(b.rot, j.ax_b)));
+            }
+            default: {  // sixdof (sleep.rs:86-103)
+                V3<T> lin = qrot(conj(a.rot), delta) - j.dref;
+                V3<T> ang = quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref);
+                T e = T(0);
+                for (int i = 0; i < 3; i++) {
+                    T vals[2] = {lin[i], ang[i]};
+                    uint32_t cfg[2] = {j.six_cfg[i], j.six_cfg[3 + i]};
+                    T los[2] = {j.six_min[i], j.six_min[3 + i]}, his[2] = {j.six_max[i], j.six_max[3 + i]};
+                    for (int k = 0; k < 2; k++) {
+                        T r = T(0);
+                        if (cfg[k] == AVBD_AXIS_LOCKED) r = std::fabs(vals[k]);
+                        else if (cfg[k] == AVBD_AXIS_LIMITED) r = fmx(fmx(los[k] - vals[k], vals[k] - his[k]), T(0));
+                        e = fmx(e, r);
+                    }
+                }
+                return e;
+            }
+        }
     }
-    bool joint_driven(const Joint<T>& j) const {
+    // joints_ext.rs:423-437: I_w^-1 wa of a solvable body, zero otherwise
+    V3<T> ang_inv_wa(uint32_t h, V3<T> wa) const {
+        if (!solvable(h)) return VZERO<T>();
+        const Body<T>& b = bodies[h];
+        T iw[3][3], inv[3][3];
+        world_inertia(b.inertia, b.rot, iw);
+        V3<T> dg{fmx(b.inertia.x, T(0)), fmx(b.inertia.y, T(0)), fmx(b.inertia.z, T(0))};
+        inverse_symmetric(iw, dg, inv);
+        return mat3_vec(inv, wa);
+    }
+    T eff_inv_mass(const Body<T>& b) const { return b.type == AVBD_BODY_DYNAMIC ? b.inv_mass : T(0); }  // rows.rs:406-412
+    bool limit_violated(const Joint<T>& j) const {  // joints_ext.rs:441-462
+        if (!j.has_lim) return false;
+        const Body<T>& a = bodies[j.a];
+        const Body<T>& b = bodies[j.b];
+        if (j.kind == AVBD_JOINT_REVOLUTE) {
+            T angle = wrap_pi(hinge_twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+            return limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG)) >= 0;
+        }
+        if (j.kind == AVBD_JOINT_PRISMATIC) {
+            V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+            V3<T> pa = a.pos + qrot(a.rot, j.la), pb = b.pos + qrot(b.rot, j.lb);
+            return limit_state(dot(pb - pa, wa) - j.ref_val, j.lo, j.hi, C<T>(K::LIMIT_SLOP_LIN)) >= 0;
+        }
+        return false;
+    }
+    // JointMotor::velocity_impulse (joint.rs:1172-1177) with the spec motor's
+    // velocity drive: the deadbeat rate correction, clamped to the budget
+    T velocity_impulse(T rate_error, T inv_eff_mass, T max_force) const {
+        if (!(dt > T(0)) || max_force <= T(0) || inv_eff_mass <= T(0)) return T(0);
+        return fclamp(rate_error / inv_eff_mass, -max_force * dt, max_force * dt);
+    }
+    // motor_impulse (joints_ext.rs:237-383): revolute and prismatic velocity
+    // motors, before the warm start, paused while a limit is violated
+    void motor_impulse() {
+        for (Joint<T>& j : joints) {
+            if (!j.has_mot || j.mot_max <= T(0) || limit_violated(j)) continue;
+            Body<T>& a = bodies[j.a];
+            Body<T>& b = bodies[j.b];
+            V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+            if (j.kind == AVBD_JOINT_REVOLUTE) {
+                T w = dot(b.angvel - a.angvel, wa);
+                V3<T> ia = ang_inv_wa(j.a, wa), ib = ang_inv_wa(j.b, wa);
+                T k = dot(ia, wa) + dot(ib, wa);
+                if (k < C<T>(K::MIN_EFFECTIVE_MASS)) continue;
+                T dj = velocity_impulse(j.mot_speed - w, k, j.mot_max);
+                if (solvable(j.a)) a.angvel = a.angvel + (-dj) * ia;
+                if (solvable(j.b)) b.angvel = b.angvel + dj * ib;
+            } else if (j.kind == AVBD_JOINT_PRISMATIC) {
+                T v = dot(b.vel - a.vel, wa);
+                T ka = eff_inv_mass(a), kb = eff_inv_mass(b);
+                T k = ka + kb;
+                if (k < C<T>(K::MIN_EFFECTIVE_MASS)) continue;
+                T dj = velocity_impulse(j.mot_speed - v, k, j.mot_max);
+                if (solvable(j.a)) a.vel = a.vel + (-dj) * ka * wa;
+                if (solvable(j.b)) b.vel = b.vel + dj * kb * wa;
+            }
+        }
+    }
+    // rope_impulse (joints_ext.rs:173-236): a stretched rope's separating
+    // velocity removed through the pair's effective mass
+    void rope_impulse() {
+        for (Joint<T>& j : joints) {
+            if (j.kind != AVBD_JOINT_ROPE) continue;
+            Body<T>& a = bodies[j.a];
+            Body<T>& b = bodies[j.b];
+            V3<T> pa = a.pos + qrot(a.rot, j.la), pb = b.pos + qrot(b.rot, j.lb);
+            V3<T> delta = pb - pa;
+            T ln = len(delta);
+            if (ln <= j.ref_val) continue;
+            V3<T> nn = delta / ln;
+            V3<T> ra = pa - a.pos, rb = pb - b.pos;
+            T ka = eff_inv_mass(a), kb = eff_inv_mass(b);
+            V3<T> ta = cross(ra, nn), tb = cross(rb, nn);
+            T k = ka + kb + dot(ang_inv_wa(j.a, ta), ta) + dot(ang_inv_wa(j.b, tb), tb);
+            if (k < C<T>(K::MIN_EFFECTIVE_MASS)) continue;
+            V3<T> va = a.vel + cross(a.angvel, ra);
+            V3<T> vb = b.vel + cross(b.angvel, rb);
+            T vsep = dot(vb - va, nn);
+            if (vsep <= T(0)) continue;
+            T dj = -vsep / k;
+            if (solvable(j.a)) {
+                V3<T> ia = ang_inv_wa(j.a, ta);
+                a.vel = a.vel - nn * (dj * ka);
+                a.angvel = a.angvel - ia * dj;
+            }
+            if (solvable(j.b)) {
+                V3<T> ib = ang_inv_wa(j.b, tb);
+                b.vel = b.vel + nn * (dj * kb);
+                b.angvel = b.angvel + ib * dj;
+            }
+        }
+    }
+    bool joint_driven(const Joint<T>& j) const {  // sleep.rs:18-28
+        if (j.has_mot && j.mot_speed != T(0) && j.mot_max > T(0)) return true;
         uint32_t m[2] = {j.a, j.b};
         for (uint32_t h : m) {
             const Body<T>& b = bodies[h];
@@ -1345,6 +1483,7 @@ template <class T> struct Engine {
     void stamp_joint_for(uint32_t h, const Joint<T>& j, T lhs[6][6], T rhs[6]) const {  // assembly.rs:255-881
         bool is_a = j.a == h;
         T sign = is_a ? T(1) : T(-1);
+        T lsign = is_a ? T(-1) : T(1);  // rows measured B minus A flip the gradient
         const Body<T>& a = bodies[j.a];
         const Body<T>& b = bodies[j.b];
         V3<T> pa = a.pos + qrot(a.rot, j.la);
@@ -1353,20 +1492,75 @@ template <class T> struct Engine {
         V3<T> pb0 = pos0[j.b] + qrot(rot0[j.b], j.lb);
         V3<T> live = pa - pb, c0v = pa0 - pb0;
         V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+        const bool fixed = j.kind == AVBD_JOINT_FIXED;
+        V3<T> r_plain = is_a ? qrot(a.rot, j.la) : qrot(b.rot, j.lb);
         V3<T> fl = VZERO<T>();
-        for (int k = 0; k < 3; k++) {
-            V3<T> axis = VZERO<T>();
-            axis[k] = T(1);
-            T c = live[k] - C<T>(K::ALPHA) * c0v[k];
-            T f = j.pen_l[k] * c + j.lam_l[k];
-            if (!row_live(c, f)) continue;
-            // Ball/Revolute levers add a zero offset (the Fixed weld's dref slot).
-            V3<T> r_side = is_a ? qrot(a.rot, j.la + VZERO<T>()) : qrot(b.rot, j.lb);
-            stamp_row(lhs, rhs, axis, j.pen_l[k], f, r_side, sign);
-            fl[k] = f;
+        // linear rows (assembly.rs:278-455)
+        if (j.kind == AVBD_JOINT_BALL || j.kind == AVBD_JOINT_REVOLUTE || fixed) {
+            for (int k = 0; k < 3; k++) {
+                V3<T> axis = VZERO<T>();
+                axis[k] = T(1);
+                V3<T> lv = fixed ? live + qrot(a.rot, j.dref) : live;
+                V3<T> iv = fixed ? c0v + qrot(rot0[j.a], j.dref) : c0v;
+                T c = lv[k] - C<T>(K::ALPHA) * iv[k];
+                T f = j.pen_l[k] * c + j.lam_l[k];
+                if (!row_live(c, f)) continue;
+                // Ball/Revolute levers add a zero offset (the Fixed weld's dref slot).
+                V3<T> r_side = is_a ? qrot(a.rot, j.la + (fixed ? j.dref : VZERO<T>())) : qrot(b.rot, j.lb);
+                stamp_row(lhs, rhs, axis, j.pen_l[k], f, r_side, sign);
+                fl[k] = f;
+            }
+        } else if (j.kind == AVBD_JOINT_PRISMATIC) {
+            V3<T> u, v;
+            tangent_basis(wa, u, v);
+            V3<T> axs[2] = {u, v};
+            for (int li = 0; li < 2; li++) {
+                T c = dot(live - C<T>(K::ALPHA) * c0v, axs[li]);
+                T f = j.pen_l[li] * c + j.lam_l[li];
+                if (!row_live(c, f)) continue;
+                stamp_row(lhs, rhs, axs[li], j.pen_l[li], f, r_plain, sign);
+                fl = fl + axs[li] * f;
+            }
+        } else if (j.kind == AVBD_JOINT_DISTANCE || j.kind == AVBD_JOINT_ROPE) {
+            T ln = len(live);
+            if (j.kind == AVBD_JOINT_DISTANCE || ln > j.ref_val) {
+                V3<T> dir = ln > C<T>(K::NEAR_ZERO) ? live / ln : VY<T>();
+                T c = (ln - j.ref_val) - C<T>(K::ALPHA) * (len(c0v) - j.ref_val);
+                T f = j.pen_l[0] * c + j.lam_l[0];
+                if (row_live(c, f)) {
+                    stamp_row(lhs, rhs, dir, j.pen_l[0], f, r_plain, sign);
+                    fl = dir * f;
+                }
+            }
+        } else if (j.kind == AVBD_JOINT_SIXDOF) {
+            for (int i = 0; i < 3; i++) {
+                V3<T> e = VZERO<T>();
+                e[i] = T(1);
+                V3<T> dir = normalize_or(qrot(a.rot, e), e);
+                if (j.six_cfg[i] == AVBD_AXIS_LOCKED) {
+                    V3<T> evec = (pb - pa) - qrot(a.rot, j.dref);
+                    T c = dot(evec, dir);
+                    T f = j.pen_l[i] * c + j.lam_l[i];
+                    if (!row_live(c, f)) continue;
+                    stamp_row(lhs, rhs, dir, j.pen_l[i], f, r_plain, lsign);
+                } else if (j.six_cfg[i] == AVBD_AXIS_LIMITED) {
+                    T sep = dot((pb - pa) - qrot(a.rot, j.dref), dir);
+                    int st = warm_limit_state(sep, j.six_min[i], j.six_max[i], C<T>(K::LIMIT_SLOP_LIN), j.sacc[i]);
+                    if (st < 0) continue;
+                    bool lower = st == 1;
+                    V3<T> axis0 = normalize_or(qrot(rot0[j.a], e), e);
+                    T initial = dot((pb0 - pa0) - qrot(rot0[j.a], j.dref), axis0);
+                    T c = regularized_limit(sep, initial, lower ? j.six_min[i] : j.six_max[i], lower);
+                    T f_raw = j.pen_l[i] * c + j.sacc[i];
+                    T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
+                    if (!row_live(c, f)) continue;
+                    stamp_row(lhs, rhs, dir, j.pen_l[i], f, r_plain, lsign);
+                }
+            }
         }
         {
-            V3<T> r = is_a ? qrot(a.rot, j.la + VZERO<T>()) : -qrot(b.rot, j.lb);
+            // geometric stiffness (rows.rs:69-88, assembly.rs:589-618)
+            V3<T> r = is_a ? qrot(a.rot, j.la + (fixed ? j.dref : VZERO<T>())) : -qrot(b.rot, j.lb);
             T hm[3][3] = {};
             T arr[3] = {r.x, r.y, r.z};
             for (int k = 0; k < 3; k++) {
@@ -1380,7 +1574,8 @@ template <class T> struct Engine {
                      len(V3<T>{hm[0][2], hm[1][2], hm[2][2]})};
             lhs[3][3] += hd.x; lhs[4][4] += hd.y; lhs[5][5] += hd.z;
         }
-        if (j.kind == AVBD_JOINT_REVOLUTE) {
+        // angular rows (assembly.rs:634-806)
+        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC) {
             V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
             V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
             V3<T> t1, t2;
@@ -1394,17 +1589,68 @@ template <class T> struct Engine {
                 V3<T> g = is_a ? cross(axa, t) : -cross(axb, t);
                 stamp_angular(lhs, rhs, g, j.pen_a[li], f);
             }
-            if (j.has_lim) {
-                T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
-                int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
-                if (st >= 0) {
+        } else if (j.kind == AVBD_JOINT_SIXDOF) {
+            V3<T> diff = quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref);
+            for (int i = 0; i < 3; i++) {
+                V3<T> e = VZERO<T>();
+                e[i] = T(1);
+                V3<T> dir = normalize_or(qrot(a.rot, e), e);
+                V3<T> g = is_a ? -dir : dir;
+                if (j.six_cfg[3 + i] == AVBD_AXIS_LOCKED) {
+                    T c = dot(diff, e);
+                    T f = j.pen_a[i] * c + j.lam_a[i];
+                    if (!row_live(c, f)) continue;
+                    stamp_angular(lhs, rhs, g, j.pen_a[i], f);
+                } else if (j.six_cfg[3 + i] == AVBD_AXIS_LIMITED) {
+                    T travel = twist(a.rot, b.rot, e) - quat_twist(j.q_ref, e);
+                    int st = warm_limit_state(travel, j.six_min[3 + i], j.six_max[3 + i], C<T>(K::LIMIT_SLOP_ANG),
+                                              j.sacc[3 + i]);
+                    if (st < 0) continue;
                     bool lower = st == 1;
-                    T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
-                    T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
-                    T f_raw = j.pen_a[2] * c + j.acc_lim;
+                    T initial = twist(rot0[j.a], rot0[j.b], e) - quat_twist(j.q_ref, e);
+                    T c = regularized_limit(travel, initial, lower ? j.six_min[3 + i] : j.six_max[3 + i], lower);
+                    T f_raw = j.pen_a[i] * c + j.sacc[3 + i];
                     T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
-                    if (row_live(c, f)) stamp_angular(lhs, rhs, is_a ? -wa : wa, j.pen_a[2], f);
+                    if (!row_live(c, f)) continue;
+                    stamp_angular(lhs, rhs, g, j.pen_a[i], f);
                 }
+            }
+        } else if (fixed) {
+            V3<T> diff = quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref);
+            V3<T> diff0 = quat_diff_vec(qmul(conj(rot0[j.a]), rot0[j.b]), j.q_ref);
+            for (int k = 0; k < 3; k++) {
+                T c = diff[k] - C<T>(K::ALPHA) * diff0[k];
+                T f = j.pen_a[k] * c + j.lam_a[k];
+                if (!row_live(c, f)) continue;
+                V3<T> e = VZERO<T>();
+                e[k] = T(1);
+                V3<T> dir = qrot(a.rot, e);
+                stamp_angular(lhs, rhs, is_a ? -dir : dir, j.pen_a[k], f);
+            }
+        }
+        // one-sided limit rows (assembly.rs:807-881)
+        if (j.has_lim && j.kind == AVBD_JOINT_REVOLUTE) {
+            T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+            int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
+            if (st >= 0) {
+                bool lower = st == 1;
+                T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
+                T f_raw = j.pen_a[2] * c + j.acc_lim;
+                T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
+                if (row_live(c, f)) stamp_angular(lhs, rhs, is_a ? -wa : wa, j.pen_a[2], f);
+            }
+        } else if (j.has_lim && j.kind == AVBD_JOINT_PRISMATIC) {
+            T sv = dot(pb - pa, wa) - j.ref_val;
+            int st = warm_limit_state(sv, j.lo, j.hi, C<T>(K::LIMIT_SLOP_LIN), j.lim_dual);
+            if (st >= 0) {
+                bool lower = st == 1;
+                V3<T> axis0 = normalize_or(qrot(rot0[j.a], j.ax_a), VZ<T>());
+                T initial = dot(pb0 - pa0, axis0) - j.ref_val;
+                T c = regularized_limit(sv, initial, lower ? j.lo : j.hi, lower);
+                T f_raw = j.pen_l[2] * c + j.lim_dual;
+                T f = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
+                if (row_live(c, f)) stamp_row(lhs, rhs, wa, j.pen_l[2], f, r_plain, lsign);
             }
         }
     }
@@ -1513,57 +1759,183 @@ template <class T> struct Engine {
                 }
             }
         }
-        for (Joint<T>& j : joints) {
-            const Body<T>& a = bodies[j.a];
-            const Body<T>& b = bodies[j.b];
-            V3<T> pa = a.pos + qrot(a.rot, j.la);
-            V3<T> pb = b.pos + qrot(b.rot, j.lb);
-            V3<T> pa0 = pos0[j.a] + qrot(rot0[j.a], j.la);
-            V3<T> pb0 = pos0[j.b] + qrot(rot0[j.b], j.lb);
-            V3<T> live = pa - pb, c0v = pa0 - pb0;
+        for (Joint<T>& j : joints) dual_joint(j);
+    }
+
+    // joints_ext.rs:574-896: the joint rows' multipliers and penalties.
+    void dual_joint(Joint<T>& j) {
+        const Body<T>& a = bodies[j.a];
+        const Body<T>& b = bodies[j.b];
+        V3<T> pa = a.pos + qrot(a.rot, j.la);
+        V3<T> pb = b.pos + qrot(b.rot, j.lb);
+        V3<T> pa0 = pos0[j.a] + qrot(rot0[j.a], j.la);
+        V3<T> pb0 = pos0[j.b] + qrot(rot0[j.b], j.lb);
+        V3<T> live = pa - pb, c0v = pa0 - pb0;
+        const T eps = C<T>(K::C_EPS);
+        auto ramp = [](T pen, T c, float beta, float cap) { return fmn(pen + C<T>(beta) * std::fabs(c), C<T>(cap)); };
+        // a finite joint stiffness makes the anchor and hinge rows of ball and
+        // revolute joints springs (penalty k, no multiplier)
+        const bool soft = joint_k > T(0) && (j.kind == AVBD_JOINT_BALL || j.kind == AVBD_JOINT_REVOLUTE);
+        if (j.kind == AVBD_JOINT_BALL || j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_FIXED) {
+            const bool fixed = j.kind == AVBD_JOINT_FIXED;
+            V3<T> lv = fixed ? live + qrot(a.rot, j.dref) : live;
+            V3<T> iv = fixed ? c0v + qrot(rot0[j.a], j.dref) : c0v;
             for (int k = 0; k < 3; k++) {
-                T c = live[k] - C<T>(K::ALPHA) * c0v[k];
-                if (joint_k > T(0)) {
+                T c = lv[k] - C<T>(K::ALPHA) * iv[k];
+                if (soft) {
                     j.pen_l[k] = joint_k;
-                } else if (std::fabs(c) >= C<T>(K::C_EPS)) {
-                    {
-                        j.lam_l[k] += j.pen_l[k] * c;
-                        j.pen_l[k] = fmn(j.pen_l[k] + C<T>(K::BETA) * std::fabs(c), C<T>(K::PENALTY_MAX));
+                } else if (std::fabs(c) >= eps) {
+                    j.lam_l[k] += j.pen_l[k] * c;
+                    j.pen_l[k] = ramp(j.pen_l[k], c, K::BETA, K::PENALTY_MAX);
+                }
+            }
+        } else if (j.kind == AVBD_JOINT_PRISMATIC) {
+            V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+            V3<T> u, v;
+            tangent_basis(wa, u, v);
+            V3<T> axs[2] = {u, v};
+            for (int li = 0; li < 2; li++) {
+                T c = dot(live - C<T>(K::ALPHA) * c0v, axs[li]);
+                if (std::fabs(c) >= eps) {
+                    j.lam_l[li] += j.pen_l[li] * c;
+                    j.pen_l[li] = ramp(j.pen_l[li], c, K::BETA, K::PENALTY_MAX);
+                }
+            }
+        } else if (j.kind == AVBD_JOINT_DISTANCE) {
+            T c = (len(live) - j.ref_val) - C<T>(K::ALPHA) * (len(c0v) - j.ref_val);
+            if (std::fabs(c) >= eps) {
+                j.lam_l[0] += j.pen_l[0] * c;
+                j.pen_l[0] = ramp(j.pen_l[0], c, K::BETA, K::PENALTY_MAX);
+            }
+        } else if (j.kind == AVBD_JOINT_ROPE) {
+            T ln = len(live);
+            if (ln > j.ref_val) {
+                T c = (ln - j.ref_val) - C<T>(K::ALPHA) * (len(c0v) - j.ref_val);
+                if (std::fabs(c) >= eps) {
+                    j.lam_l[0] = fmx(j.lam_l[0] + j.pen_l[0] * c, T(0));
+                    j.pen_l[0] = ramp(j.pen_l[0], c, K::BETA, K::LIM_PEN_MAX);
+                }
+            } else {
+                j.lam_l[0] = T(0);
+            }
+        } else if (j.kind == AVBD_JOINT_SIXDOF) {
+            for (int i = 0; i < 3; i++) {
+                V3<T> e = VZERO<T>();
+                e[i] = T(1);
+                V3<T> dir = normalize_or(qrot(a.rot, e), e);
+                if (j.six_cfg[i] == AVBD_AXIS_LOCKED) {
+                    T c = dot((pb - pa) - qrot(a.rot, j.dref), dir);
+                    if (std::fabs(c) >= eps) {
+                        j.lam_l[i] += j.pen_l[i] * c;
+                        j.pen_l[i] = ramp(j.pen_l[i], c, K::BETA, K::PENALTY_MAX);
+                    }
+                } else if (j.six_cfg[i] == AVBD_AXIS_LIMITED) {
+                    T sep = dot((pb - pa) - qrot(a.rot, j.dref), dir);
+                    int st = warm_limit_state(sep, j.six_min[i], j.six_max[i], C<T>(K::LIMIT_SLOP_LIN), j.sacc[i]);
+                    if (st >= 0) {
+                        bool lower = st == 1;
+                        V3<T> axis0 = normalize_or(qrot(rot0[j.a], e), e);
+                        T initial = dot((pb0 - pa0) - qrot(rot0[j.a], j.dref), axis0);
+                        T c = regularized_limit(sep, initial, lower ? j.six_min[i] : j.six_max[i], lower);
+                        if (std::fabs(c) >= eps) {
+                            T f = j.pen_l[i] * c + j.sacc[i];
+                            j.sacc[i] = lower ? fmn(f, T(0)) : fmx(f, T(0));
+                            j.pen_l[i] = ramp(j.pen_l[i], c, K::BETA, K::LIM_PEN_MAX);
+                        }
+                    } else {
+                        j.sacc[i] = T(0);
                     }
                 }
             }
-            if (j.kind == AVBD_JOINT_REVOLUTE) {
-                V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
-                V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
-                V3<T> t1, t2;
-                tangent_basis(axa0, t1, t2);
-                V3<T> ts[2] = {t1, t2};
-                for (int li = 0; li < 2; li++) {
-                    T c = dot(ts[li], axa - axb) - C<T>(K::ALPHA) * dot(ts[li], axa0 - axb0);
-                    if (joint_k > T(0)) {
-                        j.pen_a[li] = joint_k;
-                        continue;
+            V3<T> diff = quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref);
+            for (int i = 0; i < 3; i++) {
+                V3<T> e = VZERO<T>();
+                e[i] = T(1);
+                if (j.six_cfg[3 + i] == AVBD_AXIS_LOCKED) {
+                    T c = dot(diff, e);
+                    if (std::fabs(c) >= eps) {
+                        j.lam_a[i] += j.pen_a[i] * c;
+                        j.pen_a[i] = ramp(j.pen_a[i], c, K::BETA_ANG, K::PENALTY_MAX);
                     }
-                    if (std::fabs(c) < C<T>(K::C_EPS)) continue;
-                    j.lam_a[li] = j.pen_a[li] * c + j.lam_a[li];
-                    j.pen_a[li] = fmn(j.pen_a[li] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::PENALTY_MAX));
-                }
-                if (j.has_lim) {
-                    T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
-                    int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
+                } else if (j.six_cfg[3 + i] == AVBD_AXIS_LIMITED) {
+                    T travel = twist(a.rot, b.rot, e) - quat_twist(j.q_ref, e);
+                    int st = warm_limit_state(travel, j.six_min[3 + i], j.six_max[3 + i], C<T>(K::LIMIT_SLOP_ANG),
+                                              j.sacc[3 + i]);
                     if (st >= 0) {
                         bool lower = st == 1;
-                        T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
-                        T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
-                        if (std::fabs(c) >= C<T>(K::C_EPS)) {
-                            T f = j.pen_a[2] * c + j.acc_lim;
-                            j.acc_lim = lower ? fmn(f, T(0)) : fmx(f, T(0));
-                            j.pen_a[2] = fmn(j.pen_a[2] + C<T>(K::BETA_ANG) * std::fabs(c), C<T>(K::LIM_PEN_MAX));
+                        T initial = twist(rot0[j.a], rot0[j.b], e) - quat_twist(j.q_ref, e);
+                        T c = regularized_limit(travel, initial, lower ? j.six_min[3 + i] : j.six_max[3 + i], lower);
+                        if (std::fabs(c) >= eps) {
+                            T f = j.pen_a[i] * c + j.sacc[3 + i];
+                            j.sacc[3 + i] = lower ? fmn(f, T(0)) : fmx(f, T(0));
+                            j.pen_a[i] = ramp(j.pen_a[i], c, K::BETA_ANG, K::LIM_PEN_MAX);
                         }
                     } else {
-                        j.acc_lim = T(0);
+                        j.sacc[3 + i] = T(0);
                     }
                 }
+            }
+        }
+        // angular equality rows
+        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC) {
+            V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
+            V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
+            V3<T> t1, t2;
+            tangent_basis(axa0, t1, t2);
+            V3<T> ts[2] = {t1, t2};
+            for (int li = 0; li < 2; li++) {
+                T c = dot(ts[li], axa - axb) - C<T>(K::ALPHA) * dot(ts[li], axa0 - axb0);
+                if (soft) {
+                    j.pen_a[li] = joint_k;
+                    continue;
+                }
+                if (std::fabs(c) < eps) continue;
+                j.lam_a[li] = j.pen_a[li] * c + j.lam_a[li];
+                j.pen_a[li] = ramp(j.pen_a[li], c, K::BETA_ANG, K::PENALTY_MAX);
+            }
+        } else if (j.kind == AVBD_JOINT_FIXED) {
+            V3<T> diff = quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref);
+            V3<T> diff0 = quat_diff_vec(qmul(conj(rot0[j.a]), rot0[j.b]), j.q_ref);
+            for (int k = 0; k < 3; k++) {
+                T c = diff[k] - C<T>(K::ALPHA) * diff0[k];
+                if (std::fabs(c) < eps) continue;
+                j.lam_a[k] += j.pen_a[k] * c;
+                j.pen_a[k] = ramp(j.pen_a[k], c, K::BETA_ANG, K::PENALTY_MAX);
+            }
+        }
+        // one-sided limits
+        if (j.has_lim && j.kind == AVBD_JOINT_REVOLUTE) {
+            T angle = wrap_pi(twist(a.rot, b.rot, j.ax_a) - j.ref_val);
+            int st = warm_limit_state(angle, j.lo, j.hi, C<T>(K::LIMIT_SLOP_ANG), j.acc_lim);
+            if (st >= 0) {
+                bool lower = st == 1;
+                T initial = wrap_pi(twist(rot0[j.a], rot0[j.b], j.ax_a) - j.ref_val);
+                T c = regularized_limit(angle, initial, lower ? j.lo : j.hi, lower);
+                if (std::fabs(c) >= eps) {
+                    T f = j.pen_a[2] * c + j.acc_lim;
+                    j.acc_lim = lower ? fmn(f, T(0)) : fmx(f, T(0));
+                    j.pen_a[2] = ramp(j.pen_a[2], c, K::BETA_ANG, K::LIM_PEN_MAX);
+                }
+            } else {
+                j.acc_lim = T(0);
+            }
+        } else if (j.has_lim && j.kind == AVBD_JOINT_PRISMATIC) {
+            V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+            T sv = dot(pb - pa, wa) - j.ref_val;
+            int st = warm_limit_state(sv, j.lo, j.hi, C<T>(K::LIMIT_SLOP_LIN), j.lim_dual);
+            if (st >= 0) {
+                bool lower = st == 1;
+                V3<T> axis0 = normalize_or(qrot(rot0[j.a], j.ax_a), VZ<T>());
+                T initial = dot(pb0 - pa0, axis0) - j.ref_val;
+                T c = regularized_limit(sv, initial, lower ? j.lo : j.hi, lower);
+                if (std::fabs(c) >= eps) {
+                    T f_raw = j.pen_l[2] * c + j.lim_dual;
+                    j.lim_dual = lower ? fmn(f_raw, T(0)) : fmx(f_raw, T(0));
+                    j.pen_l[2] = ramp(j.pen_l[2], c, K::BETA, K::LIM_PEN_MAX);
+                }
+            } else {
+                j.acc_lim = T(0);
+                j.lim_dual = T(0);
             }
         }
     }
@@ -1777,6 +2149,8 @@ template <class T> struct Engine {
             b.torque = VZERO<T>();
             b.angvel = b.angvel + mat3_vec(inv, tq) * dt;
         }
+        motor_impulse();
+        rope_impulse();
         pre_vel.resize(n);
         for (uint32_t h = 0; h < n; h++) pre_vel[h] = bodies[h].vel;  // mod.rs:874-876
         if (prm.enable_ccd) ccd_pass();
@@ -1809,7 +2183,8 @@ template <class T> struct Engine {
                 j.lam_a[k] *= ag;
                 j.pen_l[k] = fclamp(j.pen_l[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
                 j.pen_a[k] = fclamp(j.pen_a[k] * C<T>(K::GAMMA), C<T>(K::PENALTY_MIN), C<T>(K::PENALTY_MAX));
-                if (joint_k > T(0)) {  // soft rows: anchors and hinge alignment (not the limit)
+                if (joint_k > T(0) && (j.kind == AVBD_JOINT_BALL || j.kind == AVBD_JOINT_REVOLUTE)) {
+                    // soft rows: anchors and hinge alignment (not the limit)
                     j.pen_l[k] = joint_k;
                     if (k < 2) j.pen_a[k] = joint_k;
                 }
@@ -1953,11 +2328,26 @@ template <class T> struct Engine {
     }
 
     int add_joint(const AvbdJointDesc& d, uint32_t& handle) {  // mod.rs:1310-1529
-        for (int k = 0; k < 3; k++)
-            if (!std::isfinite(d.local_anchor_a[k]) || !std::isfinite(d.local_anchor_b[k]) ||
-                !std::isfinite(d.local_axis_a[k]) || !std::isfinite(d.local_axis_b[k]))
+        // validate_joint (migration.rs:160-330): anchors and axes finite, bounds ordered, motors finite
+        auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
+        auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
+        if (d.kind > AVBD_JOINT_SIXDOF) return AVBD_ERR_UNSUPPORTED;
+        if (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+        const bool axial = d.kind == AVBD_JOINT_REVOLUTE || d.kind == AVBD_JOINT_PRISMATIC;
+        if (axial) {
+            if (!finite3(d.local_axis_a) || !finite3(d.local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+            if (d.has_limit && !bounds_ok(d.limit_min, d.limit_max)) return AVBD_ERR_JOINT_BAD_BOUNDS;
+            if (d.has_motor && !(std::isfinite(d.motor_speed) && std::isfinite(d.motor_max) && d.motor_max >= 0.0f))
                 return AVBD_ERR_JOINT_NONFINITE;
-        if (d.kind != AVBD_JOINT_BALL && d.kind != AVBD_JOINT_REVOLUTE) return AVBD_ERR_UNSUPPORTED;
+        }
+        if (d.kind == AVBD_JOINT_SIXDOF)
+            for (int k = 0; k < 6; k++) {
+                if (d.axis_config[k] > AVBD_AXIS_LIMITED) return AVBD_ERR_INVALID_ARG;
+                if (d.axis_config[k] == AVBD_AXIS_LIMITED && !bounds_ok(d.axis_min[k], d.axis_max[k]))
+                    return AVBD_ERR_JOINT_BAD_BOUNDS;
+            }
+        if (d.kind == AVBD_JOINT_ROPE && !(std::isfinite(d.max_distance) && d.max_distance > 0.0f))
+            return AVBD_ERR_JOINT_BAD_BOUNDS;
         wake_body(d.body_a);
         wake_body(d.body_b);
         if (d.body_a == d.body_b) return AVBD_ERR_JOINT_SELF;
@@ -1968,18 +2358,49 @@ template <class T> struct Engine {
         j.lb = {T(d.local_anchor_b[0]), T(d.local_anchor_b[1]), T(d.local_anchor_b[2])};
         j.ax_a = VX<T>(); j.ax_b = VX<T>();
         j.ref_val = T(0);
-        if (d.kind == AVBD_JOINT_REVOLUTE) {
+        j.q_ref = Qt<T>{T(0), T(0), T(0), T(1)};
+        j.dref = VZERO<T>();
+        // resolve_joint (joint.rs:1251-1400)
+        const Body<T>& ba = bodies[j.a];
+        const Body<T>& bb = bodies[j.b];
+        if (axial) {
             V3<T> aa{T(d.local_axis_a[0]), T(d.local_axis_a[1]), T(d.local_axis_a[2])};
             V3<T> ab{T(d.local_axis_b[0]), T(d.local_axis_b[1]), T(d.local_axis_b[2])};
             if (len2(aa) < C<T>(K::DEGENERATE_LEN2) || len2(ab) < C<T>(K::DEGENERATE_LEN2)) return AVBD_ERR_JOINT_BAD_AXIS;
             j.ax_a = normalize_or(aa, VZ<T>());
             j.ax_b = normalize_or(ab, VZ<T>());
-            j.ref_val = hinge_twist(bodies[j.a].rot, bodies[j.b].rot, j.ax_a);
+            if (d.kind == AVBD_JOINT_REVOLUTE) {
+                j.ref_val = hinge_twist(ba.rot, bb.rot, j.ax_a);
+            } else {
+                V3<T> wa = normalize_or(qrot(ba.rot, j.ax_a), VZ<T>());
+                V3<T> pa0 = ba.pos + qrot(ba.rot, j.la);
+                V3<T> pb0 = bb.pos + qrot(bb.rot, j.lb);
+                j.ref_val = dot(pb0 - pa0, wa);
+            }
             j.has_lim = d.has_limit != 0;
             j.lo = T(d.limit_min);
             j.hi = T(d.limit_max);
+            j.has_mot = d.has_motor != 0;
+            j.mot_speed = T(d.motor_speed);
+            j.mot_max = T(d.motor_max);
+        } else if (d.kind == AVBD_JOINT_FIXED || d.kind == AVBD_JOINT_SIXDOF) {
+            j.q_ref = qmul(conj(ba.rot), bb.rot);
+            V3<T> ra = qrot(ba.rot, j.la), rb = qrot(bb.rot, j.lb);
+            j.dref = qrot(conj(ba.rot), (bb.pos + rb) - (ba.pos + ra));
+            for (int k = 0; k < 6; k++) {
+                j.six_cfg[k] = d.kind == AVBD_JOINT_SIXDOF ? d.axis_config[k] : AVBD_AXIS_FREE;
+                j.six_min[k] = T(d.axis_min[k]);
+                j.six_max[k] = T(d.axis_max[k]);
+            }
+        } else if (d.kind == AVBD_JOINT_DISTANCE) {
+            V3<T> ra = qrot(ba.rot, j.la), rb = qrot(bb.rot, j.lb);
+            j.ref_val = len((bb.pos + rb) - (ba.pos + ra));
+        } else if (d.kind == AVBD_JOINT_ROPE) {
+            j.ref_val = T(d.max_distance);
         }
         j.acc_lim = T(0);
+        j.lim_dual = T(0);
+        for (int k = 0; k < 6; k++) j.sacc[k] = T(0);
         for (int k = 0; k < 3; k++) {
             j.lam_l[k] = j.lam_a[k] = T(0);
             j.pen_l[k] = j.pen_a[k] = C<T>(K::JOINT_PENALTY_INIT);
@@ -2349,6 +2770,8 @@ int oracle_export_state(OracleWorld* w, AvbdBody* bodies, AvbdBodyAux* aux, Avbd
                     s.pen_l[c] = float(j.pen_l[c]); s.pen_a[c] = float(j.pen_a[c]);
                 }
                 s.acc_lim = float(j.acc_lim);
+                s.lim_dual = float(j.lim_dual);
+                for (int c = 0; c < 6; c++) s.sacc[c] = float(j.sacc[c]);
             }
     });
     return AVBD_OK;
@@ -2402,6 +2825,8 @@ int oracle_import_state(OracleWorld* w, const AvbdBody* bodies, const AvbdBodyAu
                     j.pen_l[c] = TT(joints[i].pen_l[c]); j.pen_a[c] = TT(joints[i].pen_a[c]);
                 }
                 j.acc_lim = TT(joints[i].acc_lim);
+                j.lim_dual = TT(joints[i].lim_dual);
+                for (int c = 0; c < 6; c++) j.sacc[c] = TT(joints[i].sacc[c]);
             }
     });
     return AVBD_OK;

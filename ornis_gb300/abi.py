@@ -18,6 +18,7 @@ AVBD_ERR_JOINT_SELF = -10
 AVBD_ERR_JOINT_HANDLES = -11
 AVBD_ERR_JOINT_BAD_AXIS = -12
 AVBD_ERR_JOINT_NONFINITE = -13
+AVBD_ERR_JOINT_BAD_BOUNDS = -14
 
 # limits of the allocation-free entry point (avbd_scene_step_static)
 STATIC_MAX_BODIES = 128
@@ -40,6 +41,15 @@ FLAG_TRIGGER = 1
 
 JOINT_BALL = 0
 JOINT_REVOLUTE = 1
+JOINT_PRISMATIC = 2
+JOINT_FIXED = 3
+JOINT_DISTANCE = 4
+JOINT_ROPE = 5
+JOINT_SIXDOF = 6
+
+AXIS_FREE = 0
+AXIS_LOCKED = 1
+AXIS_LIMITED = 2
 
 MAX_POINTS = 8
 
@@ -86,6 +96,13 @@ class AvbdJointDesc(C.Structure):
         ("has_limit", C.c_int32),
         ("limit_min", C.c_float),
         ("limit_max", C.c_float),
+        ("has_motor", C.c_int32),
+        ("motor_speed", C.c_float),
+        ("motor_max", C.c_float),
+        ("max_distance", C.c_float),
+        ("axis_config", C.c_uint32 * 6),
+        ("axis_min", C.c_float * 6),
+        ("axis_max", C.c_float * 6),
     ]
 
 
@@ -139,6 +156,8 @@ class AvbdJointState(C.Structure):
         ("pen_l", F3),
         ("pen_a", F3),
         ("acc_lim", C.c_float),
+        ("lim_dual", C.c_float),
+        ("sacc", C.c_float * 6),
     ]
 
 
@@ -221,7 +240,10 @@ def default_params(gravity=(0.0, -9.81, 0.0), step_dt=1.0 / 60.0, iterations=10,
 
 
 def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0),
-               limit=None):
+               limit=None, motor=None, max_distance=0.0, axes=None):
+    """A joint record.  limit = (min, max); motor = (target speed, max
+    torque or force); axes (sixdof) = 6 entries, each "free", "locked" or
+    (min, max), linear x y z then angular x y z."""
     d = AvbdJointDesc()
     d.kind = kind
     d.body_a = a
@@ -233,4 +255,16 @@ def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0
     if limit is not None:
         d.has_limit = 1
         d.limit_min, d.limit_max = float(limit[0]), float(limit[1])
+    if motor is not None:
+        d.has_motor = 1
+        d.motor_speed, d.motor_max = float(motor[0]), float(motor[1])
+    d.max_distance = float(max_distance)
+    for i, ax in enumerate(axes or ()):
+        if ax == "free":
+            d.axis_config[i] = AXIS_FREE
+        elif ax == "locked":
+            d.axis_config[i] = AXIS_LOCKED
+        else:
+            d.axis_config[i] = AXIS_LIMITED
+            d.axis_min[i], d.axis_max[i] = float(ax[0]), float(ax[1])
     return d

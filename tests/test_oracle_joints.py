@@ -1,0 +1,165 @@
+"""The joint kinds beyond Ball and Revolute on the oracle: the reference's
+behavioural gates (crates/physics/tests/avbd_engine.rs) restated — hinge
+motor (:552-596), prismatic slider on its line and at its limit (:598-646),
+prismatic motor (:782-822), fixed weld (:891-938), distance rod (:940-968),
+six-DOF all locked / free axis / angular limit (:1452-1556) — plus a rope
+that never exceeds its length, and the admission errors of validate_joint
+(migration.rs:160-330).  Reference order, dt 1/60, 10 iterations."""
+import math
+
+import numpy as np
+
+from ornis_gb300 import abi
+
+import oracle_api as O
+
+DT = 1.0 / 60.0
+
+
+def world(recs, gravity=(0.0, -9.81, 0.0)):
+    w = O.OracleWorld(abi.default_params(gravity=gravity))
+    w.add_bodies(O.bodies_to_array(recs))
+    return w
+
+
+def add(w, d):
+    rc, h = w.add_joint(d)
+    assert rc == 0, rc
+    return h
+
+
+def z_twist(q):  # avbd_engine.rs:502-504
+    return 2.0 * math.asin(float(q[2]))
+
+
+def test_hinge_motor_spins_up():
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.05], [0, 0, 0], 0.0)
+    anchor.flags = abi.FLAG_TRIGGER
+    w = world([anchor, O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 0, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_REVOLUTE, 0, 1, [0, 0, 0], [0, 0, 0], [0, 0, 1], [0, 0, 1], motor=(3.0, 20.0)))
+    for _ in range(300):
+        w.step(DT)
+    mean = 0.0
+    for _ in range(60):
+        w.step(DT)
+        mean += w.bodies()["angular_velocity"][1][2]
+    assert abs(mean / 60.0 - 3.0) < 0.6
+
+
+def test_prismatic_slider_holds_line_and_limit():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.25, 0.25, 0.25], [0, 0, 0], 0.0),
+               O.body_new(abi.SHAPE_SPHERE, [0.25], [0, -2.9, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [0, 0, 0], [0, 1, 0], [0, 1, 0], [0, 1, 0], limit=(-2.0, 0.0)))
+    for _ in range(300):
+        w.step(DT)
+        p = w.bodies()["position"][1]
+        assert abs(p[0]) < 0.08 and abs(p[2]) < 0.08, p
+    assert -5.4 < w.bodies()["position"][1][1] < -4.4
+
+
+def test_prismatic_motor_drives():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.25, 0.25, 0.25], [0, 0, 0], 0.0),
+               O.body_new(abi.SHAPE_SPHERE, [0.25], [1, 0, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [0, 0, 0], [-1, 0, 0], [1, 0, 0], [1, 0, 0], motor=(2.0, 50.0)))
+    for _ in range(300):
+        w.step(DT)
+    b = w.bodies()
+    assert abs(b["velocity"][1][0] - 2.0) < 0.4
+    assert abs(b["position"][1][1]) < 0.15 and abs(b["position"][1][2]) < 0.1
+
+
+def test_fixed_weld_holds():
+    w = world([O.body_new(abi.SHAPE_BOX, [5, 1, 5], [0, -1, 0], 0.0),
+               O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [-0.5, 3, 0], 1.0),
+               O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0.5, 3, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_FIXED, 1, 2, [0.5, 0, 0], [-0.5, 0, 0]))
+    for _ in range(300):
+        w.step(DT)
+    b = w.bodies()
+    assert abs(np.linalg.norm(b["position"][2] - b["position"][1]) - 1.0) < 0.15
+    assert b["position"][1][1] > 0.2 and b["position"][2][1] > 0.2
+
+
+def test_distance_rod_holds_length():
+    w = world([O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 0, 0], 0.0),
+               O.body_new(abi.SHAPE_SPHERE, [0.25], [2, 0, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_DISTANCE, 0, 1, [0, 0, 0], [0, 0, 0]))
+    swung = False
+    for _ in range(300):
+        w.step(DT)
+        p = w.bodies()["position"][1]
+        assert abs(np.linalg.norm(p) - 2.0) < 0.25
+        swung |= p[1] < -0.5
+    assert swung
+
+
+def test_rope_never_stretches_past_its_length():
+    # a bob 1 m from the anchor on a 2 m rope: it falls slack, then the rope
+    # catches it and it swings on a 2 m radius
+    w = world([O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 0, 0], 0.0),
+               O.body_new(abi.SHAPE_SPHERE, [0.25], [1, 0, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_ROPE, 0, 1, [0, 0, 0], [0, 0, 0], max_distance=2.0))
+    longest = 0.0
+    for _ in range(300):
+        w.step(DT)
+        longest = max(longest, float(np.linalg.norm(w.bodies()["position"][1])))
+    assert 1.9 < longest < 2.25
+
+
+def test_sixdof_all_locked_behaves_like_fixed():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
+               O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 1.4, 0], 1.0)])
+    add(w, abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0], axes=["locked"] * 6))
+    for _ in range(180):
+        w.step(DT)
+    b = w.bodies()
+    assert abs((b["position"][1] - b["position"][0])[1] - 1.4) < 0.05
+
+
+def test_sixdof_free_axis_slides_but_locked_holds():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
+               O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [1, 0, 0], 1.0)], gravity=(0, 0, 0))
+    add(w, abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0],
+                          axes=["free", "locked", "locked", "locked", "locked", "locked"]))
+    b = w.bodies()
+    b["velocity"][1] = [3.0, 1.0, 0.0]
+    w.set_bodies(b)
+    for _ in range(60):
+        w.step(DT)
+    b = w.bodies()
+    d = b["position"][1] - b["position"][0]
+    assert d[0] > 1.5 and abs(d[1]) < 0.08
+
+
+def test_sixdof_angular_limit_blocks_spin():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 0.0),
+               O.body_new(abi.SHAPE_BOX, [0.4, 0.4, 0.4], [0, 0, 0], 1.0)], gravity=(0, 0, 0))
+    add(w, abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0],
+                          axes=["locked"] * 5 + [(-0.2, 0.2)]))
+    b = w.bodies()
+    b["angular_velocity"][1] = [0.0, 0.0, 8.0]
+    w.set_bodies(b)
+    for _ in range(120):
+        w.step(DT)
+    assert abs(z_twist(w.bodies()["orientation"][1])) < 0.4
+
+
+def test_joint_admission_errors():
+    w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
+               O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [2, 0, 0], 1.0)])
+    nan = float("nan")
+    cases = [
+        (abi.joint_desc(abi.JOINT_BALL, 0, 1, [nan, 0, 0], [0, 0, 0]), abi.AVBD_ERR_JOINT_BAD_AXIS),
+        (abi.joint_desc(abi.JOINT_REVOLUTE, 0, 1, [0, 0, 0], [0, 0, 0], [0, 0, 1], [0, 0, 1], limit=(1.0, -1.0)),
+         abi.AVBD_ERR_JOINT_BAD_BOUNDS),
+        (abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [0, 0, 0], [0, 0, 0], [1, 0, 0], [1, 0, 0], motor=(nan, 1.0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [0, 0, 0], [0, 0, 0], [0, 0, 0], [1, 0, 0]),
+         abi.AVBD_ERR_JOINT_BAD_AXIS),
+        (abi.joint_desc(abi.JOINT_ROPE, 0, 1, [0, 0, 0], [0, 0, 0], max_distance=0.0), abi.AVBD_ERR_JOINT_BAD_BOUNDS),
+        (abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0], axes=["locked"] * 5 + [(0.3, -0.3)]),
+         abi.AVBD_ERR_JOINT_BAD_BOUNDS),
+    ]
+    for d, code in cases:
+        assert w.add_joint(d)[0] == code
+    assert w.add_joint(abi.joint_desc(abi.JOINT_FIXED, 0, 1, [0, 0, 0], [0, 0, 0]))[0] == 0
