@@ -479,7 +479,8 @@ int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* bodies, uin
 /* Advance the world `steps` steps of `substeps` fixed substeps (as
  * avbd_world_step_graph) and keep a device checkpoint of the full step
  * state every `checkpoint_every` steps, for avbd_adjoint_backward.  Worlds
- * with rolling / torsion friction return AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
+ * with rolling / torsion friction, motors, or joints other than Ball and
+ * Revolute return AVBD_ERR_UNSUPPORTED.  The rollout runs the split primal launch
  * (avbd_set_tuning lanes 0) and orders every body's contact pairs (the
  * static bodies' too), which the world keeps afterwards; retuning the
  * world before the backward invalidates the recording.  A new forward

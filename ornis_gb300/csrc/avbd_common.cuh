@@ -116,18 +116,63 @@ static __device__ __forceinline__ int32_t find_old_pair(const DW& w, uint32_t a,
     return -1;
 }
 
-// sleep.rs:30-40 (Ball, Revolute)
+// sixdof axis configuration word: 2 bits per axis (linear x y z, angular x y z)
+static __host__ __device__ __forceinline__ uint32_t axis_cfg(uint32_t cfg, int axis) { return (cfg >> (2 * axis)) & 3u; }
+// (min, max) of sixdof axis k
+static __device__ __forceinline__ float2 axis_window(const DW& w, uint32_t j, int k) {
+    float4 v = w.j_six[3 * (size_t)j + (k >> 1)];
+    return (k & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+}
+// sleep.rs:30-105: how far a joint is from its assembly pose
 static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];
     V3 pa = ld3(w.pos[ab.x]), pb = ld3(w.pos[ab.y]);
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     V3 delta = (pb + qrot(qb, ld3(w.j_lb[j]))) - (pa + qrot(qa, ld3(w.j_la[j])));
-    if (w.j_kind[j] == AVBD_JOINT_BALL) return len(delta);
+    const uint32_t kind = w.j_kind[j];
+    if (kind == AVBD_JOINT_BALL) return len(delta);
     V3 axis = qrot(qa, ld3(w.j_axa[j]));
-    return fmaxf(len(delta), len(axis - qrot(qb, ld3(w.j_axb[j]))));
+    if (kind == AVBD_JOINT_REVOLUTE) return fmaxf(len(delta), len(axis - qrot(qb, ld3(w.j_axb[j]))));
+    const float refv = w.j_ref[j].x;
+    if (kind == AVBD_JOINT_FIXED)
+        return fmaxf(len(delta - qrot(qa, ld3(w.j_dref[j]))), len(quat_diff_vec(qmul(conj(qa), qb), ldq(w.j_qref[j]))));
+    if (kind == AVBD_JOINT_DISTANCE) return fabsf(len(delta) - refv);
+    if (kind == AVBD_JOINT_ROPE) return fmaxf(len(delta) - refv, 0.0f);
+    if (kind == AVBD_JOINT_PRISMATIC) {
+        float e = len(delta - axis * dot(delta, axis));
+        float4 lim = w.j_lim[j];
+        if (lim.z != 0.0f) {
+            float value = dot(delta, axis) - refv;
+            e = fmaxf(e, fmaxf(lim.x - value, value - lim.y));
+        }
+        return fmaxf(e, len(axis - qrot(qb, ld3(w.j_axb[j]))));
+    }
+    // sixdof (sleep.rs:86-103)
+    V3 lin = qrot(conj(qa), delta) - ld3(w.j_dref[j]);
+    V3 ang = quat_diff_vec(qmul(conj(qa), qb), ldq(w.j_qref[j]));
+    const uint32_t cfg = w.j_cfg[j];
+    float e = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        float vals[2] = {lin[i], ang[i]};
+        for (int k = 0; k < 2; k++) {
+            const int axis_i = i + 3 * k;
+            const uint32_t c = axis_cfg(cfg, axis_i);
+            float r = 0.0f;
+            if (c == AVBD_AXIS_LOCKED) {
+                r = fabsf(vals[k]);
+            } else if (c == AVBD_AXIS_LIMITED) {
+                float2 win = axis_window(w, j, axis_i);
+                r = fmaxf(fmaxf(win.x - vals[k], vals[k] - win.y), 0.0f);
+            }
+            e = fmaxf(e, r);
+        }
+    }
+    return e;
 }
-// sleep.rs:18-27: a non-dynamic member moved by its driver (no motors here)
+// sleep.rs:18-27: a running motor, or a non-dynamic member moved by its driver
 static __device__ __forceinline__ bool joint_driven(const DW& w, uint32_t j) {
+    const float4 ref = w.j_ref[j];
+    if (ref.z != 0.0f && ref.w > 0.0f) return true;
     uint2 ab = w.j_ab[j];
     uint32_t m[2] = {ab.x, ab.y};
     for (int k = 0; k < 2; k++) {

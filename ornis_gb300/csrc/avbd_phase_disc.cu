@@ -592,7 +592,9 @@ __global__ void k_decay_joints(DW w) {
     float4 pa = make_float4(fclamp(d.x * GAMMA, PENALTY_MIN, PENALTY_MAX), fclamp(d.y * GAMMA, PENALTY_MIN, PENALTY_MAX),
                             fclamp(d.z * GAMMA, PENALTY_MIN, PENALTY_MAX), 0.0f);
     const float K = w.joint_k;
-    if (K > 0.0f) {  // soft rows (anchors and hinge alignment, not the limit) are springs of stiffness K
+    const uint32_t kind = w.j_kind[j];
+    if (K > 0.0f && (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE)) {
+        // soft rows (anchors and hinge alignment, not the limit) are springs of stiffness K
         pl = make_float4(K, K, K, 0.0f);
         pa.x = K;
         pa.y = K;

@@ -99,7 +99,119 @@ __global__ void k_torque(DW w) {
     V3 om = ld3(w.angvel[h]) + mat3_vec(inv, ld3(tq4)) * w.dt;
     w.angvel[h] = st3(om, 0.0f);
 }
-void launch_torque(const DW& w, cudaStream_t st) { k_torque<<<nblk(w.N, 256), 256, 0, st>>>(w); }
+
+// ---- motor and rope impulses (mod.rs:872-873, joints_ext.rs:173-420) ---------
+// Deadbeat velocity impulses of velocity motors (revolute, prismatic) and of
+// stretched ropes, after the torque and before the warm start.  The
+// reference applies them joint by joint in order (each sees the velocities
+// the earlier ones left), so one thread per scene walks that scene's motor
+// and rope joints in joint order: all motors, then all ropes.
+static __device__ V3 ang_inv_wa(const DW& w, uint32_t h, V3 wa) {  // joints_ext.rs:423-437
+    if (!solvable(w, h)) return V0();
+    V3 in = ld3(w.inertia[h]);
+    float iw[3][3], inv[3][3];
+    world_inertia(in, ldq(w.rot[h]), iw);
+    V3 dg{fmaxf(in.x, 0.0f), fmaxf(in.y, 0.0f), fmaxf(in.z, 0.0f)};
+    inverse_symmetric(iw, dg, inv);
+    return mat3_vec(inv, wa);
+}
+static __device__ __forceinline__ float eff_inv_mass(const DW& w, uint32_t h) {  // rows.rs:406-412
+    return is_dynamic(w, h) ? w.inv_mass[h] : 0.0f;
+}
+// JointMotor::velocity_impulse (joint.rs:1172-1177)
+static __device__ __forceinline__ float velocity_impulse(const DW& w, float rate_error, float inv_eff, float max_f) {
+    if (!(w.dt > 0.0f) || max_f <= 0.0f || inv_eff <= 0.0f) return 0.0f;
+    return fclamp(rate_error / inv_eff, -max_f * w.dt, max_f * w.dt);
+}
+static __device__ bool limit_violated(const DW& w, uint32_t j) {  // joints_ext.rs:441-462
+    float4 lim = w.j_lim[j];
+    if (lim.z == 0.0f) return false;
+    uint2 ab = w.j_ab[j];
+    Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
+    float4 axa4 = w.j_axa[j];
+    if (w.j_kind[j] == AVBD_JOINT_REVOLUTE) {
+        float angle = wrap_pi(hinge_twist(qa, qb, ld3(axa4)) - axa4.w);
+        return limit_state(angle, lim.x, lim.y, LIMIT_SLOP_ANG) >= 0;
+    }
+    if (w.j_kind[j] == AVBD_JOINT_PRISMATIC) {
+        V3 wa = normalize_or(qrot(qa, ld3(axa4)), VZ());
+        V3 pa = ld3(w.pos[ab.x]) + qrot(qa, ld3(w.j_la[j])), pb = ld3(w.pos[ab.y]) + qrot(qb, ld3(w.j_lb[j]));
+        return limit_state(dot(pb - pa, wa) - w.j_ref[j].x, lim.x, lim.y, LIMIT_SLOP_LIN) >= 0;
+    }
+    return false;
+}
+static __device__ void motor_impulse(const DW& w, uint32_t j) {  // joints_ext.rs:237-383
+    float4 ref = w.j_ref[j];
+    if (!(ref.w > 0.0f) || limit_violated(w, j)) return;
+    uint2 ab = w.j_ab[j];
+    const uint32_t a = ab.x, b = ab.y;
+    V3 wa = normalize_or(qrot(ldq(w.rot[a]), ld3(w.j_axa[j])), VZ());
+    if (w.j_kind[j] == AVBD_JOINT_REVOLUTE) {
+        float om = dot(ld3(w.angvel[b]) - ld3(w.angvel[a]), wa);
+        V3 ia = ang_inv_wa(w, a, wa), ib = ang_inv_wa(w, b, wa);
+        float k = dot(ia, wa) + dot(ib, wa);
+        if (k < MIN_EFFECTIVE_MASS) return;
+        float dj = velocity_impulse(w, ref.z - om, k, ref.w);
+        if (solvable(w, a)) w.angvel[a] = st3(ld3(w.angvel[a]) + (-dj) * ia, 0.0f);
+        if (solvable(w, b)) w.angvel[b] = st3(ld3(w.angvel[b]) + dj * ib, 0.0f);
+    } else if (w.j_kind[j] == AVBD_JOINT_PRISMATIC) {
+        float v = dot(ld3(w.vel[b]) - ld3(w.vel[a]), wa);
+        float ka = eff_inv_mass(w, a), kb = eff_inv_mass(w, b);
+        float k = ka + kb;
+        if (k < MIN_EFFECTIVE_MASS) return;
+        float dj = velocity_impulse(w, ref.z - v, k, ref.w);
+        if (solvable(w, a)) w.vel[a] = st3(ld3(w.vel[a]) + (-dj) * ka * wa, 0.0f);
+        if (solvable(w, b)) w.vel[b] = st3(ld3(w.vel[b]) + dj * kb * wa, 0.0f);
+    }
+}
+static __device__ void rope_impulse(const DW& w, uint32_t j) {  // joints_ext.rs:173-236
+    uint2 ab = w.j_ab[j];
+    const uint32_t a = ab.x, b = ab.y;
+    V3 xa = ld3(w.pos[a]), xb = ld3(w.pos[b]);
+    V3 pa = xa + qrot(ldq(w.rot[a]), ld3(w.j_la[j])), pb = xb + qrot(ldq(w.rot[b]), ld3(w.j_lb[j]));
+    V3 delta = pb - pa;
+    float ln = len(delta);
+    if (ln <= w.j_ref[j].x) return;
+    V3 n = delta / ln;
+    V3 ra = pa - xa, rb = pb - xb;
+    float ka = eff_inv_mass(w, a), kb = eff_inv_mass(w, b);
+    V3 ta = cross(ra, n), tb = cross(rb, n);
+    float k = ka + kb + dot(ang_inv_wa(w, a, ta), ta) + dot(ang_inv_wa(w, b, tb), tb);
+    if (k < MIN_EFFECTIVE_MASS) return;
+    V3 va = ld3(w.vel[a]) + cross(ld3(w.angvel[a]), ra);
+    V3 vb = ld3(w.vel[b]) + cross(ld3(w.angvel[b]), rb);
+    float vsep = dot(vb - va, n);
+    if (vsep <= 0.0f) return;
+    float dj = -vsep / k;
+    if (solvable(w, a)) {
+        V3 ia = ang_inv_wa(w, a, ta);
+        w.vel[a] = st3(ld3(w.vel[a]) - n * (dj * ka), 0.0f);
+        w.angvel[a] = st3(ld3(w.angvel[a]) - ia * dj, 0.0f);
+    }
+    if (solvable(w, b)) {
+        V3 ib = ang_inv_wa(w, b, tb);
+        w.vel[b] = st3(ld3(w.vel[b]) + n * (dj * kb), 0.0f);
+        w.angvel[b] = st3(ld3(w.angvel[b]) + ib * dj, 0.0f);
+    }
+}
+__global__ void k_joint_impulses(DW w) {
+    uint32_t sc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sc >= (uint32_t)w.S) return;
+    const uint32_t k0 = w.jimp_off[sc], k1 = w.jimp_off[sc + 1];
+    for (uint32_t k = k0; k < k1; k++) motor_impulse(w, w.jimp_list[k]);
+    for (uint32_t k = k0; k < k1; k++)
+        if (w.j_kind[w.jimp_list[k]] == AVBD_JOINT_ROPE) rope_impulse(w, w.jimp_list[k]);
+    if (w.pre_vel)  // the velocity snapshot is taken after the impulses (mod.rs:874-876)
+        for (uint32_t k = k0; k < k1; k++) {
+            uint2 ab = w.j_ab[w.jimp_list[k]];
+            w.pre_vel[ab.x] = w.vel[ab.x];
+            w.pre_vel[ab.y] = w.vel[ab.y];
+        }
+}
+void launch_torque(const DW& w, cudaStream_t st) {
+    k_torque<<<nblk(w.N, 256), 256, 0, st>>>(w);
+    if (w.n_imp) k_joint_impulses<<<nblk(w.S, 64), 64, 0, st>>>(w);
+}
 
 // ---- broadphase ---------------------------------------------------------------
 // shape_min_dimension (rows.rs:373-403)

@@ -111,11 +111,14 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
     }
 }
 
-// Joint rows for body h (assembly.rs:255-881): Ball, Revolute and its limit.
+// Joint rows for body h (assembly.rs:255-881): Ball, Revolute (and its
+// limit), Prismatic (and its limit), Fixed, Distance, Rope, SixDof.
 static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint32_t h, Sys& s) {
     uint2 ab = w.j_ab[j];
+    const uint32_t kind = w.j_kind[j];
     bool is_a = ab.x == h;
     float sign = is_a ? 1.0f : -1.0f;
+    float lsign = is_a ? -1.0f : 1.0f;  // rows measured B minus A flip the gradient
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
     V3 la = ld3(w.j_la[j]), lb = ld3(w.j_lb[j]);
@@ -124,23 +127,86 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
     V3 live = pa - pb, c0v = pa0 - pb0;
     float4 axa4 = w.j_axa[j];
     V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
+    V3 wa = normalize_or(qrot(qa, axa_l), VZ());
     float4 pl = w.j_pen_l[j], ll = w.j_lam_l[j], pa4 = w.j_pen_a[j], la4 = w.j_lam_a[j];
     float penl[3] = {pl.x, pl.y, pl.z}, laml[3] = {ll.x, ll.y, ll.z};
+    float pena[3] = {pa4.x, pa4.y, pa4.z}, lama[3] = {la4.x, la4.y, la4.z};
+    const bool fixed = kind == AVBD_JOINT_FIXED;
+    const V3 dref = fixed || kind == AVBD_JOINT_SIXDOF ? ld3(w.j_dref[j]) : V0();
+    const float4 ref = w.j_ref[j];
+    V3 r_plain = is_a ? qrot(qa, la) : qrot(qb, lb);
     V3 fl = V0();
-    // Ball/Revolute levers carry a zero offset in the weld-offset slot
-    V3 lever = is_a ? qrot(qa, la + V0()) : qrot(qb, lb);
-    for (int k = 0; k < 3; k++) {
-        V3 axis = V0();
-        axis[k] = 1.0f;
-        float cc = live[k] - ALPHA * c0v[k];
-        float f = penl[k] * cc + laml[k];
-        if (!row_live(cc, f)) continue;
-        stamp_row(s, axis, penl[k], f, lever, sign);
-        fl[k] = f;
+    // linear rows
+    if (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE || fixed) {
+        // Ball/Revolute levers carry a zero offset in the weld-offset slot
+        V3 lever = is_a ? qrot(qa, la + (fixed ? dref : V0())) : qrot(qb, lb);
+        V3 lv = fixed ? live + qrot(qa, dref) : live;
+        V3 iv = fixed ? c0v + qrot(qa0, dref) : c0v;
+        for (int k = 0; k < 3; k++) {
+            V3 axis = V0();
+            axis[k] = 1.0f;
+            float cc = lv[k] - ALPHA * iv[k];
+            float f = penl[k] * cc + laml[k];
+            if (!row_live(cc, f)) continue;
+            stamp_row(s, axis, penl[k], f, lever, sign);
+            fl[k] = f;
+        }
+    } else if (kind == AVBD_JOINT_PRISMATIC) {
+        V3 u = tangent_t1(wa);
+        V3 v = cross(u, wa);
+        V3 axs[2] = {u, v};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(live - ALPHA * c0v, axs[li]);
+            float f = penl[li] * cc + laml[li];
+            if (!row_live(cc, f)) continue;
+            stamp_row(s, axs[li], penl[li], f, r_plain, sign);
+            fl = fl + axs[li] * f;
+        }
+    } else if (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE) {
+        float ln = len(live);
+        if (kind == AVBD_JOINT_DISTANCE || ln > ref.x) {
+            V3 dir = ln > NEAR_ZERO ? live / ln : VY();
+            float cc = (ln - ref.x) - ALPHA * (len(c0v) - ref.x);
+            float f = penl[0] * cc + laml[0];
+            if (row_live(cc, f)) {
+                stamp_row(s, dir, penl[0], f, r_plain, sign);
+                fl = dir * f;
+            }
+        }
+    } else if (kind == AVBD_JOINT_SIXDOF) {
+        const uint32_t cfg = w.j_cfg[j];
+        const float4 sa0 = w.j_sacc[2 * (size_t)j];
+        const float sacc[3] = {sa0.x, sa0.y, sa0.z};
+        for (int i = 0; i < 3; i++) {
+            const uint32_t c = axis_cfg(cfg, i);
+            if (c == AVBD_AXIS_FREE) continue;
+            V3 e = V0();
+            e[i] = 1.0f;
+            V3 dir = normalize_or(qrot(qa, e), e);
+            if (c == AVBD_AXIS_LOCKED) {
+                float cc = dot((pb - pa) - qrot(qa, dref), dir);
+                float f = penl[i] * cc + laml[i];
+                if (!row_live(cc, f)) continue;
+                stamp_row(s, dir, penl[i], f, r_plain, lsign);
+            } else {
+                float2 win = axis_window(w, j, i);
+                float sep = dot((pb - pa) - qrot(qa, dref), dir);
+                int stt = warm_limit_state(sep, win.x, win.y, LIMIT_SLOP_LIN, sacc[i]);
+                if (stt < 0) continue;
+                bool lower = stt == 1;
+                V3 axis0 = normalize_or(qrot(qa0, e), e);
+                float initial = dot((pb0 - pa0) - qrot(qa0, dref), axis0);
+                float cc = regularized_limit(sep, initial, lower ? win.x : win.y, lower);
+                float f_raw = penl[i] * cc + sacc[i];
+                float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+                if (!row_live(cc, f)) continue;
+                stamp_row(s, dir, penl[i], f, r_plain, lsign);
+            }
+        }
     }
     {
         // geometric stiffness (rows.rs:69-88, assembly.rs:589-618)
-        V3 r = is_a ? qrot(qa, la + V0()) : -qrot(qb, lb);
+        V3 r = is_a ? qrot(qa, la + (fixed ? dref : V0())) : -qrot(qb, lb);
         float arr[3] = {r.x, r.y, r.z};
         float hm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         for (int k = 0; k < 3; k++) {
@@ -158,22 +224,68 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
         s.h[tri(4, 4)] += len(V3{hm[0][1], hm[1][1], hm[2][1]});
         s.h[tri(5, 5)] += len(V3{hm[0][2], hm[1][2], hm[2][2]});
     }
-    if (w.j_kind[j] != AVBD_JOINT_REVOLUTE) return;
-    V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
-    V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
-    V3 t1 = tangent_t1(axa0);
-    V3 t2 = cross(t1, axa0);
-    V3 ts[2] = {t1, t2};
-    float pens[2] = {pa4.x, pa4.y}, lams[2] = {la4.x, la4.y};
-    for (int li = 0; li < 2; li++) {
-        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
-        float f = pens[li] * cc + lams[li];
-        if (!row_live(cc, f)) continue;
-        stamp_angular(s, is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]), pens[li], f);
+    // angular rows
+    if (kind == AVBD_JOINT_REVOLUTE || kind == AVBD_JOINT_PRISMATIC) {
+        V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
+        V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
+        V3 t1 = tangent_t1(axa0);
+        V3 t2 = cross(t1, axa0);
+        V3 ts[2] = {t1, t2};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+            float f = pena[li] * cc + lama[li];
+            if (!row_live(cc, f)) continue;
+            stamp_angular(s, is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]), pena[li], f);
+        }
+    } else if (kind == AVBD_JOINT_SIXDOF) {
+        const uint32_t cfg = w.j_cfg[j];
+        const Q qref = ldq(w.j_qref[j]);
+        const float4 sa0 = w.j_sacc[2 * (size_t)j], sa1 = w.j_sacc[2 * (size_t)j + 1];
+        const float sacc[3] = {sa0.w, sa1.x, sa1.y};
+        V3 diff = quat_diff_vec(qmul(conj(qa), qb), qref);
+        for (int i = 0; i < 3; i++) {
+            const uint32_t c = axis_cfg(cfg, 3 + i);
+            if (c == AVBD_AXIS_FREE) continue;
+            V3 e = V0();
+            e[i] = 1.0f;
+            V3 dir = normalize_or(qrot(qa, e), e);
+            V3 g = is_a ? -dir : dir;
+            if (c == AVBD_AXIS_LOCKED) {
+                float cc = dot(diff, e);
+                float f = pena[i] * cc + lama[i];
+                if (!row_live(cc, f)) continue;
+                stamp_angular(s, g, pena[i], f);
+            } else {
+                float2 win = axis_window(w, j, 3 + i);
+                float travel = hinge_twist(qa, qb, e) - quat_twist(qref, e);
+                int stt = warm_limit_state(travel, win.x, win.y, LIMIT_SLOP_ANG, sacc[i]);
+                if (stt < 0) continue;
+                bool lower = stt == 1;
+                float initial = hinge_twist(qa0, qb0, e) - quat_twist(qref, e);
+                float cc = regularized_limit(travel, initial, lower ? win.x : win.y, lower);
+                float f_raw = pena[i] * cc + sacc[i];
+                float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+                if (!row_live(cc, f)) continue;
+                stamp_angular(s, g, pena[i], f);
+            }
+        }
+    } else if (fixed) {
+        const Q qref = ldq(w.j_qref[j]);
+        V3 diff = quat_diff_vec(qmul(conj(qa), qb), qref);
+        V3 diff0 = quat_diff_vec(qmul(conj(qa0), qb0), qref);
+        for (int k = 0; k < 3; k++) {
+            float cc = diff[k] - ALPHA * diff0[k];
+            float f = pena[k] * cc + lama[k];
+            if (!row_live(cc, f)) continue;
+            V3 e = V0();
+            e[k] = 1.0f;
+            V3 dir = qrot(qa, e);
+            stamp_angular(s, is_a ? -dir : dir, pena[k], f);
+        }
     }
+    // one-sided limit rows
     float4 lim = w.j_lim[j];
-    if (lim.z != 0.0f) {
-        V3 wa = normalize_or(axa, VZ());
+    if (lim.z != 0.0f && kind == AVBD_JOINT_REVOLUTE) {
         float refv = axa4.w;
         float angle = wrap_pi(hinge_twist(qa, qb, axa_l) - refv);
         int stt = warm_limit_state(angle, lim.x, lim.y, LIMIT_SLOP_ANG, lim.w);
@@ -184,6 +296,18 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             float f_raw = pa4.z * cc + lim.w;
             float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
             if (row_live(cc, f)) stamp_angular(s, is_a ? -wa : wa, pa4.z, f);
+        }
+    } else if (lim.z != 0.0f && kind == AVBD_JOINT_PRISMATIC) {
+        float sv = dot(pb - pa, wa) - ref.x;
+        int stt = warm_limit_state(sv, lim.x, lim.y, LIMIT_SLOP_LIN, ref.y);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            V3 axis0 = normalize_or(qrot(qa0, axa_l), VZ());
+            float initial = dot(pb0 - pa0, axis0) - ref.x;
+            float cc = regularized_limit(sv, initial, lower ? lim.x : lim.y, lower);
+            float f_raw = pl.z * cc + ref.y;
+            float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+            if (row_live(cc, f)) stamp_row(s, wa, pl.z, f, r_plain, lsign);
         }
     }
 }
@@ -547,8 +671,13 @@ __global__ void __launch_bounds__(CHUNK) k_dual_pairs(DW w) {
         __syncthreads();
     }
 }
+// joints_ext.rs:574-896: the joint rows' multipliers and penalties
+static __device__ __forceinline__ float ramp(float pen, float c, float beta, float cap) {
+    return fminf(pen + beta * fabsf(c), cap);
+}
 static __device__ void dual_joint(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];
+    const uint32_t kind = w.j_kind[j];
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
     V3 la = ld3(w.j_la[j]), lb = ld3(w.j_lb[j]);
@@ -557,43 +686,161 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
     V3 live = pa - pb, c0v = pa0 - pb0;
     float4 ll = w.j_lam_l[j], pl = w.j_pen_l[j];
     float laml[3] = {ll.x, ll.y, ll.z}, penl[3] = {pl.x, pl.y, pl.z};
-    // a soft joint (finite stiffness K) is a spring: penalty K, lambda zero;
-    // a hard one is the reference's dual ascent
-    const float K = w.joint_k;
-    for (int k = 0; k < 3; k++) {
-        float cc = live[k] - ALPHA * c0v[k];
-        if (K > 0.0f) {
-            penl[k] = K;
-        } else if (fabsf(cc) >= C_EPS) {
-            laml[k] += penl[k] * cc;
-            penl[k] = fminf(penl[k] + BETA * fabsf(cc), PENALTY_MAX);
-        }
-    }
-    w.j_lam_l[j] = make_float4(laml[0], laml[1], laml[2], 0.0f);
-    w.j_pen_l[j] = make_float4(penl[0], penl[1], penl[2], 0.0f);
-    if (w.j_kind[j] != AVBD_JOINT_REVOLUTE) return;
-    float4 axa4 = w.j_axa[j];
-    V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
-    V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
-    V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
-    V3 t1 = tangent_t1(axa0);
-    V3 t2 = cross(t1, axa0);
-    V3 ts[2] = {t1, t2};
     float4 la4 = w.j_lam_a[j], pa4 = w.j_pen_a[j];
     float lama[3] = {la4.x, la4.y, la4.z}, pena[3] = {pa4.x, pa4.y, pa4.z};
-    for (int li = 0; li < 2; li++) {
-        float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
-        if (K > 0.0f) {
-            pena[li] = K;
-            continue;
+    float4 ref = w.j_ref[j];
+    // a soft joint (finite stiffness K) is a spring: penalty K, lambda zero,
+    // for the anchor and hinge rows of ball and revolute joints; a hard one
+    // is the reference's dual ascent
+    const float K = w.joint_k;
+    const bool soft = K > 0.0f && (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE);
+    const bool fixed = kind == AVBD_JOINT_FIXED;
+    if (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE || fixed) {
+        const V3 dref = fixed ? ld3(w.j_dref[j]) : V0();
+        V3 lv = fixed ? live + qrot(qa, dref) : live;
+        V3 iv = fixed ? c0v + qrot(qa0, dref) : c0v;
+        for (int k = 0; k < 3; k++) {
+            float cc = lv[k] - ALPHA * iv[k];
+            if (soft) {
+                penl[k] = K;
+            } else if (fabsf(cc) >= C_EPS) {
+                laml[k] += penl[k] * cc;
+                penl[k] = ramp(penl[k], cc, BETA, PENALTY_MAX);
+            }
         }
-        if (fabsf(cc) < C_EPS) continue;
-        lama[li] = pena[li] * cc + lama[li];
-        pena[li] = fminf(pena[li] + BETA_ANG * fabsf(cc), PENALTY_MAX);
+    } else if (kind == AVBD_JOINT_PRISMATIC) {
+        V3 wa = normalize_or(qrot(qa, ld3(w.j_axa[j])), VZ());
+        V3 u = tangent_t1(wa);
+        V3 v = cross(u, wa);
+        V3 axs[2] = {u, v};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(live - ALPHA * c0v, axs[li]);
+            if (fabsf(cc) >= C_EPS) {
+                laml[li] += penl[li] * cc;
+                penl[li] = ramp(penl[li], cc, BETA, PENALTY_MAX);
+            }
+        }
+    } else if (kind == AVBD_JOINT_DISTANCE) {
+        float cc = (len(live) - ref.x) - ALPHA * (len(c0v) - ref.x);
+        if (fabsf(cc) >= C_EPS) {
+            laml[0] += penl[0] * cc;
+            penl[0] = ramp(penl[0], cc, BETA, PENALTY_MAX);
+        }
+    } else if (kind == AVBD_JOINT_ROPE) {
+        float ln = len(live);
+        if (ln > ref.x) {
+            float cc = (ln - ref.x) - ALPHA * (len(c0v) - ref.x);
+            if (fabsf(cc) >= C_EPS) {
+                laml[0] = fmaxf(laml[0] + penl[0] * cc, 0.0f);
+                penl[0] = ramp(penl[0], cc, BETA, LIM_PEN_MAX);
+            }
+        } else {
+            laml[0] = 0.0f;
+        }
+    } else if (kind == AVBD_JOINT_SIXDOF) {
+        const uint32_t cfg = w.j_cfg[j];
+        const V3 dref = ld3(w.j_dref[j]);
+        const Q qref = ldq(w.j_qref[j]);
+        float4 sa0 = w.j_sacc[2 * (size_t)j], sa1 = w.j_sacc[2 * (size_t)j + 1];
+        float sacc[6] = {sa0.x, sa0.y, sa0.z, sa0.w, sa1.x, sa1.y};
+        for (int i = 0; i < 3; i++) {
+            const uint32_t c = axis_cfg(cfg, i);
+            if (c == AVBD_AXIS_FREE) continue;
+            V3 e = V0();
+            e[i] = 1.0f;
+            V3 dir = normalize_or(qrot(qa, e), e);
+            float sep = dot((pb - pa) - qrot(qa, dref), dir);
+            if (c == AVBD_AXIS_LOCKED) {
+                if (fabsf(sep) >= C_EPS) {
+                    laml[i] += penl[i] * sep;
+                    penl[i] = ramp(penl[i], sep, BETA, PENALTY_MAX);
+                }
+            } else {
+                float2 win = axis_window(w, j, i);
+                int stt = warm_limit_state(sep, win.x, win.y, LIMIT_SLOP_LIN, sacc[i]);
+                if (stt >= 0) {
+                    bool lower = stt == 1;
+                    V3 axis0 = normalize_or(qrot(qa0, e), e);
+                    float initial = dot((pb0 - pa0) - qrot(qa0, dref), axis0);
+                    float cc = regularized_limit(sep, initial, lower ? win.x : win.y, lower);
+                    if (fabsf(cc) >= C_EPS) {
+                        float f = penl[i] * cc + sacc[i];
+                        sacc[i] = lower ? fminf(f, 0.0f) : fmaxf(f, 0.0f);
+                        penl[i] = ramp(penl[i], cc, BETA, LIM_PEN_MAX);
+                    }
+                } else {
+                    sacc[i] = 0.0f;
+                }
+            }
+        }
+        V3 diff = quat_diff_vec(qmul(conj(qa), qb), qref);
+        for (int i = 0; i < 3; i++) {
+            const uint32_t c = axis_cfg(cfg, 3 + i);
+            if (c == AVBD_AXIS_FREE) continue;
+            V3 e = V0();
+            e[i] = 1.0f;
+            if (c == AVBD_AXIS_LOCKED) {
+                float cc = dot(diff, e);
+                if (fabsf(cc) >= C_EPS) {
+                    lama[i] += pena[i] * cc;
+                    pena[i] = ramp(pena[i], cc, BETA_ANG, PENALTY_MAX);
+                }
+            } else {
+                float2 win = axis_window(w, j, 3 + i);
+                float travel = hinge_twist(qa, qb, e) - quat_twist(qref, e);
+                int stt = warm_limit_state(travel, win.x, win.y, LIMIT_SLOP_ANG, sacc[3 + i]);
+                if (stt >= 0) {
+                    bool lower = stt == 1;
+                    float initial = hinge_twist(qa0, qb0, e) - quat_twist(qref, e);
+                    float cc = regularized_limit(travel, initial, lower ? win.x : win.y, lower);
+                    if (fabsf(cc) >= C_EPS) {
+                        float f = pena[i] * cc + sacc[3 + i];
+                        sacc[3 + i] = lower ? fminf(f, 0.0f) : fmaxf(f, 0.0f);
+                        pena[i] = ramp(pena[i], cc, BETA_ANG, LIM_PEN_MAX);
+                    }
+                } else {
+                    sacc[3 + i] = 0.0f;
+                }
+            }
+        }
+        w.j_sacc[2 * (size_t)j] = make_float4(sacc[0], sacc[1], sacc[2], sacc[3]);
+        w.j_sacc[2 * (size_t)j + 1] = make_float4(sacc[4], sacc[5], 0.0f, 0.0f);
     }
+    // angular equality rows
+    if (kind == AVBD_JOINT_REVOLUTE || kind == AVBD_JOINT_PRISMATIC) {
+        float4 axa4 = w.j_axa[j];
+        V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
+        V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
+        V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
+        V3 t1 = tangent_t1(axa0);
+        V3 t2 = cross(t1, axa0);
+        V3 ts[2] = {t1, t2};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(ts[li], axa - axb) - ALPHA * dot(ts[li], axa0 - axb0);
+            if (soft) {
+                pena[li] = K;
+                continue;
+            }
+            if (fabsf(cc) < C_EPS) continue;
+            lama[li] = pena[li] * cc + lama[li];
+            pena[li] = ramp(pena[li], cc, BETA_ANG, PENALTY_MAX);
+        }
+    } else if (fixed) {
+        const Q qref = ldq(w.j_qref[j]);
+        V3 diff = quat_diff_vec(qmul(conj(qa), qb), qref);
+        V3 diff0 = quat_diff_vec(qmul(conj(qa0), qb0), qref);
+        for (int k = 0; k < 3; k++) {
+            float cc = diff[k] - ALPHA * diff0[k];
+            if (fabsf(cc) < C_EPS) continue;
+            lama[k] += pena[k] * cc;
+            pena[k] = ramp(pena[k], cc, BETA_ANG, PENALTY_MAX);
+        }
+    }
+    // one-sided limits
     float4 lim = w.j_lim[j];
-    if (lim.z != 0.0f) {
-        float refv = axa4.w;
+    if (lim.z != 0.0f && kind == AVBD_JOINT_REVOLUTE) {
+        V3 axa_l = ld3(w.j_axa[j]);
+        float refv = w.j_axa[j].w;
         float angle = wrap_pi(hinge_twist(qa, qb, axa_l) - refv);
         int stt = warm_limit_state(angle, lim.x, lim.y, LIMIT_SLOP_ANG, lim.w);
         if (stt >= 0) {
@@ -603,13 +850,36 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
             if (fabsf(cc) >= C_EPS) {
                 float f = pena[2] * cc + lim.w;
                 lim.w = lower ? fminf(f, 0.0f) : fmaxf(f, 0.0f);
-                pena[2] = fminf(pena[2] + BETA_ANG * fabsf(cc), LIM_PEN_MAX);
+                pena[2] = ramp(pena[2], cc, BETA_ANG, LIM_PEN_MAX);
             }
         } else {
             lim.w = 0.0f;
         }
         w.j_lim[j] = lim;
+    } else if (lim.z != 0.0f && kind == AVBD_JOINT_PRISMATIC) {
+        V3 axa_l = ld3(w.j_axa[j]);
+        V3 wa = normalize_or(qrot(qa, axa_l), VZ());
+        float sv = dot(pb - pa, wa) - ref.x;
+        int stt = warm_limit_state(sv, lim.x, lim.y, LIMIT_SLOP_LIN, ref.y);
+        if (stt >= 0) {
+            bool lower = stt == 1;
+            V3 axis0 = normalize_or(qrot(qa0, axa_l), VZ());
+            float initial = dot(pb0 - pa0, axis0) - ref.x;
+            float cc = regularized_limit(sv, initial, lower ? lim.x : lim.y, lower);
+            if (fabsf(cc) >= C_EPS) {
+                float f_raw = penl[2] * cc + ref.y;
+                ref.y = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
+                penl[2] = ramp(penl[2], cc, BETA, LIM_PEN_MAX);
+            }
+        } else {
+            lim.w = 0.0f;
+            ref.y = 0.0f;
+        }
+        w.j_lim[j] = lim;
+        w.j_ref[j] = ref;
     }
+    w.j_lam_l[j] = make_float4(laml[0], laml[1], laml[2], 0.0f);
+    w.j_pen_l[j] = make_float4(penl[0], penl[1], penl[2], 0.0f);
     w.j_lam_a[j] = make_float4(lama[0], lama[1], lama[2], 0.0f);
     w.j_pen_a[j] = make_float4(pena[0], pena[1], pena[2], 0.0f);
 }

@@ -44,10 +44,17 @@ static __host__ __device__ __forceinline__ float rem_euclid(float x, float m) {
     return r < 0.0f ? r + fabsf(m) : r;
 }
 static __host__ __device__ __forceinline__ float wrap_pi(float x) { return rem_euclid(x + PI_F, TAU_F) - PI_F; }
-static __host__ __device__ __forceinline__ float hinge_twist(Q qa, Q qb, V3 axis) {  // sequential_impulse/joints.rs:38-48
-    Q q = qmul(conj(qa), qb);
+static __host__ __device__ __forceinline__ float quat_twist(Q q, V3 axis) {  // sequential_impulse/joints.rs:44-48
     float t = 2.0f * crm::atan2f(dot(V3{q.x, q.y, q.z}, axis), q.w);
     return rem_euclid(t + PI_F, TAU_F) - PI_F;
+}
+static __host__ __device__ __forceinline__ float hinge_twist(Q qa, Q qb, V3 axis) {  // :38-43
+    return quat_twist(qmul(conj(qa), qb), axis);
+}
+static __host__ __device__ __forceinline__ int limit_state(float v, float lo, float hi, float slop) {  // rows.rs:156-164
+    if (v <= lo + slop) return 1;
+    if (v >= hi - slop) return 0;
+    return -1;
 }
 static __host__ __device__ __forceinline__ int warm_limit_state(float v, float lo, float hi, float slop, float force) {  // rows.rs:156-183
     if (v <= lo + slop) return 1;

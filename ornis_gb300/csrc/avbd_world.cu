@@ -26,9 +26,14 @@ namespace {
 struct JointRec {
     uint32_t kind, a, b;
     float la[3], lb[3], axa[3], axb[3];
-    float ref;
+    float ref;   // revolute reference twist
+    float refv;  // prismatic reference length, distance rest length, rope maximum
     int32_t has_lim;
     float lo, hi;
+    float mot_speed, mot_max;  // velocity motor (mot_max 0: none)
+    float qref[4], dref[3];    // fixed / sixdof assembly references
+    uint32_t cfg;              // sixdof axis configuration, 2 bits per axis
+    float six_min[6], six_max[6];
     AvbdJointState st;
 };
 
@@ -277,6 +282,10 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.j_kind = m.get<uint32_t>(J); w.j_ab = m.get<uint2>(J);
     w.j_la = m.get<float4>(J); w.j_lb = m.get<float4>(J); w.j_axa = m.get<float4>(J); w.j_axb = m.get<float4>(J);
     w.j_lim = m.get<float4>(J);
+    w.j_ref = m.get<float4>(J); w.j_dref = m.get<float4>(J); w.j_qref = m.get<float4>(J);
+    w.j_cfg = m.get<uint32_t>(J); w.j_six = m.get<float4>(3 * (size_t)J); w.j_sacc = m.get<float4>(2 * (size_t)J);
+    w.jimp_off = m.get<uint32_t>(S + 1);
+    w.jimp_list = m.get<uint32_t>(J);
     w.j_lam_l = m.get<float4>(J); w.j_lam_a = m.get<float4>(J); w.j_pen_l = m.get<float4>(J); w.j_pen_a = m.get<float4>(J);
     w.jofs = m.get<uint32_t>(N + 1);
     w.jlist = m.get<uint32_t>(2 * J);
@@ -592,12 +601,37 @@ static int upload_all(AvbdWorld* W) {
     std::vector<int32_t> comp(N, -1);
     for (uint32_t h = 0; h < N; h++)
         if (in_joint[h]) comp[h] = find((int32_t)h);
-    std::vector<uint32_t> j_kind(J);
+    std::vector<uint32_t> j_kind(J), j_cfg(J);
     std::vector<uint2> j_ab(J);
     std::vector<float4> j_la(J), j_lb(J), j_axa(J), j_axb(J), j_lim(J), jll(J), jla(J), jpl(J), jpa(J);
+    std::vector<float4> j_ref(J), j_dref(J), j_qref(J), j_six(3 * (size_t)J), j_sacc(2 * (size_t)J);
+    // joints with a motor or a rope, per scene in joint order
+    std::vector<uint32_t> jimp_off(S + 1, 0), jimp_list;
+    {
+        std::vector<std::vector<uint32_t>> per(S);
+        for (uint32_t i = 0; i < J; i++) {
+            const JointRec& j = W->joints[i];
+            if (j.mot_max > 0.0f || j.kind == AVBD_JOINT_ROPE) per[scene_of[j.a]].push_back(i);
+        }
+        for (uint32_t sc = 0; sc < S; sc++) {
+            jimp_off[sc] = (uint32_t)jimp_list.size();
+            jimp_list.insert(jimp_list.end(), per[sc].begin(), per[sc].end());
+        }
+        jimp_off[S] = (uint32_t)jimp_list.size();
+        w.n_imp = (int)jimp_list.size();
+    }
     for (uint32_t i = 0; i < J; i++) {
         const JointRec& j = W->joints[i];
         j_kind[i] = j.kind;
+        j_cfg[i] = j.cfg;
+        j_ref[i] = make_float4(j.refv, j.st.lim_dual, j.mot_speed, j.mot_max);
+        j_dref[i] = make_float4(j.dref[0], j.dref[1], j.dref[2], 0.0f);
+        j_qref[i] = make_float4(j.qref[0], j.qref[1], j.qref[2], j.qref[3]);
+        for (int k = 0; k < 3; k++)
+            j_six[3 * (size_t)i + k] = make_float4(j.six_min[2 * k], j.six_max[2 * k], j.six_min[2 * k + 1],
+                                                   j.six_max[2 * k + 1]);
+        j_sacc[2 * (size_t)i] = make_float4(j.st.sacc[0], j.st.sacc[1], j.st.sacc[2], j.st.sacc[3]);
+        j_sacc[2 * (size_t)i + 1] = make_float4(j.st.sacc[4], j.st.sacc[5], 0.0f, 0.0f);
         j_ab[i] = make_uint2(j.a, j.b);
         j_la[i] = make_float4(j.la[0], j.la[1], j.la[2], 0.0f);
         j_lb[i] = make_float4(j.lb[0], j.lb[1], j.lb[2], 0.0f);
@@ -675,6 +709,11 @@ static int upload_all(AvbdWorld* W) {
     up(w.j_la, j_la.data(), J * 16); up(w.j_lb, j_lb.data(), J * 16);
     up(w.j_axa, j_axa.data(), J * 16); up(w.j_axb, j_axb.data(), J * 16);
     up(w.j_lim, j_lim.data(), J * 16);
+    up(w.j_ref, j_ref.data(), J * 16); up(w.j_dref, j_dref.data(), J * 16); up(w.j_qref, j_qref.data(), J * 16);
+    up(w.j_cfg, j_cfg.data(), J * 4); up(w.j_six, j_six.data(), 3 * (size_t)J * 16);
+    up(w.j_sacc, j_sacc.data(), 2 * (size_t)J * 16);
+    up((void*)w.jimp_off, jimp_off.data(), (S + 1) * 4);
+    up((void*)w.jimp_list, jimp_list.data(), jimp_list.size() * 4);
     up(w.j_lam_l, jll.data(), J * 16); up(w.j_lam_a, jla.data(), J * 16);
     up(w.j_pen_l, jpl.data(), J * 16); up(w.j_pen_a, jpa.data(), J * 16);
     up(w.p_ab, pab.data(), P * 8); up(w.p_n, pn.data(), P * 16); up(w.p_mu, pmu.data(), P * 8);
@@ -740,8 +779,10 @@ static int download_all(AvbdWorld* W) {
         CK(cudaMemcpyAsync(qroll.data(), w.q_roll, Q * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(qm.data(), w.q_matched, Q * 4, cudaMemcpyDeviceToHost, st));
     }
-    std::vector<float4> jll(J), jla(J), jpl(J), jpa(J), jlim(J);
+    std::vector<float4> jll(J), jla(J), jpl(J), jpa(J), jlim(J), jref(J), jsacc(2 * (size_t)J);
     if (J) {
+        CK(cudaMemcpyAsync(jref.data(), w.j_ref, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jsacc.data(), w.j_sacc, 2 * (size_t)J * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jll.data(), w.j_lam_l, J * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jla.data(), w.j_lam_a, J * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jpl.data(), w.j_pen_l, J * 16, cudaMemcpyDeviceToHost, st));
@@ -779,6 +820,9 @@ static int download_all(AvbdWorld* W) {
         s.pen_l[0] = jpl[i].x; s.pen_l[1] = jpl[i].y; s.pen_l[2] = jpl[i].z;
         s.pen_a[0] = jpa[i].x; s.pen_a[1] = jpa[i].y; s.pen_a[2] = jpa[i].z;
         s.acc_lim = jlim[i].w;
+        s.lim_dual = jref[i].y;
+        const float4 s0 = jsacc[2 * (size_t)i], s1 = jsacc[2 * (size_t)i + 1];
+        s.sacc[0] = s0.x; s.sacc[1] = s0.y; s.sacc[2] = s0.z; s.sacc[3] = s0.w; s.sacc[4] = s1.x; s.sacc[5] = s1.y;
     }
     W->host_valid = true;
     return AVBD_OK;
@@ -1540,27 +1584,34 @@ int avbd_world_wake_body(AvbdWorld* W, uint32_t handle) {
 
 int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle) {
     if (!W || !d) return AVBD_ERR_INVALID_ARG;
-    for (int k = 0; k < 3; k++)
-        if (!std::isfinite(d->local_anchor_a[k]) || !std::isfinite(d->local_anchor_b[k]) ||
-            !std::isfinite(d->local_axis_a[k]) || !std::isfinite(d->local_axis_b[k]))
+    // validate_joint (migration.rs:160-330): anchors and axes finite, bounds
+    // ordered, motor fields finite, a rope longer than zero
+    auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
+    auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
+    if (d->kind > AVBD_JOINT_SIXDOF) return AVBD_ERR_UNSUPPORTED;
+    if (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+    const bool axial = d->kind == AVBD_JOINT_REVOLUTE || d->kind == AVBD_JOINT_PRISMATIC;
+    if (axial) {
+        if (!finite3(d->local_axis_a) || !finite3(d->local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+        if (d->has_limit && !bounds_ok(d->limit_min, d->limit_max)) return AVBD_ERR_JOINT_BAD_BOUNDS;
+        if (d->has_motor && !(std::isfinite(d->motor_speed) && std::isfinite(d->motor_max) && d->motor_max >= 0.0f))
             return AVBD_ERR_JOINT_NONFINITE;
-    if (d->kind != AVBD_JOINT_BALL && d->kind != AVBD_JOINT_REVOLUTE) return AVBD_ERR_UNSUPPORTED;
+    }
+    if (d->kind == AVBD_JOINT_SIXDOF)
+        for (int k = 0; k < 6; k++) {
+            if (d->axis_config[k] > AVBD_AXIS_LIMITED) return AVBD_ERR_INVALID_ARG;
+            if (d->axis_config[k] == AVBD_AXIS_LIMITED && !bounds_ok(d->axis_min[k], d->axis_max[k]))
+                return AVBD_ERR_JOINT_BAD_BOUNDS;
+        }
+    if (d->kind == AVBD_JOINT_ROPE && !(std::isfinite(d->max_distance) && d->max_distance > 0.0f))
+        return AVBD_ERR_JOINT_BAD_BOUNDS;
     cudaSetDevice(W->device);
     int rc = host_edit(W);
     if (rc) return rc;
     uint32_t n = (uint32_t)W->bodies.size();
     // a new constraint wakes both members (mod.rs:1320-1321)
     for (uint32_t h : {d->body_a, d->body_b})
-        if (h < n && W->aux[h].asleep) {
-            W->aux[h].asleep = 0;
-            W->aux[h].sleep_timer = 0.0f;
-            AvbdBody& b = W->bodies[h];
-            if (b.body_type == AVBD_BODY_DYNAMIC) {
-                bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
-                b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
-                rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
-            }
-        }
+        if (h < n) wake_host(W, h);
     if (d->body_a == d->body_b) return AVBD_ERR_JOINT_SELF;
     if (d->body_a >= n || d->body_b >= n) return AVBD_ERR_JOINT_HANDLES;
     // both members must live in the same scene
@@ -1575,21 +1626,51 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     std::memcpy(j.la, d->local_anchor_a, 12);
     std::memcpy(j.lb, d->local_anchor_b, 12);
     j.axa[0] = 1.0f; j.axb[0] = 1.0f;
-    if (d->kind == AVBD_JOINT_REVOLUTE) {  // joint.rs:1280-1294
+    j.qref[3] = 1.0f;
+    // resolve_joint (joint.rs:1251-1400), in the reference's f32 operation order
+    using namespace avbd;
+    const AvbdBody& ba = W->bodies[j.a];
+    const AvbdBody& bb = W->bodies[j.b];
+    const Q qa{ba.orientation[0], ba.orientation[1], ba.orientation[2], ba.orientation[3]};
+    const Q qb{bb.orientation[0], bb.orientation[1], bb.orientation[2], bb.orientation[3]};
+    const V3 xa{ba.position[0], ba.position[1], ba.position[2]}, xb{bb.position[0], bb.position[1], bb.position[2]};
+    const V3 la{j.la[0], j.la[1], j.la[2]}, lb{j.lb[0], j.lb[1], j.lb[2]};
+    if (axial) {
         const float* aa = d->local_axis_a;
         const float* ab = d->local_axis_b;
-        float la2 = (aa[0] * aa[0] + aa[1] * aa[1]) + aa[2] * aa[2];
-        float lb2 = (ab[0] * ab[0] + ab[1] * ab[1]) + ab[2] * ab[2];
-        if (la2 < 1e-12f || lb2 < 1e-12f) return AVBD_ERR_JOINT_BAD_AXIS;
-        float ra = 1.0f / std::sqrt(la2), rb = 1.0f / std::sqrt(lb2);
-        for (int k = 0; k < 3; k++) {
-            j.axa[k] = aa[k] * ra;
-            j.axb[k] = ab[k] * rb;
+        V3 va{aa[0], aa[1], aa[2]}, vb{ab[0], ab[1], ab[2]};
+        if (len2(va) < 1e-12f || len2(vb) < 1e-12f) return AVBD_ERR_JOINT_BAD_AXIS;
+        V3 na = normalize_or(va, VZ()), nb = normalize_or(vb, VZ());
+        j.axa[0] = na.x; j.axa[1] = na.y; j.axa[2] = na.z;
+        j.axb[0] = nb.x; j.axb[1] = nb.y; j.axb[2] = nb.z;
+        if (d->kind == AVBD_JOINT_REVOLUTE) {
+            j.ref = hinge_twist_host(ba.orientation, bb.orientation, j.axa);
+        } else {
+            V3 wa = normalize_or(qrot(qa, na), VZ());
+            j.refv = dot((xb + qrot(qb, lb)) - (xa + qrot(qa, la)), wa);
         }
-        j.ref = hinge_twist_host(W->bodies[j.a].orientation, W->bodies[j.b].orientation, j.axa);
         j.has_lim = d->has_limit;
         j.lo = d->limit_min;
         j.hi = d->limit_max;
+        if (d->has_motor) {
+            j.mot_speed = d->motor_speed;
+            j.mot_max = d->motor_max;
+        }
+    } else if (d->kind == AVBD_JOINT_FIXED || d->kind == AVBD_JOINT_SIXDOF) {
+        Q r = qmul(conj(qa), qb);
+        j.qref[0] = r.x; j.qref[1] = r.y; j.qref[2] = r.z; j.qref[3] = r.w;
+        V3 dr = qrot(conj(qa), (xb + qrot(qb, lb)) - (xa + qrot(qa, la)));
+        j.dref[0] = dr.x; j.dref[1] = dr.y; j.dref[2] = dr.z;
+        if (d->kind == AVBD_JOINT_SIXDOF)
+            for (int k = 0; k < 6; k++) {
+                j.cfg |= (d->axis_config[k] & 3u) << (2 * k);
+                j.six_min[k] = d->axis_min[k];
+                j.six_max[k] = d->axis_max[k];
+            }
+    } else if (d->kind == AVBD_JOINT_DISTANCE) {
+        j.refv = len((xb + qrot(qb, lb)) - (xa + qrot(qa, la)));
+    } else if (d->kind == AVBD_JOINT_ROPE) {
+        j.refv = d->max_distance;
     }
     for (int k = 0; k < 3; k++) {
         j.st.pen_l[k] = 1.0f;  // JOINT_PENALTY_INIT
@@ -2138,6 +2219,9 @@ int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t 
     if (!W || steps <= 0 || substeps <= 0 || every <= 0) return AVBD_ERR_INVALID_ARG;
     for (const AvbdBody& b : W->bodies)
         if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f) return AVBD_ERR_UNSUPPORTED;
+    // the reverse sweep differentiates ball and revolute rows without motors
+    for (const JointRec& j : W->joints)
+        if (j.kind > AVBD_JOINT_REVOLUTE || j.mot_max > 0.0f) return AVBD_ERR_UNSUPPORTED;
     int rc = begin_steps(W);
     if (rc) return rc;
     if (W->tune.primal_lanes != 0) {

@@ -29,6 +29,8 @@ constexpr float SLEEP_TIME = 0.5f;
 constexpr float WAKE_IMPACT_SPEED = 0.5f;
 constexpr float WAKE_PENETRATION = 0.01f;
 constexpr float LIMIT_SLOP_ANG = 0.005f;
+constexpr float LIMIT_SLOP_LIN = 0.002f;      // mod.rs:222
+constexpr float MIN_EFFECTIVE_MASS = 1e-10f;  // constants.rs:16
 constexpr float LIM_PEN_MAX = 1e4f;
 constexpr float ROLL_PEN = 100.0f;
 constexpr float MIN_TOI_DISP_LENGTH = 1e-9f;
@@ -147,13 +149,24 @@ struct DW {
     int32_t* colour;
     int32_t* comp;  // joint component id (-1: no joint)
 
-    // joints (Ball / Revolute)
+    // joints (AvbdJoint, avbd/mod.rs:327-402)
     uint32_t* j_kind;
     uint2* j_ab;
-    float4 *j_la, *j_lb, *j_axa, *j_axb;  // w of j_axa = reference twist
+    float4 *j_la, *j_lb, *j_axa, *j_axb;  // w of j_axa = reference twist (revolute)
     float4* j_lim;                         // lo, hi, has_limit, acc_lim
     float4 *j_lam_l, *j_lam_a, *j_pen_l, *j_pen_a;
+    // reference length (prismatic) / rest length (distance) / maximum (rope),
+    // prismatic limit force, motor target speed, motor budget (0: no motor)
+    float4* j_ref;
+    float4 *j_dref, *j_qref;  // fixed / sixdof assembly anchor separation (A's frame) and qa^-1 qb
+    uint32_t* j_cfg;          // sixdof axis configuration: 2 bits per axis, linear x y z then angular
+    float4* j_six;            // 3 per joint: (min, max) of the six axes in pairs
+    float4* j_sacc;           // 2 per joint: sixdof limited-axis forces (6 used)
     const uint32_t *jofs, *jlist;  // per-body joint adjacency (N+1, 2J)
+    // joints with a motor or a rope, per scene in joint order (their velocity
+    // impulses run before the warm start); n_imp of them in all
+    const uint32_t *jimp_off, *jimp_list;
+    int n_imp;
 
     // contact pairs: current generation (read by the solver) ...
     uint2* p_ab;
