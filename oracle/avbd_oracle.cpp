@@ -1063,7 +1063,12 @@ template <class T> struct Engine {
             if (p.a == ia && p.b == ib) return &p;
         return nullptr;
     }
-    static bool no_collide_kind(uint32_t k) { return k == AVBD_JOINT_BALL || k == AVBD_JOINT_REVOLUTE; }
+    // rows.rs:434-474: joined bodies do not collide, except through weld-like
+    // Fixed and SixDof joints (their contact is structural)
+    static bool no_collide_kind(uint32_t k) {
+        return k == AVBD_JOINT_BALL || k == AVBD_JOINT_REVOLUTE || k == AVBD_JOINT_PRISMATIC ||
+               k == AVBD_JOINT_DISTANCE || k == AVBD_JOINT_ROPE;
+    }
 
     bool discover_pair(uint32_t ia, uint32_t ib, Discovered& out) const {
         const Body<T>& a = bodies[ia];

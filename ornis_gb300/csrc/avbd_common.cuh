@@ -68,10 +68,22 @@ static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uin
     uint2 fa = w.filter[a], fb = w.filter[b];
     return (fa.x & fb.y) != 0u && (fb.x & fa.y) != 0u;
 }
-// a joint links a and b (every kind on this path is no-collide, rows.rs:457-474)
+// a joint links a and b (the swept cast skips every joined partner, mod.rs:887-917)
 static __device__ __forceinline__ bool jointed(const DW& w, uint32_t a, uint32_t b) {
     for (uint32_t k = w.jofs[a]; k < w.jofs[a + 1]; k++) {
         uint2 ab = w.j_ab[w.jlist[k]];
+        if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return true;
+    }
+    return false;
+}
+// a joint that turns contact off links a and b (rows.rs:434-474): every kind
+// but the weld-like Fixed and SixDof, whose contact is structural
+static __device__ __forceinline__ bool jointed_no_collide(const DW& w, uint32_t a, uint32_t b) {
+    for (uint32_t k = w.jofs[a]; k < w.jofs[a + 1]; k++) {
+        const uint32_t j = w.jlist[k];
+        uint2 ab = w.j_ab[j];
+        const uint32_t kind = w.j_kind[j];
+        if (kind == AVBD_JOINT_FIXED || kind == AVBD_JOINT_SIXDOF) continue;
         if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return true;
     }
     return false;

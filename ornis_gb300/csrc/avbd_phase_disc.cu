@@ -29,7 +29,7 @@ static __device__ __forceinline__ bool discover_pre(const DW& w, uint32_t a, uin
     r.old = -1;
     if (!pair_allowed(w, a, b)) return false;
     if (info_trigger(w.info[a]) || info_trigger(w.info[b])) return false;  // triggers form no contact pair here
-    if (jointed(w, a, b)) return false;
+    if (jointed_no_collide(w, a, b)) return false;
     r.ra = w.shp[a].w;
     r.rb = w.shp[b].w;
     if (len(ld3(w.pos[a]) - ld3(w.pos[b])) > r.ra + r.rb + GEN_MARGIN) return false;

@@ -357,7 +357,9 @@ static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, cons
 
 // One thread per body: rows accumulate in the reference's order (pairs in
 // ascending index — B-side pairs precede A-side ones — then joints).
-template <int MINB>
+// JOINTS: the instantiation for worlds with joints (the joint-free one keeps
+// the joint rows' code and registers out of the contact-only kernels)
+template <int MINB, bool JOINTS>
 __global__ void __launch_bounds__(128, MINB) k_primal_thread(DW w, int colour) {
     if (aborted_solve(w)) return;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -377,14 +379,15 @@ __global__ void __launch_bounds__(128, MINB) k_primal_thread(DW w, int colour) {
         load_ctx(w, p, c);
         for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, true, s);
     }
-    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+    if (JOINTS)
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
     apply_solve(w, h, s);
 }
 
 // L lanes per body: the body's incident pairs are dealt round-robin over the
 // lanes, the partial systems are summed with shuffles, lane 0 adds the
 // inertial block and the joints and solves.
-template <int L>
+template <int L, bool JOINTS>
 __global__ void k_primal_lanes(DW w, int colour) {
     if (aborted_solve(w)) return;
     uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -421,7 +424,8 @@ __global__ void k_primal_lanes(DW w, int colour) {
     for (int k = 0; k < 21; k++) t.h[k] += s.h[k];
 #pragma unroll
     for (int k = 0; k < 6; k++) t.r[k] += s.r[k];
-    for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, t);
+    if (JOINTS)
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, t);
     apply_solve(w, h, t);
 }
 
@@ -581,6 +585,7 @@ __global__ void __launch_bounds__(CHUNK) k_side_rows(DW w, int colour) {
         __syncthreads();  // the chunk's entries are read before the next chunk is sorted
     }
 }
+template <bool JOINTS>
 __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
     if (aborted_solve(w)) return;
     const uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
@@ -590,7 +595,8 @@ __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
         inertial_block(w, h, s);
         const uint32_t k0 = w.offA[h] + w.offB[h], k1 = min(w.offA[h + 1] + w.offB[h + 1], w.contrib_slots);
         for (uint32_t k = k0; k < k1; k++) add_slot(s, w.contrib + (size_t)k * 7);
-        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+        if (JOINTS)
+            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
         apply_solve(w, h, s);
     }
 }
@@ -943,7 +949,7 @@ static __device__ __forceinline__ void block_scan(uint32_t* a, uint32_t n, uint3
     __syncthreads();
 }
 
-template <int BS, int MINB>
+template <int BS, int MINB, bool JOINTS>
 __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
     if (aborted_solve(w)) return;
     __shared__ uint32_t s_list[SCENE_MAX_BODIES];      // swept bodies grouped by colour
@@ -1041,7 +1047,8 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
                         __syncthreads();
                     }
                     if (tid < nb) {
-                        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+                        if (JOINTS)
+                            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
                         apply_solve(w, h, s);
                     }
                     i0 = i1;
@@ -1049,7 +1056,7 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
                 __syncthreads();  // this colour's poses before the next colour reads them
             }
             for (uint32_t p = p0 + tid; p < p1; p += BS) dual_pair(w, p);
-            if (w.J)
+            if (JOINTS)
                 for (uint32_t h = b0 + tid; h < b1; h += BS)
                     for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
                         uint32_t j = w.jlist[k];
@@ -1060,7 +1067,7 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
     }
 }
 
-template <int BS, int MINB>
+template <int BS, int MINB, bool JOINTS>
 static void scene_solve_launch(const DW& w, cudaStream_t st) {
     const size_t smem = (size_t)BS * 7 * sizeof(float4);
     static int grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device ordinal
@@ -1068,21 +1075,26 @@ static void scene_solve_launch(const DW& w, cudaStream_t st) {
     cudaGetDevice(&dev);
     int& g = grid[dev & 7];
     if (!g) {
-        cudaFuncSetAttribute(k_scene_solve<BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_scene_solve<BS, MINB, JOINTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_solve<BS, MINB>, BS, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_solve<BS, MINB, JOINTS>, BS, smem);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g = max(1, per_sm) * max(1, sms);
     }
-    k_scene_solve<BS, MINB><<<min(g, max(1, w.S)), BS, smem, st>>>(w);
+    k_scene_solve<BS, MINB, JOINTS><<<min(g, max(1, w.S)), BS, smem, st>>>(w);
+}
+template <bool JOINTS>
+static void scene_solve_block(const DW& w, int block, cudaStream_t st) {
+    switch (block) {
+        case 128: scene_solve_launch<128, 4, JOINTS>(w, st); break;
+        case 512: scene_solve_launch<512, 1, JOINTS>(w, st); break;
+        default: scene_solve_launch<256, 2, JOINTS>(w, st); break;
+    }
 }
 void launch_scene_solve(const DW& w, const Tune& tune, cudaStream_t st) {
     cudaMemsetAsync(w.ctr + C_SCENE_Q, 0, sizeof(uint32_t), st);
-    switch (tune.primal_block) {
-        case 128: scene_solve_launch<128, 4>(w, st); break;
-        case 512: scene_solve_launch<512, 1>(w, st); break;
-        default: scene_solve_launch<256, 2>(w, st); break;
-    }
+    if (w.J) scene_solve_block<true>(w, tune.primal_block, st);
+    else scene_solve_block<false>(w, tune.primal_block, st);
 }
 
 // The per-scene solve's fallback for a world with a scene above its limit is
@@ -1095,25 +1107,30 @@ void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st) {
     k_side_starts<<<1, 32, 0, st>>>(w);
     k_side_place<<<gsz(w.pair_cap, SIDE_BLOCK), SIDE_BLOCK, 0, st>>>(w);
 }
-void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
+template <bool J>
+static void primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
     int bs = tune.primal_block;
     switch (launch_lanes(tune)) {
         case 0:
             k_side_rows<<<gsz((size_t)w.pair_cap * 2, 128), 128, 0, st>>>(w, c);
-            k_side_solve<<<gsz(max_bodies, 128), 128, 0, st>>>(w, c);
+            k_side_solve<J><<<gsz(max_bodies, 128), 128, 0, st>>>(w, c);
             break;
         case 1:
             // occupancy variants of the thread-per-body kernel: 4, 6 or 8
             // resident 128-thread blocks per SM (128, 80 or 64 registers)
-            if (tune.primal_minb >= 8) k_primal_thread<8><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
-            else if (tune.primal_minb >= 6) k_primal_thread<6><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
-            else k_primal_thread<4><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            if (tune.primal_minb >= 8) k_primal_thread<8, J><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            else if (tune.primal_minb >= 6) k_primal_thread<6, J><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
+            else k_primal_thread<4, J><<<nblk(max_bodies, bs), bs, 0, st>>>(w, c);
             break;
-        case 4: k_primal_lanes<4><<<nblk((size_t)max_bodies * 4, bs), bs, 0, st>>>(w, c); break;
-        case 8: k_primal_lanes<8><<<nblk((size_t)max_bodies * 8, bs), bs, 0, st>>>(w, c); break;
-        case 16: k_primal_lanes<16><<<nblk((size_t)max_bodies * 16, bs), bs, 0, st>>>(w, c); break;
-        default: k_primal_lanes<32><<<nblk((size_t)max_bodies * 32, bs), bs, 0, st>>>(w, c); break;
+        case 4: k_primal_lanes<4, J><<<nblk((size_t)max_bodies * 4, bs), bs, 0, st>>>(w, c); break;
+        case 8: k_primal_lanes<8, J><<<nblk((size_t)max_bodies * 8, bs), bs, 0, st>>>(w, c); break;
+        case 16: k_primal_lanes<16, J><<<nblk((size_t)max_bodies * 16, bs), bs, 0, st>>>(w, c); break;
+        default: k_primal_lanes<32, J><<<nblk((size_t)max_bodies * 32, bs), bs, 0, st>>>(w, c); break;
     }
+}
+void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
+    if (w.J) primal_colour<true>(w, tune, c, max_bodies, st);
+    else primal_colour<false>(w, tune, c, max_bodies, st);
 }
 void launch_dual(const DW& w, const Tune& tune, cudaStream_t st) {
     k_dual_pairs<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);

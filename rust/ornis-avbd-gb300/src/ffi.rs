@@ -16,6 +16,7 @@ pub const AVBD_ERR_JOINT_SELF: i32 = -10;
 pub const AVBD_ERR_JOINT_HANDLES: i32 = -11;
 pub const AVBD_ERR_JOINT_BAD_AXIS: i32 = -12;
 pub const AVBD_ERR_JOINT_NONFINITE: i32 = -13;
+pub const AVBD_ERR_JOINT_BAD_BOUNDS: i32 = -14;
 
 pub const AVBD_SHAPE_SPHERE: u32 = 0;
 pub const AVBD_SHAPE_BOX: u32 = 1;
@@ -32,6 +33,16 @@ pub const AVBD_FLAG_TRIGGER: u32 = 1;
 
 pub const AVBD_JOINT_BALL: u32 = 0;
 pub const AVBD_JOINT_REVOLUTE: u32 = 1;
+pub const AVBD_JOINT_PRISMATIC: u32 = 2;
+pub const AVBD_JOINT_FIXED: u32 = 3;
+pub const AVBD_JOINT_DISTANCE: u32 = 4;
+pub const AVBD_JOINT_ROPE: u32 = 5;
+pub const AVBD_JOINT_SIXDOF: u32 = 6;
+
+pub const AVBD_AXIS_FREE: u32 = 0;
+pub const AVBD_AXIS_LOCKED: u32 = 1;
+pub const AVBD_AXIS_LIMITED: u32 = 2;
+pub const AVBD_ABI_VERSION: i32 = 2;
 
 pub const AVBD_MAX_POINTS: usize = 8;
 pub const AVBD_PRIMAL_SCENES: i32 = -1;
@@ -77,6 +88,13 @@ pub struct AvbdJointDesc {
     pub has_limit: i32,
     pub limit_min: f32,
     pub limit_max: f32,
+    pub has_motor: i32,
+    pub motor_speed: f32,
+    pub motor_max: f32,
+    pub max_distance: f32,
+    pub axis_config: [u32; 6],
+    pub axis_min: [f32; 6],
+    pub axis_max: [f32; 6],
 }
 
 #[repr(C)]
@@ -130,6 +148,8 @@ pub struct AvbdJointState {
     pub pen_l: [f32; 3],
     pub pen_a: [f32; 3],
     pub acc_lim: f32,
+    pub lim_dual: f32,
+    pub sacc: [f32; 6],
 }
 
 #[repr(C)]

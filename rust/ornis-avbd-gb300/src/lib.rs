@@ -36,6 +36,8 @@ pub enum Error {
     JointBadAxis,
     /// `JointError::NonFinite`
     JointNonFinite,
+    /// `JointError::BadBounds`
+    JointBadBounds,
     Other(i32),
 }
 
@@ -53,6 +55,7 @@ impl Error {
             AVBD_ERR_JOINT_HANDLES => Error::JointHandles,
             AVBD_ERR_JOINT_BAD_AXIS => Error::JointBadAxis,
             AVBD_ERR_JOINT_NONFINITE => Error::JointNonFinite,
+            AVBD_ERR_JOINT_BAD_BOUNDS => Error::JointBadBounds,
             other => Error::Other(other),
         })
     }
