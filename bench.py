@@ -190,6 +190,11 @@ def workload(args):
         bodies, offs, joints = scenes.ragdolls(counts)
         params, nsub = scenes.params_for("ragdoll_8192")
         return bodies, offs, joints, params, nsub
+    if args.workload == "large_100k":
+        # one scene of 100,000 bodies dropped over a 200 x 200 m ground plane
+        bodies = scenes.large_100k()
+        params, nsub = scenes.params_for("large_100k")
+        return bodies, np.array([0, len(bodies)], dtype=np.uint32), [], params, nsub
     bodies, offs, _ = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
     return bodies, offs, [], params, nsub
@@ -206,10 +211,16 @@ def shard(bodies, offs, rank, world):
 
 
 TRAJECTORY_STEPS = 240  # the batched and articulated workloads' trajectories
+TRAJECTORY = {"batched_4096": 240, "ragdoll_8192": 240, "large_100k": 300}
 
 
-def timed_steps(args, total=TRAJECTORY_STEPS):
+def trajectory_len(args):
+    return TRAJECTORY.get(getattr(args, "workload", "batched_4096"), TRAJECTORY_STEPS)
+
+
+def timed_steps(args, total=None):
     """Trajectory steps the timed region covers (the state before each)."""
+    total = total or trajectory_len(args)
     if args.start is not None:
         return list(range(args.start, args.start + args.steps))
     if args.steps >= total:
@@ -217,11 +228,11 @@ def timed_steps(args, total=TRAJECTORY_STEPS):
     return [int((i + 0.5) * total / args.steps) for i in range(args.steps)]
 
 
-def describe_steps(steps):
+def describe_steps(steps, total=TRAJECTORY_STEPS):
     if steps == list(range(steps[0], steps[0] + len(steps))):
         return f"steps {steps[0]}..{steps[0] + len(steps)} from the initial drop"
     stride = steps[1] - steps[0] if len(steps) > 1 else 0
-    return (f"{len(steps)} single steps spread over the {TRAJECTORY_STEPS}-step trajectory (steps {steps[0]}, "
+    return (f"{len(steps)} single steps spread over the {total}-step trajectory (steps {steps[0]}, "
             f"{steps[0] + stride}, ..., {steps[-1]}; the steps between them run untimed)")
 
 
@@ -356,7 +367,56 @@ def adjoint_cpu_baseline(bodies, offs, ball, params, nsub, steps, per_core=1):
     }
 
 
-def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
+def _large_cpu_worker(job):
+    """One oracle step of the large scene in the reference's order, timed."""
+    st, params_tuple, nsub, cores = job
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+
+    p = abi.default_params(step_dt=params_tuple[0], iterations=params_tuple[1])
+    o = O.OracleWorld(p, mode=O.REFERENCE, threads=cores)
+    o.add_bodies(st["bodies"])
+    o.import_state(st)
+    t0 = time.perf_counter()
+    o.step_fixed(nsub)
+    return time.perf_counter() - t0
+
+
+def large_cpu_baseline(states, params, nsub, ndyn, at, limit_s=90.0):
+    """The oracle's Reference step of the one-scene 100k workload on the host
+    cores, from the device's state at a few of the timed trajectory steps.
+    The reference's CPU step is quadratic here (all-pairs discovery, a linear
+    pair lookup per discovered pair), so the sample is a few steps, each
+    timed alone in a child process and given at most limit_s seconds; a
+    step that runs out counts as limit_s, which makes the rate an upper
+    bound of the reference's."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    secs, capped = [], 0
+    ctx = mp.get_context("spawn")
+    for st in states:
+        pool = ctx.Pool(1)
+        try:
+            r = pool.apply_async(_large_cpu_worker, ((st, (params.step_dt, params.iterations), nsub, cores),))
+            secs.append(r.get(timeout=limit_s))
+        except mp.TimeoutError:
+            secs.append(limit_s)
+            capped += 1
+        finally:
+            pool.terminate()
+            pool.join()
+        print(f"[large] cpu step {len(secs)}: {secs[-1]:.1f} s", file=sys.stderr, flush=True)
+    return {"value": ndyn * len(secs) / sum(secs), "unit": "body-steps/s", "cores": cores, "kind": "port",
+            "per_step_s": secs, "steps_cut_at_limit": capped, "upper_bound": capped > 0,
+            "sample": f"{len(secs)} of the timed steps (trajectory steps {at}), each one oracle step in the "
+                      f"reference's order (all-pairs discovery split over {cores} threads as the reference splits "
+                      f"it with rayon, linear pair lookup, serial sweep) from the device's state at that step, "
+                      f"in a child process given {limit_s:.0f} s (a step cut there counts as {limit_s:.0f} s, so the "
+                      f"rate is then an upper bound); rate = body-steps / summed seconds"}
+
+
+def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True, threads=1):
     """Part of the oracle leg: per-substep parity of the benchmarked world
     against the oracle on a seeded sample of its scenes, at the world's
     current state, for `steps` steps.  Before every substep, each sampled
@@ -387,7 +447,7 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
             sub = P.scene_state(st, offs, sc)
             pair = []
             for dbl in (False, True):
-                o = O.OracleWorld(params, mode=O.COLOURED, use_double=dbl)
+                o = O.OracleWorld(params, mode=O.COLOURED, use_double=dbl, threads=threads)
                 o.split_sums(split)
                 o.add_bodies(sub["bodies"])
                 o.import_state(sub)
@@ -419,10 +479,46 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True):
 
 
 # ---------------------------------------------------------------------------
+def run_reference_large(args):
+    """The reference's CPU step on the one-scene 100k workload: the oracle in
+    the reference's order from the initial drop, three steps timed (each
+    step is quadratic in bodies; the rate is extrapolated from them)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_api as O
+
+    bodies = scenes.large_100k()
+    params, nsub = scenes.params_for("large_100k")
+    cores = os.cpu_count() or 1
+    o = O.OracleWorld(params, mode=O.REFERENCE, threads=cores)
+    o.add_bodies(bodies)
+    secs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        o.step_fixed(nsub)
+        secs.append(time.perf_counter() - t0)
+    ndyn = scenes.dynamic_count(bodies)
+    v = ndyn * len(secs) / sum(secs)
+    cb = {"value": v, "unit": "body-steps/s", "cores": cores, "kind": "port", "per_step_s": secs,
+          "sample": f"steps 0..3 of the 300-step trajectory from the initial drop, the oracle in the reference's "
+                    f"order (all-pairs discovery over {cores} threads, linear pair lookup, serial sweep); rate "
+                    f"extrapolated from those three steps"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
+            "steps": len(secs), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene)",
+            "config": {"workload": "large_100k", "scenes": 1, "dynamic_bodies": ndyn, "dt": params.step_dt,
+                       "substeps": nsub, "iterations": params.iterations, "trajectory": "steps 0..3"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     d = dist_init(args.gpus)
     if d is not None and d[1] != 0:
         return 0
+    if args.workload == "large_100k":
+        return run_reference_large(args)
     bodies, offs, counts = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
     steps = timed_steps(args)
@@ -449,6 +545,9 @@ def run_ours(args):
     bodies_all, offs_all, joints_all, params, nsub = workload(args)
     if world > 1 and joints_all:
         raise SystemExit("the articulated workload runs on one GPU (two scenes)")
+    if world > 1 and args.workload == "large_100k":
+        raise SystemExit("the large workload is one scene: it runs on one GPU")
+    large = args.workload == "large_100k"
     bodies, offs = shard(bodies_all, offs_all, rank, world) if world > 1 else (bodies_all, offs_all)
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
@@ -492,9 +591,22 @@ def run_ours(args):
     if d:
         d[0].barrier()
     t0 = time.perf_counter()
-    ms = run_sampled(lambda k: w.step_graph(nsub * k), lambda k: w.step_timed(nsub * k, use_graph=True), steps)
+    if large:
+        # the one scene's state is about L2's size: evict it before every timed step
+        def timed_one(k):
+            total = 0.0
+            for _ in range(k):
+                w.flush_cache()
+                total += w.step_timed(nsub, use_graph=True)
+            return total
+
+        ms = run_sampled(lambda k: w.step_graph(nsub * k), timed_one, steps)
+    else:
+        ms = run_sampled(lambda k: w.step_graph(nsub * k), lambda k: w.step_timed(nsub * k, use_graph=True), steps)
     clk.mark(t0, time.perf_counter())
     clk.__exit__()
+    if large:
+        print(f"[large] timed {len(steps)} steps: {ms:.1f} ms", file=sys.stderr, flush=True)
     if d:
         (ms,), (nd,) = combine_ranks(d[0], f"cuda:{device}", worst=[ms], total=[ndyn])
         ndyn_total = int(nd)
@@ -507,8 +619,11 @@ def run_ours(args):
     par = None
     if args.parity_scenes > 0 and not joints_all:
         lanes = tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)
-        par = oracle_parity(w, offs, params, nsub, nscenes=args.parity_scenes, steps=args.parity_steps,
-                            split=lanes <= 0)
+        if large:
+            print("[large] oracle parity", file=sys.stderr, flush=True)
+        par = oracle_parity(w, offs, params, nsub, nscenes=args.parity_scenes,
+                            steps=min(args.parity_steps, 1) if large else args.parity_steps,
+                            split=lanes <= 0, threads=(os.cpu_count() or 1) if large else 1)
     # ---- per-phase profile at the end of the trajectory: primal roofline ---
     phases, info = w.profile_substep()
     lanes = tuned[0][0] if tuned else (args.lanes if args.lanes is not None else 1)
@@ -546,6 +661,18 @@ def run_ours(args):
     if d:
         (e2e_max,), _ = combine_ranks(d[0], f"cuda:{device}", worst=[e2e_s])
         e2e = ndyn_total * len(e2e_steps) / e2e_max
+    cb = None
+    if large and args.cpu_per_core > 0:
+        # the device's state at three of the timed steps (early, middle, late)
+        at = sorted({steps[len(steps) // 6], steps[len(steps) // 2], steps[-1]})
+        w.import_state(s0)
+        states, cur = [], 0
+        for t in at:
+            if t > cur:
+                w.step_graph(nsub * (t - cur))
+            cur = t
+            states.append(w.export_state())
+        cb = large_cpu_baseline(states, params, nsub, ndyn, at)
     w.close()
     if rank != 0:
         return 0
@@ -554,16 +681,15 @@ def run_ours(args):
     # the one-scene and CPU comparisons belong to the batched workload (the
     # ragdoll scenes are 45k and 78k bodies: the oracle's all-pairs discovery
     # does not finish a step in bounded time)
-    if args.plain_scenes > 0 and not joints_all:
+    if args.plain_scenes > 0 and not joints_all and not large:
         plain = plain_rate(bodies_all, offs_all, params, nsub, args)
     adj = None
-    if args.adjoint_scenes > 0 and world == 1 and not joints_all:
+    if args.adjoint_scenes > 0 and world == 1 and not joints_all and not large:
         adj = adjoint_rate(args)
     rag = None
-    if args.ragdoll_adjoint_steps > 0 and world == 1:
+    if args.ragdoll_adjoint_steps > 0 and world == 1 and not large:
         rag = ragdoll_adjoint_rate(args)
-    cb = None
-    if args.cpu_per_core > 0 and world == 1 and not joints_all:
+    if args.cpu_per_core > 0 and world == 1 and not joints_all and not large:
         cb = cpu_baseline(bodies_all, offs_all, params, nsub, steps, per_core=args.cpu_per_core)
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
@@ -571,9 +697,10 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes, no dataset)",
         "config": {"workload": args.workload, "scenes": len(offs_all) - 1, "dynamic_bodies": ndyn_total,
                    "joints": len(joints_all),
-                   "dt": 1 / 120, "substeps": nsub, "iterations": params.iterations,
-                   "trajectory": describe_steps(steps),
-                   "l2": "state larger than L2 (GB-scale pair/point arrays), no flush",
+                   "dt": params.step_dt, "substeps": nsub, "iterations": params.iterations,
+                   "trajectory": describe_steps(steps, trajectory_len(args)),
+                   "l2": ("256 MB write before every timed step (the scene's state is about L2's size)" if large
+                          else "state larger than L2 (GB-scale pair/point arrays), no flush"),
                    "graph": True, "precision": "fast" if args.fast else "exact",
                    "primal_launch": {"lanes": tuned[0][0], "block": tuned[0][1], "min_blocks_per_sm": tuned[0][2],
                                      "by_work": tuned[0][3], "tuned_at_step": args.tune_at,
@@ -778,8 +905,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
-    ap.add_argument("--workload", default="batched_4096", choices=["batched_4096", "ragdoll_8192"],
-                    help="ragdoll_8192: 8192 15-capsule ragdolls with ball/hinge joints in two scenes")
+    ap.add_argument("--workload", default="batched_4096", choices=["batched_4096", "ragdoll_8192", "large_100k"],
+                    help="ragdoll_8192: 8192 15-capsule ragdolls with ball/hinge joints in two scenes; "
+                         "large_100k: one scene of 100,000 bodies, dt 1/60, 1 substep, 10 iterations, 300 steps")
     ap.add_argument("--start", type=int, default=None,
                     help="time the contiguous window [start, start + steps) instead of steps spread over the "
                          "trajectory")

@@ -389,6 +389,14 @@ int avbd_set_work_order(AvbdWorld* world, int by_work);
  * sweep.  Both give the same candidate set.  No reference counterpart. */
 int avbd_set_broadphase(AvbdWorld* world, int small_scene_max);
 
+/* How the device-wide path sweeps a large scene: rows = 1 (default) cuts
+ * space into cells at least as wide as the scene's widest box, sorts the
+ * bodies by the Morton code of their (y, z) cell row and then by min x, and
+ * sweeps each body's row and the four forward neighbouring rows; rows = 0
+ * sorts by min x alone and sweeps once.  Both give the same candidate set.
+ * No reference counterpart. */
+int avbd_set_sweep(AvbdWorld* world, int rows);
+
 int avbd_abi_version(void);
 
 /* ---- measurement (no reference counterpart: the reference publishes no
@@ -398,6 +406,12 @@ int avbd_abi_version(void);
  * and return their device time in *ms, from CUDA events recorded on the
  * world's stream before the first and after the last substep. */
 int avbd_world_step_timed(AvbdWorld* world, int32_t substeps, int32_t use_graph, float* ms);
+
+/* Evict the world's state from the L2 cache: write a 256 MB scratch array
+ * (twice the GB300's L2, allocated on the first call, freed with the world)
+ * on the world's stream and wait for it.  For timing a state smaller than
+ * L2 without carrying it over in cache between timed steps. */
+int avbd_world_flush_cache(AvbdWorld* world);
 
 /* Advance one substep through plain launches with a CUDA event between the
  * phases.  ms[9]: wake+torque, broadphase, CCD, discovery, post-discovery,

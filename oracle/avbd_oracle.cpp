@@ -1058,7 +1058,22 @@ template <class T> struct Engine {
         std::vector<std::pair<V3<T>, V3<T>>> fresh;
         bool wake_vote;
     };
+    // The reference scans the pair vector (rows.rs:546, :811).  The Coloured
+    // schedule keeps the vector in (a, b) order, so there (the checker's
+    // mode, not the timed reference order) a binary search finds the same
+    // pair; pairs_sorted is set at the start of each discovery.
+    bool pairs_sorted = false;
     const Pair<T>* find_pair(uint32_t ia, uint32_t ib) const {
+        if (pairs_sorted) {
+            size_t lo = 0, hi = pairs.size();
+            while (lo < hi) {
+                size_t m = (lo + hi) / 2;
+                const Pair<T>& p = pairs[m];
+                if (p.a < ia || (p.a == ia && p.b < ib)) lo = m + 1;
+                else hi = m;
+            }
+            return lo < pairs.size() && pairs[lo].a == ia && pairs[lo].b == ib ? &pairs[lo] : nullptr;
+        }
         for (const Pair<T>& p : pairs)
             if (p.a == ia && p.b == ib) return &p;
         return nullptr;
@@ -1201,6 +1216,9 @@ template <class T> struct Engine {
     // generate_pairs (rows.rs:767-943)
     void generate_pairs() {
         uint32_t n = (uint32_t)bodies.size();
+        pairs_sorted = mode == COLOURED;
+        for (size_t k = 1; pairs_sorted && k < pairs.size(); k++)
+            pairs_sorted = pairs[k - 1].a < pairs[k].a || (pairs[k - 1].a == pairs[k].a && pairs[k - 1].b < pairs[k].b);
         std::vector<Discovered> disc;
         if (threads > 1 && n > 256) {
             // Parallel over the first index, like the rayon split at rows.rs:769-782;

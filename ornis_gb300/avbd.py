@@ -68,12 +68,14 @@ def lib():
             "avbd_set_work_order": [vp, C.c_int],
             "avbd_abi_version": [],
             "avbd_world_step_timed": [vp, C.c_int32, C.c_int32, C.POINTER(C.c_float)],
+            "avbd_world_flush_cache": [vp],
             "avbd_world_profile_substep": [vp, vp, vp],
             "avbd_world_graph_nodes": [vp, C.POINTER(u32)],
             "avbd_scene_step_static": [C.POINTER(abi.AvbdParams), vp, u32, C.c_int32, vp],
             "avbd_world_graph_nodes_emit": [vp, C.POINTER(u32)],
             "avbd_set_events": [vp, C.c_int32],
             "avbd_set_broadphase": [vp, C.c_int],
+            "avbd_set_sweep": [vp, C.c_int],
             "avbd_world_drain_contact_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_drain_trigger_events": [vp, vp, u32, C.POINTER(u32)],
             "avbd_world_event_counts": [vp, vp],
@@ -229,6 +231,10 @@ class AvbdWorld:
         _check(lib().avbd_world_step_timed(self.h, int(substeps), int(use_graph), C.byref(ms)), "step_timed")
         return ms.value
 
+    def flush_cache(self):
+        """Evict the world's state from L2 (a 256 MB write on its stream)."""
+        _check(lib().avbd_world_flush_cache(self.h), "flush_cache")
+
     def profile_substep(self):
         ms = np.zeros(9, np.float32)
         info = np.zeros(5, np.uint32)
@@ -263,6 +269,10 @@ class AvbdWorld:
 
     def set_broadphase(self, small_scene_max):
         _check(lib().avbd_set_broadphase(self.h, int(small_scene_max)), "set_broadphase")
+
+    def set_sweep(self, rows):
+        """Large scenes: 1 sweeps Morton-ordered cell rows, 0 one x-sweep (same candidates)."""
+        _check(lib().avbd_set_sweep(self.h, int(rows)), "set_sweep")
 
     def set_tuning(self, lanes, block):
         _check(lib().avbd_set_tuning(self.h, int(lanes), int(block)), "set_tuning")

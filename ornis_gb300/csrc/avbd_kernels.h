@@ -19,6 +19,7 @@ struct Tune {
     int primal_block = 128;      // threads per block of the primal kernel (per-scene solve: 128, 256, 512)
     int primal_minb = 4;         // resident blocks per SM the thread-per-body primal is built for
     int small_scene_max = 2048;  // scenes up to this many bodies use the one-CTA broadphase
+    int sweep_rows = 1;          // larger scenes: 1 sweep per Morton-ordered cell row, 0 one x-sweep
     int fast = 0;                // 1: the fast build of the iteration kernels
     int sort_work = 0;           // 1: order each colour's bodies by incident-pair count
 };
@@ -46,6 +47,10 @@ struct BroadphasePlan {
     int n_small = 0;
     std::vector<std::pair<uint32_t, uint32_t>> large;  // body ranges sorted device-wide
     uint32_t *keys_alt = nullptr, *vals_alt = nullptr, *hist = nullptr, *scan_tmp = nullptr;
+    // large scenes: sweep per row of cells in Morton order (1) or one x-sweep (0)
+    int rows = 1;
+    uint32_t* row_key = nullptr;  // per body of the largest scene: its row's Morton code
+    float* ext = nullptr;         // per large scene: the widest AABB edge
 };
 void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st);
 void launch_ccd(const DW& w, cudaStream_t st);

@@ -338,6 +338,120 @@ __global__ void k_sap_sweep(DW w, uint32_t n) {
         if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
     }
 }
+// Large scenes, cell rows: space is cut into cells at least as wide as the
+// scene's widest AABB (so overlapping boxes have centres in the same or
+// adjacent cells along every axis); a row is the cells of one (y, z) cell
+// pair, all x.  Bodies are sorted by (row Morton code, min x) with two
+// stable radix sorts; each body sweeps its own row forward in x as the
+// one-axis sweep does, and the four rows of the forward half of its (y, z)
+// neighbourhood over the x window its box can reach.  Every overlapping pair
+// is tested exactly once, with the same closed-interval test: the candidate
+// set is the one-axis sweep's.  Cell coordinates are taken in double from
+// the boxes' float bounds, with a 1% wider cell, so that rounding cannot
+// move a pair more than one cell apart.
+__device__ __forceinline__ uint32_t part1by1(uint32_t x) {
+    x &= 0xffffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+// Cell coordinate of a centre: floor(c / cell) shifted into [0, 65534]
+// (clamping keeps adjacent cells adjacent; 65535 would collide with the
+// half-space key).
+__device__ __forceinline__ int cell_of(double c, double cell) {
+    double k = floor(c / cell) + 32768.0;
+    return (int)fmin(fmax(k, 0.0), 65534.0);
+}
+__device__ __forceinline__ uint32_t row_code(int cy, int cz) { return (part1by1(cy) << 1) | part1by1(cz); }
+__device__ __forceinline__ double row_cell(float wmax) { return 1.01 * (double)wmax; }
+__device__ __forceinline__ void row_cells(const DW& w, uint32_t h, double cell, int& cy, int& cz) {
+    float4 lo = w.aabb_lo[h], hi = w.aabb_hi[h];
+    cy = cell_of(0.5 * ((double)lo.y + (double)hi.y), cell);
+    cz = cell_of(0.5 * ((double)lo.z + (double)hi.z), cell);
+}
+// the scene's widest AABB edge (boxes are cubes here; every axis is taken)
+__global__ void k_sap_extent(DW w, uint32_t b0, uint32_t b1, float* ext) {
+    float m = 0.0f;
+    for (uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x; h < b1; h += gridDim.x * blockDim.x) {
+        if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) continue;
+        float4 lo = w.aabb_lo[h], hi = w.aabb_hi[h];
+        m = fmaxf(m, fmaxf(hi.x - lo.x, fmaxf(hi.y - lo.y, hi.z - lo.z)));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax((int*)ext, __float_as_int(m));  // m >= 0: int order
+}
+__global__ void k_sap_row_keys(DW w, uint32_t b0, uint32_t b1, const float* ext, uint32_t* row_key) {
+    uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= b1) return;
+    bool plane = info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE;
+    uint32_t rk = 0xffffffffu;
+    if (!plane) {
+        int cy, cz;
+        row_cells(w, h, row_cell(*ext), cy, cz);
+        rk = row_code(cy, cz);
+    }
+    w.sort_key[h - b0] = plane ? 0xffffffffu : f2key(w.aabb_lo[h].x);
+    w.sort_idx[h - b0] = h;
+    row_key[h - b0] = rk;
+}
+// after the sort by min x: the row codes in that order (the second sort's keys)
+__global__ void k_sap_row_gather(DW w, uint32_t b0, uint32_t n, const uint32_t* row_key) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w.sort_key[i] = row_key[w.sort_idx[i] - b0];
+}
+// first sorted slot in [lo, hi) whose row code is >= key
+__device__ __forceinline__ uint32_t row_lower(const uint32_t* keys, uint32_t lo, uint32_t hi, uint32_t key) {
+    while (lo < hi) {
+        uint32_t m = (lo + hi) >> 1;
+        if (keys[m] < key) lo = m + 1;
+        else hi = m;
+    }
+    return lo;
+}
+__global__ void k_sap_row_sweep(DW w, uint32_t n, const float* ext) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t rk = w.sort_key[i];
+    if (rk == 0xffffffffu) return;  // half-spaces sort last
+    const uint32_t a = w.sort_idx[i];
+    const float4 alo = w.aabb_lo[a], ahi = w.aabb_hi[a];
+    for (uint32_t j = i + 1; j < n && w.sort_key[j] == rk; j++) {
+        uint32_t b = w.sort_idx[j];
+        float4 blo = w.aabb_lo[b];
+        if (blo.x > ahi.x) break;
+        if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
+    }
+    const float wmax = *ext;
+    int cy, cz;
+    row_cells(w, a, row_cell(wmax), cy, cz);
+    // a neighbour's box reaches x >= alo.x only if its min x is at least this
+    const double reach = (double)alo.x - 1.01 * (double)wmax - 1e-6 * fabs((double)alo.x);
+    const int dy[4] = {0, 1, 1, 1}, dz[4] = {1, -1, 0, 1};
+    for (int k = 0; k < 4; k++) {
+        int ny = cy + dy[k], nz = cz + dz[k];
+        if (ny > 65534 || nz < 0 || nz > 65534) continue;
+        const uint32_t nk = row_code(ny, nz);
+        uint32_t r0 = row_lower(w.sort_key, 0, n, nk);
+        uint32_t r1 = row_lower(w.sort_key, r0, n, nk + 1u);
+        // first slot of the row whose min x reaches the window
+        uint32_t lo = r0, hi = r1;
+        while (lo < hi) {
+            uint32_t m = (lo + hi) >> 1;
+            if ((double)w.aabb_lo[w.sort_idx[m]].x < reach) lo = m + 1;
+            else hi = m;
+        }
+        for (uint32_t j = lo; j < r1; j++) {
+            uint32_t b = w.sort_idx[j];
+            float4 blo = w.aabb_lo[b];
+            if (blo.x > ahi.x) break;
+            float4 bhi = w.aabb_hi[b];
+            if (alo.x <= bhi.x && overlap_yz(alo, ahi, blo, bhi)) emit_candidate(w, a, b);
+        }
+    }
+}
+
 // Half-space bodies have an unbounded prefilter radius (rows.rs:290), so the
 // reference narrowphases every (plane, body) pair.  A pair can only survive
 // discovery if it already exists (an empty shell is kept) or if the body can
@@ -374,6 +488,17 @@ void launch_broadphase(const DW& w, const BroadphasePlan& plan, cudaStream_t st)
     for (size_t i = 0; i < plan.large.size(); i++) {
         uint32_t b0 = plan.large[i].first, b1 = plan.large[i].second;
         uint32_t n = b1 - b0;
+        if (plan.rows) {
+            float* ext = plan.ext + i;
+            cudaMemsetAsync(ext, 0, sizeof(float), st);
+            k_sap_extent<<<std::min<unsigned>(nblk(n, 256), 4u * 152u), 256, 0, st>>>(w, b0, b1, ext);
+            k_sap_row_keys<<<nblk(n, 256), 256, 0, st>>>(w, b0, b1, ext, plan.row_key);
+            radix_sort_pairs(w.sort_key, w.sort_idx, plan.keys_alt, plan.vals_alt, n, plan.hist, plan.scan_tmp, st);
+            k_sap_row_gather<<<nblk(n, 256), 256, 0, st>>>(w, b0, n, plan.row_key);
+            radix_sort_pairs(w.sort_key, w.sort_idx, plan.keys_alt, plan.vals_alt, n, plan.hist, plan.scan_tmp, st);
+            k_sap_row_sweep<<<nblk(n, 128), 128, 0, st>>>(w, n, ext);
+            continue;
+        }
         k_sap_keys<<<nblk(n, 256), 256, 0, st>>>(w, b0, b1);
         radix_sort_pairs(w.sort_key, w.sort_idx, plan.keys_alt, plan.vals_alt, n, plan.hist, plan.scan_tmp, st);
         k_sap_sweep<<<nblk(n, 128), 128, 0, st>>>(w, n);

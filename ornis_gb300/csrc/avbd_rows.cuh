@@ -129,45 +129,55 @@ static __host__ __device__ __forceinline__ void stamp_angular(Sys& s, V3 g, floa
     s.r[3] += f * g.x; s.r[4] += f * g.y; s.r[5] += f * g.z;
 }
 
-// Dense LDL^T without pivoting (assembly.rs:25-69).  Returns false on a
-// breakdown pivot (<= 1e-12); the body then skips its update.
-static __host__ __device__ __forceinline__ bool solve_6x6(const Sys& s, float x[6]) {
-    float l[6][6];
-    float d[6];
+// Dense LDL^T without pivoting (assembly.rs:25-69), as a factorisation and
+// a solve: l holds the strict lower triangle of L row-major ((i, j), j < i,
+// at i*(i-1)/2 + j), dg the pivots.  Returns false on a breakdown pivot
+// (<= 1e-12); the body then skips its update.
+static __host__ __device__ __forceinline__ int stri(int i, int j) { return i * (i - 1) / 2 + j; }
+static __host__ __device__ __forceinline__ bool ldl_factor(const float h[21], float l[15], float dg[6]) {
 #pragma unroll
     for (int i = 0; i < 6; i++) {
 #pragma unroll
         for (int j = 0; j <= i; j++) {
-            float v = s.h[tri(i, j)];
+            float v = h[tri(i, j)];
 #pragma unroll
-            for (int k = 0; k < j; k++) v -= l[i][k] * d[k] * l[j][k];
+            for (int k = 0; k < j; k++) v -= l[stri(i, k)] * dg[k] * l[stri(j, k)];
             if (i == j) {
                 if (v <= DEGENERATE_LEN2) return false;
-                d[i] = v;
-                l[i][i] = 1.0f;
+                dg[i] = v;
             } else {
-                l[i][j] = v / d[j];
+                l[stri(i, j)] = v / dg[j];
             }
         }
     }
+    return true;
+}
+// x = -(L D L^T)^-1 r
+static __host__ __device__ __forceinline__ void ldl_solve(const float l[15], const float dg[6], const float r[6],
+                                                          float x[6]) {
     float y[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
-        float v = -s.r[i];
+        float v = -r[i];
 #pragma unroll
-        for (int k = 0; k < i; k++) v -= l[i][k] * y[k];
+        for (int k = 0; k < i; k++) v -= l[stri(i, k)] * y[k];
         y[i] = v;
     }
     float z[6];
 #pragma unroll
-    for (int i = 0; i < 6; i++) z[i] = y[i] / d[i];
+    for (int i = 0; i < 6; i++) z[i] = y[i] / dg[i];
 #pragma unroll
     for (int i = 5; i >= 0; i--) {
         float v = z[i];
 #pragma unroll
-        for (int k = i + 1; k < 6; k++) v -= l[k][i] * x[k];
+        for (int k = i + 1; k < 6; k++) v -= l[stri(k, i)] * x[k];
         x[i] = v;
     }
+}
+static __host__ __device__ __forceinline__ bool solve_6x6(const Sys& s, float x[6]) {
+    float l[15], dg[6];
+    if (!ldl_factor(s.h, l, dg)) return false;
+    ldl_solve(l, dg, s.r, x);
     return true;
 }
 

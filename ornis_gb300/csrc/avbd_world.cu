@@ -174,6 +174,7 @@ struct AvbdWorld {
     AvbdBody* d_stage = nullptr;
     uint32_t* h_ctr = nullptr;  // pinned copy of the device counters
     uint32_t ev_cap0 = 0;
+    void* flush_buf = nullptr;  // L2 eviction scratch (avbd_world_flush_cache)
     AvbdCounters cum{};
     float time_debt = 0.0f;
     int last_ncol = 0;
@@ -343,6 +344,9 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     W->plan.keys_alt = m.get<uint32_t>(max_large);
     W->plan.vals_alt = m.get<uint32_t>(max_large);
     W->plan.hist = m.get<uint32_t>(radix_hist_words(max_large));
+    W->plan.rows = W->tune.sweep_rows;
+    W->plan.row_key = m.get<uint32_t>(max_large);
+    W->plan.ext = m.get<float>(W->plan.large.size());
     size_t scan_words = std::max({scan_tmp_words((size_t)N + 1), scan_tmp_words(radix_hist_words(max_large)),
                                   scan_tmp_words(radix_hist_words(N))});
     W->scan_tmp = m.get<uint32_t>(scan_words + 16);
@@ -1406,6 +1410,7 @@ int avbd_world_destroy(AvbdWorld* W) {
     W->evmem.release();
     W->hullmem.release();
     if (W->h_ctr) cudaFreeHost(W->h_ctr);
+    if (W->flush_buf) cudaFree(W->flush_buf);
     if (W->st) cudaStreamDestroy(W->st);
     delete W;
     return AVBD_OK;
@@ -2062,6 +2067,17 @@ int avbd_set_broadphase(AvbdWorld* W, int small_scene_max) {
     return AVBD_OK;
 }
 
+int avbd_set_sweep(AvbdWorld* W, int rows) {
+    if (!W || rows < 0 || rows > 1) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = host_edit(W);  // the sweep plan is built with the device buffers
+    if (rc) return rc;
+    W->tune.sweep_rows = rows;
+    W->n_alloc = 0;
+    free_graphs(W);
+    return AVBD_OK;
+}
+
 int avbd_abi_version(void) { return AVBD_ABI_VERSION; }
 
 // Bracket a region for profilers started with collection off
@@ -2089,6 +2105,16 @@ int avbd_world_step_timed(AvbdWorld* W, int32_t substeps, int32_t use_graph, flo
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int avbd_world_flush_cache(AvbdWorld* W) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    const size_t bytes = size_t(256) << 20;
+    if (!W->flush_buf) CK(cudaMalloc(&W->flush_buf, bytes));
+    CK(cudaMemsetAsync(W->flush_buf, W->cum.steps & 0xff, bytes, W->st));
+    CK(cudaStreamSynchronize(W->st));
+    return AVBD_OK;
 }
 
 // One substep through plain launches with an event between phases:
