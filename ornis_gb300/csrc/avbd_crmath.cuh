@@ -26,6 +26,16 @@
 // Every double operation is an explicitly rounded one (no contraction), so
 // the double path gives the same bits in every build.  The constant tables
 // were printed by gen_crmath_constants.py.
+//
+// Small arguments — the per-iteration rotations and joint twists of the step
+// — first try a float stage: x + d with the Taylor correction d evaluated in
+// float (|x| <= 1/16, or |y/x| <= 1/16 with x > 0 for atan2; t = y/x carried
+// as t_hi + t_lo from the exact division remainder), the sum split exactly by
+// Knuth's two-sum into s + e, and s accepted when |e| plus a bound of the
+// evaluation error stays below half the gap from s to its neighbour on e's
+// side (Ziv's test again, one level down).  The GB300's FP64 rate is a small
+// fraction of its FP32 rate, and the float stage settles almost every call of
+// the step; a rejected argument goes on to the double stage.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -301,6 +311,91 @@ CRM_HD DD horner_dd(const double* c, int n, DD z) {
     return p;
 }
 
+// ---- float stage ----------------------------------------------------------------
+#ifdef __CUDA_ARCH__
+#define CRF_MUL(a, b) __fmul_rn((a), (b))
+#define CRF_ADD(a, b) __fadd_rn((a), (b))
+#define CRF_SUB(a, b) __fsub_rn((a), (b))
+#define CRF_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#define CRF_DIV(a, b) __fdiv_rn((a), (b))
+#else
+#define CRF_MUL(a, b) ((a) * (b))
+#define CRF_ADD(a, b) ((a) + (b))
+#define CRF_SUB(a, b) ((a) - (b))
+#define CRF_FMA(a, b, c) std::fma((a), (b), (c))
+#define CRF_DIV(a, b) ((a) / (b))
+#endif
+// s + e = a + b exactly (Knuth's two-sum; round to nearest, no overflow)
+CRM_HD void two_sum_f(float a, float b, float& s, float& e) {
+    s = CRF_ADD(a, b);
+    float bb = CRF_SUB(s, a);
+    e = CRF_ADD(CRF_SUB(a, CRF_SUB(s, bb)), CRF_SUB(b, bb));
+}
+// The value lies in [s + e - err, s + e + err], s = fl(s + e): s is its
+// correctly rounded float when neither end crosses the midpoint between s
+// and its neighbour on that side (the gaps below and above s differ at a
+// power of two).  The comparisons keep a 1% margin over the rounding of
+// e +- err.
+CRM_HD bool float_stage_ok(float s, float e, float err) {
+#ifdef AVBD_CRMATH_TEST_DOUBLE  // tests: skip the float stage
+    return false;
+#else
+    if (!(fabsf(s) < 3.0e38f) || fabsf(s) < 0x1p-100f) return false;
+    const float up = CRF_MUL(CRF_SUB(next_up(s), s), 0.5f);    // exact
+    const float dn = CRF_MUL(CRF_SUB(s, next_down(s)), 0.5f);  // exact
+    return CRF_MUL(CRF_ADD(e, err), 1.01f) < up && CRF_MUL(CRF_SUB(err, e), 1.01f) < dn;
+#endif
+}
+// x + x^3 (c1 + z (c2 + z c3)), z = x^2, |x| <= 1/16: the sin and asin
+// stages.  The series' next term is below 2^-36 |x|.
+CRM_HD bool odd_stage(float x, float c1, float c2, float c3, float& out) {
+    const float z = CRF_MUL(x, x);
+    const float p = CRF_FMA(CRF_FMA(c3, z, c2), z, c1);
+    const float d = CRF_MUL(CRF_MUL(x, z), p);
+    float s, e;
+    two_sum_f(x, d, s, e);
+    const float err = CRF_FMA(fabsf(d), 0x1p-20f, CRF_MUL(fabsf(x), 0x1p-36f));
+    out = s;
+    return float_stage_ok(s, e, err);
+}
+CRM_HD bool sin_stage(float x, float& out) {
+    return fabsf(x) <= 0.0625f && odd_stage(x, -0x1.555556p-3f, 0x1.111112p-7f, -0x1.a01a02p-13f, out);
+}
+// 1 + z (-1/2 + z (1/24 - z/720)), |x| <= 1/16; next term below 2^-47
+CRM_HD bool cos_stage(float x, float& out) {
+    if (!(fabsf(x) <= 0.0625f)) return false;
+    const float z = CRF_MUL(x, x);
+    const float d = CRF_MUL(z, CRF_FMA(CRF_FMA(-0x1.6c16c2p-10f, z, 0x1.555556p-5f), z, -0.5f));
+    float s, e;
+    two_sum_f(1.0f, d, s, e);
+    const float err = CRF_FMA(fabsf(d), 0x1p-20f, 0x1p-45f);
+    out = s;
+    return float_stage_ok(s, e, err);
+}
+CRM_HD bool asin_stage(float x, float& out) {
+    // asin: x + x^3 (1/6 + z (3/40 + z 15/336)); the next term is below 2^-37 |x|
+    return fabsf(x) <= 0.0625f && odd_stage(x, 0x1.555556p-3f, 0x1.333334p-4f, 0x1.6db6dcp-5f, out);
+}
+// atan2(y, x) for x > 0, |y| <= x/16: t = y/x = th + tl, atan(t) = t + t^3 (-1/3
+// + z (1/5 - z/7)); the next term is below 2^-35 |t|.
+CRM_HD bool atan2_stage(float y, float x, float& out) {
+    // y/x's remainder y - th x is exact only if it stays above the subnormal range
+    if (!(x > 0.0f) || !(x < 3.0e38f) || !(fabsf(y) <= CRF_MUL(x, 0.0625f)) || fabsf(y) < 0x1p-90f) return false;
+    const float th = CRF_DIV(y, x);
+    const float tl = CRF_DIV(CRF_FMA(-th, x, y), x);  // the remainder y - th x is exact
+    const float z = CRF_MUL(th, th);
+    const float p = CRF_FMA(CRF_FMA(-0x1.24924ap-3f, z, 0x1.99999ap-3f), z, -0x1.555556p-2f);
+    const float tail = CRF_MUL(CRF_MUL(th, z), p);
+    const float d = CRF_ADD(tl, tail);
+    float s, e;
+    two_sum_f(th, d, s, e);
+    // the tail's rounding, the sum's, and the tail taken at th instead of t
+    // (|t - th| <= 2^-24 |th|, the tail's slope |t|^2 <= 2^-8) with the series' rest
+    const float err = CRF_FMA(CRF_ADD(fabsf(tail), fabsf(tl)), 0x1p-20f, CRF_MUL(fabsf(th), 0x1p-31f));
+    out = s;
+    return float_stage_ok(s, e, err);
+}
+
 // ---- sin, cos -----------------------------------------------------------------
 CRM_HD uint64_t mul_hi64(uint64_t a, uint64_t b) {
 #ifdef __CUDA_ARCH__
@@ -420,6 +515,8 @@ CRM_HD void reduce(float x, DD& r, int& j) {
 CRM_HD float sinf(float x) {
     if (!(fabsf(x) <= 3.4028235e38f)) return x - x;  // NaN for NaN and infinities
     if (x == 0.0f) return x;
+    float f;
+    if (sin_stage(x, f)) return f;
     DD r;
     int j;
     reduce(x, r, j);
@@ -428,6 +525,8 @@ CRM_HD float sinf(float x) {
 CRM_HD float cosf(float x) {
     if (!(fabsf(x) <= 3.4028235e38f)) return x - x;
     if (x == 0.0f) return 1.0f;
+    float f;
+    if (cos_stage(x, f)) return f;
     DD r;
     int j;
     reduce(x, r, j);
@@ -443,11 +542,18 @@ CRM_HD void sincosf(float x, float* s, float* c) {
         *c = 1.0f;
         return;
     }
+    float fs, fc;
+    const bool ks = sin_stage(x, fs), kc = cos_stage(x, fc);
+    if (ks && kc) {
+        *s = fs;
+        *c = fc;
+        return;
+    }
     DD r;
     int j;
     reduce(x, r, j);
-    *s = sincos_finish(r, j, true, x < 0.0f ? -1.0f : 1.0f);
-    *c = sincos_finish(r, j, false, 1.0f);
+    *s = ks ? fs : sincos_finish(r, j, true, x < 0.0f ? -1.0f : 1.0f);
+    *c = kc ? fc : sincos_finish(r, j, false, 1.0f);
 }
 
 // ---- asin ------------------------------------------------------------------------
@@ -456,6 +562,8 @@ CRM_HD float asinf(float x) {
     const float ax = fabsf(x);
     if (!(ax <= 1.0f)) return (x - x) / (x - x);  // NaN for NaN and |x| > 1
     if (x == 0.0f) return x;
+    float f;
+    if (asin_stage(x, f)) return f;
     const double sgn = x < 0.0f ? -1.0 : 1.0;
     const double a = (double)ax;
     double y;
@@ -516,6 +624,8 @@ CRM_HD float atan2f(float y, float x) {
         if (ay == INF) return sy * dd_to_float(cst(C_PI2));
         return xneg ? sy * dd_to_float(cst(C_PI)) : sy * 0.0f;
     }
+    float f;
+    if (atan2_stage(y, x, f)) return f;
     const bool swap = ay > ax;
     const double num = swap ? (double)ax : (double)ay, den = swap ? (double)ay : (double)ax;
     const double t = CRM_DIV(num, den);  // [0, 1]

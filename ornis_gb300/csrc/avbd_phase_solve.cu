@@ -113,9 +113,14 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
 
 // Joint rows for body h (assembly.rs:255-881): Ball, Revolute (and its
 // limit), Prismatic (and its limit), Fixed, Distance, Rope, SixDof.
+// ALL = false: the instantiation for worlds whose joints are all ball and
+// revolute joints (the other kinds' rows would cost it registers).
+template <bool ALL>
 static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint32_t h, Sys& s) {
     uint2 ab = w.j_ab[j];
     const uint32_t kind = w.j_kind[j];
+    const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
+    const bool k_dist = ALL && (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE);
     bool is_a = ab.x == h;
     float sign = is_a ? 1.0f : -1.0f;
     float lsign = is_a ? -1.0f : 1.0f;  // rows measured B minus A flip the gradient
@@ -131,8 +136,8 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
     float4 pl = w.j_pen_l[j], ll = w.j_lam_l[j], pa4 = w.j_pen_a[j], la4 = w.j_lam_a[j];
     float penl[3] = {pl.x, pl.y, pl.z}, laml[3] = {ll.x, ll.y, ll.z};
     float pena[3] = {pa4.x, pa4.y, pa4.z}, lama[3] = {la4.x, la4.y, la4.z};
-    const bool fixed = kind == AVBD_JOINT_FIXED;
-    const V3 dref = fixed || kind == AVBD_JOINT_SIXDOF ? ld3(w.j_dref[j]) : V0();
+    const bool fixed = ALL && kind == AVBD_JOINT_FIXED;
+    const V3 dref = fixed || k_six ? ld3(w.j_dref[j]) : V0();
     const float4 ref = w.j_ref[j];
     V3 r_plain = is_a ? qrot(qa, la) : qrot(qb, lb);
     V3 fl = V0();
@@ -151,7 +156,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             stamp_row(s, axis, penl[k], f, lever, sign);
             fl[k] = f;
         }
-    } else if (kind == AVBD_JOINT_PRISMATIC) {
+    } else if (k_pri) {
         V3 u = tangent_t1(wa);
         V3 v = cross(u, wa);
         V3 axs[2] = {u, v};
@@ -162,7 +167,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             stamp_row(s, axs[li], penl[li], f, r_plain, sign);
             fl = fl + axs[li] * f;
         }
-    } else if (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE) {
+    } else if (k_dist) {
         float ln = len(live);
         if (kind == AVBD_JOINT_DISTANCE || ln > ref.x) {
             V3 dir = ln > NEAR_ZERO ? live / ln : VY();
@@ -173,7 +178,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
                 fl = dir * f;
             }
         }
-    } else if (kind == AVBD_JOINT_SIXDOF) {
+    } else if (k_six) {
         const uint32_t cfg = w.j_cfg[j];
         const float4 sa0 = w.j_sacc[2 * (size_t)j];
         const float sacc[3] = {sa0.x, sa0.y, sa0.z};
@@ -225,7 +230,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
         s.h[tri(5, 5)] += len(V3{hm[0][2], hm[1][2], hm[2][2]});
     }
     // angular rows
-    if (kind == AVBD_JOINT_REVOLUTE || kind == AVBD_JOINT_PRISMATIC) {
+    if (kind == AVBD_JOINT_REVOLUTE || k_pri) {
         V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
         V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
         V3 t1 = tangent_t1(axa0);
@@ -237,7 +242,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             if (!row_live(cc, f)) continue;
             stamp_angular(s, is_a ? cross(axa, ts[li]) : -cross(axb, ts[li]), pena[li], f);
         }
-    } else if (kind == AVBD_JOINT_SIXDOF) {
+    } else if (k_six) {
         const uint32_t cfg = w.j_cfg[j];
         const Q qref = ldq(w.j_qref[j]);
         const float4 sa0 = w.j_sacc[2 * (size_t)j], sa1 = w.j_sacc[2 * (size_t)j + 1];
@@ -297,7 +302,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             float f = lower ? fminf(f_raw, 0.0f) : fmaxf(f_raw, 0.0f);
             if (row_live(cc, f)) stamp_angular(s, is_a ? -wa : wa, pa4.z, f);
         }
-    } else if (lim.z != 0.0f && kind == AVBD_JOINT_PRISMATIC) {
+    } else if (lim.z != 0.0f && k_pri) {
         float sv = dot(pb - pa, wa) - ref.x;
         int stt = warm_limit_state(sv, lim.x, lim.y, LIMIT_SLOP_LIN, ref.y);
         if (stt >= 0) {
@@ -357,9 +362,10 @@ static __device__ __forceinline__ void apply_solve(const DW& w, uint32_t h, cons
 
 // One thread per body: rows accumulate in the reference's order (pairs in
 // ascending index — B-side pairs precede A-side ones — then joints).
-// JOINTS: the instantiation for worlds with joints (the joint-free one keeps
-// the joint rows' code and registers out of the contact-only kernels)
-template <int MINB, bool JOINTS>
+// JT: 0 for worlds without joints (the joint rows' code and registers stay
+// out of the contact-only kernels), 1 with ball and revolute joints only,
+// 2 with any joint kind.
+template <int MINB, int JT>
 __global__ void __launch_bounds__(128, MINB) k_primal_thread(DW w, int colour) {
     if (aborted_solve(w)) return;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -379,15 +385,15 @@ __global__ void __launch_bounds__(128, MINB) k_primal_thread(DW w, int colour) {
         load_ctx(w, p, c);
         for (uint32_t q = 0; q < c.np; q++) stamp_point(w, c, p, q, true, s);
     }
-    if (JOINTS)
-        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+    if (JT)
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint<JT == 2>(w, w.jlist[k], h, s);
     apply_solve(w, h, s);
 }
 
 // L lanes per body: the body's incident pairs are dealt round-robin over the
 // lanes, the partial systems are summed with shuffles, lane 0 adds the
 // inertial block and the joints and solves.
-template <int L, bool JOINTS>
+template <int L, int JT>
 __global__ void k_primal_lanes(DW w, int colour) {
     if (aborted_solve(w)) return;
     uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -424,8 +430,8 @@ __global__ void k_primal_lanes(DW w, int colour) {
     for (int k = 0; k < 21; k++) t.h[k] += s.h[k];
 #pragma unroll
     for (int k = 0; k < 6; k++) t.r[k] += s.r[k];
-    if (JOINTS)
-        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, t);
+    if (JT)
+        for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint<JT == 2>(w, w.jlist[k], h, t);
     apply_solve(w, h, t);
 }
 
@@ -558,7 +564,7 @@ static __device__ __forceinline__ uint32_t chunk_sort(uint32_t* cnt, uint32_t* e
     __syncthreads();
     return n;
 }
-__global__ void __launch_bounds__(CHUNK) k_side_rows(DW w, int colour) {
+__global__ void __launch_bounds__(CHUNK, 4) k_side_rows(DW w, int colour) {
     if (aborted_solve(w)) return;
     __shared__ uint32_t s_cnt[MAX_PTS + 1], s_ent[CHUNK];
     const uint32_t s0 = w.side_cnt[colour], s1 = w.side_cnt[colour + 1];
@@ -585,7 +591,7 @@ __global__ void __launch_bounds__(CHUNK) k_side_rows(DW w, int colour) {
         __syncthreads();  // the chunk's entries are read before the next chunk is sorted
     }
 }
-template <bool JOINTS>
+template <int JT>
 __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
     if (aborted_solve(w)) return;
     const uint32_t c0 = w.col_cnt[colour], c1 = w.col_cnt[colour + 1];
@@ -595,8 +601,8 @@ __global__ void __launch_bounds__(128) k_side_solve(DW w, int colour) {
         inertial_block(w, h, s);
         const uint32_t k0 = w.offA[h] + w.offB[h], k1 = min(w.offA[h + 1] + w.offB[h + 1], w.contrib_slots);
         for (uint32_t k = k0; k < k1; k++) add_slot(s, w.contrib + (size_t)k * 7);
-        if (JOINTS)
-            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+        if (JT)
+            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint<JT == 2>(w, w.jlist[k], h, s);
         apply_solve(w, h, s);
     }
 }
@@ -681,9 +687,11 @@ __global__ void __launch_bounds__(CHUNK) k_dual_pairs(DW w) {
 static __device__ __forceinline__ float ramp(float pen, float c, float beta, float cap) {
     return fminf(pen + beta * fabsf(c), cap);
 }
+template <bool ALL>
 static __device__ void dual_joint(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];
     const uint32_t kind = w.j_kind[j];
+    const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
     V3 la = ld3(w.j_la[j]), lb = ld3(w.j_lb[j]);
@@ -700,7 +708,7 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
     // is the reference's dual ascent
     const float K = w.joint_k;
     const bool soft = K > 0.0f && (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE);
-    const bool fixed = kind == AVBD_JOINT_FIXED;
+    const bool fixed = ALL && kind == AVBD_JOINT_FIXED;
     if (kind == AVBD_JOINT_BALL || kind == AVBD_JOINT_REVOLUTE || fixed) {
         const V3 dref = fixed ? ld3(w.j_dref[j]) : V0();
         V3 lv = fixed ? live + qrot(qa, dref) : live;
@@ -714,7 +722,7 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
                 penl[k] = ramp(penl[k], cc, BETA, PENALTY_MAX);
             }
         }
-    } else if (kind == AVBD_JOINT_PRISMATIC) {
+    } else if (k_pri) {
         V3 wa = normalize_or(qrot(qa, ld3(w.j_axa[j])), VZ());
         V3 u = tangent_t1(wa);
         V3 v = cross(u, wa);
@@ -726,13 +734,13 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
                 penl[li] = ramp(penl[li], cc, BETA, PENALTY_MAX);
             }
         }
-    } else if (kind == AVBD_JOINT_DISTANCE) {
+    } else if (ALL && kind == AVBD_JOINT_DISTANCE) {
         float cc = (len(live) - ref.x) - ALPHA * (len(c0v) - ref.x);
         if (fabsf(cc) >= C_EPS) {
             laml[0] += penl[0] * cc;
             penl[0] = ramp(penl[0], cc, BETA, PENALTY_MAX);
         }
-    } else if (kind == AVBD_JOINT_ROPE) {
+    } else if (ALL && kind == AVBD_JOINT_ROPE) {
         float ln = len(live);
         if (ln > ref.x) {
             float cc = (ln - ref.x) - ALPHA * (len(c0v) - ref.x);
@@ -743,7 +751,7 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
         } else {
             laml[0] = 0.0f;
         }
-    } else if (kind == AVBD_JOINT_SIXDOF) {
+    } else if (k_six) {
         const uint32_t cfg = w.j_cfg[j];
         const V3 dref = ld3(w.j_dref[j]);
         const Q qref = ldq(w.j_qref[j]);
@@ -813,7 +821,7 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
         w.j_sacc[2 * (size_t)j + 1] = make_float4(sacc[4], sacc[5], 0.0f, 0.0f);
     }
     // angular equality rows
-    if (kind == AVBD_JOINT_REVOLUTE || kind == AVBD_JOINT_PRISMATIC) {
+    if (kind == AVBD_JOINT_REVOLUTE || k_pri) {
         float4 axa4 = w.j_axa[j];
         V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
         V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
@@ -862,7 +870,7 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
             lim.w = 0.0f;
         }
         w.j_lim[j] = lim;
-    } else if (lim.z != 0.0f && kind == AVBD_JOINT_PRISMATIC) {
+    } else if (lim.z != 0.0f && k_pri) {
         V3 axa_l = ld3(w.j_axa[j]);
         V3 wa = normalize_or(qrot(qa, axa_l), VZ());
         float sv = dot(pb - pa, wa) - ref.x;
@@ -889,10 +897,11 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
     w.j_lam_a[j] = make_float4(lama[0], lama[1], lama[2], 0.0f);
     w.j_pen_a[j] = make_float4(pena[0], pena[1], pena[2], 0.0f);
 }
+template <bool ALL>
 __global__ void k_dual_joints(DW w) {
     if (aborted_solve(w)) return;
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < (uint32_t)w.J) dual_joint(w, j);
+    if (j < (uint32_t)w.J) dual_joint<ALL>(w, j);
 }
 
 // ---- per-scene solve: one block walks a scene through every iteration ---------
@@ -949,7 +958,7 @@ static __device__ __forceinline__ void block_scan(uint32_t* a, uint32_t n, uint3
     __syncthreads();
 }
 
-template <int BS, int MINB, bool JOINTS>
+template <int BS, int MINB, int JT>
 __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
     if (aborted_solve(w)) return;
     __shared__ uint32_t s_list[SCENE_MAX_BODIES];      // swept bodies grouped by colour
@@ -1047,8 +1056,8 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
                         __syncthreads();
                     }
                     if (tid < nb) {
-                        if (JOINTS)
-                            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint(w, w.jlist[k], h, s);
+                        if (JT)
+                            for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) stamp_joint<JT == 2>(w, w.jlist[k], h, s);
                         apply_solve(w, h, s);
                     }
                     i0 = i1;
@@ -1056,18 +1065,18 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
                 __syncthreads();  // this colour's poses before the next colour reads them
             }
             for (uint32_t p = p0 + tid; p < p1; p += BS) dual_pair(w, p);
-            if (JOINTS)
+            if (JT)
                 for (uint32_t h = b0 + tid; h < b1; h += BS)
                     for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
                         uint32_t j = w.jlist[k];
-                        if (w.j_ab[j].x == h) dual_joint(w, j);
+                        if (w.j_ab[j].x == h) dual_joint<JT == 2>(w, j);
                     }
             __syncthreads();
         }
     }
 }
 
-template <int BS, int MINB, bool JOINTS>
+template <int BS, int MINB, int JT>
 static void scene_solve_launch(const DW& w, cudaStream_t st) {
     const size_t smem = (size_t)BS * 7 * sizeof(float4);
     static int grid[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per device ordinal
@@ -1075,26 +1084,27 @@ static void scene_solve_launch(const DW& w, cudaStream_t st) {
     cudaGetDevice(&dev);
     int& g = grid[dev & 7];
     if (!g) {
-        cudaFuncSetAttribute(k_scene_solve<BS, MINB, JOINTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_scene_solve<BS, MINB, JT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_solve<BS, MINB, JOINTS>, BS, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scene_solve<BS, MINB, JT>, BS, smem);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         g = max(1, per_sm) * max(1, sms);
     }
-    k_scene_solve<BS, MINB, JOINTS><<<min(g, max(1, w.S)), BS, smem, st>>>(w);
+    k_scene_solve<BS, MINB, JT><<<min(g, max(1, w.S)), BS, smem, st>>>(w);
 }
-template <bool JOINTS>
+template <int JT>
 static void scene_solve_block(const DW& w, int block, cudaStream_t st) {
     switch (block) {
-        case 128: scene_solve_launch<128, 4, JOINTS>(w, st); break;
-        case 512: scene_solve_launch<512, 1, JOINTS>(w, st); break;
-        default: scene_solve_launch<256, 2, JOINTS>(w, st); break;
+        case 128: scene_solve_launch<128, 4, JT>(w, st); break;
+        case 512: scene_solve_launch<512, 1, JT>(w, st); break;
+        default: scene_solve_launch<256, 2, JT>(w, st); break;
     }
 }
 void launch_scene_solve(const DW& w, const Tune& tune, cudaStream_t st) {
     cudaMemsetAsync(w.ctr + C_SCENE_Q, 0, sizeof(uint32_t), st);
-    if (w.J) scene_solve_block<true>(w, tune.primal_block, st);
-    else scene_solve_block<false>(w, tune.primal_block, st);
+    if (!w.J) scene_solve_block<0>(w, tune.primal_block, st);
+    else if (!w.j_all) scene_solve_block<1>(w, tune.primal_block, st);
+    else scene_solve_block<2>(w, tune.primal_block, st);
 }
 
 // The per-scene solve's fallback for a world with a scene above its limit is
@@ -1107,7 +1117,7 @@ void launch_solve_prep(const DW& w, const Tune& tune, cudaStream_t st) {
     k_side_starts<<<1, 32, 0, st>>>(w);
     k_side_place<<<gsz(w.pair_cap, SIDE_BLOCK), SIDE_BLOCK, 0, st>>>(w);
 }
-template <bool J>
+template <int J>
 static void primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
     int bs = tune.primal_block;
     switch (launch_lanes(tune)) {
@@ -1129,12 +1139,16 @@ static void primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bod
     }
 }
 void launch_primal_colour(const DW& w, const Tune& tune, int c, uint32_t max_bodies, cudaStream_t st) {
-    if (w.J) primal_colour<true>(w, tune, c, max_bodies, st);
-    else primal_colour<false>(w, tune, c, max_bodies, st);
+    if (!w.J) primal_colour<0>(w, tune, c, max_bodies, st);
+    else if (!w.j_all) primal_colour<1>(w, tune, c, max_bodies, st);
+    else primal_colour<2>(w, tune, c, max_bodies, st);
 }
 void launch_dual(const DW& w, const Tune& tune, cudaStream_t st) {
     k_dual_pairs<<<gsz(w.pair_cap, 128), 128, 0, st>>>(w);
-    if (w.J) k_dual_joints<<<nblk(w.J, 128), 128, 0, st>>>(w);
+    if (w.J) {
+        if (w.j_all) k_dual_joints<true><<<nblk(w.J, 128), 128, 0, st>>>(w);
+        else k_dual_joints<false><<<nblk(w.J, 128), 128, 0, st>>>(w);
+    }
 }
 void launch_iteration(const DW& w, const Tune& tune, int ncolours, cudaStream_t st) {
     for (int c = 0; c < ncolours; c++) AVBD_SOLVE_NS::launch_primal_colour(w, tune, c, (uint32_t)w.N, st);

@@ -709,6 +709,9 @@ static int upload_all(AvbdWorld* W) {
     up((void*)w.jofs, jofs.data(), (N + 1) * 4);
     up((void*)w.jlist, jlist.data(), 2 * J * 4);
     up(w.j_kind, j_kind.data(), J * 4);
+    // the joint rows' kernels come in a ball-and-revolute instantiation
+    w.j_all = 0;
+    for (uint32_t k : j_kind) w.j_all |= (k != AVBD_JOINT_BALL && k != AVBD_JOINT_REVOLUTE) ? 1 : 0;
     up(w.j_ab, j_ab.data(), J * 8);
     up(w.j_la, j_la.data(), J * 16); up(w.j_lb, j_lb.data(), J * 16);
     up(w.j_axa, j_axa.data(), J * 16); up(w.j_axb, j_axb.data(), J * 16);

@@ -113,6 +113,7 @@ struct DW {
     int N;  // bodies
     int S;  // scenes
     int J;  // joints
+    int j_all;  // 1: a joint is neither a ball nor a revolute joint (the all-kinds solve kernels)
     float dt;
     V3 gravity;
     int iterations;

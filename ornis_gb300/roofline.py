@@ -23,6 +23,16 @@ iteration's primal and dual: its algorithmic bytes are iterations x (primal
 across the iterations, so its DRAM traffic is below these bytes.
 """
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture)
+# per algorithmic byte of the split primal (k_side_rows + k_side_solve, all
+# launches of one step): 512 scenes of the batched workload at step 200,
+# exact build, 96 non-empty colour launches of each kernel moved 4,836 MB
+# against 764 MB of model bytes.  The bench scales it to its own launches by
+# the model bytes (the same mix of bodies, points and pairs per byte).
+SPLIT_TRAFFIC_PER_MODEL_BYTE = 6.33
+TRAFFIC_SOURCE = ("ncu capture (512 scenes, step 200, exact build): 6.33 DRAM bytes per model byte, "
+                  "scaled to this launch by its model bytes")
+
 PRIMAL_BODY_B = 128
 PRIMAL_POINT_B = 48
 PAIR_HEADER_B = 32
@@ -82,7 +92,8 @@ def primal_roofline(phases_ms, info, peak, kind="thread", iterations=1):
         "unit": "GB/s",
         "frac": achieved / peak_gbs,
         "peak_source": f"{source} (MEASURED_PEAKS.json hbm_gbs)" if source == "measured" else "fallback 6.8 TB/s",
-        "traffic": None,
+        "traffic": SPLIT_TRAFFIC_PER_MODEL_BYTE * b / max(1, info["colours"]) if kind == "split" else None,
+        "traffic_source": TRAFFIC_SOURCE if kind == "split" else None,
         "bytes_per_launch": b / max(1, info["colours"]),
         "launch_ms": per_launch_ms,
         "model": "v1: 128 B/swept body + 48 B/point + 32 B/pair per iteration",

@@ -68,6 +68,16 @@ int main(int argc, char** argv) {
         }
         t2.check(a, b, avbd::crm::atan2f(a, b), (float)atan2l((long double)a, (long double)b));
     }
+    // the float stage of atan2: x near 1 (unit quaternions' w), |y| up to x/16
+    for (long i = 0; i < randoms * 10; i++) {
+        uint64_t r = next_u64();
+        float x = u2f(0x3f700000u + (uint32_t)(r & 0xfffffu));  // [0.9375, 1)
+        if (i % 3 == 0) x = u2f(0x3f800000u + (uint32_t)(r & 0x7fffffu));  // [1, 2)
+        int ex = (int)((r >> 24) & 31);  // |y| in [2^-(4+ex+1), 2^-(4+ex)) x
+        float y = x * u2f(0x3f800000u + (uint32_t)((r >> 32) & 0x7fffffu)) * ldexpf(1.0f, -5 - ex);
+        if ((r >> 63) & 1) y = -y;
+        t2.check(y, x, avbd::crm::atan2f(y, x), (float)atan2l((long double)y, (long double)x));
+    }
     for (Tally* t : {&ts, &tc, &tsc, &ta, &t2}) printf("%s %ld %ld\n", t->name, t->n, t->bad);
     return 0;
 }

@@ -2,13 +2,15 @@
 (ornis_gb300/csrc/avbd_crmath.cuh, built with nvcc as host code) against
 long-double references rounded once to float, on the host (no GPU).
 
-Two builds: the normal one (double evaluation, double-double only when
-Ziv's rounding test fails) and one that takes the double-double path for
-every argument, so that the rarely taken path is checked over the same
-sweep.  The sweep: every 40961st bit pattern of all 2^32 floats (signs,
-subnormals, huge arguments, NaN, infinities), every 7th float in
-[2^-14, 4), every 3rd float in [1/2, 1] for asin, and random pairs plus
-special values for atan2.  Every result must be bit-identical to the
+Three builds: the normal one (the float stage for small arguments, the
+double evaluation, double-double only when Ziv's rounding test fails), one
+without the float stage (the double evaluation checked over the whole
+sweep), and one that takes the double-double path for every argument, so
+that the rarely taken path is checked over the same sweep.  The sweep: every
+40961st bit pattern of all 2^32 floats (signs, subnormals, huge arguments,
+NaN, infinities), every 7th float in [2^-14, 4), every 3rd float in [1/2, 1]
+for asin, random pairs plus special values for atan2, and a million atan2
+arguments of the float stage (x near 1, |y| up to x/16).  Every result must be bit-identical to the
 reference (NaN to NaN)."""
 import os
 import re
@@ -41,9 +43,13 @@ def _sweep(tmp_path, extra, args):
     return res, out.stdout
 
 
-@pytest.mark.parametrize("slow", [False, True], ids=["double", "double-double"])
-def test_correctly_rounded_against_long_double(tmp_path, slow):
-    res, log = _sweep(tmp_path, ["-DAVBD_CRMATH_TEST_SLOW"] if slow else [], [40961, 100000])
+BUILDS = {"float": [], "double": ["-DAVBD_CRMATH_TEST_DOUBLE"],
+          "double-double": ["-DAVBD_CRMATH_TEST_DOUBLE", "-DAVBD_CRMATH_TEST_SLOW"]}
+
+
+@pytest.mark.parametrize("build", list(BUILDS))
+def test_correctly_rounded_against_long_double(tmp_path, build):
+    res, log = _sweep(tmp_path, BUILDS[build], [40961, 100000])
     for name, (n, bad) in res.items():
         assert n > 100000, (name, n)
         assert bad == 0, log
