@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define AVBD_ABI_VERSION 2
+#define AVBD_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 #define AVBD_OK 0
@@ -72,6 +72,15 @@ extern "C" {
 #define AVBD_JOINT_DISTANCE 4  /* JointKind::Distance  (rod of the assembly length)  */
 #define AVBD_JOINT_ROPE 5      /* JointKind::Rope      (max_distance)                */
 #define AVBD_JOINT_SIXDOF 6    /* JointKind::SixDof    (axis_config per axis)        */
+#define AVBD_JOINT_MOTOR 7     /* JointKind::Motor     (free velocity drive, no rows) */
+#define AVBD_JOINT_SPRING 8    /* JointKind::Spring    (spring-damper along the anchors) */
+
+/* JointMotor of a spring (joint.rs:951-996) */
+#define AVBD_MOTOR_VELOCITY 0  /* MotorKind::Velocity */
+#define AVBD_MOTOR_POSITION 1  /* MotorKind::Position */
+#define AVBD_MOTOR_SERVO 2     /* MotorKind::Servo */
+#define AVBD_MODEL_ACCELERATION 0 /* MotorModel::AccelerationBased (the default) */
+#define AVBD_MODEL_FORCE 1        /* MotorModel::ForceBased */
 
 /* SixDof per-axis configuration (AxisConfig, joint.rs) */
 #define AVBD_AXIS_FREE 0
@@ -124,6 +133,25 @@ typedef struct AvbdJointDesc {
     uint32_t axis_config[6]; /* sixdof: linear x y z, angular x y z in body A's assembly frame */
     float axis_min[6];       /* sixdof limited axes: travel window */
     float axis_max[6];
+    /* free motor (JointKind::Motor): B-minus-A velocity targets in the world
+     * frame, the force and torque budgets, and the assembly pull (0..1,
+     * validated; the AVBD step runs the velocity drive only, as the
+     * reference's does) */
+    float motor_linear[3];
+    float motor_angular[3];
+    float motor_max_force;
+    float motor_max_torque;
+    float motor_correction;
+    /* spring (JointKind::Spring): its JointMotor — rest length
+     * (target_position), target_velocity, stiffness, damping, max_force,
+     * kind (AVBD_MOTOR_*) and model (AVBD_MODEL_*) */
+    float spring_rest;
+    float spring_velocity;
+    float spring_stiffness;
+    float spring_damping;
+    float spring_max_force;
+    uint32_t spring_kind;
+    uint32_t spring_model;
 } AvbdJointDesc;
 
 /* Solver parameters.  avbd_default_params() fills the reference's constants
@@ -277,8 +305,14 @@ int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
  * length <= 0 -> AVBD_ERR_JOINT_BAD_BOUNDS, non-finite motor fields ->
  * AVBD_ERR_JOINT_NONFINITE, then both bodies wake, then self / invalid
  * handles; a degenerate hinge or slide axis -> AVBD_ERR_JOINT_BAD_AXIS.
+ * A free motor: non-finite targets or budgets, or a negative budget ->
+ * AVBD_ERR_JOINT_NONFINITE, a correction outside [0, 1] ->
+ * AVBD_ERR_JOINT_BAD_BOUNDS (its anchors are not used).  A spring's motor
+ * (validate_motor, migration.rs:366-394): non-finite targets, a negative or
+ * non-finite stiffness, damping or budget -> AVBD_ERR_JOINT_NONFINITE.
  * Kinds: Ball, Revolute (limit, velocity motor), Prismatic (limit, velocity
- * motor), Fixed, Distance, Rope, SixDof. */
+ * motor), Fixed, Distance, Rope, SixDof, Motor (free velocity drive),
+ * Spring; Wheel and Gear joints -> AVBD_ERR_UNSUPPORTED. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 
 /* PhysicsEngine::remove_joint (engine.rs, avbd/mod.rs:1531-1540): both

@@ -595,6 +595,12 @@ template <class T> struct Joint {  // AvbdJoint (avbd/mod.rs:327-402)
     uint32_t six_cfg[6];
     T six_min[6], six_max[6];
     T sacc[6];
+    // free motor (JointKind::Motor): velocity targets and budgets
+    V3<T> mot_lin, mot_ang;
+    T mot_force, mot_torque;
+    // spring (JointKind::Spring): its JointMotor
+    T spr_vel, spr_k, spr_c, spr_max;
+    uint32_t spr_kind, spr_model;
     T lam_l[3], lam_a[3], pen_l[3], pen_a[3];
 };
 
@@ -872,8 +878,10 @@ template <class T> struct Engine {
             case AVBD_JOINT_BALL: return len(delta);
             case AVBD_JOINT_REVOLUTE: return fmx(len(delta), len(axis - qrot(b.rot, j.ax_b)));
             case AVBD_JOINT_FIXED:
+            case AVBD_JOINT_MOTOR:  // a free motor: the assembly deviation (sleep.rs:76-82)
                 return fmx(len(delta - qrot(a.rot, j.dref)), len(quat_diff_vec(qmul(conj(a.rot), b.rot), j.q_ref)));
-            case AVBD_JOINT_DISTANCE: return std::fabs(len(delta) - j.ref_val);
+            case AVBD_JOINT_DISTANCE:
+            case AVBD_JOINT_SPRING: return std::fabs(len(delta) - j.ref_val);  // a spring: about its rest
             case AVBD_JOINT_ROPE: return fmx(len(delta) - j.ref_val, T(0));
             case AVBD_JOINT_PRISMATIC: {
                 V3<T> perp = delta - axis * dot(delta, axis);
@@ -937,8 +945,36 @@ template <class T> struct Engine {
     }
     // motor_impulse (joints_ext.rs:237-383): revolute and prismatic velocity
     // motors, before the warm start, paused while a limit is violated
+    // free_motor_impulse (joints_ext.rs:384-420): per world axis, the
+    // deadbeat linear then angular drive of B relative to A
+    void free_motor_impulse(Joint<T>& j) {
+        Body<T>& a = bodies[j.a];
+        Body<T>& b = bodies[j.b];
+        const V3<T> axes[3] = {VX<T>(), VY<T>(), VZ<T>()};
+        for (const V3<T>& axis : axes) {
+            T v = dot(b.vel - a.vel, axis);
+            T ka = eff_inv_mass(a), kb = eff_inv_mass(b);
+            T dj = velocity_impulse(dot(j.mot_lin, axis) - v, ka + kb, j.mot_force);
+            if (dj != T(0)) {
+                if (solvable(j.a)) a.vel = a.vel + axis * (-dj * ka);
+                if (solvable(j.b)) b.vel = b.vel + axis * (dj * kb);
+            }
+            T w = dot(b.angvel - a.angvel, axis);
+            V3<T> ia = ang_inv_wa(j.a, axis), ib = ang_inv_wa(j.b, axis);
+            T k = dot(ia, axis) + dot(ib, axis);
+            T dw = velocity_impulse(dot(j.mot_ang, axis) - w, k, j.mot_torque);
+            if (dw != T(0)) {
+                if (solvable(j.a)) a.angvel = a.angvel + (-dw) * ia;
+                if (solvable(j.b)) b.angvel = b.angvel + dw * ib;
+            }
+        }
+    }
     void motor_impulse() {
         for (Joint<T>& j : joints) {
+            if (j.kind == AVBD_JOINT_MOTOR) {  // free motors carry their drive inline
+                free_motor_impulse(j);
+                continue;
+            }
             if (!j.has_mot || j.mot_max <= T(0) || limit_violated(j)) continue;
             Body<T>& a = bodies[j.a];
             Body<T>& b = bodies[j.b];
@@ -998,6 +1034,16 @@ template <class T> struct Engine {
     }
     bool joint_driven(const Joint<T>& j) const {  // sleep.rs:18-28
         if (j.has_mot && j.mot_speed != T(0) && j.mot_max > T(0)) return true;
+        // JointMotor::keeps_awake (joint.rs:1116-1126) of a spring
+        if (j.kind == AVBD_JOINT_SPRING && j.spr_max > T(0) &&
+            (j.spr_kind == AVBD_MOTOR_VELOCITY ? j.spr_vel != T(0) : (j.spr_k > T(0) || j.spr_vel != T(0))))
+            return true;
+        // MotorDrive::keeps_awake (joint.rs:474-477)
+        if (j.kind == AVBD_JOINT_MOTOR && ((j.mot_force > T(0) && (j.mot_lin.x != T(0) || j.mot_lin.y != T(0) ||
+                                                                   j.mot_lin.z != T(0))) ||
+                                          (j.mot_torque > T(0) && (j.mot_ang.x != T(0) || j.mot_ang.y != T(0) ||
+                                                                   j.mot_ang.z != T(0)))))
+            return true;
         uint32_t m[2] = {j.a, j.b};
         for (uint32_t h : m) {
             const Body<T>& b = bodies[h];
@@ -1082,7 +1128,7 @@ template <class T> struct Engine {
     // Fixed and SixDof joints (their contact is structural)
     static bool no_collide_kind(uint32_t k) {
         return k == AVBD_JOINT_BALL || k == AVBD_JOINT_REVOLUTE || k == AVBD_JOINT_PRISMATIC ||
-               k == AVBD_JOINT_DISTANCE || k == AVBD_JOINT_ROPE;
+               k == AVBD_JOINT_DISTANCE || k == AVBD_JOINT_ROPE || k == AVBD_JOINT_MOTOR || k == AVBD_JOINT_SPRING;
     }
 
     bool discover_pair(uint32_t ia, uint32_t ib, Discovered& out) const {
@@ -1553,6 +1599,27 @@ template <class T> struct Engine {
                 if (row_live(c, f)) {
                     stamp_row(lhs, rhs, dir, j.pen_l[0], f, r_plain, sign);
                     fl = dir * f;
+                }
+            }
+        } else if (j.kind == AVBD_JOINT_SPRING) {
+            // position-level spring about the rest length (assembly.rs:363-425):
+            // penalty from the stiffness, damping from the step delta, no dual
+            T ln = len(live);
+            V3<T> dir = ln > C<T>(K::NEAR_ZERO) ? live / ln : VY<T>();
+            T s = ln - j.ref_val;
+            T s0 = len(c0v) - j.ref_val;
+            T ka = eff_inv_mass(a), kb = eff_inv_mass(b);
+            T m = ka + kb > C<T>(K::NEAR_ZERO) ? T(1) / (ka + kb) : T(0);
+            if (m > T(0)) {
+                T stiff = j.spr_model == AVBD_MODEL_FORCE ? j.spr_k : j.spr_k * m;
+                T dampc = j.spr_model == AVBD_MODEL_FORCE ? j.spr_c : j.spr_c * m;
+                if (stiff > T(0)) {
+                    T f = stiff * s + dampc * (s - s0) / dt;
+                    stamp_row(lhs, rhs, dir, stiff, f, r_plain, sign);
+                } else if (dampc > T(0)) {  // a pure damper: the viscous row only
+                    T pen_v = dampc / dt;
+                    T f = dampc * (s - s0) / dt;
+                    stamp_row(lhs, rhs, dir, pen_v, f, r_plain, sign);
                 }
             }
         } else if (j.kind == AVBD_JOINT_SIXDOF) {
@@ -2354,8 +2421,16 @@ template <class T> struct Engine {
         // validate_joint (migration.rs:160-330): anchors and axes finite, bounds ordered, motors finite
         auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
         auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-        if (d.kind > AVBD_JOINT_SIXDOF) return AVBD_ERR_UNSUPPORTED;
-        if (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+        if (d.kind > AVBD_JOINT_SPRING) return AVBD_ERR_UNSUPPORTED;
+        if (d.kind != AVBD_JOINT_MOTOR && (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)))
+            return AVBD_ERR_JOINT_BAD_AXIS;
+        if (d.kind == AVBD_JOINT_MOTOR) {  // migration.rs:331-356
+            if (!finite3(d.motor_linear) || !finite3(d.motor_angular)) return AVBD_ERR_JOINT_NONFINITE;
+            if (!(std::isfinite(d.motor_max_force) && d.motor_max_force >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+            if (!(std::isfinite(d.motor_max_torque) && d.motor_max_torque >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+            if (!(std::isfinite(d.motor_correction) && d.motor_correction >= 0.0f && d.motor_correction <= 1.0f))
+                return AVBD_ERR_JOINT_BAD_BOUNDS;
+        }
         const bool axial = d.kind == AVBD_JOINT_REVOLUTE || d.kind == AVBD_JOINT_PRISMATIC;
         if (axial) {
             if (!finite3(d.local_axis_a) || !finite3(d.local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
@@ -2371,6 +2446,12 @@ template <class T> struct Engine {
             }
         if (d.kind == AVBD_JOINT_ROPE && !(std::isfinite(d.max_distance) && d.max_distance > 0.0f))
             return AVBD_ERR_JOINT_BAD_BOUNDS;
+        if (d.kind == AVBD_JOINT_SPRING) {  // validate_motor (migration.rs:366-394)
+            if (!std::isfinite(d.spring_rest) || !std::isfinite(d.spring_velocity)) return AVBD_ERR_JOINT_NONFINITE;
+            for (float v : {d.spring_stiffness, d.spring_damping, d.spring_max_force})
+                if (!(std::isfinite(v) && v >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+            if (d.spring_kind > AVBD_MOTOR_SERVO || d.spring_model > AVBD_MODEL_FORCE) return AVBD_ERR_INVALID_ARG;
+        }
         wake_body(d.body_a);
         wake_body(d.body_b);
         if (d.body_a == d.body_b) return AVBD_ERR_JOINT_SELF;
@@ -2379,6 +2460,7 @@ template <class T> struct Engine {
         j.a = d.body_a; j.b = d.body_b; j.kind = d.kind;
         j.la = {T(d.local_anchor_a[0]), T(d.local_anchor_a[1]), T(d.local_anchor_a[2])};
         j.lb = {T(d.local_anchor_b[0]), T(d.local_anchor_b[1]), T(d.local_anchor_b[2])};
+        if (d.kind == AVBD_JOINT_MOTOR) j.la = j.lb = VZERO<T>();  // a free motor has no anchors
         j.ax_a = VX<T>(); j.ax_b = VX<T>();
         j.ref_val = T(0);
         j.q_ref = Qt<T>{T(0), T(0), T(0), T(1)};
@@ -2406,7 +2488,8 @@ template <class T> struct Engine {
             j.has_mot = d.has_motor != 0;
             j.mot_speed = T(d.motor_speed);
             j.mot_max = T(d.motor_max);
-        } else if (d.kind == AVBD_JOINT_FIXED || d.kind == AVBD_JOINT_SIXDOF) {
+        } else if (d.kind == AVBD_JOINT_FIXED || d.kind == AVBD_JOINT_SIXDOF || d.kind == AVBD_JOINT_MOTOR) {
+            // the assembly pose (a free motor's only for its rest residual)
             j.q_ref = qmul(conj(ba.rot), bb.rot);
             V3<T> ra = qrot(ba.rot, j.la), rb = qrot(bb.rot, j.lb);
             j.dref = qrot(conj(ba.rot), (bb.pos + rb) - (ba.pos + ra));
@@ -2420,6 +2503,23 @@ template <class T> struct Engine {
             j.ref_val = len((bb.pos + rb) - (ba.pos + ra));
         } else if (d.kind == AVBD_JOINT_ROPE) {
             j.ref_val = T(d.max_distance);
+        }
+        j.mot_lin = {T(d.motor_linear[0]), T(d.motor_linear[1]), T(d.motor_linear[2])};
+        j.mot_ang = {T(d.motor_angular[0]), T(d.motor_angular[1]), T(d.motor_angular[2])};
+        j.mot_force = T(d.motor_max_force);
+        j.mot_torque = T(d.motor_max_torque);
+        if (d.kind != AVBD_JOINT_MOTOR) {
+            j.mot_lin = j.mot_ang = VZERO<T>();
+            j.mot_force = j.mot_torque = T(0);
+        }
+        if (d.kind == AVBD_JOINT_SPRING) {  // the rest length rides in the motor (mod.rs:1487-1493)
+            j.ref_val = T(d.spring_rest);
+            j.spr_vel = T(d.spring_velocity);
+            j.spr_k = T(d.spring_stiffness);
+            j.spr_c = T(d.spring_damping);
+            j.spr_max = T(d.spring_max_force);
+            j.spr_kind = d.spring_kind;
+            j.spr_model = d.spring_model;
         }
         j.acc_lim = T(0);
         j.lim_dual = T(0);

@@ -46,6 +46,10 @@ JOINT_FIXED = 3
 JOINT_DISTANCE = 4
 JOINT_ROPE = 5
 JOINT_SIXDOF = 6
+JOINT_MOTOR = 7
+JOINT_SPRING = 8
+MOTOR_VELOCITY, MOTOR_POSITION, MOTOR_SERVO = 0, 1, 2
+MODEL_ACCELERATION, MODEL_FORCE = 0, 1
 
 AXIS_FREE = 0
 AXIS_LOCKED = 1
@@ -103,6 +107,18 @@ class AvbdJointDesc(C.Structure):
         ("axis_config", C.c_uint32 * 6),
         ("axis_min", C.c_float * 6),
         ("axis_max", C.c_float * 6),
+        ("motor_linear", F3),
+        ("motor_angular", F3),
+        ("motor_max_force", C.c_float),
+        ("motor_max_torque", C.c_float),
+        ("motor_correction", C.c_float),
+        ("spring_rest", C.c_float),
+        ("spring_velocity", C.c_float),
+        ("spring_stiffness", C.c_float),
+        ("spring_damping", C.c_float),
+        ("spring_max_force", C.c_float),
+        ("spring_kind", C.c_uint32),
+        ("spring_model", C.c_uint32),
     ]
 
 
@@ -240,10 +256,13 @@ def default_params(gravity=(0.0, -9.81, 0.0), step_dt=1.0 / 60.0, iterations=10,
 
 
 def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0),
-               limit=None, motor=None, max_distance=0.0, axes=None):
+               limit=None, motor=None, max_distance=0.0, axes=None, drive=None, spring=None):
     """A joint record.  limit = (min, max); motor = (target speed, max
     torque or force); axes (sixdof) = 6 entries, each "free", "locked" or
-    (min, max), linear x y z then angular x y z."""
+    (min, max), linear x y z then angular x y z; drive (free motor) =
+    (linear target, angular target, max force, max torque, correction);
+    spring = (rest, target velocity, stiffness, damping, max force, kind,
+    model)."""
     d = AvbdJointDesc()
     d.kind = kind
     d.body_a = a
@@ -267,4 +286,14 @@ def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0
         else:
             d.axis_config[i] = AXIS_LIMITED
             d.axis_min[i], d.axis_max[i] = float(ax[0]), float(ax[1])
+    if drive is not None:
+        lin, ang, fmax, tmax, corr = drive
+        d.motor_linear[:] = list(map(float, lin))
+        d.motor_angular[:] = list(map(float, ang))
+        d.motor_max_force, d.motor_max_torque, d.motor_correction = float(fmax), float(tmax), float(corr)
+    if spring is not None:
+        rest, vel, k, c, fmax, kind_, model = spring
+        d.spring_rest, d.spring_velocity, d.spring_stiffness = float(rest), float(vel), float(k)
+        d.spring_damping, d.spring_max_force = float(c), float(fmax)
+        d.spring_kind, d.spring_model = int(kind_), int(model)
     return d

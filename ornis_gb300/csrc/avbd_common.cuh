@@ -88,6 +88,9 @@ static __device__ __forceinline__ bool jointed_no_collide(const DW& w, uint32_t 
     }
     return false;
 }
+static __device__ __forceinline__ float eff_inv_mass(const DW& w, uint32_t h) {  // rows.rs:406-412
+    return is_dynamic(w, h) ? w.inv_mass[h] : 0.0f;
+}
 // mod.rs:833-842 with RigidBody::wake_restore (body.rs:412-418)
 static __device__ __forceinline__ void wake_body(const DW& w, uint32_t h) {
     if (!w.asleep[h]) return;
@@ -146,9 +149,9 @@ static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j
     V3 axis = qrot(qa, ld3(w.j_axa[j]));
     if (kind == AVBD_JOINT_REVOLUTE) return fmaxf(len(delta), len(axis - qrot(qb, ld3(w.j_axb[j]))));
     const float refv = w.j_ref[j].x;
-    if (kind == AVBD_JOINT_FIXED)
+    if (kind == AVBD_JOINT_FIXED || kind == AVBD_JOINT_MOTOR)  // a free motor: its assembly deviation
         return fmaxf(len(delta - qrot(qa, ld3(w.j_dref[j]))), len(quat_diff_vec(qmul(conj(qa), qb), ldq(w.j_qref[j]))));
-    if (kind == AVBD_JOINT_DISTANCE) return fabsf(len(delta) - refv);
+    if (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_SPRING) return fabsf(len(delta) - refv);
     if (kind == AVBD_JOINT_ROPE) return fmaxf(len(delta) - refv, 0.0f);
     if (kind == AVBD_JOINT_PRISMATIC) {
         float e = len(delta - axis * dot(delta, axis));
@@ -184,7 +187,18 @@ static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j
 // sleep.rs:18-27: a running motor, or a non-dynamic member moved by its driver
 static __device__ __forceinline__ bool joint_driven(const DW& w, uint32_t j) {
     const float4 ref = w.j_ref[j];
-    if (ref.z != 0.0f && ref.w > 0.0f) return true;
+    if (w.j_kind[j] == AVBD_JOINT_SPRING) {  // JointMotor::keeps_awake (joint.rs:1116-1126)
+        const float4 m = w.j_axb[j];  // stiffness, damping, max_force, target_velocity
+        const bool velocity_kind = (w.j_cfg[j] & 15u) == AVBD_MOTOR_VELOCITY;
+        if (m.z > 0.0f && (velocity_kind ? m.w != 0.0f : (m.x > 0.0f || m.w != 0.0f))) return true;
+    } else if (w.j_kind[j] == AVBD_JOINT_MOTOR) {  // MotorDrive::keeps_awake (joint.rs:474-477)
+        const float4 lin = w.j_axa[j], ang = w.j_axb[j];
+        if ((ref.z > 0.0f && (lin.x != 0.0f || lin.y != 0.0f || lin.z != 0.0f)) ||
+            (ref.w > 0.0f && (ang.x != 0.0f || ang.y != 0.0f || ang.z != 0.0f)))
+            return true;
+    } else if (ref.z != 0.0f && ref.w > 0.0f) {
+        return true;
+    }
     uint2 ab = w.j_ab[j];
     uint32_t m[2] = {ab.x, ab.y};
     for (int k = 0; k < 2; k++) {

@@ -115,9 +115,6 @@ static __device__ V3 ang_inv_wa(const DW& w, uint32_t h, V3 wa) {  // joints_ext
     inverse_symmetric(iw, dg, inv);
     return mat3_vec(inv, wa);
 }
-static __device__ __forceinline__ float eff_inv_mass(const DW& w, uint32_t h) {  // rows.rs:406-412
-    return is_dynamic(w, h) ? w.inv_mass[h] : 0.0f;
-}
 // JointMotor::velocity_impulse (joint.rs:1172-1177)
 static __device__ __forceinline__ float velocity_impulse(const DW& w, float rate_error, float inv_eff, float max_f) {
     if (!(w.dt > 0.0f) || max_f <= 0.0f || inv_eff <= 0.0f) return 0.0f;
@@ -140,7 +137,39 @@ static __device__ bool limit_violated(const DW& w, uint32_t j) {  // joints_ext.
     }
     return false;
 }
+// free_motor_impulse (joints_ext.rs:384-420): per world axis, the deadbeat
+// linear then angular drive of B relative to A (MotorDrive's impulses,
+// joint.rs:485-499, are velocity_impulse's formula)
+static __device__ void free_motor_impulse(const DW& w, uint32_t j) {
+    const uint2 ab = w.j_ab[j];
+    const uint32_t a = ab.x, b = ab.y;
+    const V3 lin = ld3(w.j_axa[j]), ang = ld3(w.j_axb[j]);
+    const float4 ref = w.j_ref[j];
+    for (int i = 0; i < 3; i++) {
+        V3 axis = V0();
+        axis[i] = 1.0f;
+        float v = dot(ld3(w.vel[b]) - ld3(w.vel[a]), axis);
+        float ka = eff_inv_mass(w, a), kb = eff_inv_mass(w, b);
+        float dj = velocity_impulse(w, dot(lin, axis) - v, ka + kb, ref.z);
+        if (dj != 0.0f) {
+            if (solvable(w, a)) w.vel[a] = st3(ld3(w.vel[a]) + axis * (-dj * ka), 0.0f);
+            if (solvable(w, b)) w.vel[b] = st3(ld3(w.vel[b]) + axis * (dj * kb), 0.0f);
+        }
+        float om = dot(ld3(w.angvel[b]) - ld3(w.angvel[a]), axis);
+        V3 ia = ang_inv_wa(w, a, axis), ib = ang_inv_wa(w, b, axis);
+        float k = dot(ia, axis) + dot(ib, axis);
+        float dw = velocity_impulse(w, dot(ang, axis) - om, k, ref.w);
+        if (dw != 0.0f) {
+            if (solvable(w, a)) w.angvel[a] = st3(ld3(w.angvel[a]) + (-dw) * ia, 0.0f);
+            if (solvable(w, b)) w.angvel[b] = st3(ld3(w.angvel[b]) + dw * ib, 0.0f);
+        }
+    }
+}
 static __device__ void motor_impulse(const DW& w, uint32_t j) {  // joints_ext.rs:237-383
+    if (w.j_kind[j] == AVBD_JOINT_MOTOR) {  // free motors carry their drive inline
+        free_motor_impulse(w, j);
+        return;
+    }
     float4 ref = w.j_ref[j];
     if (!(ref.w > 0.0f) || limit_violated(w, j)) return;
     uint2 ab = w.j_ab[j];

@@ -121,6 +121,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
     const uint32_t kind = w.j_kind[j];
     const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
     const bool k_dist = ALL && (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE);
+    const bool k_spr = ALL && kind == AVBD_JOINT_SPRING;
     bool is_a = ab.x == h;
     float sign = is_a ? 1.0f : -1.0f;
     float lsign = is_a ? -1.0f : 1.0f;  // rows measured B minus A flip the gradient
@@ -176,6 +177,24 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
             if (row_live(cc, f)) {
                 stamp_row(s, dir, penl[0], f, r_plain, sign);
                 fl = dir * f;
+            }
+        }
+    } else if (k_spr) {
+        // position-level spring about the rest length (assembly.rs:363-425):
+        // penalty from the stiffness, damping from the step delta, no dual
+        const float ln = len(live);
+        const V3 dir = ln > NEAR_ZERO ? live / ln : VY();
+        const float sv = ln - ref.x, s0 = len(c0v) - ref.x;
+        const float ka = eff_inv_mass(w, ab.x), kb = eff_inv_mass(w, ab.y);
+        const float m = ka + kb > NEAR_ZERO ? 1.0f / (ka + kb) : 0.0f;
+        if (m > 0.0f) {
+            const float4 mo = w.j_axb[j];  // stiffness, damping, max_force, target_velocity
+            const bool force = (w.j_cfg[j] >> 4) == AVBD_MODEL_FORCE;
+            const float stiff = force ? mo.x : mo.x * m, dampc = force ? mo.y : mo.y * m;
+            if (stiff > 0.0f) {
+                stamp_row(s, dir, stiff, stiff * sv + dampc * (sv - s0) / w.dt, r_plain, sign);
+            } else if (dampc > 0.0f) {  // a pure damper: the viscous row only
+                stamp_row(s, dir, dampc / w.dt, dampc * (sv - s0) / w.dt, r_plain, sign);
             }
         }
     } else if (k_six) {

@@ -31,7 +31,11 @@ struct JointRec {
     int32_t has_lim;
     float lo, hi;
     float mot_speed, mot_max;  // velocity motor (mot_max 0: none)
-    float qref[4], dref[3];    // fixed / sixdof assembly references
+    float qref[4], dref[3];    // fixed / sixdof / free-motor assembly references
+    float mlin[3], mang[3];    // free motor: B-minus-A velocity targets (world frame)
+    float mforce, mtorque;     // free motor budgets
+    float spr[4];              // spring: stiffness, damping, max_force, target_velocity
+    uint32_t spr_mode;         // spring: kind | model << 4
     uint32_t cfg;              // sixdof axis configuration, 2 bits per axis
     float six_min[6], six_max[6];
     AvbdJointState st;
@@ -615,7 +619,8 @@ static int upload_all(AvbdWorld* W) {
         std::vector<std::vector<uint32_t>> per(S);
         for (uint32_t i = 0; i < J; i++) {
             const JointRec& j = W->joints[i];
-            if (j.mot_max > 0.0f || j.kind == AVBD_JOINT_ROPE) per[scene_of[j.a]].push_back(i);
+            if (j.mot_max > 0.0f || j.kind == AVBD_JOINT_ROPE || j.kind == AVBD_JOINT_MOTOR)
+                per[scene_of[j.a]].push_back(i);
         }
         for (uint32_t sc = 0; sc < S; sc++) {
             jimp_off[sc] = (uint32_t)jimp_list.size();
@@ -641,6 +646,19 @@ static int upload_all(AvbdWorld* W) {
         j_lb[i] = make_float4(j.lb[0], j.lb[1], j.lb[2], 0.0f);
         j_axa[i] = make_float4(j.axa[0], j.axa[1], j.axa[2], j.ref);
         j_axb[i] = make_float4(j.axb[0], j.axb[1], j.axb[2], 0.0f);
+        if (j.kind == AVBD_JOINT_MOTOR) {
+            // a free motor has no axes: its targets ride in the axis slots and
+            // its budgets in the motor slots of j_ref
+            j_axa[i] = make_float4(j.mlin[0], j.mlin[1], j.mlin[2], 0.0f);
+            j_axb[i] = make_float4(j.mang[0], j.mang[1], j.mang[2], 0.0f);
+            j_ref[i] = make_float4(0.0f, 0.0f, j.mforce, j.mtorque);
+        }
+        if (j.kind == AVBD_JOINT_SPRING) {
+            // a spring has no axes: its motor rides in the B-axis slot, its
+            // kind and model in the configuration word
+            j_axb[i] = make_float4(j.spr[0], j.spr[1], j.spr[2], j.spr[3]);
+            j_cfg[i] = j.spr_mode;
+        }
         j_lim[i] = make_float4(j.lo, j.hi, j.has_lim ? 1.0f : 0.0f, j.st.acc_lim);
         jll[i] = make_float4(j.st.lam_l[0], j.st.lam_l[1], j.st.lam_l[2], 0.0f);
         jla[i] = make_float4(j.st.lam_a[0], j.st.lam_a[1], j.st.lam_a[2], 0.0f);
@@ -1596,8 +1614,17 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     // ordered, motor fields finite, a rope longer than zero
     auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
     auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-    if (d->kind > AVBD_JOINT_SIXDOF) return AVBD_ERR_UNSUPPORTED;
-    if (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b)) return AVBD_ERR_JOINT_BAD_AXIS;
+    if (d->kind > AVBD_JOINT_SPRING) return AVBD_ERR_UNSUPPORTED;
+    const bool motor = d->kind == AVBD_JOINT_MOTOR;
+    // a free motor has no anchors (migration.rs:250-252); its drive is checked instead (:331-356)
+    if (!motor && (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b))) return AVBD_ERR_JOINT_BAD_AXIS;
+    if (motor) {
+        if (!finite3(d->motor_linear) || !finite3(d->motor_angular)) return AVBD_ERR_JOINT_NONFINITE;
+        if (!(std::isfinite(d->motor_max_force) && d->motor_max_force >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+        if (!(std::isfinite(d->motor_max_torque) && d->motor_max_torque >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+        if (!(std::isfinite(d->motor_correction) && d->motor_correction >= 0.0f && d->motor_correction <= 1.0f))
+            return AVBD_ERR_JOINT_BAD_BOUNDS;
+    }
     const bool axial = d->kind == AVBD_JOINT_REVOLUTE || d->kind == AVBD_JOINT_PRISMATIC;
     if (axial) {
         if (!finite3(d->local_axis_a) || !finite3(d->local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
@@ -1613,6 +1640,12 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
         }
     if (d->kind == AVBD_JOINT_ROPE && !(std::isfinite(d->max_distance) && d->max_distance > 0.0f))
         return AVBD_ERR_JOINT_BAD_BOUNDS;
+    if (d->kind == AVBD_JOINT_SPRING) {  // validate_motor (migration.rs:366-394)
+        if (!std::isfinite(d->spring_rest) || !std::isfinite(d->spring_velocity)) return AVBD_ERR_JOINT_NONFINITE;
+        for (float v : {d->spring_stiffness, d->spring_damping, d->spring_max_force})
+            if (!(std::isfinite(v) && v >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+        if (d->spring_kind > AVBD_MOTOR_SERVO || d->spring_model > AVBD_MODEL_FORCE) return AVBD_ERR_INVALID_ARG;
+    }
     cudaSetDevice(W->device);
     int rc = host_edit(W);
     if (rc) return rc;
@@ -1631,8 +1664,10 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     j.kind = d->kind;
     j.a = d->body_a;
     j.b = d->body_b;
-    std::memcpy(j.la, d->local_anchor_a, 12);
-    std::memcpy(j.lb, d->local_anchor_b, 12);
+    if (!motor) {
+        std::memcpy(j.la, d->local_anchor_a, 12);
+        std::memcpy(j.lb, d->local_anchor_b, 12);
+    }
     j.axa[0] = 1.0f; j.axb[0] = 1.0f;
     j.qref[3] = 1.0f;
     // resolve_joint (joint.rs:1251-1400), in the reference's f32 operation order
@@ -1664,7 +1699,8 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
             j.mot_speed = d->motor_speed;
             j.mot_max = d->motor_max;
         }
-    } else if (d->kind == AVBD_JOINT_FIXED || d->kind == AVBD_JOINT_SIXDOF) {
+    } else if (d->kind == AVBD_JOINT_FIXED || d->kind == AVBD_JOINT_SIXDOF || motor) {
+        // the assembly pose (a free motor's only for its rest residual)
         Q r = qmul(conj(qa), qb);
         j.qref[0] = r.x; j.qref[1] = r.y; j.qref[2] = r.z; j.qref[3] = r.w;
         V3 dr = qrot(conj(qa), (xb + qrot(qb, lb)) - (xa + qrot(qa, la)));
@@ -1679,6 +1715,20 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
         j.refv = len((xb + qrot(qb, lb)) - (xa + qrot(qa, la)));
     } else if (d->kind == AVBD_JOINT_ROPE) {
         j.refv = d->max_distance;
+    }
+    if (d->kind == AVBD_JOINT_SPRING) {  // the rest length rides in the motor (mod.rs:1487-1493)
+        j.refv = d->spring_rest;
+        j.spr[0] = d->spring_stiffness;
+        j.spr[1] = d->spring_damping;
+        j.spr[2] = d->spring_max_force;
+        j.spr[3] = d->spring_velocity;
+        j.spr_mode = d->spring_kind | (d->spring_model << 4);
+    }
+    if (motor) {
+        std::memcpy(j.mlin, d->motor_linear, 12);
+        std::memcpy(j.mang, d->motor_angular, 12);
+        j.mforce = d->motor_max_force;
+        j.mtorque = d->motor_max_torque;
     }
     for (int k = 0; k < 3; k++) {
         j.st.pen_l[k] = 1.0f;  // JOINT_PENALTY_INIT

@@ -1,5 +1,6 @@
 //! Raw declarations of `include/ornis_avbd.h`: `#[repr(C)]` mirrors of its
-//! records (same field order and sizes; `AvbdBody` is 136 bytes) and its
+//! records (same field order and sizes; `AvbdBody` is 136 bytes,
+//! `AvbdJointDesc` 224) and its
 //! `extern "C"` entry points.  Every function returns an `i32` status: 0 or a
 //! negative `AVBD_ERR_*` code.
 
@@ -38,11 +39,18 @@ pub const AVBD_JOINT_FIXED: u32 = 3;
 pub const AVBD_JOINT_DISTANCE: u32 = 4;
 pub const AVBD_JOINT_ROPE: u32 = 5;
 pub const AVBD_JOINT_SIXDOF: u32 = 6;
+pub const AVBD_JOINT_MOTOR: u32 = 7;
+pub const AVBD_JOINT_SPRING: u32 = 8;
+pub const AVBD_MOTOR_VELOCITY: u32 = 0;
+pub const AVBD_MOTOR_POSITION: u32 = 1;
+pub const AVBD_MOTOR_SERVO: u32 = 2;
+pub const AVBD_MODEL_ACCELERATION: u32 = 0;
+pub const AVBD_MODEL_FORCE: u32 = 1;
 
 pub const AVBD_AXIS_FREE: u32 = 0;
 pub const AVBD_AXIS_LOCKED: u32 = 1;
 pub const AVBD_AXIS_LIMITED: u32 = 2;
-pub const AVBD_ABI_VERSION: i32 = 2;
+pub const AVBD_ABI_VERSION: i32 = 3;
 
 pub const AVBD_MAX_POINTS: usize = 8;
 pub const AVBD_PRIMAL_SCENES: i32 = -1;
@@ -95,6 +103,20 @@ pub struct AvbdJointDesc {
     pub axis_config: [u32; 6],
     pub axis_min: [f32; 6],
     pub axis_max: [f32; 6],
+    /// free motor (`JointKind::Motor`): B-minus-A velocity targets, budgets, assembly pull
+    pub motor_linear: [f32; 3],
+    pub motor_angular: [f32; 3],
+    pub motor_max_force: f32,
+    pub motor_max_torque: f32,
+    pub motor_correction: f32,
+    /// spring (`JointKind::Spring`): its `JointMotor`
+    pub spring_rest: f32,
+    pub spring_velocity: f32,
+    pub spring_stiffness: f32,
+    pub spring_damping: f32,
+    pub spring_max_force: f32,
+    pub spring_kind: u32,
+    pub spring_model: u32,
 }
 
 #[repr(C)]

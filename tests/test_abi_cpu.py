@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_abi_version_and_defaults():
-    assert lib().avbd_abi_version() == 2
+    assert lib().avbd_abi_version() == 3
     p = abi.AvbdParams()
     assert lib().avbd_default_params(C.byref(p)) == 0
     assert abs(p.step_dt - 1 / 60) < 1e-9 and p.iterations == 10 and p.max_substeps == 4
@@ -47,7 +47,7 @@ def test_record_sizes():
     assert C.sizeof(abi.AvbdBody) == 136
     assert C.sizeof(abi.AvbdPointState) == 68
     assert abi.BODY_DTYPE.itemsize == 136
-    assert C.sizeof(abi.AvbdJointDesc) == 160
+    assert C.sizeof(abi.AvbdJointDesc) == 224
     assert C.sizeof(abi.AvbdJointState) == 80
 
 

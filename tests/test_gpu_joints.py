@@ -1,7 +1,8 @@
 """The joint kinds beyond Ball and Revolute on the CUDA path, per step from
 identical state against the oracle (Coloured order): the reference's
 behavioural joint scenes (hinge motor, prismatic slider at its limit,
-prismatic motor, fixed weld, distance rod, six-DOF locked / free / limited)
+prismatic motor, fixed weld, distance rod, six-DOF locked / free / limited,
+free motor, spring oscillator and damper)
 plus a rope, a mixed scene where every kind meets contacts, and a batch of
 two such scenes equal to each scene alone.  The exact build computes the
 oracle's arithmetic, so poses are identical; the parity bars (integers
@@ -57,6 +58,33 @@ def test_prismatic_slider_limit_and_motor():
     assert b["velocity"][1][0] > 1.0
 
 
+def test_free_motor():
+    """A box driven along +x across a floor by a free motor from a static
+    anchor (motor_joint.rs:90-110), per step; then a spin drive without
+    gravity."""
+    recs, drive = T._motor_scene()
+    b = run_pair(recs, [drive], 120)
+    assert b["velocity"][1][0] > 1.0
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 5, 0], 0.0)
+    ball = O.body_new(abi.SHAPE_SPHERE, [0.5], [0, 0, 0], 1.0)
+    b = run_pair([anchor, ball], [abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0],
+                                                 drive=((0.5, 0.0, 0.0), (0.0, 3.0, 0.0), 2.0, 0.05, 0.0))],
+                 60, gravity=(0.0, 0.0, 0.0))
+    assert b["angular_velocity"][1][1] > 0.5
+
+
+@pytest.mark.parametrize("model", [abi.MODEL_ACCELERATION, abi.MODEL_FORCE])
+def test_spring(model):
+    """The spring oscillator (p6_rope_spring_motor.rs:193-216) per step."""
+    recs, d = T._spring_scene(model)
+    run_pair(recs, [d], 150, gravity=(0.0, 0.0, 0.0))
+    recs, d = T._spring_scene(model, stiffness=0.0, damping=4.0)
+
+    def push(arr):
+        arr["velocity"][1] = [0.0, -3.0, 0.0]
+    run_pair(recs, [d], 60, gravity=(0.0, 0.0, 0.0), setup=push)
+
+
 def test_fixed_distance_and_rope():
     floor = O.body_new(abi.SHAPE_BOX, [5, 1, 5], [0, -1, 0], 0.0)
     run_pair([floor, O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [-0.5, 3, 0], 1.0),
@@ -96,7 +124,8 @@ def test_sixdof_locked_free_and_limited():
 
 def zoo(x0):
     """Every joint kind in one scene with contacts: a slider-mounted arm,
-    a welded pair, a rod, a rope and a six-DOF pair falling onto a floor."""
+    a welded pair, a rod, a rope, a six-DOF pair, a free motor pushing
+    the rod's end and a spring, falling onto a floor."""
     rec = [O.body_new(abi.SHAPE_BOX, [6, 0.5, 6], [x0, -0.5, 0], 0.0),
            O.body_new(abi.SHAPE_BOX, [0.2, 0.2, 0.2], [x0, 4, 0], 0.0)]
     for k, (shape, p) in enumerate([(abi.SHAPE_BOX, [0.3, 0.3, 0.3]), (abi.SHAPE_SPHERE, [0.3]),
@@ -112,7 +141,11 @@ def zoo(x0):
           abi.joint_desc(abi.JOINT_DISTANCE, 5, 6, [0, 0, 0], [0, 0, 0]),
           abi.joint_desc(abi.JOINT_ROPE, 1, 7, [0, 0, 0], [0, 0, 0], max_distance=3.0),
           abi.joint_desc(abi.JOINT_SIXDOF, 8, 9, [0, 0, 0], [0, 0, 0],
-                         axes=["locked", (-0.2, 0.3), "free", "locked", (-0.4, 0.4), "locked"])]
+                         axes=["locked", (-0.2, 0.3), "free", "locked", (-0.4, 0.4), "locked"]),
+          abi.joint_desc(abi.JOINT_MOTOR, 1, 6, [0, 0, 0], [0, 0, 0],
+                         drive=((0.5, 0.0, 0.0), (0.0, 1.0, 0.0), 3.0, 0.5, 0.2)),
+          abi.joint_desc(abi.JOINT_SPRING, 3, 9, [0.2, 0, 0], [0, 0.2, 0],
+                         spring=(1.2, 0.0, 40.0, 3.0, 1e4, abi.MOTOR_POSITION, abi.MODEL_ACCELERATION))]
     return rec, js
 
 
@@ -157,7 +190,10 @@ def test_admission_errors_equal_the_oracle():
              abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [0, 0, 0], [0, 0, 0], [0, 0, 0], [1, 0, 0]),
              abi.joint_desc(abi.JOINT_ROPE, 0, 1, [0, 0, 0], [0, 0, 0], max_distance=0.0),
              abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0], axes=["locked"] * 5 + [(0.3, -0.3)]),
-             abi.joint_desc(abi.JOINT_FIXED, 0, 0, [0, 0, 0], [0, 0, 0])]
+             abi.joint_desc(abi.JOINT_FIXED, 0, 0, [0, 0, 0], [0, 0, 0]),
+             abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((nan, 0, 0), (0, 0, 0), 1, 1, 0)),
+             abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), -1, 1, 0)),
+             abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), 1, 1, 2))]
     o = O.OracleWorld()
     o.add_bodies(O.bodies_to_array(recs))
     g = AvbdWorld(abi.default_params(), bodies=O.bodies_to_array(recs))

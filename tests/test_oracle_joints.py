@@ -2,12 +2,15 @@
 behavioural gates (crates/physics/tests/avbd_engine.rs) restated — hinge
 motor (:552-596), prismatic slider on its line and at its limit (:598-646),
 prismatic motor (:782-822), fixed weld (:891-938), distance rod (:940-968),
-six-DOF all locked / free axis / angular limit (:1452-1556) — plus a rope
-that never exceeds its length, and the admission errors of validate_joint
-(migration.rs:160-330).  Reference order, dt 1/60, 10 iterations."""
+six-DOF all locked / free axis / angular limit (:1452-1556), the free motor
+(crates/physics/tests/motor_joint.rs:90-110), the spring oscillator
+(p6_rope_spring_motor.rs:193-216) — plus a rope that never
+exceeds its length, the free motor's angular drive and budget, and the
+admission errors of validate_joint (migration.rs:160-356).  Reference order, dt 1/60, 10 iterations."""
 import math
 
 import numpy as np
+import pytest
 
 from ornis_gb300 import abi
 
@@ -144,6 +147,107 @@ def test_sixdof_angular_limit_blocks_spin():
     assert abs(z_twist(w.bodies()["orientation"][1])) < 0.4
 
 
+def _motor_scene():
+    """A box resting on a static floor box, driven along +x by a free motor
+    from a static anchor above (motor_joint.rs:38-57, :90-110)."""
+    floor = O.body_new(abi.SHAPE_BOX, [10.0, 0.5, 10.0], [0, -0.5, 0], 0.0)
+    block = O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0.5, 0], 1.0)
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 5, 0], 0.0)
+    drive = abi.joint_desc(abi.JOINT_MOTOR, 2, 1, [0, 0, 0], [0, 0, 0],
+                           drive=((2.0, 0.0, 0.0), (0.0, 0.0, 0.0), 8.0, 10.0, 0.0))
+    return [floor, block, anchor], drive
+
+
+def test_free_motor_drives_box_against_friction():
+    # avbd_motor_drives_box_to_target_against_friction (motor_joint.rs:90-110)
+    recs, drive = _motor_scene()
+    w = world(recs)
+    add(w, drive)
+    for _ in range(300):
+        w.step(DT)
+    v = w.bodies()["velocity"][1]
+    assert abs(v[0] - 2.0) < 0.4, v
+
+
+def test_free_motor_spins_to_angular_target_within_budget():
+    """No gravity: the angular drive reaches its target, and a starved
+    budget changes the rate by at most max_torque dt through the body's
+    inverse inertia per step."""
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 5, 0], 0.0)
+    ball = O.body_new(abi.SHAPE_SPHERE, [0.5], [0, 0, 0], 1.0)
+    w = world([anchor, ball], gravity=(0.0, 0.0, 0.0))
+    add(w, abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0],
+                          drive=((0.0, 0.0, 0.0), (0.0, 3.0, 0.0), 0.0, 50.0, 0.0)))
+    for _ in range(30):
+        w.step(DT)
+    assert abs(w.bodies()["angular_velocity"][1][1] - 3.0) < 1e-3
+    w2 = world([anchor, ball], gravity=(0.0, 0.0, 0.0))
+    add(w2, abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0],
+                           drive=((0.0, 0.0, 0.0), (0.0, 3.0, 0.0), 0.0, 0.01, 0.0)))
+    w2.step(DT)
+    inertia = 0.4 * 1.0 * 0.5 ** 2  # solid sphere
+    assert 0.0 < w2.bodies()["angular_velocity"][1][1] <= 0.01 * DT / inertia * 1.001
+
+
+def test_free_motor_bodies_do_not_collide():
+    # rows.rs:434-474: the free motor is on the no-collide list
+    a = O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0.5, 0], 1.0)
+    b = O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0.3, 0.5, 0], 1.0)
+    w = world([a, b], gravity=(0.0, 0.0, 0.0))
+    add(w, abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0],
+                          drive=((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), 1.0, 1.0, 0.3)))
+    w.step(DT)
+    assert w.counters().pairs == 0
+
+
+def _spring_scene(model=abi.MODEL_ACCELERATION, stiffness=30.0, damping=6.0):
+    """A ball on a spring stretched to 2.5 times its rest length from a static
+    anchor, zero gravity (p6_rope_spring_motor.rs:120-160, :193-216)."""
+    anchor = O.body_new(abi.SHAPE_SPHERE, [0.1], [0, 0, 0], 0.0)
+    bob = O.body_new(abi.SHAPE_SPHERE, [0.2], [0, -2.5, 0], 1.0)
+    d = abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0.5, 0],
+                       spring=(1.0, 0.0, stiffness, damping, 1e6, abi.MOTOR_POSITION, model))
+    return [anchor, bob], d
+
+
+def spring_length(w):
+    b = w.bodies()
+    q = b["orientation"][1]
+    qv, qw = q[:3].astype(np.float64), float(q[3])
+    lb = np.array([0.0, 0.5, 0.0])
+    rot = lb + 2.0 * qw * np.cross(qv, lb) + 2.0 * np.cross(qv, np.cross(qv, lb))
+    return float(np.linalg.norm(b["position"][1] + rot - b["position"][0]))
+
+
+@pytest.mark.parametrize("model", [abi.MODEL_ACCELERATION, abi.MODEL_FORCE])
+def test_spring_oscillator_settles_at_rest_length(model):
+    # avbd_spring_oscillator_settles_at_rest_length (p6_rope_spring_motor.rs:193-216)
+    recs, d = _spring_scene(model)
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    add(w, d)
+    lengths = []
+    for _ in range(600):
+        w.step(DT)
+        lengths.append(spring_length(w))
+    assert abs(lengths[-1] - 1.0) < 0.1, lengths[-1]
+    assert np.linalg.norm(w.bodies()["velocity"][1]) < 0.4
+    assert min(lengths) < 1.2  # it oscillated through its rest length
+
+
+def test_spring_damper_only_slows_without_centering():
+    recs, d = _spring_scene(stiffness=0.0, damping=4.0)
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    b = w.bodies()
+    b["velocity"][1] = [0.0, -3.0, 0.0]
+    w.set_bodies(b)
+    add(w, d)
+    for _ in range(120):
+        w.step(DT)
+    v = np.linalg.norm(w.bodies()["velocity"][1])
+    assert 0.0 < v < 1.5
+    assert spring_length(w) > 2.0  # no rest-length pull
+
+
 def test_joint_admission_errors():
     w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
                O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [2, 0, 0], 1.0)])
@@ -160,6 +264,31 @@ def test_joint_admission_errors():
         (abi.joint_desc(abi.JOINT_SIXDOF, 0, 1, [0, 0, 0], [0, 0, 0], axes=["locked"] * 5 + [(0.3, -0.3)]),
          abi.AVBD_ERR_JOINT_BAD_BOUNDS),
     ]
+    inf = float("inf")
+    cases += [
+        (abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((nan, 0, 0), (0, 0, 0), 1.0, 1.0, 0.0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), -1.0, 1.0, 0.0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), 1.0, inf, 0.0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), 1.0, 1.0, 1.5)),
+         abi.AVBD_ERR_JOINT_BAD_BOUNDS),
+    ]
+    P = abi.MOTOR_POSITION
+    cases += [
+        (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(nan, 0, 1, 1, 1, P, 0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(1, 0, -1, 1, 1, P, 0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(1, 0, 1, inf, 1, P, 0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(1, 0, 1, 1, -2, P, 0)),
+         abi.AVBD_ERR_JOINT_NONFINITE),
+    ]
     for d, code in cases:
         assert w.add_joint(d)[0] == code
+    # a free motor has no anchors: they are not checked
+    assert w.add_joint(abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [nan, 0, 0], [0, 0, 0],
+                                      drive=((0, 0, 0), (0, 0, 0), 1.0, 1.0, 0.3)))[0] == 0
     assert w.add_joint(abi.joint_desc(abi.JOINT_FIXED, 0, 1, [0, 0, 0], [0, 0, 0]))[0] == 0
