@@ -74,6 +74,7 @@ extern "C" {
 #define AVBD_JOINT_SIXDOF 6    /* JointKind::SixDof    (axis_config per axis)        */
 #define AVBD_JOINT_MOTOR 7     /* JointKind::Motor     (free velocity drive, no rows) */
 #define AVBD_JOINT_SPRING 8    /* JointKind::Spring    (spring-damper along the anchors) */
+#define AVBD_JOINT_WHEEL 9     /* JointKind::Wheel     (suspension slide + axle spin)    */
 
 /* JointMotor of a spring (joint.rs:951-996) */
 #define AVBD_MOTOR_VELOCITY 0  /* MotorKind::Velocity */
@@ -152,6 +153,14 @@ typedef struct AvbdJointDesc {
     float spring_max_force;
     uint32_t spring_kind;
     uint32_t spring_model;
+    /* wheel (JointKind::Wheel): local_axis_a/b are the suspension axes;
+     * the spin axles, and the suspension's frequency (Hz; 0 = rigid) and
+     * damping ratio (WheelSuspension); the axle motor is has_motor /
+     * motor_speed / motor_max */
+    float local_axle_a[3];
+    float local_axle_b[3];
+    float suspension_hz;
+    float suspension_damping;
 } AvbdJointDesc;
 
 /* Solver parameters.  avbd_default_params() fills the reference's constants
@@ -310,9 +319,14 @@ int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
  * AVBD_ERR_JOINT_BAD_BOUNDS (its anchors are not used).  A spring's motor
  * (validate_motor, migration.rs:366-394): non-finite targets, a negative or
  * non-finite stiffness, damping or budget -> AVBD_ERR_JOINT_NONFINITE.
+ * A wheel: non-finite suspension or axle axes -> AVBD_ERR_JOINT_BAD_AXIS, a
+ * negative or non-finite frequency or damping ratio ->
+ * AVBD_ERR_JOINT_NONFINITE, a degenerate suspension axis ->
+ * AVBD_ERR_JOINT_BAD_AXIS.
  * Kinds: Ball, Revolute (limit, velocity motor), Prismatic (limit, velocity
  * motor), Fixed, Distance, Rope, SixDof, Motor (free velocity drive),
- * Spring; Wheel and Gear joints -> AVBD_ERR_UNSUPPORTED. */
+ * Spring, Wheel (velocity motor about the axle); Gear joints ->
+ * AVBD_ERR_UNSUPPORTED. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 
 /* PhysicsEngine::remove_joint (engine.rs, avbd/mod.rs:1531-1540): both

@@ -79,6 +79,7 @@ struct K {
     static constexpr float CONTACT_BEGIN_SLOP = 0.005f;    // trigger.rs:68
     static constexpr float CONTACT_HIT_THRESHOLD = 1.0f;   // trigger.rs:63
     static constexpr float DEGENERATE_LEN2 = 1e-12f;
+    static constexpr float POS_CORRECTION_EPS = 1e-6f;  // constants.rs:71
     static constexpr float NEAR_ZERO = 1e-9f;
     static constexpr float SHAPE_TOUCH = 1e-3f;
     static constexpr float AXIS_REST_LEN2 = 1e-16f;
@@ -601,6 +602,9 @@ template <class T> struct Joint {  // AvbdJoint (avbd/mod.rs:327-402)
     // spring (JointKind::Spring): its JointMotor
     T spr_vel, spr_k, spr_c, spr_max;
     uint32_t spr_kind, spr_model;
+    // wheel (JointKind::Wheel): spin axles, suspension frequency and damping ratio
+    V3<T> bx_a, bx_b;
+    T susp_hz, susp_zeta;
     T lam_l[3], lam_a[3], pen_l[3], pen_a[3];
 };
 
@@ -611,6 +615,12 @@ template <class T> static V3<T> tangent_t1(V3<T> n) {  // math.rs:152-160
 template <class T> static void tangent_basis(V3<T> n, V3<T>& t1, V3<T>& t2) {
     t1 = tangent_t1(n);
     t2 = cross(t1, n);
+}
+// math.rs:179-186: the axle made orthogonal to the suspension axis
+template <class T> static V3<T> orthogonalize_axle(V3<T> s, V3<T> axle) {
+    V3<T> a = axle - s * dot(axle, s);
+    if (len2(a) < C<T>(K::POS_CORRECTION_EPS)) return tangent_t1(s);
+    return normalize(a);
 }
 
 // avbd/rows.rs helpers
@@ -883,14 +893,18 @@ template <class T> struct Engine {
             case AVBD_JOINT_DISTANCE:
             case AVBD_JOINT_SPRING: return std::fabs(len(delta) - j.ref_val);  // a spring: about its rest
             case AVBD_JOINT_ROPE: return fmx(len(delta) - j.ref_val, T(0));
-            case AVBD_JOINT_PRISMATIC: {
+            case AVBD_JOINT_PRISMATIC:
+            case AVBD_JOINT_WHEEL: {
                 V3<T> perp = delta - axis * dot(delta, axis);
                 T e = len(perp);
                 if (j.has_lim) {
                     T value = dot(delta, axis) - j.ref_val;
                     e = fmx(e, fmx(j.lo - value, value - j.hi));
                 }
-                return fmx(e, len(axis - qrot(b.rot, j.ax_b)));
+                if (j.kind == AVBD_JOINT_PRISMATIC) return fmx(e, len(axis - qrot(b.rot, j.ax_b)));
+                e = fmx(e, len(qrot(a.rot, j.bx_a) - qrot(b.rot, j.bx_b)));
+                if (j.susp_hz <= T(0)) e = fmx(e, std::fabs(dot(delta, axis) - j.ref_val));
+                return e;
             }
             default: {  // sixdof (sleep.rs:86-103)
                 V3<T> lin = qrot(conj(a.rot), delta) - j.dref;
@@ -995,6 +1009,15 @@ template <class T> struct Engine {
                 T dj = velocity_impulse(j.mot_speed - v, k, j.mot_max);
                 if (solvable(j.a)) a.vel = a.vel + (-dj) * ka * wa;
                 if (solvable(j.b)) b.vel = b.vel + dj * kb * wa;
+            } else if (j.kind == AVBD_JOINT_WHEEL) {  // spin about the axle (joints_ext.rs:337-371)
+                V3<T> xa = normalize_or(qrot(a.rot, j.bx_a), VZ<T>());
+                T w = dot(b.angvel - a.angvel, xa);
+                V3<T> ia = ang_inv_wa(j.a, xa), ib = ang_inv_wa(j.b, xa);
+                T k = dot(ia, xa) + dot(ib, xa);
+                if (k < C<T>(K::MIN_EFFECTIVE_MASS)) continue;
+                T dj = velocity_impulse(j.mot_speed - w, k, j.mot_max);
+                if (solvable(j.a)) a.angvel = a.angvel + (-dj) * ia;
+                if (solvable(j.b)) b.angvel = b.angvel + dj * ib;
             }
         }
     }
@@ -1128,7 +1151,8 @@ template <class T> struct Engine {
     // Fixed and SixDof joints (their contact is structural)
     static bool no_collide_kind(uint32_t k) {
         return k == AVBD_JOINT_BALL || k == AVBD_JOINT_REVOLUTE || k == AVBD_JOINT_PRISMATIC ||
-               k == AVBD_JOINT_DISTANCE || k == AVBD_JOINT_ROPE || k == AVBD_JOINT_MOTOR || k == AVBD_JOINT_SPRING;
+               k == AVBD_JOINT_DISTANCE || k == AVBD_JOINT_ROPE || k == AVBD_JOINT_MOTOR || k == AVBD_JOINT_SPRING ||
+               k == AVBD_JOINT_WHEEL;
     }
 
     bool discover_pair(uint32_t ia, uint32_t ib, Discovered& out) const {
@@ -1601,6 +1625,38 @@ template <class T> struct Engine {
                     fl = dir * f;
                 }
             }
+        } else if (j.kind == AVBD_JOINT_WHEEL) {
+            // two rows across the suspension axis and the suspension spring
+            // along it (assembly.rs:521-581); a zero frequency makes the
+            // spring a rigid row on slot 2
+            V3<T> u, v;
+            tangent_basis(wa, u, v);
+            V3<T> axs[2] = {u, v};
+            for (int li = 0; li < 2; li++) {
+                T c = dot(live - C<T>(K::ALPHA) * c0v, axs[li]);
+                T f = j.pen_l[li] * c + j.lam_l[li];
+                if (!row_live(c, f)) continue;
+                stamp_row(lhs, rhs, axs[li], j.pen_l[li], f, r_plain, sign);
+                fl = fl + axs[li] * f;
+            }
+            T sv = dot(pb - pa, wa) - j.ref_val;
+            V3<T> wa0 = normalize_or(qrot(rot0[j.a], j.ax_a), VZ<T>());
+            if (j.susp_hz > T(0)) {
+                T ka = eff_inv_mass(a), kb = eff_inv_mass(b);
+                T m = ka + kb > C<T>(K::NEAR_ZERO) ? T(1) / (ka + kb) : T(0);
+                if (m > T(0)) {
+                    T omega = C<T>(K::TAU) * j.susp_hz;
+                    T stiff = m * omega * omega;
+                    T dampc = T(2) * m * j.susp_zeta * omega;
+                    T s0 = dot(pb0 - pa0, wa0) - j.ref_val;
+                    T f = stiff * sv + dampc * (sv - s0) / dt;
+                    stamp_row(lhs, rhs, wa, stiff, f, r_plain, lsign);
+                }
+            } else {
+                T c = sv - C<T>(K::ALPHA) * (dot(pb0 - pa0, wa0) - j.ref_val);
+                T f = j.pen_l[2] * c + j.lam_l[2];
+                if (row_live(c, f)) stamp_row(lhs, rhs, wa, j.pen_l[2], f, r_plain, lsign);
+            }
         } else if (j.kind == AVBD_JOINT_SPRING) {
             // position-level spring about the rest length (assembly.rs:363-425):
             // penalty from the stiffness, damping from the step delta, no dual
@@ -1664,10 +1720,12 @@ template <class T> struct Engine {
                      len(V3<T>{hm[0][2], hm[1][2], hm[2][2]})};
             lhs[3][3] += hd.x; lhs[4][4] += hd.y; lhs[5][5] += hd.z;
         }
-        // angular rows (assembly.rs:634-806)
-        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC) {
-            V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
-            V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
+        // angular rows (assembly.rs:634-806); a wheel's pair keys on its axle
+        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC || j.kind == AVBD_JOINT_WHEEL) {
+            const bool wheel = j.kind == AVBD_JOINT_WHEEL;
+            const V3<T> hxa = wheel ? j.bx_a : j.ax_a, hxb = wheel ? j.bx_b : j.ax_b;
+            V3<T> axa = qrot(a.rot, hxa), axb = qrot(b.rot, hxb);
+            V3<T> axa0 = qrot(rot0[j.a], hxa), axb0 = qrot(rot0[j.b], hxb);
             V3<T> t1, t2;
             tangent_basis(axa0, t1, t2);
             V3<T> ts[2] = {t1, t2};
@@ -1891,6 +1949,29 @@ template <class T> struct Engine {
                     j.pen_l[li] = ramp(j.pen_l[li], c, K::BETA, K::PENALTY_MAX);
                 }
             }
+        } else if (j.kind == AVBD_JOINT_WHEEL) {
+            // the rows across the suspension axis, and the rigid suspension
+            // row when the frequency is zero (joints_ext.rs:738-764); a live
+            // spring carries no dual state
+            V3<T> wa = normalize_or(qrot(a.rot, j.ax_a), VZ<T>());
+            V3<T> u, v;
+            tangent_basis(wa, u, v);
+            V3<T> axs[2] = {u, v};
+            for (int li = 0; li < 2; li++) {
+                T c = dot(live - C<T>(K::ALPHA) * c0v, axs[li]);
+                if (std::fabs(c) >= eps) {
+                    j.lam_l[li] += j.pen_l[li] * c;
+                    j.pen_l[li] = ramp(j.pen_l[li], c, K::BETA, K::PENALTY_MAX);
+                }
+            }
+            if (j.susp_hz <= T(0)) {
+                V3<T> wa0 = normalize_or(qrot(rot0[j.a], j.ax_a), VZ<T>());
+                T c = (-dot(live, wa) - j.ref_val) - C<T>(K::ALPHA) * (-dot(pa0 - pb0, wa0) - j.ref_val);
+                if (std::fabs(c) >= eps) {
+                    j.lam_l[2] += j.pen_l[2] * c;
+                    j.pen_l[2] = ramp(j.pen_l[2], c, K::BETA, K::LIM_PEN_MAX);
+                }
+            }
         } else if (j.kind == AVBD_JOINT_DISTANCE) {
             T c = (len(live) - j.ref_val) - C<T>(K::ALPHA) * (len(c0v) - j.ref_val);
             if (std::fabs(c) >= eps) {
@@ -1966,10 +2047,12 @@ template <class T> struct Engine {
                 }
             }
         }
-        // angular equality rows
-        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC) {
-            V3<T> axa = qrot(a.rot, j.ax_a), axb = qrot(b.rot, j.ax_b);
-            V3<T> axa0 = qrot(rot0[j.a], j.ax_a), axb0 = qrot(rot0[j.b], j.ax_b);
+        // angular equality rows (a wheel's keyed on its axle, joints_ext.rs:789-803)
+        if (j.kind == AVBD_JOINT_REVOLUTE || j.kind == AVBD_JOINT_PRISMATIC || j.kind == AVBD_JOINT_WHEEL) {
+            const bool wheel = j.kind == AVBD_JOINT_WHEEL;
+            const V3<T> hxa = wheel ? j.bx_a : j.ax_a, hxb = wheel ? j.bx_b : j.ax_b;
+            V3<T> axa = qrot(a.rot, hxa), axb = qrot(b.rot, hxb);
+            V3<T> axa0 = qrot(rot0[j.a], hxa), axb0 = qrot(rot0[j.b], hxb);
             V3<T> t1, t2;
             tangent_basis(axa0, t1, t2);
             V3<T> ts[2] = {t1, t2};
@@ -2421,7 +2504,7 @@ template <class T> struct Engine {
         // validate_joint (migration.rs:160-330): anchors and axes finite, bounds ordered, motors finite
         auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
         auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-        if (d.kind > AVBD_JOINT_SPRING) return AVBD_ERR_UNSUPPORTED;
+        if (d.kind > AVBD_JOINT_WHEEL) return AVBD_ERR_UNSUPPORTED;
         if (d.kind != AVBD_JOINT_MOTOR && (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)))
             return AVBD_ERR_JOINT_BAD_AXIS;
         if (d.kind == AVBD_JOINT_MOTOR) {  // migration.rs:331-356
@@ -2435,6 +2518,15 @@ template <class T> struct Engine {
         if (axial) {
             if (!finite3(d.local_axis_a) || !finite3(d.local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
             if (d.has_limit && !bounds_ok(d.limit_min, d.limit_max)) return AVBD_ERR_JOINT_BAD_BOUNDS;
+            if (d.has_motor && !(std::isfinite(d.motor_speed) && std::isfinite(d.motor_max) && d.motor_max >= 0.0f))
+                return AVBD_ERR_JOINT_NONFINITE;
+        }
+        if (d.kind == AVBD_JOINT_WHEEL) {  // migration.rs:284-314
+            if (!finite3(d.local_axis_a) || !finite3(d.local_axis_b) || !finite3(d.local_axle_a) ||
+                !finite3(d.local_axle_b))
+                return AVBD_ERR_JOINT_BAD_AXIS;
+            if (!(std::isfinite(d.suspension_hz) && d.suspension_hz >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+            if (!(std::isfinite(d.suspension_damping) && d.suspension_damping >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
             if (d.has_motor && !(std::isfinite(d.motor_speed) && std::isfinite(d.motor_max) && d.motor_max >= 0.0f))
                 return AVBD_ERR_JOINT_NONFINITE;
         }
@@ -2488,6 +2580,25 @@ template <class T> struct Engine {
             j.has_mot = d.has_motor != 0;
             j.mot_speed = T(d.motor_speed);
             j.mot_max = T(d.motor_max);
+        } else if (d.kind == AVBD_JOINT_WHEEL) {  // joint.rs:1352-1379
+            V3<T> sa{T(d.local_axis_a[0]), T(d.local_axis_a[1]), T(d.local_axis_a[2])};
+            V3<T> sb{T(d.local_axis_b[0]), T(d.local_axis_b[1]), T(d.local_axis_b[2])};
+            if (len2(sa) < C<T>(K::DEGENERATE_LEN2) || len2(sb) < C<T>(K::DEGENERATE_LEN2)) return AVBD_ERR_JOINT_BAD_AXIS;
+            j.ax_a = normalize_or(sa, VY<T>());
+            j.ax_b = normalize_or(sb, VY<T>());
+            V3<T> xa{T(d.local_axle_a[0]), T(d.local_axle_a[1]), T(d.local_axle_a[2])};
+            V3<T> xb{T(d.local_axle_b[0]), T(d.local_axle_b[1]), T(d.local_axle_b[2])};
+            j.bx_a = orthogonalize_axle(j.ax_a, xa);
+            j.bx_b = orthogonalize_axle(j.ax_b, xb);
+            V3<T> wa = normalize_or(qrot(ba.rot, j.ax_a), VZ<T>());
+            V3<T> pa0 = ba.pos + qrot(ba.rot, j.la);
+            V3<T> pb0 = bb.pos + qrot(bb.rot, j.lb);
+            j.ref_val = dot(pb0 - pa0, wa);
+            j.has_mot = d.has_motor != 0;
+            j.mot_speed = T(d.motor_speed);
+            j.mot_max = T(d.motor_max);
+            j.susp_hz = T(d.suspension_hz);
+            j.susp_zeta = T(d.suspension_damping);
         } else if (d.kind == AVBD_JOINT_FIXED || d.kind == AVBD_JOINT_SIXDOF || d.kind == AVBD_JOINT_MOTOR) {
             // the assembly pose (a free motor's only for its rest residual)
             j.q_ref = qmul(conj(ba.rot), bb.rot);

@@ -48,6 +48,7 @@ JOINT_ROPE = 5
 JOINT_SIXDOF = 6
 JOINT_MOTOR = 7
 JOINT_SPRING = 8
+JOINT_WHEEL = 9
 MOTOR_VELOCITY, MOTOR_POSITION, MOTOR_SERVO = 0, 1, 2
 MODEL_ACCELERATION, MODEL_FORCE = 0, 1
 
@@ -119,6 +120,10 @@ class AvbdJointDesc(C.Structure):
         ("spring_max_force", C.c_float),
         ("spring_kind", C.c_uint32),
         ("spring_model", C.c_uint32),
+        ("local_axle_a", F3),
+        ("local_axle_b", F3),
+        ("suspension_hz", C.c_float),
+        ("suspension_damping", C.c_float),
     ]
 
 
@@ -256,13 +261,14 @@ def default_params(gravity=(0.0, -9.81, 0.0), step_dt=1.0 / 60.0, iterations=10,
 
 
 def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0),
-               limit=None, motor=None, max_distance=0.0, axes=None, drive=None, spring=None):
+               limit=None, motor=None, max_distance=0.0, axes=None, drive=None, spring=None, wheel=None):
     """A joint record.  limit = (min, max); motor = (target speed, max
     torque or force); axes (sixdof) = 6 entries, each "free", "locked" or
     (min, max), linear x y z then angular x y z; drive (free motor) =
     (linear target, angular target, max force, max torque, correction);
     spring = (rest, target velocity, stiffness, damping, max force, kind,
-    model)."""
+    model); wheel = (axle a, axle b, suspension Hz, damping ratio), axis_a/b
+    being the suspension axes."""
     d = AvbdJointDesc()
     d.kind = kind
     d.body_a = a
@@ -296,4 +302,9 @@ def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0
         d.spring_rest, d.spring_velocity, d.spring_stiffness = float(rest), float(vel), float(k)
         d.spring_damping, d.spring_max_force = float(c), float(fmax)
         d.spring_kind, d.spring_model = int(kind_), int(model)
+    if wheel is not None:
+        xa, xb, hz, zeta = wheel
+        d.local_axle_a[:] = list(map(float, xa))
+        d.local_axle_b[:] = list(map(float, xb))
+        d.suspension_hz, d.suspension_damping = float(hz), float(zeta)
     return d

@@ -162,6 +162,12 @@ static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j
         }
         return fmaxf(e, len(axis - qrot(qb, ld3(w.j_axb[j]))));
     }
+    if (kind == AVBD_JOINT_WHEEL) {  // sleep.rs:54-70: axles in the weld-reference slots
+        float e = len(delta - axis * dot(delta, axis));
+        e = fmaxf(e, len(qrot(qa, ld3(w.j_dref[j])) - qrot(qb, ld3(w.j_qref[j]))));
+        if (w.j_lim[j].x <= 0.0f) e = fmaxf(e, fabsf(dot(delta, axis) - refv));
+        return e;
+    }
     // sixdof (sleep.rs:86-103)
     V3 lin = qrot(conj(qa), delta) - ld3(w.j_dref[j]);
     V3 ang = quat_diff_vec(qmul(conj(qa), qb), ldq(w.j_qref[j]));

@@ -36,8 +36,13 @@
 // side (Ziv's test again, one level down).  The GB300's FP64 rate is a small
 // fraction of its FP32 rate, and the float stage settles almost every call of
 // the step; a rejected argument goes on to the double stage.
+//
+// The header also compiles as plain C++ (no CUDA compiler): the host
+// definitions alone.
 #pragma once
+#ifdef __CUDACC__
 #include <cuda_runtime.h>
+#endif
 #include <stdint.h>
 
 #include <cmath>
@@ -65,10 +70,15 @@ namespace crm {
 #define CRM_D2F(a) static_cast<float>(a)
 #define CRM_T(name) name##_h
 #endif
+#ifdef __CUDACC__
 #define CRM_HD __host__ __device__ __forceinline__
 #define CRM_TABLE(type, name, ...)                      \
     static __constant__ const type name##_d[] = __VA_ARGS__; \
     static const type name##_h[] = __VA_ARGS__;
+#else
+#define CRM_HD static inline
+#define CRM_TABLE(type, name, ...) static const type name##_h[] = __VA_ARGS__;
+#endif
 
 // bits 1..512 of 2/pi after the binary point
 CRM_TABLE(uint64_t, k_two_over_pi, {
@@ -462,7 +472,11 @@ CRM_HD int reduce_pio2(float ax, DD& r) {
 }
 // The double-double evaluations run about once in 2^24 arguments: kept out
 // of line so that the fast paths stay small.
+#ifdef __CUDACC__
 #define CRM_SLOW static __host__ __device__ __noinline__
+#else
+#define CRM_SLOW static __attribute__((noinline))
+#endif
 CRM_SLOW float sincos_slow(DD r, bool use_sin, double sgn) {
     DD zz = dd_mul(r, r);
     int n = terms(use_sin ? 0 : 1, z_class(zz.hi), true);

@@ -183,6 +183,15 @@ static __device__ void motor_impulse(const DW& w, uint32_t j) {  // joints_ext.r
         float dj = velocity_impulse(w, ref.z - om, k, ref.w);
         if (solvable(w, a)) w.angvel[a] = st3(ld3(w.angvel[a]) + (-dj) * ia, 0.0f);
         if (solvable(w, b)) w.angvel[b] = st3(ld3(w.angvel[b]) + dj * ib, 0.0f);
+    } else if (w.j_kind[j] == AVBD_JOINT_WHEEL) {  // spin about the axle (joints_ext.rs:337-371)
+        V3 xa = normalize_or(qrot(ldq(w.rot[a]), ld3(w.j_dref[j])), VZ());
+        float om = dot(ld3(w.angvel[b]) - ld3(w.angvel[a]), xa);
+        V3 ia = ang_inv_wa(w, a, xa), ib = ang_inv_wa(w, b, xa);
+        float k = dot(ia, xa) + dot(ib, xa);
+        if (k < MIN_EFFECTIVE_MASS) return;
+        float dj = velocity_impulse(w, ref.z - om, k, ref.w);
+        if (solvable(w, a)) w.angvel[a] = st3(ld3(w.angvel[a]) + (-dj) * ia, 0.0f);
+        if (solvable(w, b)) w.angvel[b] = st3(ld3(w.angvel[b]) + dj * ib, 0.0f);
     } else if (w.j_kind[j] == AVBD_JOINT_PRISMATIC) {
         float v = dot(ld3(w.vel[b]) - ld3(w.vel[a]), wa);
         float ka = eff_inv_mass(w, a), kb = eff_inv_mass(w, b);

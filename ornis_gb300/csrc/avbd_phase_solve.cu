@@ -121,7 +121,7 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
     const uint32_t kind = w.j_kind[j];
     const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
     const bool k_dist = ALL && (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE);
-    const bool k_spr = ALL && kind == AVBD_JOINT_SPRING;
+    const bool k_spr = ALL && kind == AVBD_JOINT_SPRING, k_whl = ALL && kind == AVBD_JOINT_WHEEL;
     bool is_a = ab.x == h;
     float sign = is_a ? 1.0f : -1.0f;
     float lsign = is_a ? -1.0f : 1.0f;  // rows measured B minus A flip the gradient
@@ -178,6 +178,37 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
                 stamp_row(s, dir, penl[0], f, r_plain, sign);
                 fl = dir * f;
             }
+        }
+    } else if (k_whl) {
+        // two rows across the suspension axis and the suspension spring
+        // along it (assembly.rs:521-581); a zero frequency makes the spring a
+        // rigid row on slot 2
+        V3 u = tangent_t1(wa);
+        V3 v = cross(u, wa);
+        V3 axs[2] = {u, v};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(live - ALPHA * c0v, axs[li]);
+            float f = penl[li] * cc + laml[li];
+            if (!row_live(cc, f)) continue;
+            stamp_row(s, axs[li], penl[li], f, r_plain, sign);
+            fl = fl + axs[li] * f;
+        }
+        const float4 susp = w.j_lim[j];  // frequency, damping ratio
+        const float sv = dot(pb - pa, wa) - ref.x;
+        const V3 wa0 = normalize_or(qrot(qa0, axa_l), VZ());
+        if (susp.x > 0.0f) {
+            const float ka = eff_inv_mass(w, ab.x), kb = eff_inv_mass(w, ab.y);
+            const float m = ka + kb > NEAR_ZERO ? 1.0f / (ka + kb) : 0.0f;
+            if (m > 0.0f) {
+                const float omega = TAU_F * susp.x;
+                const float stiff = m * omega * omega, dampc = 2.0f * m * susp.y * omega;
+                const float s0 = dot(pb0 - pa0, wa0) - ref.x;
+                stamp_row(s, wa, stiff, stiff * sv + dampc * (sv - s0) / w.dt, r_plain, lsign);
+            }
+        } else {
+            const float cc = sv - ALPHA * (dot(pb0 - pa0, wa0) - ref.x);
+            const float f = penl[2] * cc + laml[2];
+            if (row_live(cc, f)) stamp_row(s, wa, penl[2], f, r_plain, lsign);
         }
     } else if (k_spr) {
         // position-level spring about the rest length (assembly.rs:363-425):
@@ -248,10 +279,11 @@ static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint
         s.h[tri(4, 4)] += len(V3{hm[0][1], hm[1][1], hm[2][1]});
         s.h[tri(5, 5)] += len(V3{hm[0][2], hm[1][2], hm[2][2]});
     }
-    // angular rows
-    if (kind == AVBD_JOINT_REVOLUTE || k_pri) {
-        V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
-        V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
+    // angular rows (a wheel's pair keys on its axle, in the weld-reference slots)
+    if (kind == AVBD_JOINT_REVOLUTE || k_pri || k_whl) {
+        const V3 hxa = k_whl ? ld3(w.j_dref[j]) : axa_l, hxb = k_whl ? ld3(w.j_qref[j]) : axb_l;
+        V3 axa = qrot(qa, hxa), axb = qrot(qb, hxb);
+        V3 axa0 = qrot(qa0, hxa), axb0 = qrot(qb0, hxb);
         V3 t1 = tangent_t1(axa0);
         V3 t2 = cross(t1, axa0);
         V3 ts[2] = {t1, t2};
@@ -753,6 +785,29 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
                 penl[li] = ramp(penl[li], cc, BETA, PENALTY_MAX);
             }
         }
+    } else if (ALL && kind == AVBD_JOINT_WHEEL) {
+        // the rows across the suspension axis, and the rigid suspension row
+        // when the frequency is zero (joints_ext.rs:738-764); a live spring
+        // carries no dual state
+        V3 wa = normalize_or(qrot(qa, ld3(w.j_axa[j])), VZ());
+        V3 u = tangent_t1(wa);
+        V3 v = cross(u, wa);
+        V3 axs[2] = {u, v};
+        for (int li = 0; li < 2; li++) {
+            float cc = dot(live - ALPHA * c0v, axs[li]);
+            if (fabsf(cc) >= C_EPS) {
+                laml[li] += penl[li] * cc;
+                penl[li] = ramp(penl[li], cc, BETA, PENALTY_MAX);
+            }
+        }
+        if (w.j_lim[j].x <= 0.0f) {
+            V3 wa0 = normalize_or(qrot(qa0, ld3(w.j_axa[j])), VZ());
+            float cc = (-dot(live, wa) - ref.x) - ALPHA * (-dot(pa0 - pb0, wa0) - ref.x);
+            if (fabsf(cc) >= C_EPS) {
+                laml[2] += penl[2] * cc;
+                penl[2] = ramp(penl[2], cc, BETA, LIM_PEN_MAX);
+            }
+        }
     } else if (ALL && kind == AVBD_JOINT_DISTANCE) {
         float cc = (len(live) - ref.x) - ALPHA * (len(c0v) - ref.x);
         if (fabsf(cc) >= C_EPS) {
@@ -839,10 +894,10 @@ static __device__ void dual_joint(const DW& w, uint32_t j) {
         w.j_sacc[2 * (size_t)j] = make_float4(sacc[0], sacc[1], sacc[2], sacc[3]);
         w.j_sacc[2 * (size_t)j + 1] = make_float4(sacc[4], sacc[5], 0.0f, 0.0f);
     }
-    // angular equality rows
-    if (kind == AVBD_JOINT_REVOLUTE || k_pri) {
-        float4 axa4 = w.j_axa[j];
-        V3 axa_l = ld3(axa4), axb_l = ld3(w.j_axb[j]);
+    // angular equality rows (a wheel's keyed on its axle, joints_ext.rs:789-803)
+    if (kind == AVBD_JOINT_REVOLUTE || k_pri || (ALL && kind == AVBD_JOINT_WHEEL)) {
+        const bool whl = ALL && kind == AVBD_JOINT_WHEEL;
+        V3 axa_l = whl ? ld3(w.j_dref[j]) : ld3(w.j_axa[j]), axb_l = whl ? ld3(w.j_qref[j]) : ld3(w.j_axb[j]);
         V3 axa = qrot(qa, axa_l), axb = qrot(qb, axb_l);
         V3 axa0 = qrot(qa0, axa_l), axb0 = qrot(qb0, axb_l);
         V3 t1 = tangent_t1(axa0);

@@ -72,6 +72,12 @@ static __host__ __device__ __forceinline__ V3 tangent_t1(V3 n) {  // math.rs:152
     V3 axis = fabsf(n.x) < TANGENT_REF_AXIS_DOT ? VX() : VY();
     return normalize_or(cross(n, axis), VZ());
 }
+// math.rs:179-186: the wheel's axle made orthogonal to its suspension axis
+static __host__ __device__ __forceinline__ V3 orthogonalize_axle(V3 s, V3 axle) {
+    V3 a = axle - s * dot(axle, s);
+    if (len2(a) < POS_CORRECTION_EPS) return tangent_t1(s);
+    return normalize(a);
+}
 static __host__ __device__ __forceinline__ void world_inertia(V3 inertia, Q rot, float m[3][3]) {  // rows.rs:194-207
     V3 c[3];
     mat3_cols(rot, c);

@@ -18,6 +18,7 @@
 
 #include "avbd_crmath.cuh"
 #include "avbd_kernels.h"
+#include "avbd_rows.cuh"
 
 using namespace avbd;
 
@@ -36,6 +37,8 @@ struct JointRec {
     float mforce, mtorque;     // free motor budgets
     float spr[4];              // spring: stiffness, damping, max_force, target_velocity
     uint32_t spr_mode;         // spring: kind | model << 4
+    float bxa[3], bxb[3];      // wheel: spin axles
+    float susp[2];             // wheel: suspension frequency (Hz) and damping ratio
     uint32_t cfg;              // sixdof axis configuration, 2 bits per axis
     float six_min[6], six_max[6];
     AvbdJointState st;
@@ -658,6 +661,13 @@ static int upload_all(AvbdWorld* W) {
             // kind and model in the configuration word
             j_axb[i] = make_float4(j.spr[0], j.spr[1], j.spr[2], j.spr[3]);
             j_cfg[i] = j.spr_mode;
+        }
+        if (j.kind == AVBD_JOINT_WHEEL) {
+            // a wheel's axles ride in the weld-reference slots, its suspension
+            // in the limit slot (a wheel has no limit: has_limit stays 0)
+            j_dref[i] = make_float4(j.bxa[0], j.bxa[1], j.bxa[2], 0.0f);
+            j_qref[i] = make_float4(j.bxb[0], j.bxb[1], j.bxb[2], 0.0f);
+            j_lim[i] = make_float4(j.susp[0], j.susp[1], 0.0f, 0.0f);
         }
         j_lim[i] = make_float4(j.lo, j.hi, j.has_lim ? 1.0f : 0.0f, j.st.acc_lim);
         jll[i] = make_float4(j.st.lam_l[0], j.st.lam_l[1], j.st.lam_l[2], 0.0f);
@@ -1614,7 +1624,7 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     // ordered, motor fields finite, a rope longer than zero
     auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
     auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-    if (d->kind > AVBD_JOINT_SPRING) return AVBD_ERR_UNSUPPORTED;
+    if (d->kind > AVBD_JOINT_WHEEL) return AVBD_ERR_UNSUPPORTED;
     const bool motor = d->kind == AVBD_JOINT_MOTOR;
     // a free motor has no anchors (migration.rs:250-252); its drive is checked instead (:331-356)
     if (!motor && (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b))) return AVBD_ERR_JOINT_BAD_AXIS;
@@ -1629,6 +1639,15 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     if (axial) {
         if (!finite3(d->local_axis_a) || !finite3(d->local_axis_b)) return AVBD_ERR_JOINT_BAD_AXIS;
         if (d->has_limit && !bounds_ok(d->limit_min, d->limit_max)) return AVBD_ERR_JOINT_BAD_BOUNDS;
+        if (d->has_motor && !(std::isfinite(d->motor_speed) && std::isfinite(d->motor_max) && d->motor_max >= 0.0f))
+            return AVBD_ERR_JOINT_NONFINITE;
+    }
+    if (d->kind == AVBD_JOINT_WHEEL) {  // migration.rs:284-314
+        if (!finite3(d->local_axis_a) || !finite3(d->local_axis_b) || !finite3(d->local_axle_a) ||
+            !finite3(d->local_axle_b))
+            return AVBD_ERR_JOINT_BAD_AXIS;
+        if (!(std::isfinite(d->suspension_hz) && d->suspension_hz >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
+        if (!(std::isfinite(d->suspension_damping) && d->suspension_damping >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
         if (d->has_motor && !(std::isfinite(d->motor_speed) && std::isfinite(d->motor_max) && d->motor_max >= 0.0f))
             return AVBD_ERR_JOINT_NONFINITE;
     }
@@ -1699,6 +1718,26 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
             j.mot_speed = d->motor_speed;
             j.mot_max = d->motor_max;
         }
+    } else if (d->kind == AVBD_JOINT_WHEEL) {  // joint.rs:1352-1379
+        const float* sa = d->local_axis_a;
+        const float* sb = d->local_axis_b;
+        V3 va{sa[0], sa[1], sa[2]}, vb{sb[0], sb[1], sb[2]};
+        if (len2(va) < 1e-12f || len2(vb) < 1e-12f) return AVBD_ERR_JOINT_BAD_AXIS;
+        V3 na = normalize_or(va, VY()), nb = normalize_or(vb, VY());
+        j.axa[0] = na.x; j.axa[1] = na.y; j.axa[2] = na.z;
+        j.axb[0] = nb.x; j.axb[1] = nb.y; j.axb[2] = nb.z;
+        V3 axle_a = orthogonalize_axle(na, V3{d->local_axle_a[0], d->local_axle_a[1], d->local_axle_a[2]});
+        V3 axle_b = orthogonalize_axle(nb, V3{d->local_axle_b[0], d->local_axle_b[1], d->local_axle_b[2]});
+        j.bxa[0] = axle_a.x; j.bxa[1] = axle_a.y; j.bxa[2] = axle_a.z;
+        j.bxb[0] = axle_b.x; j.bxb[1] = axle_b.y; j.bxb[2] = axle_b.z;
+        V3 wa = normalize_or(qrot(qa, na), VZ());
+        j.refv = dot((xb + qrot(qb, lb)) - (xa + qrot(qa, la)), wa);
+        if (d->has_motor) {
+            j.mot_speed = d->motor_speed;
+            j.mot_max = d->motor_max;
+        }
+        j.susp[0] = d->suspension_hz;
+        j.susp[1] = d->suspension_damping;
     } else if (d->kind == AVBD_JOINT_FIXED || d->kind == AVBD_JOINT_SIXDOF || motor) {
         // the assembly pose (a free motor's only for its rest residual)
         Q r = qmul(conj(qa), qb);

@@ -48,6 +48,7 @@ constexpr float TANGENT_REF_AXIS_DOT = 0.9f;
 constexpr float JOINT_REST_ERROR = 0.005f;
 constexpr float PI_F = 3.14159265358979323846f;
 constexpr float TAU_F = 6.28318530717958647692f;
+constexpr float POS_CORRECTION_EPS = 1e-6f;  // constants.rs:71
 constexpr int MAX_PTS = AVBD_MAX_POINTS;
 constexpr int MAX_COLOURS = 64;
 constexpr int CCD_ROUNDS = 8;

@@ -1,6 +1,6 @@
 //! Raw declarations of `include/ornis_avbd.h`: `#[repr(C)]` mirrors of its
 //! records (same field order and sizes; `AvbdBody` is 136 bytes,
-//! `AvbdJointDesc` 224) and its
+//! `AvbdJointDesc` 256) and its
 //! `extern "C"` entry points.  Every function returns an `i32` status: 0 or a
 //! negative `AVBD_ERR_*` code.
 
@@ -41,6 +41,7 @@ pub const AVBD_JOINT_ROPE: u32 = 5;
 pub const AVBD_JOINT_SIXDOF: u32 = 6;
 pub const AVBD_JOINT_MOTOR: u32 = 7;
 pub const AVBD_JOINT_SPRING: u32 = 8;
+pub const AVBD_JOINT_WHEEL: u32 = 9;
 pub const AVBD_MOTOR_VELOCITY: u32 = 0;
 pub const AVBD_MOTOR_POSITION: u32 = 1;
 pub const AVBD_MOTOR_SERVO: u32 = 2;
@@ -117,6 +118,11 @@ pub struct AvbdJointDesc {
     pub spring_max_force: f32,
     pub spring_kind: u32,
     pub spring_model: u32,
+    /// wheel (`JointKind::Wheel`): spin axles and the suspension
+    pub local_axle_a: [f32; 3],
+    pub local_axle_b: [f32; 3],
+    pub suspension_hz: f32,
+    pub suspension_damping: f32,
 }
 
 #[repr(C)]

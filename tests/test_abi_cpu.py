@@ -47,7 +47,7 @@ def test_record_sizes():
     assert C.sizeof(abi.AvbdBody) == 136
     assert C.sizeof(abi.AvbdPointState) == 68
     assert abi.BODY_DTYPE.itemsize == 136
-    assert C.sizeof(abi.AvbdJointDesc) == 224
+    assert C.sizeof(abi.AvbdJointDesc) == 256
     assert C.sizeof(abi.AvbdJointState) == 80
 
 

@@ -4,7 +4,8 @@ motor (:552-596), prismatic slider on its line and at its limit (:598-646),
 prismatic motor (:782-822), fixed weld (:891-938), distance rod (:940-968),
 six-DOF all locked / free axis / angular limit (:1452-1556), the free motor
 (crates/physics/tests/motor_joint.rs:90-110), the spring oscillator
-(p6_rope_spring_motor.rs:193-216) — plus a rope that never
+(p6_rope_spring_motor.rs:193-216), the wheel's axle motor and suspension
+(avbd_engine.rs:969-1061) — plus a rope that never
 exceeds its length, the free motor's angular drive and budget, and the
 admission errors of validate_joint (migration.rs:160-356).  Reference order, dt 1/60, 10 iterations."""
 import math
@@ -248,6 +249,50 @@ def test_spring_damper_only_slows_without_centering():
     assert spring_length(w) > 2.0  # no rest-length pull
 
 
+def _wheel_motor_scene():
+    """A wheel spun about its z axle by a motor, zero gravity
+    (avbd_engine.rs:1020-1061)."""
+    anchor = O.body_new(abi.SHAPE_BOX, [0.2, 0.2, 0.2], [0, 0, 0], 0.0)
+    wheel = O.body_new(abi.SHAPE_BOX, [0.2, 0.2, 0.1], [0, -0.5, 0], 1.0)
+    d = abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0], motor=(6.0, 50.0),
+                       wheel=((0, 0, 1), (0, 0, 1), 2.0, 0.5))
+    return [anchor, wheel], d
+
+
+def _wheel_suspension_scene(hz=3.0):
+    """A 2 kg chassis sprung over a 1 kg wheel, both falling
+    (avbd_engine.rs:969-1017)."""
+    chassis = O.body_new(abi.SHAPE_BOX, [0.5, 0.2, 0.3], [0, 1, 0], 2.0)
+    wheel = O.body_new(abi.SHAPE_BOX, [0.25, 0.25, 0.15], [0, 0, 0], 1.0)
+    d = abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0],
+                       wheel=((0, 0, 1), (0, 0, 1), hz, 0.7))
+    return [chassis, wheel], d
+
+
+def test_wheel_motor_spins_axle():
+    recs, d = _wheel_motor_scene()
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    add(w, d)
+    for _ in range(240):
+        w.step(DT)
+    assert abs(w.bodies()["angular_velocity"][1][2] - 6.0) < 1.5
+
+
+@pytest.mark.parametrize("hz", [3.0, 0.0])
+def test_wheel_suspension_holds_chassis(hz):
+    # avbd_wheel_suspension_holds_chassis; a zero frequency is the rigid row
+    recs, d = _wheel_suspension_scene(hz)
+    w = world(recs)
+    add(w, d)
+    for _ in range(300):
+        w.step(DT)
+    p = w.bodies()["position"]
+    sep = p[0][1] - p[1][1]
+    assert 0.5 <= sep <= 1.1, sep
+    if hz == 0.0:
+        assert abs(sep - 1.0) < 0.05, sep
+
+
 def test_joint_admission_errors():
     w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
                O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [2, 0, 0], 1.0)])
@@ -285,6 +330,21 @@ def test_joint_admission_errors():
          abi.AVBD_ERR_JOINT_NONFINITE),
         (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(1, 0, 1, 1, -2, P, 0)),
          abi.AVBD_ERR_JOINT_NONFINITE),
+    ]
+    Wz = ((0, 0, 1), (0, 0, 1), 2.0, 0.5)
+    cases += [
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, nan, 0], [0, 1, 0], wheel=Wz),
+         abi.AVBD_ERR_JOINT_BAD_AXIS),
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0],
+                        wheel=((0, 0, inf), (0, 0, 1), 2.0, 0.5)), abi.AVBD_ERR_JOINT_BAD_AXIS),
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0],
+                        wheel=((0, 0, 1), (0, 0, 1), -1.0, 0.5)), abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0],
+                        wheel=((0, 0, 1), (0, 0, 1), 2.0, nan)), abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 0], motor=(1.0, -1.0),
+                        wheel=Wz), abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, 0, 0], [0, 1, 0], wheel=Wz),
+         abi.AVBD_ERR_JOINT_BAD_AXIS),
     ]
     for d, code in cases:
         assert w.add_joint(d)[0] == code
