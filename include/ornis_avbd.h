@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define AVBD_ABI_VERSION 3
+#define AVBD_ABI_VERSION 4
 
 /* ---- status codes ------------------------------------------------------ */
 #define AVBD_OK 0
@@ -42,12 +42,17 @@ extern "C" {
 #define AVBD_ERR_TIMEOUT (-4)        /* a bounded device wait gave up          */
 #define AVBD_ERR_NONFINITE (-5)      /* NaN/Inf in an input body               */
 #define AVBD_ERR_UNSUPPORTED (-6)    /* shape / joint kind not implemented     */
+#define AVBD_ERR_FORMAT (-7)         /* not a snapshot of this format version,
+                                        or a damaged one                       */
+#define AVBD_ERR_IO (-8)             /* a snapshot file could not be read or
+                                        written                                */
 /* joint admission errors, mirroring JointError (avbd/mod.rs:1323-1328) */
 #define AVBD_ERR_JOINT_SELF (-10)    /* JointError::SelfJoint                  */
 #define AVBD_ERR_JOINT_HANDLES (-11) /* JointError::InvalidHandles             */
 #define AVBD_ERR_JOINT_BAD_AXIS (-12)/* JointError::BadAxis                    */
 #define AVBD_ERR_JOINT_NONFINITE (-13) /* JointError::NonFinite (motor fields)   */
 #define AVBD_ERR_JOINT_BAD_BOUNDS (-14)/* JointError::BadBounds (limits, rope)     */
+#define AVBD_ERR_JOINT_UNKNOWN_REF (-15)/* JointError::UnknownRef (a gear's joints) */
 
 /* ---- enums --------------------------------------------------------------- */
 /* Shape variants on the path (collision/shape.rs); shape_params meaning:     */
@@ -75,6 +80,7 @@ extern "C" {
 #define AVBD_JOINT_MOTOR 7     /* JointKind::Motor     (free velocity drive, no rows) */
 #define AVBD_JOINT_SPRING 8    /* JointKind::Spring    (spring-damper along the anchors) */
 #define AVBD_JOINT_WHEEL 9     /* JointKind::Wheel     (suspension slide + axle spin)    */
+#define AVBD_JOINT_GEAR 10     /* JointKind::Gear      (couples two revolute / prismatic joints) */
 
 /* JointMotor of a spring (joint.rs:951-996) */
 #define AVBD_MOTOR_VELOCITY 0  /* MotorKind::Velocity */
@@ -161,6 +167,14 @@ typedef struct AvbdJointDesc {
     float local_axle_b[3];
     float suspension_hz;
     float suspension_damping;
+    /* gear (JointKind::Gear): the handles of the two revolute or prismatic
+     * joints it couples and the ratio (coordinate_a + ratio * coordinate_b
+     * stays at its value at creation); body_a and body_b are the gear's own
+     * bodies (admission, support for sleep) and its anchors are not used */
+    uint32_t gear_joint_a;
+    uint32_t gear_joint_b;
+    float gear_ratio;
+    uint32_t reserved;
 } AvbdJointDesc;
 
 /* Solver parameters.  avbd_default_params() fills the reference's constants
@@ -219,6 +233,12 @@ typedef struct AvbdJointState {
     float acc_lim;   /* revolute limit accumulator */
     float lim_dual;  /* prismatic limit force */
     float sacc[6];   /* sixdof limited-axis forces: linear x y z, angular x y z */
+    /* gear: the coupled joints' coordinates at the last step start (raw and
+     * unwrapped across turns, gear_mem in avbd/mod.rs:377-383); gear_mem_set
+     * 0 until the gear's first step */
+    float gear_raw[2];
+    float gear_cont[2];
+    uint32_t gear_mem_set;
 } AvbdJointState;
 
 /* Per-step observability counters (the reference exposes sleeping_count(),
@@ -299,7 +319,8 @@ int avbd_world_add_hull(AvbdWorld* world, const float* verts, uint32_t nverts, c
 
 /* PhysicsEngine::remove_body (engine.rs:40-43, avbd/mod.rs:1241-1300): the
  * last body moves into the freed handle; pairs and joints of the removed
- * body are dropped, the others renumbered; trigger pairs of the removed body
+ * body are dropped (with the gears that couple those joints), the others
+ * renumbered; trigger pairs of the removed body
  * report Exited, touches and queued contact events are cleared, every
  * sleeping body wakes.  A pair whose two handles change order under the
  * renumbering is dropped at once: the reference keeps it until its next
@@ -322,17 +343,21 @@ int avbd_world_remove_body(AvbdWorld* world, uint32_t handle);
  * A wheel: non-finite suspension or axle axes -> AVBD_ERR_JOINT_BAD_AXIS, a
  * negative or non-finite frequency or damping ratio ->
  * AVBD_ERR_JOINT_NONFINITE, a degenerate suspension axis ->
- * AVBD_ERR_JOINT_BAD_AXIS.
+ * AVBD_ERR_JOINT_BAD_AXIS.  A gear (mod.rs:1329-1404): a non-finite ratio ->
+ * AVBD_ERR_JOINT_NONFINITE, then both bodies wake, then self / invalid
+ * handles, then a coupled joint that does not exist ->
+ * AVBD_ERR_JOINT_UNKNOWN_REF, one that is neither revolute nor prismatic ->
+ * AVBD_ERR_UNSUPPORTED.
  * Kinds: Ball, Revolute (limit, velocity motor), Prismatic (limit, velocity
  * motor), Fixed, Distance, Rope, SixDof, Motor (free velocity drive),
- * Spring, Wheel (velocity motor about the axle); Gear joints ->
- * AVBD_ERR_UNSUPPORTED. */
+ * Spring, Wheel (velocity motor about the axle), Gear. */
 int avbd_world_add_joint(AvbdWorld* world, const AvbdJointDesc* desc, uint32_t* handle);
 
 /* PhysicsEngine::remove_joint (engine.rs, avbd/mod.rs:1531-1540): both
- * bodies of the joint wake, the joint and its warm state go, and the handles
- * of later joints move down by one (the reference's Vec::retain).  An invalid
- * handle is a no-op. */
+ * bodies of the joint wake, the joint and its warm state go, gears that
+ * couple it go too, and the handles of later joints move down (the
+ * reference's retain_joints, mod.rs:766-784, joint_remap migration.rs:74-115).
+ * An invalid handle is a no-op. */
 int avbd_world_remove_joint(AvbdWorld* world, uint32_t handle);
 
 /* PhysicsEngine::wake_body (engine.rs:109, avbd/mod.rs:1599-1601): a sleeping
@@ -383,6 +408,59 @@ int avbd_world_import_state(AvbdWorld* world, const AvbdBody* bodies,
                             const AvbdBodyAux* aux, const AvbdPairState* pairs,
                             const AvbdPointState* points, uint32_t npairs,
                             const AvbdJointState* joints);
+
+/* ---- on-disk snapshot ------------------------------------------------------
+ * A versioned, bit-faithful capture of a whole world: parameters, scene
+ * offsets, bodies with their solver state (previous poses, sleep timers),
+ * contact pairs and points with their warm state, joints with their
+ * assembly references and warm state, convex hulls, the world's settings
+ * (launch tuning, precision, event period, joint stiffness, the fixed-step
+ * accumulator's remainder) and the event state: the previous touch set, the
+ * previous trigger overlap set, the drop counters and the undrained event
+ * queues.  A world made from a snapshot continues bit for bit as the saved
+ * world would have (the reference's WorldSnapshot makes the same promise
+ * for the sequential-impulse engine and refuses AVBD, snapshot.rs:1-60,
+ * :815-830; this closes that gap).
+ *
+ * Layout: a 128-byte header (magic "ORNAVBD\0", format version, the
+ * writer's ABI version, an endianness mark, the size of every record the
+ * payload holds, the counts, the total size and a 64-bit FNV-1a checksum of
+ * the payload) followed by the payload sections in a fixed order.  A reader
+ * refuses, with AVBD_ERR_FORMAT, any other format version, record size or
+ * endianness, a truncated or oversized buffer and a checksum mismatch —
+ * never a silent reinterpretation (the reference's VersionMismatch,
+ * snapshot.rs:815-830).  Queued events beyond the loaded world's queue
+ * capacity are refused the same way. */
+#define AVBD_SNAPSHOT_FORMAT 1
+
+typedef struct AvbdSnapshotInfo {
+    uint32_t format;          /* format version of the snapshot              */
+    uint32_t abi;             /* avbd_abi_version() of the writer            */
+    uint32_t nbodies, nscenes, npairs, njoints, nhulls;
+    uint32_t ntouch;          /* previous touch set: touching pairs          */
+    uint32_t ntrigger;        /* previous trigger overlap set                */
+    uint32_t ncontact_events; /* undrained contact events                    */
+    uint32_t ntrigger_events; /* undrained trigger events                    */
+    uint32_t reserved;
+    uint64_t bytes;           /* the whole snapshot, header included         */
+    uint64_t substeps;        /* substeps the saved world had taken          */
+} AvbdSnapshotInfo;
+
+/* Write the world's snapshot into buf.  *size receives the snapshot's size;
+ * buf may be NULL to ask for it (then nothing is written).  A non-NULL buf
+ * with cap < *size -> AVBD_ERR_CAPACITY, nothing written. */
+int avbd_world_snapshot(AvbdWorld* world, void* buf, uint64_t cap, uint64_t* size);
+
+/* A new world on `device` from a snapshot (the caller destroys it). */
+int avbd_world_from_snapshot(const void* buf, uint64_t size, int device, AvbdWorld** out);
+
+/* Validate a snapshot as a load would on the host (header, checksum and
+ * contents) and describe it; needs no GPU. */
+int avbd_snapshot_info(const void* buf, uint64_t size, AvbdSnapshotInfo* info);
+
+/* The same to and from a file (written whole, then renamed into place). */
+int avbd_world_save(AvbdWorld* world, const char* path);
+int avbd_world_load(const char* path, int device, AvbdWorld** out);
 
 /* Colour of every body in the last substep's primal sweep (-1 = not swept:
  * static, kinematic, asleep). */

@@ -605,7 +605,23 @@ template <class T> struct Joint {  // AvbdJoint (avbd/mod.rs:327-402)
     // wheel (JointKind::Wheel): spin axles, suspension frequency and damping ratio
     V3<T> bx_a, bx_b;
     T susp_hz, susp_zeta;
+    // gear (JointKind::Gear): the coupled joints, the ratio, and the
+    // coordinates at the last step start (gear_mem, avbd/mod.rs:373-383)
+    uint32_t gb[2];
+    T gratio;
+    bool gmem_set;
+    T graw[2], gcont[2];
     T lam_l[3], lam_a[3], pen_l[3], pen_a[3];
+};
+
+// One side of a gear (GearSide, avbd/mod.rs:304-317): the coupled joint's
+// bodies, whether it turns (revolute) or slides (prismatic), its live world
+// axis, the slide's anchor levers and its continuous coordinate.
+template <class T> struct GearSide {
+    uint32_t a, b;
+    bool angular;
+    V3<T> axis, ra, rb;
+    T coord;
 };
 
 template <class T> static V3<T> tangent_t1(V3<T> n) {  // math.rs:152-160
@@ -879,7 +895,74 @@ template <class T> struct Engine {
     }
 
     // ---- joints / sleep (avbd/sleep.rs) ----
+    // ---- gears (joints_ext.rs:34-160) ----
+    // A revolute joint's twist or a prismatic joint's slide from its assembly
+    // reference (joints_ext.rs:37-51).
+    T joint_coordinate(const Joint<T>& r) const {
+        const Body<T>& a = bodies[r.a];
+        const Body<T>& b = bodies[r.b];
+        if (r.kind == AVBD_JOINT_REVOLUTE) return hinge_twist(a.rot, b.rot, r.ax_a) - r.ref_val;
+        V3<T> wa = normalize_or(qrot(a.rot, r.ax_a), VZ<T>());
+        V3<T> pa = a.pos + qrot(a.rot, r.la);
+        V3<T> pb = b.pos + qrot(b.rot, r.lb);
+        return dot(pb - pa, wa) - r.ref_val;
+    }
+    // Once per step: the coupled joints' raw coordinates, and the continuous
+    // ones unwrapped across turns for hinges (joints_ext.rs:55-118).
+    void update_gear_mem() {
+        for (Joint<T>& g : joints) {
+            if (g.kind != AVBD_JOINT_GEAR) continue;
+            T raw[2];
+            bool ang[2];
+            for (int k = 0; k < 2; k++) {
+                const Joint<T>& r = joints[g.gb[k]];
+                raw[k] = joint_coordinate(r);
+                ang[k] = r.kind == AVBD_JOINT_REVOLUTE;
+            }
+            for (int k = 0; k < 2; k++) {
+                T cont = g.gmem_set && ang[k] ? g.gcont[k] + wrap_pi(raw[k] - g.graw[k]) : raw[k];
+                g.graw[k] = raw[k];
+                g.gcont[k] = cont;
+            }
+            g.gmem_set = true;
+        }
+    }
+    // The live sides of a gear (joints_ext.rs:120-160).
+    void gear_sides(const Joint<T>& g, GearSide<T> sd[2]) const {
+        for (int k = 0; k < 2; k++) {
+            const Joint<T>& r = joints[g.gb[k]];
+            const Body<T>& ba = bodies[r.a];
+            const Body<T>& bb = bodies[r.b];
+            T raw = joint_coordinate(r);
+            GearSide<T>& s = sd[k];
+            s.a = r.a;
+            s.b = r.b;
+            s.angular = r.kind == AVBD_JOINT_REVOLUTE;
+            s.axis = normalize_or(qrot(ba.rot, r.ax_a), VZ<T>());
+            s.ra = s.angular ? VZERO<T>() : qrot(ba.rot, r.la);
+            s.rb = s.angular ? VZERO<T>() : qrot(bb.rot, r.lb);
+            s.coord = g.gmem_set && s.angular ? g.gcont[k] + wrap_pi(raw - g.graw[k]) : raw;
+        }
+    }
+    T gear_error(const Joint<T>& g) const {  // C = coord_a + ratio coord_b - constant
+        GearSide<T> sd[2];
+        gear_sides(g, sd);
+        return sd[0].coord + g.gratio * sd[1].coord - g.ref_val;
+    }
+    // The bodies a joint holds (sleep.rs:9-16): a gear's are its coupled
+    // joints' bodies.
+    void joint_members(const Joint<T>& j, uint32_t m[4]) const {
+        if (j.kind == AVBD_JOINT_GEAR) {
+            const Joint<T>& x = joints[j.gb[0]];
+            const Joint<T>& y = joints[j.gb[1]];
+            m[0] = x.a; m[1] = x.b; m[2] = y.a; m[3] = y.b;
+        } else {
+            m[0] = j.a; m[1] = j.b; m[2] = j.a; m[3] = j.b;
+        }
+    }
+
     T joint_rest_error(const Joint<T>& j) const {  // sleep.rs:30-105
+        if (j.kind == AVBD_JOINT_GEAR) return std::fabs(gear_error(j));
         const Body<T>& a = bodies[j.a];
         const Body<T>& b = bodies[j.b];
         V3<T> delta = (b.pos + qrot(b.rot, j.lb)) - (a.pos + qrot(a.rot, j.la));
@@ -1067,7 +1150,8 @@ template <class T> struct Engine {
                                           (j.mot_torque > T(0) && (j.mot_ang.x != T(0) || j.mot_ang.y != T(0) ||
                                                                    j.mot_ang.z != T(0)))))
             return true;
-        uint32_t m[2] = {j.a, j.b};
+        uint32_t m[4];
+        joint_members(j, m);
         for (uint32_t h : m) {
             const Body<T>& b = bodies[h];
             if (b.type != AVBD_BODY_DYNAMIC && (b.pos != prev_pos[h] || b.rot != prev_rot[h])) return true;
@@ -1078,7 +1162,8 @@ template <class T> struct Engine {
         for (;;) {
             bool changed = false;
             for (const Joint<T>& j : joints) {
-                uint32_t mem[4] = {j.a, j.b, j.a, j.b};
+                uint32_t mem[4];
+                joint_members(j, mem);
                 bool any = false;
                 for (uint32_t h : mem)
                     if (bodies[h].type == AVBD_BODY_DYNAMIC && flags[h] == value) any = true;
@@ -1100,7 +1185,8 @@ template <class T> struct Engine {
         }
         for (const Joint<T>& j : joints) {
             if (joint_driven(j) || joint_rest_error(j) > C<T>(K::JOINT_REST_ERROR)) {
-                uint32_t mem[2] = {j.a, j.b};
+                uint32_t mem[4];
+                joint_members(j, mem);
                 for (uint32_t h : mem)
                     if (bodies[h].type == AVBD_BODY_DYNAMIC) awake[h] = 1;
             }
@@ -1112,7 +1198,11 @@ template <class T> struct Engine {
     std::vector<uint8_t> joint_sleep_ready() const {
         std::vector<uint8_t> ready(bodies.size(), 1);
         for (const Joint<T>& j : joints)
-            if (joint_driven(j) || joint_rest_error(j) > C<T>(K::JOINT_REST_ERROR)) { ready[j.a] = 0; ready[j.b] = 0; }
+            if (joint_driven(j) || joint_rest_error(j) > C<T>(K::JOINT_REST_ERROR)) {
+                uint32_t mem[4];
+                joint_members(j, mem);
+                for (uint32_t h : mem) ready[h] = 0;
+            }
         propagate_joint_flags(ready, 0);
         return ready;
     }
@@ -1573,7 +1663,34 @@ template <class T> struct Engine {
         }
     }
 
+    // A gear's rows on body h, one of its coupled joints' bodies
+    // (assembly.rs:426-454 slides, :650-682 hinges): the shared force on
+    // the position-level row C = coord_a + ratio coord_b - constant, with
+    // the slide sides first, then the hinge sides.
+    void stamp_gear_for(uint32_t h, const Joint<T>& j, T lhs[6][6], T rhs[6]) const {
+        GearSide<T> sd[2];
+        gear_sides(j, sd);
+        T c = sd[0].coord + j.gratio * sd[1].coord - j.ref_val;
+        T f = j.pen_l[0] * c + j.lam_l[0];
+        if (!row_live(c, f)) return;
+        const T coef[2] = {T(1), j.gratio};
+        for (int k = 0; k < 2; k++) {
+            const GearSide<T>& side = sd[k];
+            if (side.angular || (h != side.a && h != side.b)) continue;
+            T lsign = h == side.a ? T(-1) : T(1);
+            V3<T> r = h == side.a ? side.ra : side.rb;
+            stamp_row(lhs, rhs, side.axis, j.pen_l[0] * coef[k] * coef[k], f * coef[k], r, lsign);
+        }
+        for (int k = 0; k < 2; k++) {
+            const GearSide<T>& side = sd[k];
+            if (!side.angular || (h != side.a && h != side.b)) continue;
+            V3<T> g = h == side.a ? -side.axis : side.axis;
+            stamp_angular(lhs, rhs, g, j.pen_l[0] * coef[k] * coef[k], f * coef[k]);
+        }
+    }
+
     void stamp_joint_for(uint32_t h, const Joint<T>& j, T lhs[6][6], T rhs[6]) const {  // assembly.rs:255-881
+        if (j.kind == AVBD_JOINT_GEAR) return stamp_gear_for(h, j, lhs, rhs);
         bool is_a = j.a == h;
         T sign = is_a ? T(1) : T(-1);
         T lsign = is_a ? T(-1) : T(1);  // rows measured B minus A flip the gradient
@@ -1821,8 +1938,8 @@ template <class T> struct Engine {
         if (faithful_scan) {
             for (uint32_t pi = 0; pi < pairs.size(); pi++)
                 if (pairs[pi].a == h || pairs[pi].b == h) stamp_contacts_for(h, pi, lhs, rhs);
-            for (const Joint<T>& j : joints)
-                if (j.a == h || j.b == h) stamp_joint_for(h, j, lhs, rhs);
+            for (const Joint<T>& j : joints)  // gears stamp on their coupled joints' bodies
+                if (j.a == h || j.b == h || j.kind == AVBD_JOINT_GEAR) stamp_joint_for(h, j, lhs, rhs);
         } else if (split_sums) {
             for (uint32_t pi : adj_pairs[h]) {
                 T lp[6][6] = {};
@@ -1907,7 +2024,17 @@ template <class T> struct Engine {
                 }
             }
         }
-        for (Joint<T>& j : joints) dual_joint(j);
+        for (Joint<T>& j : joints)
+            if (j.kind != AVBD_JOINT_GEAR) dual_joint(j);
+        // gears after every other joint (joints_ext.rs:897-918), penalty
+        // capped like a limit's
+        for (Joint<T>& g : joints) {
+            if (g.kind != AVBD_JOINT_GEAR) continue;
+            T c = gear_error(g);
+            if (std::fabs(c) < C<T>(K::C_EPS)) continue;
+            g.lam_l[0] = g.lam_l[0] + g.pen_l[0] * c;
+            g.pen_l[0] = fmn(g.pen_l[0] + C<T>(K::BETA) * std::fabs(c), C<T>(K::LIM_PEN_MAX));
+        }
     }
 
     // joints_ext.rs:574-896: the joint rows' multipliers and penalties.
@@ -2120,8 +2247,17 @@ template <class T> struct Engine {
         auto solved = [&](uint32_t h) { return solvable(h) && !asleep[h]; };
         for (const Pair<T>& p : pairs)
             if (!p.points.empty() && solved(p.a) && solved(p.b)) { nb[p.a].push_back(p.b); nb[p.b].push_back(p.a); }
-        for (const Joint<T>& j : joints)
+        for (const Joint<T>& j : joints) {
+            if (j.kind == AVBD_JOINT_GEAR) {  // a gear couples its coupled joints' bodies
+                uint32_t m[4];
+                joint_members(j, m);
+                for (uint32_t x : m)
+                    for (uint32_t y : m)
+                        if (x != y && solved(x) && solved(y)) nb[x].push_back(y);
+                continue;
+            }
             if (solved(j.a) && solved(j.b)) { nb[j.a].push_back(j.b); nb[j.b].push_back(j.a); }
+        }
         std::vector<uint32_t> order;
         for (uint32_t h = 0; h < n; h++) {
             colour[h] = -1;
@@ -2155,6 +2291,13 @@ template <class T> struct Engine {
             if (pairs[pi].b != pairs[pi].a) adj_pairs[pairs[pi].b].push_back(pi);
         }
         for (uint32_t ji = 0; ji < joints.size(); ji++) {
+            if (joints[ji].kind == AVBD_JOINT_GEAR) {  // once on each of its coupled joints' bodies
+                uint32_t m[4];
+                joint_members(joints[ji], m);
+                for (uint32_t h : m)
+                    if (adj_joints[h].empty() || adj_joints[h].back() != ji) adj_joints[h].push_back(ji);
+                continue;
+            }
             adj_joints[joints[ji].a].push_back(ji);
             adj_joints[joints[ji].b].push_back(ji);
         }
@@ -2172,6 +2315,7 @@ template <class T> struct Engine {
             if (len(disp) <= C<T>(K::CCD_TRAVEL_GATE_FRACTION) * shape_min_dimension(bodies[h])) continue;
             std::vector<uint32_t> joined;
             for (const Joint<T>& j : joints) {
+                if (j.kind == AVBD_JOINT_GEAR) continue;  // a gear joins no bodies (mod.rs:903-906)
                 if (j.a == h) joined.push_back(j.b);
                 else if (j.b == h) joined.push_back(j.a);
             }
@@ -2308,6 +2452,7 @@ template <class T> struct Engine {
     void step_inner(bool emit = true) {
         ensure_scratch();
         wake_joint_motion();
+        update_gear_mem();
         uint32_t n = (uint32_t)bodies.size();
         ccd_ev.clear();
         for (uint32_t h = 0; h < n; h++) {
@@ -2451,6 +2596,34 @@ template <class T> struct Engine {
     // the freed slot; pairs and joints of the removed body go, the others are
     // renumbered; handle-keyed event state is cleared or remapped; every
     // sleeper wakes.
+    // retain_joints (mod.rs:766-784) with joint_remap (migration.rs:74-115):
+    // a gear whose coupled joint goes goes too; the survivors move down and
+    // gears follow their joints' new handles.
+    void retain_joints(std::vector<uint8_t> gone) {
+        for (bool changed = true; changed;) {
+            changed = false;
+            for (size_t i = 0; i < joints.size(); i++)
+                if (!gone[i] && joints[i].kind == AVBD_JOINT_GEAR && (gone[joints[i].gb[0]] || gone[joints[i].gb[1]])) {
+                    gone[i] = 1;
+                    changed = true;
+                }
+        }
+        std::vector<uint32_t> remap(joints.size(), 0);
+        uint32_t next = 0;
+        for (size_t i = 0; i < joints.size(); i++) remap[i] = gone[i] ? 0u : next++;
+        std::vector<Joint<T>> kept;
+        for (size_t i = 0; i < joints.size(); i++) {
+            if (gone[i]) continue;
+            Joint<T> j = joints[i];
+            if (j.kind == AVBD_JOINT_GEAR) {
+                j.gb[0] = remap[j.gb[0]];
+                j.gb[1] = remap[j.gb[1]];
+            }
+            kept.push_back(j);
+        }
+        joints.swap(kept);
+    }
+
     void remove_body(uint32_t hi) {
         if (hi >= bodies.size()) return;
         uint32_t last = (uint32_t)bodies.size() - 1;
@@ -2470,14 +2643,13 @@ template <class T> struct Engine {
             kept.push_back(std::move(p));
         }
         pairs.swap(kept);
-        std::vector<Joint<T>> kj;
+        std::vector<uint8_t> gone(joints.size(), 0);
+        for (size_t i = 0; i < joints.size(); i++) gone[i] = joints[i].a == hi || joints[i].b == hi;
+        retain_joints(gone);
         for (Joint<T>& j : joints) {
-            if (j.a == hi || j.b == hi) continue;
             j.a = map(j.a);
             j.b = map(j.b);
-            kj.push_back(j);
         }
-        joints.swap(kj);
         prev_touch.clear();
         std::set<Key> remapped;
         for (const Key& k : prev_trigger) {
@@ -2504,8 +2676,10 @@ template <class T> struct Engine {
         // validate_joint (migration.rs:160-330): anchors and axes finite, bounds ordered, motors finite
         auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
         auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-        if (d.kind > AVBD_JOINT_WHEEL) return AVBD_ERR_UNSUPPORTED;
-        if (d.kind != AVBD_JOINT_MOTOR && (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)))
+        if (d.kind > AVBD_JOINT_GEAR) return AVBD_ERR_UNSUPPORTED;
+        const bool gear = d.kind == AVBD_JOINT_GEAR;
+        if (gear && !std::isfinite(d.gear_ratio)) return AVBD_ERR_JOINT_NONFINITE;  // migration.rs:193-200
+        if (!gear && d.kind != AVBD_JOINT_MOTOR && (!finite3(d.local_anchor_a) || !finite3(d.local_anchor_b)))
             return AVBD_ERR_JOINT_BAD_AXIS;
         if (d.kind == AVBD_JOINT_MOTOR) {  // migration.rs:331-356
             if (!finite3(d.motor_linear) || !finite3(d.motor_angular)) return AVBD_ERR_JOINT_NONFINITE;
@@ -2550,6 +2724,29 @@ template <class T> struct Engine {
         if (d.body_a >= bodies.size() || d.body_b >= bodies.size()) return AVBD_ERR_JOINT_HANDLES;
         Joint<T> j{};
         j.a = d.body_a; j.b = d.body_b; j.kind = d.kind;
+        if (gear) {  // mod.rs:1329-1404: the coupled joints exist and are hinges or slides
+            if (d.gear_joint_a >= joints.size() || d.gear_joint_b >= joints.size()) return AVBD_ERR_JOINT_UNKNOWN_REF;
+            for (uint32_t r : {d.gear_joint_a, d.gear_joint_b})
+                if (joints[r].kind != AVBD_JOINT_REVOLUTE && joints[r].kind != AVBD_JOINT_PRISMATIC)
+                    return AVBD_ERR_UNSUPPORTED;
+            j.la = j.lb = VZERO<T>();
+            j.ax_a = j.ax_b = j.bx_a = j.bx_b = VX<T>();
+            j.q_ref = Qt<T>{T(0), T(0), T(0), T(1)};
+            j.dref = VZERO<T>();
+            j.gb[0] = d.gear_joint_a;
+            j.gb[1] = d.gear_joint_b;
+            j.gratio = T(d.gear_ratio);
+            j.ref_val = joint_coordinate(joints[j.gb[0]]) + j.gratio * joint_coordinate(joints[j.gb[1]]);
+            j.gmem_set = false;
+            for (int k = 0; k < 6; k++) j.sacc[k] = T(0);
+            for (int k = 0; k < 3; k++) {
+                j.lam_l[k] = j.lam_a[k] = T(0);
+                j.pen_l[k] = j.pen_a[k] = C<T>(K::JOINT_PENALTY_INIT);
+            }
+            joints.push_back(j);
+            handle = (uint32_t)(joints.size() - 1);
+            return AVBD_OK;
+        }
         j.la = {T(d.local_anchor_a[0]), T(d.local_anchor_a[1]), T(d.local_anchor_a[2])};
         j.lb = {T(d.local_anchor_b[0]), T(d.local_anchor_b[1]), T(d.local_anchor_b[2])};
         if (d.kind == AVBD_JOINT_MOTOR) j.la = j.lb = VZERO<T>();  // a free motor has no anchors
@@ -2798,7 +2995,9 @@ int oracle_remove_joint(OracleWorld* w, uint32_t handle) {
         if (handle < E.joints.size()) {
             E.wake_body(E.joints[handle].a);
             E.wake_body(E.joints[handle].b);
-            E.joints.erase(E.joints.begin() + handle);
+            std::vector<uint8_t> gone(E.joints.size(), 0);
+            gone[handle] = 1;
+            E.retain_joints(gone);
         }
     });
     return AVBD_OK;
@@ -3006,6 +3205,11 @@ int oracle_export_state(OracleWorld* w, AvbdBody* bodies, AvbdBodyAux* aux, Avbd
                 s.acc_lim = float(j.acc_lim);
                 s.lim_dual = float(j.lim_dual);
                 for (int c = 0; c < 6; c++) s.sacc[c] = float(j.sacc[c]);
+                for (int c = 0; c < 2; c++) {
+                    s.gear_raw[c] = j.kind == AVBD_JOINT_GEAR ? float(j.graw[c]) : 0.0f;
+                    s.gear_cont[c] = j.kind == AVBD_JOINT_GEAR ? float(j.gcont[c]) : 0.0f;
+                }
+                s.gear_mem_set = j.kind == AVBD_JOINT_GEAR && j.gmem_set ? 1u : 0u;
             }
     });
     return AVBD_OK;
@@ -3061,6 +3265,13 @@ int oracle_import_state(OracleWorld* w, const AvbdBody* bodies, const AvbdBodyAu
                 j.acc_lim = TT(joints[i].acc_lim);
                 j.lim_dual = TT(joints[i].lim_dual);
                 for (int c = 0; c < 6; c++) j.sacc[c] = TT(joints[i].sacc[c]);
+                if (j.kind == AVBD_JOINT_GEAR) {
+                    for (int c = 0; c < 2; c++) {
+                        j.graw[c] = TT(joints[i].gear_raw[c]);
+                        j.gcont[c] = TT(joints[i].gear_cont[c]);
+                    }
+                    j.gmem_set = joints[i].gear_mem_set != 0;
+                }
             }
     });
     return AVBD_OK;

@@ -14,11 +14,14 @@ AVBD_ERR_DEVICE = -3
 AVBD_ERR_TIMEOUT = -4
 AVBD_ERR_NONFINITE = -5
 AVBD_ERR_UNSUPPORTED = -6
+AVBD_ERR_FORMAT = -7
+AVBD_ERR_IO = -8
 AVBD_ERR_JOINT_SELF = -10
 AVBD_ERR_JOINT_HANDLES = -11
 AVBD_ERR_JOINT_BAD_AXIS = -12
 AVBD_ERR_JOINT_NONFINITE = -13
 AVBD_ERR_JOINT_BAD_BOUNDS = -14
+AVBD_ERR_JOINT_UNKNOWN_REF = -15
 
 # limits of the allocation-free entry point (avbd_scene_step_static)
 STATIC_MAX_BODIES = 128
@@ -49,6 +52,7 @@ JOINT_SIXDOF = 6
 JOINT_MOTOR = 7
 JOINT_SPRING = 8
 JOINT_WHEEL = 9
+JOINT_GEAR = 10
 MOTOR_VELOCITY, MOTOR_POSITION, MOTOR_SERVO = 0, 1, 2
 MODEL_ACCELERATION, MODEL_FORCE = 0, 1
 
@@ -124,6 +128,10 @@ class AvbdJointDesc(C.Structure):
         ("local_axle_b", F3),
         ("suspension_hz", C.c_float),
         ("suspension_damping", C.c_float),
+        ("gear_joint_a", C.c_uint32),
+        ("gear_joint_b", C.c_uint32),
+        ("gear_ratio", C.c_float),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -179,7 +187,27 @@ class AvbdJointState(C.Structure):
         ("acc_lim", C.c_float),
         ("lim_dual", C.c_float),
         ("sacc", C.c_float * 6),
+        ("gear_raw", C.c_float * 2),
+        ("gear_cont", C.c_float * 2),
+        ("gear_mem_set", C.c_uint32),
     ]
+
+
+SNAPSHOT_FORMAT = 1
+SNAPSHOT_HEADER_BYTES = 128
+SNAPSHOT_MAGIC = b"ORNAVBD\0"
+SNAPSHOT_SETTINGS_BYTES = 48       # launch tuning, precision, event period, joint stiffness, accumulator
+SNAPSHOT_JOINT_RECORD_BYTES = 364  # a joint as the world holds it (assembly references resolved)
+SNAPSHOT_EVENT_WORDS = 16
+
+
+class AvbdSnapshotInfo(C.Structure):
+    _fields_ = [("format", C.c_uint32), ("abi", C.c_uint32),
+                ("nbodies", C.c_uint32), ("nscenes", C.c_uint32), ("npairs", C.c_uint32),
+                ("njoints", C.c_uint32), ("nhulls", C.c_uint32),
+                ("ntouch", C.c_uint32), ("ntrigger", C.c_uint32),
+                ("ncontact_events", C.c_uint32), ("ntrigger_events", C.c_uint32), ("reserved", C.c_uint32),
+                ("bytes", C.c_uint64), ("substeps", C.c_uint64)]
 
 
 class AvbdCounters(C.Structure):
@@ -261,14 +289,15 @@ def default_params(gravity=(0.0, -9.81, 0.0), step_dt=1.0 / 60.0, iterations=10,
 
 
 def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0),
-               limit=None, motor=None, max_distance=0.0, axes=None, drive=None, spring=None, wheel=None):
+               limit=None, motor=None, max_distance=0.0, axes=None, drive=None, spring=None, wheel=None,
+               gear=None):
     """A joint record.  limit = (min, max); motor = (target speed, max
     torque or force); axes (sixdof) = 6 entries, each "free", "locked" or
     (min, max), linear x y z then angular x y z; drive (free motor) =
     (linear target, angular target, max force, max torque, correction);
     spring = (rest, target velocity, stiffness, damping, max force, kind,
     model); wheel = (axle a, axle b, suspension Hz, damping ratio), axis_a/b
-    being the suspension axes."""
+    being the suspension axes; gear = (joint a, joint b, ratio)."""
     d = AvbdJointDesc()
     d.kind = kind
     d.body_a = a
@@ -307,4 +336,6 @@ def joint_desc(kind, a, b, anchor_a, anchor_b, axis_a=(1, 0, 0), axis_b=(1, 0, 0
         d.local_axle_a[:] = list(map(float, xa))
         d.local_axle_b[:] = list(map(float, xb))
         d.suspension_hz, d.suspension_damping = float(hz), float(zeta)
+    if gear is not None:
+        d.gear_joint_a, d.gear_joint_b, d.gear_ratio = int(gear[0]), int(gear[1]), float(gear[2])
     return d

@@ -85,6 +85,11 @@ def lib():
             "avbd_adjoint_trace": [vp, vp, vp, C.c_int32, C.POINTER(C.c_int32)],
             "avbd_set_joint_stiffness": [vp, C.c_float],
             "avbd_adjoint_grad_joint_stiffness": [vp, vp],
+            "avbd_world_snapshot": [vp, vp, C.c_uint64, C.POINTER(C.c_uint64)],
+            "avbd_world_from_snapshot": [vp, C.c_uint64, C.c_int, C.POINTER(vp)],
+            "avbd_snapshot_info": [vp, C.c_uint64, C.POINTER(abi.AvbdSnapshotInfo)],
+            "avbd_world_save": [vp, C.c_char_p],
+            "avbd_world_load": [C.c_char_p, C.c_int, C.POINTER(vp)],
         }
         for name, args in sigs.items():
             fn = getattr(L, name)
@@ -131,6 +136,16 @@ def scene_step_static(params, bodies, substeps):
     return out
 
 
+def snapshot_info(data):
+    """Header of a world snapshot (avbd_snapshot_info): validated, checksum
+    included, without a GPU.  Raises AvbdError(AVBD_ERR_FORMAT) for anything
+    that is not an intact snapshot of this format version."""
+    buf = bytes(data)
+    info = abi.AvbdSnapshotInfo()
+    _check(lib().avbd_snapshot_info(buf, len(buf), C.byref(info)), "avbd_snapshot_info")
+    return info
+
+
 class AvbdWorld:
     """One AVBD world on one GPU: one scene (AvbdEngine) or many (a batch)."""
 
@@ -147,6 +162,43 @@ class AvbdWorld:
         else:
             _check(lib().avbd_world_create(C.byref(self.params), device, C.byref(h)), "avbd_world_create")
         self.h = h
+
+    @classmethod
+    def _adopt(cls, h, params):
+        self = cls.__new__(cls)
+        self.h = h
+        self.params = params
+        return self
+
+    @classmethod
+    def from_snapshot(cls, data, device=0):
+        """A new world from the bytes of AvbdWorld.snapshot() (avbd_world_from_snapshot)."""
+        buf = bytes(data)
+        h = C.c_void_p()
+        _check(lib().avbd_world_from_snapshot(buf, len(buf), device, C.byref(h)), "avbd_world_from_snapshot")
+        off = abi.SNAPSHOT_HEADER_BYTES
+        return cls._adopt(h, abi.AvbdParams.from_buffer_copy(buf[off:off + C.sizeof(abi.AvbdParams)]))
+
+    @classmethod
+    def load(cls, path, device=0):
+        """A new world from a snapshot file (avbd_world_load)."""
+        h = C.c_void_p()
+        _check(lib().avbd_world_load(os.fsencode(path), device, C.byref(h)), "avbd_world_load")
+        with open(path, "rb") as f:
+            head = f.read(abi.SNAPSHOT_HEADER_BYTES + C.sizeof(abi.AvbdParams))
+        return cls._adopt(h, abi.AvbdParams.from_buffer_copy(head[abi.SNAPSHOT_HEADER_BYTES:]))
+
+    def snapshot(self):
+        """The whole world as snapshot bytes (avbd_world_snapshot)."""
+        n = C.c_uint64()
+        _check(lib().avbd_world_snapshot(self.h, None, 0, C.byref(n)), "avbd_world_snapshot")
+        buf = C.create_string_buffer(n.value)
+        _check(lib().avbd_world_snapshot(self.h, buf, n.value, C.byref(n)), "avbd_world_snapshot")
+        return buf.raw[: n.value]
+
+    def save(self, path):
+        """Write the world's snapshot to a file (avbd_world_save)."""
+        _check(lib().avbd_world_save(self.h, os.fsencode(path)), "avbd_world_save")
 
     def close(self):
         if getattr(self, "h", None):

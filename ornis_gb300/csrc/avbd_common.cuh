@@ -68,10 +68,13 @@ static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uin
     uint2 fa = w.filter[a], fb = w.filter[b];
     return (fa.x & fb.y) != 0u && (fb.x & fa.y) != 0u;
 }
-// a joint links a and b (the swept cast skips every joined partner, mod.rs:887-917)
+// a joint links a and b (the swept cast skips every joined partner but a
+// gear's, mod.rs:887-917)
 static __device__ __forceinline__ bool jointed(const DW& w, uint32_t a, uint32_t b) {
     for (uint32_t k = w.jofs[a]; k < w.jofs[a + 1]; k++) {
-        uint2 ab = w.j_ab[w.jlist[k]];
+        const uint32_t j = w.jlist[k];
+        uint2 ab = w.j_ab[j];
+        if (w.j_kind[j] == AVBD_JOINT_GEAR) continue;
         if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return true;
     }
     return false;
@@ -83,7 +86,7 @@ static __device__ __forceinline__ bool jointed_no_collide(const DW& w, uint32_t 
         const uint32_t j = w.jlist[k];
         uint2 ab = w.j_ab[j];
         const uint32_t kind = w.j_kind[j];
-        if (kind == AVBD_JOINT_FIXED || kind == AVBD_JOINT_SIXDOF) continue;
+        if (kind == AVBD_JOINT_FIXED || kind == AVBD_JOINT_SIXDOF || kind == AVBD_JOINT_GEAR) continue;
         if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return true;
     }
     return false;
@@ -138,8 +141,86 @@ static __device__ __forceinline__ float2 axis_window(const DW& w, uint32_t j, in
     float4 v = w.j_six[3 * (size_t)j + (k >> 1)];
     return (k & 1) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
 }
+// ---- gears (joints_ext.rs:34-160) ----
+// One side of a gear (GearSide, avbd/mod.rs:304-317): the coupled joint's
+// bodies, whether it turns (revolute) or slides (prismatic), its live world
+// axis, the slide's anchor levers and its continuous coordinate.
+struct GearSide {
+    uint32_t a, b;
+    bool angular;
+    V3 axis, ra, rb;
+    float coord;
+};
+// A revolute joint's twist or a prismatic joint's slide from its assembly
+// reference (joints_ext.rs:37-51); the side's axis and levers on the way.
+static __device__ __forceinline__ float joint_coordinate(const DW& w, uint32_t r, GearSide* s = nullptr) {
+    const uint2 ab = w.j_ab[r];
+    const Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
+    const float4 axa4 = w.j_axa[r];
+    const V3 axis = ld3(axa4);
+    const bool angular = w.j_kind[r] == AVBD_JOINT_REVOLUTE;
+    const V3 wa = normalize_or(qrot(qa, axis), VZ());
+    float raw;
+    V3 ra = V0(), rb = V0();
+    if (angular) {
+        raw = hinge_twist(qa, qb, axis) - axa4.w;
+    } else {
+        ra = qrot(qa, ld3(w.j_la[r]));
+        rb = qrot(qb, ld3(w.j_lb[r]));
+        const V3 pa = ld3(w.pos[ab.x]) + ra, pb = ld3(w.pos[ab.y]) + rb;
+        raw = dot(pb - pa, wa) - w.j_ref[r].x;
+    }
+    if (s) {
+        s->a = ab.x;
+        s->b = ab.y;
+        s->angular = angular;
+        s->axis = wa;
+        s->ra = ra;
+        s->rb = rb;
+    }
+    return raw;
+}
+// Side k of gear g, its coordinate unwrapped across turns against the step
+// start for a hinge (joints_ext.rs:120-160).
+static __device__ __forceinline__ GearSide gear_side(const DW& w, uint32_t g, int k) {
+    const uint2 gb = w.j_gb[g];
+    GearSide s;
+    const float raw = joint_coordinate(w, k ? gb.y : gb.x, &s);
+    const float4 m = w.j_gmem[g];
+    s.coord = w.j_gset[g] && s.angular ? (k ? m.w : m.z) + wrap_pi(raw - (k ? m.y : m.x)) : raw;
+    return s;
+}
+// C = coordinate_a + ratio coordinate_b - constant
+static __device__ __forceinline__ float gear_error(const DW& w, uint32_t g, const GearSide& sa, const GearSide& sb) {
+    return sa.coord + w.j_dref[g].x * sb.coord - w.j_ref[g].x;
+}
+// The bodies a joint holds (sleep.rs:9-16), how many: a joint's two, a
+// gear's coupled joints' four (a body may repeat).
+static __device__ __forceinline__ int joint_members(const DW& w, uint32_t j, uint32_t m[4]) {
+    if (w.j_kind[j] == AVBD_JOINT_GEAR) {
+        const uint2 gb = w.j_gb[j];
+        const uint2 x = w.j_ab[gb.x], y = w.j_ab[gb.y];
+        m[0] = x.x; m[1] = x.y; m[2] = y.x; m[3] = y.y;
+        return 4;
+    }
+    const uint2 ab = w.j_ab[j];
+    m[0] = ab.x; m[1] = ab.y;
+    return 2;
+}
+
+// The body whose walk over its joints updates a joint's multipliers in the
+// per-scene solve: a joint's first body, a gear's first coupled body (a gear
+// is listed only on its coupled joints' bodies).
+static __device__ __forceinline__ uint32_t joint_dual_owner(const DW& w, uint32_t j) {
+    return w.j_kind[j] == AVBD_JOINT_GEAR ? w.j_ab[w.j_gb[j].x].x : w.j_ab[j].x;
+}
+
 // sleep.rs:30-105: how far a joint is from its assembly pose
 static __device__ __forceinline__ float joint_rest_error(const DW& w, uint32_t j) {
+    if (w.j_kind[j] == AVBD_JOINT_GEAR) {
+        const GearSide sa = gear_side(w, j, 0), sb = gear_side(w, j, 1);
+        return fabsf(gear_error(w, j, sa, sb));
+    }
     uint2 ab = w.j_ab[j];
     V3 pa = ld3(w.pos[ab.x]), pb = ld3(w.pos[ab.y]);
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
@@ -205,9 +286,9 @@ static __device__ __forceinline__ bool joint_driven(const DW& w, uint32_t j) {
     } else if (ref.z != 0.0f && ref.w > 0.0f) {
         return true;
     }
-    uint2 ab = w.j_ab[j];
-    uint32_t m[2] = {ab.x, ab.y};
-    for (int k = 0; k < 2; k++) {
+    uint32_t m[4];
+    const int nm = joint_members(w, j, m);
+    for (int k = 0; k < nm; k++) {
         uint32_t h = m[k];
         if (is_dynamic(w, h)) continue;
         float4 p = w.pos[h], pp = w.prev_pos[h], q = w.rot[h], pq = w.prev_rot[h];

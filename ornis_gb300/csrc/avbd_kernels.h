@@ -41,6 +41,7 @@ int radix_pass(const uint32_t* keys, const uint32_t* vals, uint32_t* okeys, uint
 // per substep phases
 void launch_begin_substep(const DW& w, cudaStream_t st);
 void launch_wake_joint_motion(const DW& w, cudaStream_t st);
+void launch_gear_mem(const DW& w, cudaStream_t st);
 void launch_torque(const DW& w, cudaStream_t st);
 struct BroadphasePlan {
     const uint32_t* small_scenes = nullptr;  // device list of scenes swept by one CTA each

@@ -660,7 +660,15 @@ static __device__ __forceinline__ int jp_pick(const DW& w, volatile int32_t* col
         if (w.p_np[p]) visit(w.p_ab[p].x);
     }
     for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1] && ready; k++) {
-        uint2 ab = w.j_ab[w.jlist[k]];
+        const uint32_t j = w.jlist[k];
+        if (w.j_kind[j] == AVBD_JOINT_GEAR) {  // a gear couples its coupled joints' bodies
+            uint32_t m[4];
+            const int nm = joint_members(w, j, m);
+            for (int i = 0; i < nm; i++)
+                if (m[i] != h) visit(m[i]);
+            continue;
+        }
+        uint2 ab = w.j_ab[j];
         visit(ab.x == h ? ab.y : ab.x);
     }
     if (!ready) return -2;

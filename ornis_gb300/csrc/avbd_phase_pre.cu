@@ -46,9 +46,10 @@ __global__ void k_joint_wake(DW w) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= (uint32_t)w.J) return;
     if (joint_driven(w, j) || joint_rest_error(w, j) > JOINT_REST_ERROR) {
-        uint2 ab = w.j_ab[j];
-        if (is_dynamic(w, ab.x)) w.flag[ab.x] = 1;
-        if (is_dynamic(w, ab.y)) w.flag[ab.y] = 1;
+        uint32_t m[4];
+        const int nm = joint_members(w, j, m);
+        for (int k = 0; k < nm; k++)
+            if (is_dynamic(w, m[k])) w.flag[m[k]] = 1;
     }
 }
 // propagate_joint_flags (sleep.rs:152-175) with value 1: one awake dynamic
@@ -82,6 +83,26 @@ void launch_wake_joint_motion(const DW& w, cudaStream_t st) {
     k_wake_apply<<<gb, 256, 0, st>>>(w);
 }
 void launch_wake_apply(const DW& w, cudaStream_t st) { k_wake_apply<<<nblk(w.N, 256), 256, 0, st>>>(w); }
+
+// Once per step, after the first wake pass: each gear's coupled joints'
+// raw coordinates and the continuous ones, unwrapped across turns for
+// hinges (update_gear_mem, joints_ext.rs:55-118).
+__global__ void k_gear_mem(DW w) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint32_t)w.J || w.j_kind[g] != AVBD_JOINT_GEAR) return;
+    const uint2 gb = w.j_gb[g];
+    const float4 m = w.j_gmem[g];
+    const bool set = w.j_gset[g] != 0u;
+    GearSide sa, sb;
+    const float ra = joint_coordinate(w, gb.x, &sa), rb = joint_coordinate(w, gb.y, &sb);
+    const float ca = set && sa.angular ? m.z + wrap_pi(ra - m.x) : ra;
+    const float cb = set && sb.angular ? m.w + wrap_pi(rb - m.y) : rb;
+    w.j_gmem[g] = make_float4(ra, rb, ca, cb);
+    w.j_gset[g] = 1u;
+}
+void launch_gear_mem(const DW& w, cudaStream_t st) {
+    if (w.n_gear) k_gear_mem<<<nblk(w.J, 128), 128, 0, st>>>(w);
+}
 
 // ---- torque -> angular velocity (mod.rs:855-871) ---------------------------
 __global__ void k_torque(DW w) {

@@ -115,10 +115,38 @@ static __device__ __forceinline__ void stamp_point(const DW& w, const PairCtx& c
 // limit), Prismatic (and its limit), Fixed, Distance, Rope, SixDof.
 // ALL = false: the instantiation for worlds whose joints are all ball and
 // revolute joints (the other kinds' rows would cost it registers).
+// A gear's rows on body h, one of its coupled joints' bodies
+// (assembly.rs:426-454 slides, :650-682 hinges): the shared force on the
+// position-level row C = coord_a + ratio coord_b - constant, the slide
+// sides first, then the hinge sides.
+static __device__ __forceinline__ void stamp_gear(const DW& w, uint32_t j, uint32_t h, Sys& s) {
+    const GearSide sd[2] = {gear_side(w, j, 0), gear_side(w, j, 1)};
+    const float c = gear_error(w, j, sd[0], sd[1]);
+    const float pen = w.j_pen_l[j].x;
+    const float f = pen * c + w.j_lam_l[j].x;
+    if (!row_live(c, f)) return;
+    const float coef[2] = {1.0f, w.j_dref[j].x};
+    for (int k = 0; k < 2; k++) {
+        const GearSide& side = sd[k];
+        if (side.angular || (h != side.a && h != side.b)) continue;
+        stamp_row(s, side.axis, pen * coef[k] * coef[k], f * coef[k], h == side.a ? side.ra : side.rb,
+                  h == side.a ? -1.0f : 1.0f);
+    }
+    for (int k = 0; k < 2; k++) {
+        const GearSide& side = sd[k];
+        if (!side.angular || (h != side.a && h != side.b)) continue;
+        stamp_angular(s, h == side.a ? -side.axis : side.axis, pen * coef[k] * coef[k], f * coef[k]);
+    }
+}
+
 template <bool ALL>
 static __device__ __forceinline__ void stamp_joint(const DW& w, uint32_t j, uint32_t h, Sys& s) {
     uint2 ab = w.j_ab[j];
     const uint32_t kind = w.j_kind[j];
+    if (ALL && kind == AVBD_JOINT_GEAR) {
+        stamp_gear(w, j, h, s);
+        return;
+    }
     const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
     const bool k_dist = ALL && (kind == AVBD_JOINT_DISTANCE || kind == AVBD_JOINT_ROPE);
     const bool k_spr = ALL && kind == AVBD_JOINT_SPRING, k_whl = ALL && kind == AVBD_JOINT_WHEEL;
@@ -742,6 +770,20 @@ template <bool ALL>
 static __device__ void dual_joint(const DW& w, uint32_t j) {
     uint2 ab = w.j_ab[j];
     const uint32_t kind = w.j_kind[j];
+    if (ALL && kind == AVBD_JOINT_GEAR) {
+        // reads only bodies and its own state: its place after every other
+        // joint (joints_ext.rs:897-918) cannot change it; penalty capped
+        // like a limit's
+        const GearSide sa = gear_side(w, j, 0), sb = gear_side(w, j, 1);
+        const float c = gear_error(w, j, sa, sb);
+        if (fabsf(c) < C_EPS) return;
+        float4 ll = w.j_lam_l[j], pl = w.j_pen_l[j];
+        ll.x = ll.x + pl.x * c;
+        pl.x = ramp(pl.x, c, BETA, LIM_PEN_MAX);
+        w.j_lam_l[j] = ll;
+        w.j_pen_l[j] = pl;
+        return;
+    }
     const bool k_pri = ALL && kind == AVBD_JOINT_PRISMATIC, k_six = ALL && kind == AVBD_JOINT_SIXDOF;
     Q qa = ldq(w.rot[ab.x]), qb = ldq(w.rot[ab.y]);
     Q qa0 = ldq(w.rot0[ab.x]), qb0 = ldq(w.rot0[ab.y]);
@@ -1143,7 +1185,7 @@ __global__ void __launch_bounds__(BS, MINB) k_scene_solve(DW w) {
                 for (uint32_t h = b0 + tid; h < b1; h += BS)
                     for (uint32_t k = w.jofs[h]; k < w.jofs[h + 1]; k++) {
                         uint32_t j = w.jlist[k];
-                        if (w.j_ab[j].x == h) dual_joint<JT == 2>(w, j);
+                        if (joint_dual_owner(w, j) == h) dual_joint<JT == 2>(w, j);
                     }
             __syncthreads();
         }
@@ -1253,9 +1295,9 @@ __global__ void k_ready_joint(DW w) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= (uint32_t)w.J) return;
     if (joint_driven(w, j) || joint_rest_error(w, j) > JOINT_REST_ERROR) {
-        uint2 ab = w.j_ab[j];
-        w.flag[ab.x] &= (uint8_t)~1u;
-        w.flag[ab.y] &= (uint8_t)~1u;
+        uint32_t m[4];
+        const int nm = joint_members(w, j, m);
+        for (int k = 0; k < nm; k++) w.flag[m[k]] &= (uint8_t)~1u;
     }
 }
 __global__ void k_ready_gather(DW w) {

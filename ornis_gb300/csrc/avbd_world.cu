@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "avbd_crmath.cuh"
@@ -39,10 +40,31 @@ struct JointRec {
     uint32_t spr_mode;         // spring: kind | model << 4
     float bxa[3], bxb[3];      // wheel: spin axles
     float susp[2];             // wheel: suspension frequency (Hz) and damping ratio
+    uint32_t gb[2];            // gear: the coupled joints
+    float gratio;              // gear: coordinate_a + gratio coordinate_b stays at ref
     uint32_t cfg;              // sixdof axis configuration, 2 bits per axis
     float six_min[6], six_max[6];
     AvbdJointState st;
 };
+
+// The bodies a joint holds, each once (sleep.rs:9-16): its two bodies, or
+// for a gear the bodies of the two joints it couples.
+int joint_members_host(const std::vector<JointRec>& js, uint32_t ji, uint32_t m[4]) {
+    const JointRec& j = js[ji];
+    if (j.kind != AVBD_JOINT_GEAR) {
+        m[0] = j.a;
+        m[1] = j.b;
+        return 2;
+    }
+    const uint32_t c[4] = {js[j.gb[0]].a, js[j.gb[0]].b, js[j.gb[1]].a, js[j.gb[1]].b};
+    int n = 0;
+    for (uint32_t x : c) {
+        bool seen = false;
+        for (int k = 0; k < n; k++) seen = seen || m[k] == x;
+        if (!seen) m[n++] = x;
+    }
+    return n;
+}
 
 struct Alloc {
     std::vector<void*> ptrs;
@@ -240,20 +262,28 @@ static void free_graphs(AvbdWorld* W, bool settings_changed = true) {
 // half-space pairs; surviving pairs never outnumber candidates.
 static uint32_t default_cand_cap(uint32_t n) { return 12u * n + 4096u; }
 
+// The previous touch set (handle keyed, CSR by the higher handle) held on the
+// device, read for a world of N bodies: bodies added since have no touches.
+// Empty when the device holds none.
+static void read_touch_set(AvbdWorld* W, uint32_t N, std::vector<uint32_t>& tof, std::vector<uint32_t>& tkeys) {
+    tof.clear();
+    tkeys.clear();
+    if (!W->w.toff || !W->w.evs) return;
+    uint32_t on = (uint32_t)W->w.N, par = 0;
+    tof.resize(on + 1);
+    cudaMemcpy(tof.data(), W->w.toff, (on + 1) * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(&par, W->w.evs + EV_PAR, 4, cudaMemcpyDeviceToHost);
+    tkeys.resize(tof[on]);
+    if (!tkeys.empty())
+        cudaMemcpy(tkeys.data(), (par & 1u) ? W->w.tk1 : W->w.tk0, tkeys.size() * 4, cudaMemcpyDeviceToHost);
+    tof.resize(N + 1, tof[on]);
+}
+
 static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap) {
     W->mem_gen++;
-    // the previous touch set (handle keyed) survives a reallocation
+    // the previous touch set survives a reallocation
     std::vector<uint32_t> tof, tkeys;
-    if (W->w.toff && W->w.evs) {
-        uint32_t on = (uint32_t)W->w.N, par = 0;
-        tof.resize(on + 1);
-        cudaMemcpy(tof.data(), W->w.toff, (on + 1) * 4, cudaMemcpyDeviceToHost);
-        cudaMemcpy(&par, W->w.evs + EV_PAR, 4, cudaMemcpyDeviceToHost);
-        tkeys.resize(tof[on]);
-        if (!tkeys.empty())
-            cudaMemcpy(tkeys.data(), (par & 1u) ? W->w.tk1 : W->w.tk0, tkeys.size() * 4, cudaMemcpyDeviceToHost);
-        tof.resize(N + 1, tof[on]);  // bodies added since: no touches
-    }
+    read_touch_set(W, N, tof, tkeys);
     W->mem.release();
     free_graphs(W);
     Alloc& m = W->mem;
@@ -295,8 +325,9 @@ static int alloc_device(AvbdWorld* W, uint32_t N, uint32_t J, uint32_t cand_cap)
     w.jimp_off = m.get<uint32_t>(S + 1);
     w.jimp_list = m.get<uint32_t>(J);
     w.j_lam_l = m.get<float4>(J); w.j_lam_a = m.get<float4>(J); w.j_pen_l = m.get<float4>(J); w.j_pen_a = m.get<float4>(J);
+    w.j_gb = m.get<uint2>(J); w.j_gmem = m.get<float4>(J); w.j_gset = m.get<uint32_t>(J);
     w.jofs = m.get<uint32_t>(N + 1);
-    w.jlist = m.get<uint32_t>(2 * J);
+    w.jlist = m.get<uint32_t>(4 * (size_t)J);
     for (int b = 0; b < 2; b++) {
         PairBuf& p = W->pb[b];
         p.ab = m.get<uint2>(cand_cap); p.n = m.get<float4>(cand_cap); p.mu = m.get<float2>(cand_cap);
@@ -582,16 +613,22 @@ static int upload_all(AvbdWorld* W) {
         prev_pos[h] = make_float4(a.prev_position[0], a.prev_position[1], a.prev_position[2], 0.0f);
         prev_rot[h] = make_float4(a.prev_orientation[0], a.prev_orientation[1], a.prev_orientation[2], a.prev_orientation[3]);
     }
-    // joints: adjacency (ascending joint index per body) and components over
-    // joints whose members are both dynamic (sleep.rs:152-175)
-    std::vector<uint32_t> jofs(N + 1, 0), jlist(2 * J);
-    for (const JointRec& j : W->joints) { jofs[j.a + 1]++; jofs[j.b + 1]++; }
-    for (uint32_t h = 0; h < N; h++) jofs[h + 1] += jofs[h];
+    // joints: adjacency (ascending joint index per body; a gear on each body
+    // of its coupled joints) and components over the dynamic members of each
+    // joint (sleep.rs:152-175)
+    std::vector<uint32_t> jofs(N + 1, 0), jlist;
     {
+        uint32_t m[4];
+        for (uint32_t ji = 0; ji < J; ji++) {
+            const int nm = joint_members_host(W->joints, ji, m);
+            for (int k = 0; k < nm; k++) jofs[m[k] + 1]++;
+        }
+        for (uint32_t h = 0; h < N; h++) jofs[h + 1] += jofs[h];
+        jlist.resize(jofs[N]);
         std::vector<uint32_t> curj(jofs.begin(), jofs.end() - 1);
         for (uint32_t ji = 0; ji < J; ji++) {
-            jlist[curj[W->joints[ji].a]++] = ji;
-            jlist[curj[W->joints[ji].b]++] = ji;
+            const int nm = joint_members_host(W->joints, ji, m);
+            for (int k = 0; k < nm; k++) jlist[curj[m[k]]++] = ji;
         }
     }
     std::vector<int32_t> parent(N);
@@ -601,11 +638,16 @@ static int upload_all(AvbdWorld* W) {
         return x;
     };
     std::vector<uint8_t> in_joint(N, 0);
-    for (const JointRec& j : W->joints) {
-        bool da = W->bodies[j.a].body_type == AVBD_BODY_DYNAMIC, db = W->bodies[j.b].body_type == AVBD_BODY_DYNAMIC;
-        if (da && db) {
-            in_joint[j.a] = in_joint[j.b] = 1;
-            int32_t ra = find((int32_t)j.a), rb = find((int32_t)j.b);
+    for (uint32_t ji = 0; ji < J; ji++) {
+        uint32_t m[4], d[4];
+        const int nm = joint_members_host(W->joints, ji, m);
+        int nd = 0;
+        for (int k = 0; k < nm; k++)
+            if (W->bodies[m[k]].body_type == AVBD_BODY_DYNAMIC) d[nd++] = m[k];
+        if (nd < 2) continue;  // one dynamic member wakes or freezes only itself
+        for (int k = 0; k < nd; k++) {
+            in_joint[d[k]] = 1;
+            int32_t ra = find((int32_t)d[k]), rb = find((int32_t)d[0]);
             if (ra != rb) parent[ra] = rb;
         }
     }
@@ -636,6 +678,7 @@ static int upload_all(AvbdWorld* W) {
         const JointRec& j = W->joints[i];
         j_kind[i] = j.kind;
         j_cfg[i] = j.cfg;
+        j_lim[i] = make_float4(j.lo, j.hi, j.has_lim ? 1.0f : 0.0f, j.st.acc_lim);
         j_ref[i] = make_float4(j.refv, j.st.lim_dual, j.mot_speed, j.mot_max);
         j_dref[i] = make_float4(j.dref[0], j.dref[1], j.dref[2], 0.0f);
         j_qref[i] = make_float4(j.qref[0], j.qref[1], j.qref[2], j.qref[3]);
@@ -662,14 +705,18 @@ static int upload_all(AvbdWorld* W) {
             j_axb[i] = make_float4(j.spr[0], j.spr[1], j.spr[2], j.spr[3]);
             j_cfg[i] = j.spr_mode;
         }
+        if (j.kind == AVBD_JOINT_GEAR) {
+            // a gear's ratio rides in the weld-offset slot, its constant in j_ref.x
+            j_dref[i] = make_float4(j.gratio, 0.0f, 0.0f, 0.0f);
+            j_ref[i] = make_float4(j.refv, 0.0f, 0.0f, 0.0f);
+        }
         if (j.kind == AVBD_JOINT_WHEEL) {
             // a wheel's axles ride in the weld-reference slots, its suspension
             // in the limit slot (a wheel has no limit: has_limit stays 0)
             j_dref[i] = make_float4(j.bxa[0], j.bxa[1], j.bxa[2], 0.0f);
             j_qref[i] = make_float4(j.bxb[0], j.bxb[1], j.bxb[2], 0.0f);
-            j_lim[i] = make_float4(j.susp[0], j.susp[1], 0.0f, 0.0f);
+            j_lim[i] = make_float4(j.susp[0], j.susp[1], 0.0f, j.st.acc_lim);
         }
-        j_lim[i] = make_float4(j.lo, j.hi, j.has_lim ? 1.0f : 0.0f, j.st.acc_lim);
         jll[i] = make_float4(j.st.lam_l[0], j.st.lam_l[1], j.st.lam_l[2], 0.0f);
         jla[i] = make_float4(j.st.lam_a[0], j.st.lam_a[1], j.st.lam_a[2], 0.0f);
         jpl[i] = make_float4(j.st.pen_l[0], j.st.pen_l[1], j.st.pen_l[2], 0.0f);
@@ -735,11 +782,28 @@ static int upload_all(AvbdWorld* W) {
     up(w.prev_rot, prev_rot.data(), N * 16);
     up(w.comp, comp.data(), N * 4);
     up((void*)w.jofs, jofs.data(), (N + 1) * 4);
-    up((void*)w.jlist, jlist.data(), 2 * J * 4);
+    up((void*)w.jlist, jlist.data(), jlist.size() * 4);
     up(w.j_kind, j_kind.data(), J * 4);
     // the joint rows' kernels come in a ball-and-revolute instantiation
     w.j_all = 0;
     for (uint32_t k : j_kind) w.j_all |= (k != AVBD_JOINT_BALL && k != AVBD_JOINT_REVOLUTE) ? 1 : 0;
+    {
+        std::vector<uint2> gb(J, make_uint2(0u, 0u));
+        std::vector<float4> gmem(J, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        std::vector<uint32_t> gset(J, 0u);
+        w.n_gear = 0;
+        for (uint32_t i = 0; i < J; i++) {
+            const JointRec& j = W->joints[i];
+            if (j.kind != AVBD_JOINT_GEAR) continue;
+            w.n_gear++;
+            gb[i] = make_uint2(j.gb[0], j.gb[1]);
+            gmem[i] = make_float4(j.st.gear_raw[0], j.st.gear_raw[1], j.st.gear_cont[0], j.st.gear_cont[1]);
+            gset[i] = j.st.gear_mem_set;
+        }
+        up(w.j_gb, gb.data(), J * 8);
+        up(w.j_gmem, gmem.data(), J * 16);
+        up(w.j_gset, gset.data(), J * 4);
+    }
     up(w.j_ab, j_ab.data(), J * 8);
     up(w.j_la, j_la.data(), J * 16); up(w.j_lb, j_lb.data(), J * 16);
     up(w.j_axa, j_axa.data(), J * 16); up(w.j_axb, j_axb.data(), J * 16);
@@ -814,8 +878,11 @@ static int download_all(AvbdWorld* W) {
         CK(cudaMemcpyAsync(qroll.data(), w.q_roll, Q * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(qm.data(), w.q_matched, Q * 4, cudaMemcpyDeviceToHost, st));
     }
-    std::vector<float4> jll(J), jla(J), jpl(J), jpa(J), jlim(J), jref(J), jsacc(2 * (size_t)J);
+    std::vector<float4> jll(J), jla(J), jpl(J), jpa(J), jlim(J), jref(J), jsacc(2 * (size_t)J), jgmem(J);
+    std::vector<uint32_t> jgset(J);
     if (J) {
+        CK(cudaMemcpyAsync(jgmem.data(), w.j_gmem, J * 16, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(jgset.data(), w.j_gset, J * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jref.data(), w.j_ref, J * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jsacc.data(), w.j_sacc, 2 * (size_t)J * 16, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(jll.data(), w.j_lam_l, J * 16, cudaMemcpyDeviceToHost, st));
@@ -848,6 +915,27 @@ static int download_all(AvbdWorld* W) {
             q.matched = qm[d];
         }
     }
+    // The device keeps a static body's pairs in discovery order unless the
+    // world sorts them (sort_static): the host model lists pairs in
+    // ascending (a, b), whatever order the device holds.
+    auto ab_less = [&](uint32_t x, uint32_t y) {
+        const AvbdPairState &px = W->pairs[x], &py = W->pairs[y];
+        return px.a != py.a ? px.a < py.a : px.b < py.b;
+    };
+    std::vector<uint32_t> perm(P);
+    std::iota(perm.begin(), perm.end(), 0u);
+    if (!std::is_sorted(perm.begin(), perm.end(), ab_less)) {
+        std::sort(perm.begin(), perm.end(), ab_less);
+        std::vector<AvbdPairState> sp(P);
+        std::vector<AvbdPointState> sq(Q);
+        for (uint32_t i = 0; i < P; i++) {
+            sp[i] = W->pairs[perm[i]];
+            std::memcpy(&sq[(size_t)i * MAX_PTS], &W->points[(size_t)perm[i] * MAX_PTS],
+                        MAX_PTS * sizeof(AvbdPointState));
+        }
+        W->pairs.swap(sp);
+        W->points.swap(sq);
+    }
     for (uint32_t i = 0; i < J; i++) {
         AvbdJointState& s = W->joints[i].st;
         s.lam_l[0] = jll[i].x; s.lam_l[1] = jll[i].y; s.lam_l[2] = jll[i].z;
@@ -858,6 +946,11 @@ static int download_all(AvbdWorld* W) {
         s.lim_dual = jref[i].y;
         const float4 s0 = jsacc[2 * (size_t)i], s1 = jsacc[2 * (size_t)i + 1];
         s.sacc[0] = s0.x; s.sacc[1] = s0.y; s.sacc[2] = s0.z; s.sacc[3] = s0.w; s.sacc[4] = s1.x; s.sacc[5] = s1.y;
+        if (W->joints[i].kind == AVBD_JOINT_GEAR) {
+            s.gear_raw[0] = jgmem[i].x; s.gear_raw[1] = jgmem[i].y;
+            s.gear_cont[0] = jgmem[i].z; s.gear_cont[1] = jgmem[i].w;
+            s.gear_mem_set = jgset[i];
+        }
     }
     W->host_valid = true;
     return AVBD_OK;
@@ -886,6 +979,7 @@ static void enqueue_front(AvbdWorld* W, bool emit) {
     const DW& w = W->w;
     launch_begin_substep(w, st);
     launch_wake_joint_motion(w, st);
+    launch_gear_mem(w, st);
     launch_torque(w, st);
     launch_broadphase(w, W->plan, st);
     launch_ccd(w, st);
@@ -1375,6 +1469,19 @@ static int drain(AvbdWorld* W, int which, T* out, uint32_t cap, uint32_t* n) {
     return AVBD_OK;
 }
 
+// The world's stream and pinned counters on `device`; the world is deleted
+// when that fails.
+static int open_device(AvbdWorld* W, int device) {
+    W->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&W->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&W->h_ctr, C_NUM * 4) != cudaSuccess) {
+        if (W->st) cudaStreamDestroy(W->st);
+        delete W;
+        return AVBD_ERR_DEVICE;
+    }
+    return AVBD_OK;
+}
+
 extern "C" {
 
 int avbd_default_params(AvbdParams* p) {
@@ -1397,12 +1504,8 @@ int avbd_world_create(const AvbdParams* params, int device, AvbdWorld** out) {
         return AVBD_ERR_INVALID_ARG;
     AvbdWorld* W = new AvbdWorld();
     W->prm = *params;
-    W->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&W->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMallocHost(&W->h_ctr, C_NUM * 4) != cudaSuccess) {
-        delete W;
-        return AVBD_ERR_DEVICE;
-    }
+    int rc = open_device(W, device);
+    if (rc) return rc;
     W->scene_off = {0, 0};
     *out = W;
     return AVBD_OK;
@@ -1506,6 +1609,52 @@ int avbd_world_add_hull(AvbdWorld* W, const float* verts, uint32_t nv, const uin
 // PhysicsEngine::remove_body (mod.rs:1241-1300) on a one-scene world.
 // AvbdEngine::wake_body (mod.rs:833-842) with RigidBody::wake_restore
 // (body.rs:412-418) on the host model: a sleeper's mass and inertia return.
+// A revolute joint's twist or a prismatic joint's slide from its assembly
+// reference (joints_ext.rs:37-51), from the host's body records.
+static float joint_coordinate_host(const AvbdWorld* W, const JointRec& r) {
+    using namespace avbd;
+    const AvbdBody& ba = W->bodies[r.a];
+    const AvbdBody& bb = W->bodies[r.b];
+    const Q qa{ba.orientation[0], ba.orientation[1], ba.orientation[2], ba.orientation[3]};
+    const Q qb{bb.orientation[0], bb.orientation[1], bb.orientation[2], bb.orientation[3]};
+    const V3 axis{r.axa[0], r.axa[1], r.axa[2]};
+    if (r.kind == AVBD_JOINT_REVOLUTE) return hinge_twist(qa, qb, axis) - r.ref;
+    const V3 wa = normalize_or(qrot(qa, axis), VZ());
+    const V3 pa = V3{ba.position[0], ba.position[1], ba.position[2]} + qrot(qa, V3{r.la[0], r.la[1], r.la[2]});
+    const V3 pb = V3{bb.position[0], bb.position[1], bb.position[2]} + qrot(qb, V3{r.lb[0], r.lb[1], r.lb[2]});
+    return dot(pb - pa, wa) - r.refv;
+}
+
+// retain_joints (mod.rs:766-784) with joint_remap (migration.rs:74-115):
+// the joints marked gone go, a gear whose coupled joint goes goes too, the
+// survivors move down and gears follow their joints' new handles.
+static void retain_joints(AvbdWorld* W, std::vector<uint8_t> gone) {
+    std::vector<JointRec>& js = W->joints;
+    for (bool changed = true; changed;) {
+        changed = false;
+        for (size_t i = 0; i < js.size(); i++)
+            if (!gone[i] && js[i].kind == AVBD_JOINT_GEAR && (gone[js[i].gb[0]] || gone[js[i].gb[1]])) {
+                gone[i] = 1;
+                changed = true;
+            }
+    }
+    std::vector<uint32_t> remap(js.size(), 0u);
+    uint32_t next = 0;
+    for (size_t i = 0; i < js.size(); i++) remap[i] = gone[i] ? 0u : next++;
+    std::vector<JointRec> kept;
+    kept.reserve(next);
+    for (size_t i = 0; i < js.size(); i++) {
+        if (gone[i]) continue;
+        JointRec j = js[i];
+        if (j.kind == AVBD_JOINT_GEAR) {
+            j.gb[0] = remap[j.gb[0]];
+            j.gb[1] = remap[j.gb[1]];
+        }
+        kept.push_back(j);
+    }
+    js.swap(kept);
+}
+
 static void wake_host(AvbdWorld* W, uint32_t h) {
     AvbdBodyAux& a = W->aux[h];
     if (!a.asleep) return;
@@ -1581,14 +1730,13 @@ int avbd_world_remove_body(AvbdWorld* W, uint32_t hi) {
     }
     W->pairs.swap(pairs);
     W->points.swap(points);
-    std::vector<JointRec> joints;
-    for (JointRec j : W->joints) {
-        if (j.a == hi || j.b == hi) continue;
+    std::vector<uint8_t> gone(W->joints.size(), 0);
+    for (size_t i = 0; i < W->joints.size(); i++) gone[i] = W->joints[i].a == hi || W->joints[i].b == hi;
+    retain_joints(W, std::move(gone));
+    for (JointRec& j : W->joints) {
         j.a = map(j.a);
         j.b = map(j.b);
-        joints.push_back(j);
     }
-    W->joints.swap(joints);
     // every sleeper wakes (mod.rs:1294-1296, body.rs:412-418)
     for (uint32_t h = 0; h < last; h++) wake_host(W, h);
     W->scene_off.back() = last;
@@ -1605,7 +1753,9 @@ int avbd_world_remove_joint(AvbdWorld* W, uint32_t handle) {
     // (mod.rs:1531-1540, retain_joints mod.rs:766-784)
     wake_host(W, W->joints[handle].a);
     wake_host(W, W->joints[handle].b);
-    W->joints.erase(W->joints.begin() + handle);
+    std::vector<uint8_t> gone(W->joints.size(), 0);
+    gone[handle] = 1;
+    retain_joints(W, std::move(gone));
     return AVBD_OK;
 }
 
@@ -1624,10 +1774,12 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     // ordered, motor fields finite, a rope longer than zero
     auto finite3 = [](const float* v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); };
     auto bounds_ok = [](float lo, float hi) { return std::isfinite(lo) && std::isfinite(hi) && lo <= hi; };
-    if (d->kind > AVBD_JOINT_WHEEL) return AVBD_ERR_UNSUPPORTED;
-    const bool motor = d->kind == AVBD_JOINT_MOTOR;
+    if (d->kind > AVBD_JOINT_GEAR) return AVBD_ERR_UNSUPPORTED;
+    const bool motor = d->kind == AVBD_JOINT_MOTOR, gear = d->kind == AVBD_JOINT_GEAR;
+    // a gear is checked for its ratio alone (migration.rs:193-200)
+    if (gear && !std::isfinite(d->gear_ratio)) return AVBD_ERR_JOINT_NONFINITE;
     // a free motor has no anchors (migration.rs:250-252); its drive is checked instead (:331-356)
-    if (!motor && (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b))) return AVBD_ERR_JOINT_BAD_AXIS;
+    if (!motor && !gear && (!finite3(d->local_anchor_a) || !finite3(d->local_anchor_b))) return AVBD_ERR_JOINT_BAD_AXIS;
     if (motor) {
         if (!finite3(d->motor_linear) || !finite3(d->motor_angular)) return AVBD_ERR_JOINT_NONFINITE;
         if (!(std::isfinite(d->motor_max_force) && d->motor_max_force >= 0.0f)) return AVBD_ERR_JOINT_NONFINITE;
@@ -1683,6 +1835,32 @@ int avbd_world_add_joint(AvbdWorld* W, const AvbdJointDesc* d, uint32_t* handle)
     j.kind = d->kind;
     j.a = d->body_a;
     j.b = d->body_b;
+    if (gear) {
+        // mod.rs:1329-1404: the coupled joints exist and are hinges or
+        // slides; the constant is their coordinates' combination now
+        const uint32_t ja = d->gear_joint_a, jb = d->gear_joint_b;
+        if (ja >= W->joints.size() || jb >= W->joints.size()) return AVBD_ERR_JOINT_UNKNOWN_REF;
+        for (uint32_t r : {ja, jb})
+            if (W->joints[r].kind != AVBD_JOINT_REVOLUTE && W->joints[r].kind != AVBD_JOINT_PRISMATIC)
+                return AVBD_ERR_UNSUPPORTED;
+        // and all its bodies live in the gear's scene
+        for (uint32_t r : {ja, jb})
+            if (scene_of(W->joints[r].a) != scene_of(d->body_a)) return AVBD_ERR_JOINT_HANDLES;
+        j.axa[0] = 1.0f; j.axb[0] = 1.0f;
+        j.bxa[0] = 1.0f; j.bxb[0] = 1.0f;
+        j.qref[3] = 1.0f;
+        j.gb[0] = ja;
+        j.gb[1] = jb;
+        j.gratio = d->gear_ratio;
+        j.refv = joint_coordinate_host(W, W->joints[ja]) + j.gratio * joint_coordinate_host(W, W->joints[jb]);
+        for (int k = 0; k < 3; k++) {
+            j.st.pen_l[k] = 1.0f;  // JOINT_PENALTY_INIT
+            j.st.pen_a[k] = 1.0f;
+        }
+        W->joints.push_back(j);
+        if (handle) *handle = (uint32_t)(W->joints.size() - 1);
+        return AVBD_OK;
+    }
     if (!motor) {
         std::memcpy(j.la, d->local_anchor_a, 12);
         std::memcpy(j.lb, d->local_anchor_b, 12);
@@ -2229,6 +2407,7 @@ int avbd_world_profile_substep(AvbdWorld* W, float* ms, uint32_t* info) {
     CK(cudaEventRecord(ev[0], st));
     launch_begin_substep(w, st);
     launch_wake_joint_motion(w, st);
+    launch_gear_mem(w, st);
     launch_torque(w, st);
     CK(cudaEventRecord(ev[1], st));
     launch_broadphase(w, W->plan, st);
@@ -2515,6 +2694,434 @@ int avbd_adjoint_backward(AvbdWorld* W, const float* grad_final, float* grad_ini
         }
     }
     return snap_restore(W, t->fin);
+}
+
+}  // extern "C"
+
+// ---- on-disk snapshot ---------------------------------------------------------------
+// A whole world as bytes: a fixed 128-byte header, then the payload sections
+// in the order snap_payload writes them.  The header's record sizes tie the
+// payload to this format version (JointRec is stored as the world holds it,
+// its assembly references already resolved: re-admitting the joints at the
+// saved poses would resolve them again from other poses).
+namespace {
+
+constexpr char SNAP_MAGIC[8] = {'O', 'R', 'N', 'A', 'V', 'B', 'D', '\0'};
+constexpr uint32_t SNAP_ENDIAN = 0x01020304u;
+
+struct SnapHeader {
+    char magic[8];
+    uint32_t format, abi, header_bytes, endian;
+    uint32_t rec[10];  // record sizes: params, settings, body, aux, pair, point, joint, contact event,
+                       // trigger event; points per pair
+    uint32_t cnt[10];  // bodies, scenes, pairs, joints, hulls, touching pairs, trigger overlaps,
+                       // queued contact events, queued trigger events, event words
+    uint64_t bytes, checksum, substeps;
+};
+static_assert(sizeof(SnapHeader) == 128, "the snapshot header is 128 bytes");
+
+// The world's settings that change what a step computes or reports.
+struct SnapSettings {
+    int32_t primal_lanes, primal_block, primal_minb, small_scene_max, sweep_rows, fast, sort_work;
+    int32_t ev_period, sort_static;
+    float joint_k, time_debt;
+    uint32_t reserved;
+};
+static_assert(sizeof(SnapSettings) == 48, "settings record");
+// Format 1 stores the joint record as the world holds it: a change of its
+// layout is a new format version.
+static_assert(sizeof(JointRec) == 364, "format 1 joint record");
+
+// The event state a snapshot carries.
+struct SnapEvents {
+    uint32_t evs[EV_NUM] = {};
+    std::vector<uint32_t> tof, tkeys;         // previous touch set (CSR by the higher handle)
+    std::vector<unsigned long long> trig;     // previous trigger overlaps, (b << 32 | a)
+    std::vector<AvbdContactEvent> ce;         // undrained queues
+    std::vector<AvbdTriggerEvent> te;
+};
+
+// FNV-1a, 64-bit (Fowler, Noll, Vo): offset basis 14695981039346656037,
+// prime 1099511628211, one byte at a time.
+uint64_t fnv1a64(const uint8_t* p, uint64_t n) {
+    uint64_t h = 14695981039346656037ull;
+    for (uint64_t i = 0; i < n; i++) {
+        h ^= p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+struct SnapOut {  // counts when p is null
+    uint8_t* p = nullptr;
+    uint64_t n = 0;
+    void put(const void* src, uint64_t bytes) {
+        if (p && bytes) std::memcpy(p + n, src, bytes);
+        n += bytes;
+    }
+    template <class T> void vec(const std::vector<T>& v) { put(v.data(), v.size() * sizeof(T)); }
+};
+
+struct SnapIn {
+    const uint8_t* p;
+    uint64_t n, at = 0;
+    bool ok = true;
+    bool get(void* dst, uint64_t bytes) {
+        if (!ok || bytes > n - at) return ok = false;
+        if (bytes) std::memcpy(dst, p + at, bytes);
+        at += bytes;
+        return true;
+    }
+    template <class T> bool vec(std::vector<T>& v, uint64_t count) {
+        if (!ok || count > (n - at) / sizeof(T)) return ok = false;
+        v.resize(count);
+        return get(v.data(), count * sizeof(T));
+    }
+};
+
+void snap_records(SnapHeader& h) {
+    const uint32_t rec[10] = {sizeof(AvbdParams), sizeof(SnapSettings), sizeof(AvbdBody), sizeof(AvbdBodyAux),
+                              sizeof(AvbdPairState), sizeof(AvbdPointState), sizeof(JointRec),
+                              sizeof(AvbdContactEvent), sizeof(AvbdTriggerEvent), (uint32_t)MAX_PTS};
+    std::memcpy(h.rec, rec, sizeof(rec));
+}
+
+// Header checks shared by every reader: magic, format, layout, size, checksum.
+int snap_check(const void* buf, uint64_t size, SnapHeader& h) {
+    if (!buf) return AVBD_ERR_INVALID_ARG;
+    if (size < sizeof(SnapHeader)) return AVBD_ERR_FORMAT;
+    std::memcpy(&h, buf, sizeof(h));
+    SnapHeader want{};
+    snap_records(want);
+    if (std::memcmp(h.magic, SNAP_MAGIC, 8) || h.endian != SNAP_ENDIAN || h.format != AVBD_SNAPSHOT_FORMAT ||
+        h.header_bytes != sizeof(SnapHeader) || std::memcmp(h.rec, want.rec, sizeof(want.rec)) ||
+        h.cnt[9] != EV_NUM || h.bytes != size)
+        return AVBD_ERR_FORMAT;
+    const uint8_t* p = (const uint8_t*)buf;
+    if (fnv1a64(p + sizeof(h), size - sizeof(h)) != h.checksum) return AVBD_ERR_FORMAT;
+    return AVBD_OK;
+}
+
+// The event state of a world: empty while it has no device arrays.
+int snap_capture_events(AvbdWorld* W, SnapEvents& e) {
+    const uint32_t N = (uint32_t)W->bodies.size();
+    e.tof.assign(N + 1, 0);
+    if (!W->w.evs) return AVBD_OK;
+    CK(cudaStreamSynchronize(W->st));
+    read_touch_set(W, N, e.tof, e.tkeys);
+    if (e.tof.size() != N + 1) e.tof.assign(N + 1, 0);
+    CK(cudaMemcpy(e.evs, W->w.evs, sizeof(e.evs), cudaMemcpyDeviceToHost));
+    const uint32_t nt = std::min<uint32_t>(e.evs[EV_TRIG_PREV], TRIG_CAP);
+    const uint32_t nce = std::min<uint32_t>(e.evs[EV_N], W->w.ev_cap);
+    const uint32_t nte = std::min<uint32_t>(e.evs[EV_TN], W->w.tev_cap);
+    e.trig.resize(nt);
+    e.ce.resize(nce);
+    e.te.resize(nte);
+    if (nt) CK(cudaMemcpy(e.trig.data(), W->w.trig_prev, nt * 8ull, cudaMemcpyDeviceToHost));
+    if (nce) CK(cudaMemcpy(e.ce.data(), W->w.ev, nce * sizeof(AvbdContactEvent), cudaMemcpyDeviceToHost));
+    if (nte) CK(cudaMemcpy(e.te.data(), W->w.tev, nte * sizeof(AvbdTriggerEvent), cudaMemcpyDeviceToHost));
+    // the keys are written back into the first key buffer; scratch words cleared
+    e.evs[EV_PAR] = 0;
+    e.evs[EV_TRIG_NOW] = 0;
+    e.evs[EV_TRIG_PREV] = nt;
+    e.evs[EV_N] = nce;
+    e.evs[EV_TN] = nte;
+    for (int k = EV_TRIG_OVF + 1; k < EV_NUM; k++) e.evs[k] = 0;
+    return AVBD_OK;
+}
+
+void snap_payload(const AvbdWorld* W, const SnapEvents& e, SnapOut& o) {
+    SnapSettings s{};
+    s.primal_lanes = W->tune.primal_lanes;
+    s.primal_block = W->tune.primal_block;
+    s.primal_minb = W->tune.primal_minb;
+    s.small_scene_max = W->tune.small_scene_max;
+    s.sweep_rows = W->tune.sweep_rows;
+    s.fast = W->tune.fast;
+    s.sort_work = W->tune.sort_work;
+    s.ev_period = W->ev_period;
+    s.sort_static = W->w.sort_static;
+    s.joint_k = W->w.joint_k;
+    s.time_debt = W->time_debt;
+    o.put(&W->prm, sizeof(AvbdParams));
+    o.put(&s, sizeof(s));
+    o.vec(W->scene_off);
+    o.vec(W->bodies);
+    o.vec(W->aux);
+    o.vec(W->pairs);
+    o.vec(W->points);
+    o.vec(W->joints);
+    for (const HostHull& hh : W->hulls) {
+        const uint32_t nv = (uint32_t)hh.v.size(), nf = (uint32_t)hh.f.size();
+        o.put(&nv, 4);
+        o.put(&nf, 4);
+        o.put(hh.unit_inertia, 12);
+        o.put(&hh.bound, 4);
+        o.put(&hh.min_ext, 4);
+        o.vec(hh.v);
+        o.vec(hh.f);
+    }
+    o.put(e.evs, sizeof(e.evs));
+    o.vec(e.tof);
+    o.vec(e.tkeys);
+    o.vec(e.trig);
+    o.vec(e.ce);
+    o.vec(e.te);
+}
+
+// Everything a loaded world's host model needs, checked before any device
+// work: every index the device will follow stays inside its array.
+int snap_parse(const void* buf, uint64_t size, AvbdWorld* W, SnapEvents& e) {
+    SnapHeader h;
+    int rc = snap_check(buf, size, h);
+    if (rc) return rc;
+    const uint32_t N = h.cnt[0], S = h.cnt[1], P = h.cnt[2], J = h.cnt[3], H = h.cnt[4];
+    SnapIn in{(const uint8_t*)buf, size, sizeof(SnapHeader)};
+    SnapSettings s{};
+    in.get(&W->prm, sizeof(AvbdParams));
+    in.get(&s, sizeof(s));
+    in.vec(W->scene_off, (uint64_t)S + 1);
+    in.vec(W->bodies, N);
+    in.vec(W->aux, N);
+    in.vec(W->pairs, P);
+    in.vec(W->points, (uint64_t)P * MAX_PTS);
+    in.vec(W->joints, J);
+    for (uint32_t k = 0; k < H && in.ok; k++) {
+        HostHull hh;
+        uint32_t nv = 0, nf = 0;
+        in.get(&nv, 4);
+        in.get(&nf, 4);
+        in.get(hh.unit_inertia, 12);
+        in.get(&hh.bound, 4);
+        in.get(&hh.min_ext, 4);
+        in.vec(hh.v, nv);
+        in.vec(hh.f, nf);
+        if (!in.ok || nv == 0 || nf % 3) return AVBD_ERR_FORMAT;
+        for (uint32_t x : hh.f)
+            if (x >= nv) return AVBD_ERR_FORMAT;
+        W->hulls.push_back(std::move(hh));
+    }
+    in.get(e.evs, sizeof(e.evs));
+    in.vec(e.tof, (uint64_t)N + 1);
+    in.vec(e.tkeys, h.cnt[5]);
+    in.vec(e.trig, h.cnt[6]);
+    in.vec(e.ce, h.cnt[7]);
+    in.vec(e.te, h.cnt[8]);
+    if (!in.ok || in.at != size) return AVBD_ERR_FORMAT;
+    // parameters and settings as the setters would accept them
+    const AvbdParams& p = W->prm;
+    if (!(p.step_dt > 0.0f) || !std::isfinite(p.step_dt) || p.iterations < 0 || p.max_substeps < 1)
+        return AVBD_ERR_FORMAT;
+    const int lanes_ok[] = {AVBD_PRIMAL_SCENES, 0, 1, 4, 8, 16, 32};
+    if (std::find(std::begin(lanes_ok), std::end(lanes_ok), s.primal_lanes) == std::end(lanes_ok) ||
+        s.primal_block < 32 || s.primal_block > 1024 || s.primal_block % 32 ||
+        (s.primal_lanes == 1 && s.primal_block > 128) ||
+        (s.primal_lanes == AVBD_PRIMAL_SCENES && s.primal_block != 128 && s.primal_block != 256 &&
+         s.primal_block != 512) ||
+        (s.primal_minb != 4 && s.primal_minb != 6 && s.primal_minb != 8) || s.small_scene_max < 0 ||
+        s.small_scene_max > 2048 || (s.sweep_rows != 0 && s.sweep_rows != 1) || !std::isfinite(s.joint_k) ||
+        s.joint_k < 0.0f || !std::isfinite(s.time_debt))
+        return AVBD_ERR_FORMAT;
+    W->tune.primal_lanes = s.primal_lanes;
+    W->tune.primal_block = s.primal_block;
+    W->tune.primal_minb = s.primal_minb;
+    W->tune.small_scene_max = s.small_scene_max;
+    W->tune.sweep_rows = s.sweep_rows;
+    W->tune.fast = s.fast ? 1 : 0;
+    W->tune.sort_work = s.sort_work ? 1 : 0;
+    W->ev_period = s.ev_period < 0 ? -1 : s.ev_period;
+    W->w.sort_static = s.sort_static ? 1 : 0;
+    W->w.joint_k = s.joint_k;
+    W->time_debt = s.time_debt;
+    W->cum.steps = h.substeps;
+    // scenes, bodies, pairs, joints
+    if (S == 0 || W->scene_off[0] != 0 || W->scene_off[S] != N) return AVBD_ERR_FORMAT;
+    for (uint32_t k = 0; k < S; k++)
+        if (W->scene_off[k + 1] < W->scene_off[k]) return AVBD_ERR_FORMAT;
+    auto scene_of = [&](uint32_t x) {
+        return (uint32_t)(std::upper_bound(W->scene_off.begin(), W->scene_off.end(), x) - W->scene_off.begin()) - 1;
+    };
+    for (const AvbdBody& b : W->bodies) {
+        if (!body_finite(b)) return AVBD_ERR_FORMAT;
+        if (b.shape == AVBD_SHAPE_HULL && !((size_t)b.shape_params[0] < W->hulls.size())) return AVBD_ERR_FORMAT;
+    }
+    for (const AvbdPairState& q : W->pairs)
+        if (q.a >= q.b || q.b >= N || q.npoints > (uint32_t)MAX_PTS || scene_of(q.a) != scene_of(q.b))
+            return AVBD_ERR_FORMAT;
+    for (const JointRec& j : W->joints) {
+        if (j.kind > AVBD_JOINT_GEAR || j.a >= N || j.b >= N || j.a == j.b || scene_of(j.a) != scene_of(j.b))
+            return AVBD_ERR_FORMAT;
+        if (j.kind != AVBD_JOINT_GEAR) continue;
+        for (uint32_t r : j.gb)
+            if (r >= J || (W->joints[r].kind != AVBD_JOINT_REVOLUTE && W->joints[r].kind != AVBD_JOINT_PRISMATIC) ||
+                scene_of(W->joints[r].a) != scene_of(j.a))
+                return AVBD_ERR_FORMAT;
+    }
+    // event state: a CSR over the bodies, each row's lower handles ascending
+    if (e.tof[0] != 0 || e.tof[N] != e.tkeys.size()) return AVBD_ERR_FORMAT;
+    for (uint32_t b = 0; b < N; b++) {
+        if (e.tof[b + 1] < e.tof[b]) return AVBD_ERR_FORMAT;
+        for (uint32_t k = e.tof[b]; k < e.tof[b + 1]; k++)
+            if (e.tkeys[k] >= b || (k > e.tof[b] && e.tkeys[k] <= e.tkeys[k - 1])) return AVBD_ERR_FORMAT;
+    }
+    if (e.trig.size() > (size_t)TRIG_CAP) return AVBD_ERR_FORMAT;
+    for (size_t k = 0; k < e.trig.size(); k++) {
+        const unsigned long long t = e.trig[k];
+        if ((uint32_t)(t >> 32) >= N || (uint32_t)t >= (uint32_t)(t >> 32) || (k && t <= e.trig[k - 1]))
+            return AVBD_ERR_FORMAT;
+    }
+    if (e.evs[EV_N] != e.ce.size() || e.evs[EV_TN] != e.te.size() || e.evs[EV_TRIG_PREV] != e.trig.size() ||
+        e.evs[EV_PAR] != 0)
+        return AVBD_ERR_FORMAT;
+    return AVBD_OK;
+}
+
+// Put a parsed event state into a world whose device arrays were just made.
+int snap_restore_events(AvbdWorld* W, const SnapEvents& e) {
+    DW& w = W->w;
+    const uint32_t N = (uint32_t)W->bodies.size();
+    if (!w.evs) return (e.tkeys.empty() && e.trig.empty() && e.ce.empty() && e.te.empty()) ? AVBD_OK : AVBD_ERR_FORMAT;
+    if (e.ce.size() > w.ev_cap || e.te.size() > w.tev_cap || e.tkeys.size() > W->cand_cap || (uint32_t)w.N != N)
+        return AVBD_ERR_FORMAT;
+    CK(cudaStreamSynchronize(W->st));
+    CK(cudaMemcpy(w.evs, e.evs, sizeof(e.evs), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.toff, e.tof.data(), ((size_t)N + 1) * 4, cudaMemcpyHostToDevice));
+    if (!e.tkeys.empty()) CK(cudaMemcpy(w.tk0, e.tkeys.data(), e.tkeys.size() * 4, cudaMemcpyHostToDevice));
+    if (!e.trig.empty()) CK(cudaMemcpy(w.trig_prev, e.trig.data(), e.trig.size() * 8, cudaMemcpyHostToDevice));
+    if (!e.ce.empty())
+        CK(cudaMemcpy(w.ev, e.ce.data(), e.ce.size() * sizeof(AvbdContactEvent), cudaMemcpyHostToDevice));
+    if (!e.te.empty())
+        CK(cudaMemcpy(w.tev, e.te.data(), e.te.size() * sizeof(AvbdTriggerEvent), cudaMemcpyHostToDevice));
+    return AVBD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int avbd_snapshot_info(const void* buf, uint64_t size, AvbdSnapshotInfo* info) {
+    if (!info) return AVBD_ERR_INVALID_ARG;
+    SnapHeader h;
+    int rc = snap_check(buf, size, h);
+    if (rc) return rc;
+    {
+        // every check a load makes on the host, the contents included
+        AvbdWorld probe;
+        SnapEvents e;
+        rc = snap_parse(buf, size, &probe, e);
+        if (rc) return rc;
+    }
+    std::memset(info, 0, sizeof(*info));
+    info->format = h.format;
+    info->abi = h.abi;
+    info->nbodies = h.cnt[0];
+    info->nscenes = h.cnt[1];
+    info->npairs = h.cnt[2];
+    info->njoints = h.cnt[3];
+    info->nhulls = h.cnt[4];
+    info->ntouch = h.cnt[5];
+    info->ntrigger = h.cnt[6];
+    info->ncontact_events = h.cnt[7];
+    info->ntrigger_events = h.cnt[8];
+    info->bytes = h.bytes;
+    info->substeps = h.substeps;
+    return AVBD_OK;
+}
+
+int avbd_world_snapshot(AvbdWorld* W, void* buf, uint64_t cap, uint64_t* size) {
+    if (!W || !size) return AVBD_ERR_INVALID_ARG;
+    cudaSetDevice(W->device);
+    int rc = download_all(W);
+    if (rc) return rc;
+    SnapEvents e;
+    rc = snap_capture_events(W, e);
+    if (rc) return rc;
+    SnapOut count;
+    snap_payload(W, e, count);
+    *size = sizeof(SnapHeader) + count.n;
+    if (!buf) return AVBD_OK;
+    if (cap < *size) return AVBD_ERR_CAPACITY;
+    SnapHeader h{};
+    std::memcpy(h.magic, SNAP_MAGIC, 8);
+    h.format = AVBD_SNAPSHOT_FORMAT;
+    h.abi = AVBD_ABI_VERSION;
+    h.header_bytes = sizeof(SnapHeader);
+    h.endian = SNAP_ENDIAN;
+    snap_records(h);
+    const uint32_t cnt[10] = {(uint32_t)W->bodies.size(), (uint32_t)W->scene_off.size() - 1,
+                              (uint32_t)W->pairs.size(), (uint32_t)W->joints.size(), (uint32_t)W->hulls.size(),
+                              (uint32_t)e.tkeys.size(), (uint32_t)e.trig.size(), (uint32_t)e.ce.size(),
+                              (uint32_t)e.te.size(), (uint32_t)EV_NUM};
+    std::memcpy(h.cnt, cnt, sizeof(cnt));
+    h.bytes = *size;
+    h.substeps = W->cum.steps;
+    uint8_t* p = (uint8_t*)buf;
+    SnapOut out{p + sizeof(SnapHeader), 0};
+    snap_payload(W, e, out);
+    h.checksum = fnv1a64(p + sizeof(SnapHeader), out.n);
+    std::memcpy(p, &h, sizeof(h));
+    return AVBD_OK;
+}
+
+int avbd_world_from_snapshot(const void* buf, uint64_t size, int device, AvbdWorld** out) {
+    if (!buf || !out) return AVBD_ERR_INVALID_ARG;
+    // the whole snapshot is checked on the host before any device work
+    AvbdWorld* W = new AvbdWorld();
+    SnapEvents e;
+    int rc = snap_parse(buf, size, W, e);
+    if (rc) {
+        delete W;
+        return rc;
+    }
+    rc = open_device(W, device);
+    if (rc) return rc;
+    if (!W->bodies.empty()) {
+        // room for the saved touch set in the key buffers
+        W->cand_cap = std::max<uint32_t>(W->cand_cap, (uint32_t)e.tkeys.size() + 1024u);
+        rc = upload_all(W);
+        if (!rc) rc = snap_restore_events(W, e);
+    } else {
+        rc = snap_restore_events(W, e);
+    }
+    if (rc) {
+        avbd_world_destroy(W);
+        return rc;
+    }
+    *out = W;
+    return AVBD_OK;
+}
+
+int avbd_world_save(AvbdWorld* W, const char* path) {
+    if (!W || !path) return AVBD_ERR_INVALID_ARG;
+    uint64_t n = 0;
+    int rc = avbd_world_snapshot(W, nullptr, 0, &n);
+    if (rc) return rc;
+    std::vector<uint8_t> buf(n);
+    rc = avbd_world_snapshot(W, buf.data(), n, &n);
+    if (rc) return rc;
+    std::string tmp = std::string(path) + ".partial";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return AVBD_ERR_IO;
+    const bool ok = std::fwrite(buf.data(), 1, n, f) == n;
+    if (std::fclose(f) != 0 || !ok || std::rename(tmp.c_str(), path) != 0) {
+        std::remove(tmp.c_str());
+        return AVBD_ERR_IO;
+    }
+    return AVBD_OK;
+}
+
+int avbd_world_load(const char* path, int device, AvbdWorld** out) {
+    if (!path || !out) return AVBD_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return AVBD_ERR_IO;
+    std::vector<uint8_t> buf;
+    uint8_t chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+    const bool err = std::ferror(f) != 0;
+    std::fclose(f);
+    if (err) return AVBD_ERR_IO;
+    return avbd_world_from_snapshot(buf.data(), buf.size(), device, out);
 }
 
 }  // extern "C"

@@ -164,7 +164,16 @@ struct DW {
     uint32_t* j_cfg;          // sixdof axis configuration: 2 bits per axis, linear x y z then angular
     float4* j_six;            // 3 per joint: (min, max) of the six axes in pairs
     float4* j_sacc;           // 2 per joint: sixdof limited-axis forces (6 used)
-    const uint32_t *jofs, *jlist;  // per-body joint adjacency (N+1, 2J)
+    // gears (j_dref.x = ratio, j_ref.x = the constant): the coupled joints,
+    // their coordinates at the last step start (raw a, raw b, unwrapped a,
+    // unwrapped b) and whether those are set yet
+    uint2* j_gb;
+    float4* j_gmem;
+    uint32_t* j_gset;
+    int n_gear;
+    // per-body joint adjacency (N+1; 4J): a joint on its two bodies, a gear
+    // once on each body of its coupled joints, ascending joint index
+    const uint32_t *jofs, *jlist;
     // joints with a motor or a rope, per scene in joint order (their velocity
     // impulses run before the warm start); n_imp of them in all
     const uint32_t *jimp_off, *jimp_list;

@@ -1,6 +1,6 @@
 //! Raw declarations of `include/ornis_avbd.h`: `#[repr(C)]` mirrors of its
 //! records (same field order and sizes; `AvbdBody` is 136 bytes,
-//! `AvbdJointDesc` 256) and its
+//! `AvbdJointDesc` 272, `AvbdJointState` 100) and its
 //! `extern "C"` entry points.  Every function returns an `i32` status: 0 or a
 //! negative `AVBD_ERR_*` code.
 
@@ -13,11 +13,18 @@ pub const AVBD_ERR_DEVICE: i32 = -3;
 pub const AVBD_ERR_TIMEOUT: i32 = -4;
 pub const AVBD_ERR_NONFINITE: i32 = -5;
 pub const AVBD_ERR_UNSUPPORTED: i32 = -6;
+pub const AVBD_ERR_FORMAT: i32 = -7;
+pub const AVBD_ERR_IO: i32 = -8;
+pub const AVBD_SNAPSHOT_FORMAT: u32 = 1;
+pub const AVBD_STATIC_MAX_BODIES: u32 = 128;
+pub const AVBD_STATIC_PAIR_CAP: u32 = 2048;
+pub const AVBD_STATIC_SCRATCH_BYTES: u32 = 3481600;
 pub const AVBD_ERR_JOINT_SELF: i32 = -10;
 pub const AVBD_ERR_JOINT_HANDLES: i32 = -11;
 pub const AVBD_ERR_JOINT_BAD_AXIS: i32 = -12;
 pub const AVBD_ERR_JOINT_NONFINITE: i32 = -13;
 pub const AVBD_ERR_JOINT_BAD_BOUNDS: i32 = -14;
+pub const AVBD_ERR_JOINT_UNKNOWN_REF: i32 = -15;
 
 pub const AVBD_SHAPE_SPHERE: u32 = 0;
 pub const AVBD_SHAPE_BOX: u32 = 1;
@@ -42,6 +49,7 @@ pub const AVBD_JOINT_SIXDOF: u32 = 6;
 pub const AVBD_JOINT_MOTOR: u32 = 7;
 pub const AVBD_JOINT_SPRING: u32 = 8;
 pub const AVBD_JOINT_WHEEL: u32 = 9;
+pub const AVBD_JOINT_GEAR: u32 = 10;
 pub const AVBD_MOTOR_VELOCITY: u32 = 0;
 pub const AVBD_MOTOR_POSITION: u32 = 1;
 pub const AVBD_MOTOR_SERVO: u32 = 2;
@@ -51,7 +59,7 @@ pub const AVBD_MODEL_FORCE: u32 = 1;
 pub const AVBD_AXIS_FREE: u32 = 0;
 pub const AVBD_AXIS_LOCKED: u32 = 1;
 pub const AVBD_AXIS_LIMITED: u32 = 2;
-pub const AVBD_ABI_VERSION: i32 = 3;
+pub const AVBD_ABI_VERSION: i32 = 4;
 
 pub const AVBD_MAX_POINTS: usize = 8;
 pub const AVBD_PRIMAL_SCENES: i32 = -1;
@@ -123,6 +131,11 @@ pub struct AvbdJointDesc {
     pub local_axle_b: [f32; 3],
     pub suspension_hz: f32,
     pub suspension_damping: f32,
+    /// gear (`JointKind::Gear`): the coupled joints and the ratio
+    pub gear_joint_a: u32,
+    pub gear_joint_b: u32,
+    pub gear_ratio: f32,
+    pub reserved: u32,
 }
 
 #[repr(C)]
@@ -178,6 +191,10 @@ pub struct AvbdJointState {
     pub acc_lim: f32,
     pub lim_dual: f32,
     pub sacc: [f32; 6],
+    /// gear: the coupled joints' coordinates at the last step start
+    pub gear_raw: [f32; 2],
+    pub gear_cont: [f32; 2],
+    pub gear_mem_set: u32,
 }
 
 #[repr(C)]
@@ -211,6 +228,26 @@ pub struct AvbdTriggerEvent {
     pub body_a: u32,
     pub body_b: u32,
     pub entered: u32,
+}
+
+/// What `avbd_snapshot_info` reports about a snapshot.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct AvbdSnapshotInfo {
+    pub format: u32,
+    pub abi: u32,
+    pub nbodies: u32,
+    pub nscenes: u32,
+    pub npairs: u32,
+    pub njoints: u32,
+    pub nhulls: u32,
+    pub ntouch: u32,
+    pub ntrigger: u32,
+    pub ncontact_events: u32,
+    pub ntrigger_events: u32,
+    pub reserved: u32,
+    pub bytes: u64,
+    pub substeps: u64,
 }
 
 /// Opaque world handle.
@@ -275,6 +312,11 @@ extern "C" {
         npairs: u32,
         joints: *const AvbdJointState,
     ) -> i32;
+    pub fn avbd_world_snapshot(world: *mut AvbdWorld, buf: *mut u8, cap: u64, size: *mut u64) -> i32;
+    pub fn avbd_world_from_snapshot(buf: *const u8, size: u64, device: i32, out: *mut *mut AvbdWorld) -> i32;
+    pub fn avbd_snapshot_info(buf: *const u8, size: u64, info: *mut AvbdSnapshotInfo) -> i32;
+    pub fn avbd_world_save(world: *mut AvbdWorld, path: *const std::os::raw::c_char) -> i32;
+    pub fn avbd_world_load(path: *const std::os::raw::c_char, device: i32, out: *mut *mut AvbdWorld) -> i32;
     pub fn avbd_world_get_colours(world: *mut AvbdWorld, colours: *mut i32, n: u32) -> i32;
     pub fn avbd_body_init(out: *mut AvbdBody, shape: u32, params: *const f32, position: *const f32, mass: f32) -> i32;
     pub fn avbd_set_tuning(world: *mut AvbdWorld, primal_lanes: i32, primal_block: i32) -> i32;

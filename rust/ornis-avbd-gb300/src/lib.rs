@@ -28,6 +28,11 @@ pub enum Error {
     Timeout,
     NonFinite,
     Unsupported,
+    /// Not an intact snapshot of this format version (the reference's
+    /// `SnapshotError::VersionMismatch`, snapshot.rs:815-830, and damage).
+    Format,
+    /// A snapshot file could not be read or written.
+    Io,
     /// `JointError::SelfJoint` (avbd/mod.rs:1323-1328)
     JointSelf,
     /// `JointError::InvalidHandles`
@@ -38,6 +43,8 @@ pub enum Error {
     JointNonFinite,
     /// `JointError::BadBounds`
     JointBadBounds,
+    /// `JointError::UnknownRef` (a gear's coupled joint does not exist)
+    JointUnknownRef,
     Other(i32),
 }
 
@@ -51,11 +58,14 @@ impl Error {
             AVBD_ERR_TIMEOUT => Error::Timeout,
             AVBD_ERR_NONFINITE => Error::NonFinite,
             AVBD_ERR_UNSUPPORTED => Error::Unsupported,
+            AVBD_ERR_FORMAT => Error::Format,
+            AVBD_ERR_IO => Error::Io,
             AVBD_ERR_JOINT_SELF => Error::JointSelf,
             AVBD_ERR_JOINT_HANDLES => Error::JointHandles,
             AVBD_ERR_JOINT_BAD_AXIS => Error::JointBadAxis,
             AVBD_ERR_JOINT_NONFINITE => Error::JointNonFinite,
             AVBD_ERR_JOINT_BAD_BOUNDS => Error::JointBadBounds,
+            AVBD_ERR_JOINT_UNKNOWN_REF => Error::JointUnknownRef,
             other => Error::Other(other),
         })
     }
@@ -94,6 +104,38 @@ impl World {
 
     pub fn raw(&self) -> *mut AvbdWorld {
         self.raw
+    }
+
+    /// The whole world as a versioned snapshot: a world made from it
+    /// continues bit for bit, events included.
+    pub fn snapshot(&mut self) -> Result<Vec<u8>, Error> {
+        let mut n = 0u64;
+        Error::check(unsafe { avbd_world_snapshot(self.raw, std::ptr::null_mut(), 0, &mut n) })?;
+        let mut buf = vec![0u8; n as usize];
+        Error::check(unsafe { avbd_world_snapshot(self.raw, buf.as_mut_ptr(), n, &mut n) })?;
+        buf.truncate(n as usize);
+        Ok(buf)
+    }
+
+    /// A new world on `device` from `snapshot`'s bytes.
+    pub fn from_snapshot(bytes: &[u8], device: i32) -> Result<Self, Error> {
+        let mut raw = std::ptr::null_mut();
+        Error::check(unsafe { avbd_world_from_snapshot(bytes.as_ptr(), bytes.len() as u64, device, &mut raw) })?;
+        Ok(World { raw })
+    }
+
+    /// Write the snapshot to `path` (whole, then renamed into place).
+    pub fn save(&mut self, path: &std::path::Path) -> Result<(), Error> {
+        let c = path_cstring(path)?;
+        Error::check(unsafe { avbd_world_save(self.raw, c.as_ptr()) })
+    }
+
+    /// A new world on `device` from a snapshot file.
+    pub fn load(path: &std::path::Path, device: i32) -> Result<Self, Error> {
+        let c = path_cstring(path)?;
+        let mut raw = std::ptr::null_mut();
+        Error::check(unsafe { avbd_world_load(c.as_ptr(), device, &mut raw) })?;
+        Ok(World { raw })
     }
 
     /// `PhysicsEngine::add_body`: returns the first new handle.
@@ -183,6 +225,18 @@ impl World {
         unsafe { avbd_world_get_counters(self.raw, &mut c) };
         c
     }
+}
+
+fn path_cstring(path: &std::path::Path) -> Result<std::ffi::CString, Error> {
+    let s = path.to_str().ok_or(Error::InvalidArg)?;
+    std::ffi::CString::new(s).map_err(|_| Error::InvalidArg)
+}
+
+/// Validate a snapshot on the host (header, checksum, contents) without a GPU.
+pub fn snapshot_info(bytes: &[u8]) -> Result<AvbdSnapshotInfo, Error> {
+    let mut info = AvbdSnapshotInfo::default();
+    Error::check(unsafe { avbd_snapshot_info(bytes.as_ptr(), bytes.len() as u64, &mut info) })?;
+    Ok(info)
 }
 
 impl Drop for World {

@@ -2,9 +2,9 @@
 identical state against the oracle (Coloured order): the reference's
 behavioural joint scenes (hinge motor, prismatic slider at its limit,
 prismatic motor, fixed weld, distance rod, six-DOF locked / free / limited,
-free motor, spring oscillator and damper, wheel axle motor and suspension)
-plus a rope, a mixed scene where every kind meets contacts, and a batch of
-two such scenes equal to each scene alone.  The exact build computes the
+free motor, spring oscillator and damper, wheel axle motor and suspension,
+gears over hinges and sliders) plus a rope, a mixed scene where every kind
+meets contacts, and a batch of two such scenes equal to each scene alone.  The exact build computes the
 oracle's arithmetic, so poses are identical; the parity bars (integers
 identical, poses within 1e-5) are asserted too.  Admission errors equal the
 oracle's."""
@@ -92,11 +92,51 @@ def test_wheel():
     recs, d = T._wheel_motor_scene()
     b = run_pair(recs, [d], 120, gravity=(0.0, 0.0, 0.0))
     assert b["angular_velocity"][1][2] > 2.0
-    # the sprung suspension differs from the oracle in the last bit of a
-    # pose now and then (cause not found): held to the 1e-5 bar only
     for hz in (3.0, 0.0):
         recs, d = T._wheel_suspension_scene(hz)
-        run_pair(recs, [d], 120, exact=hz == 0.0)
+        run_pair(recs, [d], 120)
+
+
+def test_gears():
+    """The 2:1 hinge gear past a half turn of its driven hinge, and the
+    slider pair through a host teleport, per step."""
+    recs, joints = T._gear_hinge_scene()
+    b = run_pair(recs, joints, 180, gravity=(0.0, 0.0, 0.0))
+    assert abs(T.z_twist(b["orientation"][1])) > 0.5
+    recs, joints = T._gear_slider_scene()
+    params = abi.default_params()
+    o, g = P.make_pair(O.bodies_to_array(recs), params, joints)
+    for step in range(160):
+        if step == 80:
+            for w in (o, g):
+                arr = w.bodies()
+                arr["position"][1][0] += 4.0
+                w.set_bodies(arr)
+        so, sg = P.step_from_oracle_state(o, g)
+        assert max(P.compare_states(so, sg, params.step_dt, o, g)) == 0.0
+    p = g.bodies()["position"]
+    assert p[1][0] - 1.0 > 2.0 and p[2][0] - 3.0 > 2.0
+
+
+def test_gear_goes_with_its_joint():
+    """Removing a coupled joint or one of its bodies removes the gear
+    (joint_remap, migration.rs:74-115), on the device as in the oracle."""
+    recs, joints = T._gear_hinge_scene()
+    for edit in ("joint", "body"):
+        o, g = P.make_pair(O.bodies_to_array(recs), abi.default_params(gravity=(0.0, 0.0, 0.0)), joints)
+        for w in (o, g):
+            w.add_joint(abi.joint_desc(abi.JOINT_GEAR, 1, 2, [0, 0, 0], [0, 0, 0], gear=(1, 0, 0.5)))
+        for _ in range(20):
+            P.step_from_oracle_state(o, g)
+        for w in (o, g):
+            if edit == "joint":
+                w.remove_joint(1)
+            else:
+                w.remove_body(2)
+        assert len(g.export_state()["joints"]) == len(o.export_state()["joints"]) == 1
+        for _ in range(20):
+            so, sg = P.step_from_oracle_state(o, g)
+            assert max(P.compare_states(so, sg, 1.0 / 60.0, o, g)) == 0.0
 
 
 def test_fixed_distance_and_rope():
@@ -139,8 +179,8 @@ def test_sixdof_locked_free_and_limited():
 def zoo(x0):
     """Every joint kind in one scene with contacts: a slider-mounted arm,
     a welded pair, a rod, a rope, a six-DOF pair, a free motor pushing
-    the rod's end, a spring and a driven wheel (rigid suspension), falling
-    onto a floor."""
+    the rod's end, a spring, a driven sprung wheel and a gear between the
+    slider and the hinge, falling onto a floor."""
     rec = [O.body_new(abi.SHAPE_BOX, [6, 0.5, 6], [x0, -0.5, 0], 0.0),
            O.body_new(abi.SHAPE_BOX, [0.2, 0.2, 0.2], [x0, 4, 0], 0.0)]
     for k, (shape, p) in enumerate([(abi.SHAPE_BOX, [0.3, 0.3, 0.3]), (abi.SHAPE_SPHERE, [0.3]),
@@ -162,7 +202,9 @@ def zoo(x0):
           abi.joint_desc(abi.JOINT_SPRING, 3, 9, [0.2, 0, 0], [0, 0.2, 0],
                          spring=(1.2, 0.0, 40.0, 3.0, 1e4, abi.MOTOR_POSITION, abi.MODEL_ACCELERATION)),
           abi.joint_desc(abi.JOINT_WHEEL, 4, 7, [0, -0.3, 0], [0, 0.3, 0], [0, 1, 0], [0, 1, 0], motor=(4.0, 2.0),
-                         wheel=((0, 0, 1), (0, 0, 1), 0.0, 0.6))]
+                         wheel=((0, 0, 1), (0, 0, 1), 2.5, 0.6)),
+          # the slider and the hinge geared together (a slide side and a turn side sharing body 2)
+          abi.joint_desc(abi.JOINT_GEAR, 2, 3, [0, 0, 0], [0, 0, 0], gear=(0, 1, 0.3))]
     return rec, js
 
 
@@ -187,6 +229,9 @@ def test_joint_batch_equals_scenes_alone():
         alone[1].add_joint(d)
         d.body_a += n0
         d.body_b += n0
+        if d.kind == abi.JOINT_GEAR:  # joint handles of the batch world
+            d.gear_joint_a += len(j0)
+            d.gear_joint_b += len(j0)
         batch.add_joint(d)
     for _ in range(60):
         batch.step_graph(nsub)
@@ -210,7 +255,11 @@ def test_admission_errors_equal_the_oracle():
              abi.joint_desc(abi.JOINT_FIXED, 0, 0, [0, 0, 0], [0, 0, 0]),
              abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((nan, 0, 0), (0, 0, 0), 1, 1, 0)),
              abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), -1, 1, 0)),
-             abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), 1, 1, 2))]
+             abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [0, 0, 0], [0, 0, 0], drive=((0, 0, 0), (0, 0, 0), 1, 1, 2)),
+             abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0], gear=(0, 0, nan)),
+             abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0], gear=(5, 6, 1.0)),
+             abi.joint_desc(abi.JOINT_BALL, 0, 1, [0, 0, 0], [0, 0, 0]),  # admitted: a gear over it is not
+             abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0], gear=(0, 0, 1.0))]
     o = O.OracleWorld()
     o.add_bodies(O.bodies_to_array(recs))
     g = AvbdWorld(abi.default_params(), bodies=O.bodies_to_array(recs))
@@ -221,4 +270,5 @@ def test_admission_errors_equal_the_oracle():
             got = 0
         except AvbdError as e:
             got = e.code
-        assert got == want != 0
+        assert got == want
+        assert got != 0 or d.kind == abi.JOINT_BALL

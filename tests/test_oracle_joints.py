@@ -5,7 +5,8 @@ prismatic motor (:782-822), fixed weld (:891-938), distance rod (:940-968),
 six-DOF all locked / free axis / angular limit (:1452-1556), the free motor
 (crates/physics/tests/motor_joint.rs:90-110), the spring oscillator
 (p6_rope_spring_motor.rs:193-216), the wheel's axle motor and suspension
-(avbd_engine.rs:969-1061) — plus a rope that never
+(avbd_engine.rs:969-1061), the gears (a 2:1 hinge pair, :1359-1450; two
+sliders through a teleport, :822-889) — plus a rope that never
 exceeds its length, the free motor's angular drive and budget, and the
 admission errors of validate_joint (migration.rs:160-356).  Reference order, dt 1/60, 10 iterations."""
 import math
@@ -293,6 +294,96 @@ def test_wheel_suspension_holds_chassis(hz):
         assert abs(sep - 1.0) < 0.05, sep
 
 
+def _gear_hinge_scene():
+    """Motor-driven hinge A coupled 2:1 to a free hinge B on a static mount,
+    no gravity (avbd_engine.rs:1359-1410)."""
+    recs = [O.body_new(abi.SHAPE_BOX, [0.2, 0.2, 0.2], [0, 0, 0], 0.0),
+            O.body_new(abi.SHAPE_BOX, [0.1, 0.6, 0.1], [0, 0.6, 0], 1.0),
+            O.body_new(abi.SHAPE_BOX, [0.1, 0.6, 0.1], [1, 0.6, 0], 1.0)]
+    joints = [abi.joint_desc(abi.JOINT_REVOLUTE, 0, 1, [0, 0, 0], [0, -0.6, 0], [0, 0, 1], [0, 0, 1],
+                             motor=(1.5, 20.0)),
+              abi.joint_desc(abi.JOINT_REVOLUTE, 0, 2, [1, 0, 0], [0, -0.6, 0], [0, 0, 1], [0, 0, 1]),
+              abi.joint_desc(abi.JOINT_GEAR, 1, 2, [0, 0, 0], [0, 0, 0], gear=(0, 1, 2.0))]
+    return recs, joints
+
+
+def _gear_slider_scene():
+    """Two sliders on a static anchor, the first motor-driven, coupled with
+    ratio -1 (co-directional travel; avbd_engine.rs:822-855)."""
+    recs = [O.body_new(abi.SHAPE_BOX, [0.25, 0.25, 0.25], [0, 0, 0], 0.0),
+            O.body_new(abi.SHAPE_SPHERE, [0.25], [1, 0, 0], 1.0),
+            O.body_new(abi.SHAPE_SPHERE, [0.25], [3, 0, 0], 1.0)]
+    joints = [abi.joint_desc(abi.JOINT_PRISMATIC, 0, 1, [1, 0, 0], [0, 0, 0], [1, 0, 0], [1, 0, 0],
+                             motor=(2.0, 50.0)),
+              abi.joint_desc(abi.JOINT_PRISMATIC, 0, 2, [3, 0, 0], [0, 0, 0], [1, 0, 0], [1, 0, 0]),
+              abi.joint_desc(abi.JOINT_GEAR, 1, 2, [0, 0, 0], [0, 0, 0], gear=(0, 1, -1.0))]
+    return recs, joints
+
+
+def atan_twist(q):  # the folding-free twist of avbd_engine.rs:1431-1433
+    return 2.0 * math.atan2(float(q[2]), float(q[3]))
+
+
+def wrap(x):
+    return (x + math.pi) % (2.0 * math.pi) - math.pi
+
+
+def test_gear_couples_hinges_two_to_one():
+    recs, joints = _gear_hinge_scene()
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    for d in joints:
+        add(w, d)
+    ua = ub = pa = pb = 0.0
+    for i in range(180):
+        w.step(DT)
+        q = w.bodies()["orientation"]
+        xa, xb = atan_twist(q[1]), atan_twist(q[2])
+        if i == 0:
+            pa, pb = xa, xb
+        ua += wrap(xa - pa)
+        ub += wrap(xb - pb)
+        pa, pb = xa, xb
+    assert abs(z_twist(w.bodies()["orientation"][1])) > 0.5
+    assert abs(ua + 2.0 * ub) < 0.35 * max(abs(ua), 1.0), (ua, ub)
+    assert abs(ua) > math.pi  # the motor turned hinge A past a half turn: the unwrap held
+
+
+def test_gear_sliders_travel_together_through_a_teleport():
+    recs, joints = _gear_slider_scene()
+    w = world(recs)
+    for d in joints:
+        add(w, d)
+    for _ in range(120):
+        w.step(DT)
+    b = w.bodies()
+    b["position"][1][0] += 4.0  # a host teleport: meters never wrap like angles
+    w.set_bodies(b)
+    for _ in range(120):
+        w.step(DT)
+    p = w.bodies()["position"]
+    sa, sb = p[1][0] - 1.0, p[2][0] - 3.0
+    assert sa > 2.0 and sb > 2.0, (sa, sb)
+    assert abs(sa - sb) < 0.6, (sa, sb)
+
+
+def test_gear_goes_with_its_joint():
+    """Removing a coupled joint removes the gear (joint_remap,
+    migration.rs:74-115); the survivors move down."""
+    recs, joints = _gear_hinge_scene()
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    for d in joints:
+        add(w, d)
+    add(w, abi.joint_desc(abi.JOINT_GEAR, 1, 2, [0, 0, 0], [0, 0, 0], gear=(1, 0, 0.5)))
+    w.remove_joint(1)
+    assert len(w.export_state()["joints"]) == 1
+    recs, joints = _gear_hinge_scene()
+    w = world(recs, gravity=(0.0, 0.0, 0.0))
+    for d in joints:
+        add(w, d)
+    w.remove_body(2)  # hinge B's body: the hinge and the gear go
+    assert len(w.export_state()["joints"]) == 1
+
+
 def test_joint_admission_errors():
     w = world([O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 0, 0], 1.0),
                O.body_new(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [2, 0, 0], 1.0)])
@@ -331,6 +422,14 @@ def test_joint_admission_errors():
         (abi.joint_desc(abi.JOINT_SPRING, 0, 1, [0, 0, 0], [0, 0, 0], spring=(1, 0, 1, 1, -2, P, 0)),
          abi.AVBD_ERR_JOINT_NONFINITE),
     ]
+    # gears (mod.rs:1329-1404; avbd_engine.rs:183-255): a non-finite ratio,
+    # a joint that does not exist, a joint that is neither hinge nor slide
+    cases += [
+        (abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0], gear=(0, 0, nan)), abi.AVBD_ERR_JOINT_NONFINITE),
+        (abi.joint_desc(abi.JOINT_GEAR, 1, 1, [0, 0, 0], [0, 0, 0], gear=(7, 8, 2.0)), abi.AVBD_ERR_JOINT_SELF),
+        (abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0], gear=(7, 8, 2.0)),
+         abi.AVBD_ERR_JOINT_UNKNOWN_REF),
+    ]
     Wz = ((0, 0, 1), (0, 0, 1), 2.0, 0.5)
     cases += [
         (abi.joint_desc(abi.JOINT_WHEEL, 0, 1, [0, 0, 0], [0, 0, 0], [0, nan, 0], [0, 1, 0], wheel=Wz),
@@ -352,3 +451,6 @@ def test_joint_admission_errors():
     assert w.add_joint(abi.joint_desc(abi.JOINT_MOTOR, 0, 1, [nan, 0, 0], [0, 0, 0],
                                       drive=((0, 0, 0), (0, 0, 0), 1.0, 1.0, 0.3)))[0] == 0
     assert w.add_joint(abi.joint_desc(abi.JOINT_FIXED, 0, 1, [0, 0, 0], [0, 0, 0]))[0] == 0
+    # a gear over joints that neither turn nor slide (the motor and the weld)
+    assert w.add_joint(abi.joint_desc(abi.JOINT_GEAR, 0, 1, [0, 0, 0], [0, 0, 0],
+                                      gear=(0, 1, 1.0)))[0] == abi.AVBD_ERR_UNSUPPORTED
