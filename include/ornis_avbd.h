@@ -63,6 +63,10 @@ extern "C" {
 #define AVBD_SHAPE_CYLINDER 4  /* [radius, half_height, -], axis = local +Y     */
 #define AVBD_SHAPE_CONE 5      /* [radius, half_height, -], apex at +half_height */
 #define AVBD_SHAPE_HULL 6      /* [hull index, -, -]: a hull of avbd_world_add_hull */
+#define AVBD_SHAPE_ROUND 7     /* [shape id, -, -]: a rounded shape of avbd_world_add_round */
+#define AVBD_SHAPE_COMPOUND 8  /* [shape id, -, -]: a compound of avbd_world_add_compound */
+#define AVBD_SHAPE_HEIGHTFIELD 9 /* [terrain id, -, -]: a grid of avbd_world_add_heightfield */
+#define AVBD_SHAPE_TRIMESH 10  /* [mesh id, -, -]: a triangle mesh of avbd_world_add_trimesh */
 
 #define AVBD_BODY_DYNAMIC 0   /* BodyType::Dynamic   */
 #define AVBD_BODY_STATIC 1    /* BodyType::Static    */
@@ -176,6 +180,16 @@ typedef struct AvbdJointDesc {
     float gear_ratio;
     uint32_t reserved;
 } AvbdJointDesc;
+
+/* A part of a rounded or compound shape (Shape::Round's inner, a compound
+ * child with its Pose; collision/shape.rs:95-135, :144-230). */
+typedef struct AvbdShapePart {
+    uint32_t shape;       /* AVBD_SHAPE_SPHERE .. AVBD_SHAPE_HULL (no half-space)  */
+    float params[3];      /* as a body's shape_params (a hull: its id)            */
+    float border_radius;  /* a Shape::Round around the part: > 0; 0 = none        */
+    float position[3];    /* pose in the compound's frame (a rounded shape: unused) */
+    float orientation[4]; /* x y z w                                              */
+} AvbdShapePart;
 
 /* Solver parameters.  avbd_default_params() fills the reference's constants
  * (avbd/mod.rs:154-247, :1205-1210); dt, iterations and the substep count
@@ -317,6 +331,48 @@ int avbd_world_add_bodies(AvbdWorld* world, const AvbdBody* bodies, uint32_t n,
 int avbd_world_add_hull(AvbdWorld* world, const float* verts, uint32_t nverts, const uint32_t* faces,
                         uint32_t nfaces, const float* unit_inertia, uint32_t* hull_id);
 
+/* Shape::try_round (collision/shape.rs:563-575): `inner` is a primitive part
+ * (sphere, box, capsule, cylinder, cone or a hull already added) and its
+ * border_radius the skin, finite and > 0 (AVBD_ERR_INVALID_ARG otherwise; a
+ * half-space or a nested rounded or compound inner -> AVBD_ERR_UNSUPPORTED).
+ * Bodies of shape AVBD_SHAPE_ROUND name the returned id in shape_params[0].
+ * unit_inertia is the body-frame inertia per unit mass (Shape::try_inertia
+ * (1)), used when a sleeping body wakes; bodies carry their own in their
+ * records.  Distances peel the skin (distance.rs:519-545, :654-685). */
+int avbd_world_add_round(AvbdWorld* world, const AvbdShapePart* inner, const float* unit_inertia, uint32_t* id);
+
+/* Shape::try_compound (shape.rs:556-561): n >= 1 primitive parts, each
+ * optionally rounded (border_radius > 0) and placed by its pose; an empty
+ * list or a non-finite or negative radius -> AVBD_ERR_INVALID_ARG, a
+ * half-space or nested compound part -> AVBD_ERR_UNSUPPORTED.  Distances
+ * take the deepest part in order (distance.rs:550-599); compound against
+ * compound is separation, as in the reference.  Bodies of shape
+ * AVBD_SHAPE_COMPOUND name the id in shape_params[0]. */
+int avbd_world_add_compound(AvbdWorld* world, const AvbdShapePart* parts, uint32_t n, const float* unit_inertia,
+                            uint32_t* id);
+
+/* Heightfield::new (collision/shape.rs:1485-1505, invariants.rs:403-425):
+ * rows x cols row-major heights (rows along +Z, cols along +X) on a grid of
+ * spacing `cell`, centred on the body; an empty grid, a non-positive or
+ * non-finite cell -> AVBD_ERR_INVALID_ARG, a non-finite height ->
+ * AVBD_ERR_NONFINITE.  Distances take the nearest overlapped column, each a
+ * solid box from the lowest sample up (distance.rs:246-350); terrain
+ * against terrain, and terrain against a triangle mesh, are separation.
+ * Bodies of shape AVBD_SHAPE_HEIGHTFIELD name the id in shape_params[0]. */
+int avbd_world_add_heightfield(AvbdWorld* world, uint32_t rows, uint32_t cols, float cell, const float* heights,
+                               uint32_t* id);
+
+/* TriMesh::from_indexed (shape.rs:1646-1772): vertices (3 floats each) and
+ * triangles (3 indices each); degenerate triangles are dropped, an index out
+ * of range -> AVBD_ERR_INVALID_ARG, a non-finite vertex ->
+ * AVBD_ERR_NONFINITE.  Each kept triangle becomes a centroid-relative hull
+ * under a median-split AABB tree built as the reference builds it
+ * (shape.rs:1793-1890); distances take the nearest triangle the tree
+ * overlaps (distance.rs:416-517).  Mesh against mesh is separation.  Bodies
+ * of shape AVBD_SHAPE_TRIMESH name the id in shape_params[0]. */
+int avbd_world_add_trimesh(AvbdWorld* world, const float* verts, uint32_t nverts, const uint32_t* tris,
+                           uint32_t ntris, uint32_t* id);
+
 /* PhysicsEngine::remove_body (engine.rs:40-43, avbd/mod.rs:1241-1300): the
  * last body moves into the freed handle; pairs and joints of the removed
  * body are dropped (with the gears that couple those joints), the others
@@ -415,7 +471,8 @@ int avbd_world_import_state(AvbdWorld* world, const AvbdBody* bodies,
  * contact pairs and points with their warm state, joints with their
  * assembly references and warm state, convex hulls, the world's settings
  * (launch tuning, precision, event period, joint stiffness, the fixed-step
- * accumulator's remainder) and the event state: the previous touch set, the
+ * accumulator's remainder), rounded and compound shapes, and the event
+ * state: the previous touch set, the
  * previous trigger overlap set, the drop counters and the undrained event
  * queues.  A world made from a snapshot continues bit for bit as the saved
  * world would have (the reference's WorldSnapshot makes the same promise
@@ -431,7 +488,7 @@ int avbd_world_import_state(AvbdWorld* world, const AvbdBody* bodies,
  * never a silent reinterpretation (the reference's VersionMismatch,
  * snapshot.rs:815-830).  Queued events beyond the loaded world's queue
  * capacity are refused the same way. */
-#define AVBD_SNAPSHOT_FORMAT 1
+#define AVBD_SNAPSHOT_FORMAT 2
 
 typedef struct AvbdSnapshotInfo {
     uint32_t format;          /* format version of the snapshot              */

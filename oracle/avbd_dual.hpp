@@ -113,6 +113,8 @@ template <class V> inline orc::DualT<V> fabs(const orc::DualT<V>& a) {
     return orc::dual_apply(a, std::fabs(a.v), a.v < V(0) ? -1.0 : 1.0);
 }
 template <class V> inline orc::DualT<V> abs(const orc::DualT<V>& a) { return fabs(a); }
+// a step function: derivative zero
+template <class V> inline orc::DualT<V> floor(const orc::DualT<V>& a) { return orc::dual_apply(a, std::floor(a.v), 0.0); }
 template <class V> inline orc::DualT<V> fmin(const orc::DualT<V>& a, const orc::DualT<V>& b) {
     return (b.v < a.v || std::isnan(a.v)) ? b : a;
 }

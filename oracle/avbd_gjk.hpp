@@ -58,6 +58,9 @@ template <class T> static V3<T> support_any(const ShapeRef<T>& s, V3<T> dir) {
                 }
             return best;
         }
+        case AVBD_SHAPE_HEIGHTFIELD:
+        case AVBD_SHAPE_TRIMESH:
+            return pos;  // no support of its own (gjk.rs:141-155): its origin
         default:
             return support(s.shape, s.sp, pos, rot, dir);
     }

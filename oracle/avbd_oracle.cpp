@@ -106,6 +106,50 @@ template <class T> struct Hull {
     T bound = T(0), min_ext = T(0);
     V3<T> unit_inertia{};  // body-frame inertia per unit mass (ConvexHull::try_inertia)
 };
+// A part of a rounded or compound shape (Shape::Round's inner, a compound
+// child with its Pose; collision/shape.rs:95-135, :144-230): a primitive, a
+// border radius (0: not rounded) and its pose in the parent frame.
+template <class T> struct Part {
+    uint32_t shape;
+    V3<T> sp;
+    T radius;
+    V3<T> pos;
+    Qt<T> rot;
+    const Hull<T>* hull;
+};
+// A rounded shape (one part, identity pose) or a compound (its children in
+// order), with the measures the engine reads from it.
+template <class T> struct ExtShape {
+    bool compound = false;
+    std::vector<Part<T>> parts;
+    V3<T> unit_inertia{};
+    T bound = T(0), min_dim = T(0);
+};
+// Heightfield (shape.rs:352-361): row-major heights, rows along +Z and cols
+// along +X, spacing `cell`, and the sample range.
+template <class T> struct HField {
+    uint32_t rows = 0, cols = 0;
+    T cell = T(0);
+    std::vector<T> h;
+    T y_min = T(0), y_max = T(0);
+};
+// One node of a mesh's median-split tree (BvhNode / BvhLink, shape.rs:411-455):
+// a leaf owns order[a .. a+b), an inner node branches to nodes a and b.
+template <class T> struct BNode {
+    V3<T> lo, hi;
+    bool leaf;
+    uint32_t a, b;
+};
+// TriMesh (shape.rs:377-396): centroid-relative triangle hulls, their
+// centroids, the tree and its permutation, the longest vertex, the
+// shortest edge.
+template <class T> struct TMesh {
+    std::deque<Hull<T>> tris;
+    std::vector<V3<T>> cent;
+    std::vector<BNode<T>> nodes;
+    std::vector<uint32_t> order;
+    T bound = T(0), min_feature = T(0);
+};
 // bound (rows.rs:268-272: the longest vertex) and smallest extent
 // (shape.rs:1468-1479) of a hull
 template <class T> static void hull_measures(Hull<T>& h) {
@@ -123,6 +167,9 @@ template <class T> static void hull_measures(Hull<T>& h) {
 }
 template <class T> struct Body {
     const Hull<T>* hull = nullptr;  // AVBD_SHAPE_HULL only
+    const ExtShape<T>* ext = nullptr;  // AVBD_SHAPE_ROUND, AVBD_SHAPE_COMPOUND
+    const HField<T>* hf = nullptr;     // AVBD_SHAPE_HEIGHTFIELD
+    const TMesh<T>* mesh = nullptr;    // AVBD_SHAPE_TRIMESH
     V3<T> pos;
     Qt<T> rot;
     V3<T> vel, angvel, torque;
@@ -142,8 +189,13 @@ template <class T> struct ShapeRef {
     V3<T> pos;
     Qt<T> rot;
     const Hull<T>* hull;
+    const ExtShape<T>* ext;
+    const HField<T>* hf;
+    const TMesh<T>* mesh;
 };
-template <class T> static ShapeRef<T> sref(const Body<T>& b) { return {&b, b.shape, b.sp, b.pos, b.rot, b.hull}; }
+template <class T> static ShapeRef<T> sref(const Body<T>& b) {
+    return {&b, b.shape, b.sp, b.pos, b.rot, b.hull, b.ext, b.hf, b.mesh};
+}
 
 template <class T> struct Dist {
     T dist;
@@ -563,6 +615,222 @@ template <class T> static Dist<T> shape_distance(const ShapeRef<T>& a, const Sha
     return capsule_capsule(a.pos, a.rot, a.sp.x, a.sp.y, b.pos, b.rot, b.sp.x, b.sp.y);
 }
 
+// Rounded-shape distance offset (distance.rs:519-545): the rounded surface
+// sits `r` closer along the witness axis; an infinite distance stays.
+template <class T> static Dist<T> round_offset(Dist<T> d, T r, bool first, V3<T> pos_a, V3<T> pos_b) {
+    if (!std::isfinite(d.dist)) return d;
+    V3<T> axis = d.pb - d.pa;
+    if (len2(axis) <= C<T>(gjk::COINCIDENT_LEN2)) axis = pos_b - pos_a;
+    V3<T> n = normalize_or(axis, VX<T>());
+    if (first) return {d.dist - r, d.pa + n * r, d.pb};
+    return {d.dist - r, d.pa, d.pb - n * r};
+}
+// Pose::world_rot (shape.rs:119-134): the child's rotation under its parent,
+// normalized, or the parent's for a degenerate product.
+template <class T> static Qt<T> pose_world_rot(Qt<T> parent, Qt<T> local) {
+    Qt<T> q = qmul(parent, local);
+    T l2 = (q.x * q.x + q.y * q.y) + (q.z * q.z + q.w * q.w);
+    if (std::isfinite(q.x) && std::isfinite(q.y) && std::isfinite(q.z) && std::isfinite(q.w) &&
+        l2 > C<T>(K::DEGENERATE_LEN2))
+        return qnormalize(q);
+    return parent;
+}
+template <class T> static Dist<T> shape_distance_any(const ShapeRef<T>& a, const ShapeRef<T>& b);
+// Shape::aabb (shape.rs:619-680) of a primitive.
+template <class T> static void prim_aabb(const ShapeRef<T>& s, V3<T>& lo, V3<T>& hi) {
+    auto absv = [](V3<T> v) { return V3<T>{std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)}; };
+    V3<T> r;
+    switch (s.shape) {
+        case AVBD_SHAPE_SPHERE: r = {s.sp.x, s.sp.x, s.sp.x}; break;
+        case AVBD_SHAPE_BOX:
+            r = (absv(qrot(s.rot, VX<T>())) * s.sp.x + absv(qrot(s.rot, VY<T>())) * s.sp.y) +
+                absv(qrot(s.rot, VZ<T>())) * s.sp.z;
+            break;
+        case AVBD_SHAPE_HULL: {
+            V3<T> mn{std::numeric_limits<T>::infinity(), std::numeric_limits<T>::infinity(),
+                     std::numeric_limits<T>::infinity()};
+            V3<T> mx = -mn;
+            if (!s.hull || s.hull->verts.empty()) {
+                lo = hi = s.pos;
+                return;
+            }
+            for (const V3<T>& v : s.hull->verts) {
+                V3<T> w = s.pos + qrot(s.rot, v);
+                mn = {fmn(mn.x, w.x), fmn(mn.y, w.y), fmn(mn.z, w.z)};
+                mx = {fmx(mx.x, w.x), fmx(mx.y, w.y), fmx(mx.z, w.z)};
+            }
+            lo = mn;
+            hi = mx;
+            return;
+        }
+        default: {  // capsule, cylinder, cone: the axis shell plus the radius
+            V3<T> e = absv(qrot(s.rot, VY<T>())) * s.sp.y;
+            r = {e.x + s.sp.x, e.y + s.sp.x, e.z + s.sp.x};
+        }
+    }
+    lo = s.pos - r;
+    hi = s.pos + r;
+}
+// The convex side's AABB corners in the frame of (pos, rot): their bounds.
+template <class T> static void local_window(const ShapeRef<T>& convex, V3<T> pos, Qt<T> rot, V3<T>& lo, V3<T>& hi) {
+    V3<T> amin, amax;
+    prim_aabb(convex, amin, amax);
+    const Qt<T> inv = conj(rot);
+    lo = {std::numeric_limits<T>::infinity(), std::numeric_limits<T>::infinity(), std::numeric_limits<T>::infinity()};
+    hi = -lo;
+    for (int i = 0; i < 8; i++) {
+        V3<T> corner{(i & 1) ? amax.x : amin.x, (i & 2) ? amax.y : amin.y, (i & 4) ? amax.z : amin.z};
+        V3<T> l = qrot(inv, corner - pos);
+        lo = {fmn(lo.x, l.x), fmn(lo.y, l.y), fmn(lo.z, l.z)};
+        hi = {fmx(hi.x, l.x), fmx(hi.y, l.y), fmx(hi.z, l.z)};
+    }
+}
+// heightfield_convex (distance.rs:246-350): the nearest of the overlapped
+// columns, each a solid box from the lowest sample up to its height (a
+// flat one a one-cell skirt); `first`: the terrain owns pa.
+template <class T> static Dist<T> hf_convex(const ShapeRef<T>& t, const ShapeRef<T>& convex, bool first) {
+    const HField<T>& hf = *t.hf;
+    const T inf = std::numeric_limits<T>::infinity();
+    V3<T> lo, hi;
+    local_window(convex, t.pos, t.rot, lo, hi);
+    const T half = C<T>(K::HALF);
+    // the column index along x serves the rows too (distance.rs:299-303)
+    auto col_at = [&](T x, uint32_t n) -> uint32_t {
+        T f = std::floor(x / hf.cell + T(hf.cols - 1) * half);
+        if (!(f > T(0))) return 0u;  // NaN and below zero clamp to 0
+        return f >= T(n - 1) ? n - 1 : (uint32_t)(double)f;
+    };
+    const uint32_t c0 = col_at(lo.x, hf.cols), c1 = col_at(hi.x, hf.cols);
+    const uint32_t r0 = col_at(lo.z, hf.rows), r1 = col_at(hi.z, hf.rows);
+    const T x_origin = -T(hf.cols - 1) * half * hf.cell, z_origin = -T(hf.rows - 1) * half * hf.cell;
+    bool have = false;
+    Dist<T> best{};
+    for (uint32_t row = r0; row <= r1; row++)
+        for (uint32_t col = c0; col <= c1; col++) {
+            const T h = hf.h[(size_t)row * hf.cols + col];
+            const T y_low = h - hf.y_min >= C<T>(1e-4f) ? hf.y_min : h - fmx(hf.cell, C<T>(1e-3f));
+            V3<T> mn{x_origin + T(col) * hf.cell, y_low, z_origin + T(row) * hf.cell};
+            V3<T> mx{mn.x + hf.cell, fmx(h, y_low), mn.z + hf.cell};
+            V3<T> center = (mn + mx) * half;
+            V3<T> hl = (mx - mn) * half;
+            hl = {fmx(hl.x, T(0)), fmx(hl.y, T(0)), fmx(hl.z, T(0))};
+            ShapeRef<T> column{nullptr, AVBD_SHAPE_BOX, hl, t.pos + qrot(t.rot, center), t.rot, nullptr};
+            Dist<T> d = shape_distance(column, convex);
+            if (!have || d.dist < best.dist) {
+                best = d;
+                have = true;
+            }
+        }
+    if (!have) return first ? Dist<T>{inf, t.pos, convex.pos} : Dist<T>{inf, convex.pos, t.pos};
+    return first ? best : Dist<T>{best.dist, best.pb, best.pa};
+}
+// trimesh_convex (distance.rs:416-517): the nearest of the triangles whose
+// tree boxes overlap the convex side's window, walked last-in-first-out; the
+// winner's witnesses come back swapped when the mesh is the first shape and
+// as found when it is the second (the reference's own order, kept).
+template <class T> static Dist<T> mesh_convex(const ShapeRef<T>& m, const ShapeRef<T>& convex, bool first) {
+    const TMesh<T>& mesh = *m.mesh;
+    const T inf = std::numeric_limits<T>::infinity();
+    const Dist<T> none = first ? Dist<T>{inf, m.pos, convex.pos} : Dist<T>{inf, convex.pos, m.pos};
+    if (mesh.tris.empty()) return none;
+    V3<T> lo, hi;
+    local_window(convex, m.pos, m.rot, lo, hi);
+    bool have = false;
+    Dist<T> best{};
+    uint32_t stack[64];
+    size_t len = 1;
+    stack[0] = 0;
+    while (len > 0) {
+        const uint32_t ni = stack[--len];
+        if (ni >= mesh.nodes.size()) continue;
+        const BNode<T>& node = mesh.nodes[ni];
+        if (node.hi.x < lo.x || node.lo.x > hi.x || node.hi.y < lo.y || node.lo.y > hi.y || node.hi.z < lo.z ||
+            node.lo.z > hi.z)
+            continue;
+        if (node.leaf) {
+            const size_t end = std::min<size_t>((size_t)node.a + node.b, mesh.order.size());
+            for (size_t o = node.a; o < end; o++) {
+                const uint32_t tri = mesh.order[o];
+                if (tri >= mesh.tris.size()) continue;
+                ShapeRef<T> th{nullptr, AVBD_SHAPE_HULL, VZERO<T>(), m.pos + qrot(m.rot, mesh.cent[tri]), m.rot,
+                               &mesh.tris[tri]};
+                Dist<T> d = shape_distance(th, convex);
+                if (!have || d.dist < best.dist) {
+                    best = d;
+                    have = true;
+                }
+            }
+        } else {
+            if (len + 2 > 64) break;  // depth guard: keep the best so far
+            stack[len] = node.a;
+            stack[len + 1] = node.b;
+            len += 2;
+        }
+    }
+    if (!have) return none;
+    return first ? Dist<T>{best.dist, best.pb, best.pa} : best;
+}
+// shape_distance below the rounded and compound arms (distance.rs:706-745):
+// half-spaces, terrain, meshes, then the primitive pairs.
+template <class T> static Dist<T> shape_distance_leaf(const ShapeRef<T>& a, const ShapeRef<T>& b) {
+    const T inf = std::numeric_limits<T>::infinity();
+    if (a.shape == AVBD_SHAPE_HALFSPACE || b.shape == AVBD_SHAPE_HALFSPACE) return shape_distance(a, b);
+    const bool ta = a.shape == AVBD_SHAPE_HEIGHTFIELD, tb = b.shape == AVBD_SHAPE_HEIGHTFIELD;
+    const bool ma = a.shape == AVBD_SHAPE_TRIMESH, mb = b.shape == AVBD_SHAPE_TRIMESH;
+    if ((ta && !a.hf) || (tb && !b.hf) || (ma && !a.mesh) || (mb && !b.mesh)) return {inf, a.pos, b.pos};
+    // terrain against terrain or a mesh, mesh against mesh: separation
+    if ((ta || ma) && (tb || mb)) return {inf, a.pos, b.pos};
+    if (ta) return hf_convex(a, b, true);
+    if (tb) return hf_convex(b, a, false);
+    if (ma) return mesh_convex(a, b, true);
+    if (mb) return mesh_convex(b, a, false);
+    return shape_distance(a, b);
+}
+// compound_distance (distance.rs:550-599): the child that reports the
+// smallest distance, children in order; `first`: the compound owns pa.
+template <class T> static Dist<T> compound_distance(const ShapeRef<T>& c, const ShapeRef<T>& other, bool first) {
+    bool have = false;
+    Dist<T> best{};
+    for (const Part<T>& part : c.ext->parts) {
+        ShapeRef<T> child{nullptr, part.shape, part.sp, c.pos + qrot(c.rot, part.pos), pose_world_rot(c.rot, part.rot),
+                          part.hull, nullptr};
+        Dist<T> d = shape_distance_leaf(child, other);
+        // a rounded child peels inside its own query (distance.rs:654-685)
+        if (part.radius > T(0)) d = round_offset(d, part.radius, true, child.pos, other.pos);
+        if (!have || d.dist < best.dist) {
+            best = d;
+            have = true;
+        }
+    }
+    if (!have) return first ? Dist<T>{std::numeric_limits<T>::infinity(), c.pos, other.pos}
+                            : Dist<T>{std::numeric_limits<T>::infinity(), other.pos, c.pos};
+    return first ? best : Dist<T>{best.dist, best.pb, best.pa};
+}
+// shape_distance's wrapper arms (distance.rs:648-705): rounded shapes peel
+// first (a's, then b's), then compounds expand; compound-vs-compound is
+// separation.  Rounded inners and compound children are primitives here.
+template <class T> static Dist<T> shape_distance_any(const ShapeRef<T>& a, const ShapeRef<T>& b) {
+    const bool ext_a = a.shape == AVBD_SHAPE_ROUND || a.shape == AVBD_SHAPE_COMPOUND;
+    const bool ext_b = b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND;
+    if ((ext_a && !a.ext) || (ext_b && !b.ext)) return {std::numeric_limits<T>::infinity(), a.pos, b.pos};
+    if (a.shape == AVBD_SHAPE_ROUND) {
+        const Part<T>& in = a.ext->parts[0];
+        ShapeRef<T> inner{nullptr, in.shape, in.sp, a.pos, a.rot, in.hull, nullptr};
+        return round_offset(shape_distance_any(inner, b), in.radius, true, a.pos, b.pos);
+    }
+    if (b.shape == AVBD_SHAPE_ROUND) {
+        const Part<T>& in = b.ext->parts[0];
+        ShapeRef<T> inner{nullptr, in.shape, in.sp, b.pos, b.rot, in.hull, nullptr};
+        return round_offset(shape_distance_any(a, inner), in.radius, false, a.pos, b.pos);
+    }
+    if (a.shape == AVBD_SHAPE_COMPOUND) {
+        if (b.shape == AVBD_SHAPE_COMPOUND) return {std::numeric_limits<T>::infinity(), a.pos, b.pos};
+        return compound_distance(a, b, true);
+    }
+    if (b.shape == AVBD_SHAPE_COMPOUND) return compound_distance(b, a, false);
+    return shape_distance_leaf(a, b);
+}
+
 // ---- AVBD engine (avbd/*) ------------------------------------------------------
 template <class T> struct Point {
     V3<T> ra, rb;
@@ -725,6 +993,8 @@ template <class T> static T bound_radius(const Body<T>& b) {  // rows.rs:253-292
         case AVBD_SHAPE_CYLINDER:
         case AVBD_SHAPE_CONE: return std::sqrt(b.sp.x * b.sp.x + b.sp.y * b.sp.y);
         case AVBD_SHAPE_HULL: return b.hull ? b.hull->bound : T(0);
+        case AVBD_SHAPE_ROUND:
+        case AVBD_SHAPE_COMPOUND: return b.ext ? b.ext->bound : T(0);
         default: return std::numeric_limits<T>::infinity();
     }
 }
@@ -736,6 +1006,10 @@ template <class T> static T shape_min_dimension(const Body<T>& b) {  // rows.rs:
         case AVBD_SHAPE_CYLINDER: return fmn(b.sp.x, b.sp.y);
         case AVBD_SHAPE_CONE: return C<T>(K::HALF) * fmn(b.sp.x, b.sp.y);
         case AVBD_SHAPE_HULL: return C<T>(K::HALF) * (b.hull ? b.hull->min_ext : T(0));
+        case AVBD_SHAPE_ROUND:
+        case AVBD_SHAPE_COMPOUND: return b.ext ? b.ext->min_dim : std::numeric_limits<T>::infinity();
+        case AVBD_SHAPE_HEIGHTFIELD: return C<T>(K::HALF) * (b.hf ? b.hf->cell : T(0));
+        case AVBD_SHAPE_TRIMESH: return C<T>(K::HALF) * (b.mesh ? b.mesh->min_feature : T(0));
         default: return std::numeric_limits<T>::infinity();
     }
 }
@@ -881,17 +1155,205 @@ template <class T> struct Engine {
         if (b.type == AVBD_BODY_DYNAMIC) {
             T m = b.mass;
             b.inv_mass = (m > T(0)) ? T(1) / m : T(0);
-            b.inertia = b.shape == AVBD_SHAPE_HULL ? (b.hull && m > T(0) && std::isfinite(m) ? b.hull->unit_inertia * m
-                                                                                         : VZERO<T>())
-                                                   : shape_inertia(b.shape, b.sp, m);
+            const bool by_unit = b.shape == AVBD_SHAPE_HULL || b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND;
+            const V3<T> unit = b.shape == AVBD_SHAPE_HULL ? (b.hull ? b.hull->unit_inertia : VZERO<T>())
+                                                          : (b.ext ? b.ext->unit_inertia : VZERO<T>());
+            b.inertia = by_unit ? (m > T(0) && std::isfinite(m) ? unit * m : VZERO<T>()) : shape_inertia(b.shape, b.sp, m);
         }
     }
     std::deque<Hull<T>> hulls;  // stable addresses: bodies point at them
+    std::deque<ExtShape<T>> exts;  // rounded and compound shapes, likewise
+    std::deque<HField<T>> hfs;     // heightfields
+    std::deque<TMesh<T>> meshes;   // triangle meshes
     void link_hull(Body<T>& b) {
         b.hull = nullptr;
-        if (b.shape != AVBD_SHAPE_HULL) return;
+        b.ext = nullptr;
+        b.hf = nullptr;
+        b.mesh = nullptr;
         double id = (double)b.sp.x;
-        if (id >= 0.0 && id < (double)hulls.size()) b.hull = &hulls[(size_t)id];
+        if (b.shape == AVBD_SHAPE_HEIGHTFIELD && id >= 0.0 && id < (double)hfs.size()) b.hf = &hfs[(size_t)id];
+        if (b.shape == AVBD_SHAPE_TRIMESH && id >= 0.0 && id < (double)meshes.size()) b.mesh = &meshes[(size_t)id];
+        if (b.shape == AVBD_SHAPE_HULL && id >= 0.0 && id < (double)hulls.size()) b.hull = &hulls[(size_t)id];
+        if ((b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND) && id >= 0.0 && id < (double)exts.size() &&
+            exts[(size_t)id].compound == (b.shape == AVBD_SHAPE_COMPOUND))
+            b.ext = &exts[(size_t)id];
+    }
+    // Heightfield::new (shape.rs:1485-1505, invariants.rs:403-425)
+    int add_hf(uint32_t rows, uint32_t cols, float cell, const float* heights, uint32_t& id) {
+        if (rows == 0 || cols == 0 || !heights) return AVBD_ERR_INVALID_ARG;
+        if (!std::isfinite(cell) || !(cell > 0.0f)) return AVBD_ERR_INVALID_ARG;
+        HField<T> f;
+        f.rows = rows;
+        f.cols = cols;
+        f.cell = T(cell);
+        T lo = std::numeric_limits<T>::infinity(), hi = -lo;
+        for (size_t i = 0; i < (size_t)rows * cols; i++) {
+            if (!std::isfinite(heights[i])) return AVBD_ERR_NONFINITE;
+            f.h.push_back(T(heights[i]));
+            lo = fmn(lo, f.h.back());  // height_range (shape.rs:1571-1583)
+            hi = fmx(hi, f.h.back());
+        }
+        f.y_min = lo;
+        f.y_max = hi;
+        id = (uint32_t)hfs.size();
+        hfs.push_back(std::move(f));
+        return AVBD_OK;
+    }
+    // TriMesh::build_bvh / split (shape.rs:1793-1890): median splits of the
+    // longest axis over a stable centroid sort, leaves of up to 4 triangles.
+    static uint32_t bvh_split(const std::vector<std::pair<V3<T>, V3<T>>>& bounds, const std::vector<V3<T>>& cent,
+                              uint32_t* order, size_t n, uint32_t base, std::vector<BNode<T>>& nodes) {
+        V3<T> lo{std::numeric_limits<T>::infinity(), std::numeric_limits<T>::infinity(),
+                 std::numeric_limits<T>::infinity()};
+        V3<T> hi = -lo;
+        for (size_t i = 0; i < n; i++) {
+            const auto& bb = bounds[order[i]];
+            lo = {fmn(lo.x, bb.first.x), fmn(lo.y, bb.first.y), fmn(lo.z, bb.first.z)};
+            hi = {fmx(hi.x, bb.second.x), fmx(hi.y, bb.second.y), fmx(hi.z, bb.second.z)};
+        }
+        const uint32_t here = (uint32_t)nodes.size();
+        nodes.push_back(BNode<T>{lo, hi, true, 0u, 0u});
+        if (n <= 4) {
+            nodes[here].a = base;
+            nodes[here].b = (uint32_t)n;
+            return here;
+        }
+        const V3<T> e = hi - lo;
+        const int axis = (e.x >= e.y && e.x >= e.z) ? 0 : (e.y >= e.z ? 1 : 2);
+        std::stable_sort(order, order + n, [&](uint32_t x, uint32_t y) { return cent[x][axis] < cent[y][axis]; });
+        const size_t mid = n / 2;
+        if (cent[order[0]][axis] == cent[order[n - 1]][axis]) {  // all equal: a leaf
+            nodes[here].a = base;
+            nodes[here].b = (uint32_t)n;
+            return here;
+        }
+        const uint32_t left = bvh_split(bounds, cent, order, mid, base, nodes);
+        const uint32_t right = bvh_split(bounds, cent, order + mid, n - mid, base + (uint32_t)mid, nodes);
+        nodes[here].leaf = false;
+        nodes[here].a = left;
+        nodes[here].b = right;
+        return here;
+    }
+    // TriMesh::from_indexed / from_triangles (shape.rs:1646-1772)
+    int add_mesh(const float* verts, uint32_t nv, const uint32_t* idx, uint32_t nt, uint32_t& id) {
+        if ((nv && !verts) || (nt && !idx)) return AVBD_ERR_INVALID_ARG;
+        std::vector<V3<T>> vs(nv);
+        for (uint32_t i = 0; i < nv; i++) {
+            for (int k = 0; k < 3; k++)
+                if (!std::isfinite(verts[3 * i + k])) return AVBD_ERR_NONFINITE;
+            vs[i] = {T(verts[3 * i]), T(verts[3 * i + 1]), T(verts[3 * i + 2])};
+        }
+        TMesh<T> m;
+        const T inf = std::numeric_limits<T>::infinity();
+        m.min_feature = inf;
+        for (uint32_t t = 0; t < nt; t++) {
+            for (int k = 0; k < 3; k++)
+                if (idx[3 * t + k] >= nv) return AVBD_ERR_INVALID_ARG;
+            const V3<T> v[3] = {vs[idx[3 * t]], vs[idx[3 * t + 1]], vs[idx[3 * t + 2]]};
+            if (len2(cross(v[1] - v[0], v[2] - v[0])) < C<T>(K::DEGENERATE_LEN2)) continue;  // a sliver
+            const V3<T> ends[3][2] = {{v[0], v[1]}, {v[1], v[2]}, {v[2], v[0]}};
+            for (const auto& e : ends) m.min_feature = fmn(m.min_feature, len(e[1] - e[0]));
+            for (const V3<T>& p : v) m.bound = fmx(m.bound, len(p));
+            const V3<T> c = (v[0] + v[1] + v[2]) / T(3);
+            m.cent.push_back(c);
+            // ConvexHull::from_vertices welds points closer than 1e-6
+            // (shape.rs:1304-1325); a triangle that welds below three
+            // points is refused here
+            Hull<T> h;
+            for (const V3<T>& p : v) {
+                const V3<T> q = p - c;
+                bool near = false;
+                for (const V3<T>& w : h.verts) near = near || len2(w - q) < C<T>(1e-6f) * C<T>(1e-6f);
+                if (!near) h.verts.push_back(q);
+            }
+            if (h.verts.size() != 3) return AVBD_ERR_INVALID_ARG;
+            h.faces = {0u, 1u, 2u, 0u, 2u, 1u};  // both windings
+            hull_measures(h);
+            m.tris.push_back(std::move(h));
+        }
+        if (m.tris.empty()) m.min_feature = T(0);
+        std::vector<std::pair<V3<T>, V3<T>>> bounds;
+        for (size_t t = 0; t < m.tris.size(); t++) {
+            V3<T> lo{inf, inf, inf}, hi = -lo;
+            for (const V3<T>& q : m.tris[t].verts) {
+                const V3<T> w = q + m.cent[t];
+                lo = {fmn(lo.x, w.x), fmn(lo.y, w.y), fmn(lo.z, w.z)};
+                hi = {fmx(hi.x, w.x), fmx(hi.y, w.y), fmx(hi.z, w.z)};
+            }
+            bounds.push_back({lo, hi});
+        }
+        m.order.resize(bounds.size());
+        for (size_t i = 0; i < m.order.size(); i++) m.order[i] = (uint32_t)i;
+        if (!m.order.empty()) bvh_split(bounds, m.cent, m.order.data(), m.order.size(), 0u, m.nodes);
+        if (m.nodes.empty()) m.nodes.push_back(BNode<T>{VZERO<T>(), VZERO<T>(), true, 0u, 0u});
+        id = (uint32_t)meshes.size();
+        meshes.push_back(std::move(m));
+        return AVBD_OK;
+    }
+    // rows.rs:253-292 and :373-403 for one part of a rounded or compound shape
+    T part_bound(const Part<T>& p) const {
+        T r;
+        switch (p.shape) {
+            case AVBD_SHAPE_SPHERE: r = p.sp.x; break;
+            case AVBD_SHAPE_BOX: r = len(p.sp); break;
+            case AVBD_SHAPE_CAPSULE: r = p.sp.y + p.sp.x; break;
+            case AVBD_SHAPE_HULL: r = p.hull ? p.hull->bound : T(0); break;
+            default: r = std::sqrt(p.sp.x * p.sp.x + p.sp.y * p.sp.y);  // cylinder, cone
+        }
+        return p.radius > T(0) ? r + fmx(p.radius, T(0)) : r;
+    }
+    T part_min_dim(const Part<T>& p) const {
+        T m;
+        switch (p.shape) {
+            case AVBD_SHAPE_SPHERE: m = p.sp.x; break;
+            case AVBD_SHAPE_BOX: m = min_element(p.sp); break;
+            case AVBD_SHAPE_CAPSULE: m = p.sp.x; break;
+            case AVBD_SHAPE_CYLINDER: m = fmn(p.sp.x, p.sp.y); break;
+            case AVBD_SHAPE_CONE: m = C<T>(K::HALF) * fmn(p.sp.x, p.sp.y); break;
+            default: m = C<T>(K::HALF) * (p.hull ? p.hull->min_ext : T(0));  // hull
+        }
+        return p.radius > T(0) ? fmn(m, fmx(p.radius, T(0)) * T(2)) : m;
+    }
+    // Shape::try_round / try_compound (shape.rs:556-575) over primitive parts
+    int add_ext(bool compound, const AvbdShapePart* parts, uint32_t n, const float* unit_inertia, uint32_t& id) {
+        if (!parts || !unit_inertia || n == 0 || (!compound && n != 1)) return AVBD_ERR_INVALID_ARG;
+        ExtShape<T> e;
+        e.compound = compound;
+        for (uint32_t i = 0; i < n; i++) {
+            const AvbdShapePart& q = parts[i];
+            if (q.shape > AVBD_SHAPE_HULL || q.shape == AVBD_SHAPE_HALFSPACE) return AVBD_ERR_UNSUPPORTED;
+            if (!compound && !(std::isfinite(q.border_radius) && q.border_radius > 0.0f)) return AVBD_ERR_INVALID_ARG;
+            if (!std::isfinite(q.border_radius) || q.border_radius < 0.0f) return AVBD_ERR_INVALID_ARG;
+            Part<T> p;
+            p.shape = q.shape;
+            p.sp = {T(q.params[0]), T(q.params[1]), T(q.params[2])};
+            p.radius = T(q.border_radius);
+            p.pos = {T(q.position[0]), T(q.position[1]), T(q.position[2])};
+            p.rot = {T(q.orientation[0]), T(q.orientation[1]), T(q.orientation[2]), T(q.orientation[3])};
+            p.hull = nullptr;
+            if (q.shape == AVBD_SHAPE_HULL) {
+                double hid = (double)q.params[0];
+                if (!(hid >= 0.0 && hid < (double)hulls.size())) return AVBD_ERR_INVALID_ARG;
+                p.hull = &hulls[(size_t)hid];
+            }
+            e.parts.push_back(p);
+        }
+        e.unit_inertia = {T(unit_inertia[0]), T(unit_inertia[1]), T(unit_inertia[2])};
+        // rows.rs:279-290, :393-400
+        if (compound) {
+            e.bound = T(0);
+            e.min_dim = std::numeric_limits<T>::infinity();
+            for (const Part<T>& p : e.parts) {
+                e.bound = fmx(e.bound, part_bound(p) + len(p.pos));
+                e.min_dim = fmn(e.min_dim, part_min_dim(p));
+            }
+        } else {
+            e.bound = part_bound(e.parts[0]);
+            e.min_dim = part_min_dim(e.parts[0]);
+        }
+        id = (uint32_t)exts.size();
+        exts.push_back(std::move(e));
+        return AVBD_OK;
     }
 
     // ---- joints / sleep (avbd/sleep.rs) ----
@@ -1255,7 +1717,7 @@ template <class T> struct Engine {
         }
         T ra = bound_radius(a), rb = bound_radius(b);
         if (len(a.pos - b.pos) > ra + rb + C<T>(K::GEN_MARGIN)) return false;
-        Dist<T> d = shape_distance(sref(a), sref(b));
+        Dist<T> d = shape_distance_any(sref(a), sref(b));
         T sgn = (a.shape == AVBD_SHAPE_BOX && b.shape == AVBD_SHAPE_BOX)
                     ? box_box_signed_gap(a.pos, a.rot, a.sp, b.pos, b.rot, b.sp)
                     : d.dist;
@@ -2335,8 +2797,8 @@ template <class T> struct Engine {
                 bool hit = false;
                 V3<T> hn{}, hp{};
                 for (int it = 0; it < 24; it++) {
-                    ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot, mb.hull};
-                    Dist<T> d = shape_distance(mv, tgt);
+                    ShapeRef<T> mv{&mb, mb.shape, mb.sp, mb.pos + dir * t, mb.rot, mb.hull, mb.ext, mb.hf, mb.mesh};
+                    Dist<T> d = shape_distance_any(mv, tgt);
                     if (d.dist <= C<T>(K::SHAPE_TOUCH)) {
                         if (t > T(0)) { hit = true; hn = normalize_or(d.pa - d.pb, -dir); hp = d.pb; }
                         break;
@@ -2951,6 +3413,31 @@ int oracle_add_bodies(OracleWorld* w, const AvbdBody* b, uint32_t n) {
 // A convex hull (centroid-relative vertices, triangle faces as 3 indices,
 // body-frame inertia per unit mass); bodies of shape AVBD_SHAPE_HULL name it
 // by index in shape_params[0].  Returns the index.
+int oracle_add_heightfield(OracleWorld* w, uint32_t rows, uint32_t cols, float cell, const float* heights,
+                           uint32_t* id) {
+    int rc = 0;
+    uint32_t out = 0;
+    DISPATCH(w, rc = E.add_hf(rows, cols, cell, heights, out));
+    if (id) *id = out;
+    return rc;
+}
+int oracle_add_trimesh(OracleWorld* w, const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt,
+                       uint32_t* id) {
+    int rc = 0;
+    uint32_t out = 0;
+    DISPATCH(w, rc = E.add_mesh(verts, nv, tris, nt, out));
+    if (id) *id = out;
+    return rc;
+}
+// Shape::try_round / try_compound over primitive parts (shape.rs:556-575).
+int oracle_add_ext(OracleWorld* w, int compound, const AvbdShapePart* parts, uint32_t n, const float* unit_inertia,
+                   uint32_t* id) {
+    int rc = 0;
+    uint32_t out = 0;
+    DISPATCH(w, rc = E.add_ext(compound != 0, parts, n, unit_inertia, out));
+    if (id) *id = out;
+    return rc;
+}
 uint32_t oracle_add_hull(OracleWorld* w, const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf,
                          const float* unit_inertia) {
     uint32_t id = 0;
@@ -2979,7 +3466,7 @@ void oracle_convex_distance(OracleWorld* w, uint32_t ia, uint32_t ib, float* out
 }
 void oracle_shape_distance(OracleWorld* w, uint32_t ia, uint32_t ib, float* out) {
     DISPATCH(w, {
-        auto d = shape_distance(sref(E.bodies[ia]), sref(E.bodies[ib]));
+        auto d = shape_distance_any(sref(E.bodies[ia]), sref(E.bodies[ib]));
         float v[10] = {(float)d.dist, 0.0f, 0.0f, 0.0f, (float)d.pa.x, (float)d.pa.y, (float)d.pa.z,
                        (float)d.pb.x, (float)d.pb.y, (float)d.pb.z};
         std::memcpy(out, v, sizeof(v));

@@ -35,6 +35,10 @@ SHAPE_HALFSPACE = 3
 SHAPE_CYLINDER = 4
 SHAPE_CONE = 5
 SHAPE_HULL = 6
+SHAPE_ROUND = 7
+SHAPE_COMPOUND = 8
+SHAPE_HEIGHTFIELD = 9
+SHAPE_TRIMESH = 10
 
 BODY_DYNAMIC = 0
 BODY_STATIC = 1
@@ -135,6 +139,32 @@ class AvbdJointDesc(C.Structure):
     ]
 
 
+class AvbdShapePart(C.Structure):
+    _fields_ = [
+        ("shape", C.c_uint32),
+        ("params", F3),
+        ("border_radius", C.c_float),
+        ("position", F3),
+        ("orientation", F4),
+    ]
+
+
+def shape_part(shape, params, border_radius=0.0, position=(0.0, 0.0, 0.0), orientation=(0.0, 0.0, 0.0, 1.0)):
+    """One part of a rounded or compound shape."""
+    p = AvbdShapePart()
+    p.shape = shape
+    pp = list(map(float, params)) + [0.0] * (3 - len(params))
+    p.params[:] = pp
+    p.border_radius = float(border_radius)
+    p.position[:] = list(map(float, position))
+    p.orientation[:] = list(map(float, orientation))
+    return p
+
+
+def parts_array(parts):
+    return (AvbdShapePart * len(parts))(*parts)
+
+
 class AvbdParams(C.Structure):
     _fields_ = [
         ("gravity", F3),
@@ -193,7 +223,7 @@ class AvbdJointState(C.Structure):
     ]
 
 
-SNAPSHOT_FORMAT = 1
+SNAPSHOT_FORMAT = 2
 SNAPSHOT_HEADER_BYTES = 128
 SNAPSHOT_MAGIC = b"ORNAVBD\0"
 SNAPSHOT_SETTINGS_BYTES = 48       # launch tuning, precision, event period, joint stiffness, accumulator

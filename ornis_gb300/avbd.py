@@ -47,6 +47,10 @@ def lib():
             "avbd_world_remove_joint": [vp, u32],
             "avbd_world_wake_body": [vp, u32],
             "avbd_world_add_hull": [vp, vp, u32, vp, u32, vp, C.POINTER(u32)],
+            "avbd_world_add_round": [vp, C.POINTER(abi.AvbdShapePart), vp, C.POINTER(u32)],
+            "avbd_world_add_compound": [vp, vp, u32, vp, C.POINTER(u32)],
+            "avbd_world_add_heightfield": [vp, u32, u32, C.c_float, vp, C.POINTER(u32)],
+            "avbd_world_add_trimesh": [vp, vp, u32, vp, u32, C.POINTER(u32)],
             "avbd_world_body_count": [vp, C.POINTER(u32)],
             "avbd_world_scene_count": [vp, C.POINTER(u32)],
             "avbd_world_get_bodies": [vp, u32, u32, vp],
@@ -227,6 +231,43 @@ class AvbdWorld:
         out = C.c_uint32()
         _check(lib().avbd_world_add_hull(self.h, abi.ptr(v), len(v) // 3, abi.ptr(f) if len(f) else None,
                                          len(f) // 3, abi.ptr(ui), C.byref(out)), "add_hull")
+        return out.value
+
+    def add_round(self, inner, unit_inertia=(1.0, 1.0, 1.0)):
+        """A rounded shape (Shape::Round) around one primitive part; bodies of
+        shape SHAPE_ROUND name the returned id."""
+        ui = np.ascontiguousarray(np.asarray(unit_inertia, dtype=np.float32))
+        out = C.c_uint32()
+        _check(lib().avbd_world_add_round(self.h, C.byref(inner), abi.ptr(ui), C.byref(out)), "add_round")
+        return out.value
+
+    def add_compound(self, parts, unit_inertia=(1.0, 1.0, 1.0)):
+        """A compound (Shape::Compound) of primitive parts; bodies of shape
+        SHAPE_COMPOUND name the returned id."""
+        ui = np.ascontiguousarray(np.asarray(unit_inertia, dtype=np.float32))
+        out = C.c_uint32()
+        arr = abi.parts_array(parts) if parts else None
+        _check(lib().avbd_world_add_compound(self.h, arr, len(parts), abi.ptr(ui), C.byref(out)), "add_compound")
+        return out.value
+
+    def add_heightfield(self, heights, cell):
+        """A heightfield (Heightfield::new) of rows x cols samples, rows along
+        +Z; static bodies of shape SHAPE_HEIGHTFIELD name the returned id."""
+        h = np.ascontiguousarray(np.asarray(heights, dtype=np.float32))
+        rows, cols = h.shape
+        out = C.c_uint32()
+        _check(lib().avbd_world_add_heightfield(self.h, rows, cols, float(cell), abi.ptr(h), C.byref(out)),
+               "add_heightfield")
+        return out.value
+
+    def add_trimesh(self, verts, tris):
+        """A triangle mesh (TriMesh::from_indexed); static bodies of shape
+        SHAPE_TRIMESH name the returned id."""
+        v = np.ascontiguousarray(np.asarray(verts, dtype=np.float32).reshape(-1))
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.uint32).reshape(-1))
+        out = C.c_uint32()
+        _check(lib().avbd_world_add_trimesh(self.h, abi.ptr(v), len(v) // 3, abi.ptr(t), len(t) // 3, C.byref(out)),
+               "add_trimesh")
         return out.value
 
     def remove_body(self, handle):

@@ -63,6 +63,218 @@ static __device__ __forceinline__ Shape shape_of(const DW& w, uint32_t h) {
     }
     return Shape{kind, V3{sp.x, sp.y, sp.z}, ld3(w.pos[h]), ldq(w.rot[h]), hull};
 }
+
+// ---- rounded and compound shapes, terrain, meshes (distance.rs:246-745) ----
+static __device__ __forceinline__ bool ext_kind(uint32_t kind) {
+    return kind == AVBD_SHAPE_ROUND || kind == AVBD_SHAPE_COMPOUND;
+}
+// shapes without a finite bound: paired with every body of their scene
+static __host__ __device__ __forceinline__ bool unbounded_kind(uint32_t kind) {
+    return kind == AVBD_SHAPE_HALFSPACE || kind == AVBD_SHAPE_HEIGHTFIELD || kind == AVBD_SHAPE_TRIMESH;
+}
+// Shape::aabb (shape.rs:619-680) of a primitive.
+static __device__ __forceinline__ void prim_aabb(const Shape& s, V3& lo, V3& hi) {
+    auto absv = [](V3 v) { return V3{fabsf(v.x), fabsf(v.y), fabsf(v.z)}; };
+    V3 r;
+    if (s.kind == AVBD_SHAPE_SPHERE) {
+        r = V3{s.p.x, s.p.x, s.p.x};
+    } else if (s.kind == AVBD_SHAPE_BOX) {
+        r = (absv(qrot(s.rot, VX())) * s.p.x + absv(qrot(s.rot, VY())) * s.p.y) + absv(qrot(s.rot, VZ())) * s.p.z;
+    } else if (s.kind == AVBD_SHAPE_HULL) {
+        if (!s.hull || s.hull->nv == 0) {
+            lo = hi = s.pos;
+            return;
+        }
+        lo = V3{INFINITY, INFINITY, INFINITY};
+        hi = V3{-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t i = 0; i < s.hull->nv; i++) {
+            const V3 w = s.pos + qrot(s.rot, ld3(s.hull->v[i]));
+            lo = V3{fminf(lo.x, w.x), fminf(lo.y, w.y), fminf(lo.z, w.z)};
+            hi = V3{fmaxf(hi.x, w.x), fmaxf(hi.y, w.y), fmaxf(hi.z, w.z)};
+        }
+        return;
+    } else {  // capsule, cylinder, cone: the axis shell plus the radius
+        const V3 e = absv(qrot(s.rot, VY())) * s.p.y;
+        r = V3{e.x + s.p.x, e.y + s.p.x, e.z + s.p.x};
+    }
+    lo = s.pos - r;
+    hi = s.pos + r;
+}
+// The convex side's AABB corners in the frame (pos, rot): their bounds.
+static __device__ __forceinline__ void local_window(const Shape& convex, V3 pos, Q rot, V3& lo, V3& hi) {
+    V3 amin, amax;
+    prim_aabb(convex, amin, amax);
+    const Q inv = conj(rot);
+    lo = V3{INFINITY, INFINITY, INFINITY};
+    hi = V3{-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < 8; i++) {
+        const V3 corner{(i & 1) ? amax.x : amin.x, (i & 2) ? amax.y : amin.y, (i & 4) ? amax.z : amin.z};
+        const V3 l = qrot(inv, corner - pos);
+        lo = V3{fminf(lo.x, l.x), fminf(lo.y, l.y), fminf(lo.z, l.z)};
+        hi = V3{fmaxf(hi.x, l.x), fmaxf(hi.y, l.y), fmaxf(hi.z, l.z)};
+    }
+}
+// heightfield_convex (distance.rs:246-350): the nearest overlapped column,
+// each a solid box from the lowest sample up to its height (a flat one a
+// one-cell skirt); `first`: the terrain owns pa.
+static __device__ __noinline__ Dist hf_convex(const DW& w, const Shape& t, const Shape& convex, bool first) {
+    const HfDesc hf = w.hfs[(uint32_t)t.p.x];
+    V3 lo, hi;
+    local_window(convex, t.pos, t.rot, lo, hi);
+    // the column index along x serves the rows too (distance.rs:299-303)
+    auto col_at = [&](float x, uint32_t n) -> uint32_t {
+        const float f = floorf(x / hf.cell + (float)(hf.cols - 1) * HALF);
+        if (!(f > 0.0f)) return 0u;
+        return f >= (float)(n - 1) ? n - 1 : (uint32_t)f;
+    };
+    const uint32_t c0 = col_at(lo.x, hf.cols), c1 = col_at(hi.x, hf.cols);
+    const uint32_t r0 = col_at(lo.z, hf.rows), r1 = col_at(hi.z, hf.rows);
+    const float x_origin = -(float)(hf.cols - 1) * HALF * hf.cell, z_origin = -(float)(hf.rows - 1) * HALF * hf.cell;
+    bool have = false;
+    Dist best{INFINITY, t.pos, convex.pos};
+    for (uint32_t row = r0; row <= r1; row++)
+        for (uint32_t col = c0; col <= c1; col++) {
+            const float h = hf.h[(size_t)row * hf.cols + col];
+            const float y_low = h - hf.y_min >= 1e-4f ? hf.y_min : h - fmaxf(hf.cell, 1e-3f);
+            const V3 mn{x_origin + (float)col * hf.cell, y_low, z_origin + (float)row * hf.cell};
+            const V3 mx{mn.x + hf.cell, fmaxf(h, y_low), mn.z + hf.cell};
+            const V3 center = (mn + mx) * HALF;
+            V3 hl = (mx - mn) * HALF;
+            hl = V3{fmaxf(hl.x, 0.0f), fmaxf(hl.y, 0.0f), fmaxf(hl.z, 0.0f)};
+            const Shape column{AVBD_SHAPE_BOX, hl, t.pos + qrot(t.rot, center), t.rot, nullptr};
+            const Dist d = shape_distance(column, convex, nullptr);
+            if (!have || d.dist < best.dist) {
+                best = d;
+                have = true;
+            }
+        }
+    if (!have) return first ? Dist{INFINITY, t.pos, convex.pos} : Dist{INFINITY, convex.pos, t.pos};
+    return first ? best : Dist{best.dist, best.pb, best.pa};
+}
+// trimesh_convex (distance.rs:416-517): the nearest triangle whose tree
+// boxes overlap the convex side's window, walked last-in-first-out; the
+// winner's witnesses come back swapped when the mesh is the first shape and
+// as found when it is the second (the reference's own order, kept).
+static __device__ __noinline__ Dist mesh_convex(const DW& w, const Shape& m, const Shape& convex, bool first) {
+    const MeshDesc mesh = w.meshes[(uint32_t)m.p.x];
+    const Dist none = first ? Dist{INFINITY, m.pos, convex.pos} : Dist{INFINITY, convex.pos, m.pos};
+    if (mesh.ntris == 0) return none;
+    V3 lo, hi;
+    local_window(convex, m.pos, m.rot, lo, hi);
+    bool have = false;
+    Dist best = none;
+    uint32_t stack[64];
+    uint32_t len = 1;
+    stack[0] = 0;
+    while (len > 0) {
+        const uint32_t ni = stack[--len];
+        if (ni >= mesh.nnodes) continue;
+        const MeshNodeD node = mesh.nodes[ni];
+        if (node.hi[0] < lo.x || node.lo[0] > hi.x || node.hi[1] < lo.y || node.lo[1] > hi.y || node.hi[2] < lo.z ||
+            node.lo[2] > hi.z)
+            continue;
+        if (node.leaf) {
+            const uint32_t end = min(node.a + node.b, mesh.norder);
+            for (uint32_t o = node.a; o < end; o++) {
+                const uint32_t tri = mesh.order[o];
+                if (tri >= mesh.ntris) continue;
+                const Shape th{AVBD_SHAPE_HULL, V0(), m.pos + qrot(m.rot, ld3(mesh.cent[tri])), m.rot, &mesh.tris[tri]};
+                const Dist d = shape_distance(th, convex, nullptr);
+                if (!have || d.dist < best.dist) {
+                    best = d;
+                    have = true;
+                }
+            }
+        } else {
+            if (len + 2 > 64) break;  // depth guard: keep the best so far
+            stack[len] = node.a;
+            stack[len + 1] = node.b;
+            len += 2;
+        }
+    }
+    if (!have) return none;
+    return first ? Dist{best.dist, best.pb, best.pa} : best;
+}
+// shape_distance below the rounded and compound arms (distance.rs:706-745):
+// half-spaces, terrain, meshes, then the primitive pairs.
+static __device__ __noinline__ Dist leaf_distance(const DW& w, const Shape& a, const Shape& b) {
+    if (a.kind == AVBD_SHAPE_HALFSPACE || b.kind == AVBD_SHAPE_HALFSPACE) return shape_distance(a, b, nullptr);
+    const bool ta = a.kind == AVBD_SHAPE_HEIGHTFIELD, tb = b.kind == AVBD_SHAPE_HEIGHTFIELD;
+    const bool ma = a.kind == AVBD_SHAPE_TRIMESH, mb = b.kind == AVBD_SHAPE_TRIMESH;
+    // terrain against terrain or a mesh, mesh against mesh: separation
+    if ((ta || ma) && (tb || mb)) return Dist{INFINITY, a.pos, b.pos};
+    if (ta) return hf_convex(w, a, b, true);
+    if (tb) return hf_convex(w, b, a, false);
+    if (ma) return mesh_convex(w, a, b, true);
+    if (mb) return mesh_convex(w, b, a, false);
+    return shape_distance(a, b, nullptr);
+}
+// The rounded surface sits r closer along the witness axis; an infinite
+// distance stays (round_offset, distance.rs:519-545).
+static __device__ __forceinline__ Dist round_offset(Dist d, float r, bool first, V3 pos_a, V3 pos_b) {
+    if (!isfinite(d.dist)) return d;
+    V3 axis = d.pb - d.pa;
+    if (len2(axis) <= gjk::COINCIDENT_LEN2) axis = pos_b - pos_a;
+    const V3 n = normalize_or(axis, VX());
+    if (first) return {d.dist - r, d.pa + n * r, d.pb};
+    return {d.dist - r, d.pa, d.pb - n * r};
+}
+// Pose::world_rot (shape.rs:119-134)
+static __device__ __forceinline__ Q pose_world_rot(Q parent, Q local) {
+    const Q q = qmul(parent, local);
+    const float l2 = (q.x * q.x + q.y * q.y) + (q.z * q.z + q.w * q.w);
+    if (isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && isfinite(q.w) && l2 > 1e-12f) return qnormalize(q);
+    return parent;
+}
+static __device__ __forceinline__ Shape part_shape(const PartDesc& pt, V3 pos, Q rot) {
+    return Shape{pt.kind, V3{pt.p.x, pt.p.y, pt.p.z}, pos, rot, pt.hull};
+}
+// compound_distance (distance.rs:550-599): the part reporting the smallest
+// distance, parts in order, each rounded part peeled inside its own query;
+// `first`: the compound owns pa.
+static __device__ __noinline__ Dist compound_distance(const DW& w, const Shape& c, const Shape& other, bool first) {
+    const ExtDesc e = w.exts[(uint32_t)c.p.x];
+    bool have = false;
+    Dist best{INFINITY, c.pos, other.pos};
+    for (uint32_t k = 0; k < e.count; k++) {
+        const PartDesc pt = w.parts[e.first + k];
+        const Shape child = part_shape(pt, c.pos + qrot(c.rot, ld3(pt.pos)), pose_world_rot(c.rot, ldq(pt.rot)));
+        Dist d = leaf_distance(w, child, other);
+        if (pt.p.w > 0.0f) d = round_offset(d, pt.p.w, true, child.pos, other.pos);
+        if (!have || d.dist < best.dist) {
+            best = d;
+            have = true;
+        }
+    }
+    if (!have) return first ? Dist{INFINITY, c.pos, other.pos} : Dist{INFINITY, other.pos, c.pos};
+    return first ? best : Dist{best.dist, best.pb, best.pa};
+}
+// shape_distance with the wrapper arms (distance.rs:648-705): rounded shapes
+// peel first (a's, then b's), then compounds expand; compound against
+// compound is separation.  Rounded inners and compound parts are primitives.
+static __device__ __noinline__ Dist ext_distance(const DW& w, const Shape& a, const Shape& b, float* sat_gap) {
+    if (a.kind <= AVBD_SHAPE_HULL && b.kind <= AVBD_SHAPE_HULL) return shape_distance(a, b, sat_gap);
+    Shape ia = a, ib = b;
+    float ra = 0.0f, rb = 0.0f;
+    if (a.kind == AVBD_SHAPE_ROUND) {
+        const PartDesc pt = w.parts[w.exts[(uint32_t)a.p.x].first];
+        ia = part_shape(pt, a.pos, a.rot);
+        ra = pt.p.w;
+    }
+    if (b.kind == AVBD_SHAPE_ROUND) {
+        const PartDesc pt = w.parts[w.exts[(uint32_t)b.p.x].first];
+        ib = part_shape(pt, b.pos, b.rot);
+        rb = pt.p.w;
+    }
+    Dist d;
+    if (ia.kind == AVBD_SHAPE_COMPOUND && ib.kind == AVBD_SHAPE_COMPOUND) d = Dist{INFINITY, a.pos, b.pos};
+    else if (ia.kind == AVBD_SHAPE_COMPOUND) d = compound_distance(w, ia, ib, true);
+    else if (ib.kind == AVBD_SHAPE_COMPOUND) d = compound_distance(w, ib, ia, false);
+    else d = leaf_distance(w, ia, ib);
+    if (b.kind == AVBD_SHAPE_ROUND) d = round_offset(d, rb, false, a.pos, b.pos);
+    if (a.kind == AVBD_SHAPE_ROUND) d = round_offset(d, ra, true, a.pos, b.pos);
+    return d;
+}
 // rows.rs:366-368
 static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uint32_t b) {
     uint2 fa = w.filter[a], fb = w.filter[b];

@@ -66,6 +66,8 @@ static __device__ __noinline__ V3 support_convex(const Shape& s, V3 dir) {
     return best;
 }
 static __device__ __forceinline__ V3 support_any(const Shape& s, V3 dir) {
+    // terrain and meshes have no support of their own (gjk.rs:141-155): the origin
+    if (s.kind == AVBD_SHAPE_HEIGHTFIELD || s.kind == AVBD_SHAPE_TRIMESH) return s.pos;
     return gjk_shape(s.kind) ? support_convex(s, dir) : support(s, dir);
 }
 

@@ -82,7 +82,7 @@ static __device__ __noinline__ Disc discover(const DW& w, uint32_t a, uint32_t b
         if (gap > bound) return r;
     }
     float sat = 0.0f;
-    r.d = shape_distance(sa, sb, &sat);
+    r.d = ext_distance(w, sa, sb, &sat);
     r.sgn = boxes ? sat : r.d.dist;
     discover_post(w, a, b, sa, sb, r);
     return r;
@@ -95,7 +95,7 @@ static __device__ __noinline__ bool trigger_overlap(const DW& w, uint32_t a, uin
     if (len(ld3(w.pos[a]) - ld3(w.pos[b])) > w.shp[a].w + w.shp[b].w + GEN_MARGIN) return false;
     Shape sa = shape_of(w, a), sb = shape_of(w, b);
     float sat = 0.0f;
-    Dist d = shape_distance(sa, sb, &sat);
+    Dist d = ext_distance(w, sa, sb, &sat);
     float sgn = (sa.kind == AVBD_SHAPE_BOX && sb.kind == AVBD_SHAPE_BOX) ? sat : d.dist;
     return sgn <= 0.0f;
 }

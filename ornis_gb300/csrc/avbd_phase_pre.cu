@@ -284,6 +284,9 @@ static __device__ __forceinline__ float min_dim(const DW& w, uint32_t kind, floa
         uint32_t id = (uint32_t)sp.x;
         return HALF * (id < w.nhulls ? w.hulls[id].min_ext : 0.0f);
     }
+    if (ext_kind(kind)) return w.exts[(uint32_t)sp.x].min_dim;
+    if (kind == AVBD_SHAPE_HEIGHTFIELD) return HALF * w.hfs[(uint32_t)sp.x].cell;
+    if (kind == AVBD_SHAPE_TRIMESH) return HALF * w.meshes[(uint32_t)sp.x].min_feature;
     return INFINITY;
 }
 // CCD mover gate (mod.rs:882-895): returns the step travel |v h| of a body
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(512) k_sap_small(DW w, const uint32_t* scenes,
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
     for (uint32_t h = b0 + threadIdx.x; h < b1; h += blockDim.x) {
-        if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) continue;
+        if (unbounded_kind(info_shape(w.info[h]))) continue;
         int k = atomicAdd(&cnt, 1);
         kv[k] = ((unsigned long long)f2key(w.aabb_lo[h].x) << 32) | h;
     }
@@ -379,7 +382,7 @@ __global__ void __launch_bounds__(512) k_sap_small(DW w, const uint32_t* scenes,
 __global__ void k_sap_keys(DW w, uint32_t b0, uint32_t b1) {
     uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= b1) return;
-    bool plane = info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE;
+    bool plane = unbounded_kind(info_shape(w.info[h]));
     w.sort_key[h - b0] = plane ? 0xffffffffu : f2key(w.aabb_lo[h].x);
     w.sort_idx[h - b0] = h;
 }
@@ -387,11 +390,11 @@ __global__ void k_sap_sweep(DW w, uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t a = w.sort_idx[i];
-    if (info_shape(w.info[a]) == AVBD_SHAPE_HALFSPACE) return;
+    if (unbounded_kind(info_shape(w.info[a]))) return;
     float4 alo = w.aabb_lo[a], ahi = w.aabb_hi[a];
     for (uint32_t j = i + 1; j < n; j++) {
         uint32_t b = w.sort_idx[j];
-        if (info_shape(w.info[b]) == AVBD_SHAPE_HALFSPACE) break;
+        if (unbounded_kind(info_shape(w.info[b]))) break;
         float4 blo = w.aabb_lo[b];
         if (blo.x > ahi.x) break;
         if (overlap_yz(alo, ahi, blo, w.aabb_hi[b])) emit_candidate(w, a, b);
@@ -434,7 +437,7 @@ __device__ __forceinline__ void row_cells(const DW& w, uint32_t h, double cell, 
 __global__ void k_sap_extent(DW w, uint32_t b0, uint32_t b1, float* ext) {
     float m = 0.0f;
     for (uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x; h < b1; h += gridDim.x * blockDim.x) {
-        if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) continue;
+        if (unbounded_kind(info_shape(w.info[h]))) continue;
         float4 lo = w.aabb_lo[h], hi = w.aabb_hi[h];
         m = fmaxf(m, fmaxf(hi.x - lo.x, fmaxf(hi.y - lo.y, hi.z - lo.z)));
     }
@@ -444,7 +447,7 @@ __global__ void k_sap_extent(DW w, uint32_t b0, uint32_t b1, float* ext) {
 __global__ void k_sap_row_keys(DW w, uint32_t b0, uint32_t b1, const float* ext, uint32_t* row_key) {
     uint32_t h = b0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= b1) return;
-    bool plane = info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE;
+    bool plane = unbounded_kind(info_shape(w.info[h]));
     uint32_t rk = 0xffffffffu;
     if (!plane) {
         int cy, cz;
@@ -521,7 +524,10 @@ __global__ void k_sap_row_sweep(DW w, uint32_t n, const float* ext) {
 __global__ void k_plane_cands(DW w) {
     uint32_t h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= (uint32_t)w.N) return;
-    if (info_shape(w.info[h]) == AVBD_SHAPE_HALFSPACE) return;
+    // an unbounded body pairs with the unbounded bodies listed before it
+    // (each such pair once; they meet as separation or a static shell)
+    const uint32_t kh = info_shape(w.info[h]);
+    const bool unb = unbounded_kind(kh);
     uint32_t s = w.scene_of[h];
     V3 x = ld3(w.pos[h]);
     float vh = len(ld3(w.vel[h]));
@@ -529,7 +535,11 @@ __global__ void k_plane_cands(DW w) {
     float rb = w.shp[h].w;
     for (uint32_t k = w.plane_off[s]; k < w.plane_off[s + 1]; k++) {
         uint32_t pl = w.plane_list[k];
-        if (find_old_pair(w, min(pl, h), max(pl, h)) < 0) {
+        if (unb && pl >= h) break;  // listed in ascending handle order
+        // two half-spaces never meet (distance.rs:619-621): not a candidate
+        if (kh == AVBD_SHAPE_HALFSPACE && info_shape(w.info[pl]) == AVBD_SHAPE_HALFSPACE) continue;
+        // terrain and meshes: no bound to prune by (rows.rs:274)
+        if (info_shape(w.info[pl]) == AVBD_SHAPE_HALFSPACE && find_old_pair(w, min(pl, h), max(pl, h)) < 0) {
             float4 sp = w.shp[pl];
             V3 n = qrot(ldq(w.rot[pl]), V3{sp.x, sp.y, sp.z});
             float dlow = dot(x - ld3(w.pos[pl]), n) - rb;
@@ -588,7 +598,7 @@ static __device__ __noinline__ Cast cast_one(const DW& w, uint32_t h, uint32_t o
     float t = 0.0f;
     for (int it = 0; it < 24; it++) {
         mv.pos = p0 + dir * t;
-        Dist d = shape_distance(mv, tg, nullptr);
+        Dist d = ext_distance(w, mv, tg, nullptr);
         if (d.dist <= SHAPE_TOUCH) {
             if (t > 0.0f) {
                 c.hit = true;

@@ -160,7 +160,8 @@ extern "C" int avbd_scene_step_static(const AvbdParams* params, const AvbdBody* 
         for (int k = 0; k < 16; k++)
             if (!std::isfinite(f[k])) return AVBD_ERR_NONFINITE;
         if (!std::isfinite(bodies[i].mass) || !std::isfinite(bodies[i].inv_mass)) return AVBD_ERR_NONFINITE;
-        if (bodies[i].shape == AVBD_SHAPE_HULL) return AVBD_ERR_UNSUPPORTED;  // hull tables live in worlds
+        // hull, rounded and compound tables live in worlds
+        if (bodies[i].shape >= AVBD_SHAPE_HULL) return AVBD_ERR_UNSUPPORTED;
     }
     unsigned char* base = nullptr;
     int rc = static_base(&base);

@@ -101,8 +101,41 @@ struct HostHull {
     float bound, min_ext;
 };
 
-float shape_bound(uint32_t shape, const float* p, const std::vector<HostHull>& hulls) {  // rows.rs:253-292
+// A rounded shape (one part) or a compound as the host keeps it, with the
+// measures the engine reads from it (rows.rs:279-290, :393-400).
+struct HostExt {
+    bool compound;
+    std::vector<AvbdShapePart> parts;
+    float unit_inertia[3];
+    float bound, min_dim;
+};
+
+// A heightfield as registered, with its sample range (shape.rs:1571-1583).
+struct HostHf {
+    uint32_t rows, cols;
+    float cell, y_min, y_max;
+    std::vector<float> h;
+};
+// A triangle mesh: the registration's input (for snapshots), its
+// centroid-relative triangle hulls, centroids, tree and permutation.
+struct HostMesh {
+    std::vector<float> verts;
+    std::vector<uint32_t> tris_in;
+    std::vector<HostHull> tris;
+    std::vector<float4> cent;
+    std::vector<MeshNodeD> nodes;
+    std::vector<uint32_t> order;
+    float bound, min_feature;
+};
+
+float shape_bound(uint32_t shape, const float* p, const std::vector<HostHull>& hulls,
+                  const std::vector<HostExt>& exts) {  // rows.rs:253-292
     switch (shape) {
+        case AVBD_SHAPE_ROUND:
+        case AVBD_SHAPE_COMPOUND: {
+            size_t id = (size_t)p[0];
+            return id < exts.size() ? exts[id].bound : 0.0f;
+        }
         case AVBD_SHAPE_SPHERE: return p[0];
         case AVBD_SHAPE_BOX: return std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]);
         case AVBD_SHAPE_CAPSULE: return p[1] + p[0];
@@ -147,7 +180,14 @@ void shape_inertia(uint32_t shape, const float* sp, float mass, float out[3]) {
     }
 }
 // rest inertia of a body: its shape's, or the hull's per-unit-mass inertia times the mass
-static void rest_inertia(const AvbdBody& b, float mass, const std::vector<HostHull>& hulls, float out[3]) {
+static void rest_inertia(const AvbdBody& b, float mass, const std::vector<HostHull>& hulls,
+                         const std::vector<HostExt>& exts, float out[3]) {
+    if (b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND) {
+        size_t id = (size_t)b.shape_params[0];
+        for (int k = 0; k < 3; k++)
+            out[k] = (id < exts.size() && mass > 0.0f && std::isfinite(mass)) ? exts[id].unit_inertia[k] * mass : 0.0f;
+        return;
+    }
     if (b.shape != AVBD_SHAPE_HULL) {
         shape_inertia(b.shape, b.shape_params, mass, out);
         return;
@@ -215,7 +255,10 @@ struct AvbdWorld {
     bool has_trig = false;
     Alloc evmem;  // the event queues: kept across reallocations of the world
     std::vector<HostHull> hulls;
-    Alloc hullmem;
+    std::vector<HostExt> exts;  // rounded and compound shapes
+    std::vector<HostHf> hfs;    // heightfields
+    std::vector<HostMesh> meshes;  // triangle meshes
+    Alloc hullmem;              // the hull, rounded, compound, terrain and mesh tables
     int graph_cols = 0;
     size_t graph_nodes = 0;       // kernel nodes in one captured substep (no events)
     size_t graph_nodes_emit = 0;  // ... in one that reports events
@@ -542,6 +585,17 @@ static int upload_all(AvbdWorld* W) {
     uint32_t S = (uint32_t)W->scene_off.size() - 1;
     if (N == 0) return AVBD_OK;
     uint32_t need = std::max(default_cand_cap(N), (uint32_t)W->pairs.size() + 1024u);
+    {
+        // terrain and meshes pair with every body of their scene (no bound)
+        uint64_t extra = 0;
+        for (uint32_t s = 0; s + 1 < (uint32_t)W->scene_off.size(); s++) {
+            uint64_t t = 0;
+            for (uint32_t h = W->scene_off[s]; h < W->scene_off[s + 1]; h++)
+                t += W->bodies[h].shape == AVBD_SHAPE_HEIGHTFIELD || W->bodies[h].shape == AVBD_SHAPE_TRIMESH;
+            extra += t * (W->scene_off[s + 1] - W->scene_off[s]);
+        }
+        need = (uint32_t)std::min<uint64_t>((uint64_t)need + extra, 0x7fffffffull);
+    }
     if (N != W->n_alloc || J != W->j_alloc || need > W->cand_cap || !W->w.ctr) {
         uint32_t cap = std::max(need, W->cand_cap);
         int rc = alloc_device(W, N, J, cap);
@@ -577,9 +631,110 @@ static int upload_all(AvbdWorld* W) {
         w.hulls = dd;
         w.nhulls = (uint32_t)desc.size();
     }
-    for (uint32_t h = 0; h < N; h++)
-        if (W->bodies[h].shape == AVBD_SHAPE_HULL && !((size_t)W->bodies[h].shape_params[0] < W->hulls.size()))
+    // rounded and compound tables, after the hulls their parts point at
+    w.exts = nullptr;
+    w.parts = nullptr;
+    w.nexts = 0;
+    if (!W->exts.empty()) {
+        size_t np = 0;
+        for (const HostExt& e : W->exts) np += e.parts.size();
+        ExtDesc* de = W->hullmem.get<ExtDesc>(W->exts.size());
+        PartDesc* dp = W->hullmem.get<PartDesc>(np);
+        if (!de || !dp) return AVBD_ERR_DEVICE;
+        std::vector<ExtDesc> ed;
+        std::vector<PartDesc> pd;
+        for (const HostExt& e : W->exts) {
+            ed.push_back(ExtDesc{(uint32_t)pd.size(), (uint32_t)e.parts.size(), e.compound ? 1u : 0u, e.min_dim});
+            for (const AvbdShapePart& q : e.parts) {
+                PartDesc d{};
+                d.p = make_float4(q.params[0], q.params[1], q.params[2], q.border_radius);
+                d.pos = make_float4(q.position[0], q.position[1], q.position[2], 0.0f);
+                d.rot = make_float4(q.orientation[0], q.orientation[1], q.orientation[2], q.orientation[3]);
+                d.kind = q.shape;
+                d.hull = q.shape == AVBD_SHAPE_HULL ? w.hulls + (size_t)q.params[0] : nullptr;
+                pd.push_back(d);
+            }
+        }
+        CK(cudaMemcpy(de, ed.data(), ed.size() * sizeof(ExtDesc), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dp, pd.data(), pd.size() * sizeof(PartDesc), cudaMemcpyHostToDevice));
+        w.exts = de;
+        w.parts = dp;
+        w.nexts = (uint32_t)ed.size();
+    }
+    w.hfs = nullptr;
+    w.meshes = nullptr;
+    w.nhfs = w.nmeshes = 0;
+    if (!W->hfs.empty()) {
+        std::vector<HfDesc> hd;
+        for (const HostHf& f : W->hfs) {
+            float* dh = W->hullmem.get<float>(f.h.size());
+            if (!dh) return AVBD_ERR_DEVICE;
+            CK(cudaMemcpy(dh, f.h.data(), f.h.size() * 4, cudaMemcpyHostToDevice));
+            hd.push_back(HfDesc{dh, f.rows, f.cols, f.cell, f.y_min});
+        }
+        HfDesc* dd = W->hullmem.get<HfDesc>(hd.size());
+        if (!dd) return AVBD_ERR_DEVICE;
+        CK(cudaMemcpy(dd, hd.data(), hd.size() * sizeof(HfDesc), cudaMemcpyHostToDevice));
+        w.hfs = dd;
+        w.nhfs = (uint32_t)hd.size();
+    }
+    if (!W->meshes.empty()) {
+        std::vector<MeshDesc> md;
+        for (const HostMesh& m : W->meshes) {
+            MeshDesc d{};
+            d.ntris = (uint32_t)m.tris.size();
+            d.nnodes = (uint32_t)m.nodes.size();
+            d.norder = (uint32_t)m.order.size();
+            d.min_feature = m.min_feature;
+            std::vector<HullDesc> th;
+            float4* dv = W->hullmem.get<float4>(3 * m.tris.size());
+            uint32_t* df = W->hullmem.get<uint32_t>(6 * m.tris.size());
+            HullDesc* dt = W->hullmem.get<HullDesc>(m.tris.size());
+            float4* dc = W->hullmem.get<float4>(m.cent.size());
+            MeshNodeD* dn = W->hullmem.get<MeshNodeD>(m.nodes.size());
+            uint32_t* dord = W->hullmem.get<uint32_t>(m.order.size());
+            if (!dv || !df || !dt || !dc || !dn || !dord) return AVBD_ERR_DEVICE;
+            for (size_t t = 0; t < m.tris.size(); t++) {
+                const HostHull& hh = m.tris[t];
+                CK(cudaMemcpy(dv + 3 * t, hh.v.data(), 3 * 16, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(df + 6 * t, hh.f.data(), 6 * 4, cudaMemcpyHostToDevice));
+                th.push_back(HullDesc{dv + 3 * t, df + 6 * t, 3u, 2u, hh.bound, hh.min_ext});
+            }
+            if (!th.empty()) CK(cudaMemcpy(dt, th.data(), th.size() * sizeof(HullDesc), cudaMemcpyHostToDevice));
+            if (!m.cent.empty()) CK(cudaMemcpy(dc, m.cent.data(), m.cent.size() * 16, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(dn, m.nodes.data(), m.nodes.size() * sizeof(MeshNodeD), cudaMemcpyHostToDevice));
+            if (!m.order.empty()) CK(cudaMemcpy(dord, m.order.data(), m.order.size() * 4, cudaMemcpyHostToDevice));
+            d.tris = dt;
+            d.cent = dc;
+            d.nodes = dn;
+            d.order = dord;
+            md.push_back(d);
+        }
+        MeshDesc* dd = W->hullmem.get<MeshDesc>(md.size());
+        if (!dd) return AVBD_ERR_DEVICE;
+        CK(cudaMemcpy(dd, md.data(), md.size() * sizeof(MeshDesc), cudaMemcpyHostToDevice));
+        w.meshes = dd;
+        w.nmeshes = (uint32_t)md.size();
+    }
+    for (uint32_t h = 0; h < N; h++) {
+        const AvbdBody& b = W->bodies[h];
+        if (b.shape > AVBD_SHAPE_TRIMESH) return AVBD_ERR_UNSUPPORTED;
+        if (b.shape == AVBD_SHAPE_HEIGHTFIELD || b.shape == AVBD_SHAPE_TRIMESH) {
+            // static colliders (shape.rs:181-192): no moving terrain or mesh
+            if (b.body_type == AVBD_BODY_DYNAMIC) return AVBD_ERR_UNSUPPORTED;
+            const size_t id = (size_t)b.shape_params[0];
+            const size_t n = b.shape == AVBD_SHAPE_HEIGHTFIELD ? W->hfs.size() : W->meshes.size();
+            if (!(b.shape_params[0] >= 0.0f && id < n)) return AVBD_ERR_INVALID_ARG;
+        }
+        if (b.shape == AVBD_SHAPE_HULL && !((size_t)b.shape_params[0] < W->hulls.size()))
             return AVBD_ERR_INVALID_ARG;  // names a hull that was never added
+        if (b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND) {
+            const size_t id = (size_t)b.shape_params[0];
+            if (!(b.shape_params[0] >= 0.0f && id < W->exts.size()) ||
+                W->exts[id].compound != (b.shape == AVBD_SHAPE_COMPOUND))
+                return AVBD_ERR_INVALID_ARG;  // names no shape of its kind
+        }
+    }
     // static per-body data
     std::vector<uint32_t> scene_of(N), info(N);
     std::vector<float4> shp(N), inertia_rest(N);
@@ -591,7 +746,9 @@ static int upload_all(AvbdWorld* W) {
         plane_off[s] = (uint32_t)plane_list.size();
         for (uint32_t h = W->scene_off[s]; h < W->scene_off[s + 1]; h++) {
             scene_of[h] = s;
-            if (W->bodies[h].shape == AVBD_SHAPE_HALFSPACE) plane_list.push_back(h);
+            const uint32_t k = W->bodies[h].shape;  // half-spaces, terrain, meshes
+            if (k == AVBD_SHAPE_HALFSPACE || k == AVBD_SHAPE_HEIGHTFIELD || k == AVBD_SHAPE_TRIMESH)
+                plane_list.push_back(h);
         }
     }
     plane_off[S] = (uint32_t)plane_list.size();
@@ -601,10 +758,10 @@ static int upload_all(AvbdWorld* W) {
         if (b.flags & AVBD_FLAG_TRIGGER) W->has_trig = true;
         info[h] = (b.shape & 15u) | ((b.body_type & 3u) << 4) | ((b.flags & AVBD_FLAG_TRIGGER) ? 64u : 0u);
         shp[h] = make_float4(b.shape_params[0], b.shape_params[1], b.shape_params[2],
-                             shape_bound(b.shape, b.shape_params, W->hulls));
+                             shape_bound(b.shape, b.shape_params, W->hulls, W->exts));
         float in[3];
         bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
-        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, in);
+        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, W->exts, in);
         inertia_rest[h] = make_float4(in[0], in[1], in[2], 0.0f);
         inv_rest[h] = free_mass ? 1.0f / b.mass : 0.0f;
         const AvbdBodyAux& a = W->aux[h];
@@ -1570,9 +1727,226 @@ int avbd_world_add_bodies(AvbdWorld* W, const AvbdBody* bodies, uint32_t n, uint
     return AVBD_OK;
 }
 
+// Shape::try_round / try_compound (collision/shape.rs:556-575) over
+// primitive parts, with the bound and minimum dimension the engine reads
+// (rows.rs:279-290, :393-400).
+static int make_ext(const AvbdWorld* W, bool compound, const AvbdShapePart* parts, uint32_t n,
+                    const float* unit_inertia, HostExt& e) {
+    if (!W || !parts || !unit_inertia || n == 0 || (!compound && n != 1)) return AVBD_ERR_INVALID_ARG;
+    e.compound = compound;
+    auto len3 = [](const float* v) { return std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]); };
+    auto part_bound = [&](const AvbdShapePart& p) {
+        float r;
+        switch (p.shape) {
+            case AVBD_SHAPE_SPHERE: r = p.params[0]; break;
+            case AVBD_SHAPE_BOX: r = len3(p.params); break;
+            case AVBD_SHAPE_CAPSULE: r = p.params[1] + p.params[0]; break;
+            case AVBD_SHAPE_HULL: r = W->hulls[(size_t)p.params[0]].bound; break;
+            default: r = std::sqrt(p.params[0] * p.params[0] + p.params[1] * p.params[1]);  // cylinder, cone
+        }
+        return p.border_radius > 0.0f ? r + std::fmax(p.border_radius, 0.0f) : r;
+    };
+    auto part_min_dim = [&](const AvbdShapePart& p) {
+        float m;
+        switch (p.shape) {
+            case AVBD_SHAPE_SPHERE: m = p.params[0]; break;
+            case AVBD_SHAPE_BOX: m = std::fmin(p.params[0], std::fmin(p.params[1], p.params[2])); break;
+            case AVBD_SHAPE_CAPSULE: m = p.params[0]; break;
+            case AVBD_SHAPE_CYLINDER: m = std::fmin(p.params[0], p.params[1]); break;
+            case AVBD_SHAPE_CONE: m = 0.5f * std::fmin(p.params[0], p.params[1]); break;
+            default: m = 0.5f * W->hulls[(size_t)p.params[0]].min_ext;  // hull
+        }
+        return p.border_radius > 0.0f ? std::fmin(m, std::fmax(p.border_radius, 0.0f) * 2.0f) : m;
+    };
+    for (uint32_t i = 0; i < n; i++) {
+        const AvbdShapePart& q = parts[i];
+        if (q.shape > AVBD_SHAPE_HULL || q.shape == AVBD_SHAPE_HALFSPACE) return AVBD_ERR_UNSUPPORTED;
+        if (!compound && !(std::isfinite(q.border_radius) && q.border_radius > 0.0f)) return AVBD_ERR_INVALID_ARG;
+        if (!std::isfinite(q.border_radius) || q.border_radius < 0.0f) return AVBD_ERR_INVALID_ARG;
+        if (q.shape == AVBD_SHAPE_HULL && !(q.params[0] >= 0.0f && (size_t)q.params[0] < W->hulls.size()))
+            return AVBD_ERR_INVALID_ARG;
+        e.parts.push_back(q);
+    }
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(unit_inertia[k])) return AVBD_ERR_NONFINITE;
+    std::memcpy(e.unit_inertia, unit_inertia, 12);
+    if (compound) {
+        e.bound = 0.0f;
+        e.min_dim = INFINITY;
+        for (const AvbdShapePart& p : e.parts) {
+            e.bound = std::fmax(e.bound, part_bound(p) + len3(p.position));
+            e.min_dim = std::fmin(e.min_dim, part_min_dim(p));
+        }
+    } else {
+        e.bound = part_bound(e.parts[0]);
+        e.min_dim = part_min_dim(e.parts[0]);
+    }
+    return AVBD_OK;
+}
+// Heightfield::new (shape.rs:1485-1505, invariants.rs:403-425) with its
+// sample range (shape.rs:1571-1583).
+static int make_hf(uint32_t rows, uint32_t cols, float cell, const float* heights, HostHf& f) {
+    if (rows == 0 || cols == 0 || !heights || !std::isfinite(cell) || !(cell > 0.0f)) return AVBD_ERR_INVALID_ARG;
+    if ((uint64_t)rows * cols > (1ull << 28)) return AVBD_ERR_INVALID_ARG;
+    f.rows = rows;
+    f.cols = cols;
+    f.cell = cell;
+    f.y_min = INFINITY;
+    f.y_max = -INFINITY;
+    f.h.assign(heights, heights + (size_t)rows * cols);
+    for (float h : f.h) {
+        if (!std::isfinite(h)) return AVBD_ERR_NONFINITE;
+        f.y_min = std::fmin(f.y_min, h);
+        f.y_max = std::fmax(f.y_max, h);
+    }
+    return AVBD_OK;
+}
+// TriMesh::build_bvh / split (shape.rs:1793-1890): median splits of the
+// longest axis over a stable centroid sort, leaves of up to 4 triangles.
+static uint32_t mesh_split(const std::vector<std::array<float, 6>>& bounds, const std::vector<float4>& cent,
+                           uint32_t* order, size_t n, uint32_t base, std::vector<MeshNodeD>& nodes) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::fmin(lo[k], bounds[order[i]][k]);
+            hi[k] = std::fmax(hi[k], bounds[order[i]][3 + k]);
+        }
+    const uint32_t here = (uint32_t)nodes.size();
+    nodes.push_back(MeshNodeD{{lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}, 1u, base, (uint32_t)n});
+    if (n <= 4) return here;
+    const float e[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    const int axis = (e[0] >= e[1] && e[0] >= e[2]) ? 0 : (e[1] >= e[2] ? 1 : 2);
+    auto key = [&](uint32_t t) { return axis == 0 ? cent[t].x : (axis == 1 ? cent[t].y : cent[t].z); };
+    std::stable_sort(order, order + n, [&](uint32_t x, uint32_t y) { return key(x) < key(y); });
+    if (key(order[0]) == key(order[n - 1])) return here;  // all equal: a leaf
+    const size_t mid = n / 2;
+    const uint32_t left = mesh_split(bounds, cent, order, mid, base, nodes);
+    const uint32_t right = mesh_split(bounds, cent, order + mid, n - mid, base + (uint32_t)mid, nodes);
+    nodes[here].leaf = 0u;
+    nodes[here].a = left;
+    nodes[here].b = right;
+    return here;
+}
+// TriMesh::from_indexed / from_triangles (shape.rs:1646-1772): slivers
+// dropped, each triangle a centroid-relative hull with both windings; a
+// triangle whose corners weld below three points (ConvexHull::from_vertices
+// welds closer than 1e-6, shape.rs:1304-1325) is refused.
+static int make_mesh(const float* verts, uint32_t nv, const uint32_t* tris, uint32_t nt, HostMesh& m) {
+    if ((nv && !verts) || (nt && !tris)) return AVBD_ERR_INVALID_ARG;
+    for (uint32_t i = 0; i < 3 * nv; i++)
+        if (!std::isfinite(verts[i])) return AVBD_ERR_NONFINITE;
+    m.verts.assign(verts, verts + 3 * (size_t)nv);
+    m.tris_in.assign(tris, tris + 3 * (size_t)nt);
+    using namespace avbd;
+    auto vert = [&](uint32_t i) { return V3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]}; };
+    m.bound = 0.0f;
+    m.min_feature = INFINITY;
+    for (uint32_t t = 0; t < nt; t++) {
+        for (int k = 0; k < 3; k++)
+            if (tris[3 * t + k] >= nv) return AVBD_ERR_INVALID_ARG;
+        const V3 v[3] = {vert(tris[3 * t]), vert(tris[3 * t + 1]), vert(tris[3 * t + 2])};
+        if (len2(cross(v[1] - v[0], v[2] - v[0])) < 1e-12f) continue;  // a sliver
+        const V3 ends[3][2] = {{v[0], v[1]}, {v[1], v[2]}, {v[2], v[0]}};
+        for (const auto& e : ends) m.min_feature = std::fmin(m.min_feature, len(e[1] - e[0]));
+        for (const V3& p : v) m.bound = std::fmax(m.bound, len(p));
+        const V3 c = (v[0] + v[1] + v[2]) / 3.0f;
+        HostHull h;
+        for (const V3& p : v) {
+            const V3 q = p - c;
+            bool near = false;
+            for (const float4& w : h.v) near = near || len2(V3{w.x, w.y, w.z} - q) < 1e-6f * 1e-6f;
+            if (!near) h.v.push_back(make_float4(q.x, q.y, q.z, 0.0f));
+        }
+        if (h.v.size() != 3) return AVBD_ERR_INVALID_ARG;
+        h.f = {0u, 1u, 2u, 0u, 2u, 1u};
+        h.unit_inertia[0] = h.unit_inertia[1] = h.unit_inertia[2] = 0.0f;
+        // the hull measures (rows.rs:268-272, shape.rs:1468-1479)
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        h.bound = 0.0f;
+        for (const float4& w : h.v) {
+            const float p[3] = {w.x, w.y, w.z};
+            h.bound = std::fmax(h.bound, std::sqrt((p[0] * p[0] + p[1] * p[1]) + p[2] * p[2]));
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::fmin(lo[k], p[k]);
+                hi[k] = std::fmax(hi[k], p[k]);
+            }
+        }
+        h.min_ext = std::fmax(std::fmin(hi[0] - lo[0], std::fmin(hi[1] - lo[1], hi[2] - lo[2])), 0.0f);
+        m.cent.push_back(make_float4(c.x, c.y, c.z, 0.0f));
+        m.tris.push_back(std::move(h));
+    }
+    if (m.tris.empty()) m.min_feature = 0.0f;
+    std::vector<std::array<float, 6>> bounds;
+    for (size_t t = 0; t < m.tris.size(); t++) {
+        std::array<float, 6> b{INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (const float4& q : m.tris[t].v) {
+            const float w[3] = {q.x + m.cent[t].x, q.y + m.cent[t].y, q.z + m.cent[t].z};
+            for (int k = 0; k < 3; k++) {
+                b[k] = std::fmin(b[k], w[k]);
+                b[3 + k] = std::fmax(b[3 + k], w[k]);
+            }
+        }
+        bounds.push_back(b);
+    }
+    m.order.resize(bounds.size());
+    std::iota(m.order.begin(), m.order.end(), 0u);
+    m.nodes.clear();
+    if (!m.order.empty()) mesh_split(bounds, m.cent, m.order.data(), m.order.size(), 0u, m.nodes);
+    if (m.nodes.empty()) m.nodes.push_back(MeshNodeD{{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, 1u, 0u, 0u});
+    return AVBD_OK;
+}
+static int add_ext(AvbdWorld* W, bool compound, const AvbdShapePart* parts, uint32_t n, const float* unit_inertia,
+                   uint32_t* id) {
+    HostExt e;
+    int rc = make_ext(W, compound, parts, n, unit_inertia, e);
+    if (rc) return rc;
+    rc = host_edit(W);  // the tables are rebuilt with the next full upload
+    if (rc) return rc;
+    if (id) *id = (uint32_t)W->exts.size();
+    W->exts.push_back(std::move(e));
+    return AVBD_OK;
+}
+
 // A convex hull shared by bodies of shape AVBD_SHAPE_HULL (ConvexHull,
 // collision/shape.rs:317-365): the reference's centroid-relative vertices and
 // triangle faces, and its inertia per unit mass (ConvexHull::try_inertia).
+int avbd_world_add_round(AvbdWorld* W, const AvbdShapePart* inner, const float* unit_inertia, uint32_t* id) {
+    return add_ext(W, false, inner, 1, unit_inertia, id);
+}
+
+int avbd_world_add_compound(AvbdWorld* W, const AvbdShapePart* parts, uint32_t n, const float* unit_inertia,
+                            uint32_t* id) {
+    return add_ext(W, true, parts, n, unit_inertia, id);
+}
+
+int avbd_world_add_heightfield(AvbdWorld* W, uint32_t rows, uint32_t cols, float cell, const float* heights,
+                               uint32_t* id) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    HostHf f;
+    int rc = make_hf(rows, cols, cell, heights, f);
+    if (rc) return rc;
+    cudaSetDevice(W->device);
+    rc = host_edit(W);  // the tables are rebuilt with the next full upload
+    if (rc) return rc;
+    if (id) *id = (uint32_t)W->hfs.size();
+    W->hfs.push_back(std::move(f));
+    return AVBD_OK;
+}
+
+int avbd_world_add_trimesh(AvbdWorld* W, const float* verts, uint32_t nverts, const uint32_t* tris, uint32_t ntris,
+                           uint32_t* id) {
+    if (!W) return AVBD_ERR_INVALID_ARG;
+    HostMesh m;
+    int rc = make_mesh(verts, nverts, tris, ntris, m);
+    if (rc) return rc;
+    cudaSetDevice(W->device);
+    rc = host_edit(W);
+    if (rc) return rc;
+    if (id) *id = (uint32_t)W->meshes.size();
+    W->meshes.push_back(std::move(m));
+    return AVBD_OK;
+}
+
 int avbd_world_add_hull(AvbdWorld* W, const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf,
                         const float* unit_inertia, uint32_t* hull_id) {
     if (!W || !unit_inertia || (nv && !verts) || (nf && !faces)) return AVBD_ERR_INVALID_ARG;
@@ -1664,7 +2038,7 @@ static void wake_host(AvbdWorld* W, uint32_t h) {
     if (b.body_type == AVBD_BODY_DYNAMIC) {
         bool free_mass = b.mass > 0.0f && std::isfinite(b.mass);
         b.inv_mass = free_mass ? 1.0f / b.mass : 0.0f;
-        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, b.inertia);
+        rest_inertia(b, free_mass ? b.mass : 0.0f, W->hulls, W->exts, b.inertia);
     }
 }
 
@@ -2515,7 +2889,8 @@ int avbd_world_drain_trigger_events(AvbdWorld* W, AvbdTriggerEvent* out, uint32_
 int avbd_adjoint_forward(AvbdWorld* W, int32_t steps, int32_t substeps, int32_t every) {
     if (!W || steps <= 0 || substeps <= 0 || every <= 0) return AVBD_ERR_INVALID_ARG;
     for (const AvbdBody& b : W->bodies)
-        if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f) return AVBD_ERR_UNSUPPORTED;
+        if (b.rolling_friction > 0.0f || b.torsion_friction > 0.0f || b.shape >= AVBD_SHAPE_ROUND)
+            return AVBD_ERR_UNSUPPORTED;
     // the reverse sweep differentiates ball and revolute rows without motors
     for (const JointRec& j : W->joints)
         if (j.kind > AVBD_JOINT_REVOLUTE || j.mot_max > 0.0f) return AVBD_ERR_UNSUPPORTED;
@@ -2728,9 +3103,10 @@ struct SnapSettings {
     uint32_t reserved;
 };
 static_assert(sizeof(SnapSettings) == 48, "settings record");
-// Format 1 stores the joint record as the world holds it: a change of its
-// layout is a new format version.
-static_assert(sizeof(JointRec) == 364, "format 1 joint record");
+// The format stores the joint record as the world holds it: a change of
+// its layout is a new format version.
+static_assert(sizeof(JointRec) == 364, "format 2 joint record");
+static_assert(sizeof(AvbdShapePart) == 48, "format 2 shape part record");
 
 // The event state a snapshot carries.
 struct SnapEvents {
@@ -2861,6 +3237,31 @@ void snap_payload(const AvbdWorld* W, const SnapEvents& e, SnapOut& o) {
         o.vec(hh.v);
         o.vec(hh.f);
     }
+    const uint32_t nx = (uint32_t)W->exts.size();
+    o.put(&nx, 4);
+    for (const HostExt& x : W->exts) {
+        const uint32_t flag = x.compound ? 1u : 0u, np = (uint32_t)x.parts.size();
+        o.put(&flag, 4);
+        o.put(&np, 4);
+        o.put(x.unit_inertia, 12);
+        o.vec(x.parts);
+    }
+    const uint32_t nf = (uint32_t)W->hfs.size(), nm = (uint32_t)W->meshes.size();
+    o.put(&nf, 4);
+    for (const HostHf& f : W->hfs) {
+        o.put(&f.rows, 4);
+        o.put(&f.cols, 4);
+        o.put(&f.cell, 4);
+        o.vec(f.h);
+    }
+    o.put(&nm, 4);
+    for (const HostMesh& m : W->meshes) {
+        const uint32_t nvf = (uint32_t)m.verts.size(), nti = (uint32_t)m.tris_in.size();
+        o.put(&nvf, 4);
+        o.put(&nti, 4);
+        o.vec(m.verts);
+        o.vec(m.tris_in);
+    }
     o.put(e.evs, sizeof(e.evs));
     o.vec(e.tof);
     o.vec(e.tkeys);
@@ -2900,6 +3301,48 @@ int snap_parse(const void* buf, uint64_t size, AvbdWorld* W, SnapEvents& e) {
         for (uint32_t x : hh.f)
             if (x >= nv) return AVBD_ERR_FORMAT;
         W->hulls.push_back(std::move(hh));
+    }
+    uint32_t nx = 0;
+    in.get(&nx, 4);
+    for (uint32_t k = 0; k < nx && in.ok; k++) {
+        uint32_t flag = 0, np = 0;
+        float ui[3];
+        std::vector<AvbdShapePart> parts;
+        in.get(&flag, 4);
+        in.get(&np, 4);
+        in.get(ui, 12);
+        in.vec(parts, np);
+        if (!in.ok || flag > 1u) return AVBD_ERR_FORMAT;
+        HostExt x;
+        if (make_ext(W, flag != 0, parts.data(), np, ui, x)) return AVBD_ERR_FORMAT;
+        W->exts.push_back(std::move(x));
+    }
+    uint32_t nf = 0, nm = 0;
+    in.get(&nf, 4);
+    for (uint32_t k = 0; k < nf && in.ok; k++) {
+        uint32_t rows = 0, cols = 0;
+        float cell = 0.0f;
+        std::vector<float> h;
+        in.get(&rows, 4);
+        in.get(&cols, 4);
+        in.get(&cell, 4);
+        in.vec(h, (uint64_t)rows * cols);
+        HostHf f;
+        if (!in.ok || make_hf(rows, cols, cell, h.data(), f)) return AVBD_ERR_FORMAT;
+        W->hfs.push_back(std::move(f));
+    }
+    in.get(&nm, 4);
+    for (uint32_t k = 0; k < nm && in.ok; k++) {
+        uint32_t nvf = 0, nti = 0;
+        std::vector<float> v;
+        std::vector<uint32_t> t;
+        in.get(&nvf, 4);
+        in.get(&nti, 4);
+        in.vec(v, nvf);
+        in.vec(t, nti);
+        HostMesh m;
+        if (!in.ok || nvf % 3 || nti % 3 || make_mesh(v.data(), nvf / 3, t.data(), nti / 3, m)) return AVBD_ERR_FORMAT;
+        W->meshes.push_back(std::move(m));
     }
     in.get(e.evs, sizeof(e.evs));
     in.vec(e.tof, (uint64_t)N + 1);
@@ -2942,8 +3385,20 @@ int snap_parse(const void* buf, uint64_t size, AvbdWorld* W, SnapEvents& e) {
         return (uint32_t)(std::upper_bound(W->scene_off.begin(), W->scene_off.end(), x) - W->scene_off.begin()) - 1;
     };
     for (const AvbdBody& b : W->bodies) {
-        if (!body_finite(b)) return AVBD_ERR_FORMAT;
+        if (!body_finite(b) || b.shape > AVBD_SHAPE_TRIMESH) return AVBD_ERR_FORMAT;
+        if (b.shape == AVBD_SHAPE_HEIGHTFIELD &&
+            (!(b.shape_params[0] >= 0.0f && (size_t)b.shape_params[0] < W->hfs.size()) ||
+             b.body_type == AVBD_BODY_DYNAMIC))
+            return AVBD_ERR_FORMAT;
+        if (b.shape == AVBD_SHAPE_TRIMESH &&
+            (!(b.shape_params[0] >= 0.0f && (size_t)b.shape_params[0] < W->meshes.size()) ||
+             b.body_type == AVBD_BODY_DYNAMIC))
+            return AVBD_ERR_FORMAT;
         if (b.shape == AVBD_SHAPE_HULL && !((size_t)b.shape_params[0] < W->hulls.size())) return AVBD_ERR_FORMAT;
+        if ((b.shape == AVBD_SHAPE_ROUND || b.shape == AVBD_SHAPE_COMPOUND) &&
+            (!(b.shape_params[0] >= 0.0f && (size_t)b.shape_params[0] < W->exts.size()) ||
+             W->exts[(size_t)b.shape_params[0]].compound != (b.shape == AVBD_SHAPE_COMPOUND)))
+            return AVBD_ERR_FORMAT;
     }
     for (const AvbdPairState& q : W->pairs)
         if (q.a >= q.b || q.b >= N || q.npoints > (uint32_t)MAX_PTS || scene_of(q.a) != scene_of(q.b))

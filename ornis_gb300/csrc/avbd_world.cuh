@@ -107,6 +107,46 @@ struct HullDesc {
     uint32_t nv, nf;
     float bound, min_ext;  // longest vertex (rows.rs:268-272), smallest extent (shape.rs:1468-1479)
 };
+// A part of a rounded or compound shape (Shape::Round's inner, a compound
+// child and its Pose, collision/shape.rs:95-135): a primitive, its params
+// (w = border radius, 0: not rounded) and its pose in the parent frame.
+struct PartDesc {
+    float4 p;
+    float4 pos;
+    float4 rot;
+    const HullDesc* hull;  // a hull part
+    uint32_t kind;
+    uint32_t pad;
+};
+// A heightfield (shape.rs:352-361): row-major heights, rows along +Z, cols
+// along +X, spacing `cell`, and its lowest sample.
+struct HfDesc {
+    const float* h;
+    uint32_t rows, cols;
+    float cell, y_min;
+};
+// One node of a mesh's median-split tree: a leaf owns order[a .. a+b), an
+// inner node branches to nodes a and b.
+struct MeshNodeD {
+    float lo[3], hi[3];
+    uint32_t leaf, a, b;
+};
+// A triangle mesh (shape.rs:377-396): centroid-relative triangle hulls, their
+// centroids, the tree and its permutation.
+struct MeshDesc {
+    const HullDesc* tris;
+    const float4* cent;
+    const MeshNodeD* nodes;
+    const uint32_t* order;
+    uint32_t ntris, nnodes, norder;
+    float min_feature;
+};
+// A rounded shape (one part, pose unused) or a compound (parts in order).
+struct ExtDesc {
+    uint32_t first, count;
+    uint32_t compound;
+    float min_dim;  // shape_min_dimension (rows.rs:393-400)
+};
 
 // Everything a kernel needs, passed by value (pointers into one world's
 // device allocations).  Scene s owns bodies [scene_off[s], scene_off[s+1]).
@@ -133,6 +173,12 @@ struct DW {
     const uint32_t* plane_list;
     const HullDesc* hulls;  // convex hulls named by AVBD_SHAPE_HULL bodies (shape_params[0])
     uint32_t nhulls;
+    const ExtDesc* exts;    // rounded and compound shapes named by their bodies (shape_params[0])
+    const PartDesc* parts;
+    uint32_t nexts;
+    const HfDesc* hfs;      // heightfields named by their bodies
+    const MeshDesc* meshes; // triangle meshes named by their bodies
+    uint32_t nhfs, nmeshes;
 
     // bodies
     float4 *pos, *rot, *vel, *angvel, *torque;

@@ -15,7 +15,7 @@ pub const AVBD_ERR_NONFINITE: i32 = -5;
 pub const AVBD_ERR_UNSUPPORTED: i32 = -6;
 pub const AVBD_ERR_FORMAT: i32 = -7;
 pub const AVBD_ERR_IO: i32 = -8;
-pub const AVBD_SNAPSHOT_FORMAT: u32 = 1;
+pub const AVBD_SNAPSHOT_FORMAT: u32 = 2;
 pub const AVBD_STATIC_MAX_BODIES: u32 = 128;
 pub const AVBD_STATIC_PAIR_CAP: u32 = 2048;
 pub const AVBD_STATIC_SCRATCH_BYTES: u32 = 3481600;
@@ -33,6 +33,10 @@ pub const AVBD_SHAPE_HALFSPACE: u32 = 3;
 pub const AVBD_SHAPE_CYLINDER: u32 = 4;
 pub const AVBD_SHAPE_CONE: u32 = 5;
 pub const AVBD_SHAPE_HULL: u32 = 6;
+pub const AVBD_SHAPE_ROUND: u32 = 7;
+pub const AVBD_SHAPE_COMPOUND: u32 = 8;
+pub const AVBD_SHAPE_HEIGHTFIELD: u32 = 9;
+pub const AVBD_SHAPE_TRIMESH: u32 = 10;
 
 pub const AVBD_BODY_DYNAMIC: u32 = 0;
 pub const AVBD_BODY_STATIC: u32 = 1;
@@ -230,6 +234,18 @@ pub struct AvbdTriggerEvent {
     pub entered: u32,
 }
 
+/// A part of a rounded or compound shape (`Shape::Round`'s inner, a
+/// compound child and its `Pose`).
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct AvbdShapePart {
+    pub shape: u32,
+    pub params: [f32; 3],
+    pub border_radius: f32,
+    pub position: [f32; 3],
+    pub orientation: [f32; 4],
+}
+
 /// What `avbd_snapshot_info` reports about a snapshot.
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
@@ -279,6 +295,35 @@ extern "C" {
         nfaces: u32,
         unit_inertia: *const f32,
         hull_id: *mut u32,
+    ) -> i32;
+    pub fn avbd_world_add_round(
+        world: *mut AvbdWorld,
+        inner: *const AvbdShapePart,
+        unit_inertia: *const f32,
+        id: *mut u32,
+    ) -> i32;
+    pub fn avbd_world_add_compound(
+        world: *mut AvbdWorld,
+        parts: *const AvbdShapePart,
+        n: u32,
+        unit_inertia: *const f32,
+        id: *mut u32,
+    ) -> i32;
+    pub fn avbd_world_add_heightfield(
+        world: *mut AvbdWorld,
+        rows: u32,
+        cols: u32,
+        cell: f32,
+        heights: *const f32,
+        id: *mut u32,
+    ) -> i32;
+    pub fn avbd_world_add_trimesh(
+        world: *mut AvbdWorld,
+        verts: *const f32,
+        nverts: u32,
+        tris: *const u32,
+        ntris: u32,
+        id: *mut u32,
     ) -> i32;
     pub fn avbd_world_remove_body(world: *mut AvbdWorld, handle: u32) -> i32;
     pub fn avbd_world_add_joint(world: *mut AvbdWorld, desc: *const AvbdJointDesc, handle: *mut u32) -> i32;

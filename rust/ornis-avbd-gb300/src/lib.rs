@@ -106,6 +106,23 @@ impl World {
         self.raw
     }
 
+    /// `Shape::Round` around one primitive part: bodies of shape
+    /// `AVBD_SHAPE_ROUND` name the returned id in `shape_params[0]`.
+    pub fn add_round(&mut self, inner: &AvbdShapePart, unit_inertia: [f32; 3]) -> Result<u32, Error> {
+        let mut id = 0u32;
+        Error::check(unsafe { avbd_world_add_round(self.raw, inner, unit_inertia.as_ptr(), &mut id) })?;
+        Ok(id)
+    }
+
+    /// `Shape::Compound` of primitive parts placed by their poses.
+    pub fn add_compound(&mut self, parts: &[AvbdShapePart], unit_inertia: [f32; 3]) -> Result<u32, Error> {
+        let mut id = 0u32;
+        Error::check(unsafe {
+            avbd_world_add_compound(self.raw, parts.as_ptr(), parts.len() as u32, unit_inertia.as_ptr(), &mut id)
+        })?;
+        Ok(id)
+    }
+
     /// The whole world as a versioned snapshot: a world made from it
     /// continues bit for bit, events included.
     pub fn snapshot(&mut self) -> Result<Vec<u8>, Error> {

@@ -74,6 +74,12 @@ def lib():
         L.oracle_remove_body.argtypes = [vp, C.c_uint32]
         L.oracle_remove_joint.argtypes = [vp, C.c_uint32]
         L.oracle_wake_body.argtypes = [vp, C.c_uint32]
+        L.oracle_add_heightfield.restype = C.c_int
+        L.oracle_add_heightfield.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, vp, C.POINTER(C.c_uint32)]
+        L.oracle_add_trimesh.restype = C.c_int
+        L.oracle_add_trimesh.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32, C.POINTER(C.c_uint32)]
+        L.oracle_add_ext.restype = C.c_int
+        L.oracle_add_ext.argtypes = [vp, C.c_int, vp, C.c_uint32, vp, C.POINTER(C.c_uint32)]
         L.oracle_add_hull.restype = C.c_uint32
         L.oracle_add_hull.argtypes = [vp, vp, C.c_uint32, vp, C.c_uint32, vp]
         L.oracle_convex_distance.argtypes = [vp, C.c_uint32, C.c_uint32, vp]
@@ -203,6 +209,36 @@ class OracleWorld:
         ui = f32(unit_inertia)
         return lib().oracle_add_hull(self.h, abi.ptr(v), len(v) // 3, abi.ptr(fc) if len(fc) else None,
                                      len(fc) // 3, abi.ptr(ui))
+
+    def add_round(self, inner, unit_inertia=(1.0, 1.0, 1.0)):
+        """A rounded shape around one primitive part; returns (status, id)."""
+        out = C.c_uint32()
+        rc = lib().oracle_add_ext(self.h, 0, C.byref(inner), 1, abi.ptr(f32(unit_inertia)), C.byref(out))
+        return rc, out.value
+
+    def add_heightfield(self, heights, cell):
+        """A heightfield of rows x cols samples (rows along +Z); returns (status, id)."""
+        h = f32(np.asarray(heights))
+        rows, cols = h.shape
+        out = C.c_uint32()
+        rc = lib().oracle_add_heightfield(self.h, rows, cols, float(cell), abi.ptr(np.ascontiguousarray(h.reshape(-1))),
+                                          C.byref(out))
+        return rc, out.value
+
+    def add_trimesh(self, verts, tris):
+        """A triangle mesh; returns (status, id)."""
+        v = f32(np.asarray(verts).reshape(-1))
+        t = np.ascontiguousarray(np.asarray(tris, dtype=np.uint32).reshape(-1))
+        out = C.c_uint32()
+        rc = lib().oracle_add_trimesh(self.h, abi.ptr(v), len(v) // 3, abi.ptr(t), len(t) // 3, C.byref(out))
+        return rc, out.value
+
+    def add_compound(self, parts, unit_inertia=(1.0, 1.0, 1.0)):
+        """A compound of primitive parts; returns (status, id)."""
+        out = C.c_uint32()
+        arr = abi.parts_array(parts) if parts else None
+        rc = lib().oracle_add_ext(self.h, 1, arr, len(parts), abi.ptr(f32(unit_inertia)), C.byref(out))
+        return rc, out.value
 
     def convex_distance(self, ia, ib):
         out = np.zeros(10, dtype=np.float32)

@@ -37,6 +37,7 @@ def snapshot(scene_offsets=(0, 0), bodies=b"", nbodies=0, tof=None, substeps=7, 
     payload += struct.pack(f"<{len(scene_offsets)}I", *scene_offsets)
     payload += bodies
     payload += bytes(C.sizeof(abi.AvbdBodyAux) * nbodies)
+    payload += struct.pack("<3I", 0, 0, 0)  # rounded and compound shapes, heightfields, meshes
     payload += bytes(4 * abi.SNAPSHOT_EVENT_WORDS)
     tof = [0] * (nbodies + 1) if tof is None else tof
     payload += struct.pack(f"<{len(tof)}I", *tof)
