@@ -252,8 +252,7 @@ static __device__ __noinline__ Dist compound_distance(const DW& w, const Shape& 
 // shape_distance with the wrapper arms (distance.rs:648-705): rounded shapes
 // peel first (a's, then b's), then compounds expand; compound against
 // compound is separation.  Rounded inners and compound parts are primitives.
-static __device__ __noinline__ Dist ext_distance(const DW& w, const Shape& a, const Shape& b, float* sat_gap) {
-    if (a.kind <= AVBD_SHAPE_HULL && b.kind <= AVBD_SHAPE_HULL) return shape_distance(a, b, sat_gap);
+static __device__ __noinline__ Dist ext_distance_wrapped(const DW& w, const Shape& a, const Shape& b) {
     Shape ia = a, ib = b;
     float ra = 0.0f, rb = 0.0f;
     if (a.kind == AVBD_SHAPE_ROUND) {
@@ -274,6 +273,11 @@ static __device__ __noinline__ Dist ext_distance(const DW& w, const Shape& a, co
     if (b.kind == AVBD_SHAPE_ROUND) d = round_offset(d, rb, false, a.pos, b.pos);
     if (a.kind == AVBD_SHAPE_ROUND) d = round_offset(d, ra, true, a.pos, b.pos);
     return d;
+}
+// Primitive pairs keep the direct call; the wrapper arms take the rest.
+static __device__ __forceinline__ Dist ext_distance(const DW& w, const Shape& a, const Shape& b, float* sat_gap) {
+    if (a.kind <= AVBD_SHAPE_HULL && b.kind <= AVBD_SHAPE_HULL) return shape_distance(a, b, sat_gap);
+    return ext_distance_wrapped(w, a, b);
 }
 // rows.rs:366-368
 static __device__ __forceinline__ bool pair_allowed(const DW& w, uint32_t a, uint32_t b) {
