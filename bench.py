@@ -190,10 +190,11 @@ def workload(args):
         bodies, offs, joints = scenes.ragdolls(counts)
         params, nsub = scenes.params_for("ragdoll_8192")
         return bodies, offs, joints, params, nsub
-    if args.workload == "large_100k":
-        # one scene of 100,000 bodies dropped over a 200 x 200 m ground plane
-        bodies = scenes.large_100k()
-        params, nsub = scenes.params_for("large_100k")
+    if args.workload in SINGLE_SCENE:
+        # one scene: 100,000 bodies dropped over a 200 x 200 m ground plane,
+        # or the 210-cube pyramid on a ground plane
+        bodies = single_scene_bodies(args.workload)
+        params, nsub = scenes.params_for(args.workload)
         return bodies, np.array([0, len(bodies)], dtype=np.uint32), [], params, nsub
     bodies, offs, _ = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
@@ -211,7 +212,12 @@ def shard(bodies, offs, rank, world):
 
 
 TRAJECTORY_STEPS = 240  # the batched and articulated workloads' trajectories
-TRAJECTORY = {"batched_4096": 240, "ragdoll_8192": 240, "large_100k": 300}
+TRAJECTORY = {"batched_4096": 240, "ragdoll_8192": 240, "large_100k": 300, "pyramid_210": 600}
+SINGLE_SCENE = ("large_100k", "pyramid_210")  # one-scene workloads: one GPU, L2 flushed per timed step
+
+
+def single_scene_bodies(name):
+    return scenes.large_100k() if name == "large_100k" else scenes.pyramid_210()
 
 
 def trajectory_len(args):
@@ -480,33 +486,34 @@ def oracle_parity(w, offs, params, nsub, nscenes=8, steps=3, split=True, threads
 
 # ---------------------------------------------------------------------------
 def run_reference_large(args):
-    """The reference's CPU step on the one-scene 100k workload: the oracle in
-    the reference's order from the initial drop, three steps timed (each
-    step is quadratic in bodies; the rate is extrapolated from them)."""
+    """The reference's CPU step on a one-scene workload: the oracle in the
+    reference's order from the initial drop, at least three steps timed and
+    more while they take under 20 s together (a step of the 100k scene is
+    quadratic in bodies: its rate is extrapolated from three)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_api as O
 
-    bodies = scenes.large_100k()
-    params, nsub = scenes.params_for("large_100k")
+    bodies = single_scene_bodies(args.workload)
+    params, nsub = scenes.params_for(args.workload)
     cores = os.cpu_count() or 1
     o = O.OracleWorld(params, mode=O.REFERENCE, threads=cores)
     o.add_bodies(bodies)
     secs = []
-    for _ in range(3):
+    while len(secs) < 3 or (sum(secs) < 20.0 and len(secs) < trajectory_len(args)):
         t0 = time.perf_counter()
         o.step_fixed(nsub)
         secs.append(time.perf_counter() - t0)
     ndyn = scenes.dynamic_count(bodies)
     v = ndyn * len(secs) / sum(secs)
     cb = {"value": v, "unit": "body-steps/s", "cores": cores, "kind": "port", "per_step_s": secs,
-          "sample": f"steps 0..3 of the 300-step trajectory from the initial drop, the oracle in the reference's "
-                    f"order (all-pairs discovery over {cores} threads, linear pair lookup, serial sweep); rate "
-                    f"extrapolated from those three steps"}
+          "sample": f"steps 0..{len(secs)} of the {trajectory_len(args)}-step trajectory from the initial drop, the "
+                    f"oracle in the reference's order (all-pairs discovery over {cores} threads, linear pair lookup, "
+                    f"serial sweep); rate from those steps"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
             "steps": len(secs), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded scene)",
-            "config": {"workload": "large_100k", "scenes": 1, "dynamic_bodies": ndyn, "dt": params.step_dt,
-                       "substeps": nsub, "iterations": params.iterations, "trajectory": "steps 0..3"},
+            "config": {"workload": args.workload, "scenes": 1, "dynamic_bodies": ndyn, "dt": params.step_dt,
+                       "substeps": nsub, "iterations": params.iterations, "trajectory": f"steps 0..{len(secs)}"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -517,7 +524,7 @@ def run_reference(args):
     d = dist_init(args.gpus)
     if d is not None and d[1] != 0:
         return 0
-    if args.workload == "large_100k":
+    if args.workload in SINGLE_SCENE:
         return run_reference_large(args)
     bodies, offs, counts = scenes.batched(args.scenes)
     params, nsub = scenes.params_for("batched_4096")
@@ -545,9 +552,9 @@ def run_ours(args):
     bodies_all, offs_all, joints_all, params, nsub = workload(args)
     if world > 1 and joints_all:
         raise SystemExit("the articulated workload runs on one GPU (two scenes)")
-    if world > 1 and args.workload == "large_100k":
-        raise SystemExit("the large workload is one scene: it runs on one GPU")
-    large = args.workload == "large_100k"
+    if world > 1 and args.workload in SINGLE_SCENE:
+        raise SystemExit("a one-scene workload runs on one GPU")
+    large = args.workload in SINGLE_SCENE
     bodies, offs = shard(bodies_all, offs_all, rank, world) if world > 1 else (bodies_all, offs_all)
     ndyn = scenes.dynamic_count(bodies)
     w = AvbdWorld(params, device=device, bodies=bodies, scene_offsets=offs)
@@ -905,9 +912,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scenes", type=int, default=4096)
-    ap.add_argument("--workload", default="batched_4096", choices=["batched_4096", "ragdoll_8192", "large_100k"],
+    ap.add_argument("--workload", default="batched_4096",
+                    choices=["batched_4096", "ragdoll_8192", "large_100k", "pyramid_210"],
                     help="ragdoll_8192: 8192 15-capsule ragdolls with ball/hinge joints in two scenes; "
-                         "large_100k: one scene of 100,000 bodies, dt 1/60, 1 substep, 10 iterations, 300 steps")
+                         "large_100k: one scene of 100,000 bodies, dt 1/60, 1 substep, 10 iterations, 300 steps; "
+                         "pyramid_210: the 210-cube pyramid on a plane, dt 1/60, 1 substep, 10 iterations, 600 steps")
     ap.add_argument("--start", type=int, default=None,
                     help="time the contiguous window [start, start + steps) instead of steps spread over the "
                          "trajectory")
