@@ -16,7 +16,7 @@ use std::cell::RefCell;
 use glam::{Quat, Vec3};
 use ornis_physics::avbd::AvbdEngine;
 use ornis_physics::body::{BodyHandle, BodyType, RigidBody};
-use ornis_physics::collision::shape::Shape;
+use ornis_physics::collision::shape::{ConvexHull, Pose, Shape};
 use ornis_physics::engine::PhysicsEngine;
 use ornis_physics::gpu::GpuAvbdDispatch;
 
@@ -26,6 +26,9 @@ use crate::{Error, World};
 pub struct CudaAvbd {
     world: RefCell<World>,
     synced: RefCell<u32>,
+    /// Per mirrored body: its shape as the library names it (table-backed
+    /// shapes are registered once, when the body is first mirrored).
+    shapes: RefCell<Vec<(u32, [f32; 3])>>,
 }
 
 // The engine is stepped by one thread at a time (PhysicsEngine: Send + Sync
@@ -34,13 +37,22 @@ unsafe impl Sync for CudaAvbd {}
 
 impl CudaAvbd {
     pub fn new(device: i32) -> Result<Self, Error> {
-        Ok(CudaAvbd { world: RefCell::new(World::new(&crate::default_params(), device)?), synced: RefCell::new(0) })
+        Ok(CudaAvbd {
+            world: RefCell::new(World::new(&crate::default_params(), device)?),
+            synced: RefCell::new(0),
+            shapes: RefCell::new(Vec::new()),
+        })
     }
 
     pub fn remove_body(&self, handle: u32) -> Result<(), Error> {
         let r = self.world.borrow_mut().remove_body(handle);
         let mut s = self.synced.borrow_mut();
         *s = s.saturating_sub(1);
+        // the last body moves into the freed handle (engine.rs:40-43)
+        let mut shapes = self.shapes.borrow_mut();
+        if (handle as usize) < shapes.len() {
+            shapes.swap_remove(handle as usize);
+        }
         r
     }
 
@@ -61,18 +73,100 @@ fn count(engine: &AvbdEngine) -> u32 {
     n
 }
 
-/// RigidBody (body.rs:248-342) to the C record.
-pub fn to_ffi(b: &RigidBody) -> AvbdBody {
-    let (shape, params) = match b.shape {
+/// A primitive shape's kind and parameters; `None` for the table-backed ones.
+fn primitive(shape: &Shape) -> Option<(u32, [f32; 3])> {
+    Some(match *shape {
         Shape::Sphere { radius } => (AVBD_SHAPE_SPHERE, [radius, 0.0, 0.0]),
         Shape::Box { half_extents } => (AVBD_SHAPE_BOX, half_extents.to_array()),
         Shape::Capsule { radius, half_height } => (AVBD_SHAPE_CAPSULE, [radius, half_height, 0.0]),
-        Shape::HalfSpace { normal } => (AVBD_SHAPE_HALFSPACE, normal.to_array()),
+        Shape::HalfSpace { normal } => (AVBD_SHAPE_HALFSPACE, normal.get().to_array()),
         Shape::Cylinder { radius, half_height } => (AVBD_SHAPE_CYLINDER, [radius, half_height, 0.0]),
         Shape::Cone { radius, half_height } => (AVBD_SHAPE_CONE, [radius, half_height, 0.0]),
-        // hulls are registered with avbd_world_add_hull and named by index
-        _ => (AVBD_SHAPE_HULL, [0.0, 0.0, 0.0]),
+        _ => return None,
+    })
+}
+
+fn unit_inertia(shape: &Shape) -> [f32; 3] {
+    shape.try_inertia(1.0).unwrap_or(Vec3::ZERO).to_array()
+}
+
+/// A part of a rounded or compound shape: a primitive or a hull (registered
+/// here), placed by `pose` (identity for a rounded shape's inner).
+fn part_of(w: &mut World, shape: &Shape, pose: Option<&Pose>) -> Result<AvbdShapePart, Error> {
+    // a rounded part carries its skin around a primitive inner
+    let (base, skin) = match shape {
+        Shape::Round { inner, border_radius } => (inner.as_ref(), *border_radius),
+        other => (other, 0.0),
     };
+    let (kind, params) = match primitive(base) {
+        Some(p) => p,
+        None => match base {
+            Shape::ConvexHull(hull) => (AVBD_SHAPE_HULL, [register_hull(w, base, hull)? as f32, 0.0, 0.0]),
+            _ => return Err(Error::Unsupported), // nested wrappers, terrain, meshes
+        },
+    };
+    Ok(AvbdShapePart {
+        shape: kind,
+        params,
+        border_radius: skin,
+        position: pose.map(|p| p.position.to_array()).unwrap_or([0.0; 3]),
+        orientation: pose.map(|p| p.rotation.to_array()).unwrap_or([0.0, 0.0, 0.0, 1.0]),
+    })
+}
+
+fn register_hull(w: &mut World, shape: &Shape, hull: &ConvexHull) -> Result<u32, Error> {
+    let verts: Vec<f32> = hull.vertices.iter().flat_map(|v| v.to_array()).collect();
+    let faces: Vec<u32> = hull.faces.iter().flat_map(|t| t.as_u32()).collect();
+    w.add_hull(&verts, &faces, unit_inertia(shape))
+}
+
+/// A body's shape as the library names it: a primitive's fields, or the id
+/// of a table-backed shape registered now (hull, rounded, compound,
+/// heightfield, triangle mesh).
+pub fn register_shape(w: &mut World, shape: &Shape) -> Result<(u32, [f32; 3]), Error> {
+    if let Some(p) = primitive(shape) {
+        return Ok(p);
+    }
+    let id = |v: u32| [v as f32, 0.0, 0.0];
+    Ok(match shape {
+        Shape::ConvexHull(hull) => (AVBD_SHAPE_HULL, id(register_hull(w, shape, hull)?)),
+        Shape::Round { .. } => {
+            let part = part_of(w, shape, None)?;
+            (AVBD_SHAPE_ROUND, id(w.add_round(&part, unit_inertia(shape))?))
+        }
+        Shape::Compound { shapes } => {
+            let parts = shapes.iter().map(|(s, pose)| part_of(w, s, Some(pose))).collect::<Result<Vec<_>, _>>()?;
+            (AVBD_SHAPE_COMPOUND, id(w.add_compound(&parts, unit_inertia(shape))?))
+        }
+        Shape::Heightfield(hf) => {
+            (AVBD_SHAPE_HEIGHTFIELD, id(w.add_heightfield(hf.rows as u32, hf.cols as u32, hf.cell, &hf.heights)?))
+        }
+        Shape::TriMesh(mesh) => {
+            // the engine keeps centroid-relative triangle hulls: the vertices
+            // come back as hull vertex + centroid (the library recomputes the
+            // centroid from them, which can differ from the original in the
+            // last bit)
+            let mut verts = Vec::new();
+            let mut tris = Vec::new();
+            for (t, tri) in mesh.tris.iter().enumerate() {
+                if let Shape::ConvexHull(h) = tri {
+                    let base = (verts.len() / 3) as u32;
+                    for v in &h.vertices {
+                        verts.extend_from_slice(&(*v + mesh.centroids[t]).to_array());
+                    }
+                    tris.extend_from_slice(&[base, base + 1, base + 2]);
+                }
+            }
+            (AVBD_SHAPE_TRIMESH, id(w.add_trimesh(&verts, &tris)?))
+        }
+        _ => return Err(Error::Unsupported),
+    })
+}
+
+/// RigidBody (body.rs:248-342) to the C record, its shape named as
+/// `register_shape` named it.
+pub fn to_ffi(b: &RigidBody, named: (u32, [f32; 3])) -> AvbdBody {
+    let (shape, params) = named;
     AvbdBody {
         position: b.position.to_array(),
         orientation: b.orientation.to_array(),
@@ -121,13 +215,21 @@ impl GpuAvbdDispatch for CudaAvbd {
         let mut w = self.world.borrow_mut();
         let n = count(engine);
         let synced = *self.synced.borrow();
+        let mut shapes = self.shapes.borrow_mut();
         if n > synced {
-            let recs: Vec<AvbdBody> =
-                (synced..n).map(|h| to_ffi(engine.get_body(BodyHandle::from(h as usize)).unwrap())).collect();
+            let mut recs = Vec::new();
+            for h in synced..n {
+                let b = engine.get_body(BodyHandle::from(h as usize)).unwrap();
+                let named = register_shape(&mut w, &b.shape).expect("a shape the library accepts");
+                shapes.push(named);
+                recs.push(to_ffi(b, named));
+            }
             w.add_bodies(&recs).expect("avbd_world_add_bodies");
             *self.synced.borrow_mut() = n;
         }
-        let recs: Vec<AvbdBody> = (0..n).map(|h| to_ffi(engine.get_body(BodyHandle::from(h as usize)).unwrap())).collect();
+        let recs: Vec<AvbdBody> = (0..n)
+            .map(|h| to_ffi(engine.get_body(BodyHandle::from(h as usize)).unwrap(), shapes[h as usize]))
+            .collect();
         w.set_bodies(0, &recs).expect("avbd_world_set_bodies");
         w.step(dt).expect("avbd_world_step");
         let mut out = vec![AvbdBody::default(); n as usize];

@@ -106,6 +106,51 @@ impl World {
         self.raw
     }
 
+    /// `ConvexHull`: centroid-relative vertices, triangle faces and the
+    /// per-unit-mass inertia; bodies of shape `AVBD_SHAPE_HULL` name the id.
+    pub fn add_hull(&mut self, verts: &[f32], faces: &[u32], unit_inertia: [f32; 3]) -> Result<u32, Error> {
+        let mut id = 0u32;
+        Error::check(unsafe {
+            avbd_world_add_hull(
+                self.raw,
+                verts.as_ptr(),
+                (verts.len() / 3) as u32,
+                if faces.is_empty() { std::ptr::null() } else { faces.as_ptr() },
+                (faces.len() / 3) as u32,
+                unit_inertia.as_ptr(),
+                &mut id,
+            )
+        })?;
+        Ok(id)
+    }
+
+    /// `Heightfield`: rows x cols row-major heights on a grid of `cell`.
+    pub fn add_heightfield(&mut self, rows: u32, cols: u32, cell: f32, heights: &[f32]) -> Result<u32, Error> {
+        if heights.len() != (rows as usize) * (cols as usize) {
+            return Err(Error::InvalidArg);
+        }
+        let mut id = 0u32;
+        Error::check(unsafe { avbd_world_add_heightfield(self.raw, rows, cols, cell, heights.as_ptr(), &mut id) })?;
+        Ok(id)
+    }
+
+    /// `TriMesh::from_indexed`: vertices (3 floats each) and triangles (3
+    /// indices each).
+    pub fn add_trimesh(&mut self, verts: &[f32], tris: &[u32]) -> Result<u32, Error> {
+        let mut id = 0u32;
+        Error::check(unsafe {
+            avbd_world_add_trimesh(
+                self.raw,
+                verts.as_ptr(),
+                (verts.len() / 3) as u32,
+                tris.as_ptr(),
+                (tris.len() / 3) as u32,
+                &mut id,
+            )
+        })?;
+        Ok(id)
+    }
+
     /// `Shape::Round` around one primitive part: bodies of shape
     /// `AVBD_SHAPE_ROUND` name the returned id in `shape_params[0]`.
     pub fn add_round(&mut self, inner: &AvbdShapePart, unit_inertia: [f32; 3]) -> Result<u32, Error> {
