@@ -37,8 +37,11 @@ Warm-up steps run from the initial state and the world is then reset to it,
 so the timed trajectory starts at step 0.  The primal launch shape is
 autotuned at step --tune-at (piles formed), then the state is reset.
 --impl reference times the CPU path alone (the reference itself is Rust and
-cannot be built here).  Under torchrun (N > 1) scenes are sharded across
-ranks (scene s -> rank s mod N), no data-path collective; rank 0 prints.
+cannot be built here).  Under a multi-process launcher (N > 1: RANK,
+WORLD_SIZE, LOCAL_RANK, MASTER_ADDR, MASTER_PORT) scenes are sharded across
+ranks (scene s -> rank s mod N), no data-path collective; the barrier and
+the max-over-ranks timing go over plain sockets (SocketRanks); rank 0
+prints.
 """
 import argparse
 import atexit
@@ -150,36 +153,85 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm), "window": window}
 
 
+class SocketRanks:
+    """The N>1 barrier and reductions over plain sockets (no PyTorch): rank 0
+    serves on MASTER_ADDR at MASTER_PORT + 1 (the launcher keeps MASTER_PORT
+    for its own store), the other ranks connect, and every collective is one
+    line of JSON each way (floats round-trip exactly).  Scenes are sharded,
+    so these carry only the timing and the body counts."""
+
+    def __init__(self, rank, world, addr, port, timeout=300.0):
+        import socket
+
+        self.rank, self.world = rank, world
+        self.peers = []
+        if rank == 0:
+            srv = socket.create_server((addr, port))
+            srv.settimeout(timeout)
+            try:
+                for _ in range(world - 1):
+                    conn, _ = srv.accept()
+                    conn.settimeout(timeout)
+                    f = conn.makefile("rw")
+                    self.peers.append((int(f.readline()), conn, f))
+            finally:
+                srv.close()
+            self.peers.sort(key=lambda p: p[0])
+        else:
+            deadline = time.monotonic() + timeout
+            while True:
+                try:
+                    conn = socket.create_connection((addr, port), timeout=5.0)
+                    break
+                except OSError:
+                    if time.monotonic() > deadline:
+                        raise
+                    time.sleep(0.2)
+            conn.settimeout(timeout)
+            self.conn, self.f = conn, conn.makefile("rw")
+            self.f.write(f"{rank}\n")
+            self.f.flush()
+
+    def allreduce(self, vals, op):
+        """Element-wise max or sum of each rank's list; every rank gets it."""
+        vals = [float(v) for v in vals]
+        if self.rank != 0:
+            self.f.write(json.dumps(vals) + "\n")
+            self.f.flush()
+            return json.loads(self.f.readline())
+        rows = [vals] + [json.loads(f.readline()) for _, _, f in self.peers]
+        red = [max(c) if op == "max" else sum(c) for c in zip(*rows)]
+        for _, _, f in self.peers:
+            f.write(json.dumps(red) + "\n")
+            f.flush()
+        return red
+
+    def barrier(self):
+        self.allreduce([0.0], "sum")
+
+    def close(self):
+        for _, conn, _ in self.peers:
+            conn.close()
+        if self.rank != 0:
+            self.conn.close()
+
+
 def dist_init(n_gpus):
-    """torch.distributed only for the N>1 barrier and max-over-ranks timing."""
+    """The N>1 rendezvous (rank, world size and local GPU from the launcher's
+    environment); None on one GPU."""
     if n_gpus <= 1 or int(os.environ.get("WORLD_SIZE", "1")) <= 1:
         return None
-    import torch
-    import torch.distributed as dist
-
     rank = int(os.environ["RANK"])
+    world = int(os.environ["WORLD_SIZE"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
-    return dist, rank, dist.get_world_size(), local
+    port = int(os.environ.get("AVBD_BENCH_PORT", int(os.environ["MASTER_PORT"]) + 1))
+    return SocketRanks(rank, world, os.environ.get("MASTER_ADDR", "127.0.0.1"), port), rank, world, local
 
 
-def combine_ranks(dist, device, worst=(), total=()):
+def combine_ranks(ranks, worst=(), total=()):
     """The job-wide view of per-rank numbers: the max over ranks of each of
-    `worst` (times) and the sum of each of `total` (counts).  `device` is
-    where the collective's tensor lives ("cuda:<n>" under NCCL, "cpu" under
-    gloo)."""
-    import torch
-
-    out = []
-    for vals, op in ((worst, dist.ReduceOp.MAX), (total, dist.ReduceOp.SUM)):
-        if not vals:
-            out.append([])
-            continue
-        t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=op)
-        out.append([float(x) for x in t.cpu().tolist()])
-    return out[0], out[1]
+    `worst` (times) and the sum of each of `total` (counts)."""
+    return (ranks.allreduce(worst, "max") if worst else []), (ranks.allreduce(total, "sum") if total else [])
 
 
 def workload(args):
@@ -615,7 +667,7 @@ def run_ours(args):
     if large:
         print(f"[large] timed {len(steps)} steps: {ms:.1f} ms", file=sys.stderr, flush=True)
     if d:
-        (ms,), (nd,) = combine_ranks(d[0], f"cuda:{device}", worst=[ms], total=[ndyn])
+        (ms,), (nd,) = combine_ranks(d[0], worst=[ms], total=[ndyn])
         ndyn_total = int(nd)
     else:
         ndyn_total = ndyn
@@ -666,7 +718,7 @@ def run_ours(args):
     d2h += io["ev"] // max(1, len(e2e_steps))
     e2e = ndyn * len(e2e_steps) / e2e_s
     if d:
-        (e2e_max,), _ = combine_ranks(d[0], f"cuda:{device}", worst=[e2e_s])
+        (e2e_max,), _ = combine_ranks(d[0], worst=[e2e_s])
         e2e = ndyn_total * len(e2e_steps) / e2e_max
     cb = None
     if large and args.cpu_per_core > 0:

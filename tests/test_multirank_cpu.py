@@ -1,15 +1,16 @@
-"""The multi-GPU bench path's host logic on the CPU, with two gloo ranks.
+"""The multi-GPU bench path's host logic on the CPU, with two ranks as plain
+processes (no GPU, no PyTorch).
 
 Scenes are independent, so ranks shard them with no exchange: rank r takes
 the scenes s with s mod N == r (bench.shard).  The job-wide numbers are the
-max over ranks of the times and the sum of the bodies (bench.combine_ranks,
-the same code the bench runs under NCCL)."""
+max over ranks of the times and the sum of the bodies (bench.combine_ranks
+over bench.SocketRanks, the rendezvous the bench uses under a launcher)."""
+import multiprocessing as mp
 import os
 import socket
 import sys
 
 import numpy as np
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 NSCENES = 12
@@ -23,30 +24,27 @@ def _free_port():
 
 
 def _rank(rank, port, q):
-    os.environ["MASTER_ADDR"] = "127.0.0.1"
-    os.environ["MASTER_PORT"] = str(port)
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(WORLD), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port - 1)})
     sys.path.insert(0, ROOT)
-    import torch.distributed as dist
-
     import bench
     from ornis_gb300 import scenes
 
-    dist.init_process_group("gloo", rank=rank, world_size=WORLD)
+    ranks, r, world, local = bench.dist_init(WORLD)
     try:
+        assert (r, world, local) == (rank, WORLD, rank)
         bodies, offs, _ = scenes.batched(NSCENES)
         mine, my_offs = bench.shard(bodies, offs, rank, WORLD)
         ndyn = scenes.dynamic_count(mine)
-        seconds = 1.5 + rank  # rank 1 is the slower one
-        worst, total = bench.combine_ranks(dist, "cpu", worst=[seconds], total=[ndyn, len(my_offs) - 1])
-        dist.barrier()
+        seconds = 1.5 + rank + 0.1  # rank 1 is the slower one; not a round number
+        worst, total = bench.combine_ranks(ranks, worst=[seconds], total=[ndyn, len(my_offs) - 1])
+        ranks.barrier()
         q.put((rank, mine, my_offs, worst, total))
     finally:
-        dist.destroy_process_group()
+        ranks.close()
 
 
-def test_two_gloo_ranks_shard_scenes_and_combine_timing():
-    import torch.multiprocessing as mp
-
+def test_two_ranks_shard_scenes_and_combine_timing():
     from ornis_gb300 import scenes
 
     ctx = mp.get_context("spawn")
@@ -73,7 +71,16 @@ def test_two_gloo_ranks_shard_scenes_and_combine_timing():
         mine, my_offs, _, _ = got[s % WORLD]
         k = s // WORLD
         np.testing.assert_array_equal(mine[my_offs[k]:my_offs[k + 1]], bodies[offs[s]:offs[s + 1]])
-    for r in range(WORLD):
-        _, _, worst, total = got[r]
-        assert worst == [1.5 + WORLD - 1]  # the slowest rank's time, on every rank
-        assert total == [float(scenes.dynamic_count(bodies)), float(NSCENES)]
+    # both ranks see the slowest rank's time (exactly) and the summed counts
+    ndyn_all = scenes.dynamic_count(bodies)
+    for rank in range(WORLD):
+        _, _, worst, total = got[rank]
+        assert worst == [1.5 + (WORLD - 1) + 0.1]
+        assert total == [float(ndyn_all), float(NSCENES)]
+
+
+def test_one_rank_needs_no_rendezvous():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.dist_init(1) is None
