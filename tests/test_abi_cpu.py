@@ -123,3 +123,36 @@ def test_rust_crate_binds_the_header():
     for k, v in consts.items():
         assert defines.get(k) == v, k
     assert set(defines) <= set(consts)
+
+
+def _c_struct_fields(hdr, name):
+    m = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), hdr, flags=re.S)
+    assert m, name
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        # "type a, b[3], c" -> a, b, c
+        parts = decl.split(",")
+        names.append(re.findall(r"(\w+)\s*(?:\[[^\]]*\])?$", parts[0].strip())[0])
+        names += [re.match(r"\s*(\w+)", q).group(1) for q in parts[1:]]
+    return names
+
+
+def _rust_struct_fields(ffi, name):
+    m = re.search(r"pub struct %s \{(.*?)\n\}" % name, ffi, flags=re.S)
+    assert m, name
+    return re.findall(r"pub (\w+):", m.group(1))
+
+
+def test_rust_records_follow_the_header():
+    """Every record the Rust crate mirrors has the header's fields in the
+    header's order (the #[repr(C)] layout then follows)."""
+    hdr = open(os.path.join(ROOT, "include", "ornis_avbd.h")).read()
+    ffi = open(os.path.join(ROOT, "rust", "ornis-avbd-gb300", "src", "ffi.rs")).read()
+    names = [n for n in re.findall(r"pub struct (Avbd\w+) \{", ffi) if _rust_struct_fields(ffi, n)]  # not opaque
+    assert len(names) >= 10
+    for name in names:
+        assert _rust_struct_fields(ffi, name) == _c_struct_fields(hdr, name), name
