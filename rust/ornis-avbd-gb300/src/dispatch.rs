@@ -18,6 +18,7 @@ use ornis_physics::avbd::AvbdEngine;
 use ornis_physics::body::{BodyHandle, BodyType, RigidBody};
 use ornis_physics::collision::shape::{ConvexHull, Pose, Shape};
 use ornis_physics::engine::PhysicsEngine;
+use ornis_physics::joint::{AxisConfig, JointKind, MotorKind, MotorModel};
 use ornis_physics::gpu::GpuAvbdDispatch;
 
 use crate::ffi::*;
@@ -161,6 +162,147 @@ pub fn register_shape(w: &mut World, shape: &Shape) -> Result<(u32, [f32; 3]), E
         }
         _ => return Err(Error::Unsupported),
     })
+}
+
+/// `JointKind` (joint.rs:209-410) to the C descriptor the library admits
+/// (`avbd_world_add_joint`), for bodies `a` and `b`.  The spring's
+/// integration choice has no device counterpart (the AVBD step integrates
+/// every spring the same way) and is not carried.
+pub fn joint_desc(kind: &JointKind, a: u32, b: u32) -> AvbdJointDesc {
+    let mut d = AvbdJointDesc { body_a: a, body_b: b, ..Default::default() };
+    let v = |x: Vec3| x.to_array();
+    match *kind {
+        JointKind::Ball { local_anchor_a, local_anchor_b } => {
+            d.kind = AVBD_JOINT_BALL;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+        }
+        JointKind::Revolute { local_anchor_a, local_anchor_b, local_axis_a, local_axis_b, limit, motor } => {
+            d.kind = AVBD_JOINT_REVOLUTE;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            d.local_axis_a = v(local_axis_a);
+            d.local_axis_b = v(local_axis_b);
+            if let Some(l) = limit {
+                d.has_limit = 1;
+                d.limit_min = l.min;
+                d.limit_max = l.max;
+            }
+            if let Some(m) = motor {
+                d.has_motor = 1;
+                d.motor_speed = m.target_speed;
+                d.motor_max = m.max_torque;
+            }
+        }
+        JointKind::Prismatic { local_anchor_a, local_anchor_b, local_axis_a, local_axis_b, limit, motor } => {
+            d.kind = AVBD_JOINT_PRISMATIC;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            d.local_axis_a = v(local_axis_a);
+            d.local_axis_b = v(local_axis_b);
+            if let Some(l) = limit {
+                d.has_limit = 1;
+                d.limit_min = l.min;
+                d.limit_max = l.max;
+            }
+            if let Some(m) = motor {
+                d.has_motor = 1;
+                d.motor_speed = m.target_speed;
+                d.motor_max = m.max_force;
+            }
+        }
+        JointKind::Fixed { local_anchor_a, local_anchor_b } => {
+            d.kind = AVBD_JOINT_FIXED;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+        }
+        JointKind::Distance { local_anchor_a, local_anchor_b } => {
+            d.kind = AVBD_JOINT_DISTANCE;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+        }
+        JointKind::Rope { local_anchor_a, local_anchor_b, max_distance } => {
+            d.kind = AVBD_JOINT_ROPE;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            d.max_distance = max_distance;
+        }
+        JointKind::Spring { local_anchor_a, local_anchor_b, motor, .. } => {
+            d.kind = AVBD_JOINT_SPRING;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            d.spring_rest = motor.target_position;
+            d.spring_velocity = motor.target_velocity;
+            d.spring_stiffness = motor.stiffness;
+            d.spring_damping = motor.damping;
+            d.spring_max_force = motor.max_force;
+            d.spring_kind = match motor.kind {
+                MotorKind::Velocity => AVBD_MOTOR_VELOCITY,
+                MotorKind::Position => AVBD_MOTOR_POSITION,
+                MotorKind::Servo => AVBD_MOTOR_SERVO,
+            };
+            d.spring_model = match motor.model {
+                MotorModel::AccelerationBased => AVBD_MODEL_ACCELERATION,
+                MotorModel::ForceBased => AVBD_MODEL_FORCE,
+            };
+        }
+        JointKind::Wheel {
+            local_anchor_a,
+            local_anchor_b,
+            local_suspension_a,
+            local_suspension_b,
+            local_axle_a,
+            local_axle_b,
+            suspension,
+            motor,
+        } => {
+            d.kind = AVBD_JOINT_WHEEL;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            d.local_axis_a = v(local_suspension_a);
+            d.local_axis_b = v(local_suspension_b);
+            d.local_axle_a = v(local_axle_a);
+            d.local_axle_b = v(local_axle_b);
+            d.suspension_hz = suspension.frequency_hz;
+            d.suspension_damping = suspension.damping_ratio;
+            if let Some(m) = motor {
+                d.has_motor = 1;
+                d.motor_speed = m.target_speed;
+                d.motor_max = m.max_torque;
+            }
+        }
+        JointKind::Gear { joint_a, joint_b, ratio } => {
+            d.kind = AVBD_JOINT_GEAR;
+            d.gear_joint_a = joint_a.index() as u32;
+            d.gear_joint_b = joint_b.index() as u32;
+            d.gear_ratio = ratio;
+        }
+        JointKind::SixDof { local_anchor_a, local_anchor_b, linear, angular } => {
+            d.kind = AVBD_JOINT_SIXDOF;
+            d.local_anchor_a = v(local_anchor_a);
+            d.local_anchor_b = v(local_anchor_b);
+            for (k, c) in linear.iter().chain(angular.iter()).enumerate() {
+                match *c {
+                    AxisConfig::Free => d.axis_config[k] = AVBD_AXIS_FREE,
+                    AxisConfig::Locked => d.axis_config[k] = AVBD_AXIS_LOCKED,
+                    AxisConfig::Limited { min, max } => {
+                        d.axis_config[k] = AVBD_AXIS_LIMITED;
+                        d.axis_min[k] = min;
+                        d.axis_max[k] = max;
+                    }
+                }
+            }
+        }
+        JointKind::Motor { linear_target, angular_target, max_force, max_torque, correction } => {
+            d.kind = AVBD_JOINT_MOTOR;
+            d.motor_linear = v(linear_target);
+            d.motor_angular = v(angular_target);
+            d.motor_max_force = max_force;
+            d.motor_max_torque = max_torque;
+            d.motor_correction = correction;
+        }
+    }
+    d
 }
 
 /// RigidBody (body.rs:248-342) to the C record, its shape named as
