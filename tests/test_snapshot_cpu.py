@@ -27,7 +27,7 @@ def records():
 
 
 def snapshot(scene_offsets=(0, 0), bodies=b"", nbodies=0, tof=None, substeps=7, fmt=abi.SNAPSHOT_FORMAT,
-             endian=0x01020304, magic=abi.SNAPSHOT_MAGIC, rec=None, trailing=b""):
+             endian=0x01020304, magic=abi.SNAPSHOT_MAGIC, rec=None, trailing=b"", shapes=b"\0" * 12):
     """A snapshot of a world without pairs, joints, hulls or events, laid out
     section by section: params, settings, scene offsets, bodies, aux, (pairs,
     points, joints, hulls: none), event words, touch CSR, (touch keys,
@@ -37,7 +37,7 @@ def snapshot(scene_offsets=(0, 0), bodies=b"", nbodies=0, tof=None, substeps=7, 
     payload += struct.pack(f"<{len(scene_offsets)}I", *scene_offsets)
     payload += bodies
     payload += bytes(C.sizeof(abi.AvbdBodyAux) * nbodies)
-    payload += struct.pack("<3I", 0, 0, 0)  # rounded and compound shapes, heightfields, meshes
+    payload += shapes  # rounded and compound shapes, heightfields, meshes (shape_sections)
     payload += bytes(4 * abi.SNAPSHOT_EVENT_WORDS)
     tof = [0] * (nbodies + 1) if tof is None else tof
     payload += struct.pack(f"<{len(tof)}I", *tof)
@@ -101,3 +101,68 @@ def test_contents_are_checked_on_the_host():
     refused(snapshot(trailing=b"\0\0\0\0"))
     # the same world without the damage is well formed
     assert snapshot_info(snapshot(scene_offsets=(0, 1), bodies=box, nbodies=1)).nbodies == 1
+
+
+def shape_sections(exts=(), hfs=(), meshes=()):
+    """The three table sections: each a count, then per rounded or compound
+    shape (flag, part count, unit inertia, parts), per heightfield (rows,
+    cols, cell, heights row by row), per mesh (vertex floats, triangle
+    indices, the floats, the indices)."""
+    out = struct.pack("<I", len(exts))
+    for flag, parts, ui in exts:
+        out += struct.pack("<2I3f", flag, len(parts), *ui) + b"".join(bytes(q) for q in parts)
+    out += struct.pack("<I", len(hfs))
+    for rows, cols, cell, h in hfs:
+        out += struct.pack(f"<2If{len(h)}f", rows, cols, cell, *h)
+    out += struct.pack("<I", len(meshes))
+    for v, t in meshes:
+        out += struct.pack(f"<2I{len(v)}f{len(t)}I", len(v), len(t), *v, *t)
+    return out
+
+
+def retyped(shape, index, mass):
+    """A body record of a table-backed shape: its kind and table index
+    patched into a box's record."""
+    b = bytearray(bytes(body(abi.SHAPE_BOX, [0.5, 0.5, 0.5], [0, 1, 0], mass)))
+    struct.pack_into("<I", b, abi.AvbdBody.shape.offset, shape)
+    struct.pack_into("<f", b, abi.AvbdBody.shape_params.offset, float(index))
+    return bytes(b)
+
+
+def test_table_shapes_are_checked_on_the_host():
+    rounded = (0, [abi.shape_part(abi.SHAPE_SPHERE, [0.3], 0.1)], (0.1, 0.1, 0.1))
+    dumbbell = (1, [abi.shape_part(abi.SHAPE_SPHERE, [0.2], position=(-0.5, 0, 0)),
+                    abi.shape_part(abi.SHAPE_SPHERE, [0.2], position=(0.5, 0, 0))], (0.1, 0.1, 0.1))
+    terrain = (2, 3, 1.0, [0.0, 0.1, 0.0, 0.2, 0.0, 0.1])
+    tri = ([0, 0, 0, 1, 0, 0, 0, 0, 1], [0, 1, 2])
+    world = [retyped(abi.SHAPE_ROUND, 0, 1.0), retyped(abi.SHAPE_COMPOUND, 1, 1.0),
+             retyped(abi.SHAPE_HEIGHTFIELD, 0, 0.0), retyped(abi.SHAPE_TRIMESH, 0, 0.0)]
+
+    def snap(bodies=world, exts=(rounded, dumbbell), hfs=(terrain,), meshes=(tri,)):
+        return snapshot(scene_offsets=(0, len(bodies)), bodies=b"".join(bodies), nbodies=len(bodies),
+                        shapes=shape_sections(exts, hfs, meshes))
+
+    assert snapshot_info(snap()).nbodies == 4
+    # a body naming a table entry that is not there, or one of the other kind
+    refused(snap(bodies=world[:2] + [retyped(abi.SHAPE_HEIGHTFIELD, 1, 0.0)] + world[3:]))
+    refused(snap(bodies=world[:3] + [retyped(abi.SHAPE_TRIMESH, 1, 0.0)]))
+    refused(snap(bodies=[retyped(abi.SHAPE_ROUND, 1, 1.0)] + world[1:]))
+    refused(snap(bodies=[world[0], retyped(abi.SHAPE_COMPOUND, 0, 1.0)] + world[2:]))
+    refused(snap(bodies=[retyped(abi.SHAPE_ROUND, -1, 1.0)] + world[1:]))
+    # terrain and meshes are never dynamic
+    refused(snap(bodies=world[:2] + [retyped(abi.SHAPE_HEIGHTFIELD, 0, 1.0)] + world[3:]))
+    refused(snap(bodies=world[:3] + [retyped(abi.SHAPE_TRIMESH, 0, 1.0)]))
+    # table entries the registration calls would refuse
+    refused(snap(exts=((2,) + rounded[1:], dumbbell)))                         # unknown flag
+    refused(snap(exts=((0, dumbbell[1], rounded[2]), dumbbell)))               # rounded with two parts
+    refused(snap(exts=((0, [abi.shape_part(abi.SHAPE_SPHERE, [0.3])], rounded[2]), dumbbell)))  # no border
+    refused(snap(exts=(rounded, (1, [abi.shape_part(abi.SHAPE_HALFSPACE, [0, 1, 0])], (0.1, 0.1, 0.1)))))
+    refused(snap(exts=(rounded, (1, [abi.shape_part(abi.SHAPE_HULL, [0])], (0.1, 0.1, 0.1)))))  # no hulls
+    refused(snap(exts=(rounded, (1, dumbbell[1], (0.1, float("nan"), 0.1)))))
+    refused(snap(hfs=((2, 3, 0.0, terrain[3]),)))                              # no cell size
+    refused(snap(hfs=((2, 3, 1.0, terrain[3][:5] + [float("inf")]),)))
+    refused(snap(meshes=((tri[0], [0, 1, 3]),)))                               # a vertex that is not there
+    refused(snap(meshes=((tri[0][:8], tri[1]),)))                              # not whole vertices
+    refused(snap(meshes=((tri[0], [0, 1]),)))                                  # not whole triangles
+    # a section shorter than its counts say: the rest of the payload is misread
+    refused(snap(hfs=((2, 3, 1.0, terrain[3][:4]),)))
